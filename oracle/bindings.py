@@ -1,0 +1,184 @@
+"""Oracle test infrastructure -- not part of the shipped library.
+
+ctypes bindings for the two CPU checker libraries built by oracle/Makefile:
+
+* ``port``: oracle/_build/libport.so, the CPU restatement of the reference's
+  hot path (oracle/port/port.cpp);
+* ``ref``:  oracle/_ref/libref.so, the reference's own sources compiled with
+  shims (oracle/ref/harness.cpp); only present where the reference checkout
+  was available at build time.
+
+Both export the same functions (prefix ``port_`` / ``ref_``), wrapped here by
+``OracleLib``. Only tests/, __graft_entry__.smoke() and bench.py's CPU
+baseline import this module.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PORT_SO = os.path.join(HERE, "_build", "libport.so")
+REF_SO = os.path.join(HERE, "_ref", "libref.so")
+REFERENCE_DIR = "/root/reference"
+PIX_FLOATS = 40
+
+
+class _SceneIn(C.Structure):
+    _fields_ = [
+        ("num_vertices", C.c_int32), ("positions", C.c_void_p), ("normals", C.c_void_p), ("uvs", C.c_void_p),
+        ("num_triangles", C.c_int32), ("indices", C.c_void_p),
+        ("num_meshes", C.c_int32), ("mesh_first", C.c_void_p), ("mesh_material", C.c_void_p),
+        ("num_materials", C.c_int32), ("materials", C.c_void_p),
+        ("env_width", C.c_int32), ("env_height", C.c_int32), ("env_rgb", C.c_void_p),
+    ]
+
+
+def build(with_reference: bool | None = None) -> None:
+    """Compile the port, and the reference harness when the reference
+    checkout exists (or when ``with_reference`` is True)."""
+    targets = ["port"]
+    if with_reference or (with_reference is None and os.path.isdir(os.path.join(REFERENCE_DIR, "src"))):
+        targets.append("ref")
+    subprocess.run(["make", "-s", "-C", HERE, "-j8"] + targets, check=True)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class OracleScene:
+    def __init__(self, lib: "OracleLib", scene):
+        self.lib = lib
+        self._keep = [np.ascontiguousarray(x) for x in (scene.positions, scene.normals, scene.uvs, scene.indices,
+                                                        scene.mesh_first, scene.mesh_material, scene.materials)]
+        env = None if scene.env is None else np.ascontiguousarray(scene.env, np.float32)
+        self._keep.append(env)
+        p, n, u, i, mf, mm, mat = self._keep[:7]
+        d = _SceneIn(p.shape[0], _ptr(p), _ptr(n), _ptr(u), i.shape[0], _ptr(i), mm.shape[0], _ptr(mf), _ptr(mm),
+                     mat.shape[0], _ptr(mat), 0 if env is None else env.shape[1], 0 if env is None else env.shape[0],
+                     _ptr(env))
+        self.handle = lib.fn("scene_create")(C.byref(d))
+        self.num_triangles = int(i.shape[0])
+
+    def close(self):
+        if self.handle:
+            self.lib.fn("scene_destroy")(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def bvh(self):
+        n = self.lib.fn("bvh_size")(self.handle)
+        boxes = np.empty((n, 6), np.float32)
+        ranges = np.empty((n, 2), np.int32)
+        order = np.empty(self.num_triangles, np.int32)
+        self.lib.fn("bvh_export")(self.handle, _ptr(boxes), _ptr(ranges), _ptr(order))
+        return boxes, ranges, order
+
+    def lights(self):
+        n = self.lib.fn("light_count")(self.handle)
+        out = np.empty((n, 8), np.float32)
+        if n:
+            self.lib.fn("light_export")(self.handle, _ptr(out))
+        return out
+
+    def trace_closest(self, rays: np.ndarray, threads: int = 8):
+        rays = np.ascontiguousarray(rays, np.float32)
+        n = rays.shape[0]
+        face = np.empty(n, np.int32)
+        t = np.empty(n, np.float32)
+        bc = np.empty((n, 3), np.float32)
+        self.lib.fn("trace_closest")(self.handle, _ptr(rays), n, _ptr(face), _ptr(t), _ptr(bc), threads)
+        return face, t, bc
+
+    def trace_shadow(self, rays: np.ndarray, threads: int = 8):
+        rays = np.ascontiguousarray(rays, np.float32)
+        occ = np.empty(rays.shape[0], np.uint8)
+        self.lib.fn("trace_shadow")(self.handle, _ptr(rays), rays.shape[0], _ptr(occ), threads)
+        return occ
+
+    def trace_stats(self, rays: np.ndarray, shadow: bool = False):
+        rays = np.ascontiguousarray(rays, np.float32)
+        out = np.zeros(3, np.uint64)
+        self.lib.fn("trace_stats")(self.handle, _ptr(rays), rays.shape[0], 1 if shadow else 0, _ptr(out))
+        return {"inner": int(out[0]), "leaves": int(out[1]), "tris": int(out[2])}
+
+    def render(self, camera, seed: int, mode: int = 0, rect=None, threads: int = 8) -> np.ndarray:
+        """Per-pixel records (h, w, 40) of the pixel rectangle (x0, y0, x1, y1)."""
+        x0, y0, x1, y1 = rect or (0, 0, camera.width, camera.height)
+        out = np.zeros((y1 - y0, x1 - x0, PIX_FLOATS), np.float32)
+        args = camera.packed(threads)
+        self.lib.fn("render")(self.handle, _ptr(args), C.c_uint64(seed), mode, x0, y0, x1, y1, _ptr(out), threads)
+        return out
+
+
+class OracleLib:
+    def __init__(self, kind: str = "port"):
+        self.kind = kind
+        path = PORT_SO if kind == "port" else REF_SO
+        if not os.path.exists(path):
+            raise FileNotFoundError(f"{path} is not built (oracle.bindings.build())")
+        self.lib = C.CDLL(path)
+        self._fns = {}
+        sig = {
+            "scene_create": (C.c_void_p, [C.c_void_p]),
+            "scene_destroy": (None, [C.c_void_p]),
+            "bvh_size": (C.c_int, [C.c_void_p]),
+            "bvh_export": (None, [C.c_void_p] * 4),
+            "light_count": (C.c_int, [C.c_void_p]),
+            "light_export": (None, [C.c_void_p, C.c_void_p]),
+            "trace_closest": (None, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+            "trace_shadow": (None, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int]),
+            "trace_stats": (None, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p]),
+            "render": (None, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                              C.c_void_p, C.c_int]),
+            "compose": (None, [C.c_void_p, C.c_int64, C.c_float, C.c_int, C.c_void_p]),
+            "gamma": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
+            "fxaa": (None, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+        }
+        for name, (res, args) in sig.items():
+            f = getattr(self.lib, f"{kind}_{name}", None)
+            if f is None:
+                continue
+            f.restype = res
+            f.argtypes = args
+            self._fns[name] = f
+
+    def fn(self, name):
+        return self._fns[name]
+
+    def scene(self, scene) -> OracleScene:
+        return OracleScene(self, scene)
+
+    def compose(self, recs: np.ndarray, exposure: float = 1.0, gamma: bool = True) -> np.ndarray:
+        recs = np.ascontiguousarray(recs, np.float32)
+        shp = recs.shape[:-1]
+        n = int(np.prod(shp))
+        out = np.empty(shp + (3,), np.float32)
+        self.fn("compose")(_ptr(recs), n, exposure, 1 if gamma else 0, _ptr(out))
+        return out
+
+    def gamma(self, rgb: np.ndarray) -> np.ndarray:
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        out = np.empty_like(rgb)
+        self.fn("gamma")(_ptr(rgb), rgb.size // 3, _ptr(out))
+        return out
+
+    def fxaa(self, rgb: np.ndarray) -> np.ndarray:
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        h, w, _ = rgb.shape
+        out = np.empty_like(rgb)
+        self.fn("fxaa")(_ptr(rgb), _ptr(out), w, h)
+        return out
+
+
+def have_ref() -> bool:
+    return os.path.exists(REF_SO)

@@ -1,0 +1,1102 @@
+// Oracle test infrastructure -- not part of the shipped library.
+//
+// CPU restatement of the reference's hot path (lemonchu/Raym0nade), used only
+// by tests/, __graft_entry__.smoke() and bench.py's CPU baseline as the
+// checker. It is pinned against the reference's own sources compiled with
+// shims (oracle/ref -> oracle/_ref/libref.so, functions ref_*): the tests
+// require identical BVH trees, identical closest-hit and shadow answers,
+// bit-identical renders under the reference's mt19937 stream, and
+// bit-identical FXAA. On machines without the reference sources the pin is
+// carried by the committed fixtures in tests/golden/ (made by
+// tests/golden/make_golden.py from the compiled reference).
+//
+// Scope of the restatement: the opaque path of the configs (constant-texel
+// materials, area lights or a lat-long sky, no media). Glass/media, alpha
+// testing and textured materials are not restated here.
+//
+// Every function cites the reference file:line it follows.
+#include "oracle_api.h"
+
+#include <glm/glm.hpp>
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <random>
+#include <thread>
+#include <vector>
+
+#include "../../raym0nade_gb300/csrc/rmn_rng.h"
+
+namespace orc {
+
+using vec2 = glm::vec<2, float>;
+using vec3 = glm::vec<3, float>;
+using vec4 = glm::vec<4, float>;
+using glm::cross;
+using glm::dot;
+using glm::length;
+using glm::normalize;
+
+constexpr float kEps = 1e-4f;                       // include/geometry.h:13
+const float kPi = 3.14159265358979323846f;          // include/geometry.h:14
+const vec3 kLum(0.3f, 0.6f, 0.1f);                  // include/geometry.h:16
+constexpr int kMaxTrys = 16;                        // src/sampling.cpp:201
+constexpr float kLightRadius = 1e-3f;               // include/sampling.h:34
+constexpr unsigned kLeafSize = 10;                  // src/bvh.cpp:16
+constexpr int kSampleCount[17] = {0, 1, 2, 2, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 5, 6};  // src/render.cpp:126
+
+// The reference's isfinite(vec) is true when ANY component is finite
+// (src/geometry.cpp:4-10).
+static bool any_finite(const vec3& v) { return std::isfinite(v.x) || std::isfinite(v.y) || std::isfinite(v.z); }
+
+static float fmix(float a, float b, float t) { return a * (1 - t) + b * t; }  // src/sampling.cpp:16-18
+static float fclampf(float x, float a, float b) { return x < a ? a : (x > b ? b : x); }  // :12-14
+
+// ---------------------------------------------------------------- scene ----
+struct Mat {
+  vec3 base, emis, trans;
+  bool has_base, has_emis, has_surf;
+  float roughness, metallic, opacity, ior;
+  int id;
+  // Material::getDiffuseColor / getEmissiveColor / getSurfaceData with one
+  // constant texel (src/material.cpp:349-383).
+  vec3 diffuse() const { return has_base ? base : vec3(1.0f); }
+  vec3 emission() const { return has_emis ? emis : vec3(0.0f); }
+  void surface(float& r, float& m) const {
+    if (!has_surf) { m = 0.0f; r = roughness; return; }
+    m = std::min(metallic, 0.99f);
+    r = std::max(roughness, 1e-3f);
+  }
+};
+
+struct Tri {
+  vec3 v[3];
+  int vid[3];  // vertex indices (normals, uvs)
+  int mat;
+  int id;      // index in the input triangle array
+};
+
+struct Box { vec3 lo, hi; };
+static Box box_union(const Box& a, const Box& b) {  // src/geometry.cpp:30-35
+  return {vec3(std::fmin(a.lo.x, b.lo.x), std::fmin(a.lo.y, b.lo.y), std::fmin(a.lo.z, b.lo.z)),
+          vec3(std::fmax(a.hi.x, b.hi.x), std::fmax(a.hi.y, b.hi.y), std::fmax(a.hi.z, b.hi.z))};
+}
+static vec3 tri_center(const Tri& f) { return (f.v[0] + f.v[1] + f.v[2]) / 3.0f; }  // src/component.cpp:37-39
+static Box tri_box(const Tri& f) {                                                    // :41-46
+  return {glm::min(f.v[0], glm::min(f.v[1], f.v[2])), glm::max(f.v[0], glm::max(f.v[1], f.v[2]))};
+}
+
+struct Node {
+  Box box;
+  int faceL = 0, faceR = 0;
+};
+
+struct Light {  // LightObject, include/component.h:47-54
+  vec3 center = vec3(0.0f), color = vec3(0.0f);
+  float power = 0.0f;
+  std::vector<Tri> faces;
+  std::vector<float> prefix;
+};
+
+struct Sky {  // SkyBox, include/component.h:56-67
+  int w = 0, h = 0;
+  std::vector<vec3> data;  // premultiplied by texel solid angle (src/component.cpp:54-67)
+  std::vector<float> prefix;
+  bool empty() const { return data.empty(); }
+};
+
+struct Stats { uint64_t inner = 0, leaves = 0, tris = 0; };
+
+struct Scene {
+  std::vector<vec3> nrm;
+  std::vector<vec2> uv;
+  std::vector<Mat> mats;
+  std::vector<Tri> tris;   // permuted in place by the builder, like Model::faces
+  std::vector<Node> nodes; // heap-indexed, children 2u and 2u+1
+  std::vector<Light> lights;
+  Sky sky;
+};
+
+// RandomDistribution, src/component.cpp:12-31.
+static void prefix_init(std::vector<float>& p, const std::vector<float>& w) {
+  p.resize(w.size());
+  p[0] = w[0];
+  for (size_t i = 1; i < w.size(); ++i) p[i] = p[i - 1] + w[i];
+}
+template <class G>
+static int prefix_draw(const std::vector<float>& p, G& gen) {
+  float x = p.back() * gen();
+  return (int)(std::lower_bound(p.begin(), p.end(), x) - p.begin());
+}
+static float prefix_pdf(const std::vector<float>& p, int i) {
+  float now = p[i];
+  if (i > 0) now -= p[i - 1];
+  return now / p.back();
+}
+
+// --------------------------------------------------------------- builder ---
+// BVH::dfs_build / nodeCount / build, src/bvh.cpp:18-54: median split on the
+// axis of largest centroid variance, std::nth_element on the centroid
+// coordinate, leaves of at most 10 triangles, heap-indexed nodes.
+static void build_rec(Scene& s, int u, int l, int r) {
+  if ((unsigned)(r - l) <= kLeafSize) {
+    Node& n = s.nodes[u];
+    n.faceL = l;
+    n.faceR = r;
+    n.box = {vec3(INFINITY), vec3(-INFINITY)};
+    for (int i = l; i < r; ++i) n.box = box_union(n.box, tri_box(s.tris[i]));
+    return;
+  }
+  vec3 sum = vec3(0), sum2 = vec3(0);
+  for (int i = l; i < r; ++i) {
+    vec3 c = tri_center(s.tris[i]);
+    sum += c;
+    sum2 += c * c;
+  }
+  vec3 var = sum2 - sum * sum / (float)(r - l);
+  int axis = 0;
+  if (var[1] > var[0]) axis = 1;
+  if (var[2] > var[0] && var[2] > var[1]) axis = 2;
+  int m = (r + l) / 2;
+  std::nth_element(s.tris.begin() + l, s.tris.begin() + m, s.tris.begin() + r,
+                   [axis](const Tri& a, const Tri& b) { return tri_center(a)[axis] < tri_center(b)[axis]; });
+  build_rec(s, u << 1, l, m);
+  build_rec(s, u << 1 | 1, m, r);
+  s.nodes[u].box = box_union(s.nodes[u << 1].box, s.nodes[u << 1 | 1].box);
+}
+static int heap_slots(int u, int n) { return ((unsigned)n <= kLeafSize) ? u : heap_slots(u << 1 | 1, (n + 1) >> 1); }
+
+// ------------------------------------------------------------- traversal ---
+struct Ray { vec3 o, d; };
+struct Hit { float tmin, tmax; int face; };
+
+// rayInBox, src/geometry.cpp:40-61 (cumulative tR += eps per axis, early
+// return once tL > tR, origin-inside rule for |d| < eps).
+static void slab(const Ray& r, const Box& b, float& tL, float& tR) {
+  for (int i = 0; i < 3; ++i) {
+    if (std::abs(r.d[i]) < kEps) {
+      if (r.o[i] < b.lo[i] || r.o[i] > b.hi[i]) { tR = -1.0f; return; }
+      continue;
+    }
+    float inv = 1.0f / r.d[i];
+    float lo = inv >= 0 ? b.lo[i] : b.hi[i];
+    float hi = inv >= 0 ? b.hi[i] : b.lo[i];
+    tL = std::fmax(tL, (lo - r.o[i]) * inv);
+    tR = std::fmin(tR, (hi - r.o[i]) * inv);
+    tR += kEps;
+    if (tL > tR) return;
+  }
+}
+
+// RayTriangleIntersection (Moller-Trumbore), src/geometry.cpp:63-87.
+static float tri_t(const Ray& r, const vec3& v0, const vec3& v1, const vec3& v2) {
+  vec3 e1 = v1 - v0, e2 = v2 - v0;
+  vec3 h = cross(r.d, e2);
+  float a = dot(e1, h);
+  if (std::abs(a) / length(e1) < kEps) return INFINITY;
+  float f = 1.0f / a;
+  vec3 s = r.o - v0;
+  float u = f * dot(s, h);
+  if (u < 0.0f || u > 1.0f) return INFINITY;
+  vec3 q = cross(s, e1);
+  float v = f * dot(r.d, q);
+  if (v < 0.0f || u + v > 1.0f) return INFINITY;
+  return f * dot(e2, q);
+}
+
+// BVH::dfs_rayHit, src/bvh.cpp:56-88: near child first (ties go right), the
+// far child only if its entry is still closer than the current hit.
+static void visit(const Scene& s, int u, const Ray& r, Hit& h, Stats* st) {
+  const Node& n = s.nodes[u];
+  if (n.faceR) {
+    if (st) { st->leaves++; st->tris += (uint64_t)(n.faceR - n.faceL); }
+    for (int i = n.faceL; i < n.faceR; ++i) {
+      const Tri& f = s.tris[i];
+      float t = tri_t(r, f.v[0], f.v[1], f.v[2]);
+      if (h.tmin < t && t < h.tmax) { h.tmax = t; h.face = i; }
+    }
+    return;
+  }
+  if (st) st->inner++;
+  float a0 = h.tmin, b0 = h.tmax, a1 = h.tmin, b1 = h.tmax;
+  slab(r, s.nodes[u << 1].box, a0, b0);
+  slab(r, s.nodes[u << 1 | 1].box, a1, b1);
+  if (a0 < a1) {
+    if (a0 < b0) visit(s, u << 1, r, h, st);
+    if (a1 < b1 && a1 < h.tmax) visit(s, u << 1 | 1, r, h, st);
+  } else {
+    if (a1 < b1) visit(s, u << 1 | 1, r, h, st);
+    if (a0 < b0 && a0 < h.tmax) visit(s, u << 1, r, h, st);
+  }
+}
+static void traverse(const Scene& s, const Ray& r, Hit& h, Stats* st) {
+  if (s.tris.empty()) return;  // the reference indexes past its node array here
+  visit(s, 1, r, h, st);
+}
+// Model::rayHit, src/model.cpp:332-341. Constant-texel materials have no
+// fully transparent texels, so the alpha-test retry never fires.
+static Hit closest(const Scene& s, const Ray& r, Stats* st = nullptr) {
+  Hit h{kEps, INFINITY, -1};
+  traverse(s, r, h, st);
+  return h;
+}
+// Model::rayHit_test, src/model.cpp:343-354.
+static bool occluded(const Scene& s, const Ray& r, float aim, Stats* st = nullptr) {
+  Hit h{kEps, aim + kEps, -1};
+  traverse(s, r, h, st);
+  return !(h.tmax >= aim);
+}
+
+// barycentric, src/geometry.cpp:89-103 -> (gamma, alpha, beta).
+static vec3 bary(const vec3& v0, const vec3& v1, const vec3& v2, const vec3& p) {
+  vec3 e1 = v1 - v0, e2 = v2 - v0;
+  vec3 n = cross(e1, e2);
+  float den = dot(n, n);
+  vec3 vp = p - v0;
+  float al = dot(cross(vp, e2), n) / den;
+  float be = dot(cross(e1, vp), n) / den;
+  float ga = 1.0f - al - be;
+  return vec3(ga, al, be);
+}
+
+// ------------------------------------------------------------- shading -----
+struct Surf {  // HitInfo, include/model.h:12-18 with defaults of src/model.cpp:4-7
+  vec3 shapeN = vec3(NAN), surfN = vec3(NAN), emis = vec3(0.0f), base = vec3(0.0f), pos = vec3(NAN);
+  float specular = 0.04f, roughness = 0.8f, metallic = 0.0f, opacity = 1.0f, eta = 1.0f;
+  int id = 0;
+  bool entering = true;
+};
+
+static bool flip_toward(vec3& v, const vec3& dir) {  // reverseFix, src/model.cpp:232-238
+  if (dot(v, dir) < 0.0f) { v *= -1.0f; return false; }
+  return true;
+}
+
+// getHitNormals, src/model.cpp:240-270.
+static void hit_normals(const Scene& s, const Tri& f, const vec3& in, const vec3& b, vec3& shapeN, vec3& surfN,
+                        bool& entering) {
+  vec3 c = cross(f.v[1] - f.v[0], f.v[2] - f.v[0]);
+  shapeN = normalize(c);
+  entering = flip_toward(shapeN, -in);
+  surfN = shapeN;
+  float area = length(c) / 2.0f;
+  if (area > 1e-2f) return;
+  vec3 n0 = s.nrm[f.vid[0]], n1 = s.nrm[f.vid[1]], n2 = s.nrm[f.vid[2]];
+  flip_toward(n0, shapeN);
+  flip_toward(n1, shapeN);
+  flip_toward(n2, shapeN);
+  surfN = normalize(b[0] * (dot(n0, shapeN) > 0.85f ? n0 : shapeN) + b[1] * (dot(n1, shapeN) > 0.85f ? n1 : shapeN) +
+                    b[2] * (dot(n2, shapeN) > 0.85f ? n2 : shapeN));
+  if (!any_finite(surfN)) surfN = shapeN;
+}
+
+// calcSurfaceNormal with the zero normal-map texel that getNormal returns
+// without a normal texture (src/model.cpp:279-298, src/material.cpp:358-363).
+static void surface_normal(const Scene& s, const Tri& f, const vec3& shapeN, vec3& surfN) {
+  const vec3 nm(0.0f);
+  vec3 e1 = f.v[1] - f.v[0], e2 = f.v[2] - f.v[0];
+  vec2 d1 = s.uv[f.vid[1]] - s.uv[f.vid[0]], d2 = s.uv[f.vid[2]] - s.uv[f.vid[0]];
+  float k = 1.0f / (d1.x * d2.y - d2.x * d1.y);
+  vec3 tu = k * (d2.y * e1 - d1.y * e2), tv = k * (-d2.x * e1 + d1.x * e2);
+  vec3 t = normalize(tu - shapeN * dot(shapeN, tu));
+  vec3 bt = normalize(tv - shapeN * dot(shapeN, tv) - t * dot(t, tv));
+  vec3 keep = surfN;
+  surfN = normalize(t * nm.x + bt * nm.y + surfN);
+  if (!any_finite(surfN)) surfN = keep;
+}
+
+// getHitInfo + getHitMaterial for constant-texel materials,
+// src/render.cpp:62-79 and src/model.cpp:300-328. Ray differentials only feed
+// texture LOD, which constant texels ignore.
+static void hit_info(const Scene& s, const Tri& f, const Ray& r, Surf& h) {
+  vec3 b = bary(f.v[0], f.v[1], f.v[2], h.pos);
+  hit_normals(s, f, r.d, b, h.shapeN, h.surfN, h.entering);
+  vec3 raw = h.surfN;
+  const Mat& m = s.mats[f.mat];
+  h.id = m.id;
+  m.surface(h.roughness, h.metallic);
+  h.opacity = m.opacity;
+  h.eta = m.ior;
+  if (h.opacity > 1.0f - kEps) h.entering = true;
+  h.base = (h.opacity < kEps) ? m.trans : m.diffuse();
+  h.emis = m.emission();
+  surface_normal(s, f, h.shapeN, h.surfN);
+  if (dot(h.surfN, r.d) >= 0.0f) h.surfN = raw;
+  if (dot(h.surfN, r.d) >= 0.0f) h.surfN = h.shapeN;
+}
+
+// ---------------------------------------------------------------- BSDF -----
+static float pow5(float x) { float x2 = x * x; return x2 * x2 * x; }           // src/sampling.cpp:20-23
+static float schlick(float u) { return pow5(fclampf(1 - u, 0, 1)); }          // :25-28
+static float gtr1(float c, float a) {                                          // :30-35
+  if (a >= 1) return 1 / kPi;
+  float a2 = a * a;
+  float t = 1 + (a2 - 1) * c * c;
+  return (a2 - 1) / (kPi * std::log(a2) * t);
+}
+static float gtr2(float c, float a) {                                          // :37-41
+  float a2 = a * a;
+  float t = 1 + (a2 - 1) * c * c;
+  return a2 / (kPi * t * t);
+}
+static float smith_g(float c, float ag) {                                      // :43-47
+  float a = ag * ag, b = c * c;
+  return 1 / (c + std::sqrt(a + b - a * b));
+}
+static void lum_clamp(vec3& v) {                                               // :238-243
+  float l = dot(v, kLum);
+  if (l > 64.0f) v /= l / 64.0f;
+}
+
+struct Bsdf {
+  vec3 in;  // direction towards the previous vertex
+  Surf s;
+
+  // BSDF::getBRDF, src/sampling.cpp:49-157 (subsurface, sheen and tints 0,
+  // clearcoat 1.5, clearcoat gloss 0.2).
+  vec3 brdf(const vec3& L) const {
+    const vec3& V = in;
+    const vec3& N = s.surfN;
+    float nl = dot(N, L), nv = dot(N, V);
+    if (nl <= 0.0f || nv <= 0.0f) return vec3(0);
+    vec3 H = normalize(L + V);
+    float nh = dot(N, H), lh = dot(L, H);
+    vec3 cd = s.base;
+    float cdl = dot(cd, kLum);
+    vec3 tint = cdl > 0.0f ? cd / cdl : vec3(1.0f);
+    vec3 spec0 = glm::mix(s.specular * glm::mix(vec3(1.0f), tint, 0.0f), cd, s.metallic);
+    vec3 sheenc = glm::mix(vec3(1.0f), tint, 0.0f);
+    float fl = schlick(nl), fv = schlick(nv);
+    float fd90 = 0.5f + 2.0f * lh * lh * s.roughness;
+    float fd = fmix(1.0f, fd90, fl) * fmix(1.0f, fd90, fv);
+    float fss90 = lh * lh * s.roughness;
+    float fss = fmix(1.0f, fss90, fl) * fmix(1.0f, fss90, fv);
+    float ss = 1.25f * (fss * (1.0f / (nl + nv) - .5f) + .5f);
+    float ds = gtr2(nh, s.roughness);
+    float fh;
+    if (s.eta <= 1.0f) {
+      fh = schlick(lh);
+    } else {
+      float ci = std::fabs(lh);
+      float si = ci * ci;
+      si = (1.0f - si) <= 0.0f ? 0.0f : std::sqrt(1.0f - si);
+      float st = s.eta * si;
+      if (st >= 1.0f) {
+        fh = 1.0f;
+      } else {
+        float ct = (1.0f - st * st) <= 0.0f ? 0.0f : std::sqrt(1.0f - st * st);
+        float r0 = (s.eta - 1.0f) / (s.eta + 1.0f);
+        r0 = r0 * r0;
+        fh = fmix(r0, 1.0f, schlick(ct));
+      }
+    }
+    vec3 fs = glm::mix(spec0, vec3(1.0f), fh);
+    float gs = smith_g(nl, s.roughness);
+    gs *= smith_g(nv, s.roughness);
+    vec3 fsheen = fh * 0.0f * sheenc;
+    float dr = gtr1(nh, fmix(.1f, .001f, 0.2f));
+    float fr = fmix(.04f, 1.0f, fh);
+    float gr = smith_g(nl, .25f) * smith_g(nv, .25f);
+    vec3 ret = ((1.0f / kPi) * fmix(fd, ss, 0.0f) * cd + fsheen);
+    ret *= (1.0f - s.metallic);
+    ret += (0.25f * 1.5f * gr * fr * dr) * glm::mix(vec3(1.0f), tint, 0.0f);
+    ret *= s.opacity;
+    ret += fs * ds * gs;
+    return ret * nl;
+  }
+  // BSDF::getBSDF, :194-199 (opaque surfaces always take the BRDF).
+  vec3 eval(const vec3& L) const { return brdf(L); }
+
+  // getTangentSpaceWithInDir, src/geometry.cpp:114-124 (the fallback branch
+  // needs dot(N, in) < -0.999, which hit shading rules out).
+  void frame(vec3& t, vec3& b) const {
+    float c = dot(s.surfN, in);
+    if (c < -1.0f + 1e-3f) {
+      vec3 v0 = std::fabs(s.surfN.x) < 0.8f ? vec3(1.0f, 0.0f, 0.0f) : vec3(0.0f, 1.0f, 0.0f);
+      t = normalize(cross(v0, s.surfN));
+      b = cross(s.surfN, t);
+      return;
+    }
+    b = normalize(cross(s.surfN, in));
+    t = cross(b, s.surfN);
+  }
+
+  // BSDF::sampleBRDF, :203-236 (GGX half-vector sampling, <= 16 tries).
+  template <class G>
+  void sample_ggx(G& gen, vec3& out, vec3& w, float& pdf, int& fails) const {
+    vec3 t, b;
+    frame(t, b);
+    for (int T = 1; T <= kMaxTrys; ++T) {
+      float u = gen(), phi = gen() * 2.0f * kPi;
+      float ct = std::sqrt((1.0f - u) / (1.0f + (s.roughness * s.roughness - 1.0f) * u));
+      float st = std::sqrt(1 - ct * ct);
+      vec3 H = st * std::cos(phi) * t + st * std::sin(phi) * b + ct * s.surfN;
+      out = 2.0f * dot(in, H) * H - in;
+      float lh = dot(out, H), ln = dot(out, s.surfN);
+      if (lh <= 0.0f || ln <= 0.0f) pdf = 0.0f;
+      else pdf = gtr2(ct, s.roughness) / (4.0f * lh);
+      if (dot(out, s.shapeN) > 0.0f && pdf > 0.0f) { w = brdf(out) / pdf; return; }
+      fails++;
+    }
+    pdf = 0.0f;
+    w = vec3(0.0f);
+    out = vec3(NAN);
+  }
+  // BSDF::sampleCos, :245-269 (cosine sampling, luminance clamp 64).
+  template <class G>
+  void sample_cos(G& gen, vec3& out, vec3& w, float& pdf, int& fails) const {
+    vec3 t, b;
+    frame(t, b);
+    for (int T = 1; T <= kMaxTrys; ++T) {
+      float u = gen(), phi = gen() * 2.0f * kPi;
+      float d = std::sqrt(u);
+      float z = std::sqrt(1 - d * d);
+      float x = d * std::cos(phi), y = d * std::sin(phi);
+      out = x * t + y * b + z * s.surfN;
+      pdf = dot(out, s.surfN) / kPi;
+      if (dot(out, s.shapeN) > 0.0f && pdf > 0.0f) {
+        w = brdf(out) / pdf;
+        lum_clamp(w);
+        return;
+      }
+      fails++;
+    }
+    pdf = 0.0f;
+    w = vec3(0.0f);
+    out = vec3(NAN);
+  }
+  // BSDF::sampleReflection, :310-340: draw both, keep one with p1 = pdf1/(pdf1+pdf2).
+  template <class G>
+  void sample_reflect(G& gen, vec3& dir, vec3& w, int& fails) const {
+    vec3 d1, d2, w1, w2;
+    int f1 = 0, f2 = 0;
+    float p1, p2;
+    sample_cos(gen, d1, w1, p1, f1);
+    sample_ggx(gen, d2, w2, p2, f2);
+    float pc = p1 / (p1 + p2);
+    if (gen() < pc) { dir = d1; w = w1; fails += f1; }
+    else { dir = d2; w = w2; fails += f2; }
+  }
+};
+
+// --------------------------------------------------------- light sampling --
+struct LSample {  // LightSample, include/sampling.h:28-32
+  vec3 bsdf, light;
+  float weight;
+};
+
+// generateRandomPointInLightFace + sampleLightFace, src/sampling.cpp:419-448.
+template <class G>
+static void light_point(const Scene& s, const Light& lo, const vec3& pos, G& gen, vec3& lp, int& fails) {
+  for (int T = 1; T <= kMaxTrys; ++T) {
+    int fi = prefix_draw(lo.prefix, gen);
+    const Tri& f = lo.faces[fi];
+    float a = gen(), b = gen();
+    if (a + b > 1.0f) { a = 1.0f - a; b = 1.0f - b; }
+    float c = 1.0f - a - b;
+    lp = a * f.v[0] + b * f.v[1] + c * f.v[2];
+    vec3 ld = normalize(lp - pos);
+    vec3 sn, un;
+    bool ent;
+    hit_normals(s, f, ld, vec3(a, b, c), sn, un, ent);
+    float cphi = dot(un, -ld);
+    if (cphi > 0.0f && gen() < cphi) return;
+    fails++;
+  }
+  lp = vec3(NAN);
+}
+
+// sampleSkyBox, src/sampling.cpp:450-465.
+template <class G>
+static void sky_dir(const Sky& k, const vec3& n, G& gen, vec3& dir, vec3& light) {
+  for (int T = 1; T <= kMaxTrys; ++T) {
+    int p = prefix_draw(k.prefix, gen);
+    int u = p % k.w, v = p / k.w;
+    float phi = kPi * (float(v) + 0.5f) / float(k.h);
+    float th = 2.0f * kPi * (float(u) + 0.5f) / float(k.w);
+    dir = vec3(-std::sin(phi) * std::sin(th), std::cos(phi), std::sin(phi) * std::cos(th));
+    if (dot(dir, n) > 0.0f) { light = k.data[p] / prefix_pdf(k.prefix, p); return; }
+  }
+  dir = vec3(NAN);
+}
+
+// SkyBox::get, src/component.cpp:120-140.
+static vec3 sky_get(const Sky& k, const vec3& dir) {
+  if (k.empty()) return vec3(0.0f);
+  float th = std::atan2(-dir.x, dir.z);
+  float phi = std::acos(dir.y);
+  if (th < 0.0f) th += 2.0f * kPi;
+  int u = (int)(th / (2.0f * kPi) * float(k.w));
+  int v = (int)(phi / kPi * float(k.h));
+  u = u < 0 ? 0 : (u >= k.w ? k.w - 1 : u);
+  v = v < 0 ? 0 : (v >= k.h ? k.h - 1 : v);
+  phi = kPi * (float(v) + 0.5f) / float(k.h);
+  float area = std::sin(phi) * 2.0f * kPi / float(k.w * k.h);
+  return k.data[v * k.w + u] / area;
+}
+
+// sampleDirectLight, src/sampling.cpp:467-527. gen_of(T) yields the generator
+// of light sample T (one stream for all T in the reference).
+template <class GenOf>
+static void direct_light(const Scene& s, const Bsdf& bs, int cnt, GenOf&& gen_of, std::vector<LSample>& out) {
+  const vec3& pos = bs.s.pos;
+  if (s.sky.empty()) {
+    std::vector<float> w;
+    w.reserve(s.lights.size());
+    for (const Light& lo : s.lights) {  // getLightObjectWeight, :406-417
+      vec3 ld = normalize(lo.center - pos);
+      float dist = length(lo.center - pos);
+      vec3 f = bs.eval(ld);
+      w.push_back(dot(f, kLum) * lo.power / (dist * dist + kLightRadius));
+    }
+    float tot = 0.0f;
+    for (float x : w) tot += x;
+    if (tot == 0.0f) return;
+    for (int T = 0; T < cnt; ++T) {
+      auto& gen = gen_of(T);
+      float rv = tot * gen();  // sample(), :396-404
+      int li = -1;
+      float acc = 0.0f;
+      for (size_t i = 0; i < w.size(); ++i) {
+        acc += w[i];
+        if (rv <= acc) { li = (int)i; break; }
+      }
+      if (li == -1) continue;
+      float pl = w[li] / tot;
+      const Light& lo = s.lights[li];
+      vec3 lp;
+      int fails = 0;
+      light_point(s, lo, pos, gen, lp, fails);
+      if (!any_finite(lp)) continue;
+      vec3 ld = normalize(lp - pos);
+      float dist = length(lp - pos);
+      if (occluded(s, {pos, ld}, dist - kEps)) continue;
+      vec3 f = bs.eval(ld);
+      lum_clamp(f);
+      vec3 L = 2.0f * kPi * lo.power * lo.color / (dist * dist + kLightRadius) / pl;
+      out.push_back({f, L, 1.0f / (float)(cnt * (fails + 1))});
+    }
+  } else {
+    for (int T = 0; T < cnt; ++T) {
+      auto& gen = gen_of(T);
+      vec3 dir, L;
+      sky_dir(s.sky, bs.s.surfN, gen, dir, L);
+      if (!any_finite(dir)) continue;
+      if (occluded(s, {pos, dir}, INFINITY)) continue;
+      vec3 f = bs.eval(dir);
+      lum_clamp(f);
+      out.push_back({f, L, 1.0f / (float)cnt});
+    }
+  }
+}
+
+// ---------------------------------------------------------- integrator -----
+// One indirect sample from the first vertex: sampleIndirectLightFromFirst-
+// Intersection (src/render.cpp:314-423) followed by the sampleRay recursion
+// (:121-312), unrolled into a loop. The recursion hands samples back up and
+// multiplies each vertex's factor into them innermost first (passBsdf,
+// mulWeight, :101-116); the loop keeps the per-depth factors and applies them
+// in that order so the float products match.
+template <class G>
+static void indirect_path(const Scene& s, const Surf& g, const vec3& eye, int maxd, G& gen,
+                          std::vector<LSample>& out) {
+  if (length(g.emis) > 0) return;
+  vec3 in = normalize(g.pos - eye);
+  Bsdf b0{-in, g};
+  float rf = g.roughness * 1.0f;
+  b0.s.eta = 1.0f / b0.s.eta;
+  float p_reflect = 1.0f;  // opaque first vertex
+  vec3 dir, w0 = vec3(NAN);
+  int f0 = 0;
+  if (!(gen() < p_reflect)) return;  // refraction branch: glass is not restated
+  b0.sample_reflect(gen, dir, w0, f0);
+  w0 /= p_reflect;
+  if (!any_finite(dir)) return;
+
+  vec3 fac[18];
+  int fails[18];
+  Ray ray{b0.s.pos, dir};
+  bool exclude = true;
+  std::vector<LSample> term;
+  int depth = 1;
+  for (;; ++depth) {
+    term.clear();
+    Hit h = closest(s, ray);
+    if (h.tmax == INFINITY) {
+      if (!exclude && !s.sky.empty()) term.push_back({vec3(1.0f), sky_get(s.sky, ray.d), 1.0f});
+      break;
+    }
+    Bsdf bs{-ray.d, Surf()};
+    bs.s.pos = ray.o + ray.d * h.tmax;
+    hit_info(s, s.tris[h.face], ray, bs.s);
+    rf = std::max(rf, 1.0f * bs.s.roughness);
+    bs.s.roughness = std::max(bs.s.roughness, rf);
+    const float p_rr = 1.0f + (0.5f - 1.0f) * std::sqrt(bs.s.roughness);
+    bool nee = p_rr < 0.9f;
+    const vec3 absorb(1.0f);  // getAbsorb in air, :83-87
+    if (length(bs.s.emis) > kEps) {
+      if (!exclude) term.push_back({absorb, bs.s.emis, 1.0f});
+      break;
+    }
+    float pr = 1.0f;
+    if (!(gen() <= pr)) break;  // opaque surfaces always reflect
+    nee = nee && bs.s.entering;
+    if (nee && (depth >= maxd || gen() > p_rr)) {
+      int cnt = kSampleCount[std::min(depth, 16)];
+      direct_light(s, bs, cnt, [&](int) -> G& { return gen; }, term);
+      float k = 1.0f / pr;
+      if (depth < maxd) k /= (1.0f - p_rr);
+      for (LSample& x : term) x.bsdf *= k;
+      break;
+    }
+    vec3 nd, w;
+    int nf = 0;
+    bs.sample_reflect(gen, nd, w, nf);
+    w /= pr;
+    if (nee) w /= p_rr;
+    if (!any_finite(nd) || depth == maxd) { term.clear(); break; }
+    w *= absorb;
+    fac[depth] = w;
+    fails[depth] = nf;
+    ray = {bs.s.pos, nd};
+    exclude = nee;
+  }
+  for (int k = depth - 1; k >= 1; --k) {
+    for (LSample& x : term) { x.light *= x.bsdf; x.bsdf = fac[k]; }
+    if (fails[k] > 0)
+      for (LSample& x : term) x.weight *= 1.0f / (float)(1 + fails[k]);
+  }
+  for (LSample& x : term) { x.light *= x.bsdf; x.bsdf = w0; }
+  if (f0 > 0)
+    for (LSample& x : term) x.weight *= 1.0f / (float)(1 + f0);
+  out.insert(out.end(), term.begin(), term.end());
+}
+
+struct Rad { vec3 r = vec3(0.0f); float var = 0.0f; };  // RadianceData
+
+// accumulateInwardRadiance(_basic), src/image.cpp:615-659: split into a
+// part along normalize(baseColor) (demodulated by |baseColor|) and the rest.
+static void acc_basic(Rad& r, const vec3& in, float w) {
+  if (!any_finite(in)) return;
+  if (!std::isfinite(w)) return;
+  r.r += in * w;
+  r.var += dot(in, in) * w;
+}
+static void accumulate(const vec3& base, const LSample& x, Rad& d, Rad& sp) {
+  if (length(x.light) < kEps) return;
+  vec3 b0 = normalize(base);
+  if (length(base) < kEps) { acc_basic(sp, x.light * x.bsdf, x.weight); return; }
+  static const vec3 white = normalize(vec3(1.0f));
+  float xy = dot(b0, white);
+  if (xy > 0.99f) { acc_basic(d, x.light * x.bsdf / base, x.weight); return; }
+  vec3 perp = normalize(cross(b0, white));
+  vec3 bp = x.bsdf - perp * dot(perp, x.bsdf);
+  float d1 = dot(bp, white), d2 = dot(bp, b0);
+  float apb = (d1 + d2) / (1 + xy), amb = (d1 - d2) / (1 - xy);
+  float B = (apb - amb) / 2.0f;
+  vec3 bb = B * b0;
+  acc_basic(d, x.light * B / length(base), x.weight);
+  acc_basic(sp, x.light * (x.bsdf - bb), x.weight);
+}
+static void calc_var(Rad& r, float e) {  // renderPixel's calcVar, src/render.cpp:510-516
+  r.r *= e;
+  r.var *= e * e;
+  r.var -= dot(r.r, r.r);
+  if (r.var < 0.0f) r.var = 0.0f;
+}
+
+struct Args {
+  vec3 pos, dir, up, right;
+  float accuracy, focus, coc, exposure, p_direct;
+  int w, h, spp, threads, maxd;
+};
+
+// Generator, src/component.cpp:5-10.
+struct MtGen {
+  std::mt19937 mt;
+  std::uniform_real_distribution<float> U;
+  explicit MtGen(uint32_t seed) : mt(seed), U(1e-6f, 1.0f - 1e-6f) {}
+  float operator()() { return U(mt); }
+};
+struct CtrGen {
+  RmnRng r;
+  float operator()() { return r.next(); }
+};
+
+// renderPixel, src/render.cpp:448-551. mode 0: one mt19937 per pixel seeded
+// with orc_pixel_seed (reference stream); mode 1: the library's counter
+// stream, one per (pixel, sample slot).
+static void render_pixel(const Scene& s, const Args& a, uint64_t seed, int mode, int x, int y, float* rec) {
+  std::memset(rec, 0, sizeof(float) * ORC_PIX_FLOATS);
+  const int id = y * a.w + x;
+  float rx = float(x) - float(a.w) / 2.0f, ry = float(y) - float(a.h) / 2.0f;
+  vec3 d = a.dir + a.accuracy * (rx * a.right + ry * a.up);
+  vec3 dir = normalize(d);
+  Ray ray{a.pos, dir};
+  Surf g;
+  Rad Dd, Ds, Id, Is;
+  int nsamples = 0, spp_i = 0;
+  Hit h = closest(s, ray);
+  vec3 base_out;
+  if (h.tmax == INFINITY) {
+    g.pos = vec3(NAN);
+    if (!s.sky.empty()) g.emis = sky_get(s.sky, dir);
+    base_out = g.base;
+  } else {
+    g.pos = ray.o + h.tmax * ray.d;
+    hit_info(s, s.tris[h.face], ray, g);
+    bool opaque = g.opacity > 1.0f - kEps;
+    vec3 keep = g.base;
+    float c0 = dot(g.base, kLum);
+    if (c0 < 2e-2 || (c0 < 0.8f && length(g.base / c0 - vec3(1.0f)) < 2e-2)) g.base[0] += 4e-2;
+    const int spp_d = int(float(a.spp) * a.p_direct);
+    spp_i = (a.spp - spp_d) * (opaque ? 1 : 16);
+
+    MtGen mt(orc_pixel_seed(seed, (uint32_t)id));
+    CtrGen ctr{rmn_rng(seed, (uint32_t)id, 0)};
+
+    // sampleDirectLightFromFirstIntersection, :425-437.
+    if (any_finite(g.pos) && !(length(g.emis) > 0)) {
+      vec3 in = normalize(g.pos - a.pos);
+      Bsdf bs{-in, g};
+      std::vector<LSample> ds;
+      if (mode == 0) {
+        direct_light(s, bs, spp_d, [&](int) -> MtGen& { return mt; }, ds);
+      } else {
+        direct_light(s, bs, spp_d, [&](int T) -> CtrGen& { ctr = CtrGen{rmn_rng(seed, (uint32_t)id, (uint32_t)T)}; return ctr; }, ds);
+      }
+      for (const LSample& x : ds) accumulate(g.base, x, Dd, Ds);
+    }
+    calc_var(Dd, a.exposure);
+    calc_var(Ds, a.exposure);
+
+    std::vector<LSample> samples;
+    for (int T = 0; T < spp_i; ++T) {
+      if (mode == 0) {
+        indirect_path(s, g, a.pos, a.maxd, mt, samples);
+      } else {
+        CtrGen c{rmn_rng(seed, (uint32_t)id, (uint32_t)(spp_d + T))};
+        indirect_path(s, g, a.pos, a.maxd, c, samples);
+      }
+    }
+    nsamples = (int)samples.size();
+    if (!samples.empty()) {
+      for (LSample& x : samples) x.weight *= 1.0f / (float)spp_i;
+      float mean = 0.0f;
+      for (const LSample& x : samples) mean += dot(x.bsdf * x.light, kLum) * x.weight;
+      vec3 base_acc = g.opacity < kEps ? vec3(0.0f) : g.base;
+      for (const LSample& x : samples) {  // per-pixel firefly clamp, :532-549
+        float c = dot(x.bsdf * x.light, kLum) * x.weight;
+        if (c / (mean - c + kEps) > 16.0f) continue;
+        accumulate(base_acc, x, Id, Is);
+      }
+      calc_var(Id, a.exposure);
+      calc_var(Is, a.exposure);
+      g.base = keep;
+    }
+    base_out = g.base;
+  }
+  const Rad* rr[4] = {&Dd, &Ds, &Id, &Is};
+  for (int k = 0; k < 4; ++k) {
+    rec[4 * k + 0] = rr[k]->r.x; rec[4 * k + 1] = rr[k]->r.y; rec[4 * k + 2] = rr[k]->r.z; rec[4 * k + 3] = rr[k]->var;
+  }
+  auto put3 = [&](int o, const vec3& v) { rec[o] = v.x; rec[o + 1] = v.y; rec[o + 2] = v.z; };
+  put3(16, base_out);
+  put3(19, g.emis);
+  put3(22, g.pos);
+  put3(25, g.shapeN);
+  put3(28, g.surfN);
+  rec[31] = g.roughness; rec[32] = g.metallic; rec[33] = g.opacity; rec[34] = g.specular; rec[35] = g.eta;
+  rec[36] = (float)g.id; rec[37] = g.entering ? 1.0f : 0.0f; rec[38] = (float)nsamples; rec[39] = (float)spp_i;
+}
+
+// ------------------------------------------------------------- post --------
+// Photo::shade(Full) + gammaCorrection, src/image.cpp:215-246 and :454-468.
+static vec3 compose(const float* rec, float exposure) {
+  vec3 rd = vec3(0.0f), rs = vec3(0.0f);
+  rd += vec3(rec[0], rec[1], rec[2]);
+  rs += vec3(rec[4], rec[5], rec[6]);
+  rd += vec3(rec[8], rec[9], rec[10]);
+  rs += vec3(rec[12], rec[13], rec[14]);
+  vec3 p = vec3(rec[16], rec[17], rec[18]) * rd + rs;
+  p += vec3(rec[19], rec[20], rec[21]) * exposure;
+  return p;
+}
+static vec3 gamma(vec3 p) {
+  p = glm::max(p, 0.0f);
+  float c = dot(p, kLum);
+  if (c > 0.75f) p = p / c * (std::tanh(3.0f * (c - 0.75f)) / 3.0f + 0.75f);
+  p = glm::min(p, 1.0f);
+  return glm::pow(p, vec3(1.0f / 2.2f));
+}
+
+// Photo::FXAA, src/image.cpp:358-452.
+static void fxaa(const float* in, float* out, int W, int H) {
+  auto px = [&](int x, int y) { const float* p = in + 3 * ((size_t)y * W + x); return vec3(p[0], p[1], p[2]); };
+  auto lum = [&](int x, int y) { return dot(px(x, y), kLum); };
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      vec3 c = px(x, y);
+      vec3 o = c;
+      float M = lum(x, y);
+      float N = y > 0 ? lum(x, y - 1) : M, S = y < H - 1 ? lum(x, y + 1) : M;
+      float E = x < W - 1 ? lum(x + 1, y) : M, Wl = x > 0 ? lum(x - 1, y) : M;
+      float lo = std::min({N, S, E, Wl}), hi = std::max({N, S, E, Wl});
+      float range = hi - lo;
+      if (!(range < std::max(0.0312f, hi * 0.125f))) {
+        float NW = (y > 0 && x > 0) ? lum(x - 1, y - 1) : M;
+        float NE = (y > 0 && x < W - 1) ? lum(x + 1, y - 1) : M;
+        float SW = (y < H - 1 && x > 0) ? lum(x - 1, y + 1) : M;
+        float SE = (y < H - 1 && x < W - 1) ? lum(x + 1, y + 1) : M;
+        float eh = std::abs((NW + Wl + SW) - (NE + E + SE)) * (1.0f / 3.0f);
+        float ev = std::abs((NW + N + NE) - (SW + S + SE)) * (1.0f / 3.0f);
+        bool horiz = eh >= ev;
+        float step = horiz ? 1.0f / float(W) : 1.0f / float(H);
+        float g = std::clamp((horiz ? eh : ev) / range, -2.0f, 2.0f);
+        vec2 uv(float(x) / float(W), float(y) / float(H));
+        vec3 best_c = c;
+        float best = 0.0f;
+        for (int i = 0; i < 12; ++i) {
+          float off = g * step * float(i + 1);
+          vec2 su = uv + vec2(horiz ? 0.0f : off, horiz ? off : 0.0f);
+          if (su.x < 0.0f || su.x > 1.0f || su.y < 0.0f || su.y > 1.0f) continue;
+          int sx = std::clamp(int(su.x * float(W)), 0, W - 1), sy = std::clamp(int(su.y * float(H)), 0, H - 1);
+          vec3 sc = px(sx, sy);
+          float dl = std::abs(dot(sc, kLum) - M);
+          if (dl > best) { best = dl; best_c = sc; }
+        }
+        float sub = std::min((std::abs(N + S - 2.0f * M) * 2.0f + std::abs(E + Wl - 2.0f * M)) * 0.25f, 1.0f);
+        o = glm::mix(c, best_c, sub * 0.75f);
+      }
+      float* q = out + 3 * ((size_t)y * W + x);
+      q[0] = o.x; q[1] = o.y; q[2] = o.z;
+    }
+}
+
+template <class F>
+static void parallel_for(long n, int threads, F&& f) {
+  if (threads <= 1 || n < 64) { for (long i = 0; i < n; ++i) f(i); return; }
+  std::atomic<long> next(0);
+  std::vector<std::thread> pool;
+  for (int t = 0; t < threads; ++t)
+    pool.emplace_back([&] {
+      for (;;) {
+        long i0 = next.fetch_add(64);
+        if (i0 >= n) break;
+        long i1 = std::min(n, i0 + 64);
+        for (long i = i0; i < i1; ++i) f(i);
+      }
+    });
+  for (auto& t : pool) t.join();
+}
+
+}  // namespace orc
+
+using namespace orc;
+
+extern "C" {
+
+// Model construction for the configs: Model::processMesh / checkLightObject /
+// SkyBox::Init / BVH::build (src/model.cpp:44-123,172-215,
+// src/component.cpp:54-67, src/bvh.cpp:48-54) on arrays instead of assimp.
+void* port_scene_create(const orc_scene_in* in) {
+  Scene* s = new Scene();
+  s->nrm.resize(in->num_vertices);
+  s->uv.resize(in->num_vertices);
+  for (int i = 0; i < in->num_vertices; ++i) {
+    s->nrm[i] = in->normals ? vec3(in->normals[3 * i], in->normals[3 * i + 1], in->normals[3 * i + 2]) : vec3(0.0f);
+    s->uv[i] = in->uvs ? vec2(in->uvs[2 * i], in->uvs[2 * i + 1]) : vec2(0.0f);
+  }
+  for (int m = 0; m < in->num_materials; ++m) {
+    const float* p = in->materials + ORC_MAT_FLOATS * m;
+    Mat q;
+    q.base = vec3(p[0], p[1], p[2]); q.has_base = p[3] != 0.0f;
+    q.emis = vec3(p[4], p[5], p[6]); q.has_emis = p[7] != 0.0f;
+    q.roughness = p[8]; q.metallic = p[9]; q.has_surf = p[10] != 0.0f;
+    q.opacity = p[11]; q.ior = p[12]; q.trans = vec3(p[13], p[14], p[15]);
+    q.id = m;
+    s->mats.push_back(q);
+  }
+  s->tris.reserve(in->num_triangles);
+  for (int mesh = 0; mesh < in->num_meshes; ++mesh) {
+    int first = in->mesh_first[mesh], last = in->mesh_first[mesh + 1], mat = in->mesh_material[mesh];
+    size_t off = s->tris.size();
+    for (int t = first; t < last; ++t) {
+      Tri f;
+      for (int k = 0; k < 3; ++k) {
+        int v = in->indices[3 * t + k];
+        f.vid[k] = v;
+        f.v[k] = vec3(in->positions[3 * v], in->positions[3 * v + 1], in->positions[3 * v + 2]);
+      }
+      f.mat = mat;
+      f.id = t;
+      s->tris.push_back(f);
+    }
+    const Mat& M = s->mats[mat];
+    if (!M.has_emis) continue;
+    // checkLightObject: the average emissive colour of a constant texel over
+    // the 8x8 grid is 64 equal adds divided by 64.
+    Light lo;
+    vec3 col(0.0f);
+    std::vector<float> fw;
+    for (size_t j = off; j < s->tris.size(); ++j) {
+      const Tri& f = s->tris[j];
+      vec3 avg(0.0f);
+      for (int i = 0; i < 64; ++i) avg += M.emission();
+      avg = avg / static_cast<float>(64);
+      float cl = dot(avg, kLum), area = length(cross(f.v[1] - f.v[0], f.v[2] - f.v[0])) / 2.0f;
+      if (cl < kEps || area < kEps) continue;
+      col += avg * area;
+      lo.faces.push_back(f);
+      fw.push_back(area * cl);
+    }
+    if (lo.faces.empty()) continue;
+    lo.color = col / dot(col, kLum);
+    for (size_t j = 0; j < lo.faces.size(); ++j) {
+      lo.power += fw[j];
+      lo.center += tri_center(lo.faces[j]) * fw[j];
+    }
+    prefix_init(lo.prefix, fw);
+    lo.center /= lo.power;
+    s->lights.push_back(lo);
+  }
+  if (in->env_rgb && in->env_width > 0 && in->env_height > 0) {
+    Sky& k = s->sky;
+    k.w = in->env_width; k.h = in->env_height;
+    k.data.resize((size_t)k.w * k.h);
+    std::vector<float> wts;
+    wts.reserve(k.data.size());
+    for (int v = 0; v < k.h; ++v)
+      for (int u = 0; u < k.w; ++u) {
+        size_t i = (size_t)v * k.w + u;
+        k.data[i] = vec3(in->env_rgb[3 * i], in->env_rgb[3 * i + 1], in->env_rgb[3 * i + 2]);
+        float phi = kPi * (float(v) + 0.5f) / float(k.h);
+        float area = std::sin(phi) * 2.0f * kPi / float(k.w * k.h);
+        k.data[i] *= area;
+        wts.push_back(dot(k.data[i], kLum));
+      }
+    prefix_init(k.prefix, wts);
+  }
+  int n = (int)s->tris.size();
+  s->nodes.assign(heap_slots(1, n) + 1, Node());
+  if (n > 0) build_rec(*s, 1, 0, n);
+  return s;
+}
+
+void port_scene_destroy(void* h) { delete static_cast<Scene*>(h); }
+
+int port_bvh_size(void* h) { return (int)static_cast<Scene*>(h)->nodes.size(); }
+
+void port_bvh_export(void* h, float* boxes, int32_t* ranges, int32_t* order) {
+  const Scene& s = *static_cast<Scene*>(h);
+  for (size_t u = 0; u < s.nodes.size(); ++u) {
+    const Node& n = s.nodes[u];
+    float b[6] = {n.box.lo.x, n.box.lo.y, n.box.lo.z, n.box.hi.x, n.box.hi.y, n.box.hi.z};
+    std::memcpy(boxes + 6 * u, b, sizeof b);
+    ranges[2 * u] = n.faceL;
+    ranges[2 * u + 1] = n.faceR;
+  }
+  for (size_t i = 0; i < s.tris.size(); ++i) order[i] = s.tris[i].id;
+}
+
+// Light objects: per light 8 floats (center, color, power, face count).
+int port_light_count(void* h) { return (int)static_cast<Scene*>(h)->lights.size(); }
+void port_light_export(void* h, float* out) {
+  const Scene& s = *static_cast<Scene*>(h);
+  for (size_t i = 0; i < s.lights.size(); ++i) {
+    const Light& l = s.lights[i];
+    float r[8] = {l.center.x, l.center.y, l.center.z, l.color.x, l.color.y, l.color.z, l.power, (float)l.faces.size()};
+    std::memcpy(out + 8 * i, r, sizeof r);
+  }
+}
+
+// rays: 8 floats each (origin, t_min, direction, t_max). Model::rayHit always
+// uses t_min = 1e-4, t_max = inf; other bounds go straight to the BVH query.
+// Output: input triangle index (-1 on a miss), t, barycentrics (gamma, alpha, beta).
+void port_trace_closest(void* h, const float* rays, int64_t n, int32_t* face, float* t, float* bc, int threads) {
+  const Scene& s = *static_cast<Scene*>(h);
+  parallel_for(n, threads, [&](long i) {
+    const float* r = rays + 8 * i;
+    Ray ray{vec3(r[0], r[1], r[2]), vec3(r[4], r[5], r[6])};
+    Hit hh{r[3], r[7], -1};
+    traverse(s, ray, hh, nullptr);
+    if (hh.face < 0) {
+      face[i] = -1; t[i] = hh.tmax; bc[3 * i] = bc[3 * i + 1] = bc[3 * i + 2] = 0.0f;
+      return;
+    }
+    const Tri& f = s.tris[hh.face];
+    face[i] = f.id;
+    t[i] = hh.tmax;
+    vec3 b = bary(f.v[0], f.v[1], f.v[2], ray.o + ray.d * hh.tmax);
+    bc[3 * i] = b.x; bc[3 * i + 1] = b.y; bc[3 * i + 2] = b.z;
+  });
+}
+
+// rays: 8 floats each (origin, unused, direction, aim depth) -> occluded.
+void port_trace_shadow(void* h, const float* rays, int64_t n, uint8_t* occ, int threads) {
+  const Scene& s = *static_cast<Scene*>(h);
+  parallel_for(n, threads, [&](long i) {
+    const float* r = rays + 8 * i;
+    occ[i] = occluded(s, {vec3(r[0], r[1], r[2]), vec3(r[4], r[5], r[6])}, r[7]) ? 1 : 0;
+  });
+}
+
+// Node and triangle visit counts of the closest-hit (mode 0) or shadow
+// (mode 1) queries of a ray batch: out = {inner nodes, leaves, triangles}.
+void port_trace_stats(void* h, const float* rays, int64_t n, int mode, uint64_t* out) {
+  const Scene& s = *static_cast<Scene*>(h);
+  Stats st;
+  for (int64_t i = 0; i < n; ++i) {
+    const float* r = rays + 8 * i;
+    Ray ray{vec3(r[0], r[1], r[2]), vec3(r[4], r[5], r[6])};
+    if (mode == 0) { Hit hh{r[3], r[7], -1}; traverse(s, ray, hh, &st); }
+    else occluded(s, ray, r[7], &st);
+  }
+  out[0] = st.inner; out[1] = st.leaves; out[2] = st.tris;
+}
+
+static Args unpack_args(const float* p) {
+  Args a;
+  a.pos = vec3(p[0], p[1], p[2]); a.dir = vec3(p[3], p[4], p[5]); a.up = vec3(p[6], p[7], p[8]);
+  a.right = vec3(p[9], p[10], p[11]);
+  a.accuracy = p[12]; a.focus = p[13]; a.coc = p[14]; a.exposure = p[15]; a.p_direct = p[16];
+  a.w = (int)p[17]; a.h = (int)p[18]; a.spp = (int)p[19]; a.threads = (int)p[20]; a.maxd = (int)p[21];
+  if (a.maxd <= 0 || a.maxd > 16) a.maxd = 16;
+  return a;
+}
+
+// Renders the pixel rectangle [x0,x1) x [y0,y1) of the image described by
+// args; out holds ORC_PIX_FLOATS per pixel of the rectangle, row-major.
+void port_render(void* h, const float* args, uint64_t seed, int mode, int x0, int y0, int x1, int y1, float* out,
+                 int threads) {
+  const Scene& s = *static_cast<Scene*>(h);
+  Args a = unpack_args(args);
+  int rw = x1 - x0;
+  long n = (long)rw * (y1 - y0);
+  parallel_for(n, threads, [&](long i) {
+    int x = x0 + (int)(i % rw), y = y0 + (int)(i / rw);
+    render_pixel(s, a, seed, mode, x, y, out + ORC_PIX_FLOATS * i);
+  });
+}
+
+// Photo::shade(Full) [+ gammaCorrection] over pixel records -> rgb.
+void port_compose(const float* recs, int64_t n, float exposure, int apply_gamma, float* rgb) {
+  for (int64_t i = 0; i < n; ++i) {
+    vec3 p = compose(recs + ORC_PIX_FLOATS * i, exposure);
+    if (apply_gamma) p = gamma(p);
+    rgb[3 * i] = p.x; rgb[3 * i + 1] = p.y; rgb[3 * i + 2] = p.z;
+  }
+}
+
+void port_gamma(const float* in, int64_t n, float* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    vec3 p = gamma(vec3(in[3 * i], in[3 * i + 1], in[3 * i + 2]));
+    out[3 * i] = p.x; out[3 * i + 1] = p.y; out[3 * i + 2] = p.z;
+  }
+}
+
+void port_fxaa(const float* in, float* out, int w, int h) { fxaa(in, out, w, h); }
+
+}  // extern "C"

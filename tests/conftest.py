@@ -1,0 +1,32 @@
+import os
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+    config.addinivalue_line("markers", "slow: long-running CPU test")
+
+
+@pytest.fixture(scope="session")
+def port():
+    from oracle import bindings
+    if not os.path.exists(bindings.PORT_SO):
+        bindings.build(with_reference=False)
+    return bindings.OracleLib("port")
+
+
+@pytest.fixture(scope="session")
+def ref():
+    from oracle import bindings
+    if not bindings.have_ref():
+        if os.path.isdir(os.path.join(bindings.REFERENCE_DIR, "src")):
+            bindings.build(with_reference=True)
+        else:
+            pytest.skip("the reference checkout is not on this machine; parity is carried by tests/golden")
+    return bindings.OracleLib("ref")

@@ -1,0 +1,124 @@
+"""Generate the golden fixtures of tests/golden from the reference itself.
+
+Run in a checkout that has the reference sources (the oracle/_ref harness is
+built from them): ``python tests/golden/make_golden.py``. Every fixture stores
+its inputs (scene arrays, rays, camera, seed) next to the reference's outputs,
+so machines without the reference -- and platforms whose numpy math differs in
+the last bit -- check the CPU restatement against the same numbers.
+
+Fixtures (numpy .npz, compressed):
+  trace_soup.npz     2,000-triangle soup + 4,096 closest-hit rays (incl.
+                     axis-parallel and duplicate-triangle tie cases) and 4,096
+                     shadow rays -> face ids, t, barycentrics, occlusion,
+                     reachable BVH nodes and the leaf-order face permutation.
+  render_cornell.npz 24 x 24 Cornell render, 16 spp, reference mt19937 stream.
+  render_sky.npz     16 x 12 render of a small heightfield under a lat-long
+                     sky (sky-mode light sampling, smooth normals).
+  post.npz           Photo::shade(Full) + gammaCorrection of render records,
+                     and Photo::FXAA of a 96 x 64 image with hard edges.
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import bindings  # noqa: E402
+from raym0nade_gb300 import scenes  # noqa: E402
+
+
+def scene_arrays(s):
+    d = dict(positions=s.positions, normals=s.normals, uvs=s.uvs, indices=s.indices, mesh_first=s.mesh_first,
+             mesh_material=s.mesh_material, materials=s.materials)
+    if s.env is not None:
+        d["env"] = s.env
+    return d
+
+
+def scene_from(z, prefix=""):
+    g = lambda k: z[prefix + k]
+    env = z[prefix + "env"] if (prefix + "env") in z else None
+    return scenes.Scene(g("positions"), g("normals"), g("uvs"), g("indices"), g("mesh_first"), g("mesh_material"),
+                        g("materials"), env)
+
+
+def reachable(ranges):
+    out, st = [], [1]
+    while st:
+        u = st.pop()
+        out.append(u)
+        if ranges[u, 1] == 0:
+            st += [2 * u, 2 * u + 1]
+    return np.array(sorted(out), np.int64)
+
+
+def tie_soup(n, seed):
+    """Random soup with a few exact duplicate triangles (exact t ties)."""
+    s = scenes.random_soup(n, seed)
+    k = 50
+    dup = s.indices[:k]
+    s.indices = np.concatenate([s.indices, dup]).astype(np.int32)
+    s.mesh_first = np.array([0, s.indices.shape[0]], np.int32)
+    return s
+
+
+def edge_rays(n, seed):
+    r = scenes.random_rays(n, seed)
+    # a quarter of the rays with one or two direction components below the
+    # 1e-4 axis-parallel cut-off of rayInBox
+    q = n // 4
+    r[:q, 4 + (np.arange(q) % 3)] = np.float32(5e-5)
+    r[: q // 2, 4 + ((np.arange(q // 2) + 1) % 3)] = np.float32(-2e-5)
+    d = r[:, 4:7].astype(np.float64)
+    r[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    return r
+
+
+def main():
+    bindings.build(with_reference=True)
+    R = bindings.OracleLib("ref")
+
+    soup = tie_soup(2000, 11)
+    rays = edge_rays(4096, 12)
+    srays = scenes.random_rays(4096, 13, shadow=True)
+    rs = R.scene(soup)
+    boxes, ranges, order = rs.bvh()
+    u = reachable(ranges)
+    face, t, bc = rs.trace_closest(rays)
+    occ = rs.trace_shadow(srays)
+    np.savez_compressed(os.path.join(HERE, "trace_soup.npz"), **scene_arrays(soup), rays=rays, shadow_rays=srays,
+                        face=face, t=t, bary=bc, occluded=occ, nodes=u, boxes=boxes[u], ranges=ranges[u], order=order)
+
+    cor = scenes.cornell()
+    cam = scenes.cornell_camera(24, 24, 16)
+    rec = R.scene(cor).render(cam, seed=2024)
+    np.savez_compressed(os.path.join(HERE, "render_cornell.npz"), **scene_arrays(cor), args=cam.packed(), seed=2024,
+                        records=rec)
+
+    hf = scenes.heightfield(24, seed=5, extent=3.0, patch=8)
+    hf.env = scenes.sky_env(64, 32, sun_radiance=50.0, sun_diameter_deg=12.0)
+    hcam = scenes.Camera((0.2, 1.6, -0.6), (0.35, -0.45, 0.82), (0.0, -1.0, 0.0), (-1.0, 0.0, 0.0), 0.05, 16, 12, 8)
+    hrec = R.scene(hf).render(hcam, seed=77)
+    np.savez_compressed(os.path.join(HERE, "render_sky.npz"), **scene_arrays(hf), args=hcam.packed(), seed=77,
+                        records=hrec)
+
+    rgb_lin = R.compose(rec, 1.0, gamma=False)
+    rgb = R.compose(rec, 1.0, gamma=True)
+    rng = np.random.default_rng(14)
+    img = np.zeros((64, 96, 3), np.float32)
+    img[:, 40:] = 0.9
+    img[20:44, 10:30] = rng.random((24, 20, 3)).astype(np.float32)
+    yy, xx = np.mgrid[0:64, 0:96]
+    img[(xx - 70) ** 2 + (yy - 30) ** 2 < 200] = (0.1, 0.2, 0.05)
+    img += rng.random(img.shape).astype(np.float32) * 0.05
+    fx = R.fxaa(img)
+    np.savez_compressed(os.path.join(HERE, "post.npz"), records=rec, linear=rgb_lin, display=rgb, fxaa_in=img,
+                        fxaa_out=fx)
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,128 @@
+"""Pin the CPU restatement (oracle/port) against the reference.
+
+Two sources of truth:
+* the reference's own sources compiled with shims (oracle/_ref, fixture
+  ``ref``) -- only where the reference checkout exists;
+* the committed fixtures of tests/golden, generated from that build by
+  tests/golden/make_golden.py -- everywhere.
+Everything here is integer/bit-level: identical trees, identical hit ids and
+t, identical occlusion answers, bit-identical renders under the reference's
+own mt19937 stream, bit-identical composite and FXAA.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from raym0nade_gb300 import scenes
+from tests.golden.make_golden import edge_rays, reachable, scene_from, tie_soup
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def same(a, b):
+    return np.array_equal(np.asarray(a), np.asarray(b), equal_nan=True)
+
+
+# ------------------------------------------------------------ golden ------
+def test_golden_trace(port):
+    z = np.load(os.path.join(GOLDEN, "trace_soup.npz"))
+    ps = port.scene(scene_from(z))
+    boxes, ranges, order = ps.bvh()
+    u = z["nodes"]
+    assert same(reachable(ranges), u)
+    assert same(boxes[u], z["boxes"]) and same(ranges[u], z["ranges"]) and same(order, z["order"])
+    face, t, bc = ps.trace_closest(z["rays"])
+    assert same(face, z["face"]) and same(t, z["t"]) and same(bc, z["bary"])
+    assert same(ps.trace_shadow(z["shadow_rays"]), z["occluded"])
+
+
+@pytest.mark.parametrize("name", ["render_cornell", "render_sky"])
+def test_golden_render(port, name):
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    a = z["args"]
+    cam = scenes.Camera(tuple(a[0:3]), tuple(a[3:6]), tuple(a[6:9]), tuple(a[9:12]), float(a[12]), int(a[17]),
+                        int(a[18]), int(a[19]), float(a[16]), float(a[15]), float(a[13]), float(a[14]), int(a[21]))
+    rec = port.scene(scene_from(z)).render(cam, seed=int(z["seed"]), mode=0)
+    ref = z["records"]
+    assert same(rec[..., :38], ref[..., :38])
+
+
+def test_golden_post(port):
+    z = np.load(os.path.join(GOLDEN, "post.npz"))
+    assert same(port.compose(z["records"], 1.0, gamma=False), z["linear"])
+    assert same(port.compose(z["records"], 1.0, gamma=True), z["display"])
+    assert same(port.fxaa(z["fxaa_in"]), z["fxaa_out"])
+
+
+# ------------------------------------------------- live reference ---------
+def _pair(port, ref, scene):
+    return port.scene(scene), ref.scene(scene)
+
+
+@pytest.mark.parametrize("n,seed", [(1, 1), (7, 2), (10, 3), (11, 4), (3000, 5), (20011, 6)])
+def test_bvh_matches_reference(port, ref, n, seed):
+    ps, rs = _pair(port, ref, scenes.random_soup(n, seed))
+    bp, rp, op = ps.bvh()
+    br, rr, orr = rs.bvh()
+    assert bp.shape == br.shape
+    u = reachable(rr)
+    assert same(reachable(rp), u)
+    assert same(bp[u], br[u]) and same(rp[u], rr[u]) and same(op, orr)
+
+
+def test_cornell_lights_match_reference(port, ref):
+    ps, rs = _pair(port, ref, scenes.cornell())
+    assert same(ps.lights(), rs.lights())
+
+
+@pytest.mark.parametrize("n", [1, 10, 5000])
+def test_trace_matches_reference(port, ref, n):
+    s = tie_soup(n, 21) if n > 60 else scenes.random_soup(n, 21)
+    ps, rs = _pair(port, ref, s)
+    rays = edge_rays(30000, 22)
+    if n <= 10:  # aim every ray at the few triangles
+        tgt = s.positions.reshape(-1, 3, 3).mean(1)[np.arange(rays.shape[0]) % n]
+        d = tgt - rays[:, 0:3]
+        rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    a, b = ps.trace_closest(rays), rs.trace_closest(rays)
+    for x, y in zip(a, b):
+        assert same(x, y)
+    sr = scenes.random_rays(30000, 23, shadow=True)
+    assert same(ps.trace_shadow(sr), rs.trace_shadow(sr))
+
+
+def test_trace_cornell_matches_reference(port, ref):
+    ps, rs = _pair(port, ref, scenes.cornell())
+    rays = scenes.random_rays(20000, 31)
+    rays[:, 0:3] = rays[:, 0:3] * 0.98 + 0.01  # inside the room
+    for x, y in zip(ps.trace_closest(rays), rs.trace_closest(rays)):
+        assert same(x, y)
+
+
+@pytest.mark.parametrize("spp,p_direct", [(16, 0.7), (5, 0.0), (3, 1.0), (9, 0.5)])
+def test_render_cornell_matches_reference(port, ref, spp, p_direct):
+    ps, rs = _pair(port, ref, scenes.cornell())
+    cam = scenes.cornell_camera(20, 20, spp, p_direct=p_direct)
+    a = ps.render(cam, seed=5 + spp)
+    b = rs.render(cam, seed=5 + spp)
+    assert same(a[..., :38], b[..., :38])
+
+
+def test_render_sky_matches_reference(port, ref):
+    hf = scenes.heightfield(20, seed=8, extent=3.0, patch=6)
+    hf.env = scenes.sky_env(48, 24, sun_radiance=80.0, sun_diameter_deg=15.0)
+    ps, rs = _pair(port, ref, hf)
+    cam = scenes.Camera((0.2, 1.6, -0.6), (0.35, -0.45, 0.82), (0.0, -1.0, 0.0), (-1.0, 0.0, 0.0), 0.05, 14, 10, 12)
+    assert same(ps.render(cam, seed=3)[..., :38], rs.render(cam, seed=3)[..., :38])
+
+
+def test_post_matches_reference(port, ref):
+    rng = np.random.default_rng(3)
+    img = (rng.random((37, 53, 3)) ** 3).astype(np.float32) * 1.4
+    img[:, 20:] += 0.5
+    assert same(port.fxaa(img), ref.fxaa(img))
+    assert same(port.gamma(img), ref.gamma(img))
+    rec = rng.random((500, 40)).astype(np.float32)
+    for g in (False, True):
+        assert same(port.compose(rec, 1.3, gamma=g), ref.compose(rec, 1.3, gamma=g))
