@@ -1,0 +1,186 @@
+/*
+ * rmn.h -- C ABI of the GB300 path-tracing core (librmn.so).
+ *
+ * This is the drop-in boundary behind the reference renderer's render.h
+ * (lemonchu/Raym0nade). The reference's only render entry point is
+ *     void render_multiThread(Model &model, const RenderArgs &args);
+ * (include/render.h:43, src/render.cpp:593-677), fed by a Model built from an
+ * FBX file (include/model.h:25-43) and RenderArgs (include/render.h:8-15).
+ * Under this ABI a caller:
+ *   1. describes the scene it would have loaded into Model as flat arrays
+ *      (rmn_scene_desc) and calls rmn_scene_create -- the host runs the
+ *      reference's BVH construction (src/bvh.cpp:18-54), light-object
+ *      construction (src/model.cpp:44-82) and sky tables
+ *      (src/component.cpp:54-67), then uploads everything to HBM;
+ *   2. renders with rmn_render (the renderPixel loop of render_multiThread,
+ *      src/render.cpp:448-551, 593-631) into caller-owned buffers;
+ *   3. post-processes with rmn_compose / rmn_fxaa (Photo::shade,
+ *      gammaCorrection and FXAA, src/image.cpp:215-246, 363-468).
+ * The ray queries of the reference's Model (Model::rayHit and
+ * Model::rayHit_test, include/model.h:41-42) are exported as
+ * rmn_trace_closest / rmn_trace_shadow.
+ *
+ * Conventions: every function returns an rmn_status; no C++ exception
+ * crosses the ABI; rmn_last_error() describes the last failure of the calling
+ * thread. Array arguments may be host memory (pageable or pinned) or device
+ * memory of the current device: the library detects which and stages host
+ * arrays through the device itself. `stream` is a cudaStream_t (NULL: the
+ * legacy default stream); calls return after their work on that stream has
+ * completed.
+ */
+#ifndef RMN_H
+#define RMN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum rmn_status {
+  RMN_OK = 0,
+  RMN_ERR_INVALID_ARGUMENT = 1,
+  RMN_ERR_CUDA = 2,           /* a CUDA runtime call failed (see rmn_last_error) */
+  RMN_ERR_OUT_OF_MEMORY = 3,
+  RMN_ERR_UNSUPPORTED = 4,    /* feature outside the GPU path (e.g. glass), see rmn_last_error */
+  RMN_ERR_DEVICE_LIMIT = 5,   /* a kernel hit one of its bounds (stack depth, wait limit) and stopped */
+  RMN_ERR_INTERNAL = 6
+} rmn_status;
+
+/* Constant-texel material, 16 floats. The reference's Material
+ * (include/material.h:26-50) samples textures; a material here holds at most
+ * one constant texel per slot, resolved exactly as Material::getDiffuseColor,
+ * getEmissiveColor and getSurfaceData resolve a texel (src/material.cpp:
+ * 349-383). */
+typedef struct rmn_material {
+  float base_color[3];   /* diffuse texel, linear RGB */
+  float has_base;        /* 0: no diffuse texture -> white */
+  float emission[3];     /* emissive texel, linear RGB */
+  float has_emission;    /* 0: no emissive texture -> black, and no light object */
+  float roughness;       /* specular texel G, or Material::roughness without one */
+  float metallic;        /* specular texel B (clamped to <= 0.99); 0 without one */
+  float has_specular;    /* 1: roughness/metallic come from a specular texel */
+  float opacity;         /* 1 opaque; < 1e-4 transmissive (not on the GPU path) */
+  float ior;
+  float transmitting_color[3];
+} rmn_material;
+
+/* Scene arrays; what Model::Model builds from an assimp scene
+ * (src/model.cpp:84-123,172-215). Triangles are grouped in meshes with one
+ * material each; a mesh whose material has an emissive texel becomes one
+ * light object (checkLightObject, src/model.cpp:44-82). */
+typedef struct rmn_scene_desc {
+  int32_t num_vertices;
+  const float* positions;      /* 3 per vertex */
+  const float* normals;        /* 3 per vertex, or NULL */
+  const float* uvs;            /* 2 per vertex, or NULL */
+  int32_t num_triangles;
+  const int32_t* indices;      /* 3 per triangle */
+  int32_t num_meshes;
+  const int32_t* mesh_first;   /* num_meshes + 1 triangle offsets, mesh_first[0] = 0 */
+  const int32_t* mesh_material;
+  int32_t num_materials;
+  const rmn_material* materials;
+  int32_t env_width, env_height;  /* lat-long sky (SkyBox, include/component.h:56-67) */
+  const float* env_rgb;           /* 3 per texel, row 0 = zenith; NULL: no sky */
+} rmn_scene_desc;
+
+typedef struct rmn_scene rmn_scene;
+
+typedef struct rmn_scene_info {
+  int32_t num_triangles;
+  int32_t num_inner_nodes;     /* 64-byte two-child nodes in HBM */
+  int32_t bvh_depth;           /* deepest leaf, root = 0 */
+  int32_t heap_slots;          /* node-array size of the reference builder */
+  int32_t num_lights;
+  int32_t num_materials;
+  int64_t device_bytes;
+} rmn_scene_info;
+
+/* A ray: 8 floats (origin, t_min, direction, t_max). Model::rayHit queries
+ * use t_min = 1e-4, t_max = +inf (src/model.cpp:333). */
+typedef struct rmn_ray {
+  float origin[3];
+  float t_min;
+  float dir[3];
+  float t_max;
+} rmn_ray;
+
+/* Closest hit: input triangle index (-1: miss), t, and the reference's
+ * barycentric(v0, v1, v2, origin + t dir) (src/geometry.cpp:89-103). */
+typedef struct rmn_hit {
+  int32_t face;
+  float t;
+  float bary[2]; /* (alpha, beta); gamma = 1 - alpha - beta */
+} rmn_hit;
+
+/* RenderArgs (include/render.h:8-15) plus the GPU's own knobs. */
+typedef struct rmn_render_args {
+  float position[3], direction[3], up[3], right[3];
+  float accuracy, focus, CoC, exposure, P_Direct;
+  int32_t width, height, spp, threads; /* threads: ignored on the GPU */
+  int32_t max_depth;                   /* 16 in the reference (src/render.cpp:125); 1..16 */
+  uint64_t seed;                       /* counter-based random stream key */
+  int32_t lanes_per_pixel;             /* 0: autotuned; else 1,2,4,8,16,32 */
+  int32_t reserved[3];
+} rmn_render_args;
+
+/* Caller-owned per-pixel outputs (width*height entries each, row-major).
+ * radiance_*: 4 floats per pixel (RadianceData: rgb, Var) for
+ * direct/indirect x diffuse/specular (Photo, include/image.h:36-39).
+ * gbuffer: 20 floats per pixel, the HitInfo of the primary hit
+ * (include/model.h:12-18) -- base colour[3], emission[3], position[3]
+ * (NaN: the primary ray missed), shape normal[3], surface normal[3],
+ * roughness, metallic, opacity, eta, material id. rmn_render needs the four
+ * radiance buffers; gbuffer may be NULL (then it lives in scratch memory). */
+typedef struct rmn_image {
+  float* radiance_Dd;
+  float* radiance_Ds;
+  float* radiance_Id;
+  float* radiance_Is;
+  float* gbuffer;
+} rmn_image;
+#define RMN_GBUFFER_FLOATS 20
+
+/* Photo::ShadeOption bits (include/image.h:17-34) used by rmn_compose. */
+enum {
+  RMN_SHADE_BASECOLOR = 1, RMN_SHADE_EMISSION = 2, RMN_SHADE_DIRECT = 4, RMN_SHADE_INDIRECT = 8,
+  RMN_SHADE_DIFFUSE = 16, RMN_SHADE_SPECULAR = 32, RMN_SHADE_FULL = 63,
+  RMN_SHADE_GAMMA = 4096, /* apply Photo::gammaCorrection */
+  RMN_SHADE_FXAA = 512    /* then Photo::FXAA (display-referred, as postProcessing does) */
+};
+
+const char* rmn_last_error(void);
+const char* rmn_version(void);
+
+/* Scene construction: replaces Model::Model's geometry/BVH/light/sky steps
+ * (src/model.cpp:172-215). */
+rmn_status rmn_scene_create(const rmn_scene_desc* desc, rmn_scene** out);
+rmn_status rmn_scene_destroy(rmn_scene* scene);
+rmn_status rmn_scene_info_get(const rmn_scene* scene, rmn_scene_info* info);
+
+/* Replaces Model::rayHit (src/model.cpp:332-341): closest hit per ray. */
+rmn_status rmn_trace_closest(rmn_scene* scene, const rmn_ray* rays, int64_t n, rmn_hit* hits, void* stream);
+
+/* Replaces Model::rayHit_test (src/model.cpp:343-354): occluded[i] = 1 iff a
+ * triangle is hit at t in (1e-4, t_max) where t_max is the aim depth. */
+rmn_status rmn_trace_shadow(rmn_scene* scene, const rmn_ray* rays, int64_t n, uint8_t* occluded, void* stream);
+
+/* Replaces the per-pixel work of render_multiThread (src/render.cpp:593-631:
+ * renderPixel for every pixel); the export/post steps are rmn_compose and
+ * rmn_fxaa. */
+rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, const rmn_image* image, void* stream);
+
+/* Photo::shade(options) [+ gammaCorrection] [+ FXAA] (src/image.cpp:215-246,
+ * 454-479) over rmn_render's buffers -> rgb (3 floats per pixel). */
+rmn_status rmn_compose(const rmn_image* image, int32_t width, int32_t height, float exposure, int32_t options,
+                       float* rgb, void* stream);
+
+/* Photo::FXAA (src/image.cpp:363-452) on an rgb image (3 floats per pixel). */
+rmn_status rmn_fxaa(const float* rgb_in, float* rgb_out, int32_t width, int32_t height, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RMN_H */

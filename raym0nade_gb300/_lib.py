@@ -1,0 +1,84 @@
+"""ctypes binding of librmn.so (include/rmn.h).
+
+The library is built in-tree by raym0nade_gb300/build.py. Loading fails loudly
+when it is missing: there is no CPU fallback anywhere in the package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+
+class Material(C.Structure):
+    _fields_ = [("base_color", C.c_float * 3), ("has_base", C.c_float), ("emission", C.c_float * 3),
+                ("has_emission", C.c_float), ("roughness", C.c_float), ("metallic", C.c_float),
+                ("has_specular", C.c_float), ("opacity", C.c_float), ("ior", C.c_float),
+                ("transmitting_color", C.c_float * 3)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("num_vertices", C.c_int32), ("positions", C.c_void_p), ("normals", C.c_void_p),
+                ("uvs", C.c_void_p), ("num_triangles", C.c_int32), ("indices", C.c_void_p),
+                ("num_meshes", C.c_int32), ("mesh_first", C.c_void_p), ("mesh_material", C.c_void_p),
+                ("num_materials", C.c_int32), ("materials", C.c_void_p), ("env_width", C.c_int32),
+                ("env_height", C.c_int32), ("env_rgb", C.c_void_p)]
+
+
+class SceneInfo(C.Structure):
+    _fields_ = [("num_triangles", C.c_int32), ("num_inner_nodes", C.c_int32), ("bvh_depth", C.c_int32),
+                ("heap_slots", C.c_int32), ("num_lights", C.c_int32), ("num_materials", C.c_int32),
+                ("device_bytes", C.c_int64)]
+
+
+class RenderArgs(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("direction", C.c_float * 3), ("up", C.c_float * 3),
+                ("right", C.c_float * 3), ("accuracy", C.c_float), ("focus", C.c_float), ("CoC", C.c_float),
+                ("exposure", C.c_float), ("P_Direct", C.c_float), ("width", C.c_int32), ("height", C.c_int32),
+                ("spp", C.c_int32), ("threads", C.c_int32), ("max_depth", C.c_int32), ("seed", C.c_uint64),
+                ("lanes_per_pixel", C.c_int32), ("reserved", C.c_int32 * 3)]
+
+
+class Image(C.Structure):
+    _fields_ = [("radiance_Dd", C.c_void_p), ("radiance_Ds", C.c_void_p), ("radiance_Id", C.c_void_p),
+                ("radiance_Is", C.c_void_p), ("gbuffer", C.c_void_p)]
+
+
+# name -> (restype, argtypes); every declaration of include/rmn.h.
+SIGNATURES = {
+    "rmn_last_error": (C.c_char_p, []),
+    "rmn_version": (C.c_char_p, []),
+    "rmn_scene_create": (C.c_int, [C.POINTER(SceneDesc), C.POINTER(C.c_void_p)]),
+    "rmn_scene_destroy": (C.c_int, [C.c_void_p]),
+    "rmn_scene_info_get": (C.c_int, [C.c_void_p, C.POINTER(SceneInfo)]),
+    "rmn_trace_closest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "rmn_trace_shadow": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
+    "rmn_render": (C.c_int, [C.c_void_p, C.POINTER(RenderArgs), C.POINTER(Image), C.c_void_p]),
+    "rmn_compose": (C.c_int, [C.POINTER(Image), C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p,
+                              C.c_void_p]),
+    "rmn_fxaa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+}
+
+_lib = None
+
+
+def load(build_if_missing: bool = False) -> C.CDLL:
+    """Load librmn.so; raise if it is not built (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise ImportError(f"{LIB_PATH} is not built; run `python -c 'import __graft_entry__ as g; g.build()'` "
+                              "or `python raym0nade_gb300/build.py`")
+        _build.build()
+    lib = C.CDLL(LIB_PATH)
+    for name, (res, args) in SIGNATURES.items():
+        f = getattr(lib, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = lib
+    return lib

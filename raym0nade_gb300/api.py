@@ -1,0 +1,285 @@
+"""Host-side mirror of the reference's render interface over the C ABI.
+
+The reference exposes ``Model`` (include/model.h:25-43, with the ray queries
+``rayHit`` / ``rayHit_test``), ``RenderArgs`` (include/render.h:8-15),
+``render_multiThread(Model&, const RenderArgs&)`` (include/render.h:43) and
+``Photo`` (include/image.h:15-67, with ``shade``, ``gammaCorrection``,
+``FXAA``, ``postProcessing``, ``save``). This module keeps those names and
+argument meanings; every call goes through librmn.so (include/rmn.h).
+
+Arrays may be numpy (host) or torch CUDA tensors (device-resident, used in
+place). Errors raise ``RmnError`` carrying the library's status and message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib
+from . import scenes as _scenes
+
+try:  # torch is plumbing for device memory and streams; optional for host-only use
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+STATUS = {0: "RMN_OK", 1: "RMN_ERR_INVALID_ARGUMENT", 2: "RMN_ERR_CUDA", 3: "RMN_ERR_OUT_OF_MEMORY",
+          4: "RMN_ERR_UNSUPPORTED", 5: "RMN_ERR_DEVICE_LIMIT", 6: "RMN_ERR_INTERNAL"}
+
+# Photo::ShadeOption (include/image.h:17-34) + the ABI's gamma bit.
+BaseColor, Emission, DirectLight, IndirectLight, Diffuse, Specular = 1, 2, 4, 8, 16, 32
+shapeNormal, surfaceNormal, DoBloom, DoFXAA, DoDepthFieldBlur = 64, 128, 256, 512, 1024
+Full = 63
+Direct_Diffuse, Direct_Specular = DirectLight | Diffuse, DirectLight | Specular
+Indirect_Diffuse, Indirect_Specular = IndirectLight | Diffuse, IndirectLight | Specular
+GAMMA = 4096
+GBUFFER_FLOATS = 20
+
+
+class RmnError(RuntimeError):
+    def __init__(self, status: int, where: str):
+        msg = _lib.load().rmn_last_error().decode(errors="replace")
+        super().__init__(f"{where}: {STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _check(status: int, where: str) -> None:
+    if status != 0:
+        raise RmnError(status, where)
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if torch is not None and isinstance(a, torch.Tensor):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def _stream(stream):
+    if stream is None:
+        return None
+    if torch is not None and isinstance(stream, torch.cuda.Stream):
+        return stream.cuda_stream
+    return int(stream)
+
+
+class Model:
+    """A scene resident in HBM; what the reference's Model holds after
+    Model::Model (faces, materials, light objects, sky map, BVH)."""
+
+    def __init__(self, scene: "_scenes.Scene"):
+        lib = _lib.load()
+        scene.check()
+        self._keep = [np.ascontiguousarray(x) for x in (scene.positions, scene.normals, scene.uvs, scene.indices,
+                                                        scene.mesh_first, scene.mesh_material, scene.materials)]
+        env = None if scene.env is None else np.ascontiguousarray(scene.env, np.float32)
+        self._keep.append(env)
+        p, n, u, i, mf, mm, mat = self._keep[:7]
+        d = _lib.SceneDesc(p.shape[0], _ptr(p), _ptr(n), _ptr(u), i.shape[0], _ptr(i), mm.shape[0], _ptr(mf),
+                           _ptr(mm), mat.shape[0], _ptr(mat), 0 if env is None else env.shape[1],
+                           0 if env is None else env.shape[0], _ptr(env))
+        h = C.c_void_p()
+        _check(lib.rmn_scene_create(C.byref(d), C.byref(h)), "rmn_scene_create")
+        self._h = h
+        self.name = scene.name
+        self.num_triangles = int(i.shape[0])
+        self._keep = None  # the library copied everything it needs
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().rmn_scene_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def info(self) -> dict:
+        s = _lib.SceneInfo()
+        _check(_lib.load().rmn_scene_info_get(self._h, C.byref(s)), "rmn_scene_info_get")
+        return {k: getattr(s, k) for k, _ in s._fields_}
+
+    def rayHit(self, rays, hits=None, stream=None):
+        """Model::rayHit over a batch. rays: (n, 8) float32 (origin, t_min,
+        dir, t_max). Returns hits (n, 4): face id (int32 bits), t, alpha, beta."""
+        n = int(rays.shape[0])
+        if hits is None:
+            hits = _empty_like_device(rays, (n, 4), np.float32)
+        _check(_lib.load().rmn_trace_closest(self._h, _ptr(rays), n, _ptr(hits), _stream(stream)),
+               "rmn_trace_closest")
+        return hits
+
+    def rayHit_test(self, rays, occluded=None, stream=None):
+        """Model::rayHit_test over a batch; t_max of each ray is its aim depth."""
+        n = int(rays.shape[0])
+        if occluded is None:
+            occluded = _empty_like_device(rays, (n,), np.uint8)
+        _check(_lib.load().rmn_trace_shadow(self._h, _ptr(rays), n, _ptr(occluded), _stream(stream)),
+               "rmn_trace_shadow")
+        return occluded
+
+
+def _empty_like_device(ref, shape, dtype):
+    if torch is not None and isinstance(ref, torch.Tensor) and ref.is_cuda:
+        tdt = {np.float32: torch.float32, np.uint8: torch.uint8}[dtype]
+        return torch.empty(shape, dtype=tdt, device=ref.device)
+    return np.empty(shape, dtype)
+
+
+def split_hits(hits):
+    """(face, t, bary(gamma, alpha, beta)) from rmn_hit records."""
+    h = hits.cpu().numpy() if (torch is not None and isinstance(hits, torch.Tensor)) else np.asarray(hits)
+    face = h[:, 0].copy().view(np.int32)
+    al, be = h[:, 2], h[:, 3]
+    ga = (np.float32(1.0) - al - be).astype(np.float32)
+    return face, h[:, 1].copy(), np.stack([ga, al, be], 1)
+
+
+@dataclass
+class RenderArgs:
+    """RenderArgs, include/render.h:8-15 (+ max_depth, seed, lanes_per_pixel)."""
+    position: tuple
+    direction: tuple
+    up: tuple
+    right: tuple
+    accuracy: float
+    focus: float = 1.0
+    CoC: float = 0.0
+    exposure: float = 1.0
+    P_Direct: float = 0.7
+    width: int = 256
+    height: int = 256
+    spp: int = 64
+    threads: int = 1
+    savePath: str = ""
+    max_depth: int = 16
+    seed: int = 1
+    lanes_per_pixel: int = 0
+
+    @staticmethod
+    def from_camera(cam: "_scenes.Camera", seed: int = 1, savePath: str = "", lanes_per_pixel: int = 0):
+        return RenderArgs(cam.position, cam.direction, cam.up, cam.right, cam.accuracy, cam.focus, cam.coc,
+                          cam.exposure, cam.p_direct, cam.width, cam.height, cam.spp, 1, savePath, cam.max_depth,
+                          seed, lanes_per_pixel)
+
+    def c(self) -> "_lib.RenderArgs":
+        a = _lib.RenderArgs()
+        for k in ("position", "direction", "up", "right"):
+            getattr(a, k)[:] = [float(x) for x in getattr(self, k)]
+        a.accuracy, a.focus, a.CoC, a.exposure, a.P_Direct = (float(self.accuracy), float(self.focus),
+                                                               float(self.CoC), float(self.exposure),
+                                                               float(self.P_Direct))
+        a.width, a.height, a.spp, a.threads = int(self.width), int(self.height), int(self.spp), int(self.threads)
+        a.max_depth, a.seed, a.lanes_per_pixel = int(self.max_depth), int(self.seed), int(self.lanes_per_pixel)
+        return a
+
+
+def parse_render_args(text: str) -> RenderArgs:
+    """A `create args` block of docs/renderArguments.txt, as
+    MyConsole::createRenderArgs reads it (src/myconsole.cpp:27-67): direction,
+    right, up, position as (D, R, U) in that basis, accuracy focus CoC
+    exposure, width height, spp threads P_Direct, savePath."""
+    tok = text.split()
+    f = [float(x) for x in tok[:16]]
+    direction, right, up = np.array(f[0:3]), np.array(f[3:6]), np.array(f[6:9])
+    D, R, U = f[9:12]
+    position = D * direction + R * right + U * up
+    width, height = int(tok[16]), int(tok[17])
+    spp, threads, p_direct = int(tok[18]), int(tok[19]), float(tok[20])
+    save = tok[21] if len(tok) > 21 else ""
+    return RenderArgs(tuple(position.astype(np.float32)), tuple(direction), tuple(up), tuple(right), f[12], f[13],
+                      f[14], f[15], p_direct, width, height, spp, threads, save)
+
+
+class Photo:
+    """Render outputs (Photo, include/image.h:15-67): four RadianceData
+    buffers (rgb + Var per pixel) and a G-buffer, on the device when torch
+    CUDA is available (else host numpy)."""
+
+    def __init__(self, width: int, height: int, exposure: float = 1.0, device=True):
+        self.width, self.height, self.exposure = width, height, exposure
+        n = width * height
+        if device and torch is not None and torch.cuda.is_available():
+            mk = lambda k: torch.zeros((n, k), dtype=torch.float32, device="cuda")
+        else:
+            mk = lambda k: np.zeros((n, k), np.float32)
+        self.radiance_Dd, self.radiance_Ds, self.radiance_Id, self.radiance_Is = mk(4), mk(4), mk(4), mk(4)
+        self.Gbuffer = mk(GBUFFER_FLOATS)
+
+    def c_image(self) -> "_lib.Image":
+        return _lib.Image(_ptr(self.radiance_Dd), _ptr(self.radiance_Ds), _ptr(self.radiance_Id),
+                          _ptr(self.radiance_Is), _ptr(self.Gbuffer))
+
+    def shade(self, options: int = Full, out=None, stream=None):
+        """Photo::shade(options) [+ gammaCorrection with GAMMA] [+ FXAA with DoFXAA]."""
+        if out is None:
+            out = _empty_like_device(self.Gbuffer, (self.height, self.width, 3), np.float32)
+        img = self.c_image()
+        _check(_lib.load().rmn_compose(C.byref(img), self.width, self.height, float(self.exposure), int(options),
+                                       _ptr(out), _stream(stream)), "rmn_compose")
+        return out
+
+    def postProcessing(self, options: int):
+        """Photo::postProcessing without bloom / depth of field: shade,
+        gammaCorrection, then FXAA if requested (src/image.cpp:470-479)."""
+        if options & (DoBloom | DoDepthFieldBlur):
+            raise RmnError(4, "Photo.postProcessing: bloom and depth of field are not on the GPU path")
+        return self.shade(options | GAMMA)
+
+    @staticmethod
+    def save(rgb, path: str) -> None:
+        """Photo::save as binary PPM: each channel * 255 truncated to a byte
+        (src/image.cpp:588-594); PNG output needs libpng, absent here."""
+        a = rgb.cpu().numpy() if (torch is not None and isinstance(rgb, torch.Tensor)) else np.asarray(rgb)
+        b = np.clip(a * 255.0, 0, 255).astype(np.uint8)
+        with open(path, "wb") as f:
+            f.write(b"P6\n%d %d\n255\n" % (b.shape[1], b.shape[0]))
+            f.write(b.tobytes())
+
+
+def render(model: Model, args: RenderArgs, photo: Photo | None = None, stream=None) -> Photo:
+    """The per-pixel work of render_multiThread (src/render.cpp:593-631)."""
+    if photo is None:
+        photo = Photo(args.width, args.height, args.exposure)
+    a = args.c()
+    img = photo.c_image()
+    _check(_lib.load().rmn_render(model.handle, C.byref(a), C.byref(img), _stream(stream)), "rmn_render")
+    return photo
+
+
+def render_multiThread(model: Model, args: RenderArgs) -> Photo:
+    """render_multiThread (include/render.h:43): render, then export the
+    images the reference exports before its denoiser runs
+    (src/render.cpp:641-653, minus spatialClamp/bloom) to savePath + '(tag).ppm'."""
+    photo = render(model, args)
+    if args.savePath:
+        d = os.path.dirname(args.savePath)
+        if d:
+            os.makedirs(d, exist_ok=True)
+        exports = [("DiffuseColor", BaseColor), ("DiffuseColor_FXAA", BaseColor | DoFXAA),
+                   ("shapeNormal", shapeNormal), ("surfaceNormal", surfaceNormal),
+                   ("Direct_Diffuse", Direct_Diffuse), ("Direct_Specular", Direct_Specular),
+                   ("Indirect_Diffuse", Indirect_Diffuse), ("Indirect_Specular", Indirect_Specular),
+                   ("Raw", Full), ("Raw_FXAA", Full | DoFXAA)]
+        for tag, opt in exports:
+            Photo.save(photo.postProcessing(opt), f"{args.savePath}({tag}).ppm")
+    return photo
+
+
+def FXAA(rgb, out=None, stream=None):
+    """Photo::FXAA on an (h, w, 3) float32 image."""
+    h, w = int(rgb.shape[0]), int(rgb.shape[1])
+    if out is None:
+        out = _empty_like_device(rgb, (h, w, 3), np.float32)
+    _check(_lib.load().rmn_fxaa(_ptr(rgb), _ptr(out), w, h, _stream(stream)), "rmn_fxaa")
+    return out

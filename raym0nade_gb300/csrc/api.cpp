@@ -1,0 +1,307 @@
+// C ABI of librmn (include/rmn.h): argument checks, host/device staging and
+// error reporting around the kernels.
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+#include "rmn_host.h"
+
+namespace rmn {
+namespace {
+thread_local char g_error[512] = "";
+
+// A caller array: device-resident (used in place) or host memory (staged
+// through a device buffer on the call's stream).
+struct Arg {
+  void* dev = nullptr;
+  bool owned = false;
+};
+
+bool is_device_ptr(const void* p) {
+  if (!p) return false;
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+rmn_status stage_in(const void* host_or_dev, size_t bytes, cudaStream_t st, Arg* out) {
+  if (is_device_ptr(host_or_dev)) {
+    out->dev = const_cast<void*>(host_or_dev);
+    return RMN_OK;
+  }
+  cudaError_t e = cudaMallocAsync(&out->dev, bytes ? bytes : 1, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (staging)");
+  out->owned = true;
+  if (bytes) {
+    e = cudaMemcpyAsync(out->dev, host_or_dev, bytes, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (host to device)");
+  }
+  return RMN_OK;
+}
+
+rmn_status stage_out(void* host_or_dev, size_t bytes, cudaStream_t st, Arg* out) {
+  if (is_device_ptr(host_or_dev)) {
+    out->dev = host_or_dev;
+    return RMN_OK;
+  }
+  cudaError_t e = cudaMallocAsync(&out->dev, bytes ? bytes : 1, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (staging)");
+  out->owned = true;
+  return RMN_OK;
+}
+
+rmn_status finish_out(void* host_or_dev, size_t bytes, cudaStream_t st, const Arg& a) {
+  if (!a.owned || !bytes) return RMN_OK;
+  cudaError_t e = cudaMemcpyAsync(host_or_dev, a.dev, bytes, cudaMemcpyDeviceToHost, st);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpyAsync (device to host)");
+  return RMN_OK;
+}
+
+void release(Arg& a, cudaStream_t st) {
+  if (a.owned && a.dev) cudaFreeAsync(a.dev, st);
+  a.dev = nullptr;
+  a.owned = false;
+}
+
+// Device status word of one call.
+struct Status {
+  int* dev = nullptr;
+  rmn_status init(cudaStream_t st) {
+    cudaError_t e = cudaMallocAsync(&dev, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (status)");
+    e = cudaMemsetAsync(dev, 0, sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync (status)");
+    return RMN_OK;
+  }
+  rmn_status check(cudaStream_t st, const char* what) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, dev, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, what);
+    if (h == kDevStackOverflow) return fail(RMN_ERR_DEVICE_LIMIT, "%s: traversal stack bound reached", what);
+    if (h != kDevOk) return fail(RMN_ERR_DEVICE_LIMIT, "%s: device status %d", what, h);
+    return RMN_OK;
+  }
+  void free(cudaStream_t st) {
+    if (dev) cudaFreeAsync(dev, st);
+    dev = nullptr;
+  }
+};
+}  // namespace
+
+rmn_status fail(rmn_status status, const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_error, sizeof g_error, fmt, ap);
+  va_end(ap);
+  return status;
+}
+
+rmn_status cuda_fail(cudaError_t err, const char* what) {
+  rmn_status s = err == cudaErrorMemoryAllocation ? RMN_ERR_OUT_OF_MEMORY : RMN_ERR_CUDA;
+  return fail(s, "%s: %s (%s)", what, cudaGetErrorName(err), cudaGetErrorString(err));
+}
+
+void clear_error() { g_error[0] = 0; }
+
+}  // namespace rmn
+
+using namespace rmn;
+
+extern "C" {
+
+const char* rmn_last_error(void) { return g_error; }
+
+const char* rmn_version(void) { return "raym0nade-gb300 0.1 (sm_103a)"; }
+
+rmn_status rmn_scene_create(const rmn_scene_desc* desc, rmn_scene** out) {
+  clear_error();
+  if (!out) return fail(RMN_ERR_INVALID_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  rmn_scene* s = new (std::nothrow) rmn_scene();
+  if (!s) return fail(RMN_ERR_OUT_OF_MEMORY, "host allocation failed");
+  cudaGetDevice(&s->device);
+  rmn_status st;
+  try {
+    st = build_scene(desc, s);
+  } catch (const std::bad_alloc&) {
+    st = fail(RMN_ERR_OUT_OF_MEMORY, "host allocation failed while building the scene");
+  } catch (...) {
+    st = fail(RMN_ERR_INTERNAL, "unexpected exception while building the scene");
+  }
+  if (st != RMN_OK) {
+    free_scene(s);
+    delete s;
+    return st;
+  }
+  *out = s;
+  return RMN_OK;
+}
+
+rmn_status rmn_scene_destroy(rmn_scene* scene) {
+  clear_error();
+  if (!scene) return RMN_OK;
+  free_scene(scene);
+  delete scene;
+  return RMN_OK;
+}
+
+rmn_status rmn_scene_info_get(const rmn_scene* scene, rmn_scene_info* info) {
+  clear_error();
+  if (!scene || !info) return fail(RMN_ERR_INVALID_ARGUMENT, "scene or info is NULL");
+  *info = scene->info;
+  return RMN_OK;
+}
+
+static rmn_status trace_common(rmn_scene* scene, const rmn_ray* rays, int64_t n, void* out, size_t out_bytes,
+                               bool shadow, void* stream) {
+  clear_error();
+  if (!scene || (n > 0 && (!rays || !out))) return fail(RMN_ERR_INVALID_ARGUMENT, "NULL scene, rays or output");
+  if (n < 0) return fail(RMN_ERR_INVALID_ARGUMENT, "negative ray count");
+  if (n == 0) return RMN_OK;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  Arg in, o;
+  Status status;
+  rmn_status r = stage_in(rays, (size_t)n * sizeof(rmn_ray), st, &in);
+  if (r == RMN_OK) r = stage_out(out, out_bytes, st, &o);
+  if (r == RMN_OK) r = status.init(st);
+  if (r == RMN_OK) {
+    cudaError_t e = shadow ? launch_trace_shadow(scene->dev, static_cast<const rmn_ray*>(in.dev), n,
+                                                 static_cast<uint8_t*>(o.dev), status.dev, st)
+                           : launch_trace_closest(scene->dev, static_cast<const rmn_ray*>(in.dev), n,
+                                                  static_cast<rmn_hit*>(o.dev), status.dev, st);
+    if (e != cudaSuccess) r = cuda_fail(e, shadow ? "trace_shadow launch" : "trace_closest launch");
+  }
+  if (r == RMN_OK) r = finish_out(out, out_bytes, st, o);
+  rmn_status r2 = status.dev ? status.check(st, shadow ? "rmn_trace_shadow" : "rmn_trace_closest") : RMN_OK;
+  release(in, st);
+  release(o, st);
+  status.free(st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (r == RMN_OK) r = r2;
+  if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
+  return r;
+}
+
+rmn_status rmn_trace_closest(rmn_scene* scene, const rmn_ray* rays, int64_t n, rmn_hit* hits, void* stream) {
+  return trace_common(scene, rays, n, hits, (size_t)n * sizeof(rmn_hit), false, stream);
+}
+
+rmn_status rmn_trace_shadow(rmn_scene* scene, const rmn_ray* rays, int64_t n, uint8_t* occluded, void* stream) {
+  return trace_common(scene, rays, n, occluded, (size_t)n, true, stream);
+}
+
+rmn_status rmn_fxaa(const float* rgb_in, float* rgb_out, int32_t width, int32_t height, void* stream) {
+  clear_error();
+  if (!rgb_in || !rgb_out || width <= 0 || height <= 0) return fail(RMN_ERR_INVALID_ARGUMENT, "bad FXAA arguments");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  size_t bytes = (size_t)width * height * 3 * sizeof(float);
+  Arg in, o;
+  rmn_status r = stage_in(rgb_in, bytes, st, &in);
+  if (r == RMN_OK) r = stage_out(rgb_out, bytes, st, &o);
+  if (r == RMN_OK) {
+    cudaError_t e = launch_fxaa(static_cast<const float*>(in.dev), static_cast<float*>(o.dev), width, height, st);
+    if (e != cudaSuccess) r = cuda_fail(e, "fxaa launch");
+  }
+  if (r == RMN_OK) r = finish_out(rgb_out, bytes, st, o);
+  release(in, st);
+  release(o, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
+  return r;
+}
+
+rmn_status rmn_compose(const rmn_image* image, int32_t width, int32_t height, float exposure, int32_t options,
+                       float* rgb, void* stream) {
+  clear_error();
+  if (!image || !rgb || width <= 0 || height <= 0 || !image->gbuffer || !image->radiance_Dd || !image->radiance_Ds ||
+      !image->radiance_Id || !image->radiance_Is)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_compose needs all four radiance buffers and the G-buffer");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  size_t npx = (size_t)width * height;
+  Arg dd, ds, id, is, gb, o, tmp;
+  rmn_status r = stage_in(image->radiance_Dd, npx * 16, st, &dd);
+  if (r == RMN_OK) r = stage_in(image->radiance_Ds, npx * 16, st, &ds);
+  if (r == RMN_OK) r = stage_in(image->radiance_Id, npx * 16, st, &id);
+  if (r == RMN_OK) r = stage_in(image->radiance_Is, npx * 16, st, &is);
+  if (r == RMN_OK) r = stage_in(image->gbuffer, npx * RMN_GBUFFER_FLOATS * 4, st, &gb);
+  if (r == RMN_OK) r = stage_out(rgb, npx * 12, st, &o);
+  bool fx = (options & RMN_SHADE_FXAA) != 0;
+  if (r == RMN_OK && fx) {
+    cudaError_t e = cudaMallocAsync(&tmp.dev, npx * 12, st);
+    if (e != cudaSuccess) r = cuda_fail(e, "cudaMallocAsync (compose)");
+    tmp.owned = true;
+  }
+  if (r == RMN_OK) {
+    float* target = fx ? static_cast<float*>(tmp.dev) : static_cast<float*>(o.dev);
+    cudaError_t e = launch_compose(static_cast<const float*>(dd.dev), static_cast<const float*>(ds.dev),
+                                   static_cast<const float*>(id.dev), static_cast<const float*>(is.dev),
+                                   static_cast<const float*>(gb.dev), width, height, exposure, options, target, st);
+    if (e == cudaSuccess && fx) e = launch_fxaa(target, static_cast<float*>(o.dev), width, height, st);
+    if (e != cudaSuccess) r = cuda_fail(e, "compose launch");
+  }
+  if (r == RMN_OK) r = finish_out(rgb, npx * 12, st, o);
+  for (Arg* a : {&dd, &ds, &id, &is, &gb, &o, &tmp}) release(*a, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
+  return r;
+}
+
+}  // extern "C"
+
+extern "C" rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, const rmn_image* image, void* stream) {
+  clear_error();
+  if (!scene || !args || !image) return fail(RMN_ERR_INVALID_ARGUMENT, "NULL scene, args or image");
+  if (!image->radiance_Dd || !image->radiance_Ds || !image->radiance_Id || !image->radiance_Is)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_render needs the four radiance buffers");
+  const rmn_render_args& a = *args;
+  if (a.width <= 0 || a.height <= 0 || (int64_t)a.width * a.height > (1LL << 30))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "image size %d x %d out of range", a.width, a.height);
+  if (a.spp < 0 || a.spp > (1 << 20)) return fail(RMN_ERR_INVALID_ARGUMENT, "spp %d out of range", a.spp);
+  if (!(a.P_Direct >= 0.0f && a.P_Direct <= 1.0f)) return fail(RMN_ERR_INVALID_ARGUMENT, "P_Direct must lie in [0, 1]");
+  if (a.max_depth < 1 || a.max_depth > 16) return fail(RMN_ERR_INVALID_ARGUMENT, "max_depth must lie in [1, 16]");
+  int k = a.lanes_per_pixel;
+  if (k != 0 && (k < 1 || k > 32 || (k & (k - 1))))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "lanes_per_pixel must be 0 or a power of two up to 32");
+  if (scene->dev.num_lights > 8) return fail(RMN_ERR_UNSUPPORTED, "more than 8 light objects");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t npx = (size_t)a.width * a.height;
+  Arg dd, ds, id, is, gb;
+  Status status;
+  rmn_status r = stage_out(image->radiance_Dd, npx * 16, st, &dd);
+  if (r == RMN_OK) r = stage_out(image->radiance_Ds, npx * 16, st, &ds);
+  if (r == RMN_OK) r = stage_out(image->radiance_Id, npx * 16, st, &id);
+  if (r == RMN_OK) r = stage_out(image->radiance_Is, npx * 16, st, &is);
+  if (r == RMN_OK) {
+    if (image->gbuffer) {
+      r = stage_out(image->gbuffer, npx * RMN_GBUFFER_FLOATS * 4, st, &gb);
+    } else {
+      cudaError_t e = cudaMallocAsync(&gb.dev, npx * RMN_GBUFFER_FLOATS * 4, st);
+      if (e != cudaSuccess) r = cuda_fail(e, "cudaMallocAsync (G-buffer)");
+      gb.owned = true;
+    }
+  }
+  if (r == RMN_OK) r = status.init(st);
+  if (r == RMN_OK) {
+    cudaError_t e = launch_render(scene->dev, a, static_cast<float*>(gb.dev), static_cast<float*>(dd.dev),
+                                  static_cast<float*>(ds.dev), static_cast<float*>(id.dev),
+                                  static_cast<float*>(is.dev), status.dev, st);
+    if (e != cudaSuccess) r = cuda_fail(e, "render launch");
+  }
+  if (r == RMN_OK) r = finish_out(image->radiance_Dd, npx * 16, st, dd);
+  if (r == RMN_OK) r = finish_out(image->radiance_Ds, npx * 16, st, ds);
+  if (r == RMN_OK) r = finish_out(image->radiance_Id, npx * 16, st, id);
+  if (r == RMN_OK) r = finish_out(image->radiance_Is, npx * 16, st, is);
+  if (r == RMN_OK && image->gbuffer) r = finish_out(image->gbuffer, npx * RMN_GBUFFER_FLOATS * 4, st, gb);
+  rmn_status r2 = status.dev ? status.check(st, "rmn_render") : RMN_OK;
+  for (Arg* x : {&dd, &ds, &id, &is, &gb}) release(*x, st);
+  status.free(st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (r == RMN_OK) r = r2;
+  if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
+  return r;
+}

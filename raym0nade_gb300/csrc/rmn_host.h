@@ -1,0 +1,47 @@
+// Host-side internals of librmn: scene object, error reporting and the
+// kernel launchers implemented in the .cu files.
+#pragma once
+#include <string>
+#include <vector>
+
+#include "../../include/rmn.h"
+#include "rmn_internal.h"
+
+struct rmn_scene {
+  DevScene dev{};
+  std::vector<void*> device_allocations;
+  rmn_scene_info info{};
+  int device = 0;
+};
+
+namespace rmn {
+
+rmn_status fail(rmn_status status, const char* fmt, ...);
+rmn_status cuda_fail(cudaError_t err, const char* what);
+void clear_error();
+
+#define RMN_CHECK_CUDA(call)                                  \
+  do {                                                        \
+    cudaError_t e_ = (call);                                  \
+    if (e_ != cudaSuccess) return ::rmn::cuda_fail(e_, #call); \
+  } while (0)
+
+rmn_status build_scene(const rmn_scene_desc* desc, rmn_scene* scene);
+void free_scene(rmn_scene* scene);
+
+// Device-side status word written by kernels that hit one of their bounds.
+enum DeviceStatus { kDevOk = 0, kDevStackOverflow = 1, kDevBadIndex = 2 };
+
+// Kernel launchers (trace.cu, render.cu, post.cu). All take device pointers.
+cudaError_t launch_trace_closest(const DevScene& s, const rmn_ray* rays, int64_t n, rmn_hit* hits, int* status,
+                                 cudaStream_t stream);
+cudaError_t launch_trace_shadow(const DevScene& s, const rmn_ray* rays, int64_t n, uint8_t* occluded, int* status,
+                                cudaStream_t stream);
+int default_lanes_per_pixel(int spp);
+cudaError_t launch_render(const DevScene& s, const rmn_render_args& a, float* gbuf, float* dd, float* ds, float* id,
+                          float* is, int* status, cudaStream_t stream);
+cudaError_t launch_fxaa(const float* in, float* out, int w, int h, cudaStream_t stream);
+cudaError_t launch_compose(const float* dd, const float* ds, const float* id, const float* is, const float* gbuf,
+                           int w, int h, float exposure, int options, float* rgb, cudaStream_t stream);
+
+}  // namespace rmn

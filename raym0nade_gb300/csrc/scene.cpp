@@ -1,0 +1,362 @@
+// Scene construction on the host and upload to HBM (rmn_scene_create).
+//
+// The BVH is the reference's own tree: BVH::dfs_build (src/bvh.cpp:18-42)
+// splits at the median of the centroid coordinate of largest variance with
+// std::nth_element and stops at <= 10 triangles. Running the same comparator
+// through std::nth_element on an array of (centroid, index) items performs
+// the same comparisons and swaps as the reference does on its Face array,
+// so the tree, the leaf order and therefore every closest-hit id are the
+// reference's. Disjoint subtrees are built on separate threads, which changes
+// nothing in the result.
+//
+// The heap-indexed tree is then flattened depth-first into 64-byte two-child
+// nodes (DevNode), and triangles are stored in leaf order with their edges
+// precomputed (e1 = v1 - v0, e2 = v2 - v0 are exactly the differences that
+// RayTriangleIntersection forms, src/geometry.cpp:65-66).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <future>
+#include <thread>
+
+#include "rmn_host.h"
+
+namespace rmn {
+namespace {
+
+struct Item {
+  float c[3];
+  int32_t id;
+};
+
+struct HeapNode {
+  float3 lo, hi;
+  int32_t faceL = 0, faceR = 0;
+};
+
+struct Builder {
+  const float3* pos;
+  const int32_t* idx;
+  std::vector<Item> items;
+  std::vector<HeapNode> heap;
+
+  float3 vtx(int tri, int k) const { return pos[idx[3 * tri + k]]; }
+
+  void leaf(int u, int l, int r) {
+    HeapNode& n = heap[u];
+    n.faceL = l;
+    n.faceR = r;
+    n.lo = f3(INFINITY);
+    n.hi = f3(-INFINITY);
+    for (int i = l; i < r; ++i) {
+      int t = items[i].id;
+      float3 a = vtx(t, 0), b = vtx(t, 1), c = vtx(t, 2);
+      float3 lo = min3(a, min3(b, c)), hi = max3(a, max3(b, c));
+      n.lo = f3(std::fmin(n.lo.x, lo.x), std::fmin(n.lo.y, lo.y), std::fmin(n.lo.z, lo.z));
+      n.hi = f3(std::fmax(n.hi.x, hi.x), std::fmax(n.hi.y, hi.y), std::fmax(n.hi.z, hi.z));
+    }
+  }
+
+  void build(int u, int l, int r, int par_depth) {
+    if ((unsigned)(r - l) <= (unsigned)RMN_LEAF_MAX) {
+      leaf(u, l, r);
+      return;
+    }
+    float3 s = f3(0.0f), s2 = f3(0.0f);
+    for (int i = l; i < r; ++i) {
+      float3 c = f3(items[i].c[0], items[i].c[1], items[i].c[2]);
+      s += c;
+      s2 += c * c;
+    }
+    float3 var = s2 - s * s / (float)(r - l);
+    int axis = 0;
+    if (var.y > var.x) axis = 1;
+    if (var.z > var.x && var.z > var.y) axis = 2;
+    int m = (r + l) / 2;
+    std::nth_element(items.begin() + l, items.begin() + m, items.begin() + r,
+                     [axis](const Item& a, const Item& b) { return a.c[axis] < b.c[axis]; });
+    if (par_depth > 0 && r - l > 65536) {
+      auto left = std::async(std::launch::async, [&] { build(u << 1, l, m, par_depth - 1); });
+      build(u << 1 | 1, m, r, par_depth - 1);
+      left.get();
+    } else {
+      build(u << 1, l, m, 0);
+      build(u << 1 | 1, m, r, 0);
+    }
+    const HeapNode &a = heap[u << 1], &b = heap[u << 1 | 1];
+    heap[u].lo = f3(std::fmin(a.lo.x, b.lo.x), std::fmin(a.lo.y, b.lo.y), std::fmin(a.lo.z, b.lo.z));
+    heap[u].hi = f3(std::fmax(a.hi.x, b.hi.x), std::fmax(a.hi.y, b.hi.y), std::fmax(a.hi.z, b.hi.z));
+  }
+};
+
+int heap_slots(int u, int n) { return ((unsigned)n <= (unsigned)RMN_LEAF_MAX) ? u : heap_slots(u << 1 | 1, (n + 1) >> 1); }
+
+struct Flattener {
+  const std::vector<HeapNode>& heap;
+  std::vector<DevNode> out;
+  int max_depth = 0;
+
+  int ref_of(int u, int depth) {
+    const HeapNode& n = heap[u];
+    if (n.faceR) {
+      max_depth = std::max(max_depth, depth);
+      return leaf_ref(n.faceL, n.faceR - n.faceL);
+    }
+    int me = (int)out.size();
+    out.emplace_back();
+    int l = ref_of(u << 1, depth + 1);
+    int r = ref_of(u << 1 | 1, depth + 1);
+    const HeapNode &L = heap[u << 1], &R = heap[u << 1 | 1];
+    DevNode& d = out[me];
+    d.a = make_float4(L.lo.x, L.lo.y, L.lo.z, L.hi.x);
+    d.b = make_float4(L.hi.y, L.hi.z, R.lo.x, R.lo.y);
+    d.c = make_float4(R.lo.z, R.hi.x, R.hi.y, R.hi.z);
+    d.d = make_int4(l, r, 0, 0);
+    return me;
+  }
+};
+
+float bits_float(int32_t i) {
+  float f;
+  std::memcpy(&f, &i, 4);
+  return f;
+}
+
+// The tangent frame of calcSurfaceNormal (src/model.cpp:279-298). With the
+// zero normal-map texel of an untextured material its only effect is to
+// renormalise the surface normal, and only when this frame is finite; the
+// frame does not depend on which side the shape normal was flipped to.
+bool tangent_frame_finite(float3 e1, float3 e2, const float* uv0, const float* uv1, const float* uv2) {
+  float d1x = uv1[0] - uv0[0], d1y = uv1[1] - uv0[1];
+  float d2x = uv2[0] - uv0[0], d2y = uv2[1] - uv0[1];
+  float k = 1.0f / (d1x * d2y - d2x * d1y);
+  float3 tu = k * (d2y * e1 - d1y * e2), tv = k * (-d2x * e1 + d1x * e2);
+  float3 sn = norm3(cross3(e1, e2));
+  float3 t = norm3(tu - sn * dot3(sn, tu));
+  float3 b = norm3(tv - sn * dot3(sn, tv) - t * dot3(t, tv));
+  return all_finite3(t) && all_finite3(b);
+}
+
+template <class T>
+rmn_status upload(rmn_scene* s, const std::vector<T>& v, const T** out) {
+  *out = nullptr;
+  if (v.empty()) return RMN_OK;
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, v.size() * sizeof(T));
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (scene)");
+  s->device_allocations.push_back(p);
+  e = cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy (scene)");
+  s->info.device_bytes += (int64_t)(v.size() * sizeof(T));
+  *out = static_cast<const T*>(p);
+  return RMN_OK;
+}
+
+}  // namespace
+
+rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
+  if (!d || !d->positions || !d->indices || !d->mesh_first || !d->mesh_material || !d->materials)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "scene description has a NULL array");
+  if (d->num_vertices <= 0 || d->num_triangles <= 0 || d->num_meshes <= 0 || d->num_materials <= 0)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "scene needs at least one vertex, triangle, mesh and material");
+  if (d->num_triangles >= (1 << 27))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "at most 2^27 - 1 triangles per scene");
+  if (d->mesh_first[0] != 0 || d->mesh_first[d->num_meshes] != d->num_triangles)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "mesh_first must start at 0 and end at num_triangles");
+  for (int m = 0; m < d->num_meshes; ++m) {
+    if (d->mesh_first[m + 1] < d->mesh_first[m]) return fail(RMN_ERR_INVALID_ARGUMENT, "mesh_first must not decrease");
+    if (d->mesh_material[m] < 0 || d->mesh_material[m] >= d->num_materials)
+      return fail(RMN_ERR_INVALID_ARGUMENT, "mesh %d has material %d out of range", m, d->mesh_material[m]);
+  }
+  for (int64_t i = 0; i < 3LL * d->num_triangles; ++i)
+    if (d->indices[i] < 0 || d->indices[i] >= d->num_vertices)
+      return fail(RMN_ERR_INVALID_ARGUMENT, "vertex index %d of triangle %lld out of range", d->indices[i],
+                  (long long)(i / 3));
+  for (int m = 0; m < d->num_materials; ++m) {
+    const rmn_material& q = d->materials[m];
+    if (!(q.opacity > 1.0f - RMN_EPS))
+      return fail(RMN_ERR_UNSUPPORTED, "material %d is transmissive (opacity %g): glass and media are not on the GPU path",
+                  m, (double)q.opacity);
+  }
+  if (d->env_rgb && (d->env_width <= 0 || d->env_height <= 0))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "sky map needs positive width and height");
+
+  const int nt = d->num_triangles;
+  std::vector<float3> pos(d->num_vertices);
+  for (int i = 0; i < d->num_vertices; ++i) pos[i] = f3(d->positions[3 * i], d->positions[3 * i + 1], d->positions[3 * i + 2]);
+
+  // ---- BVH (BVH::build, src/bvh.cpp:48-54) ----
+  Builder b;
+  b.pos = pos.data();
+  b.idx = d->indices;
+  b.items.resize(nt);
+  for (int t = 0; t < nt; ++t) {
+    float3 c = (b.vtx(t, 0) + b.vtx(t, 1) + b.vtx(t, 2)) / 3.0f;  // Face::center, src/component.cpp:37-39
+    b.items[t] = {{c.x, c.y, c.z}, t};
+  }
+  b.heap.assign(heap_slots(1, nt) + 1, HeapNode());
+  int par = std::thread::hardware_concurrency() >= 8 ? 3 : 1;
+  b.build(1, 0, nt, par);
+  Flattener fl{b.heap, {}, 0};
+  int root = fl.ref_of(1, 0);
+  if (fl.max_depth + 1 > RMN_STACK)
+    return fail(RMN_ERR_UNSUPPORTED, "BVH depth %d exceeds the traversal stack", fl.max_depth);
+
+  // ---- triangles in leaf order ----
+  std::vector<int> tri_mesh_mat(nt);
+  for (int m = 0; m < d->num_meshes; ++m)
+    for (int t = d->mesh_first[m]; t < d->mesh_first[m + 1]; ++t) tri_mesh_mat[t] = d->mesh_material[m];
+  static const float zero2[2] = {0.0f, 0.0f};
+  std::vector<float4> tri(3 * (size_t)nt), shade(3 * (size_t)nt);
+  for (int i = 0; i < nt; ++i) {
+    int t = b.items[i].id;
+    int i0 = d->indices[3 * t], i1 = d->indices[3 * t + 1], i2 = d->indices[3 * t + 2];
+    float3 v0 = pos[i0], e1 = pos[i1] - v0, e2 = pos[i2] - v0;
+    int flags = 0;
+    float area = len3(cross3(e1, e2)) / 2.0f;
+    if (!(area > 1e-2f)) flags |= RMN_TRI_SMOOTH;
+    const float* u0 = d->uvs ? d->uvs + 2 * i0 : zero2;
+    const float* u1 = d->uvs ? d->uvs + 2 * i1 : zero2;
+    const float* u2 = d->uvs ? d->uvs + 2 * i2 : zero2;
+    if (tangent_frame_finite(e1, e2, u0, u1, u2)) flags |= RMN_TRI_RENORM;
+    tri[3 * i + 0] = make_float4(v0.x, v0.y, v0.z, bits_float(t));
+    tri[3 * i + 1] = make_float4(e1.x, e1.y, e1.z, len3(e1));
+    tri[3 * i + 2] = make_float4(e2.x, e2.y, e2.z, bits_float(flags));
+    for (int k = 0; k < 3; ++k) {
+      int v = d->indices[3 * t + k];
+      float3 n = d->normals ? f3(d->normals[3 * v], d->normals[3 * v + 1], d->normals[3 * v + 2]) : f3(0.0f);
+      shade[3 * i + k] = make_float4(n.x, n.y, n.z, k == 0 ? bits_float(tri_mesh_mat[t]) : 0.0f);
+    }
+  }
+
+  // ---- materials (Material::get*, src/material.cpp:349-383) ----
+  std::vector<DevMat> mats(d->num_materials);
+  for (int m = 0; m < d->num_materials; ++m) {
+    const rmn_material& q = d->materials[m];
+    float3 base = q.has_base != 0.0f ? f3(q.base_color[0], q.base_color[1], q.base_color[2]) : f3(1.0f);
+    float3 emis = q.has_emission != 0.0f ? f3(q.emission[0], q.emission[1], q.emission[2]) : f3(0.0f);
+    float rough = q.roughness, metal = 0.0f;
+    if (q.has_specular != 0.0f) {
+      metal = std::min(q.metallic, 0.99f);
+      rough = std::max(q.roughness, 1e-3f);
+    }
+    mats[m].base = make_float4(base.x, base.y, base.z, rough);
+    mats[m].emis = make_float4(emis.x, emis.y, emis.z, metal);
+    mats[m].misc = make_float4(q.opacity, q.ior, q.has_emission != 0.0f ? 1.0f : 0.0f, (float)m);
+    mats[m].trans = make_float4(q.transmitting_color[0], q.transmitting_color[1], q.transmitting_color[2], 0.0f);
+  }
+
+  // ---- light objects (Model::checkLightObject, src/model.cpp:44-82) ----
+  // One per mesh with an emissive texel, built before the sky is loaded as
+  // in the reference (so also when a sky map is present, where they stay
+  // unused by light sampling). The average emissive colour of a constant
+  // texel over the reference's 8x8 grid is 64 equal adds divided by 64.
+  std::vector<DevLight> lights;
+  std::vector<float4> lfaces;
+  std::vector<float> lprefix;
+  for (int m = 0; m < d->num_meshes; ++m) {
+    const rmn_material& q = d->materials[d->mesh_material[m]];
+    if (q.has_emission == 0.0f) continue;
+    float3 e = f3(q.emission[0], q.emission[1], q.emission[2]);
+    float3 avg = f3(0.0f);
+    for (int i = 0; i < 64; ++i) avg += e;
+    avg = avg / (float)64;
+    float cl = dot3(avg, f3(0.3f, 0.6f, 0.1f));
+    float3 color = f3(0.0f), center = f3(0.0f);
+    float power = 0.0f;
+    std::vector<float> w;
+    std::vector<int> faces;
+    for (int t = d->mesh_first[m]; t < d->mesh_first[m + 1]; ++t) {
+      float3 v0 = pos[d->indices[3 * t]], v1 = pos[d->indices[3 * t + 1]], v2 = pos[d->indices[3 * t + 2]];
+      float area = len3(cross3(v1 - v0, v2 - v0)) / 2.0f;
+      if (cl < RMN_EPS || area < RMN_EPS) continue;
+      color += avg * area;
+      faces.push_back(t);
+      w.push_back(area * cl);
+    }
+    if (faces.empty()) continue;
+    color = color / dot3(color, f3(0.3f, 0.6f, 0.1f));
+    for (size_t j = 0; j < faces.size(); ++j) {
+      int t = faces[j];
+      float3 v0 = pos[d->indices[3 * t]], v1 = pos[d->indices[3 * t + 1]], v2 = pos[d->indices[3 * t + 2]];
+      power += w[j];
+      center += (v0 + v1 + v2) / 3.0f * w[j];
+    }
+    center /= power;
+    DevLight L{};
+    L.center = make_float4(center.x, center.y, center.z, power);
+    L.color = make_float4(color.x, color.y, color.z, (float)faces.size());
+    L.first_face = (int)(lfaces.size() / RMN_LIGHT_FACE_F4);
+    lights.push_back(L);
+    float acc = 0.0f;
+    for (size_t j = 0; j < faces.size(); ++j) {
+      int t = faces[j];
+      for (int k = 0; k < 3; ++k) {
+        float3 v = pos[d->indices[3 * t + k]];
+        lfaces.push_back(make_float4(v.x, v.y, v.z, 0.0f));
+      }
+      for (int k = 0; k < 3; ++k) {
+        int v = d->indices[3 * t + k];
+        float3 n = d->normals ? f3(d->normals[3 * v], d->normals[3 * v + 1], d->normals[3 * v + 2]) : f3(0.0f);
+        lfaces.push_back(make_float4(n.x, n.y, n.z, 0.0f));
+      }
+      acc = j == 0 ? w[0] : acc + w[j];  // RandomDistribution::Init, src/component.cpp:12-18
+      lprefix.push_back(acc);
+    }
+  }
+
+  // ---- sky (SkyBox::Init, src/component.cpp:54-67) ----
+  std::vector<float4> sky;
+  std::vector<float> sky_prefix;
+  if (d->env_rgb) {
+    const int W = d->env_width, H = d->env_height;
+    sky.resize((size_t)W * H);
+    sky_prefix.resize((size_t)W * H);
+    float acc = 0.0f;
+    for (int v = 0; v < H; ++v)
+      for (int u = 0; u < W; ++u) {
+        size_t i = (size_t)v * W + u;
+        float phi = RMN_PI * (float(v) + 0.5f) / float(H);
+        float area = std::sin(phi) * 2.0f * RMN_PI / float(W * H);
+        float3 c = f3(d->env_rgb[3 * i], d->env_rgb[3 * i + 1], d->env_rgb[3 * i + 2]) * area;
+        sky[i] = make_float4(c.x, c.y, c.z, 0.0f);
+        float l = dot3(c, f3(0.3f, 0.6f, 0.1f));
+        acc = i == 0 ? l : acc + l;
+        sky_prefix[i] = acc;
+      }
+  }
+
+  // ---- upload ----
+  s->info.num_triangles = nt;
+  s->info.num_inner_nodes = (int)fl.out.size();
+  s->info.bvh_depth = fl.max_depth;
+  s->info.heap_slots = (int)b.heap.size();
+  s->info.num_lights = (int)lights.size();
+  s->info.num_materials = d->num_materials;
+  DevScene& g = s->dev;
+  rmn_status st;
+  if ((st = upload(s, fl.out, &g.nodes)) != RMN_OK) return st;
+  if ((st = upload(s, tri, &g.tri)) != RMN_OK) return st;
+  if ((st = upload(s, shade, &g.shade)) != RMN_OK) return st;
+  if ((st = upload(s, mats, &g.mats)) != RMN_OK) return st;
+  if ((st = upload(s, lights, &g.lights)) != RMN_OK) return st;
+  if ((st = upload(s, lfaces, &g.light_faces)) != RMN_OK) return st;
+  if ((st = upload(s, lprefix, &g.light_prefix)) != RMN_OK) return st;
+  if ((st = upload(s, sky, &g.sky)) != RMN_OK) return st;
+  if ((st = upload(s, sky_prefix, &g.sky_prefix)) != RMN_OK) return st;
+  g.root = root;
+  g.num_tris = nt;
+  g.num_mats = d->num_materials;
+  g.num_lights = (int)lights.size();
+  g.sky_w = d->env_rgb ? d->env_width : 0;
+  g.sky_h = d->env_rgb ? d->env_height : 0;
+  g.depth = fl.max_depth;
+  return RMN_OK;
+}
+
+void free_scene(rmn_scene* s) {
+  for (void* p : s->device_allocations) cudaFree(p);
+  s->device_allocations.clear();
+}
+
+}  // namespace rmn

@@ -1,0 +1,369 @@
+// Device-side hit shading, BSDF and light sampling of the integrator.
+// Included by render.cu only. Each function restates the reference routine
+// it cites; expression order follows the reference so that a path run on the
+// same random numbers as the CPU oracle takes the same branches.
+#pragma once
+#include "rmn_internal.h"
+#include "trace.cuh"
+
+#define RMN_LUM f3(0.3f, 0.6f, 0.1f)  // RGB_Weight, include/geometry.h:16
+#define RMN_MAX_TRYS 16                // src/sampling.cpp:201
+
+__constant__ int c_sample_count[17] = {0, 1, 2, 2, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 5, 6};  // src/render.cpp:126
+
+struct Surf {  // HitInfo, include/model.h:12-18 (defaults src/model.cpp:4-7)
+  float3 shapeN, surfN, emis, base, pos;
+  float specular, roughness, metallic, opacity, eta;
+  int id;
+  bool entering;
+};
+
+RMN_D float fmixf(float a, float b, float t) { return a * (1 - t) + b * t; }  // src/sampling.cpp:16-18
+
+RMN_D bool flip_toward(float3& v, float3 dir) {  // reverseFix, src/model.cpp:232-238
+  if (dot3(v, dir) < 0.0f) {
+    v = v * -1.0f;
+    return false;
+  }
+  return true;
+}
+
+// getHitNormals, src/model.cpp:240-270, for a triangle given by v0 + edges
+// and its vertex normals.
+RMN_D void hit_normals(float3 e1, float3 e2, bool smooth, float3 n0, float3 n1, float3 n2, float3 in, float3 b,
+                       float3& shapeN, float3& surfN, bool& entering) {
+  float3 c = cross3(e1, e2);
+  shapeN = norm3(c);
+  entering = flip_toward(shapeN, -in);
+  surfN = shapeN;
+  if (!smooth) return;
+  flip_toward(n0, shapeN);
+  flip_toward(n1, shapeN);
+  flip_toward(n2, shapeN);
+  surfN = norm3(b.x * (dot3(n0, shapeN) > 0.85f ? n0 : shapeN) + b.y * (dot3(n1, shapeN) > 0.85f ? n1 : shapeN) +
+                b.z * (dot3(n2, shapeN) > 0.85f ? n2 : shapeN));
+  if (!any_finite3(surfN)) surfN = shapeN;
+}
+
+// getHitInfo + getHitMaterial + calcSurfaceNormal for a closest hit at
+// leaf-order triangle `i` (src/render.cpp:62-79, src/model.cpp:279-328).
+// h.pos must hold the hit position.
+RMN_D void hit_info(const DevScene& s, int i, float3 rd, Surf& h) {
+  const float4* t = s.tri + 3 * i;
+  float4 A = __ldg(t), B = __ldg(t + 1), C = __ldg(t + 2);
+  int flags = __float_as_int(C.w);
+  float3 v0 = f3(A), e1 = f3(B), e2 = f3(C);
+  float3 b = bary(v0, e1, e2, h.pos);
+  const float4* sh = s.shade + 3 * i;
+  float4 N0 = __ldg(sh);
+  int mat = __float_as_int(N0.w);
+  float3 n0 = f3(N0), n1 = f3(0.0f), n2 = f3(0.0f);
+  bool smooth = (flags & RMN_TRI_SMOOTH) != 0;
+  if (smooth) {
+    n1 = f3(__ldg(sh + 1));
+    n2 = f3(__ldg(sh + 2));
+  }
+  hit_normals(e1, e2, smooth, n0, n1, n2, rd, b, h.shapeN, h.surfN, h.entering);
+  float3 raw = h.surfN;
+  const DevMat& m = s.mats[mat];
+  float4 mb = __ldg(&m.base), me = __ldg(&m.emis), mm = __ldg(&m.misc);
+  h.id = (int)mm.w;
+  h.roughness = mb.w;
+  h.metallic = me.w;
+  h.opacity = mm.x;
+  h.eta = mm.y;
+  h.specular = 0.04f;
+  if (h.opacity > 1.0f - RMN_EPS) h.entering = true;
+  h.base = f3(mb);  // opaque materials only reach the GPU path
+  h.emis = f3(me);
+  if (flags & RMN_TRI_RENORM) {  // calcSurfaceNormal with a zero normal-map texel
+    float3 keep = h.surfN;
+    h.surfN = norm3(h.surfN + f3(0.0f));
+    if (!any_finite3(h.surfN)) h.surfN = keep;
+  }
+  if (dot3(h.surfN, rd) >= 0.0f) h.surfN = raw;
+  if (dot3(h.surfN, rd) >= 0.0f) h.surfN = h.shapeN;
+}
+
+// ------------------------------------------------------------------ BSDF --
+RMN_D float pow5f(float x) { float x2 = x * x; return x2 * x2 * x; }
+RMN_D float schlick(float u) {
+  float m = 1 - u;
+  m = m < 0 ? 0 : (m > 1 ? 1 : m);
+  return pow5f(m);
+}
+RMN_D float gtr1(float c, float a) {
+  if (a >= 1) return 1 / RMN_PI;
+  float a2 = a * a;
+  float t = 1 + (a2 - 1) * c * c;
+  return (a2 - 1) / (RMN_PI * logf(a2) * t);
+}
+RMN_D float gtr2(float c, float a) {
+  float a2 = a * a;
+  float t = 1 + (a2 - 1) * c * c;
+  return a2 / (RMN_PI * t * t);
+}
+RMN_D float smith_g(float c, float ag) {
+  float a = ag * ag, b = c * c;
+  return 1 / (c + sqrtf(a + b - a * b));
+}
+RMN_D void lum_clamp(float3& v) {  // clamp(vec3&), src/sampling.cpp:238-243
+  float l = dot3(v, RMN_LUM);
+  if (l > 64.0f) v = v / (l / 64.0f);
+}
+
+// BSDF::getBRDF, src/sampling.cpp:49-157 (subsurface, sheen, tints 0;
+// clearcoat 1.5, gloss 0.2). V = in, N = surfN.
+RMN_D float3 brdf(const Surf& s, float3 V, float3 L) {
+  const float3 N = s.surfN;
+  float nl = dot3(N, L), nv = dot3(N, V);
+  if (nl <= 0.0f || nv <= 0.0f) return f3(0.0f);
+  float3 H = norm3(L + V);
+  float nh = dot3(N, H), lh = dot3(L, H);
+  float3 cd = s.base;
+  float cdl = dot3(cd, RMN_LUM);
+  float3 tint = cdl > 0.0f ? cd / cdl : f3(1.0f);
+  float3 one_mix = mix3(f3(1.0f), tint, 0.0f);
+  float3 spec0 = mix3(s.specular * one_mix, cd, s.metallic);
+  float fl = schlick(nl), fv = schlick(nv);
+  float fd90 = 0.5f + 2.0f * lh * lh * s.roughness;
+  float fd = fmixf(1.0f, fd90, fl) * fmixf(1.0f, fd90, fv);
+  float fss90 = lh * lh * s.roughness;
+  float fss = fmixf(1.0f, fss90, fl) * fmixf(1.0f, fss90, fv);
+  float ss = 1.25f * (fss * (1.0f / (nl + nv) - .5f) + .5f);
+  float ds = gtr2(nh, s.roughness);
+  float fh;
+  if (s.eta <= 1.0f) {
+    fh = schlick(lh);
+  } else {
+    float ci = fabsf(lh);
+    float x = 1.0f - ci * ci;
+    float si = x <= 0.0f ? 0.0f : sqrtf(x);
+    float st = s.eta * si;
+    if (st >= 1.0f) {
+      fh = 1.0f;
+    } else {
+      float y = 1.0f - st * st;
+      float ct = y <= 0.0f ? 0.0f : sqrtf(y);
+      float r0 = (s.eta - 1.0f) / (s.eta + 1.0f);
+      r0 = r0 * r0;
+      fh = fmixf(r0, 1.0f, schlick(ct));
+    }
+  }
+  float3 fs = mix3(spec0, f3(1.0f), fh);
+  float gs = smith_g(nl, s.roughness);
+  gs *= smith_g(nv, s.roughness);
+  float3 fsheen = fh * 0.0f * one_mix;
+  float dr = gtr1(nh, fmixf(.1f, .001f, 0.2f));
+  float fr = fmixf(.04f, 1.0f, fh);
+  float gr = smith_g(nl, .25f) * smith_g(nv, .25f);
+  float3 ret = ((1.0f / RMN_PI) * fmixf(fd, ss, 0.0f) * cd + fsheen);
+  ret *= (1.0f - s.metallic);
+  ret += (0.25f * 1.5f * gr * fr * dr) * one_mix;
+  ret *= s.opacity;
+  ret += fs * ds * gs;
+  return ret * nl;
+}
+
+// getTangentSpaceWithInDir, src/geometry.cpp:105-124.
+RMN_D void frame(const Surf& s, float3 in, float3& t, float3& b) {
+  float c = dot3(s.surfN, in);
+  if (c < -1.0f + 1e-3f) {
+    float3 v0 = fabsf(s.surfN.x) < 0.8f ? f3(1.0f, 0.0f, 0.0f) : f3(0.0f, 1.0f, 0.0f);
+    t = norm3(cross3(v0, s.surfN));
+    b = cross3(s.surfN, t);
+    return;
+  }
+  b = norm3(cross3(s.surfN, in));
+  t = cross3(b, s.surfN);
+}
+
+// BSDF::sampleReflection (src/sampling.cpp:310-340) with sampleCos (:245-269)
+// and sampleBRDF (:203-236): both strategies are drawn in full, then one is
+// kept with probability pdf_cos / (pdf_cos + pdf_ggx).
+RMN_D void sample_reflect(const Surf& s, float3 in, RmnRng& rng, float3& dir, float3& w, int& fails) {
+  float3 t, b;
+  frame(s, in, t, b);
+  float3 d1 = f3(NAN), w1 = f3(0.0f), d2 = f3(NAN), w2 = f3(0.0f);
+  float p1 = 0.0f, p2 = 0.0f;
+  int f1 = 0, f2 = 0;
+  for (int T = 1; T <= RMN_MAX_TRYS; ++T) {  // sampleCos
+    float u = rng.next(), phi = rng.next() * 2.0f * RMN_PI;
+    float d = sqrtf(u);
+    float z = sqrtf(1 - d * d);
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    float x = d * cp, y = d * sp;
+    float3 o = x * t + y * b + z * s.surfN;
+    float pdf = dot3(o, s.surfN) / RMN_PI;
+    if (dot3(o, s.shapeN) > 0.0f && pdf > 0.0f) {
+      d1 = o;
+      w1 = brdf(s, in, o) / pdf;
+      lum_clamp(w1);
+      p1 = pdf;
+      break;
+    }
+    f1++;
+  }
+  for (int T = 1; T <= RMN_MAX_TRYS; ++T) {  // sampleBRDF (GGX half vector)
+    float u = rng.next(), phi = rng.next() * 2.0f * RMN_PI;
+    float ct = sqrtf((1.0f - u) / (1.0f + (s.roughness * s.roughness - 1.0f) * u));
+    float st = sqrtf(1 - ct * ct);
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    float3 H = st * cp * t + st * sp * b + ct * s.surfN;
+    float3 o = 2.0f * dot3(in, H) * H - in;
+    float lh = dot3(o, H), ln = dot3(o, s.surfN);
+    float pdf = (lh <= 0.0f || ln <= 0.0f) ? 0.0f : gtr2(ct, s.roughness) / (4.0f * lh);
+    if (dot3(o, s.shapeN) > 0.0f && pdf > 0.0f) {
+      d2 = o;
+      w2 = brdf(s, in, o) / pdf;
+      p2 = pdf;
+      break;
+    }
+    f2++;
+  }
+  float pc = p1 / (p1 + p2);
+  if (rng.next() < pc) {
+    dir = d1; w = w1; fails += f1;
+  } else {
+    dir = d2; w = w2; fails += f2;
+  }
+}
+
+// ---------------------------------------------------------- light sampling
+// RandomDistribution::operator() (src/component.cpp:20-24): lower_bound of
+// total * u in the prefix sums.
+RMN_D int prefix_draw(const float* p, int n, float x) {
+  int lo = 0, hi = n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(p + mid) < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// SkyBox::get, src/component.cpp:120-140.
+RMN_D float3 sky_get(const DevScene& s, float3 dir) {
+  if (s.sky_w == 0) return f3(0.0f);
+  float th = atan2f(-dir.x, dir.z);
+  float phi = acosf(dir.y);
+  if (th < 0.0f) th += 2.0f * RMN_PI;
+  int u = (int)(th / (2.0f * RMN_PI) * float(s.sky_w));
+  int v = (int)(phi / RMN_PI * float(s.sky_h));
+  u = u < 0 ? 0 : (u >= s.sky_w ? s.sky_w - 1 : u);
+  v = v < 0 ? 0 : (v >= s.sky_h ? s.sky_h - 1 : v);
+  phi = RMN_PI * (float(v) + 0.5f) / float(s.sky_h);
+  float area = sinf(phi) * 2.0f * RMN_PI / float(s.sky_w * s.sky_h);
+  return f3(__ldg(s.sky + (size_t)v * s.sky_w + u)) / area;
+}
+
+struct LSample {
+  float3 bsdf, light;
+  float weight;
+};
+
+// One sample T of sampleDirectLight (src/sampling.cpp:467-527), weights
+// precomputed by light_weights. Returns false when the sample is dropped.
+// pos = surface position, V = direction to the previous vertex.
+RMN_D bool light_weights(const DevScene& s, const Surf& sf, float3 V, float* w, float& tot) {
+  tot = 0.0f;
+  for (int i = 0; i < s.num_lights && i < 8; ++i) {  // getLightObjectWeight, :406-417
+    float4 c = __ldg(&s.lights[i].center);
+    float3 ld = norm3(f3(c) - sf.pos);
+    float dist = len3(f3(c) - sf.pos);
+    float3 f = brdf(sf, V, ld);
+    w[i] = dot3(f, RMN_LUM) * c.w / (dist * dist + 1e-3f);
+  }
+  for (int i = 0; i < s.num_lights && i < 8; ++i) tot += w[i];
+  return tot != 0.0f;
+}
+
+RMN_D bool light_sample(const DevScene& s, const Surf& sf, float3 V, const float* w, float tot, int cnt, RmnRng& rng,
+                        LSample& out, int* status) {
+  const float3 pos = sf.pos;
+  if (s.sky_w == 0) {
+    float rv = tot * rng.next();  // sample(), :396-404
+    int li = -1;
+    float acc = 0.0f;
+    for (int i = 0; i < s.num_lights && i < 8; ++i) {
+      acc += w[i];
+      if (rv <= acc) { li = i; break; }
+    }
+    if (li < 0) return false;
+    float pl = w[li] / tot;
+    const DevLight& L = s.lights[li];
+    float4 lc = __ldg(&L.center), lcol = __ldg(&L.color);
+    int nf = (int)lcol.w, first = L.first_face;
+    const float* pre = s.light_prefix + first;
+    float total = __ldg(pre + nf - 1);
+    float3 lp = f3(NAN);
+    int fails = 0;
+    for (int T = 1; T <= RMN_MAX_TRYS; ++T) {  // sampleLightFace, :436-448
+      int fi = prefix_draw(pre, nf, total * rng.next());
+      if (fi >= nf) fi = nf - 1;
+      const float4* F = s.light_faces + (size_t)(first + fi) * RMN_LIGHT_FACE_F4;
+      float3 v0 = f3(__ldg(F)), v1 = f3(__ldg(F + 1)), v2 = f3(__ldg(F + 2));
+      float a = rng.next(), b = rng.next();  // generateRandomPointInLightFace, :419-434
+      if (a + b > 1.0f) { a = 1.0f - a; b = 1.0f - b; }
+      float c = 1.0f - a - b;
+      float3 p = a * v0 + b * v1 + c * v2;
+      float3 ld = norm3(p - pos);
+      float3 e1 = v1 - v0, e2 = v2 - v0;
+      float area = len3(cross3(e1, e2)) / 2.0f;
+      bool smooth = !(area > 1e-2f);
+      float3 sn, un;
+      bool ent;
+      hit_normals(e1, e2, smooth, f3(__ldg(F + 3)), f3(__ldg(F + 4)), f3(__ldg(F + 5)), ld, f3(a, b, c), sn, un, ent);
+      float cphi = dot3(un, -ld);
+      if (cphi > 0.0f && rng.next() < cphi) { lp = p; break; }
+      fails++;
+    }
+    if (!any_finite3(lp)) return false;
+    float3 ld = norm3(lp - pos);
+    float dist = len3(lp - pos);
+    TRay r = make_tray(pos, ld);
+    float aim = dist - RMN_EPS;
+    float tmax = aim + RMN_EPS;
+    int h = trace<true, false>(s, r, RMN_EPS, tmax, aim, nullptr);
+    if (h == -2) atomicExch(status, 1);
+    if (!(tmax >= aim)) return false;
+    float3 f = brdf(sf, V, ld);
+    lum_clamp(f);
+    out.bsdf = f;
+    out.light = 2.0f * RMN_PI * lc.w * f3(lcol) / (dist * dist + 1e-3f) / pl;
+    out.weight = 1.0f / (float)(cnt * (fails + 1));
+    return true;
+  }
+  // sampleSkyBox, :450-465
+  const int npx = s.sky_w * s.sky_h;
+  const float total = __ldg(s.sky_prefix + npx - 1);
+  for (int T = 1; T <= RMN_MAX_TRYS; ++T) {
+    int p = prefix_draw(s.sky_prefix, npx, total * rng.next());
+    if (p >= npx) p = npx - 1;
+    int u = p % s.sky_w, v = p / s.sky_w;
+    float phi = RMN_PI * (float(v) + 0.5f) / float(s.sky_h);
+    float th = 2.0f * RMN_PI * (float(u) + 0.5f) / float(s.sky_w);
+    float sp = sinf(phi), cp = cosf(phi), st = sinf(th), ct = cosf(th);
+    float3 dir = f3(-sp * st, cp, sp * ct);
+    if (dot3(dir, sf.surfN) > 0.0f) {
+      float pr = __ldg(s.sky_prefix + p);
+      if (p > 0) pr -= __ldg(s.sky_prefix + p - 1);
+      float pdf = pr / total;
+      float3 light = f3(__ldg(s.sky + p)) / pdf;
+      TRay r = make_tray(pos, dir);
+      float tmax = INFINITY;
+      int h = trace<true, false>(s, r, RMN_EPS, tmax, INFINITY, nullptr);
+      if (h == -2) atomicExch(status, 1);
+      if (!(tmax >= INFINITY)) return false;
+      float3 f = brdf(sf, V, dir);
+      lum_clamp(f);
+      out.bsdf = f;
+      out.light = light;
+      out.weight = 1.0f / (float)cnt;
+      return true;
+    }
+  }
+  return false;
+}

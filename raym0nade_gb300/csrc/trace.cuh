@@ -1,0 +1,163 @@
+// Device-side BVH traversal shared by the ray-query kernels and the
+// integrator. Included by the .cu files only.
+//
+// Order of visits and every float operation follow the reference's
+// recursive BVH::dfs_rayHit (src/bvh.cpp:56-88) so that closest-hit ids are
+// the reference's:
+//  * at an inner node both child boxes are tested with rayInBox
+//    (src/geometry.cpp:40-61) from [t_min, current t_max];
+//  * the child with the smaller entry distance goes first (ties: the right
+//    child); the other is deferred on a per-thread stack together with its
+//    entry distance and is visited only if that distance is still below the
+//    current t_max when it is popped -- the moment the recursion would return
+//    to it;
+//  * a leaf tests its triangles in order and keeps t only if
+//    t_min < t < t_max (first hit wins ties).
+#pragma once
+#include "rmn_internal.h"
+
+struct TRay {
+  float3 o, d, inv;
+  int par;  // bit i: |d_i| < 1e-4 (origin-inside rule)
+  int neg;  // bit i: 1/d_i < 0
+};
+
+RMN_D TRay make_tray(float3 o, float3 d) {
+  TRay r;
+  r.o = o;
+  r.d = d;
+  r.par = (fabsf(d.x) < RMN_EPS ? 1 : 0) | (fabsf(d.y) < RMN_EPS ? 2 : 0) | (fabsf(d.z) < RMN_EPS ? 4 : 0);
+  r.inv = f3(1.0f / d.x, 1.0f / d.y, 1.0f / d.z);
+  r.neg = (r.inv.x >= 0.0f ? 0 : 1) | (r.inv.y >= 0.0f ? 0 : 2) | (r.inv.z >= 0.0f ? 0 : 4);
+  return r;
+}
+
+// One axis of rayInBox. `stop` freezes tL/tR once the reference would have
+// returned (tL > tR, or origin outside a slab the ray is parallel to).
+RMN_D void slab_axis(bool par, bool neg, float o, float inv, float lo, float hi, float& tL, float& tR, bool& stop) {
+  if (stop) return;
+  if (par) {
+    if (o < lo || o > hi) {
+      tR = -1.0f;
+      stop = true;
+    }
+    return;
+  }
+  float a = neg ? hi : lo, b = neg ? lo : hi;
+  tL = fmaxf(tL, (a - o) * inv);
+  tR = fminf(tR, (b - o) * inv);
+  tR += RMN_EPS;
+  if (tL > tR) stop = true;
+}
+
+// rayInBox + the node test `tL < tR` of dfs_rayHit.
+RMN_D bool box_hit(const TRay& r, float3 lo, float3 hi, float tmin, float tmax, float& tL) {
+  float L = tmin, R = tmax;
+  bool stop = false;
+  slab_axis(r.par & 1, r.neg & 1, r.o.x, r.inv.x, lo.x, hi.x, L, R, stop);
+  slab_axis(r.par & 2, r.neg & 2, r.o.y, r.inv.y, lo.y, hi.y, L, R, stop);
+  slab_axis(r.par & 4, r.neg & 4, r.o.z, r.inv.z, lo.z, hi.z, L, R, stop);
+  tL = L;
+  return L < R;
+}
+
+// RayTriangleIntersection (Moller-Trumbore), src/geometry.cpp:63-87.
+RMN_D float tri_t(const TRay& r, float3 v0, float3 e1, float3 e2, float len_e1) {
+  float3 h = cross3(r.d, e2);
+  float a = dot3(e1, h);
+  if (fabsf(a) / len_e1 < RMN_EPS) return INFINITY;
+  float f = 1.0f / a;
+  float3 s = r.o - v0;
+  float u = f * dot3(s, h);
+  if (u < 0.0f || u > 1.0f) return INFINITY;
+  float3 q = cross3(s, e1);
+  float v = f * dot3(r.d, q);
+  if (v < 0.0f || u + v > 1.0f) return INFINITY;
+  return f * dot3(e2, q);
+}
+
+struct TraceCounters {
+  uint32_t inner, leaves, tris;
+};
+
+// Closest hit in (tmin, tmax). Returns the leaf-order triangle index or -1;
+// tmax becomes the hit distance. With ANY set, returns as soon as a hit
+// closer than `aim` is recorded (Model::rayHit_test's question, answered
+// after the same visits as the full query up to that point).
+// Returns -2 if the stack would overflow (never for trees the builder accepts).
+template <bool ANY, bool COUNT>
+RMN_D int trace(const DevScene& s, const TRay& r, float tmin, float& tmax, float aim, TraceCounters* cnt) {
+  int hit = -1;
+  int stack_ref[RMN_STACK];
+  float stack_tl[RMN_STACK];
+  int sp = 0;
+  int cur = s.root;
+  for (;;) {
+    if (cur >= 0) {
+      const DevNode* n = s.nodes + cur;
+      float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
+      int4 D = __ldg(&n->d);
+      if (COUNT) cnt->inner++;
+      float tl0, tl1;
+      bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, tmax, tl0);
+      bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, tmax, tl1);
+      int nref, fref;
+      bool hn, hf;
+      float tlf;
+      if (tl0 < tl1) {
+        nref = D.x; hn = h0; fref = D.y; hf = h1; tlf = tl1;
+      } else {
+        nref = D.y; hn = h1; fref = D.x; hf = h0; tlf = tl0;
+      }
+      if (hn) {
+        if (hf) {
+          if (sp >= RMN_STACK) return -2;
+          stack_ref[sp] = fref;
+          stack_tl[sp] = tlf;
+          ++sp;
+        }
+        cur = nref;
+        continue;
+      }
+      if (hf && tlf < tmax) {
+        cur = fref;
+        continue;
+      }
+    } else {
+      int x = ~cur;
+      int first = x >> 4, count = x & 15;
+      if (COUNT) { cnt->leaves++; cnt->tris += count; }
+      for (int i = first; i < first + count; ++i) {
+        const float4* t = s.tri + 3 * i;
+        float4 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2);
+        float th = tri_t(r, f3(a), f3(b), f3(c), b.w);
+        if (tmin < th && th < tmax) {
+          tmax = th;
+          hit = i;
+          if (ANY && th < aim) return hit;
+        }
+      }
+    }
+    // pop: the deferred child is visited only if it still starts before the
+    // current closest hit
+    for (;;) {
+      if (sp == 0) return hit;
+      --sp;
+      if (stack_tl[sp] < tmax) {
+        cur = stack_ref[sp];
+        break;
+      }
+    }
+  }
+}
+
+// barycentric(v0, v1, v2, P), src/geometry.cpp:89-103, with e1 = v1 - v0 and
+// e2 = v2 - v0 precomputed. Returns (gamma, alpha, beta).
+RMN_D float3 bary(float3 v0, float3 e1, float3 e2, float3 p) {
+  float3 n = cross3(e1, e2);
+  float den = dot3(n, n);
+  float3 vp = p - v0;
+  float al = dot3(cross3(vp, e2), n) / den;
+  float be = dot3(cross3(e1, vp), n) / den;
+  return f3(1.0f - al - be, al, be);
+}

@@ -1,0 +1,74 @@
+"""Host-side checks of librmn.so that need no GPU: it builds for sm_103a,
+loads, and exports every function include/rmn.h declares; host helpers."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from raym0nade_gb300 import _lib, build
+    build.build()
+    return _lib.load()
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "rmn.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:const char\*|rmn_status)\s+(rmn_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("rmn_scene_create", "rmn_trace_closest", "rmn_trace_shadow", "rmn_render", "rmn_fxaa",
+                 "rmn_compose", "rmn_last_error"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from raym0nade_gb300 import _lib
+    for name in declared_functions():
+        assert hasattr(lib, name), name
+        assert name in _lib.SIGNATURES, f"{name} has no ctypes signature"
+    assert lib.rmn_version().startswith(b"raym0nade-gb300")
+
+
+def test_struct_sizes_match_header():
+    from raym0nade_gb300 import _lib
+    assert ctypes.sizeof(_lib.Material) == 64
+    assert ctypes.sizeof(_lib.RenderArgs) == 4 * 17 + 4 * 5 + 8 + 4 * 4
+    assert ctypes.sizeof(_lib.Image) == 5 * 8
+
+
+def test_parse_render_args_docs_block():
+    from raym0nade_gb300.api import parse_render_args
+    block = """0.96718 -0.2 -0.156768
+0.16 0 0.987117
+-0.1974234 -0.9798 0.032
+-16.5 -0.5 -2.25
+0.001025 15.0 32.0 200.0
+2048 1152
+0 12 0.7
+output/Bistro"""
+    a = parse_render_args(block)
+    d = np.array([0.96718, -0.2, -0.156768]); r = np.array([0.16, 0, 0.987117]); u = np.array([-0.1974234, -0.9798, 0.032])
+    assert np.allclose(a.position, -16.5 * d - 0.5 * r - 2.25 * u, atol=1e-5)
+    assert (a.width, a.height, a.spp, a.threads) == (2048, 1152, 0, 12)
+    assert a.accuracy == pytest.approx(0.001025) and a.exposure == 200.0 and a.P_Direct == pytest.approx(0.7)
+    assert a.savePath == "output/Bistro"
+
+
+def test_scene_generators_shapes():
+    from raym0nade_gb300 import scenes
+    c = scenes.cornell()
+    assert c.num_triangles == 36
+    s = scenes.random_soup(1000, 1)
+    assert s.num_triangles == 1000
+    h = scenes.heightfield(33, seed=1, extent=3.0, patch=8)
+    assert h.num_triangles == 2 * 32 * 32
+    e = scenes.sky_env(64, 32)
+    assert e.shape == (32, 64, 3) and e.max() >= 5e4
