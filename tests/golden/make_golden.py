@@ -16,6 +16,10 @@ Fixtures (numpy .npz, compressed):
                      sky (sky-mode light sampling, smooth normals).
   post.npz           Photo::shade(Full) + gammaCorrection of render records,
                      and Photo::FXAA of a 96 x 64 image with hard edges.
+  cornell_4096spp.npz  the converged reference image of the Cornell workload
+                     (256 x 256, 4096 spp, max depth 16, P_Direct 0.7):
+                     Photo::shade(Full) before gamma, float16. Made by
+                     ``python tests/golden/make_golden.py --converged``.
 """
 import os
 import sys
@@ -120,5 +124,20 @@ def main():
     print("fixtures written to", HERE)
 
 
+def converged():
+    bindings.build(with_reference=True)
+    R = bindings.OracleLib("ref")
+    cor = scenes.cornell()
+    cam = scenes.cornell_camera(256, 256, 4096)
+    rec = R.scene(cor).render(cam, seed=4096, threads=os.cpu_count() or 8)
+    lin = R.compose(rec, 1.0, gamma=False)
+    np.savez_compressed(os.path.join(HERE, "cornell_4096spp.npz"), linear=lin.astype(np.float16),
+                        args=cam.packed(), seed=4096, mean=np.float64(lin.astype(np.float64).mean()))
+    print("converged Cornell reference written")
+
+
 if __name__ == "__main__":
-    main()
+    if "--converged" in sys.argv:
+        converged()
+    else:
+        main()

@@ -1,0 +1,175 @@
+"""GPU integrator parity, through the C ABI (rmn_render).
+
+Three levels:
+* per path -- the oracle re-runs the reference's estimator on the library's
+  counter-based random streams (oracle mode 1), so both sides draw the same
+  numbers: the G-buffer must be bit-identical and nearly every pixel's
+  radiance must agree to 1e-3 (a path can still branch differently where
+  CUDA's and glibc's sinf/cosf/powf/logf differ in the last bit);
+* invariance -- the lane split of a pixel's samples (lanes_per_pixel) must
+  not change the result beyond float summation order (rtol 1e-4);
+* converged -- the reference's own renderer at 4096 spp
+  (tests/golden/cornell_4096spp.npz, made from the compiled reference) vs the
+  GPU at 4096 spp: relative MSE <= 1e-3 (on 4x4-binned images; see the
+  test for why), full-resolution error within the GPU's own noise floor, and
+  mean luminance within 0.5%.
+"""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+from raym0nade_gb300 import api, scenes  # noqa: E402
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+LUM = np.array([0.3, 0.6, 0.1], np.float32)
+
+
+def gpu_records(model, cam, seed, lanes=0, host=False):
+    args = api.RenderArgs.from_camera(cam, seed=seed, lanes_per_pixel=lanes)
+    photo = api.Photo(cam.width, cam.height, cam.exposure, device=not host)
+    api.render(model, args, photo)
+    t = lambda x: x.cpu().numpy() if isinstance(x, torch.Tensor) else x
+    g = t(photo.Gbuffer)
+    rec = np.zeros((cam.height * cam.width, 40), np.float32)
+    rec[:, 0:4], rec[:, 4:8] = t(photo.radiance_Dd), t(photo.radiance_Ds)
+    rec[:, 8:12], rec[:, 12:16] = t(photo.radiance_Id), t(photo.radiance_Is)
+    rec[:, 16:31] = g[:, 0:15]
+    rec[:, 31], rec[:, 32], rec[:, 33], rec[:, 35], rec[:, 36] = g[:, 15], g[:, 16], g[:, 17], g[:, 18], g[:, 19]
+    return rec.reshape(cam.height, cam.width, 40), photo
+
+
+def linear_image(rec):
+    rd = rec[..., 0:3] + rec[..., 8:11]
+    rs = rec[..., 4:7] + rec[..., 12:15]
+    return rec[..., 16:19] * rd + rs + rec[..., 19:22]
+
+
+def compare_paths(gpu, ora, frac=0.98):
+    # G-buffer: primary hit and shading are float-exact
+    for a, b in [(16, 19), (19, 22), (22, 25), (25, 28), (28, 31)]:
+        assert np.array_equal(gpu[..., a:b], ora[..., a:b], equal_nan=True), (a, b)
+    assert np.array_equal(gpu[..., 31:34], ora[..., 31:34])
+    li, lo = linear_image(gpu), linear_image(ora)
+    close = np.isclose(li, lo, rtol=1e-3, atol=1e-5).all(-1)
+    assert close.mean() >= frac, f"only {close.mean():.4f} of pixels agree"
+    assert abs(li.mean() - lo.mean()) <= 5e-3 * abs(lo.mean()) + 1e-6
+    return close.mean()
+
+
+@pytest.mark.parametrize("maxd", [16, 8])
+def test_cornell_paths_match_oracle(port, maxd):
+    c = scenes.cornell()
+    cam = scenes.cornell_camera(48, 48, 16, max_depth=maxd)
+    g, _ = gpu_records(api.Model(c), cam, seed=11)
+    o = port.scene(c).render(cam, seed=11, mode=1)
+    compare_paths(g, o)
+
+
+def test_sky_paths_match_oracle(port):
+    hf = scenes.heightfield(40, seed=9, extent=4.0, patch=8)
+    hf.env = scenes.sky_env(128, 64, sun_radiance=500.0, sun_diameter_deg=6.0)
+    cam = scenes.Camera((0.3, 2.0, -0.8), (0.35, -0.45, 0.82), (0.0, -1.0, 0.0), (-1.0, 0.0, 0.0), 0.03, 40, 30, 12)
+    g, _ = gpu_records(api.Model(hf), cam, seed=5)
+    o = port.scene(hf).render(cam, seed=5, mode=1)
+    compare_paths(g, o)
+
+
+@pytest.mark.parametrize("spp,p_direct", [(1, 0.7), (5, 0.0), (4, 1.0), (33, 0.5)])
+def test_sample_splits(port, spp, p_direct):
+    c = scenes.cornell()
+    cam = scenes.cornell_camera(24, 24, spp, p_direct=p_direct)
+    g, _ = gpu_records(api.Model(c), cam, seed=3)
+    o = port.scene(c).render(cam, seed=3, mode=1)
+    compare_paths(g, o)
+
+
+def test_lane_split_invariance():
+    c = scenes.cornell()
+    m = api.Model(c)
+    cam = scenes.cornell_camera(40, 40, 64)
+    base, _ = gpu_records(m, cam, seed=21, lanes=1)
+    for k in (2, 8, 32):
+        r, _ = gpu_records(m, cam, seed=21, lanes=k)
+        np.testing.assert_allclose(linear_image(r), linear_image(base), rtol=1e-4, atol=1e-6)
+        assert np.array_equal(r[..., 16:31], base[..., 16:31], equal_nan=True)
+
+
+def test_host_buffers_match_device_buffers():
+    c = scenes.cornell()
+    m = api.Model(c)
+    cam = scenes.cornell_camera(32, 32, 8)
+    d, _ = gpu_records(m, cam, seed=2)
+    h, _ = gpu_records(m, cam, seed=2, host=True)
+    assert np.array_equal(d, h, equal_nan=True)
+
+
+def test_emitter_and_miss_pixels(port):
+    c = scenes.cornell()
+    m = api.Model(c)
+    # looking up at the light from below: emissive first hits
+    up = scenes.Camera((0.5, 0.3, 0.5), (0.0, 1.0, 0.0), (0.0, 0.0, 1.0), (1.0, 0.0, 0.0), 0.02, 24, 24, 8)
+    g, _ = gpu_records(m, up, seed=4)
+    o = port.scene(c).render(up, seed=4, mode=1)
+    compare_paths(g, o)
+    assert (g[..., 19:22].sum(-1) > 0).any()
+    # looking out of the open front: every primary ray misses (no sky)
+    out = scenes.Camera((0.5, 0.5, 0.5), (0.0, 0.0, -1.0), (0.0, -1.0, 0.0), (1.0, 0.0, 0.0), 0.001, 16, 16, 8)
+    g2, _ = gpu_records(m, out, seed=4)
+    assert np.isnan(g2[..., 22]).all() and np.all(g2[..., 0:16] == 0)
+
+
+def test_render_argument_errors():
+    m = api.Model(scenes.cornell())
+    cam = scenes.cornell_camera(8, 8, 4)
+    for field, value in [("P_Direct", 1.5), ("max_depth", 0), ("max_depth", 17), ("lanes_per_pixel", 3),
+                         ("width", 0)]:
+        a = api.RenderArgs.from_camera(cam)
+        setattr(a, field, value)
+        with pytest.raises(api.RmnError) as e:
+            api.render(m, a, api.Photo(8, 8))
+        assert e.value.status == 1, field
+
+
+def _rel_mse(a, b):
+    return ((a - b) ** 2).mean() / (b ** 2).mean()
+
+
+def _bin(img, f=4):
+    h, w, c = img.shape
+    return img.reshape(h // f, f, w // f, f, c).mean((1, 3))
+
+
+def test_converged_cornell_matches_reference():
+    """North-star image parity: 256^2 Cornell at 4096 spp vs the reference's
+    own 4096-spp render (independent random streams), on the linear
+    Photo::shade(Full) image.
+
+    The reference's estimator is heavy-tailed: two independent 4096-spp
+    renders of this scene differ by a relative MSE of about 5e-3 per pixel,
+    the reference against itself included. So the 1e-3 bound is applied to
+    4x4-binned images, and at full resolution the GPU-vs-reference error must
+    stay within 1.5x the noise floor measured between two independent GPU
+    renders -- a bias in the GPU estimator would push it above that floor.
+    Mean luminance must agree within 0.5%."""
+    z = np.load(os.path.join(GOLDEN, "cornell_4096spp.npz"))
+    ref = z["linear"].astype(np.float64)
+    cam = scenes.cornell_camera(256, 256, 4096)
+    m = api.Model(scenes.cornell())
+    g, photo = gpu_records(m, cam, seed=123)
+    lin = photo.shade(api.Full).cpu().numpy().astype(np.float64)
+    assert np.allclose(lin, linear_image(g), rtol=1e-5, atol=1e-6)
+    g2, photo2 = gpu_records(m, cam, seed=456)
+    lin2 = photo2.shade(api.Full).cpu().numpy().astype(np.float64)
+    floor = _rel_mse(lin2, lin)
+    full = _rel_mse(lin, ref)
+    binned = _rel_mse(_bin(lin), _bin(ref))
+    lum_g, lum_r = (lin @ LUM).mean(), (ref @ LUM).mean()
+    print(f"rel-MSE full {full:.3e} (GPU-GPU floor {floor:.3e}), 4x4-binned {binned:.3e}, "
+          f"mean luminance {lum_g:.6f} vs {lum_r:.6f}")
+    assert binned <= 1e-3
+    assert full <= 1.5 * floor
+    assert abs(lum_g - lum_r) <= 5e-3 * lum_r
