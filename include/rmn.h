@@ -172,6 +172,38 @@ rmn_status rmn_trace_shadow(rmn_scene* scene, const rmn_ray* rays, int64_t n, ui
  * rmn_fxaa. */
 rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, const rmn_image* image, void* stream);
 
+/* Visit counters and kernel times of one render: rmn_render run twice on
+ * the same arguments -- once with counting traversal, once with CUDA events
+ * around the two kernels -- leaving the same images. For roofline figures
+ * (bytes per ray) and ray throughput; not needed to render. */
+typedef struct rmn_render_profile {
+  double primary_ms, path_ms;   /* G-buffer kernel, path kernel */
+  uint64_t closest_rays, shadow_rays;
+  uint64_t inner_visits, leaf_visits, triangle_tests;
+  uint64_t sample_slots, pixels;
+} rmn_render_profile;
+rmn_status rmn_render_profile_get(rmn_scene* scene, const rmn_render_args* args, const rmn_image* image,
+                                  rmn_render_profile* out, void* stream);
+
+/* Batched rendering: many (scene, args, image) renders of uneven size in one
+ * persistent launch -- the pixels of every item feed one G-buffer kernel and
+ * the sample tasks of every item one persistent path kernel -- optionally
+ * captured once into a CUDA graph and replayed by rmn_batch_render. The
+ * reference has no counterpart (it renders one Model per render_multiThread
+ * call, src/render.cpp:593); each item's images are identical to rmn_render's
+ * for the same arguments. All image buffers of a batch must be device memory
+ * (their addresses are baked into the batch). */
+typedef struct rmn_batch rmn_batch;
+typedef struct rmn_batch_item {
+  rmn_scene* scene;
+  rmn_render_args args;
+  rmn_image image;
+} rmn_batch_item;
+rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, int32_t use_graph, void* stream, rmn_batch** out);
+rmn_status rmn_batch_render(rmn_batch* batch, void* stream);
+rmn_status rmn_batch_profile(rmn_batch* batch, rmn_render_profile* out, void* stream);
+rmn_status rmn_batch_destroy(rmn_batch* batch);
+
 /* Photo::shade(options) [+ gammaCorrection] [+ FXAA] (src/image.cpp:215-246,
  * 454-479) over rmn_render's buffers -> rgb (3 floats per pixel). */
 rmn_status rmn_compose(const rmn_image* image, int32_t width, int32_t height, float exposure, int32_t options,

@@ -876,16 +876,16 @@ static void fxaa(const float* in, float* out, int W, int H) {
 }
 
 template <class F>
-static void parallel_for(long n, int threads, F&& f) {
-  if (threads <= 1 || n < 64) { for (long i = 0; i < n; ++i) f(i); return; }
+static void parallel_for(long n, int threads, F&& f, long chunk = 64) {
+  if (threads <= 1 || n <= chunk) { for (long i = 0; i < n; ++i) f(i); return; }
   std::atomic<long> next(0);
   std::vector<std::thread> pool;
   for (int t = 0; t < threads; ++t)
     pool.emplace_back([&] {
       for (;;) {
-        long i0 = next.fetch_add(64);
+        long i0 = next.fetch_add(chunk);
         if (i0 >= n) break;
-        long i1 = std::min(n, i0 + 64);
+        long i1 = std::min(n, i0 + chunk);
         for (long i = i0; i < i1; ++i) f(i);
       }
     });
@@ -1078,7 +1078,7 @@ void port_render(void* h, const float* args, uint64_t seed, int mode, int x0, in
   parallel_for(n, threads, [&](long i) {
     int x = x0 + (int)(i % rw), y = y0 + (int)(i / rw);
     render_pixel(s, a, seed, mode, x, y, out + ORC_PIX_FLOATS * i);
-  });
+  }, 1);
 }
 
 // Photo::shade(Full) [+ gammaCorrection] over pixel records -> rgb.

@@ -145,8 +145,8 @@ int nodeCount(int u, int n);
 void renderPixel(const Model& model, const RenderArgs& args, RenderData& renderData, Photo& image, int x, int y);
 
 template <class F>
-static void for_each_index(long n, int threads, F&& f) {
-  if (threads <= 1 || n < 64) {
+static void for_each_index(long n, int threads, F&& f, long chunk = 64) {
+  if (threads <= 1 || n <= chunk) {
     for (long i = 0; i < n; ++i) f(i);
     return;
   }
@@ -155,9 +155,9 @@ static void for_each_index(long n, int threads, F&& f) {
   for (int t = 0; t < threads; ++t)
     pool.emplace_back([&] {
       for (;;) {
-        long i0 = next.fetch_add(64);
+        long i0 = next.fetch_add(chunk);
         if (i0 >= n) break;
-        long i1 = std::min(n, i0 + 64);
+        long i1 = std::min(n, i0 + chunk);
         for (long i = i0; i < i1; ++i) f(i);
       }
     });
@@ -322,7 +322,7 @@ void ref_render(void* h, const float* args, uint64_t seed, int mode, int x0, int
     RenderData rd((int)orc_pixel_seed(seed, (uint32_t)id));
     renderPixel(m, a, rd, ph, x, y);
     put_pixel(ph, id, out + ORC_PIX_FLOATS * i);
-  });
+  }, 1);
 }
 
 void ref_compose(const float* recs, int64_t n, float exposure, int apply_gamma, float* rgb) {

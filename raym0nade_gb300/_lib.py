@@ -47,6 +47,16 @@ class Image(C.Structure):
                 ("radiance_Is", C.c_void_p), ("gbuffer", C.c_void_p)]
 
 
+class RenderProfile(C.Structure):
+    _fields_ = [("primary_ms", C.c_double), ("path_ms", C.c_double), ("closest_rays", C.c_uint64),
+                ("shadow_rays", C.c_uint64), ("inner_visits", C.c_uint64), ("leaf_visits", C.c_uint64),
+                ("triangle_tests", C.c_uint64), ("sample_slots", C.c_uint64), ("pixels", C.c_uint64)]
+
+
+class BatchItem(C.Structure):
+    _fields_ = [("scene", C.c_void_p), ("args", RenderArgs), ("image", Image)]
+
+
 # name -> (restype, argtypes); every declaration of include/rmn.h.
 SIGNATURES = {
     "rmn_last_error": (C.c_char_p, []),
@@ -57,6 +67,12 @@ SIGNATURES = {
     "rmn_trace_closest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "rmn_trace_shadow": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "rmn_render": (C.c_int, [C.c_void_p, C.POINTER(RenderArgs), C.POINTER(Image), C.c_void_p]),
+    "rmn_render_profile_get": (C.c_int, [C.c_void_p, C.POINTER(RenderArgs), C.POINTER(Image),
+                                         C.POINTER(RenderProfile), C.c_void_p]),
+    "rmn_batch_create": (C.c_int, [C.POINTER(BatchItem), C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "rmn_batch_render": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rmn_batch_profile": (C.c_int, [C.c_void_p, C.POINTER(RenderProfile), C.c_void_p]),
+    "rmn_batch_destroy": (C.c_int, [C.c_void_p]),
     "rmn_compose": (C.c_int, [C.POINTER(Image), C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p,
                               C.c_void_p]),
     "rmn_fxaa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),

@@ -257,6 +257,57 @@ def render(model: Model, args: RenderArgs, photo: Photo | None = None, stream=No
     return photo
 
 
+def render_profile(model: Model, args: RenderArgs, photo: Photo | None = None, stream=None):
+    """rmn_render_profile_get: render twice (counting, then timed) and return
+    (photo, dict of kernel times and visit counters)."""
+    if photo is None:
+        photo = Photo(args.width, args.height, args.exposure)
+    a = args.c()
+    img = photo.c_image()
+    prof = _lib.RenderProfile()
+    _check(_lib.load().rmn_render_profile_get(model.handle, C.byref(a), C.byref(img), C.byref(prof),
+                                              _stream(stream)), "rmn_render_profile_get")
+    return photo, {k: getattr(prof, k) for k, _ in prof._fields_}
+
+
+class Batch:
+    """rmn_batch: many renders in one persistent launch, optionally replayed
+    from a captured CUDA graph. Photos must live on the device."""
+
+    def __init__(self, items, use_graph: bool = True, stream=None):
+        """items: list of (Model, RenderArgs, Photo)."""
+        lib = _lib.load()
+        arr = (_lib.BatchItem * len(items))()
+        for i, (m, a, ph) in enumerate(items):
+            arr[i].scene = m.handle.value
+            arr[i].args = a.c()
+            arr[i].image = ph.c_image()
+        h = C.c_void_p()
+        _check(lib.rmn_batch_create(arr, len(items), 1 if use_graph else 0, _stream(stream), C.byref(h)),
+               "rmn_batch_create")
+        self._h = h
+        self.items = items
+
+    def render(self, stream=None):
+        _check(_lib.load().rmn_batch_render(self._h, _stream(stream)), "rmn_batch_render")
+
+    def profile(self, stream=None) -> dict:
+        prof = _lib.RenderProfile()
+        _check(_lib.load().rmn_batch_profile(self._h, C.byref(prof), _stream(stream)), "rmn_batch_profile")
+        return {k: getattr(prof, k) for k, _ in prof._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _lib.load().rmn_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def render_multiThread(model: Model, args: RenderArgs) -> Photo:
     """render_multiThread (include/render.h:43): render, then export the
     images the reference exports before its denoiser runs

@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 #include "rmn_host.h"
 
@@ -253,12 +254,7 @@ rmn_status rmn_compose(const rmn_image* image, int32_t width, int32_t height, fl
 
 }  // extern "C"
 
-extern "C" rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, const rmn_image* image, void* stream) {
-  clear_error();
-  if (!scene || !args || !image) return fail(RMN_ERR_INVALID_ARGUMENT, "NULL scene, args or image");
-  if (!image->radiance_Dd || !image->radiance_Ds || !image->radiance_Id || !image->radiance_Is)
-    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_render needs the four radiance buffers");
-  const rmn_render_args& a = *args;
+static rmn_status check_args(const rmn_render_args& a) {
   if (a.width <= 0 || a.height <= 0 || (int64_t)a.width * a.height > (1LL << 30))
     return fail(RMN_ERR_INVALID_ARGUMENT, "image size %d x %d out of range", a.width, a.height);
   if (a.spp < 0 || a.spp > (1 << 20)) return fail(RMN_ERR_INVALID_ARGUMENT, "spp %d out of range", a.spp);
@@ -267,12 +263,24 @@ extern "C" rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, 
   int k = a.lanes_per_pixel;
   if (k != 0 && (k < 1 || k > 32 || (k & (k - 1))))
     return fail(RMN_ERR_INVALID_ARGUMENT, "lanes_per_pixel must be 0 or a power of two up to 32");
+  return RMN_OK;
+}
+
+// rmn_render / rmn_render_profile_get: a one-render batch without a graph.
+static rmn_status render_one(rmn_scene* scene, const rmn_render_args* args, const rmn_image* image, void* stream,
+                             RenderProfileData* prof) {
+  clear_error();
+  if (!scene || !args || !image) return fail(RMN_ERR_INVALID_ARGUMENT, "NULL scene, args or image");
+  if (!image->radiance_Dd || !image->radiance_Ds || !image->radiance_Id || !image->radiance_Is)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_render needs the four radiance buffers");
+  const rmn_render_args& a = *args;
+  rmn_status r = check_args(a);
+  if (r != RMN_OK) return r;
   if (scene->dev.num_lights > 8) return fail(RMN_ERR_UNSUPPORTED, "more than 8 light objects");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const size_t npx = (size_t)a.width * a.height;
   Arg dd, ds, id, is, gb;
-  Status status;
-  rmn_status r = stage_out(image->radiance_Dd, npx * 16, st, &dd);
+  r = stage_out(image->radiance_Dd, npx * 16, st, &dd);
   if (r == RMN_OK) r = stage_out(image->radiance_Ds, npx * 16, st, &ds);
   if (r == RMN_OK) r = stage_out(image->radiance_Id, npx * 16, st, &id);
   if (r == RMN_OK) r = stage_out(image->radiance_Is, npx * 16, st, &is);
@@ -285,23 +293,117 @@ extern "C" rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, 
       gb.owned = true;
     }
   }
-  if (r == RMN_OK) r = status.init(st);
+  BatchState* b = nullptr;
   if (r == RMN_OK) {
-    cudaError_t e = launch_render(scene->dev, a, static_cast<float*>(gb.dev), static_cast<float*>(dd.dev),
-                                  static_cast<float*>(ds.dev), static_cast<float*>(id.dev),
-                                  static_cast<float*>(is.dev), status.dev, st);
-    if (e != cudaSuccess) r = cuda_fail(e, "render launch");
+    RenderItem it{scene, a, static_cast<float*>(gb.dev), static_cast<float*>(dd.dev), static_cast<float*>(ds.dev),
+                  static_cast<float*>(id.dev), static_cast<float*>(is.dev)};
+    r = batch_create(&it, 1, false, st, &b);
   }
+  if (r == RMN_OK) r = prof ? batch_profile(b, st, prof) : batch_launch(b, st);
   if (r == RMN_OK) r = finish_out(image->radiance_Dd, npx * 16, st, dd);
   if (r == RMN_OK) r = finish_out(image->radiance_Ds, npx * 16, st, ds);
   if (r == RMN_OK) r = finish_out(image->radiance_Id, npx * 16, st, id);
   if (r == RMN_OK) r = finish_out(image->radiance_Is, npx * 16, st, is);
   if (r == RMN_OK && image->gbuffer) r = finish_out(image->gbuffer, npx * RMN_GBUFFER_FLOATS * 4, st, gb);
-  rmn_status r2 = status.dev ? status.check(st, "rmn_render") : RMN_OK;
+  if (r == RMN_OK && b) r = batch_status(b, st);
   for (Arg* x : {&dd, &ds, &id, &is, &gb}) release(*x, st);
-  status.free(st);
   cudaError_t e = cudaStreamSynchronize(st);
-  if (r == RMN_OK) r = r2;
+  batch_destroy(b);
   if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
   return r;
 }
+
+extern "C" {
+
+rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, const rmn_image* image, void* stream) {
+  return render_one(scene, args, image, stream, nullptr);
+}
+
+static void put_profile(const RenderProfileData& p, rmn_render_profile* out) {
+  out->primary_ms = p.primary_ms;
+  out->path_ms = p.path_ms;
+  out->closest_rays = p.closest;
+  out->shadow_rays = p.shadow;
+  out->inner_visits = p.inner;
+  out->leaf_visits = p.leaves;
+  out->triangle_tests = p.tris;
+  out->sample_slots = p.slots;
+  out->pixels = p.pixels;
+}
+
+rmn_status rmn_render_profile_get(rmn_scene* scene, const rmn_render_args* args, const rmn_image* image,
+                                  rmn_render_profile* out, void* stream) {
+  if (!out) return fail(RMN_ERR_INVALID_ARGUMENT, "out is NULL");
+  RenderProfileData p{};
+  rmn_status r = render_one(scene, args, image, stream, &p);
+  if (r == RMN_OK) put_profile(p, out);
+  return r;
+}
+
+struct rmn_batch {
+  BatchState* state = nullptr;
+};
+
+rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, int32_t use_graph, void* stream, rmn_batch** out) {
+  clear_error();
+  if (!items || n <= 0 || !out) return fail(RMN_ERR_INVALID_ARGUMENT, "a batch needs at least one item");
+  *out = nullptr;
+  std::vector<RenderItem> its;
+  its.reserve(n);
+  int64_t total = 0;
+  for (int i = 0; i < n; ++i) {
+    const rmn_batch_item& b = items[i];
+    if (!b.scene) return fail(RMN_ERR_INVALID_ARGUMENT, "batch item %d has no scene", i);
+    rmn_status r = check_args(b.args);
+    if (r != RMN_OK) return fail(r, "batch item %d: %s", i, rmn_last_error());
+    if (b.scene->dev.num_lights > 8) return fail(RMN_ERR_UNSUPPORTED, "batch item %d: more than 8 light objects", i);
+    const rmn_image& im = b.image;
+    for (const void* p : {(const void*)im.radiance_Dd, (const void*)im.radiance_Ds, (const void*)im.radiance_Id,
+                          (const void*)im.radiance_Is, (const void*)im.gbuffer})
+      if (!is_device_ptr(p))
+        return fail(RMN_ERR_INVALID_ARGUMENT, "batch item %d: batch buffers (all five) must be device memory", i);
+    total += (int64_t)b.args.width * b.args.height;
+    if (total > (1LL << 31) - 1) return fail(RMN_ERR_INVALID_ARGUMENT, "a batch holds at most 2^31 - 1 pixels");
+    its.push_back(RenderItem{b.scene, b.args, im.gbuffer, im.radiance_Dd, im.radiance_Ds, im.radiance_Id,
+                             im.radiance_Is});
+  }
+  rmn_batch* bt = new (std::nothrow) rmn_batch();
+  if (!bt) return fail(RMN_ERR_OUT_OF_MEMORY, "host allocation failed");
+  rmn_status r = batch_create(its.data(), n, use_graph != 0, static_cast<cudaStream_t>(stream), &bt->state);
+  if (r != RMN_OK) {
+    delete bt;
+    return r;
+  }
+  *out = bt;
+  return RMN_OK;
+}
+
+rmn_status rmn_batch_render(rmn_batch* batch, void* stream) {
+  clear_error();
+  if (!batch || !batch->state) return fail(RMN_ERR_INVALID_ARGUMENT, "NULL batch");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rmn_status r = batch_launch(batch->state, st);
+  if (r == RMN_OK) r = batch_status(batch->state, st);
+  return r;
+}
+
+rmn_status rmn_batch_profile(rmn_batch* batch, rmn_render_profile* out, void* stream) {
+  clear_error();
+  if (!batch || !batch->state || !out) return fail(RMN_ERR_INVALID_ARGUMENT, "NULL batch or output");
+  RenderProfileData p{};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  rmn_status r = batch_profile(batch->state, st, &p);
+  if (r == RMN_OK) r = batch_status(batch->state, st);
+  if (r == RMN_OK) put_profile(p, out);
+  return r;
+}
+
+rmn_status rmn_batch_destroy(rmn_batch* batch) {
+  clear_error();
+  if (!batch) return RMN_OK;
+  batch_destroy(batch->state);
+  delete batch;
+  return RMN_OK;
+}
+
+}  // extern "C"

@@ -21,6 +21,9 @@
 //     each lane keeps its sums without its largest sample plus that sample's
 //     contribution, and the reduction merges these pairs; the surviving
 //     largest sample is dropped or added at the end. No per-sample storage.
+#include <algorithm>
+#include <vector>
+
 #include "rmn_host.h"
 #include "shade.cuh"
 
@@ -33,6 +36,33 @@ struct Params {
   int tasks;
   uint64_t seed;
 };
+
+// One render of a batch: a scene, its arguments, its output buffers and its
+// place in the batch's pixel and task numbering.
+struct Job {
+  DevScene s;
+  Params p;
+  float* gbuf;
+  float4 *dd, *ds, *id, *is;
+  int pix_begin;   // first pixel of this job in the batch's pixel numbering
+  int task_begin;  // first path task (group of 32/K pixels) of this job
+};
+
+// Batch-wide counters of the counting build.
+struct Counters {
+  unsigned long long closest, shadow, inner, leaves, tris, slots;
+};
+
+__device__ __forceinline__ int find_job(const Job* jobs, int n, int v, bool by_task) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    int b = by_task ? __ldg(&jobs[mid].task_begin) : __ldg(&jobs[mid].pix_begin);
+    if (b <= v) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
 
 // renderPixel's demodulation tweak, src/render.cpp:492-495: a faint red is
 // added to black or grey base colours (double-precision literals as there).
@@ -63,16 +93,23 @@ __device__ __forceinline__ Surf default_surf() {
 // shapeN[3] surfN[3] roughness metallic opacity eta material-id. The base
 // colour is stored untweaked; path_kernel applies renderPixel's tweak for its
 // own use and writes the tweaked colour back where the reference leaves it.
-__global__ void __launch_bounds__(128) primary_kernel(DevScene s, Params p, float* __restrict__ gbuf, int* status) {
-  int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.W * p.H) return;
+template <bool COUNT>
+__global__ void __launch_bounds__(128) primary_kernel(const Job* __restrict__ jobs, int njobs, int total_pix,
+                                                      int* status, Counters* ctr) {
+  int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= total_pix) return;
+  const Job& J = jobs[find_job(jobs, njobs, gi, false)];
+  const DevScene& s = J.s;
+  const Params& p = J.p;
+  int i = gi - J.pix_begin;
   int x = i % p.W, y = i / p.W;
   float rx = float(x) - float(p.W) / 2.0f, ry = float(y) - float(p.H) / 2.0f;
   float3 d = p.dir + p.acc * (rx * p.right + ry * p.up);
   float3 D = norm3(d);
   TRay r = make_tray(p.pos, D);
   float tmax = INFINITY;
-  int h = trace<false, false>(s, r, RMN_EPS, tmax, 0.0f, nullptr);
+  TraceCounters tc = {0, 0, 0, 0, 0};
+  int h = trace<false, COUNT>(s, r, RMN_EPS, tmax, 0.0f, &tc);
   if (h == -2) atomicExch(status, 1);
   Surf g = default_surf();
   if (h < 0) {
@@ -81,12 +118,18 @@ __global__ void __launch_bounds__(128) primary_kernel(DevScene s, Params p, floa
     g.pos = p.pos + tmax * D;
     hit_info(s, h, D, g);
   }
-  float* o = gbuf + (size_t)RMN_GBUFFER_FLOATS * i;
+  float* o = J.gbuf + (size_t)RMN_GBUFFER_FLOATS * i;
   float v[RMN_GBUFFER_FLOATS] = {g.base.x, g.base.y, g.base.z, g.emis.x, g.emis.y, g.emis.z, g.pos.x,
                                  g.pos.y, g.pos.z, g.shapeN.x, g.shapeN.y, g.shapeN.z, g.surfN.x, g.surfN.y,
                                  g.surfN.z, g.roughness, g.metallic, g.opacity, g.eta, (float)g.id};
 #pragma unroll
   for (int k = 0; k < RMN_GBUFFER_FLOATS; ++k) o[k] = v[k];
+  if (COUNT) {
+    atomicAdd(&ctr->closest, (unsigned long long)tc.closest);
+    atomicAdd(&ctr->inner, (unsigned long long)tc.inner);
+    atomicAdd(&ctr->leaves, (unsigned long long)tc.leaves);
+    atomicAdd(&ctr->tris, (unsigned long long)tc.tris);
+  }
 }
 
 struct Rad4 {
@@ -174,8 +217,9 @@ __device__ __forceinline__ void emit(Acc& a, const PathCtx& c, const LSample& ls
 
 // One indirect sample from the first vertex (sampleIndirectLightFrom-
 // FirstIntersection + the sampleRay recursion) for an opaque first vertex.
+template <bool COUNT>
 __device__ void indirect_path(const DevScene& s, const Params& p, const Surf& g, RmnRng& rng, Acc& a, float inv_spp,
-                              int* status) {
+                              int* status, TraceCounters* tc) {
   if (len3(g.emis) > 0.0f) return;
   float3 in = norm3(g.pos - p.pos);
   Surf v0 = g;
@@ -196,7 +240,7 @@ __device__ void indirect_path(const DevScene& s, const Params& p, const Surf& g,
   for (int depth = 1;; ++depth) {
     TRay r = make_tray(o, dir);
     float tmax = INFINITY;
-    int h = trace<false, false>(s, r, RMN_EPS, tmax, 0.0f, nullptr);
+    int h = trace<false, COUNT>(s, r, RMN_EPS, tmax, 0.0f, tc);
     if (h == -2) {
       atomicExch(status, 1);
       return;
@@ -228,7 +272,7 @@ __device__ void indirect_path(const DevScene& s, const Params& p, const Surf& g,
       if (s.sky_w == 0 && !light_weights(s, sf, V, lw, tot)) return;
       for (int T = 0; T < cnt; ++T) {
         LSample ls;
-        if (light_sample(s, sf, V, lw, tot, cnt, rng, ls, status)) {
+        if (light_sample<COUNT>(s, sf, V, lw, tot, cnt, rng, ls, status, tc)) {
           ls.bsdf *= k;
           emit(a, c, ls);
         }
@@ -261,20 +305,24 @@ __device__ __forceinline__ void calc_var(Rad4& r, float e) {  // renderPixel's c
   if (r.v < 0.0f) r.v = 0.0f;
 }
 
-__global__ void __launch_bounds__(128) path_kernel(DevScene s, Params p, float* __restrict__ gbuf,
-                                                   float4* __restrict__ Dd, float4* __restrict__ Ds,
-                                                   float4* __restrict__ Id, float4* __restrict__ Is,
-                                                   unsigned int* __restrict__ next, int* status) {
+template <bool COUNT>
+__global__ void __launch_bounds__(128) path_kernel(const Job* __restrict__ jobs, int njobs, int total_tasks,
+                                                   unsigned int* __restrict__ next, int* status, Counters* ctr) {
   const int lane = threadIdx.x & 31;
-  const int K = p.K, P = 32 / K;
-  const int sub = lane % K, grp = lane / K;
-  const int npix = p.W * p.H;
+  TraceCounters tc = {0, 0, 0, 0, 0};
+  unsigned long long slots_done = 0;
   for (;;) {
     unsigned int task = 0;
     if (lane == 0) task = atomicAdd(next, 1u);
     task = __shfl_sync(0xffffffffu, task, 0);
-    if (task >= (unsigned)p.tasks) return;
-    const int pixel = (int)task * P + grp;
+    if (task >= (unsigned)total_tasks) break;
+    const Job& J = jobs[find_job(jobs, njobs, (int)task, true)];
+    const DevScene& s = J.s;
+    const Params& p = J.p;
+    const int K = p.K, P = 32 / K;
+    const int sub = lane % K, grp = lane / K;
+    const int npix = p.W * p.H;
+    const int pixel = ((int)task - J.task_begin) * P + grp;
     const bool valid = pixel < npix;
     Acc a;
     a.dd = a.ds = a.id = a.is = a.mid = a.mis = rad0();
@@ -284,7 +332,7 @@ __global__ void __launch_bounds__(128) path_kernel(DevScene s, Params p, float* 
     bool hit = false;
     Surf g = default_surf();
     if (valid) {
-      const float* gb = gbuf + (size_t)RMN_GBUFFER_FLOATS * pixel;
+      const float* gb = J.gbuf + (size_t)RMN_GBUFFER_FLOATS * pixel;
       g.base = f3(gb[0], gb[1], gb[2]);
       g.emis = f3(gb[3], gb[4], gb[5]);
       g.pos = f3(gb[6], gb[7], gb[8]);
@@ -310,6 +358,7 @@ __global__ void __launch_bounds__(128) path_kernel(DevScene s, Params p, float* 
       bool have_w = false, w_done = false;
       for (int j = sub; j < slots; j += K) {
         RmnRng rng = rmn_rng(p.seed, (uint32_t)pixel, (uint32_t)j);
+        if (COUNT) slots_done++;
         if (j < spp_d) {
           if (!direct_ok) continue;
           if (!w_done) {
@@ -318,14 +367,14 @@ __global__ void __launch_bounds__(128) path_kernel(DevScene s, Params p, float* 
           }
           if (!have_w) continue;
           LSample ls;
-          if (light_sample(s, g, Vd, lw, tot, spp_d, rng, ls, status)) {
+          if (light_sample<COUNT>(s, g, Vd, lw, tot, spp_d, rng, ls, status, &tc)) {
             Rad4 d, sp;
             demodulate(g.base, ls.bsdf, ls.light, ls.weight, d, sp);
             radd(a.dd, d);
             radd(a.ds, sp);
           }
         } else {
-          indirect_path(s, p, g, rng, a, inv_spp, status);
+          indirect_path<COUNT>(s, p, g, rng, a, inv_spp, status, &tc);
         }
       }
     }
@@ -367,37 +416,67 @@ __global__ void __launch_bounds__(128) path_kernel(DevScene s, Params p, float* 
           // renderPixel restores the untweaked base colour only after
           // accumulating indirect samples; with none it returns early
           // (src/render.cpp:517-518) and the tweak stays in the G-buffer.
-          float* gb = gbuf + (size_t)RMN_GBUFFER_FLOATS * pixel;
-          gb[0] = g.base.x;
+          J.gbuf[(size_t)RMN_GBUFFER_FLOATS * pixel] = g.base.x;
         }
       }
-      Dd[pixel] = make_float4(a.dd.c.x, a.dd.c.y, a.dd.c.z, a.dd.v);
-      Ds[pixel] = make_float4(a.ds.c.x, a.ds.c.y, a.ds.c.z, a.ds.v);
-      Id[pixel] = make_float4(a.id.c.x, a.id.c.y, a.id.c.z, a.id.v);
-      Is[pixel] = make_float4(a.is.c.x, a.is.c.y, a.is.c.z, a.is.v);
+      J.dd[pixel] = make_float4(a.dd.c.x, a.dd.c.y, a.dd.c.z, a.dd.v);
+      J.ds[pixel] = make_float4(a.ds.c.x, a.ds.c.y, a.ds.c.z, a.ds.v);
+      J.id[pixel] = make_float4(a.id.c.x, a.id.c.y, a.id.c.z, a.id.v);
+      J.is[pixel] = make_float4(a.is.c.x, a.is.c.y, a.is.c.z, a.is.v);
     }
+  }
+  if (COUNT) {
+    atomicAdd(&ctr->closest, (unsigned long long)tc.closest);
+    atomicAdd(&ctr->shadow, (unsigned long long)tc.shadow);
+    atomicAdd(&ctr->inner, (unsigned long long)tc.inner);
+    atomicAdd(&ctr->leaves, (unsigned long long)tc.leaves);
+    atomicAdd(&ctr->tris, (unsigned long long)tc.tris);
+    atomicAdd(&ctr->slots, slots_done);
   }
 }
 
-int sm_count() {
+int device_sms() {
   int dev = 0, sms = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   return sms;
 }
 
+int path_blocks_per_sm() {
+  int per_sm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, path_kernel<false>, 128, 0);
+  return per_sm < 1 ? 1 : per_sm;
+}
+
 }  // namespace
 
 namespace rmn {
 
-int default_lanes_per_pixel(int spp) {
+// Lanes per pixel: the fewest (each lane then owns more of the pixel's
+// sample slots, which balances the warp and amortises per-pixel set-up) that
+// still yield about four waves of warps over the whole batch.
+int default_lanes_per_pixel(int64_t batch_pixels, int spp) {
+  const int64_t resident_warps = (int64_t)device_sms() * path_blocks_per_sm() * 4;
   int k = 1;
-  while (k * 2 <= 32 && k * 2 * 4 <= spp) k *= 2;
+  while (k < 32 && k * 2 <= (spp > 0 ? spp : 1) && batch_pixels * k / 32 < 4 * resident_warps) k *= 2;
   return k;
 }
 
-cudaError_t launch_render(const DevScene& s, const rmn_render_args& a, float* gbuf, float* dd, float* ds, float* id,
-                          float* is, int* status, cudaStream_t stream) {
+struct JobTable {
+  std::vector<Job> jobs;
+  int total_pix = 0, total_tasks = 0;
+};
+
+struct BatchState {
+  JobTable table;
+  Job* d_jobs = nullptr;
+  unsigned int* d_next = nullptr;
+  int* d_status = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+static Params make_params(const rmn_render_args& a, int K) {
   Params p;
   p.pos = f3(a.position[0], a.position[1], a.position[2]);
   p.dir = f3(a.direction[0], a.direction[1], a.direction[2]);
@@ -411,31 +490,168 @@ cudaError_t launch_render(const DevScene& s, const rmn_render_args& a, float* gb
   p.spp = a.spp;
   p.maxd = a.max_depth;
   p.spp_d = (int)((float)a.spp * a.P_Direct);  // renderPixel, src/render.cpp:497
-  p.K = a.lanes_per_pixel > 0 ? a.lanes_per_pixel : default_lanes_per_pixel(a.spp);
+  p.K = K;
   p.seed = a.seed;
   const int npix = p.W * p.H;
-  p.tasks = (npix + (32 / p.K) - 1) / (32 / p.K);
-  primary_kernel<<<(npix + 127) / 128, 128, 0, stream>>>(s, p, gbuf, status);
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return e;
-  unsigned int* next = nullptr;
-  e = cudaMallocAsync(&next, sizeof(unsigned int), stream);
-  if (e != cudaSuccess) return e;
-  e = cudaMemsetAsync(next, 0, sizeof(unsigned int), stream);
-  if (e == cudaSuccess) {
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, path_kernel, 128, 0);
-    if (per_sm < 1) per_sm = 1;
-    int blocks = sm_count() * per_sm;
-    int need = (p.tasks + 3) / 4;
-    if (need < blocks) blocks = need;
-    path_kernel<<<blocks, 128, 0, stream>>>(s, p, gbuf, reinterpret_cast<float4*>(dd), reinterpret_cast<float4*>(ds),
-                                             reinterpret_cast<float4*>(id), reinterpret_cast<float4*>(is), next,
-                                             status);
-    e = cudaGetLastError();
+  p.tasks = (npix + (32 / K) - 1) / (32 / K);
+  return p;
+}
+
+// Jobs ordered by decreasing cost per task (spp x depth), so the persistent
+// warps finish on the cheap tasks; the result does not depend on the order.
+static void build_jobs(const RenderItem* items, int n, JobTable* t) {
+  int64_t batch_pixels = 0;
+  for (int i = 0; i < n; ++i) batch_pixels += (int64_t)items[i].args.width * items[i].args.height;
+  std::vector<int> order(n);
+  for (int i = 0; i < n; ++i) order[i] = i;
+  auto cost = [&](int i) {
+    const rmn_render_args& a = items[i].args;
+    int K = a.lanes_per_pixel > 0 ? a.lanes_per_pixel : default_lanes_per_pixel(batch_pixels, a.spp);
+    return (double)a.spp * a.max_depth * (32 / K);
+  };
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+  t->jobs.clear();
+  t->total_pix = t->total_tasks = 0;
+  for (int i : order) {
+    const RenderItem& it = items[i];
+    int K = it.args.lanes_per_pixel > 0 ? it.args.lanes_per_pixel : default_lanes_per_pixel(batch_pixels, it.args.spp);
+    Job j;
+    j.s = it.scene->dev;
+    j.p = make_params(it.args, K);
+    j.gbuf = it.gbuf;
+    j.dd = reinterpret_cast<float4*>(it.dd);
+    j.ds = reinterpret_cast<float4*>(it.ds);
+    j.id = reinterpret_cast<float4*>(it.id);
+    j.is = reinterpret_cast<float4*>(it.is);
+    j.pix_begin = t->total_pix;
+    j.task_begin = t->total_tasks;
+    t->total_pix += j.p.W * j.p.H;
+    t->total_tasks += j.p.tasks;
+    t->jobs.push_back(j);
   }
-  cudaError_t f = cudaFreeAsync(next, stream);
-  return e != cudaSuccess ? e : f;
+}
+
+// Launch sequence of a batch: reset the task counter, primary kernel over
+// every pixel of every job, then the persistent path kernel. With `ctr`
+// the counting build runs (same images, plus visit counters).
+static cudaError_t launch_jobs(const void* d_jobs, int njobs, int total_pix, int total_tasks, unsigned int* d_next,
+                        int* d_status, void* d_ctr, cudaStream_t stream, cudaEvent_t* ev) {
+  const Job* jobs = static_cast<const Job*>(d_jobs);
+  Counters* ctr = static_cast<Counters*>(d_ctr);
+  cudaError_t e = cudaMemsetAsync(d_next, 0, sizeof(unsigned int), stream);
+  if (e != cudaSuccess) return e;
+  if (ev) cudaEventRecord(ev[0], stream);
+  if (ctr) primary_kernel<true><<<(total_pix + 127) / 128, 128, 0, stream>>>(jobs, njobs, total_pix, d_status, ctr);
+  else primary_kernel<false><<<(total_pix + 127) / 128, 128, 0, stream>>>(jobs, njobs, total_pix, d_status, ctr);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ev) cudaEventRecord(ev[1], stream);
+  int blocks = device_sms() * path_blocks_per_sm();
+  int need = (total_tasks + 3) / 4;
+  if (need < blocks) blocks = need < 1 ? 1 : need;
+  if (ctr) path_kernel<true><<<blocks, 128, 0, stream>>>(jobs, njobs, total_tasks, d_next, d_status, ctr);
+  else path_kernel<false><<<blocks, 128, 0, stream>>>(jobs, njobs, total_tasks, d_next, d_status, ctr);
+  if ((e = cudaGetLastError()) != cudaSuccess) return e;
+  if (ev) cudaEventRecord(ev[2], stream);
+  return cudaSuccess;
+}
+
+rmn_status batch_create(const RenderItem* items, int n, bool use_graph, cudaStream_t st, BatchState** out) {
+  *out = nullptr;
+  BatchState* b = new BatchState();
+  build_jobs(items, n, &b->table);
+  const size_t jb = sizeof(Job) * b->table.jobs.size();
+  cudaError_t e = cudaMalloc(&b->d_jobs, jb);
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_next, sizeof(unsigned int));
+  if (e == cudaSuccess) e = cudaMalloc(&b->d_status, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemcpy(b->d_jobs, b->table.jobs.data(), jb, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(b->d_status, 0, sizeof(int));
+  if (e == cudaSuccess && use_graph) {
+    cudaStream_t cs;
+    e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (e == cudaSuccess) {
+      e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t le = launch_jobs(b->d_jobs, (int)b->table.jobs.size(), b->table.total_pix, b->table.total_tasks,
+                                     b->d_next, b->d_status, nullptr, cs, nullptr);
+        e = cudaStreamEndCapture(cs, &b->graph);
+        if (e == cudaSuccess) e = le;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+      cudaStreamDestroy(cs);
+    }
+  }
+  if (e != cudaSuccess) {
+    batch_destroy(b);
+    return cuda_fail(e, "batch setup");
+  }
+  (void)st;
+  *out = b;
+  return RMN_OK;
+}
+
+rmn_status batch_launch(BatchState* b, cudaStream_t st) {
+  cudaError_t e;
+  if (b->exec) e = cudaGraphLaunch(b->exec, st);
+  else
+    e = launch_jobs(b->d_jobs, (int)b->table.jobs.size(), b->table.total_pix, b->table.total_tasks, b->d_next,
+                    b->d_status, nullptr, st, nullptr);
+  return e == cudaSuccess ? RMN_OK : cuda_fail(e, "batch launch");
+}
+
+rmn_status batch_status(BatchState* b, cudaStream_t st) {
+  int h = 0;
+  cudaError_t e = cudaMemcpyAsync(&h, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return cuda_fail(e, "render");
+  if (h) return fail(RMN_ERR_DEVICE_LIMIT, "render: traversal stack bound reached");
+  return RMN_OK;
+}
+
+// Counting run (visit counters) followed by a timed run with CUDA events
+// around each kernel on `st`. Both produce the same images as batch_launch.
+rmn_status batch_profile(BatchState* b, cudaStream_t st, RenderProfileData* prof) {
+  Counters* d_ctr = nullptr;
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
+  cudaError_t e = cudaMalloc(&d_ctr, sizeof(Counters));
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, sizeof(Counters), st);
+  for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventCreate(&ev[k]);
+  const int nj = (int)b->table.jobs.size();
+  if (e == cudaSuccess)
+    e = launch_jobs(b->d_jobs, nj, b->table.total_pix, b->table.total_tasks, b->d_next, b->d_status, d_ctr, st,
+                    nullptr);
+  if (e == cudaSuccess)
+    e = launch_jobs(b->d_jobs, nj, b->table.total_pix, b->table.total_tasks, b->d_next, b->d_status, nullptr, st, ev);
+  Counters h{};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) {
+    float a = 0.0f, c = 0.0f;
+    cudaEventElapsedTime(&a, ev[0], ev[1]);
+    cudaEventElapsedTime(&c, ev[1], ev[2]);
+    prof->primary_ms = a;
+    prof->path_ms = c;
+    prof->closest = h.closest;
+    prof->shadow = h.shadow;
+    prof->inner = h.inner;
+    prof->leaves = h.leaves;
+    prof->tris = h.tris;
+    prof->slots = h.slots;
+    prof->pixels = (unsigned long long)b->table.total_pix;
+  }
+  for (int k = 0; k < 3; ++k)
+    if (ev[k]) cudaEventDestroy(ev[k]);
+  if (d_ctr) cudaFree(d_ctr);
+  return e == cudaSuccess ? RMN_OK : cuda_fail(e, "render profile");
+}
+
+void batch_destroy(BatchState* b) {
+  if (!b) return;
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  if (b->graph) cudaGraphDestroy(b->graph);
+  if (b->d_jobs) cudaFree(b->d_jobs);
+  if (b->d_next) cudaFree(b->d_next);
+  if (b->d_status) cudaFree(b->d_status);
+  delete b;
 }
 
 }  // namespace rmn

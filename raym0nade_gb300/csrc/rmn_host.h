@@ -37,9 +37,23 @@ cudaError_t launch_trace_closest(const DevScene& s, const rmn_ray* rays, int64_t
                                  cudaStream_t stream);
 cudaError_t launch_trace_shadow(const DevScene& s, const rmn_ray* rays, int64_t n, uint8_t* occluded, int* status,
                                 cudaStream_t stream);
-int default_lanes_per_pixel(int spp);
-cudaError_t launch_render(const DevScene& s, const rmn_render_args& a, float* gbuf, float* dd, float* ds, float* id,
-                          float* is, int* status, cudaStream_t stream);
+// One render of a batch; all pointers are device memory.
+struct RenderItem {
+  const rmn_scene* scene;
+  rmn_render_args args;
+  float *gbuf, *dd, *ds, *id, *is;
+};
+struct RenderProfileData {
+  double primary_ms, path_ms;
+  unsigned long long closest, shadow, inner, leaves, tris, slots, pixels;
+};
+struct BatchState;
+int default_lanes_per_pixel(int64_t batch_pixels, int spp);
+rmn_status batch_create(const RenderItem* items, int n, bool use_graph, cudaStream_t st, BatchState** out);
+rmn_status batch_launch(BatchState* b, cudaStream_t st);
+rmn_status batch_status(BatchState* b, cudaStream_t st);
+rmn_status batch_profile(BatchState* b, cudaStream_t st, RenderProfileData* prof);
+void batch_destroy(BatchState* b);
 cudaError_t launch_fxaa(const float* in, float* out, int w, int h, cudaStream_t stream);
 cudaError_t launch_compose(const float* dd, const float* ds, const float* id, const float* is, const float* gbuf,
                            int w, int h, float exposure, int options, float* rgb, cudaStream_t stream);

@@ -280,8 +280,9 @@ RMN_D bool light_weights(const DevScene& s, const Surf& sf, float3 V, float* w, 
   return tot != 0.0f;
 }
 
+template <bool COUNT>
 RMN_D bool light_sample(const DevScene& s, const Surf& sf, float3 V, const float* w, float tot, int cnt, RmnRng& rng,
-                        LSample& out, int* status) {
+                        LSample& out, int* status, TraceCounters* tc) {
   const float3 pos = sf.pos;
   if (s.sky_w == 0) {
     float rv = tot * rng.next();  // sample(), :396-404
@@ -326,7 +327,7 @@ RMN_D bool light_sample(const DevScene& s, const Surf& sf, float3 V, const float
     TRay r = make_tray(pos, ld);
     float aim = dist - RMN_EPS;
     float tmax = aim + RMN_EPS;
-    int h = trace<true, false>(s, r, RMN_EPS, tmax, aim, nullptr);
+    int h = trace<true, COUNT>(s, r, RMN_EPS, tmax, aim, tc);
     if (h == -2) atomicExch(status, 1);
     if (!(tmax >= aim)) return false;
     float3 f = brdf(sf, V, ld);
@@ -354,7 +355,7 @@ RMN_D bool light_sample(const DevScene& s, const Surf& sf, float3 V, const float
       float3 light = f3(__ldg(s.sky + p)) / pdf;
       TRay r = make_tray(pos, dir);
       float tmax = INFINITY;
-      int h = trace<true, false>(s, r, RMN_EPS, tmax, INFINITY, nullptr);
+      int h = trace<true, COUNT>(s, r, RMN_EPS, tmax, INFINITY, tc);
       if (h == -2) atomicExch(status, 1);
       if (!(tmax >= INFINITY)) return false;
       float3 f = brdf(sf, V, dir);

@@ -76,8 +76,9 @@ RMN_D float tri_t(const TRay& r, float3 v0, float3 e1, float3 e2, float len_e1) 
   return f * dot3(e2, q);
 }
 
+// Per-thread visit counters of the counting build (rmn_render_profile).
 struct TraceCounters {
-  uint32_t inner, leaves, tris;
+  uint32_t closest, shadow, inner, leaves, tris;
 };
 
 // Closest hit in (tmin, tmax). Returns the leaf-order triangle index or -1;
@@ -92,6 +93,10 @@ RMN_D int trace(const DevScene& s, const TRay& r, float tmin, float& tmax, float
   float stack_tl[RMN_STACK];
   int sp = 0;
   int cur = s.root;
+  if (COUNT) {
+    if (ANY) cnt->shadow++;
+    else cnt->closest++;
+  }
   for (;;) {
     if (cur >= 0) {
       const DevNode* n = s.nodes + cur;

@@ -362,3 +362,45 @@ def heightfield_camera(width=1920, height=1080, spp=256, extent=200.0) -> Camera
     up_img /= np.linalg.norm(up_img)
     acc = math.tan(math.radians(30.0)) / (width / 2.0)
     return Camera(tuple(eye), tuple(f), tuple(up_img), tuple(r), acc, width, height, spp, max_depth=16)
+
+
+@dataclass
+class Instance:
+    scene: Scene
+    camera: Camera
+    seed: int
+
+
+def soup_camera(width, height, spp, max_depth) -> Camera:
+    """Outside the unit cube, looking at its centre along +z; 45 degree view."""
+    acc = math.tan(math.radians(22.5)) / (width / 2.0)
+    return Camera((0.5, 0.5, -1.2), (0.0, 0.0, 1.0), (0.0, -1.0, 0.0), (-1.0, 0.0, 0.0), acc, width, height, spp,
+                  max_depth=max_depth)
+
+
+def batch_instances(count: int = 64, seed: int = 7, env_width: int = 1024, env_height: int = 512,
+                    max_tris: int = 2_000_000) -> list:
+    """The batching workload: ``count`` scene instances, each chosen by seed
+    as a random soup or a heightfield with log-uniform triangle count in
+    [1e3, max_tris], a square image of side U[128, 1024], spp log-uniform in
+    [16, 256] and max depth U{4..16}, all lit by the synthetic sky."""
+    out = []
+    env = sky_env(env_width, env_height)
+    for i in range(count):
+        rng = np.random.default_rng(seed * 100003 + i)
+        ntris = int(math.exp(rng.uniform(math.log(1e3), math.log(max_tris))))
+        side = int(rng.uniform(128, 1025))
+        spp = int(round(math.exp(rng.uniform(math.log(16), math.log(256)))))
+        depth = int(rng.integers(4, 17))
+        if rng.random() < 0.5:
+            s = random_soup(ntris, seed=int(rng.integers(1 << 30)))
+            cam = soup_camera(side, side, spp, depth)
+        else:
+            n = max(3, int(round(math.sqrt(ntris / 2.0))) + 1)
+            s = heightfield(n, seed=int(rng.integers(1 << 30)), extent=200.0, patch=64)
+            c = heightfield_camera(side, side, spp, extent=200.0)
+            c.max_depth = depth
+            cam = c
+        s.env = env
+        out.append(Instance(s, cam, seed * 1000 + i))
+    return out
