@@ -295,10 +295,19 @@ def run_gpu(args, rank, world, dist):
     if rank != 0:
         return
     peak, peak_src = measured_peaks()
-    alg_bytes = 64 * prof["inner_visits"] + 36 * prof["triangle_tests"] + npx * (20 * 4 + 16 * 4)
-    path_share = prof["path_ms"] / max(1e-9, prof["path_ms"] + prof["primary_ms"])
-    path_ms_live = ms_b * path_share
-    achieved = alg_bytes / (path_ms_live / 1e3) / 1e9
+    # Dominant kernel: the wavefront's traversal (closest + shadow queues).
+    # Its algorithmic bytes: 64 B per inner-node visit (two child boxes),
+    # 36 B per triangle test, 32 B ray in + 8 B answer out per ray. The
+    # G-buffer kernel's primary rays are counted in the visits but not in
+    # trace_ms, so they are taken out in proportion to their rays.
+    rays = prof["closest_rays"] + prof["shadow_rays"]
+    queued = max(1, rays - npx)
+    alg_bytes = (64 * prof["inner_visits"] + 36 * prof["triangle_tests"]) * queued / max(1, rays) + 40 * queued
+    total_ms = prof["primary_ms"] + prof["path_ms"]
+    trace_share = prof["trace_ms"] / max(1e-9, total_ms)
+    logic_share = prof["logic_ms"] / max(1e-9, total_ms)
+    trace_ms_live = ms_b * trace_share
+    achieved = alg_bytes / (trace_ms_live / 1e3) / 1e9
     base, _, _ = cpu_baseline(insts) if args.cpu_baseline else (None, None, None)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -316,11 +325,11 @@ def run_gpu(args, rank, world, dist):
                 "call": "rmn_render into pinned host buffers + rmn_compose(Full|gamma|FXAA) to a host image, per instance"},
         "gpu_launches": 2 * args.steps,
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "path_kernel", "peak_source": peak_src,
-                     "bytes_model": "64 B per inner-node visit + 36 B per triangle test + 144 B per pixel",
-                     "algorithmic_bytes_per_launch": alg_bytes, "path_kernel_share": path_share},
-        "rays": {"closest": prof["closest_rays"], "shadow": prof["shadow_rays"],
-                 "Mrays_s": (prof["closest_rays"] + prof["shadow_rays"]) / (path_ms_live + ms_b * (1 - path_share)) / 1e3},
+                     "traffic": None, "kernel": "qtrace_kernel (closest + shadow queues)", "peak_source": peak_src,
+                     "bytes_model": "64 B per inner-node visit + 36 B per triangle test + 40 B per queued ray",
+                     "algorithmic_bytes_per_step": alg_bytes, "trace_share": trace_share,
+                     "logic_share": logic_share, "iterations": prof["iterations"]},
+        "rays": {"closest": prof["closest_rays"], "shadow": prof["shadow_rays"], "Mrays_s": rays / ms_b / 1e3},
         "clocks": clocks,
     }
     if base:

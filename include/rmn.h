@@ -174,10 +174,13 @@ rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, const rmn_i
 
 /* Visit counters and kernel times of one render: rmn_render run twice on
  * the same arguments -- once with counting traversal, once with CUDA events
- * around the two kernels -- leaving the same images. For roofline figures
+ * around every kernel -- leaving the same images. For roofline figures
  * (bytes per ray) and ray throughput; not needed to render. */
 typedef struct rmn_render_profile {
-  double primary_ms, path_ms;   /* G-buffer kernel, path kernel */
+  double primary_ms;            /* set-up + G-buffer kernel */
+  double path_ms;               /* wavefront iterations + finalize */
+  double logic_ms, trace_ms;    /* summed over iterations: shading/sampling kernel, the two traversal kernels */
+  int64_t iterations;
   uint64_t closest_rays, shadow_rays;
   uint64_t inner_visits, leaf_visits, triangle_tests;
   uint64_t sample_slots, pixels;

@@ -48,7 +48,8 @@ class Image(C.Structure):
 
 
 class RenderProfile(C.Structure):
-    _fields_ = [("primary_ms", C.c_double), ("path_ms", C.c_double), ("closest_rays", C.c_uint64),
+    _fields_ = [("primary_ms", C.c_double), ("path_ms", C.c_double), ("logic_ms", C.c_double),
+                ("trace_ms", C.c_double), ("iterations", C.c_int64), ("closest_rays", C.c_uint64),
                 ("shadow_rays", C.c_uint64), ("inner_visits", C.c_uint64), ("leaf_visits", C.c_uint64),
                 ("triangle_tests", C.c_uint64), ("sample_slots", C.c_uint64), ("pixels", C.c_uint64)]
 

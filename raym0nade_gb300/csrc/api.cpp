@@ -322,6 +322,9 @@ rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, const rmn_i
 static void put_profile(const RenderProfileData& p, rmn_render_profile* out) {
   out->primary_ms = p.primary_ms;
   out->path_ms = p.path_ms;
+  out->logic_ms = p.logic_ms;
+  out->trace_ms = p.trace_ms;
+  out->iterations = p.iterations;
   out->closest_rays = p.closest;
   out->shadow_rays = p.shadow;
   out->inner_visits = p.inner;

@@ -1,27 +1,41 @@
 // Integrator: the per-pixel work of render_multiThread (src/render.cpp:
 // 448-551 renderPixel, with sampleDirectLightFromFirstIntersection :425-437,
-// sampleIndirectLightFromFirstIntersection :314-423 and sampleRay :121-312).
+// sampleIndirectLightFromFirstIntersection :314-423 and sampleRay :121-312),
+// as a wavefront over a batch of renders ("jobs").
 //
-// Two kernels on one stream:
-//  1. primary_kernel -- one thread per pixel: camera ray (no jitter, as the
-//     reference), closest hit, hit shading, the +0.04-red demodulation tweak
-//     of grey base colours (:492-495), G-buffer written to HBM.
-//  2. path_kernel -- persistent warps claim groups of 32/K pixels from a
-//     global counter; the K lanes of a pixel split its spp_direct +
-//     spp_indirect sample slots round-robin. Slot j < spp_direct is light
-//     sample j of the first vertex; slot spp_direct + k is indirect path k,
-//     run iteratively (the reference's recursion keeps one throughput
-//     product and a product of 1/(1+fails) weights). Every slot draws from
-//     its own counter-based stream keyed (seed, pixel, slot), so results do
-//     not depend on K or on scheduling.
-//     The lanes of a pixel then reduce with warp shuffles. The reference's
-//     per-pixel firefly clamp (:532-547) drops sample i iff
-//     Clum_i > 16 (S - Clum_i + 1e-4) with S the sum over all samples; with
-//     non-negative luminances only the largest sample can satisfy that, so
-//     each lane keeps its sums without its largest sample plus that sample's
-//     contribution, and the reduction merges these pairs; the surviving
-//     largest sample is dropped or added at the end. No per-sample storage.
+// Work. A pixel's spp_direct + spp_indirect sample slots (slot j <
+// spp_direct: light sample j of the first vertex; slot spp_direct + k:
+// indirect path k) are cut into units of up to S consecutive slots. Every
+// slot draws from its own counter-based stream keyed (seed, pixel, slot), so
+// results do not depend on how slots are grouped or scheduled.
+//
+// Kernels, on one stream:
+//  1. primary_kernel  -- one thread per pixel of every job: camera ray (no
+//     jitter, as the reference), closest hit, hit shading -> G-buffer.
+//  2. per iteration, until no worker is left:
+//     logic_kernel    -- a pool of W workers; each advances its state machine
+//                        (take a unit, start a slot, consume the last trace
+//                        result, shade, sample, accumulate) until it needs a
+//                        ray traced, then appends itself to the closest-hit or
+//                        the shadow queue;
+//     qtrace_kernel<closest>, qtrace_kernel<shadow> -- persistent traversal
+//                        of the queues with per-lane dynamic ray fetch.
+//     Path state lives in HBM between the kernels, so traversal runs at the
+//     occupancy of a 60-register kernel and each kernel's warps execute one
+//     phase only.
+//  3. finalize_kernel -- per pixel, merges its units' partial accumulators
+//     in unit order and writes the four RadianceData buffers.
+//
+// Firefly clamp (:532-547): the reference drops sample i iff
+// Clum_i > 16 (S - Clum_i + 1e-4), S the luminance sum over the pixel's
+// indirect samples. With non-negative luminances only the largest sample can
+// satisfy that, so every unit keeps its sums without its largest sample plus
+// that sample's contributions; finalize merges these pairs and drops or adds
+// the surviving largest sample. No per-sample storage.
+#include <cooperative_groups.h>
+
 #include <algorithm>
+#include <cstddef>
 #include <vector>
 
 #include "rmn_host.h"
@@ -31,21 +45,22 @@ namespace {
 
 struct Params {
   float3 pos, dir, up, right;
-  float acc, exposure, p_direct;
-  int W, H, spp, maxd, K, spp_d;
-  int tasks;
+  float acc, exposure, p_direct, inv_spp;
+  int W, H, spp, maxd, spp_d, slots;
+  int S;  // slots per unit
+  int K;  // units per pixel
   uint64_t seed;
 };
 
 // One render of a batch: a scene, its arguments, its output buffers and its
-// place in the batch's pixel and task numbering.
+// place in the batch's pixel and unit numbering.
 struct Job {
   DevScene s;
   Params p;
   float* gbuf;
   float4 *dd, *ds, *id, *is;
-  int pix_begin;   // first pixel of this job in the batch's pixel numbering
-  int task_begin;  // first path task (group of 32/K pixels) of this job
+  int pix_begin;         // first pixel of this job in the batch
+  long long unit_begin;  // first unit of this job in the batch
 };
 
 // Batch-wide counters of the counting build.
@@ -53,12 +68,57 @@ struct Counters {
   unsigned long long closest, shadow, inner, leaves, tris, slots;
 };
 
-__device__ __forceinline__ int find_job(const Job* jobs, int n, int v, bool by_task) {
+// Per-iteration control words. The first five are cleared before every
+// logic pass; next_unit runs over the whole render.
+struct Ctl {
+  unsigned int qc, qs;            // queue lengths
+  unsigned int qc_next, qs_next;  // fetch cursors of the trace kernels
+  unsigned int live;              // workers not yet retired
+  unsigned int pad0;
+  unsigned long long next_unit;
+};
+
+// Worker pool in HBM (structure of arrays).
+struct Pool {
+  int W;
+  int4* unit;      // job, pixel, j (current slot), j1 (end of unit)
+  int4* ph;        // phase, rng counter, depth, flags
+  long long* uid;  // global unit index (partial record)
+  float4* ro;      // ray origin, t_min
+  float4* rd;      // ray direction, t_max (closest) or aim depth (shadow)
+  float2* res;     // closest: (leaf-order triangle, t); shadow: (occluded, -)
+  float4* pa;      // first-vertex factor w0, weight product wf
+  float4* pb;      // throughput product, roughness factor
+  float4* nv;      // 5 per worker: NEE vertex pos|kscale, shapeN|rough, surfN|metal, base|eta, V|tot
+  float4* lw;      // 2 per worker: light weights 0..7
+  int4* nk;        // NEE sample k, count
+  float4* pend;    // 2 per worker: pending sample bsdf|weight, light|-
+  int* qc;         // closest-hit queue (worker ids)
+  int* qs;         // shadow queue
+};
+
+// Partial accumulator of one unit: 7 float4.
+//   [0] Dd  [1] Ds  [2] Id without the largest sample  [3] Is likewise
+//   [4] Id of the largest  [5] Is of the largest  [6] (its Clum or -1, S, n, -)
+#define RMN_PART_F4 7
+
+enum Phase { PH_FETCH = 0, PH_SLOT, PH_WAIT_DIRECT, PH_WAIT_CLOSEST, PH_NEE, PH_WAIT_NEE, PH_DONE };
+enum Flags { FL_EXCLUDE = 1 };
+
+__device__ __forceinline__ int find_job_pix(const Job* jobs, int n, int v) {
   int lo = 0, hi = n - 1;
   while (lo < hi) {
     int mid = (lo + hi + 1) >> 1;
-    int b = by_task ? __ldg(&jobs[mid].task_begin) : __ldg(&jobs[mid].pix_begin);
-    if (b <= v) lo = mid;
+    if (__ldg(&jobs[mid].pix_begin) <= v) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+__device__ __forceinline__ int find_job_unit(const Job* jobs, int n, long long v) {
+  int lo = 0, hi = n - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (__ldg(&jobs[mid].unit_begin) <= v) lo = mid;
     else hi = mid - 1;
   }
   return lo;
@@ -91,14 +151,15 @@ __device__ __forceinline__ Surf default_surf() {
 
 // G-buffer record (RMN_GBUFFER_FLOATS = 20): base[3] emission[3] position[3]
 // shapeN[3] surfN[3] roughness metallic opacity eta material-id. The base
-// colour is stored untweaked; path_kernel applies renderPixel's tweak for its
-// own use and writes the tweaked colour back where the reference leaves it.
+// colour is stored untweaked; the integrator applies renderPixel's tweak for
+// its own use and finalize writes the tweaked colour back where the
+// reference leaves it.
 template <bool COUNT>
 __global__ void __launch_bounds__(128) primary_kernel(const Job* __restrict__ jobs, int njobs, int total_pix,
                                                       int* status, Counters* ctr) {
   int gi = blockIdx.x * blockDim.x + threadIdx.x;
   if (gi >= total_pix) return;
-  const Job& J = jobs[find_job(jobs, njobs, gi, false)];
+  const Job& J = jobs[find_job_pix(jobs, njobs, gi)];
   const DevScene& s = J.s;
   const Params& p = J.p;
   int i = gi - J.pix_begin;
@@ -138,6 +199,8 @@ struct Rad4 {
 };
 __device__ __forceinline__ Rad4 rad0() { return {f3(0.0f), 0.0f}; }
 __device__ __forceinline__ void radd(Rad4& a, const Rad4& b) { a.c += b.c; a.v += b.v; }
+__device__ __forceinline__ Rad4 r4(float4 v) { return {f3(v.x, v.y, v.z), v.w}; }
+__device__ __forceinline__ float4 f4(const Rad4& r) { return make_float4(r.c.x, r.c.y, r.c.z, r.v); }
 
 // accumulateInwardRadiance(_basic), src/image.cpp:615-659, as the two
 // contributions (diffuse part, specular part) of one sample.
@@ -172,18 +235,16 @@ __device__ __forceinline__ void demodulate(float3 base, float3 bsdf, float3 ligh
   basic(light * (bsdf - bb), w, sp);
 }
 
-struct Acc {
-  Rad4 dd, ds;    // direct diffuse / specular sums
-  Rad4 id, is;    // indirect sums without the largest sample
-  Rad4 mid, mis;  // the largest indirect sample's contributions
-  float mclum;    // its luminance (-1: none yet)
-  float S;        // luminance sum of all indirect samples
-  int n;          // indirect sample count
+// The largest-sample bookkeeping shared by emit (one sample into a unit) and
+// finalize (unit into pixel).
+struct Ind {
+  Rad4 id, is, mid, mis;
+  float mclum, S;
+  int n;
 };
-
-__device__ __forceinline__ void acc_indirect(Acc& a, const Rad4& d, const Rad4& s, float clum) {
-  a.S += clum;
-  a.n += 1;
+__device__ __forceinline__ void ind_add(Ind& a, const Rad4& d, const Rad4& s, float clum, float S, int n) {
+  a.S += S;
+  a.n += n;
   if (clum > a.mclum) {
     if (a.mclum >= 0.0f) {
       radd(a.id, a.mid);
@@ -192,110 +253,436 @@ __device__ __forceinline__ void acc_indirect(Acc& a, const Rad4& d, const Rad4& 
     a.mid = d;
     a.mis = s;
     a.mclum = clum;
-  } else {
+  } else if (clum >= 0.0f) {
     radd(a.id, d);
     radd(a.is, s);
   }
 }
 
-struct PathCtx {
-  float3 base;   // G-buffer base colour (tweaked), demodulation reference
-  float3 w0;     // first-vertex bsdf/pdf factor (LightSample::bsdfPdf)
-  float3 thr;    // product of the deeper vertices' factors
-  float wf;      // product of 1/(1+fails) factors
-  float inv_spp; // 1 / spp_indirect
-};
-
-__device__ __forceinline__ void emit(Acc& a, const PathCtx& c, const LSample& ls) {
-  float3 light = (ls.light * ls.bsdf) * c.thr;
-  float w = ls.weight * c.wf * c.inv_spp;
-  Rad4 d, s;
-  demodulate(c.base, c.w0, light, w, d, s);
-  float clum = dot3(c.w0 * light, RMN_LUM) * w;
-  acc_indirect(a, d, s, clum);
+__device__ __forceinline__ const float* gbuf_of(const Job& J, int pixel) {
+  return J.gbuf + (size_t)RMN_GBUFFER_FLOATS * pixel;
+}
+__device__ __forceinline__ float3 base_of(const Job& J, int pixel) {
+  const float* gb = gbuf_of(J, pixel);
+  return tweak_base(f3(gb[0], gb[1], gb[2]));
+}
+__device__ __forceinline__ Surf load_first_vertex(const Job& J, int pixel) {
+  const float* gb = gbuf_of(J, pixel);
+  Surf g = default_surf();
+  g.base = tweak_base(f3(gb[0], gb[1], gb[2]));
+  g.emis = f3(gb[3], gb[4], gb[5]);
+  g.pos = f3(gb[6], gb[7], gb[8]);
+  g.shapeN = f3(gb[9], gb[10], gb[11]);
+  g.surfN = f3(gb[12], gb[13], gb[14]);
+  g.roughness = gb[15];
+  g.metallic = gb[16];
+  g.opacity = gb[17];
+  g.eta = gb[18];
+  g.id = (int)gb[19];
+  return g;
 }
 
-// One indirect sample from the first vertex (sampleIndirectLightFrom-
-// FirstIntersection + the sampleRay recursion) for an opaque first vertex.
+// One indirect light sample into the unit's partial record: light and
+// weight finished as passBsdf/mulWeight would (src/render.cpp:101-116),
+// demodulated against the first vertex's (tweaked) base colour with the
+// first-vertex factor w0 as LightSample::bsdfPdf.
+__device__ void emit(float4* part, float3 base, float4 pa, float3 thr, float inv_spp, const LSample& ls) {
+  float3 w0 = f3(pa.x, pa.y, pa.z);
+  float3 light = (ls.light * ls.bsdf) * thr;
+  float w = ls.weight * pa.w * inv_spp;
+  Rad4 d, s;
+  demodulate(base, w0, light, w, d, s);
+  float clum = dot3(w0 * light, RMN_LUM) * w;
+  Ind a;
+  a.id = r4(part[2]);
+  a.is = r4(part[3]);
+  a.mid = r4(part[4]);
+  a.mis = r4(part[5]);
+  float4 m = part[6];
+  a.mclum = m.x;
+  a.S = m.y;
+  a.n = __float_as_int(m.z);
+  ind_add(a, d, s, clum, clum, 1);
+  part[2] = f4(a.id);
+  part[3] = f4(a.is);
+  part[4] = f4(a.mid);
+  part[5] = f4(a.mis);
+  part[6] = make_float4(a.mclum, a.S, __int_as_float(a.n), 0.0f);
+}
+
+// Warp-aggregated increment: the lanes that reach the call together take
+// consecutive values with one atomic (single-address atomics would otherwise
+// serialise a million workers per iteration).
+template <class T>
+__device__ __forceinline__ T agg_inc(T* ctr) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group g = cg::coalesced_threads();
+  T base = 0;
+  if (g.thread_rank() == 0) base = atomicAdd(ctr, (T)g.size());
+  base = g.shfl(base, 0);
+  return base + (T)g.thread_rank();
+}
+
+__device__ __forceinline__ void push(int* q, unsigned int* qn, int w) { q[agg_inc(qn)] = w; }
+
+// Advances worker w until it needs a ray traced (then it is queued) or no
+// unit is left. State machine over the reference's control flow:
+//   PH_FETCH        take the next unit (a pixel and a slot range)
+//   PH_SLOT         start slot j: a first-vertex light sample (shadow ray)
+//                   or the first bounce of an indirect path (closest-hit ray)
+//   PH_WAIT_DIRECT  shadow answer of a first-vertex light sample
+//   PH_WAIT_CLOSEST closest-hit answer of a path ray: sampleRay's body
+//   PH_NEE          next light sample of the terminating vertex
+//   PH_WAIT_NEE     shadow answer of that light sample
 template <bool COUNT>
-__device__ void indirect_path(const DevScene& s, const Params& p, const Surf& g, RmnRng& rng, Acc& a, float inv_spp,
-                              int* status, TraceCounters* tc) {
-  if (len3(g.emis) > 0.0f) return;
-  float3 in = norm3(g.pos - p.pos);
-  Surf v0 = g;
-  v0.eta = 1.0f / v0.eta;
-  float rf = g.roughness * 1.0f;
-  if (!(rng.next() < 1.0f)) return;
-  PathCtx c;
-  c.base = g.base;
-  c.inv_spp = inv_spp;
-  float3 dir;
-  int f0 = 0;
-  sample_reflect(v0, -in, rng, dir, c.w0, f0);
-  if (!any_finite3(dir)) return;
-  c.wf = f0 > 0 ? 1.0f / (float)(1 + f0) : 1.0f;
-  c.thr = f3(1.0f);
-  float3 o = g.pos;
-  bool exclude = true;
-  for (int depth = 1;; ++depth) {
-    TRay r = make_tray(o, dir);
-    float tmax = INFINITY;
-    int h = trace<false, COUNT>(s, r, RMN_EPS, tmax, 0.0f, tc);
-    if (h == -2) {
-      atomicExch(status, 1);
-      return;
-    }
-    if (h < 0) {
-      if (!exclude && s.sky_w) emit(a, c, {f3(1.0f), sky_get(s, dir), 1.0f});
-      return;
-    }
-    Surf sf = default_surf();
-    sf.pos = o + dir * tmax;
-    hit_info(s, h, dir, sf);
-    rf = fmaxf(rf, 1.0f * sf.roughness);
-    sf.roughness = fmaxf(sf.roughness, rf);
-    const float p_rr = 1.0f + (0.5f - 1.0f) * sqrtf(sf.roughness);
-    bool nee = p_rr < 0.9f;
-    if (len3(sf.emis) > RMN_EPS) {
-      if (!exclude) emit(a, c, {f3(1.0f), sf.emis, 1.0f});
-      return;
-    }
-    if (!(rng.next() <= 1.0f)) return;
-    nee = nee && sf.entering;
-    const float3 V = -dir;
-    if (nee && (depth >= p.maxd || rng.next() > p_rr)) {
-      int cnt = c_sample_count[depth < 16 ? depth : 16];
-      float k = 1.0f / 1.0f;
-      if (depth < p.maxd) k /= (1.0f - p_rr);
-      float lw[8];
-      float tot = 0.0f;
-      if (s.sky_w == 0 && !light_weights(s, sf, V, lw, tot)) return;
-      for (int T = 0; T < cnt; ++T) {
+__global__ void __launch_bounds__(128) logic_kernel(const Job* __restrict__ jobs, int njobs, Pool P, Ctl* ctl,
+                                                    long long total_units, float4* __restrict__ parts, int* status,
+                                                    Counters* ctr) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= P.W) return;
+  int4 ph = P.ph[w];
+  int phase = ph.x;
+  if (phase == PH_DONE) return;
+  int4 un = P.unit[w];
+  long long uid = P.uid[w];
+  unsigned long long slots_done = 0;
+  const Job* J = phase == PH_FETCH ? nullptr : &jobs[un.x];
+  RmnRng rng;
+  rng.key = 0;
+  rng.ctr = (unsigned)ph.y;
+  if (J) rng.key = rmn_stream_key(J->p.seed, (uint32_t)un.y, (uint32_t)un.z);
+  bool stop = false;
+  for (int guard = 0; guard < 4096 && !stop; ++guard) {
+    switch (phase) {
+      case PH_FETCH: {
+        unsigned long long u = agg_inc(&ctl->next_unit);
+        if ((long long)u >= total_units) {
+          phase = PH_DONE;
+          stop = true;
+          break;
+        }
+        uid = (long long)u;
+        int jb = find_job_unit(jobs, njobs, uid);
+        J = &jobs[jb];
+        long long local = uid - J->unit_begin;
+        int pixel = (int)(local / J->p.K), sub = (int)(local % J->p.K);
+        int j0 = sub * J->p.S, j1 = min(J->p.slots, j0 + J->p.S);
+        float4* part = parts + (size_t)uid * RMN_PART_F4;
+#pragma unroll
+        for (int k = 0; k < 6; ++k) part[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        part[6] = make_float4(-1.0f, 0.0f, __int_as_float(0), 0.0f);
+        const float* gb = gbuf_of(*J, pixel);
+        bool hit = any_finite3(f3(gb[6], gb[7], gb[8]));
+        un = make_int4(jb, pixel, hit ? j0 : j1, j1);
+        phase = PH_SLOT;
+        break;
+      }
+      case PH_SLOT: {
+        if (un.z >= un.w) {
+          phase = PH_FETCH;
+          break;
+        }
+        const Params& p = J->p;
+        const DevScene& s = J->s;
+        rng = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)un.z);
+        if (COUNT) slots_done++;
+        Surf g = load_first_vertex(*J, un.y);
+        if (un.z < p.spp_d) {
+          // sampleDirectLightFromFirstIntersection, src/render.cpp:425-437
+          if (len3(g.emis) > 0.0f) {
+            un.z++;
+            break;
+          }
+          float3 Vd = -norm3(g.pos - p.pos);
+          float lwt[8];
+          float tot = 0.0f;
+          if (s.sky_w == 0 && !light_weights(s, g, Vd, lwt, tot)) {
+            un.z++;
+            break;
+          }
+          float3 dir;
+          float aim;
+          LSample ls;
+          if (!light_gen(s, g, Vd, lwt, tot, p.spp_d, rng, dir, aim, ls)) {
+            un.z++;
+            break;
+          }
+          P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
+          P.rd[w] = make_float4(dir.x, dir.y, dir.z, aim);
+          P.pend[2 * w] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
+          P.pend[2 * w + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
+          push(P.qs, &ctl->qs, w);
+          phase = PH_WAIT_DIRECT;
+          stop = true;
+          break;
+        }
+        // sampleIndirectLightFromFirstIntersection, src/render.cpp:314-423
+        if (len3(g.emis) > 0.0f || !(rng.next() < 1.0f)) {
+          un.z++;
+          break;
+        }
+        float3 in = norm3(g.pos - p.pos);
+        Surf v0 = g;
+        v0.eta = 1.0f / v0.eta;
+        float3 dir, w0;
+        int f0 = 0;
+        sample_reflect(v0, -in, rng, dir, w0, f0);
+        if (!any_finite3(dir)) {
+          un.z++;
+          break;
+        }
+        P.pa[w] = make_float4(w0.x, w0.y, w0.z, f0 > 0 ? 1.0f / (float)(1 + f0) : 1.0f);
+        P.pb[w] = make_float4(1.0f, 1.0f, 1.0f, g.roughness * 1.0f);
+        P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
+        P.rd[w] = make_float4(dir.x, dir.y, dir.z, INFINITY);
+        ph.z = 1;           // depth of the vertex this ray will hit
+        ph.w = FL_EXCLUDE;  // the first bounce excludes direct light
+        push(P.qc, &ctl->qc, w);
+        phase = PH_WAIT_CLOSEST;
+        stop = true;
+        break;
+      }
+      case PH_WAIT_DIRECT: {
+        if (P.res[w].x == 0.0f) {
+          float4 a = P.pend[2 * w], b = P.pend[2 * w + 1];
+          Rad4 d, sp;
+          demodulate(base_of(*J, un.y), f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w, d, sp);
+          float4* part = parts + (size_t)uid * RMN_PART_F4;
+          Rad4 dd = r4(part[0]), ds = r4(part[1]);
+          radd(dd, d);
+          radd(ds, sp);
+          part[0] = f4(dd);
+          part[1] = f4(ds);
+        }
+        un.z++;
+        phase = PH_SLOT;
+        break;
+      }
+      case PH_WAIT_CLOSEST: {
+        // sampleRay's body, src/render.cpp:121-312, opaque surfaces
+        const Params& p = J->p;
+        const DevScene& s = J->s;
+        float2 res = P.res[w];
+        int h = __float_as_int(res.x);
+        float4 o4 = P.ro[w], d4 = P.rd[w];
+        float3 o = f3(o4.x, o4.y, o4.z), dir = f3(d4.x, d4.y, d4.z);
+        int depth = ph.z;
+        bool exclude = (ph.w & FL_EXCLUDE) != 0;
+        if (h == -2) {
+          atomicExch(status, 1);
+          un.z++;
+          phase = PH_SLOT;
+          break;
+        }
+        float4 pb = P.pb[w];
+        if (h < 0) {
+          if (!exclude && s.sky_w)
+            emit(parts + (size_t)uid * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp,
+                 {f3(1.0f), sky_get(s, dir), 1.0f});
+          un.z++;
+          phase = PH_SLOT;
+          break;
+        }
+        Surf sf = default_surf();
+        sf.pos = o + dir * res.y;
+        hit_info(s, h, dir, sf);
+        float rf = fmaxf(pb.w, 1.0f * sf.roughness);
+        sf.roughness = fmaxf(sf.roughness, rf);
+        const float p_rr = 1.0f + (0.5f - 1.0f) * sqrtf(sf.roughness);
+        bool nee = p_rr < 0.9f;
+        if (len3(sf.emis) > RMN_EPS) {
+          if (!exclude)
+            emit(parts + (size_t)uid * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp,
+                 {f3(1.0f), sf.emis, 1.0f});
+          un.z++;
+          phase = PH_SLOT;
+          break;
+        }
+        if (!(rng.next() <= 1.0f)) {
+          un.z++;
+          phase = PH_SLOT;
+          break;
+        }
+        nee = nee && sf.entering;
+        const float3 V = -dir;
+        if (nee && (depth >= p.maxd || rng.next() > p_rr)) {
+          int cnt = c_sample_count[depth < 16 ? depth : 16];
+          float k = 1.0f / 1.0f;
+          if (depth < p.maxd) k /= (1.0f - p_rr);
+          float lwt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          float tot = 0.0f;
+          if (s.sky_w == 0 && !light_weights(s, sf, V, lwt, tot)) {
+            un.z++;
+            phase = PH_SLOT;
+            break;
+          }
+          float4* nv = P.nv + 5 * (size_t)w;
+          nv[0] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, k);
+          nv[1] = make_float4(sf.shapeN.x, sf.shapeN.y, sf.shapeN.z, sf.roughness);
+          nv[2] = make_float4(sf.surfN.x, sf.surfN.y, sf.surfN.z, sf.metallic);
+          nv[3] = make_float4(sf.base.x, sf.base.y, sf.base.z, sf.eta);
+          nv[4] = make_float4(V.x, V.y, V.z, tot);
+          P.lw[2 * w] = make_float4(lwt[0], lwt[1], lwt[2], lwt[3]);
+          P.lw[2 * w + 1] = make_float4(lwt[4], lwt[5], lwt[6], lwt[7]);
+          P.nk[w] = make_int4(0, cnt, 0, 0);
+          phase = PH_NEE;
+          break;
+        }
+        float3 nd, wv;
+        int nf = 0;
+        sample_reflect(sf, V, rng, nd, wv, nf);
+        wv = wv / 1.0f;
+        if (nee) wv = wv / p_rr;
+        if (!any_finite3(nd) || depth == p.maxd) {
+          un.z++;
+          phase = PH_SLOT;
+          break;
+        }
+        float3 thr = f3(pb.x, pb.y, pb.z) * wv;
+        P.pb[w] = make_float4(thr.x, thr.y, thr.z, rf);
+        if (nf > 0) {
+          float4 pa = P.pa[w];
+          pa.w = pa.w * (1.0f / (float)(1 + nf));
+          P.pa[w] = pa;
+        }
+        P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
+        P.rd[w] = make_float4(nd.x, nd.y, nd.z, INFINITY);
+        ph.z = depth + 1;
+        ph.w = nee ? FL_EXCLUDE : 0;
+        push(P.qc, &ctl->qc, w);
+        stop = true;
+        break;
+      }
+      case PH_NEE: {
+        int4 nk = P.nk[w];
+        if (nk.x >= nk.y) {
+          un.z++;
+          phase = PH_SLOT;
+          break;
+        }
+        const DevScene& s = J->s;
+        const float4* nv = P.nv + 5 * (size_t)w;
+        float4 a = nv[0], b = nv[1], c = nv[2], d = nv[3], e = nv[4];
+        Surf sf = default_surf();
+        sf.pos = f3(a.x, a.y, a.z);
+        sf.shapeN = f3(b.x, b.y, b.z);
+        sf.roughness = b.w;
+        sf.surfN = f3(c.x, c.y, c.z);
+        sf.metallic = c.w;
+        sf.base = f3(d.x, d.y, d.z);
+        sf.eta = d.w;
+        float4 l0 = P.lw[2 * w], l1 = P.lw[2 * w + 1];
+        float lwt[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+        float3 dir;
+        float aim;
         LSample ls;
-        if (light_sample<COUNT>(s, sf, V, lw, tot, cnt, rng, ls, status, tc)) {
-          ls.bsdf *= k;
-          emit(a, c, ls);
+        if (!light_gen(s, sf, f3(e.x, e.y, e.z), lwt, e.w, nk.y, rng, dir, aim, ls)) {
+          P.nk[w] = make_int4(nk.x + 1, nk.y, 0, 0);
+          break;
+        }
+        ls.bsdf *= a.w;  // scaling(samples, factor), src/render.cpp:101-104
+        P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
+        P.rd[w] = make_float4(dir.x, dir.y, dir.z, aim);
+        P.pend[2 * w] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
+        P.pend[2 * w + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
+        push(P.qs, &ctl->qs, w);
+        phase = PH_WAIT_NEE;
+        stop = true;
+        break;
+      }
+      case PH_WAIT_NEE: {
+        if (P.res[w].x == 0.0f) {
+          float4 a = P.pend[2 * w], b = P.pend[2 * w + 1];
+          float4 pb = P.pb[w];
+          emit(parts + (size_t)uid * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), J->p.inv_spp,
+               {f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w});
+        }
+        int4 nk = P.nk[w];
+        P.nk[w] = make_int4(nk.x + 1, nk.y, 0, 0);
+        phase = PH_NEE;
+        break;
+      }
+      default:
+        stop = true;
+        break;
+    }
+  }
+  ph.x = phase;
+  ph.y = (int)rng.ctr;
+  P.ph[w] = ph;
+  P.unit[w] = un;
+  P.uid[w] = uid;
+  if (phase != PH_DONE) agg_inc(&ctl->live);
+  if (COUNT && slots_done) atomicAdd(&ctr->slots, slots_done);
+}
+
+constexpr int kFetchBudget = 16;  // node visits between refill checks
+
+// Persistent traversal of one queue. Each lane owns one queued worker's ray;
+// every 16 node visits, lanes whose ray is answered take the next queue
+// entries (one warp-aggregated atomic), so a warp does not wait for its
+// longest ray. The rays of a batch belong to different scenes; each lane
+// traverses its own job's BVH.
+template <bool SHADOW, bool COUNT>
+__global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Ctl* ctl, int* status,
+                                                     Counters* ctr) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  const unsigned n = SHADOW ? ctl->qs : ctl->qc;
+  unsigned int* next = SHADOW ? &ctl->qs_next : &ctl->qc_next;
+  const int* q = SHADOW ? P.qs : P.qc;
+  bool active = false, retired = false;
+  int w = 0;
+  TRay r;
+  float tmin = 0.0f, aim = 0.0f;
+  Trav t;
+  DevScene s;
+  TraceCounters tc = {0, 0, 0, 0, 0};
+  for (;;) {
+    unsigned need = __ballot_sync(0xffffffffu, !active && !retired);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(next, (unsigned)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!active && !retired) {
+        unsigned i = base + __popc(need & lt);
+        if (i < n) {
+          w = q[i];
+          float4 o = P.ro[w], d = P.rd[w];
+          s = jobs[P.unit[w].x].s;
+          r = make_tray(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
+          tmin = o.w;
+          if (SHADOW) {
+            aim = d.w;
+            trav_begin(s, t, aim + RMN_EPS);  // HitRecord(eps, aimDepth + eps)
+            if (COUNT) tc.shadow++;
+          } else {
+            trav_begin(s, t, d.w);
+            if (COUNT) tc.closest++;
+          }
+          active = true;
+        } else {
+          retired = true;
         }
       }
-      return;
     }
-    float3 nd, w;
-    int nf = 0;
-    sample_reflect(sf, V, rng, nd, w, nf);
-    w = w / 1.0f;
-    if (nee) w = w / p_rr;
-    if (!any_finite3(nd) || depth == p.maxd) return;
-    c.thr = c.thr * w;
-    if (nf > 0) c.wf = c.wf * (1.0f / (float)(1 + nf));
-    o = sf.pos;
-    dir = nd;
-    exclude = nee;
+    if (__ballot_sync(0xffffffffu, active) == 0) break;
+    if (!active) continue;
+    int st = trav_run<SHADOW, COUNT>(s, r, tmin, aim, t, kFetchBudget, &tc);
+    if (st == 0) continue;
+    if (SHADOW) P.res[w] = make_float2(st == -2 ? 0.0f : ((t.tmax >= aim) ? 0.0f : 1.0f), 0.0f);
+    else P.res[w] = make_float2(__int_as_float(st == -2 ? -2 : t.hit), t.tmax);
+    if (st == -2) atomicExch(status, 1);
+    active = false;
   }
-}
-
-__device__ __forceinline__ float shfl(float v, int off) { return __shfl_xor_sync(0xffffffffu, v, off); }
-__device__ __forceinline__ Rad4 shfl4(const Rad4& r, int off) {
-  return {f3(shfl(r.c.x, off), shfl(r.c.y, off), shfl(r.c.z, off)), shfl(r.v, off)};
+  if (COUNT) {
+    atomicAdd(&ctr->closest, (unsigned long long)tc.closest);
+    atomicAdd(&ctr->shadow, (unsigned long long)tc.shadow);
+    atomicAdd(&ctr->inner, (unsigned long long)tc.inner);
+    atomicAdd(&ctr->leaves, (unsigned long long)tc.leaves);
+    atomicAdd(&ctr->tris, (unsigned long long)tc.tris);
+  }
 }
 
 __device__ __forceinline__ void calc_var(Rad4& r, float e) {  // renderPixel's calcVar, src/render.cpp:510-516
@@ -305,134 +692,54 @@ __device__ __forceinline__ void calc_var(Rad4& r, float e) {  // renderPixel's c
   if (r.v < 0.0f) r.v = 0.0f;
 }
 
-template <bool COUNT>
-__global__ void __launch_bounds__(128) path_kernel(const Job* __restrict__ jobs, int njobs, int total_tasks,
-                                                   unsigned int* __restrict__ next, int* status, Counters* ctr) {
-  const int lane = threadIdx.x & 31;
-  TraceCounters tc = {0, 0, 0, 0, 0};
-  unsigned long long slots_done = 0;
-  for (;;) {
-    unsigned int task = 0;
-    if (lane == 0) task = atomicAdd(next, 1u);
-    task = __shfl_sync(0xffffffffu, task, 0);
-    if (task >= (unsigned)total_tasks) break;
-    const Job& J = jobs[find_job(jobs, njobs, (int)task, true)];
-    const DevScene& s = J.s;
-    const Params& p = J.p;
-    const int K = p.K, P = 32 / K;
-    const int sub = lane % K, grp = lane / K;
-    const int npix = p.W * p.H;
-    const int pixel = ((int)task - J.task_begin) * P + grp;
-    const bool valid = pixel < npix;
-    Acc a;
-    a.dd = a.ds = a.id = a.is = a.mid = a.mis = rad0();
-    a.mclum = -1.0f;
-    a.S = 0.0f;
-    a.n = 0;
-    bool hit = false;
-    Surf g = default_surf();
-    if (valid) {
-      const float* gb = J.gbuf + (size_t)RMN_GBUFFER_FLOATS * pixel;
-      g.base = f3(gb[0], gb[1], gb[2]);
-      g.emis = f3(gb[3], gb[4], gb[5]);
-      g.pos = f3(gb[6], gb[7], gb[8]);
-      g.shapeN = f3(gb[9], gb[10], gb[11]);
-      g.surfN = f3(gb[12], gb[13], gb[14]);
-      g.roughness = gb[15];
-      g.metallic = gb[16];
-      g.opacity = gb[17];
-      g.eta = gb[18];
-      g.id = (int)gb[19];
-      hit = any_finite3(g.pos);
-      if (hit) g.base = tweak_base(g.base);
+// Per pixel: merge the partial records of its K units in unit order, apply
+// the firefly clamp and calcVar, write the RadianceData buffers; write the
+// tweaked base colour back where renderPixel leaves it tweaked.
+__global__ void __launch_bounds__(128) finalize_kernel(const Job* __restrict__ jobs, int njobs, int total_pix,
+                                                       const float4* __restrict__ parts) {
+  int gi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (gi >= total_pix) return;
+  const Job& J = jobs[find_job_pix(jobs, njobs, gi)];
+  const Params& p = J.p;
+  const int pixel = gi - J.pix_begin;
+  float* gb = J.gbuf + (size_t)RMN_GBUFFER_FLOATS * pixel;
+  bool hit = any_finite3(f3(gb[6], gb[7], gb[8]));
+  Rad4 dd = rad0(), ds = rad0();
+  Ind a;
+  a.id = a.is = a.mid = a.mis = rad0();
+  a.mclum = -1.0f;
+  a.S = 0.0f;
+  a.n = 0;
+  if (hit) {
+    const float4* pr = parts + (size_t)(J.unit_begin + (long long)pixel * p.K) * RMN_PART_F4;
+    for (int k = 0; k < p.K; ++k, pr += RMN_PART_F4) {
+      radd(dd, r4(pr[0]));
+      radd(ds, r4(pr[1]));
+      float4 m = pr[6];
+      radd(a.id, r4(pr[2]));
+      radd(a.is, r4(pr[3]));
+      ind_add(a, r4(pr[4]), r4(pr[5]), m.x, m.y, __float_as_int(m.z));
     }
-    if (hit) {
-      const int spp_d = p.spp_d;
-      const int spp_i = (p.spp - spp_d) * 1;  // opaque first vertex
-      const int slots = spp_d + spp_i;
-      const float inv_spp = 1.0f / (float)spp_i;
-      const bool direct_ok = !(len3(g.emis) > 0.0f);
-      float3 Vd = -norm3(g.pos - p.pos);
-      float lw[8];
-      float tot = 0.0f;
-      bool have_w = false, w_done = false;
-      for (int j = sub; j < slots; j += K) {
-        RmnRng rng = rmn_rng(p.seed, (uint32_t)pixel, (uint32_t)j);
-        if (COUNT) slots_done++;
-        if (j < spp_d) {
-          if (!direct_ok) continue;
-          if (!w_done) {
-            have_w = s.sky_w != 0 || light_weights(s, g, Vd, lw, tot);
-            w_done = true;
-          }
-          if (!have_w) continue;
-          LSample ls;
-          if (light_sample<COUNT>(s, g, Vd, lw, tot, spp_d, rng, ls, status, &tc)) {
-            Rad4 d, sp;
-            demodulate(g.base, ls.bsdf, ls.light, ls.weight, d, sp);
-            radd(a.dd, d);
-            radd(a.ds, sp);
-          }
-        } else {
-          indirect_path<COUNT>(s, p, g, rng, a, inv_spp, status, &tc);
-        }
+    calc_var(dd, p.exposure);
+    calc_var(ds, p.exposure);
+    if (a.n > 0) {
+      if (!(a.mclum / (a.S - a.mclum + RMN_EPS) > 16.0f)) {
+        radd(a.id, a.mid);
+        radd(a.is, a.mis);
       }
-    }
-    // reduce over the K lanes of each pixel
-    for (int off = K >> 1; off >= 1; off >>= 1) {
-      radd(a.dd, shfl4(a.dd, off));
-      radd(a.ds, shfl4(a.ds, off));
-      radd(a.id, shfl4(a.id, off));
-      radd(a.is, shfl4(a.is, off));
-      Rad4 omid = shfl4(a.mid, off), omis = shfl4(a.mis, off);
-      float om = shfl(a.mclum, off);
-      a.S += shfl(a.S, off);
-      a.n += __shfl_xor_sync(0xffffffffu, a.n, off);
-      if (om > a.mclum) {
-        if (a.mclum >= 0.0f) {
-          radd(a.id, a.mid);
-          radd(a.is, a.mis);
-        }
-        a.mid = omid;
-        a.mis = omis;
-        a.mclum = om;
-      } else if (om >= 0.0f) {
-        radd(a.id, omid);
-        radd(a.is, omis);
-      }
-    }
-    if (valid && sub == 0) {
-      if (hit) {
-        calc_var(a.dd, p.exposure);
-        calc_var(a.ds, p.exposure);
-        if (a.n > 0) {
-          if (!(a.mclum / (a.S - a.mclum + RMN_EPS) > 16.0f)) {
-            radd(a.id, a.mid);
-            radd(a.is, a.mis);
-          }
-          calc_var(a.id, p.exposure);
-          calc_var(a.is, p.exposure);
-        } else {
-          // renderPixel restores the untweaked base colour only after
-          // accumulating indirect samples; with none it returns early
-          // (src/render.cpp:517-518) and the tweak stays in the G-buffer.
-          J.gbuf[(size_t)RMN_GBUFFER_FLOATS * pixel] = g.base.x;
-        }
-      }
-      J.dd[pixel] = make_float4(a.dd.c.x, a.dd.c.y, a.dd.c.z, a.dd.v);
-      J.ds[pixel] = make_float4(a.ds.c.x, a.ds.c.y, a.ds.c.z, a.ds.v);
-      J.id[pixel] = make_float4(a.id.c.x, a.id.c.y, a.id.c.z, a.id.v);
-      J.is[pixel] = make_float4(a.is.c.x, a.is.c.y, a.is.c.z, a.is.v);
+      calc_var(a.id, p.exposure);
+      calc_var(a.is, p.exposure);
+    } else {
+      // renderPixel restores the untweaked base colour only after
+      // accumulating indirect samples; with none it returns early
+      // (src/render.cpp:517-518) and the tweak stays in the G-buffer.
+      gb[0] = tweak_base(f3(gb[0], gb[1], gb[2])).x;
     }
   }
-  if (COUNT) {
-    atomicAdd(&ctr->closest, (unsigned long long)tc.closest);
-    atomicAdd(&ctr->shadow, (unsigned long long)tc.shadow);
-    atomicAdd(&ctr->inner, (unsigned long long)tc.inner);
-    atomicAdd(&ctr->leaves, (unsigned long long)tc.leaves);
-    atomicAdd(&ctr->tris, (unsigned long long)tc.tris);
-    atomicAdd(&ctr->slots, slots_done);
-  }
+  J.dd[pixel] = f4(dd);
+  J.ds[pixel] = f4(ds);
+  J.id[pixel] = f4(a.id);
+  J.is[pixel] = f4(a.is);
 }
 
 int device_sms() {
@@ -442,9 +749,10 @@ int device_sms() {
   return sms;
 }
 
-int path_blocks_per_sm() {
+template <class K>
+int blocks_per_sm(K kernel) {
   int per_sm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, path_kernel<false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, 128, 0);
   return per_sm < 1 ? 1 : per_sm;
 }
 
@@ -452,31 +760,33 @@ int path_blocks_per_sm() {
 
 namespace rmn {
 
-// Lanes per pixel: the fewest (each lane then owns more of the pixel's
-// sample slots, which balances the warp and amortises per-pixel set-up) that
-// still yield about four waves of warps over the whole batch.
-int default_lanes_per_pixel(int64_t batch_pixels, int spp) {
-  const int64_t resident_warps = (int64_t)device_sms() * path_blocks_per_sm() * 4;
-  int k = 1;
-  while (k < 32 && k * 2 <= (spp > 0 ? spp : 1) && batch_pixels * k / 32 < 4 * resident_warps) k *= 2;
-  return k;
-}
+// Slots per work unit. A unit is the work of one worker between two fetches;
+// shorter units shorten the drain at the end of a render, longer ones need
+// fewer partial records (112 B each).
+constexpr int kDefaultSlotsPerUnit = 16;
+constexpr int kDefaultPoolWorkers = 1 << 20;
+constexpr int kIterationsPerChunk = 8;
+constexpr long long kMaxIterations = 1LL << 22;  // bound on the iteration loop; a finite render never reaches it
 
 struct JobTable {
   std::vector<Job> jobs;
-  int total_pix = 0, total_tasks = 0;
+  int total_pix = 0;
+  long long total_units = 0;
 };
 
 struct BatchState {
   JobTable table;
   Job* d_jobs = nullptr;
-  unsigned int* d_next = nullptr;
+  Ctl* d_ctl = nullptr;
   int* d_status = nullptr;
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
+  float4* d_parts = nullptr;
+  Pool pool{};
+  std::vector<void*> allocs;
+  cudaGraphExec_t init_exec = nullptr, chunk_exec = nullptr, fin_exec = nullptr;
+  bool use_graph = false;
 };
 
-static Params make_params(const rmn_render_args& a, int K) {
+static Params make_params(const rmn_render_args& a) {
   Params p;
   p.pos = f3(a.position[0], a.position[1], a.position[2]);
   p.dir = f3(a.direction[0], a.direction[1], a.direction[2]);
@@ -490,93 +800,232 @@ static Params make_params(const rmn_render_args& a, int K) {
   p.spp = a.spp;
   p.maxd = a.max_depth;
   p.spp_d = (int)((float)a.spp * a.P_Direct);  // renderPixel, src/render.cpp:497
-  p.K = K;
+  const int spp_i = (a.spp - p.spp_d) * 1;      // opaque first vertex
+  p.inv_spp = 1.0f / (float)spp_i;
+  p.slots = p.spp_d + spp_i;
+  // lanes_per_pixel > 0 fixes the number of units per pixel; 0 cuts the
+  // slots into units of kDefaultSlotsPerUnit.
+  if (a.lanes_per_pixel > 0) {
+    p.K = a.lanes_per_pixel;
+    p.S = (p.slots + p.K - 1) / p.K;
+    if (p.S < 1) p.S = 1;
+  } else {
+    p.S = kDefaultSlotsPerUnit;
+    p.K = (p.slots + p.S - 1) / p.S;
+    if (p.K < 1) p.K = 1;
+  }
   p.seed = a.seed;
-  const int npix = p.W * p.H;
-  p.tasks = (npix + (32 / K) - 1) / (32 / K);
   return p;
 }
 
-// Jobs ordered by decreasing cost per task (spp x depth), so the persistent
-// warps finish on the cheap tasks; the result does not depend on the order.
+// Jobs ordered by decreasing depth (the longest paths start first), so the
+// pool drains on cheap units; results do not depend on the order.
 static void build_jobs(const RenderItem* items, int n, JobTable* t) {
-  int64_t batch_pixels = 0;
-  for (int i = 0; i < n; ++i) batch_pixels += (int64_t)items[i].args.width * items[i].args.height;
   std::vector<int> order(n);
   for (int i = 0; i < n; ++i) order[i] = i;
-  auto cost = [&](int i) {
-    const rmn_render_args& a = items[i].args;
-    int K = a.lanes_per_pixel > 0 ? a.lanes_per_pixel : default_lanes_per_pixel(batch_pixels, a.spp);
-    return (double)a.spp * a.max_depth * (32 / K);
-  };
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) { return cost(a) > cost(b); });
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return items[a].args.max_depth > items[b].args.max_depth; });
   t->jobs.clear();
-  t->total_pix = t->total_tasks = 0;
+  t->total_pix = 0;
+  t->total_units = 0;
   for (int i : order) {
     const RenderItem& it = items[i];
-    int K = it.args.lanes_per_pixel > 0 ? it.args.lanes_per_pixel : default_lanes_per_pixel(batch_pixels, it.args.spp);
     Job j;
     j.s = it.scene->dev;
-    j.p = make_params(it.args, K);
+    j.p = make_params(it.args);
     j.gbuf = it.gbuf;
     j.dd = reinterpret_cast<float4*>(it.dd);
     j.ds = reinterpret_cast<float4*>(it.ds);
     j.id = reinterpret_cast<float4*>(it.id);
     j.is = reinterpret_cast<float4*>(it.is);
     j.pix_begin = t->total_pix;
-    j.task_begin = t->total_tasks;
+    j.unit_begin = t->total_units;
     t->total_pix += j.p.W * j.p.H;
-    t->total_tasks += j.p.tasks;
+    t->total_units += (long long)j.p.W * j.p.H * j.p.K;
     t->jobs.push_back(j);
   }
 }
 
-// Launch sequence of a batch: reset the task counter, primary kernel over
-// every pixel of every job, then the persistent path kernel. With `ctr`
-// the counting build runs (same images, plus visit counters).
-static cudaError_t launch_jobs(const void* d_jobs, int njobs, int total_pix, int total_tasks, unsigned int* d_next,
-                        int* d_status, void* d_ctr, cudaStream_t stream, cudaEvent_t* ev) {
-  const Job* jobs = static_cast<const Job*>(d_jobs);
-  Counters* ctr = static_cast<Counters*>(d_ctr);
-  cudaError_t e = cudaMemsetAsync(d_next, 0, sizeof(unsigned int), stream);
+static cudaError_t launch_init(BatchState* b, cudaStream_t st, Counters* ctr) {
+  const int nj = (int)b->table.jobs.size(), tp = b->table.total_pix;
+  cudaError_t e = cudaMemsetAsync(b->d_ctl, 0, sizeof(Ctl), st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->pool.ph, 0, sizeof(int4) * (size_t)b->pool.W, st);
   if (e != cudaSuccess) return e;
-  if (ev) cudaEventRecord(ev[0], stream);
-  if (ctr) primary_kernel<true><<<(total_pix + 127) / 128, 128, 0, stream>>>(jobs, njobs, total_pix, d_status, ctr);
-  else primary_kernel<false><<<(total_pix + 127) / 128, 128, 0, stream>>>(jobs, njobs, total_pix, d_status, ctr);
+  if (ctr) primary_kernel<true><<<(tp + 127) / 128, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
+  else primary_kernel<false><<<(tp + 127) / 128, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_iteration(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t* ev = nullptr) {
+  const int nj = (int)b->table.jobs.size();
+  cudaError_t e = cudaMemsetAsync(b->d_ctl, 0, offsetof(Ctl, pad0), st);
+  if (e != cudaSuccess) return e;
+  if (ev) cudaEventRecord(ev[0], st);
+  const int lb = (b->pool.W + 127) / 128;
+  if (ctr)
+    logic_kernel<true><<<lb, 128, 0, st>>>(b->d_jobs, nj, b->pool, b->d_ctl, b->table.total_units, b->d_parts,
+                                           b->d_status, ctr);
+  else
+    logic_kernel<false><<<lb, 128, 0, st>>>(b->d_jobs, nj, b->pool, b->d_ctl, b->table.total_units, b->d_parts,
+                                            b->d_status, ctr);
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (ev) cudaEventRecord(ev[1], stream);
-  int blocks = device_sms() * path_blocks_per_sm();
-  int need = (total_tasks + 3) / 4;
-  if (need < blocks) blocks = need < 1 ? 1 : need;
-  if (ctr) path_kernel<true><<<blocks, 128, 0, stream>>>(jobs, njobs, total_tasks, d_next, d_status, ctr);
-  else path_kernel<false><<<blocks, 128, 0, stream>>>(jobs, njobs, total_tasks, d_next, d_status, ctr);
-  if ((e = cudaGetLastError()) != cudaSuccess) return e;
-  if (ev) cudaEventRecord(ev[2], stream);
-  return cudaSuccess;
+  if (ev) cudaEventRecord(ev[1], st);
+  int tb = device_sms() * (ctr ? blocks_per_sm(qtrace_kernel<false, true>) : blocks_per_sm(qtrace_kernel<false, false>));
+  if (tb > lb) tb = lb;
+  if (ctr) {
+    qtrace_kernel<false, true><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->d_ctl, b->d_status, ctr);
+    qtrace_kernel<true, true><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->d_ctl, b->d_status, ctr);
+  } else {
+    qtrace_kernel<false, false><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->d_ctl, b->d_status, ctr);
+    qtrace_kernel<true, false><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->d_ctl, b->d_status, ctr);
+  }
+  if (ev) cudaEventRecord(ev[3], st);
+  return cudaGetLastError();
+}
+
+static cudaError_t launch_finalize(BatchState* b, cudaStream_t st) {
+  const int nj = (int)b->table.jobs.size(), tp = b->table.total_pix;
+  finalize_kernel<<<(tp + 127) / 128, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_parts);
+  return cudaGetLastError();
+}
+
+template <class F>
+static cudaError_t capture(cudaStream_t cs, F&& body, cudaGraphExec_t* out) {
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t le = body();
+  e = cudaStreamEndCapture(cs, &g);
+  if (e == cudaSuccess) e = le;
+  if (e == cudaSuccess) e = cudaGraphInstantiate(out, g, 0);
+  if (g) cudaGraphDestroy(g);
+  return e;
+}
+
+// The whole render: init (counters, pool, G-buffer), iterations in chunks
+// until every worker has retired, finalize. The host reads the live-worker
+// count after each chunk; kMaxIterations bounds the loop.
+struct KernelTimes {
+  double logic_ms = 0.0, trace_ms = 0.0;
+  long long iterations = 0;
+  cudaEvent_t e[kIterationsPerChunk][4] = {};
+};
+
+static rmn_status run(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t* ev, KernelTimes* kt = nullptr) {
+  const bool graph = b->use_graph && !ctr && !kt;
+  cudaError_t e;
+  if (ev) cudaEventRecord(ev[0], st);
+  e = graph ? cudaGraphLaunch(b->init_exec, st) : launch_init(b, st, ctr);
+  if (e != cudaSuccess) return cuda_fail(e, "render init");
+  if (ev) cudaEventRecord(ev[1], st);
+  Ctl h{};
+  h.live = 1;
+  unsigned int last_live = 0xffffffffu;
+  unsigned long long last_next = 0;
+  int stalled = 0;
+  long long iters = 0;
+  while (h.live) {
+    if (graph) {
+      e = cudaGraphLaunch(b->chunk_exec, st);
+    } else {
+      for (int k = 0; k < kIterationsPerChunk && e == cudaSuccess; ++k)
+        e = launch_iteration(b, st, ctr, kt ? kt->e[k] : nullptr);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "render iteration");
+    iters += kIterationsPerChunk;
+    e = cudaMemcpyAsync(&h, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(e, "render iteration");
+    if (kt) {
+      for (int k = 0; k < kIterationsPerChunk; ++k) {
+        float a = 0.0f, c = 0.0f;
+        cudaEventElapsedTime(&a, kt->e[k][0], kt->e[k][1]);
+        cudaEventElapsedTime(&c, kt->e[k][1], kt->e[k][3]);
+        kt->logic_ms += a;
+        kt->trace_ms += c;
+      }
+      kt->iterations += kIterationsPerChunk;
+    }
+    // Every iteration answers every queued ray, so a chunk that neither
+    // retires a worker nor hands out a unit is only possible while paths are
+    // long; 4096 such chunks in a row (>32k bounces) means no progress.
+    if (h.live == last_live && h.next_unit == last_next) {
+      if (++stalled > 4096) return fail(RMN_ERR_DEVICE_LIMIT, "render: no progress over 32768 iterations");
+    } else {
+      stalled = 0;
+    }
+    last_live = h.live;
+    last_next = h.next_unit;
+    if (iters > kMaxIterations) return fail(RMN_ERR_DEVICE_LIMIT, "render: iteration bound reached");
+  }
+  e = graph ? cudaGraphLaunch(b->fin_exec, st) : launch_finalize(b, st);
+  if (e != cudaSuccess) return cuda_fail(e, "render finalize");
+  if (ev) cudaEventRecord(ev[2], st);
+  return RMN_OK;
+}
+
+void batch_destroy(BatchState* b) {
+  if (!b) return;
+  if (b->init_exec) cudaGraphExecDestroy(b->init_exec);
+  if (b->chunk_exec) cudaGraphExecDestroy(b->chunk_exec);
+  if (b->fin_exec) cudaGraphExecDestroy(b->fin_exec);
+  for (void* p : b->allocs) cudaFree(p);
+  delete b;
 }
 
 rmn_status batch_create(const RenderItem* items, int n, bool use_graph, cudaStream_t st, BatchState** out) {
   *out = nullptr;
   BatchState* b = new BatchState();
   build_jobs(items, n, &b->table);
+  b->use_graph = use_graph;
+  long long W = std::min<long long>(b->table.total_units, kDefaultPoolWorkers);
+  if (W < 1) W = 1;
+  W = (W + 127) / 128 * 128;
+  Pool& P = b->pool;
+  P.W = (int)W;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](void** p, size_t bytes) {
+    if (e != cudaSuccess) return;
+    e = cudaMalloc(p, bytes ? bytes : 16);
+    if (e == cudaSuccess) b->allocs.push_back(*p);
+  };
   const size_t jb = sizeof(Job) * b->table.jobs.size();
-  cudaError_t e = cudaMalloc(&b->d_jobs, jb);
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_next, sizeof(unsigned int));
-  if (e == cudaSuccess) e = cudaMalloc(&b->d_status, sizeof(int));
+  alloc((void**)&b->d_jobs, jb);
+  alloc((void**)&b->d_ctl, sizeof(Ctl));
+  alloc((void**)&b->d_status, sizeof(int));
+  alloc((void**)&b->d_parts, sizeof(float4) * RMN_PART_F4 * (size_t)b->table.total_units);
+  alloc((void**)&P.unit, sizeof(int4) * W);
+  alloc((void**)&P.ph, sizeof(int4) * W);
+  alloc((void**)&P.uid, sizeof(long long) * W);
+  alloc((void**)&P.ro, sizeof(float4) * W);
+  alloc((void**)&P.rd, sizeof(float4) * W);
+  alloc((void**)&P.res, sizeof(float2) * W);
+  alloc((void**)&P.pa, sizeof(float4) * W);
+  alloc((void**)&P.pb, sizeof(float4) * W);
+  alloc((void**)&P.nv, sizeof(float4) * 5 * W);
+  alloc((void**)&P.lw, sizeof(float4) * 2 * W);
+  alloc((void**)&P.nk, sizeof(int4) * W);
+  alloc((void**)&P.pend, sizeof(float4) * 2 * W);
+  alloc((void**)&P.qc, sizeof(int) * W);
+  alloc((void**)&P.qs, sizeof(int) * W);
   if (e == cudaSuccess) e = cudaMemcpy(b->d_jobs, b->table.jobs.data(), jb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(b->d_status, 0, sizeof(int));
   if (e == cudaSuccess && use_graph) {
     cudaStream_t cs;
     e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
     if (e == cudaSuccess) {
-      e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-      if (e == cudaSuccess) {
-        cudaError_t le = launch_jobs(b->d_jobs, (int)b->table.jobs.size(), b->table.total_pix, b->table.total_tasks,
-                                     b->d_next, b->d_status, nullptr, cs, nullptr);
-        e = cudaStreamEndCapture(cs, &b->graph);
-        if (e == cudaSuccess) e = le;
-      }
-      if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, b->graph, 0);
+      e = capture(cs, [&] { return launch_init(b, cs, nullptr); }, &b->init_exec);
+      if (e == cudaSuccess)
+        e = capture(cs,
+                    [&] {
+                      for (int k = 0; k < kIterationsPerChunk; ++k) {
+                        cudaError_t le = launch_iteration(b, cs, nullptr);
+                        if (le != cudaSuccess) return le;
+                      }
+                      return cudaSuccess;
+                    },
+                    &b->chunk_exec);
+      if (e == cudaSuccess) e = capture(cs, [&] { return launch_finalize(b, cs); }, &b->fin_exec);
       cudaStreamDestroy(cs);
     }
   }
@@ -589,14 +1038,7 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, cudaStre
   return RMN_OK;
 }
 
-rmn_status batch_launch(BatchState* b, cudaStream_t st) {
-  cudaError_t e;
-  if (b->exec) e = cudaGraphLaunch(b->exec, st);
-  else
-    e = launch_jobs(b->d_jobs, (int)b->table.jobs.size(), b->table.total_pix, b->table.total_tasks, b->d_next,
-                    b->d_status, nullptr, st, nullptr);
-  return e == cudaSuccess ? RMN_OK : cuda_fail(e, "batch launch");
-}
+rmn_status batch_launch(BatchState* b, cudaStream_t st) { return run(b, st, nullptr, nullptr); }
 
 rmn_status batch_status(BatchState* b, cudaStream_t st) {
   int h = 0;
@@ -608,28 +1050,39 @@ rmn_status batch_status(BatchState* b, cudaStream_t st) {
 }
 
 // Counting run (visit counters) followed by a timed run with CUDA events
-// around each kernel on `st`. Both produce the same images as batch_launch.
+// around the G-buffer kernel and around the iterations + finalize. Both
+// produce the same images as batch_launch.
 rmn_status batch_profile(BatchState* b, cudaStream_t st, RenderProfileData* prof) {
   Counters* d_ctr = nullptr;
   cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
   cudaError_t e = cudaMalloc(&d_ctr, sizeof(Counters));
   if (e == cudaSuccess) e = cudaMemsetAsync(d_ctr, 0, sizeof(Counters), st);
   for (int k = 0; k < 3 && e == cudaSuccess; ++k) e = cudaEventCreate(&ev[k]);
-  const int nj = (int)b->table.jobs.size();
-  if (e == cudaSuccess)
-    e = launch_jobs(b->d_jobs, nj, b->table.total_pix, b->table.total_tasks, b->d_next, b->d_status, d_ctr, st,
-                    nullptr);
-  if (e == cudaSuccess)
-    e = launch_jobs(b->d_jobs, nj, b->table.total_pix, b->table.total_tasks, b->d_next, b->d_status, nullptr, st, ev);
+  rmn_status r = e == cudaSuccess ? RMN_OK : cuda_fail(e, "render profile");
+  KernelTimes kt;
+  for (int k = 0; k < kIterationsPerChunk && r == RMN_OK; ++k)
+    for (int j = 0; j < 4 && r == RMN_OK; ++j)
+      if (cudaEventCreate(&kt.e[k][j]) != cudaSuccess) r = fail(RMN_ERR_CUDA, "cudaEventCreate");
+  if (r == RMN_OK) r = run(b, st, d_ctr, nullptr);
+  if (r == RMN_OK) r = run(b, st, nullptr, ev, &kt);
+  for (int k = 0; k < kIterationsPerChunk; ++k)
+    for (int j = 0; j < 4; ++j)
+      if (kt.e[k][j]) cudaEventDestroy(kt.e[k][j]);
   Counters h{};
-  if (e == cudaSuccess) e = cudaMemcpyAsync(&h, d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e == cudaSuccess) {
+  if (r == RMN_OK) {
+    e = cudaMemcpyAsync(&h, d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) r = cuda_fail(e, "render profile");
+  }
+  if (r == RMN_OK) {
     float a = 0.0f, c = 0.0f;
     cudaEventElapsedTime(&a, ev[0], ev[1]);
     cudaEventElapsedTime(&c, ev[1], ev[2]);
     prof->primary_ms = a;
     prof->path_ms = c;
+    prof->logic_ms = kt.logic_ms;
+    prof->trace_ms = kt.trace_ms;
+    prof->iterations = kt.iterations;
     prof->closest = h.closest;
     prof->shadow = h.shadow;
     prof->inner = h.inner;
@@ -641,17 +1094,7 @@ rmn_status batch_profile(BatchState* b, cudaStream_t st, RenderProfileData* prof
   for (int k = 0; k < 3; ++k)
     if (ev[k]) cudaEventDestroy(ev[k]);
   if (d_ctr) cudaFree(d_ctr);
-  return e == cudaSuccess ? RMN_OK : cuda_fail(e, "render profile");
-}
-
-void batch_destroy(BatchState* b) {
-  if (!b) return;
-  if (b->exec) cudaGraphExecDestroy(b->exec);
-  if (b->graph) cudaGraphDestroy(b->graph);
-  if (b->d_jobs) cudaFree(b->d_jobs);
-  if (b->d_next) cudaFree(b->d_next);
-  if (b->d_status) cudaFree(b->d_status);
-  delete b;
+  return r;
 }
 
 }  // namespace rmn

@@ -44,11 +44,12 @@ struct RenderItem {
   float *gbuf, *dd, *ds, *id, *is;
 };
 struct RenderProfileData {
-  double primary_ms, path_ms;
+  double primary_ms, path_ms, logic_ms, trace_ms;
+  long long iterations;
   unsigned long long closest, shadow, inner, leaves, tris, slots, pixels;
 };
 struct BatchState;
-int default_lanes_per_pixel(int64_t batch_pixels, int spp);
+
 rmn_status batch_create(const RenderItem* items, int n, bool use_graph, cudaStream_t st, BatchState** out);
 rmn_status batch_launch(BatchState* b, cudaStream_t st);
 rmn_status batch_status(BatchState* b, cudaStream_t st);

@@ -280,9 +280,15 @@ RMN_D bool light_weights(const DevScene& s, const Surf& sf, float3 V, float* w, 
   return tot != 0.0f;
 }
 
-template <bool COUNT>
-RMN_D bool light_sample(const DevScene& s, const Surf& sf, float3 V, const float* w, float tot, int cnt, RmnRng& rng,
-                        LSample& out, int* status, TraceCounters* tc) {
+// One sample T of sampleDirectLight (src/sampling.cpp:467-527) up to its
+// shadow test: draws the light (or sky texel), the point and the rejection
+// loop, and returns the shadow ray (from sf.pos along `dir`, occluded iff a
+// hit lies nearer than `aim`) together with the sample the reference keeps
+// if that ray is unoccluded (bsdf value clamped at luminance 64, light,
+// weight). Returns false when the sample is dropped before any shadow test.
+// Light weights `w` / `tot` come from light_weights (light mode only).
+RMN_D bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float* w, float tot, int cnt, RmnRng& rng,
+                     float3& dir, float& aim, LSample& out) {
   const float3 pos = sf.pos;
   if (s.sky_w == 0) {
     float rv = tot * rng.next();  // sample(), :396-404
@@ -322,15 +328,10 @@ RMN_D bool light_sample(const DevScene& s, const Surf& sf, float3 V, const float
       fails++;
     }
     if (!any_finite3(lp)) return false;
-    float3 ld = norm3(lp - pos);
+    dir = norm3(lp - pos);
     float dist = len3(lp - pos);
-    TRay r = make_tray(pos, ld);
-    float aim = dist - RMN_EPS;
-    float tmax = aim + RMN_EPS;
-    int h = trace<true, COUNT>(s, r, RMN_EPS, tmax, aim, tc);
-    if (h == -2) atomicExch(status, 1);
-    if (!(tmax >= aim)) return false;
-    float3 f = brdf(sf, V, ld);
+    aim = dist - RMN_EPS;
+    float3 f = brdf(sf, V, dir);
     lum_clamp(f);
     out.bsdf = f;
     out.light = 2.0f * RMN_PI * lc.w * f3(lcol) / (dist * dist + 1e-3f) / pl;
@@ -347,21 +348,17 @@ RMN_D bool light_sample(const DevScene& s, const Surf& sf, float3 V, const float
     float phi = RMN_PI * (float(v) + 0.5f) / float(s.sky_h);
     float th = 2.0f * RMN_PI * (float(u) + 0.5f) / float(s.sky_w);
     float sp = sinf(phi), cp = cosf(phi), st = sinf(th), ct = cosf(th);
-    float3 dir = f3(-sp * st, cp, sp * ct);
-    if (dot3(dir, sf.surfN) > 0.0f) {
+    float3 d = f3(-sp * st, cp, sp * ct);
+    if (dot3(d, sf.surfN) > 0.0f) {
       float pr = __ldg(s.sky_prefix + p);
       if (p > 0) pr -= __ldg(s.sky_prefix + p - 1);
       float pdf = pr / total;
-      float3 light = f3(__ldg(s.sky + p)) / pdf;
-      TRay r = make_tray(pos, dir);
-      float tmax = INFINITY;
-      int h = trace<true, COUNT>(s, r, RMN_EPS, tmax, INFINITY, tc);
-      if (h == -2) atomicExch(status, 1);
-      if (!(tmax >= INFINITY)) return false;
-      float3 f = brdf(sf, V, dir);
+      dir = d;
+      aim = INFINITY;
+      float3 f = brdf(sf, V, d);
       lum_clamp(f);
       out.bsdf = f;
-      out.light = light;
+      out.light = f3(__ldg(s.sky + p)) / pdf;
       out.weight = 1.0f / (float)cnt;
       return true;
     }

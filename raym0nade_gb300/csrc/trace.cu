@@ -2,51 +2,74 @@
 // occlusion (Model::rayHit_test, src/model.cpp:343-354) over ray batches in
 // HBM.
 //
-// Work distribution: a persistent grid (a multiple of the SM count) whose
-// warps claim 32-ray batches from a global counter, so warps that drew short
-// rays move on instead of idling while long rays of a static partition
-// finish.
+// Work distribution: a persistent grid (a multiple of the SM count). Each
+// lane owns one ray at a time; every 16 node visits the lanes whose ray is
+// answered take new rays from a global counter (one warp-aggregated atomic),
+// so a warp no longer waits for its longest ray (Aila & Laine, "Understanding
+// the efficiency of ray traversal on GPUs", HPG 2009: persistent threads with
+// dynamic ray fetch).
 #include "rmn_host.h"
 #include "trace.cuh"
 
 namespace {
 
-__device__ __forceinline__ float int_float(int i) { return __int_as_float(i); }
+constexpr int kFetchBudget = 16;  // node visits between refill checks
 
 template <bool SHADOW>
 __global__ void __launch_bounds__(128) trace_kernel(DevScene s, const float4* __restrict__ rays, int64_t n,
                                                     float4* __restrict__ hits, uint8_t* __restrict__ occ,
                                                     unsigned long long* __restrict__ next, int* status) {
   const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  bool active = false, retired = false;
+  int64_t i = 0;
+  TRay r;
+  float tmin = 0.0f, aim = 0.0f;
+  Trav t;
   for (;;) {
-    unsigned long long base = 0;
-    if (lane == 0) base = atomicAdd(next, 32ULL);
-    base = __shfl_sync(0xffffffffu, base, 0);
-    if (base >= (unsigned long long)n) return;
-    int64_t i = (int64_t)base + lane;
-    if (i >= n) continue;
-    float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
-    TRay r = make_tray(f3(r0.x, r0.y, r0.z), f3(r1.x, r1.y, r1.z));
-    if (SHADOW) {
-      // HitRecord(eps, aimDepth + eps); occluded iff the hit is nearer than aimDepth.
-      float aim = r1.w;
-      float tmax = aim + RMN_EPS;
-      int h = trace<true, false>(s, r, RMN_EPS, tmax, aim, nullptr);
-      if (h == -2) atomicExch(status, (int)rmn::kDevStackOverflow);
-      occ[i] = (tmax >= aim) ? 0 : 1;
-    } else {
-      float tmax = r1.w;
-      int h = trace<false, false>(s, r, r0.w, tmax, 0.0f, nullptr);
-      if (h == -2) atomicExch(status, (int)rmn::kDevStackOverflow);
-      if (h < 0) {
-        hits[i] = make_float4(int_float(-1), tmax, 0.0f, 0.0f);
-      } else {
-        const float4* t = s.tri + 3 * h;
-        float4 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2);
-        float3 bc = bary(f3(a), f3(b), f3(c), r.o + r.d * tmax);
-        hits[i] = make_float4(a.w, tmax, bc.y, bc.z);
+    // lanes without a ray take the next ones from the batch
+    unsigned need = __ballot_sync(0xffffffffu, !active && !retired);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(next, (unsigned long long)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!active && !retired) {
+        i = (int64_t)(base + __popc(need & lt));
+        if (i < n) {
+          float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
+          r = make_tray(f3(r0.x, r0.y, r0.z), f3(r1.x, r1.y, r1.z));
+          if (SHADOW) {
+            // HitRecord(eps, aimDepth + eps); occluded iff nearer than aimDepth.
+            tmin = RMN_EPS;
+            aim = r1.w;
+            trav_begin(s, t, aim + RMN_EPS);
+          } else {
+            tmin = r0.w;
+            trav_begin(s, t, r1.w);
+          }
+          active = true;
+        } else {
+          retired = true;
+        }
       }
     }
+    if (__ballot_sync(0xffffffffu, active) == 0) return;
+    if (!active) continue;
+    int st = trav_run<SHADOW, false>(s, r, tmin, aim, t, kFetchBudget, nullptr);
+    if (st == 0) continue;
+    if (st == -2) atomicExch(status, (int)rmn::kDevStackOverflow);
+    if (SHADOW) {
+      occ[i] = (t.tmax >= aim) ? 0 : 1;
+    } else if (t.hit < 0) {
+      hits[i] = make_float4(__int_as_float(-1), t.tmax, 0.0f, 0.0f);
+    } else {
+      const float4* tp = s.tri + 3 * t.hit;
+      float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+      float3 bc = bary(f3(a), f3(b), f3(c), r.o + r.d * t.tmax);
+      hits[i] = make_float4(a.w, t.tmax, bc.y, bc.z);
+    }
+    active = false;
   }
 }
 

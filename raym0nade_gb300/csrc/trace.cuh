@@ -81,31 +81,44 @@ struct TraceCounters {
   uint32_t closest, shadow, inner, leaves, tris;
 };
 
-// Closest hit in (tmin, tmax). Returns the leaf-order triangle index or -1;
-// tmax becomes the hit distance. With ANY set, returns as soon as a hit
-// closer than `aim` is recorded (Model::rayHit_test's question, answered
-// after the same visits as the full query up to that point).
-// Returns -2 if the stack would overflow (never for trees the builder accepts).
-template <bool ANY, bool COUNT>
-RMN_D int trace(const DevScene& s, const TRay& r, float tmin, float& tmax, float aim, TraceCounters* cnt) {
-  int hit = -1;
+// Resumable traversal state: the deferred children (reference plus entry
+// distance) and the current node, so a warp can hand a lane a new ray while
+// its other lanes are still traversing.
+struct Trav {
+  int cur;   // next node reference to visit
+  int sp;
+  int hit;   // leaf-order triangle index of the closest hit so far, -1 none
+  float tmax;
   int stack_ref[RMN_STACK];
   float stack_tl[RMN_STACK];
-  int sp = 0;
-  int cur = s.root;
-  if (COUNT) {
-    if (ANY) cnt->shadow++;
-    else cnt->closest++;
-  }
+};
+
+RMN_D void trav_begin(const DevScene& s, Trav& t, float tmax) {
+  t.cur = s.root;
+  t.sp = 0;
+  t.hit = -1;
+  t.tmax = tmax;
+}
+
+// Visits up to `budget` nodes (an inner node or a whole leaf counts one).
+// Returns 1 when the query is answered (t.hit / t.tmax final), 0 when the
+// budget ran out first, -2 if the stack would overflow (never for trees the
+// builder accepts). With ANY set, answers as soon as a hit closer than `aim`
+// is recorded (Model::rayHit_test's question, after the same visits as the
+// closest-hit query up to that point).
+template <bool ANY, bool COUNT>
+RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav& t, int budget, TraceCounters* cnt) {
   for (;;) {
+    if (budget-- <= 0) return 0;
+    int cur = t.cur;
     if (cur >= 0) {
       const DevNode* n = s.nodes + cur;
       float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
       int4 D = __ldg(&n->d);
       if (COUNT) cnt->inner++;
       float tl0, tl1;
-      bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, tmax, tl0);
-      bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, tmax, tl1);
+      bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, t.tmax, tl0);
+      bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, t.tmax, tl1);
       int nref, fref;
       bool hn, hf;
       float tlf;
@@ -116,16 +129,16 @@ RMN_D int trace(const DevScene& s, const TRay& r, float tmin, float& tmax, float
       }
       if (hn) {
         if (hf) {
-          if (sp >= RMN_STACK) return -2;
-          stack_ref[sp] = fref;
-          stack_tl[sp] = tlf;
-          ++sp;
+          if (t.sp >= RMN_STACK) return -2;
+          t.stack_ref[t.sp] = fref;
+          t.stack_tl[t.sp] = tlf;
+          ++t.sp;
         }
-        cur = nref;
+        t.cur = nref;
         continue;
       }
-      if (hf && tlf < tmax) {
-        cur = fref;
+      if (hf && tlf < t.tmax) {
+        t.cur = fref;
         continue;
       }
     } else {
@@ -133,27 +146,42 @@ RMN_D int trace(const DevScene& s, const TRay& r, float tmin, float& tmax, float
       int first = x >> 4, count = x & 15;
       if (COUNT) { cnt->leaves++; cnt->tris += count; }
       for (int i = first; i < first + count; ++i) {
-        const float4* t = s.tri + 3 * i;
-        float4 a = __ldg(t), b = __ldg(t + 1), c = __ldg(t + 2);
+        const float4* tp = s.tri + 3 * i;
+        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
         float th = tri_t(r, f3(a), f3(b), f3(c), b.w);
-        if (tmin < th && th < tmax) {
-          tmax = th;
-          hit = i;
-          if (ANY && th < aim) return hit;
+        if (tmin < th && th < t.tmax) {
+          t.tmax = th;
+          t.hit = i;
+          if (ANY && th < aim) return 1;
         }
       }
     }
     // pop: the deferred child is visited only if it still starts before the
     // current closest hit
     for (;;) {
-      if (sp == 0) return hit;
-      --sp;
-      if (stack_tl[sp] < tmax) {
-        cur = stack_ref[sp];
+      if (t.sp == 0) return 1;
+      --t.sp;
+      if (t.stack_tl[t.sp] < t.tmax) {
+        t.cur = t.stack_ref[t.sp];
         break;
       }
     }
   }
+}
+
+// One whole query: closest hit in (tmin, tmax). Returns the leaf-order
+// triangle index or -1 (tmax becomes the hit distance), -2 on stack overflow.
+template <bool ANY, bool COUNT>
+RMN_D int trace(const DevScene& s, const TRay& r, float tmin, float& tmax, float aim, TraceCounters* cnt) {
+  Trav t;
+  trav_begin(s, t, tmax);
+  if (COUNT) {
+    if (ANY) cnt->shadow++;
+    else cnt->closest++;
+  }
+  int st = trav_run<ANY, COUNT>(s, r, tmin, aim, t, 0x7fffffff, cnt);
+  tmax = t.tmax;
+  return st == -2 ? -2 : t.hit;
 }
 
 // barycentric(v0, v1, v2, P), src/geometry.cpp:89-103, with e1 = v1 - v0 and

@@ -148,9 +148,10 @@ def _photo_from_records(rec):
     r = torch.from_numpy(rec.reshape(-1, 40)).cuda()
     p.radiance_Dd.copy_(r[:, 0:4]); p.radiance_Ds.copy_(r[:, 4:8])
     p.radiance_Id.copy_(r[:, 8:12]); p.radiance_Is.copy_(r[:, 12:16])
-    g = torch.zeros((h * w, 16), device="cuda")
+    g = torch.zeros((h * w, api.GBUFFER_FLOATS), device="cuda")
     g[:, 0:3] = r[:, 16:19]; g[:, 3:6] = r[:, 19:22]; g[:, 6:9] = r[:, 22:25]
     g[:, 9:12] = r[:, 25:28]; g[:, 12:15] = r[:, 28:31]; g[:, 15] = r[:, 31]
+    g[:, 16] = r[:, 32]; g[:, 17] = r[:, 33]; g[:, 18] = r[:, 35]; g[:, 19] = r[:, 36]
     p.Gbuffer.copy_(g)
     return p
 
