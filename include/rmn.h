@@ -212,6 +212,20 @@ rmn_status rmn_batch_destroy(rmn_batch* batch);
 rmn_status rmn_compose(const rmn_image* image, int32_t width, int32_t height, float exposure, int32_t options,
                        float* rgb, void* stream);
 
+/* rmn_compose without any device allocation. No counterpart in the
+ * reference. For callers that cannot allocate device memory (an engine whose
+ * arena allocator owns the device memory, or a frame loop that must not let
+ * cudaMalloc/cudaFree synchronise the device): the image between compose and
+ * FXAA lives in a fixed file-scope device array of RMN_NOALLOC_MAX_PIXELS
+ * pixels (24 MiB, held by every GPU that loads the library); larger images
+ * are rejected with RMN_ERR_INVALID_ARGUMENT. All buffers must be device
+ * memory. The first call on each device resolves the array's address
+ * (cudaGetSymbolAddress) and must come before any stream capture. Calls share
+ * the array: calls whose work overlaps on the GPU race. */
+#define RMN_NOALLOC_MAX_PIXELS (1 << 21)
+rmn_status rmn_compose_noalloc(const rmn_image* image, int32_t width, int32_t height, float exposure,
+                               int32_t options, float* rgb, void* stream);
+
 /* Photo::FXAA (src/image.cpp:363-452) on an rgb image (3 floats per pixel). */
 rmn_status rmn_fxaa(const float* rgb_in, float* rgb_out, int32_t width, int32_t height, void* stream);
 

@@ -76,6 +76,8 @@ SIGNATURES = {
     "rmn_batch_destroy": (C.c_int, [C.c_void_p]),
     "rmn_compose": (C.c_int, [C.POINTER(Image), C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p,
                               C.c_void_p]),
+    "rmn_compose_noalloc": (C.c_int, [C.POINTER(Image), C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p,
+                                      C.c_void_p]),
     "rmn_fxaa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
 }
 

@@ -94,6 +94,8 @@ struct Status {
 };
 }  // namespace
 
+bool is_device_pointer(const void* p) { return is_device_ptr(p); }
+
 rmn_status fail(rmn_status status, const char* fmt, ...) {
   va_list ap;
   va_start(ap, fmt);

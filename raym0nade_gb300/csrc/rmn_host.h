@@ -17,6 +17,7 @@ struct rmn_scene {
 namespace rmn {
 
 rmn_status fail(rmn_status status, const char* fmt, ...);
+bool is_device_pointer(const void* p);  // device or managed memory of the current context
 rmn_status cuda_fail(cudaError_t err, const char* what);
 void clear_error();
 
