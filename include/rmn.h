@@ -122,8 +122,9 @@ typedef struct rmn_render_args {
   int32_t width, height, spp, threads; /* threads: ignored on the GPU */
   int32_t max_depth;                   /* 16 in the reference (src/render.cpp:125); 1..16 */
   uint64_t seed;                       /* counter-based random stream key */
-  int32_t lanes_per_pixel;             /* 0: autotuned; else 1,2,4,8,16,32 */
-  int32_t reserved[3];
+  int32_t lanes_per_pixel;             /* work units per pixel (0: from slots_per_unit); 1..64 */
+  int32_t slots_per_unit;              /* sample slots per work unit (0: library default 16) */
+  int32_t reserved[2];
 } rmn_render_args;
 
 /* Caller-owned per-pixel outputs (width*height entries each, row-major).
@@ -140,6 +141,8 @@ typedef struct rmn_image {
   float* radiance_Id;
   float* radiance_Is;
   float* gbuffer;
+  int32_t* dropped; /* optional: per pixel, the indirect sample the firefly clamp
+                       (src/render.cpp:532-547) dropped, as slot * 8 + sample, or -1 */
 } rmn_image;
 #define RMN_GBUFFER_FLOATS 20
 
@@ -202,10 +205,52 @@ typedef struct rmn_batch_item {
   rmn_render_args args;
   rmn_image image;
 } rmn_batch_item;
-rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, int32_t use_graph, void* stream, rmn_batch** out);
+/* Launch knobs of a batch; NULL options = {1, 0}. */
+typedef struct rmn_batch_options {
+  int32_t use_graph;     /* replay the wavefront iterations from captured CUDA graphs */
+  int32_t pool_workers;  /* concurrent paths in flight (0: library default, 2^20) */
+  int32_t reserved[2];
+} rmn_batch_options;
+rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_batch_options* options, void* stream,
+                            rmn_batch** out);
 rmn_status rmn_batch_render(rmn_batch* batch, void* stream);
 rmn_status rmn_batch_profile(rmn_batch* batch, rmn_render_profile* out, void* stream);
 rmn_status rmn_batch_destroy(rmn_batch* batch);
+
+/* Project-written autotuner for batches. Times candidate launch
+ * configurations -- slots per work unit in {4, 8, 16, 32, 64} x worker pool
+ * in {2^18, 2^19, 2^20, 2^21} -- on a proxy of the batch whose images keep
+ * every item's scene, spp, depth and field of view but only `pixel_fraction`
+ * (0 < f <= 1) of its pixels, and returns the fastest. Set each item's
+ * slots_per_unit and the batch's pool_workers from the result. The images do
+ * not depend on the choice beyond float summation order. */
+typedef struct rmn_tune_result {
+  int32_t slots_per_unit, pool_workers;
+  double best_ms, default_ms;  /* proxy render time: best and library default */
+  int32_t candidates;
+  int32_t reserved;
+} rmn_tune_result;
+rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixel_fraction, rmn_tune_result* out,
+                              void* stream);
+
+/* Adjoint of rmn_render (path-replay backpropagation). No counterpart in the
+ * reference. Given a forward rmn_render of `scene` with `args` -- its
+ * G-buffer and its `dropped` record, both required in `image` -- and
+ * d_image = dL/dI for the linear composed image
+ *   I = base (*) (Dd + Id) + Ds + Is + emission * exposure
+ * (Photo::shade(Full), src/image.cpp:215-246; rmn_compose with
+ * RMN_SHADE_FULL and no gamma), 3 floats per pixel, writes
+ * d_materials[m * RMN_GRAD_PER_MATERIAL + k] = dL/d(parameter k of material
+ * m): k = 0..2 the base colour (rmn_material.base_color as resolved: white
+ * without a diffuse texel), 3 the roughness (as resolved), 4 the emission
+ * scale s (emission = s * rmn_material.emission, at s = 1). The paths are
+ * recomputed from the same random streams, so the gradient is that of the
+ * forward's own estimate; sampling that depends on the roughness enters by
+ * its score function (the estimate is unbiased, not the derivative of one
+ * realisation). Buffers may be host or device memory. */
+#define RMN_GRAD_PER_MATERIAL 5
+rmn_status rmn_adjoint(const rmn_scene* scene, const rmn_render_args* args, const rmn_image* image,
+                       const float* d_image, float* d_materials, void* stream);
 
 /* Photo::shade(options) [+ gammaCorrection] [+ FXAA] (src/image.cpp:215-246,
  * 454-479) over rmn_render's buffers -> rgb (3 floats per pixel). */

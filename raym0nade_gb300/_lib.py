@@ -39,12 +39,12 @@ class RenderArgs(C.Structure):
                 ("right", C.c_float * 3), ("accuracy", C.c_float), ("focus", C.c_float), ("CoC", C.c_float),
                 ("exposure", C.c_float), ("P_Direct", C.c_float), ("width", C.c_int32), ("height", C.c_int32),
                 ("spp", C.c_int32), ("threads", C.c_int32), ("max_depth", C.c_int32), ("seed", C.c_uint64),
-                ("lanes_per_pixel", C.c_int32), ("reserved", C.c_int32 * 3)]
+                ("lanes_per_pixel", C.c_int32), ("slots_per_unit", C.c_int32), ("reserved", C.c_int32 * 2)]
 
 
 class Image(C.Structure):
     _fields_ = [("radiance_Dd", C.c_void_p), ("radiance_Ds", C.c_void_p), ("radiance_Id", C.c_void_p),
-                ("radiance_Is", C.c_void_p), ("gbuffer", C.c_void_p)]
+                ("radiance_Is", C.c_void_p), ("gbuffer", C.c_void_p), ("dropped", C.c_void_p)]
 
 
 class RenderProfile(C.Structure):
@@ -58,6 +58,15 @@ class BatchItem(C.Structure):
     _fields_ = [("scene", C.c_void_p), ("args", RenderArgs), ("image", Image)]
 
 
+class BatchOptions(C.Structure):
+    _fields_ = [("use_graph", C.c_int32), ("pool_workers", C.c_int32), ("reserved", C.c_int32 * 2)]
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("slots_per_unit", C.c_int32), ("pool_workers", C.c_int32), ("best_ms", C.c_double),
+                ("default_ms", C.c_double), ("candidates", C.c_int32), ("reserved", C.c_int32)]
+
+
 # name -> (restype, argtypes); every declaration of include/rmn.h.
 SIGNATURES = {
     "rmn_last_error": (C.c_char_p, []),
@@ -68,9 +77,13 @@ SIGNATURES = {
     "rmn_trace_closest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "rmn_trace_shadow": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "rmn_render": (C.c_int, [C.c_void_p, C.POINTER(RenderArgs), C.POINTER(Image), C.c_void_p]),
+    "rmn_adjoint": (C.c_int, [C.c_void_p, C.POINTER(RenderArgs), C.POINTER(Image), C.c_void_p, C.c_void_p,
+                              C.c_void_p]),
     "rmn_render_profile_get": (C.c_int, [C.c_void_p, C.POINTER(RenderArgs), C.POINTER(Image),
                                          C.POINTER(RenderProfile), C.c_void_p]),
-    "rmn_batch_create": (C.c_int, [C.POINTER(BatchItem), C.c_int32, C.c_int32, C.c_void_p, C.POINTER(C.c_void_p)]),
+    "rmn_batch_create": (C.c_int, [C.POINTER(BatchItem), C.c_int32, C.POINTER(BatchOptions), C.c_void_p,
+                                   C.POINTER(C.c_void_p)]),
+    "rmn_batch_autotune": (C.c_int, [C.POINTER(BatchItem), C.c_int32, C.c_float, C.POINTER(TuneResult), C.c_void_p]),
     "rmn_batch_render": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rmn_batch_profile": (C.c_int, [C.c_void_p, C.POINTER(RenderProfile), C.c_void_p]),
     "rmn_batch_destroy": (C.c_int, [C.c_void_p]),

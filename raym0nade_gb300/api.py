@@ -165,12 +165,14 @@ class RenderArgs:
     max_depth: int = 16
     seed: int = 1
     lanes_per_pixel: int = 0
+    slots_per_unit: int = 0
 
     @staticmethod
-    def from_camera(cam: "_scenes.Camera", seed: int = 1, savePath: str = "", lanes_per_pixel: int = 0):
+    def from_camera(cam: "_scenes.Camera", seed: int = 1, savePath: str = "", lanes_per_pixel: int = 0,
+                    slots_per_unit: int = 0):
         return RenderArgs(cam.position, cam.direction, cam.up, cam.right, cam.accuracy, cam.focus, cam.coc,
                           cam.exposure, cam.p_direct, cam.width, cam.height, cam.spp, 1, savePath, cam.max_depth,
-                          seed, lanes_per_pixel)
+                          seed, lanes_per_pixel, slots_per_unit)
 
     def c(self) -> "_lib.RenderArgs":
         a = _lib.RenderArgs()
@@ -181,6 +183,7 @@ class RenderArgs:
                                                                float(self.P_Direct))
         a.width, a.height, a.spp, a.threads = int(self.width), int(self.height), int(self.spp), int(self.threads)
         a.max_depth, a.seed, a.lanes_per_pixel = int(self.max_depth), int(self.seed), int(self.lanes_per_pixel)
+        a.slots_per_unit = int(self.slots_per_unit)
         return a
 
 
@@ -211,14 +214,16 @@ class Photo:
         n = width * height
         if device and torch is not None and torch.cuda.is_available():
             mk = lambda k: torch.zeros((n, k), dtype=torch.float32, device="cuda")
+            self.dropped = torch.full((n,), -1, dtype=torch.int32, device="cuda")
         else:
             mk = lambda k: np.zeros((n, k), np.float32)
+            self.dropped = np.full((n,), -1, np.int32)
         self.radiance_Dd, self.radiance_Ds, self.radiance_Id, self.radiance_Is = mk(4), mk(4), mk(4), mk(4)
         self.Gbuffer = mk(GBUFFER_FLOATS)
 
     def c_image(self) -> "_lib.Image":
         return _lib.Image(_ptr(self.radiance_Dd), _ptr(self.radiance_Ds), _ptr(self.radiance_Id),
-                          _ptr(self.radiance_Is), _ptr(self.Gbuffer))
+                          _ptr(self.radiance_Is), _ptr(self.Gbuffer), _ptr(getattr(self, "dropped", None)))
 
     def shade(self, options: int = Full, out=None, stream=None):
         """Photo::shade(options) [+ gammaCorrection with GAMMA] [+ FXAA with DoFXAA]."""
@@ -257,6 +262,27 @@ def render(model: Model, args: RenderArgs, photo: Photo | None = None, stream=No
     return photo
 
 
+GRAD_PER_MATERIAL = 5  # base colour r, g, b; roughness; emission scale
+
+
+def adjoint(model: Model, args: RenderArgs, photo: Photo, d_image, d_materials=None, stream=None):
+    """rmn_adjoint: dL/d(material parameters) for dL/dI of the linear composed
+    image of `photo` (a forward render of `model` with `args`). d_image:
+    (H*W, 3) float32; returns (num_materials, 5) float32 (base r, g, b,
+    roughness, emission scale), on the device when d_image is a CUDA tensor."""
+    n = model.info()["num_materials"]
+    if d_materials is None:
+        if torch is not None and isinstance(d_image, torch.Tensor):
+            d_materials = torch.zeros((n, GRAD_PER_MATERIAL), dtype=torch.float32, device=d_image.device)
+        else:
+            d_materials = np.zeros((n, GRAD_PER_MATERIAL), np.float32)
+    a = args.c()
+    img = photo.c_image()
+    _check(_lib.load().rmn_adjoint(model.handle, C.byref(a), C.byref(img), _ptr(d_image), _ptr(d_materials),
+                                   _stream(stream)), "rmn_adjoint")
+    return d_materials
+
+
 def render_profile(model: Model, args: RenderArgs, photo: Photo | None = None, stream=None):
     """rmn_render_profile_get: render twice (counting, then timed) and return
     (photo, dict of kernel times and visit counters)."""
@@ -270,21 +296,36 @@ def render_profile(model: Model, args: RenderArgs, photo: Photo | None = None, s
     return photo, {k: getattr(prof, k) for k, _ in prof._fields_}
 
 
+def _batch_items(items):
+    arr = (_lib.BatchItem * len(items))()
+    for i, (m, a, ph) in enumerate(items):
+        arr[i].scene = m.handle.value
+        arr[i].args = a.c()
+        arr[i].image = ph.c_image()
+    return arr
+
+
+def autotune(items, pixel_fraction: float = 1.0 / 16, stream=None) -> dict:
+    """rmn_batch_autotune over (Model, RenderArgs, Photo) items: the fastest
+    slots per unit and pool size on a proxy with `pixel_fraction` of the
+    pixels."""
+    res = _lib.TuneResult()
+    _check(_lib.load().rmn_batch_autotune(_batch_items(items), len(items), float(pixel_fraction), C.byref(res),
+                                          _stream(stream)), "rmn_batch_autotune")
+    return {k: getattr(res, k) for k, _ in res._fields_ if k != "reserved"}
+
+
 class Batch:
     """rmn_batch: many renders in one persistent launch, optionally replayed
     from a captured CUDA graph. Photos must live on the device."""
 
-    def __init__(self, items, use_graph: bool = True, stream=None):
+    def __init__(self, items, use_graph: bool = True, stream=None, pool_workers: int = 0):
         """items: list of (Model, RenderArgs, Photo)."""
         lib = _lib.load()
-        arr = (_lib.BatchItem * len(items))()
-        for i, (m, a, ph) in enumerate(items):
-            arr[i].scene = m.handle.value
-            arr[i].args = a.c()
-            arr[i].image = ph.c_image()
+        arr = _batch_items(items)
         h = C.c_void_p()
-        _check(lib.rmn_batch_create(arr, len(items), 1 if use_graph else 0, _stream(stream), C.byref(h)),
-               "rmn_batch_create")
+        opt = _lib.BatchOptions(1 if use_graph else 0, int(pool_workers))
+        _check(lib.rmn_batch_create(arr, len(items), C.byref(opt), _stream(stream), C.byref(h)), "rmn_batch_create")
         self._h = h
         self.items = items
 

@@ -2,7 +2,9 @@
 // error reporting around the kernels.
 #include <cstdarg>
 #include <cstdio>
+#include <cmath>
 #include <cstring>
+#include <algorithm>
 #include <new>
 #include <vector>
 
@@ -263,8 +265,9 @@ static rmn_status check_args(const rmn_render_args& a) {
   if (!(a.P_Direct >= 0.0f && a.P_Direct <= 1.0f)) return fail(RMN_ERR_INVALID_ARGUMENT, "P_Direct must lie in [0, 1]");
   if (a.max_depth < 1 || a.max_depth > 16) return fail(RMN_ERR_INVALID_ARGUMENT, "max_depth must lie in [1, 16]");
   int k = a.lanes_per_pixel;
-  if (k != 0 && (k < 1 || k > 32 || (k & (k - 1))))
-    return fail(RMN_ERR_INVALID_ARGUMENT, "lanes_per_pixel must be 0 or a power of two up to 32");
+  if (k < 0 || k > 64) return fail(RMN_ERR_INVALID_ARGUMENT, "lanes_per_pixel must lie in [0, 64]");
+  if (a.slots_per_unit < 0 || a.slots_per_unit > (1 << 20))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "slots_per_unit must lie in [0, 2^20]");
   return RMN_OK;
 }
 
@@ -281,8 +284,9 @@ static rmn_status render_one(rmn_scene* scene, const rmn_render_args* args, cons
   if (scene->dev.num_lights > 8) return fail(RMN_ERR_UNSUPPORTED, "more than 8 light objects");
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   const size_t npx = (size_t)a.width * a.height;
-  Arg dd, ds, id, is, gb;
+  Arg dd, ds, id, is, gb, dr;
   r = stage_out(image->radiance_Dd, npx * 16, st, &dd);
+  if (r == RMN_OK && image->dropped) r = stage_out(image->dropped, npx * 4, st, &dr);
   if (r == RMN_OK) r = stage_out(image->radiance_Ds, npx * 16, st, &ds);
   if (r == RMN_OK) r = stage_out(image->radiance_Id, npx * 16, st, &id);
   if (r == RMN_OK) r = stage_out(image->radiance_Is, npx * 16, st, &is);
@@ -298,8 +302,8 @@ static rmn_status render_one(rmn_scene* scene, const rmn_render_args* args, cons
   BatchState* b = nullptr;
   if (r == RMN_OK) {
     RenderItem it{scene, a, static_cast<float*>(gb.dev), static_cast<float*>(dd.dev), static_cast<float*>(ds.dev),
-                  static_cast<float*>(id.dev), static_cast<float*>(is.dev)};
-    r = batch_create(&it, 1, false, st, &b);
+                  static_cast<float*>(id.dev), static_cast<float*>(is.dev), static_cast<int*>(dr.dev)};
+    r = batch_create(&it, 1, false, 0, st, &b);
   }
   if (r == RMN_OK) r = prof ? batch_profile(b, st, prof) : batch_launch(b, st);
   if (r == RMN_OK) r = finish_out(image->radiance_Dd, npx * 16, st, dd);
@@ -307,8 +311,9 @@ static rmn_status render_one(rmn_scene* scene, const rmn_render_args* args, cons
   if (r == RMN_OK) r = finish_out(image->radiance_Id, npx * 16, st, id);
   if (r == RMN_OK) r = finish_out(image->radiance_Is, npx * 16, st, is);
   if (r == RMN_OK && image->gbuffer) r = finish_out(image->gbuffer, npx * RMN_GBUFFER_FLOATS * 4, st, gb);
+  if (r == RMN_OK && image->dropped) r = finish_out(image->dropped, npx * 4, st, dr);
   if (r == RMN_OK && b) r = batch_status(b, st);
-  for (Arg* x : {&dd, &ds, &id, &is, &gb}) release(*x, st);
+  for (Arg* x : {&dd, &ds, &id, &is, &gb, &dr}) release(*x, st);
   cudaError_t e = cudaStreamSynchronize(st);
   batch_destroy(b);
   if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
@@ -316,6 +321,35 @@ static rmn_status render_one(rmn_scene* scene, const rmn_render_args* args, cons
 }
 
 extern "C" {
+
+rmn_status rmn_adjoint(const rmn_scene* scene, const rmn_render_args* args, const rmn_image* image,
+                       const float* d_image, float* d_materials, void* stream) {
+  clear_error();
+  if (!scene || !args || !image || !d_image || !d_materials)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "NULL scene, args, image, d_image or d_materials");
+  if (!image->gbuffer || !image->dropped)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_adjoint needs the forward's G-buffer and dropped-sample record");
+  const rmn_render_args& a = *args;
+  rmn_status r = check_args(a);
+  if (r != RMN_OK) return r;
+  if (scene->dev.num_lights > 8) return fail(RMN_ERR_UNSUPPORTED, "more than 8 light objects");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t npx = (size_t)a.width * a.height;
+  const size_t nm = (size_t)scene->dev.num_mats * RMN_GRAD_PER_MATERIAL;
+  Arg gb, dr, di, dm;
+  r = stage_in(image->gbuffer, npx * RMN_GBUFFER_FLOATS * 4, st, &gb);
+  if (r == RMN_OK) r = stage_in(image->dropped, npx * 4, st, &dr);
+  if (r == RMN_OK) r = stage_in(d_image, npx * 12, st, &di);
+  if (r == RMN_OK) r = stage_out(d_materials, nm * 4, st, &dm);
+  if (r == RMN_OK)
+    r = launch_adjoint(scene, a, static_cast<const float*>(gb.dev), static_cast<const int*>(dr.dev),
+                       static_cast<const float*>(di.dev), static_cast<float*>(dm.dev), st);
+  if (r == RMN_OK) r = finish_out(d_materials, nm * 4, st, dm);
+  for (Arg* x : {&gb, &dr, &di, &dm}) release(*x, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
+  return r;
+}
 
 rmn_status rmn_render(rmn_scene* scene, const rmn_render_args* args, const rmn_image* image, void* stream) {
   return render_one(scene, args, image, stream, nullptr);
@@ -349,11 +383,31 @@ struct rmn_batch {
   BatchState* state = nullptr;
 };
 
-rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, int32_t use_graph, void* stream, rmn_batch** out) {
+static rmn_status make_items(const rmn_batch_item* items, int32_t n, std::vector<RenderItem>& its, bool device_only);
+
+rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_batch_options* options, void* stream,
+                            rmn_batch** out) {
   clear_error();
   if (!items || n <= 0 || !out) return fail(RMN_ERR_INVALID_ARGUMENT, "a batch needs at least one item");
   *out = nullptr;
+  rmn_batch_options opt = options ? *options : rmn_batch_options{1, 0, {0, 0}};
+  if (opt.pool_workers < 0) return fail(RMN_ERR_INVALID_ARGUMENT, "pool_workers must be >= 0");
   std::vector<RenderItem> its;
+  rmn_status r = make_items(items, n, its, true);
+  if (r != RMN_OK) return r;
+  rmn_batch* bt = new (std::nothrow) rmn_batch();
+  if (!bt) return fail(RMN_ERR_OUT_OF_MEMORY, "host allocation failed");
+  r = batch_create(its.data(), n, opt.use_graph != 0, opt.pool_workers, static_cast<cudaStream_t>(stream), &bt->state);
+  if (r != RMN_OK) {
+    delete bt;
+    return r;
+  }
+  *out = bt;
+  return RMN_OK;
+}
+
+static rmn_status make_items(const rmn_batch_item* items, int32_t n, std::vector<RenderItem>& its, bool device_only) {
+  its.clear();
   its.reserve(n);
   int64_t total = 0;
   for (int i = 0; i < n; ++i) {
@@ -365,22 +419,91 @@ rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, int32_t use_
     const rmn_image& im = b.image;
     for (const void* p : {(const void*)im.radiance_Dd, (const void*)im.radiance_Ds, (const void*)im.radiance_Id,
                           (const void*)im.radiance_Is, (const void*)im.gbuffer})
-      if (!is_device_ptr(p))
+      if (device_only && !is_device_ptr(p))
         return fail(RMN_ERR_INVALID_ARGUMENT, "batch item %d: batch buffers (all five) must be device memory", i);
     total += (int64_t)b.args.width * b.args.height;
     if (total > (1LL << 31) - 1) return fail(RMN_ERR_INVALID_ARGUMENT, "a batch holds at most 2^31 - 1 pixels");
+    if (im.dropped && device_only && !is_device_ptr(im.dropped))
+      return fail(RMN_ERR_INVALID_ARGUMENT, "batch item %d: batch buffers must be device memory", i);
     its.push_back(RenderItem{b.scene, b.args, im.gbuffer, im.radiance_Dd, im.radiance_Ds, im.radiance_Id,
-                             im.radiance_Is});
+                             im.radiance_Is, im.dropped});
   }
-  rmn_batch* bt = new (std::nothrow) rmn_batch();
-  if (!bt) return fail(RMN_ERR_OUT_OF_MEMORY, "host allocation failed");
-  rmn_status r = batch_create(its.data(), n, use_graph != 0, static_cast<cudaStream_t>(stream), &bt->state);
-  if (r != RMN_OK) {
-    delete bt;
-    return r;
-  }
-  *out = bt;
   return RMN_OK;
+}
+
+rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixel_fraction, rmn_tune_result* out,
+                              void* stream) {
+  clear_error();
+  if (!items || n <= 0 || !out) return fail(RMN_ERR_INVALID_ARGUMENT, "autotune needs at least one item and an output");
+  if (!(pixel_fraction > 0.0f && pixel_fraction <= 1.0f))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "pixel_fraction must lie in (0, 1]");
+  std::vector<RenderItem> its;
+  rmn_status r = make_items(items, n, its, false);
+  if (r != RMN_OK) return r;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // Proxy renders: the same scenes, spp, depth and field of view at a
+  // fraction of the pixels, into buffers owned by the tuner.
+  const float scale = std::sqrt(pixel_fraction);
+  std::vector<void*> bufs;
+  cudaError_t e = cudaSuccess;
+  for (RenderItem& it : its) {
+    rmn_render_args& a = it.args;
+    int w = std::max(8, (int)std::lround(a.width * scale)), h = std::max(8, (int)std::lround(a.height * scale));
+    a.accuracy *= (float)a.width / (float)w;
+    a.width = w;
+    a.height = h;
+    a.lanes_per_pixel = 0;
+    it.dropped = nullptr;
+    float** dst[5] = {&it.gbuf, &it.dd, &it.ds, &it.id, &it.is};
+    size_t bytes[5] = {(size_t)w * h * RMN_GBUFFER_FLOATS * 4, (size_t)w * h * 16, (size_t)w * h * 16,
+                       (size_t)w * h * 16, (size_t)w * h * 16};
+    for (int k = 0; k < 5 && e == cudaSuccess; ++k) {
+      void* p = nullptr;
+      e = cudaMalloc(&p, bytes[k]);
+      if (e == cudaSuccess) {
+        bufs.push_back(p);
+        *dst[k] = static_cast<float*>(p);
+      }
+    }
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  if (e == cudaSuccess) e = cudaEventCreate(&e0);
+  if (e == cudaSuccess) e = cudaEventCreate(&e1);
+  if (e != cudaSuccess) r = cuda_fail(e, "autotune set-up");
+  const int slots[] = {4, 8, 16, 32, 64};
+  const int pools[] = {1 << 18, 1 << 19, 1 << 20, 1 << 21};
+  rmn_tune_result best{16, 1 << 20, 1e30, 0.0, 0, 0};
+  for (int si = 0; si < 5 && r == RMN_OK; ++si)
+    for (int pi = 0; pi < 4 && r == RMN_OK; ++pi) {
+      for (RenderItem& it : its) it.args.slots_per_unit = slots[si];
+      BatchState* b = nullptr;
+      r = batch_create(its.data(), n, true, pools[pi], st, &b);
+      if (r != RMN_OK) break;
+      r = batch_launch(b, st);  // warm-up
+      if (r == RMN_OK) {
+        cudaEventRecord(e0, st);
+        r = batch_launch(b, st);
+        cudaEventRecord(e1, st);
+      }
+      if (r == RMN_OK) r = batch_status(b, st);
+      float ms = 0.0f;
+      if (r == RMN_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(RMN_ERR_CUDA, "event timing");
+      batch_destroy(b);
+      if (r != RMN_OK) break;
+      best.candidates++;
+      if (slots[si] == 16 && pools[pi] == (1 << 20)) best.default_ms = ms;
+      if (ms < best.best_ms) {
+        best.best_ms = ms;
+        best.slots_per_unit = slots[si];
+        best.pool_workers = pools[pi];
+      }
+    }
+  if (e0) cudaEventDestroy(e0);
+  if (e1) cudaEventDestroy(e1);
+  cudaStreamSynchronize(st);
+  for (void* p : bufs) cudaFree(p);
+  if (r == RMN_OK) *out = best;
+  return r;
 }
 
 rmn_status rmn_batch_render(rmn_batch* batch, void* stream) {

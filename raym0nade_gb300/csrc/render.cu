@@ -39,18 +39,10 @@
 #include <vector>
 
 #include "rmn_host.h"
-#include "shade.cuh"
+#include "integrator.cuh"
 
 namespace {
 
-struct Params {
-  float3 pos, dir, up, right;
-  float acc, exposure, p_direct, inv_spp;
-  int W, H, spp, maxd, spp_d, slots;
-  int S;  // slots per unit
-  int K;  // units per pixel
-  uint64_t seed;
-};
 
 // One render of a batch: a scene, its arguments, its output buffers and its
 // place in the batch's pixel and unit numbering.
@@ -59,6 +51,7 @@ struct Job {
   Params p;
   float* gbuf;
   float4 *dd, *ds, *id, *is;
+  int* dropped;          // optional: per pixel, the sample the firefly clamp dropped
   int pix_begin;         // first pixel of this job in the batch
   long long unit_begin;  // first unit of this job in the batch
 };
@@ -99,7 +92,8 @@ struct Pool {
 
 // Partial accumulator of one unit: 7 float4.
 //   [0] Dd  [1] Ds  [2] Id without the largest sample  [3] Is likewise
-//   [4] Id of the largest  [5] Is of the largest  [6] (its Clum or -1, S, n, -)
+//   [4] Id of the largest  [5] Is of the largest
+//   [6] (its Clum or -1, S, n, its sample id = slot * 8 + index in the path's samples)
 #define RMN_PART_F4 7
 
 enum Phase { PH_FETCH = 0, PH_SLOT, PH_WAIT_DIRECT, PH_WAIT_CLOSEST, PH_NEE, PH_WAIT_NEE, PH_DONE };
@@ -124,30 +118,7 @@ __device__ __forceinline__ int find_job_unit(const Job* jobs, int n, long long v
   return lo;
 }
 
-// renderPixel's demodulation tweak, src/render.cpp:492-495: a faint red is
-// added to black or grey base colours (double-precision literals as there).
-__device__ __forceinline__ float3 tweak_base(float3 b) {
-  float c0 = dot3(b, RMN_LUM);
-  if ((double)c0 < 2e-2 || (c0 < 0.8f && (double)len3(b / c0 - f3(1.0f)) < 2e-2)) b.x = (float)((double)b.x + 4e-2);
-  return b;
-}
 
-__device__ __forceinline__ Surf default_surf() {
-  Surf g;
-  g.shapeN = f3(NAN);
-  g.surfN = f3(NAN);
-  g.emis = f3(0.0f);
-  g.base = f3(0.0f);
-  g.pos = f3(NAN);
-  g.specular = 0.04f;
-  g.roughness = 0.8f;
-  g.metallic = 0.0f;
-  g.opacity = 1.0f;
-  g.eta = 1.0f;
-  g.id = 0;
-  g.entering = true;
-  return g;
-}
 
 // G-buffer record (RMN_GBUFFER_FLOATS = 20): base[3] emission[3] position[3]
 // shapeN[3] surfN[3] roughness metallic opacity eta material-id. The base
@@ -193,56 +164,15 @@ __global__ void __launch_bounds__(128) primary_kernel(const Job* __restrict__ jo
   }
 }
 
-struct Rad4 {
-  float3 c;
-  float v;
-};
-__device__ __forceinline__ Rad4 rad0() { return {f3(0.0f), 0.0f}; }
-__device__ __forceinline__ void radd(Rad4& a, const Rad4& b) { a.c += b.c; a.v += b.v; }
-__device__ __forceinline__ Rad4 r4(float4 v) { return {f3(v.x, v.y, v.z), v.w}; }
-__device__ __forceinline__ float4 f4(const Rad4& r) { return make_float4(r.c.x, r.c.y, r.c.z, r.v); }
-
-// accumulateInwardRadiance(_basic), src/image.cpp:615-659, as the two
-// contributions (diffuse part, specular part) of one sample.
-__device__ __forceinline__ bool basic(float3 in, float w, Rad4& out) {
-  if (!any_finite3(in) || !finite1(w)) return false;
-  out.c = in * w;
-  out.v = dot3(in, in) * w;
-  return true;
-}
-__device__ __forceinline__ void demodulate(float3 base, float3 bsdf, float3 light, float w, Rad4& d, Rad4& sp) {
-  d = rad0();
-  sp = rad0();
-  if (len3(light) < RMN_EPS) return;
-  float3 b0 = norm3(base);
-  if (len3(base) < RMN_EPS) {
-    basic(light * bsdf, w, sp);
-    return;
-  }
-  const float3 white = norm3(f3(1.0f));
-  float xy = dot3(b0, white);
-  if (xy > 0.99f) {
-    basic(light * bsdf / base, w, d);
-    return;
-  }
-  float3 perp = norm3(cross3(b0, white));
-  float3 bp = bsdf - perp * dot3(perp, bsdf);
-  float d1 = dot3(bp, white), d2 = dot3(bp, b0);
-  float apb = (d1 + d2) / (1 + xy), amb = (d1 - d2) / (1 - xy);
-  float B = (apb - amb) / 2.0f;
-  float3 bb = B * b0;
-  basic(light * B / len3(base), w, d);
-  basic(light * (bsdf - bb), w, sp);
-}
 
 // The largest-sample bookkeeping shared by emit (one sample into a unit) and
 // finalize (unit into pixel).
 struct Ind {
   Rad4 id, is, mid, mis;
   float mclum, S;
-  int n;
+  int n, mid_sample;
 };
-__device__ __forceinline__ void ind_add(Ind& a, const Rad4& d, const Rad4& s, float clum, float S, int n) {
+__device__ __forceinline__ void ind_add(Ind& a, const Rad4& d, const Rad4& s, float clum, float S, int n, int sid) {
   a.S += S;
   a.n += n;
   if (clum > a.mclum) {
@@ -253,6 +183,7 @@ __device__ __forceinline__ void ind_add(Ind& a, const Rad4& d, const Rad4& s, fl
     a.mid = d;
     a.mis = s;
     a.mclum = clum;
+    a.mid_sample = sid;
   } else if (clum >= 0.0f) {
     radd(a.id, d);
     radd(a.is, s);
@@ -286,7 +217,7 @@ __device__ __forceinline__ Surf load_first_vertex(const Job& J, int pixel) {
 // weight finished as passBsdf/mulWeight would (src/render.cpp:101-116),
 // demodulated against the first vertex's (tweaked) base colour with the
 // first-vertex factor w0 as LightSample::bsdfPdf.
-__device__ void emit(float4* part, float3 base, float4 pa, float3 thr, float inv_spp, const LSample& ls) {
+__device__ void emit(float4* part, float3 base, float4 pa, float3 thr, float inv_spp, const LSample& ls, int sid) {
   float3 w0 = f3(pa.x, pa.y, pa.z);
   float3 light = (ls.light * ls.bsdf) * thr;
   float w = ls.weight * pa.w * inv_spp;
@@ -302,12 +233,13 @@ __device__ void emit(float4* part, float3 base, float4 pa, float3 thr, float inv
   a.mclum = m.x;
   a.S = m.y;
   a.n = __float_as_int(m.z);
-  ind_add(a, d, s, clum, clum, 1);
+  a.mid_sample = __float_as_int(m.w);
+  ind_add(a, d, s, clum, clum, 1, sid);
   part[2] = f4(a.id);
   part[3] = f4(a.is);
   part[4] = f4(a.mid);
   part[5] = f4(a.mis);
-  part[6] = make_float4(a.mclum, a.S, __int_as_float(a.n), 0.0f);
+  part[6] = make_float4(a.mclum, a.S, __int_as_float(a.n), __int_as_float(a.mid_sample));
 }
 
 // Warp-aggregated increment: the lanes that reach the call together take
@@ -370,7 +302,7 @@ __global__ void __launch_bounds__(128) logic_kernel(const Job* __restrict__ jobs
         float4* part = parts + (size_t)uid * RMN_PART_F4;
 #pragma unroll
         for (int k = 0; k < 6; ++k) part[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        part[6] = make_float4(-1.0f, 0.0f, __int_as_float(0), 0.0f);
+        part[6] = make_float4(-1.0f, 0.0f, __int_as_float(0), __int_as_float(-1));
         const float* gb = gbuf_of(*J, pixel);
         bool hit = any_finite3(f3(gb[6], gb[7], gb[8]));
         un = make_int4(jb, pixel, hit ? j0 : j1, j1);
@@ -478,7 +410,7 @@ __global__ void __launch_bounds__(128) logic_kernel(const Job* __restrict__ jobs
         if (h < 0) {
           if (!exclude && s.sky_w)
             emit(parts + (size_t)uid * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp,
-                 {f3(1.0f), sky_get(s, dir), 1.0f});
+                 {f3(1.0f), sky_get(s, dir), 1.0f}, un.z * 8);
           un.z++;
           phase = PH_SLOT;
           break;
@@ -493,7 +425,7 @@ __global__ void __launch_bounds__(128) logic_kernel(const Job* __restrict__ jobs
         if (len3(sf.emis) > RMN_EPS) {
           if (!exclude)
             emit(parts + (size_t)uid * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp,
-                 {f3(1.0f), sf.emis, 1.0f});
+                 {f3(1.0f), sf.emis, 1.0f}, un.z * 8);
           un.z++;
           phase = PH_SLOT;
           break;
@@ -595,7 +527,7 @@ __global__ void __launch_bounds__(128) logic_kernel(const Job* __restrict__ jobs
           float4 a = P.pend[2 * w], b = P.pend[2 * w + 1];
           float4 pb = P.pb[w];
           emit(parts + (size_t)uid * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), J->p.inv_spp,
-               {f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w});
+               {f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w}, un.z * 8 + P.nk[w].x);
         }
         int4 nk = P.nk[w];
         P.nk[w] = make_int4(nk.x + 1, nk.y, 0, 0);
@@ -685,12 +617,6 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
   }
 }
 
-__device__ __forceinline__ void calc_var(Rad4& r, float e) {  // renderPixel's calcVar, src/render.cpp:510-516
-  r.c *= e;
-  r.v *= e * e;
-  r.v -= dot3(r.c, r.c);
-  if (r.v < 0.0f) r.v = 0.0f;
-}
 
 // Per pixel: merge the partial records of its K units in unit order, apply
 // the firefly clamp and calcVar, write the RadianceData buffers; write the
@@ -710,6 +636,8 @@ __global__ void __launch_bounds__(128) finalize_kernel(const Job* __restrict__ j
   a.mclum = -1.0f;
   a.S = 0.0f;
   a.n = 0;
+  a.mid_sample = -1;
+  int dropped = -1;
   if (hit) {
     const float4* pr = parts + (size_t)(J.unit_begin + (long long)pixel * p.K) * RMN_PART_F4;
     for (int k = 0; k < p.K; ++k, pr += RMN_PART_F4) {
@@ -718,7 +646,7 @@ __global__ void __launch_bounds__(128) finalize_kernel(const Job* __restrict__ j
       float4 m = pr[6];
       radd(a.id, r4(pr[2]));
       radd(a.is, r4(pr[3]));
-      ind_add(a, r4(pr[4]), r4(pr[5]), m.x, m.y, __float_as_int(m.z));
+      ind_add(a, r4(pr[4]), r4(pr[5]), m.x, m.y, __float_as_int(m.z), __float_as_int(m.w));
     }
     calc_var(dd, p.exposure);
     calc_var(ds, p.exposure);
@@ -726,6 +654,8 @@ __global__ void __launch_bounds__(128) finalize_kernel(const Job* __restrict__ j
       if (!(a.mclum / (a.S - a.mclum + RMN_EPS) > 16.0f)) {
         radd(a.id, a.mid);
         radd(a.is, a.mis);
+      } else {
+        dropped = a.mid_sample;
       }
       calc_var(a.id, p.exposure);
       calc_var(a.is, p.exposure);
@@ -740,6 +670,7 @@ __global__ void __launch_bounds__(128) finalize_kernel(const Job* __restrict__ j
   J.ds[pixel] = f4(ds);
   J.id[pixel] = f4(a.id);
   J.is[pixel] = f4(a.is);
+  if (J.dropped) J.dropped[pixel] = dropped;
 }
 
 int device_sms() {
@@ -760,10 +691,6 @@ int blocks_per_sm(K kernel) {
 
 namespace rmn {
 
-// Slots per work unit. A unit is the work of one worker between two fetches;
-// shorter units shorten the drain at the end of a render, longer ones need
-// fewer partial records (112 B each).
-constexpr int kDefaultSlotsPerUnit = 16;
 constexpr int kDefaultPoolWorkers = 1 << 20;
 constexpr int kIterationsPerChunk = 8;
 constexpr long long kMaxIterations = 1LL << 22;  // bound on the iteration loop; a finite render never reaches it
@@ -786,37 +713,6 @@ struct BatchState {
   bool use_graph = false;
 };
 
-static Params make_params(const rmn_render_args& a) {
-  Params p;
-  p.pos = f3(a.position[0], a.position[1], a.position[2]);
-  p.dir = f3(a.direction[0], a.direction[1], a.direction[2]);
-  p.up = f3(a.up[0], a.up[1], a.up[2]);
-  p.right = f3(a.right[0], a.right[1], a.right[2]);
-  p.acc = a.accuracy;
-  p.exposure = a.exposure;
-  p.p_direct = a.P_Direct;
-  p.W = a.width;
-  p.H = a.height;
-  p.spp = a.spp;
-  p.maxd = a.max_depth;
-  p.spp_d = (int)((float)a.spp * a.P_Direct);  // renderPixel, src/render.cpp:497
-  const int spp_i = (a.spp - p.spp_d) * 1;      // opaque first vertex
-  p.inv_spp = 1.0f / (float)spp_i;
-  p.slots = p.spp_d + spp_i;
-  // lanes_per_pixel > 0 fixes the number of units per pixel; 0 cuts the
-  // slots into units of kDefaultSlotsPerUnit.
-  if (a.lanes_per_pixel > 0) {
-    p.K = a.lanes_per_pixel;
-    p.S = (p.slots + p.K - 1) / p.K;
-    if (p.S < 1) p.S = 1;
-  } else {
-    p.S = kDefaultSlotsPerUnit;
-    p.K = (p.slots + p.S - 1) / p.S;
-    if (p.K < 1) p.K = 1;
-  }
-  p.seed = a.seed;
-  return p;
-}
 
 // Jobs ordered by decreasing depth (the longest paths start first), so the
 // pool drains on cheap units; results do not depend on the order.
@@ -838,6 +734,7 @@ static void build_jobs(const RenderItem* items, int n, JobTable* t) {
     j.ds = reinterpret_cast<float4*>(it.ds);
     j.id = reinterpret_cast<float4*>(it.id);
     j.is = reinterpret_cast<float4*>(it.is);
+    j.dropped = it.dropped;
     j.pix_begin = t->total_pix;
     j.unit_begin = t->total_units;
     t->total_pix += j.p.W * j.p.H;
@@ -973,12 +870,13 @@ void batch_destroy(BatchState* b) {
   delete b;
 }
 
-rmn_status batch_create(const RenderItem* items, int n, bool use_graph, cudaStream_t st, BatchState** out) {
+rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, cudaStream_t st,
+                        BatchState** out) {
   *out = nullptr;
   BatchState* b = new BatchState();
   build_jobs(items, n, &b->table);
   b->use_graph = use_graph;
-  long long W = std::min<long long>(b->table.total_units, kDefaultPoolWorkers);
+  long long W = std::min<long long>(b->table.total_units, pool_workers > 0 ? pool_workers : kDefaultPoolWorkers);
   if (W < 1) W = 1;
   W = (W + 127) / 128 * 128;
   Pool& P = b->pool;

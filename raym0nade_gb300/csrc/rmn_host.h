@@ -43,6 +43,7 @@ struct RenderItem {
   const rmn_scene* scene;
   rmn_render_args args;
   float *gbuf, *dd, *ds, *id, *is;
+  int* dropped;  // optional
 };
 struct RenderProfileData {
   double primary_ms, path_ms, logic_ms, trace_ms;
@@ -51,11 +52,17 @@ struct RenderProfileData {
 };
 struct BatchState;
 
-rmn_status batch_create(const RenderItem* items, int n, bool use_graph, cudaStream_t st, BatchState** out);
+rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, cudaStream_t st,
+                        BatchState** out);
 rmn_status batch_launch(BatchState* b, cudaStream_t st);
 rmn_status batch_status(BatchState* b, cudaStream_t st);
 rmn_status batch_profile(BatchState* b, cudaStream_t st, RenderProfileData* prof);
 void batch_destroy(BatchState* b);
+
+// Adjoint of one render (adjoint.cu): device buffers only; dmat receives
+// num_materials * RMN_GRAD_PER_MATERIAL floats.
+rmn_status launch_adjoint(const rmn_scene* scene, const rmn_render_args& args, const float* gbuf, const int* dropped,
+                          const float* dimg, float* dmat, cudaStream_t st);
 cudaError_t launch_fxaa(const float* in, float* out, int w, int h, cudaStream_t stream);
 cudaError_t launch_compose(const float* dd, const float* ds, const float* id, const float* is, const float* gbuf,
                            int w, int h, float exposure, int options, float* rgb, cudaStream_t stream);

@@ -98,7 +98,8 @@ struct __align__(16) DevLight {
   float4 center;  // xyz, w = power
   float4 color;   // xyz, w = face count (float)
   int first_face; // into light_faces / light_prefix
-  int pad[3];
+  int material;   // material of the emissive mesh
+  int pad[2];
 };
 // Light face: 6 float4 -- v0, v1, v2 (w unused), n0, n1, n2.
 #define RMN_LIGHT_FACE_F4 6

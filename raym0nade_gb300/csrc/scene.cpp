@@ -287,6 +287,7 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
     L.center = make_float4(center.x, center.y, center.z, power);
     L.color = make_float4(color.x, color.y, color.z, (float)faces.size());
     L.first_face = (int)(lfaces.size() / RMN_LIGHT_FACE_F4);
+    L.material = d->mesh_material[m];
     lights.push_back(L);
     float acc = 0.0f;
     for (size_t j = 0; j < faces.size(); ++j) {

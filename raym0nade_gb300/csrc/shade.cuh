@@ -181,12 +181,34 @@ RMN_D void frame(const Surf& s, float3 in, float3& t, float3& b) {
 // BSDF::sampleReflection (src/sampling.cpp:310-340) with sampleCos (:245-269)
 // and sampleBRDF (:203-236): both strategies are drawn in full, then one is
 // kept with probability pdf_cos / (pdf_cos + pdf_ggx).
-RMN_D void sample_reflect(const Surf& s, float3 in, RmnRng& rng, float3& dir, float3& w, int& fails) {
+//
+// With `ad`, the draw also reports what its adjoint needs (ReflectAD).
+struct ReflectAD {
+  int cos_branch;  // 1: the cosine sample was kept
+  int clamped;     // the kept factor was luminance-clamped (cosine branch only)
+  // d/dr of log(probability of the draws) + d/dr log(1 / kept pdf), r the
+  // roughness the draw used: the score of every GGX half vector drawn
+  // (accepted or not), the score of the branch choice (probability pc or
+  // 1 - pc, pc depending on r through the GGX pdf), and, for the GGX
+  // branch, the derivative of dividing by its pdf.
+  float score;
+};
+// d/dr log GTR2(c, r) = 2/r - 4 r c^2 / (1 + (r^2 - 1) c^2): the roughness
+// score of a GGX half vector with cos(theta_h) = c.
+RMN_D float dlog_gtr2(float c, float r) {
+  if (!(r > 1e-6f)) return 0.0f;
+  float t = 1.0f + (r * r - 1.0f) * c * c;
+  return 2.0f / r - 4.0f * r * c * c / t;
+}
+RMN_D void sample_reflect(const Surf& s, float3 in, RmnRng& rng, float3& dir, float3& w, int& fails,
+                          ReflectAD* ad = nullptr) {
   float3 t, b;
   frame(s, in, t, b);
   float3 d1 = f3(NAN), w1 = f3(0.0f), d2 = f3(NAN), w2 = f3(0.0f);
   float p1 = 0.0f, p2 = 0.0f;
   int f1 = 0, f2 = 0;
+  float sc = 0.0f, g2 = 0.0f;  // adjoint: GGX scores of all tries, of the kept try
+  bool cl1 = false;
   for (int T = 1; T <= RMN_MAX_TRYS; ++T) {  // sampleCos
     float u = rng.next(), phi = rng.next() * 2.0f * RMN_PI;
     float d = sqrtf(u);
@@ -199,6 +221,7 @@ RMN_D void sample_reflect(const Surf& s, float3 in, RmnRng& rng, float3& dir, fl
     if (dot3(o, s.shapeN) > 0.0f && pdf > 0.0f) {
       d1 = o;
       w1 = brdf(s, in, o) / pdf;
+      if (ad) cl1 = dot3(w1, RMN_LUM) > 64.0f;
       lum_clamp(w1);
       p1 = pdf;
       break;
@@ -208,6 +231,7 @@ RMN_D void sample_reflect(const Surf& s, float3 in, RmnRng& rng, float3& dir, fl
   for (int T = 1; T <= RMN_MAX_TRYS; ++T) {  // sampleBRDF (GGX half vector)
     float u = rng.next(), phi = rng.next() * 2.0f * RMN_PI;
     float ct = sqrtf((1.0f - u) / (1.0f + (s.roughness * s.roughness - 1.0f) * u));
+    if (ad) sc += dlog_gtr2(ct, s.roughness);
     float st = sqrtf(1 - ct * ct);
     float sp, cp;
     sincosf(phi, &sp, &cp);
@@ -219,6 +243,7 @@ RMN_D void sample_reflect(const Surf& s, float3 in, RmnRng& rng, float3& dir, fl
       d2 = o;
       w2 = brdf(s, in, o) / pdf;
       p2 = pdf;
+      if (ad) g2 = dlog_gtr2(ct, s.roughness);
       break;
     }
     f2++;
@@ -226,8 +251,18 @@ RMN_D void sample_reflect(const Surf& s, float3 in, RmnRng& rng, float3& dir, fl
   float pc = p1 / (p1 + p2);
   if (rng.next() < pc) {
     dir = d1; w = w1; fails += f1;
+    if (ad) {
+      ad->cos_branch = 1;
+      ad->clamped = cl1;
+      ad->score = sc - (p2 > 0.0f ? (1.0f - pc) * g2 : 0.0f);
+    }
   } else {
     dir = d2; w = w2; fails += f2;
+    if (ad) {
+      ad->cos_branch = 0;
+      ad->clamped = 0;
+      ad->score = sc + (p1 + p2 > 0.0f ? pc * g2 : 0.0f) - g2;
+    }
   }
 }
 
@@ -288,7 +323,7 @@ RMN_D bool light_weights(const DevScene& s, const Surf& sf, float3 V, float* w, 
 // weight). Returns false when the sample is dropped before any shadow test.
 // Light weights `w` / `tot` come from light_weights (light mode only).
 RMN_D bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float* w, float tot, int cnt, RmnRng& rng,
-                     float3& dir, float& aim, LSample& out) {
+                     float3& dir, float& aim, LSample& out, int* light_index = nullptr) {
   const float3 pos = sf.pos;
   if (s.sky_w == 0) {
     float rv = tot * rng.next();  // sample(), :396-404
@@ -299,6 +334,7 @@ RMN_D bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float* w
       if (rv <= acc) { li = i; break; }
     }
     if (li < 0) return false;
+    if (light_index) *light_index = li;
     float pl = w[li] / tot;
     const DevLight& L = s.lights[li];
     float4 lc = __ldg(&L.center), lcol = __ldg(&L.color);
@@ -339,6 +375,7 @@ RMN_D bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float* w
     return true;
   }
   // sampleSkyBox, :450-465
+  if (light_index) *light_index = -1;
   const int npx = s.sky_w * s.sky_h;
   const float total = __ldg(s.sky_prefix + npx - 1);
   for (int T = 1; T <= RMN_MAX_TRYS; ++T) {
@@ -364,4 +401,90 @@ RMN_D bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float* w
     }
   }
   return false;
+}
+
+// ------------------------------------------------------------ derivatives --
+// BSDF::getBRDF and its derivatives with respect to the base colour (one
+// channel each: the BRDF is affine in it, tints being zero) and to the
+// roughness, differentiated by hand from the expressions of brdf() above.
+// The specular lobe's colour depends on the base colour only through
+// metallic (Cspec0 = mix(0.04, base, metallic)).
+RMN_D float3 brdf_d(const Surf& s, float3 V, float3 L, float3& d_base, float3& d_rough) {
+  d_base = f3(0.0f);
+  d_rough = f3(0.0f);
+  const float3 N = s.surfN;
+  float nl = dot3(N, L), nv = dot3(N, V);
+  if (nl <= 0.0f || nv <= 0.0f) return f3(0.0f);
+  float3 H = norm3(L + V);
+  float nh = dot3(N, H), lh = dot3(L, H);
+  const float r = s.roughness, m = s.metallic;
+  float fl = schlick(nl), fv = schlick(nv);
+  float fd90 = 0.5f + 2.0f * lh * lh * r;
+  float ml = fmixf(1.0f, fd90, fl), mv = fmixf(1.0f, fd90, fv);
+  float fd = ml * mv;
+  float dfd = 2.0f * lh * lh * (fl * mv + ml * fv);
+  float a2 = r * r, t = 1 + (a2 - 1) * nh * nh;
+  float ds = a2 / (RMN_PI * t * t);
+  float dds = (2.0f * r / (RMN_PI * t * t)) * (1.0f - 2.0f * a2 * nh * nh / t);
+  float fh;
+  if (s.eta <= 1.0f) {
+    fh = schlick(lh);
+  } else {
+    float ci = fabsf(lh);
+    float x = 1.0f - ci * ci;
+    float si = x <= 0.0f ? 0.0f : sqrtf(x);
+    float st = s.eta * si;
+    if (st >= 1.0f) {
+      fh = 1.0f;
+    } else {
+      float y = 1.0f - st * st;
+      float ct = y <= 0.0f ? 0.0f : sqrtf(y);
+      float r0 = (s.eta - 1.0f) / (s.eta + 1.0f);
+      r0 = r0 * r0;
+      fh = fmixf(r0, 1.0f, schlick(ct));
+    }
+  }
+  float3 spec0 = f3(0.04f) * (1.0f - m) + s.base * m;
+  float3 fs = spec0 * (1.0f - fh) + f3(fh);
+  auto G = [](float c, float ag, float& dG) {
+    float a = ag * ag, b = c * c;
+    float q = sqrtf(a + b - a * b);
+    float g = 1 / (c + q);
+    dG = -(ag * (1.0f - b) / q) * g * g;
+    return g;
+  };
+  float dgl, dgv;
+  float gl = G(nl, r, dgl), gv = G(nv, r, dgv);
+  float gs = gl * gv, dgs = dgl * gv + gl * dgv;
+  float dr = gtr1(nh, fmixf(.1f, .001f, 0.2f));
+  float fr = fmixf(.04f, 1.0f, fh);
+  float gr = smith_g(nl, .25f) * smith_g(nv, .25f);
+  float3 ret = (1.0f / RMN_PI) * fd * s.base * (1.0f - m) + f3(0.25f * 1.5f * gr * fr * dr);
+  ret = ret * s.opacity + fs * ds * gs;
+  d_base = f3(((1.0f / RMN_PI) * fd * (1.0f - m) * s.opacity + m * (1.0f - fh) * ds * gs) * nl);
+  d_rough = ((1.0f / RMN_PI) * dfd * (1.0f - m) * s.opacity * s.base + fs * (dds * gs + ds * dgs)) * nl;
+  return ret * nl;
+}
+
+// Log-derivatives of a path factor v = clamp64(f) * k, f = brdf_d's value,
+// k a scalar that depends on neither the base colour nor the roughness of
+// the brdf (clamp64: the luminance clamp of src/sampling.cpp:238-243).
+// With A = dS/dv (*) v the factor's adjoint and S = sum(A) (the sample's
+// contribution is linear in v), the factor adds
+//   dS/dbase = A (*) l - S q,   dS/dr = A . lr.
+// Unclamped: l = df_base / f, q = 0, lr = df_rough / f per channel. Clamped
+// (v = f 64 / lum(f)): l as before, q = LUM (*) df_base / lum(f) and
+// lr = df_rough / f - lum(df_rough) / lum(f).
+RMN_D void factor_logd(float3 f, float3 df_base, float3 df_rough, bool clamped, float3& l, float3& q, float3& lr) {
+  auto ratio = [](float a, float b) { return b != 0.0f ? a / b : 0.0f; };
+  l = f3(ratio(df_base.x, f.x), ratio(df_base.y, f.y), ratio(df_base.z, f.z));
+  lr = f3(ratio(df_rough.x, f.x), ratio(df_rough.y, f.y), ratio(df_rough.z, f.z));
+  q = f3(0.0f);
+  if (clamped) {
+    float L = dot3(f, RMN_LUM);
+    if (L > 0.0f) {
+      q = f3(0.3f * df_base.x, 0.6f * df_base.y, 0.1f * df_base.z) / L;
+      lr = lr - f3(dot3(df_rough, RMN_LUM) / L);
+    }
+  }
 }

@@ -206,6 +206,57 @@ def cornell(materials: list | None = None, wall_materials=None) -> Scene:
     return _assemble(meshes, materials, name="cornell")
 
 
+CORNELL16_LIGHT = 5  # material index of the emitter in cornell16
+
+
+def cornell16_params(seed: int = 11) -> np.ndarray:
+    """Parameters of the 16-material Cornell variant, (16, 5) float64 rows
+    (base r, g, b, roughness, emission scale): base ~ U[0.1, 0.9]^3,
+    roughness ~ U[0.1, 0.8], scale 1; the emitter keeps base 0.78 and
+    roughness 0.8."""
+    rng = np.random.default_rng(seed)
+    p = np.zeros((16, 5))
+    p[:, 0:3] = rng.uniform(0.1, 0.9, (16, 3))
+    p[:, 3] = rng.uniform(0.1, 0.8, 16)
+    p[:, 4] = 1.0
+    p[CORNELL16_LIGHT, 0:3] = 0.78
+    p[CORNELL16_LIGHT, 3] = 0.8
+    return p
+
+
+def cornell16(params: np.ndarray | None = None) -> Scene:
+    """The Cornell box with 16 materials: floor 0, ceiling 1, back wall 2,
+    right wall 3, left wall 4, light 5 (emission (17, 12, 4) times its scale),
+    short box top 6, front and bottom 7, back 8, left 9, right 10, tall box
+    11-15 likewise. ``params`` as cornell16_params (default seed 11); every
+    material is a constant texel without a specular texel (metallic 0)."""
+    p = cornell16_params() if params is None else np.asarray(params, np.float64)
+    mats = []
+    for i in range(16):
+        em = tuple(np.asarray(CORNELL_LIGHT) * p[i, 4]) if i == CORNELL16_LIGHT else None
+        mats.append(material(tuple(p[i, 0:3]), emission=em, roughness=float(p[i, 3])))
+    meshes = []
+    zero2 = lambda k: np.zeros((k, 2), np.float32)
+    for mat, quad in enumerate([
+        ((0, 0, 0), (1, 0, 0), (1, 0, 1), (0, 0, 1)),
+        ((0, 1, 0), (0, 1, 1), (1, 1, 1), (1, 1, 0)),
+        ((0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)),
+        ((1, 0, 0), (1, 1, 0), (1, 1, 1), (1, 0, 1)),
+        ((0, 0, 0), (0, 0, 1), (0, 1, 1), (0, 1, 0)),
+    ]):
+        q, n = _quad(*quad)
+        meshes.append((q, n, zero2(6), mat))
+    y = 1.0 - 1e-3
+    q, n = _quad((0.375, y, 0.375), (0.625, y, 0.375), (0.625, y, 0.625), (0.375, y, 0.625))
+    meshes.append((q, n, zero2(6), CORNELL16_LIGHT))
+    for first, box in [(6, (0.65, 0.35, 0.3, 0.3, 0.3, 15.0)), (11, (0.33, 0.62, 0.3, 0.6, 0.3, -18.0))]:
+        q, n = _box(*box)
+        # faces of _box: top, bottom, front, back, left, right (two triangles each)
+        for f, mat in enumerate([first, first + 1, first + 1, first + 2, first + 3, first + 4]):
+            meshes.append((q[6 * f:6 * f + 6], n[6 * f:6 * f + 6], zero2(6), mat))
+    return _assemble(meshes, mats, name="cornell16")
+
+
 def cornell_camera(width=256, height=256, spp=64, max_depth=16, p_direct=0.7) -> Camera:
     """Camera at (0.5, 0.5, -1.4) looking +z; 40 degree field of view across
     ``width`` pixels (accuracy = tan(20 deg) / (width / 2)); image rows run

@@ -131,7 +131,7 @@ def test_emitter_and_miss_pixels(port):
 def test_render_argument_errors():
     m = api.Model(scenes.cornell())
     cam = scenes.cornell_camera(8, 8, 4)
-    for field, value in [("P_Direct", 1.5), ("max_depth", 0), ("max_depth", 17), ("lanes_per_pixel", 3),
+    for field, value in [("P_Direct", 1.5), ("max_depth", 0), ("max_depth", 17), ("lanes_per_pixel", 65),
                          ("width", 0)]:
         a = api.RenderArgs.from_camera(cam)
         setattr(a, field, value)

@@ -41,7 +41,7 @@ def test_struct_sizes_match_header():
     from raym0nade_gb300 import _lib
     assert ctypes.sizeof(_lib.Material) == 64
     assert ctypes.sizeof(_lib.RenderArgs) == 4 * 17 + 4 * 5 + 8 + 4 * 4
-    assert ctypes.sizeof(_lib.Image) == 5 * 8
+    assert ctypes.sizeof(_lib.Image) == 6 * 8
 
 
 def test_parse_render_args_docs_block():
