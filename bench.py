@@ -196,6 +196,57 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def adjoint_timing(args, stream, flush, barrier):
+    """Adjoint / forward time on the 16-material Cornell box: 512x512, 32 spp,
+    max depth 16; dL/dI of the L2 loss to a target rendered at parameters
+    perturbed by up to +-10%. Both passes on device buffers, timed with CUDA
+    events on the stream after W warm-ups, L2 flushed before each."""
+    import numpy as np
+    import torch
+    from raym0nade_gb300 import api, scenes
+    p0 = scenes.cornell16_params()
+    rng = np.random.default_rng(5)
+    pt = p0.copy()
+    pt[:, 0:4] *= rng.uniform(0.9, 1.1, (16, 4))
+    pt[:, 4] *= 1.1
+    w, spp = 512, 32
+    cam = scenes.cornell_camera(w, w, spp, max_depth=16)
+    mt = api.Model(scenes.cornell16(pt))
+    target = api.render(mt, api.RenderArgs.from_camera(cam, seed=99), stream=stream).shade(api.Full, stream=stream)
+    m = api.Model(scenes.cornell16(p0))
+    a = api.RenderArgs.from_camera(cam, seed=1)
+    ph = api.Photo(w, w)
+    api.render(m, a, ph, stream)
+    g = (2.0 * (ph.shade(api.Full, stream=stream) - target)).reshape(-1, 3).contiguous()
+    grad = api.adjoint(m, a, ph, g, stream=stream)
+
+    def timeit(fn):
+        for _ in range(args.warmup):
+            fn()
+        barrier()
+        ms = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.current_stream().wait_stream(stream)
+            stream.wait_stream(torch.cuda.current_stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(sum(ms)) / len(ms)
+
+    fwd = timeit(lambda: api.render(m, a, ph, stream))
+    adj = timeit(lambda: api.adjoint(m, a, ph, g, grad, stream))
+    paths = w * w * spp
+    return {"workload": "cornell16: 16 materials, 512x512, 32 spp, max depth 16, L2 loss to a target at "
+                        "+-10% parameters; gradients of 16 x 5 parameters",
+            "forward_ms": fwd, "adjoint_ms": adj, "adjoint_over_forward": adj / fwd,
+            "forward_Mpaths_s": paths / fwd / 1e3, "adjoint_Mpaths_s": paths / adj / 1e3,
+            "call": "rmn_render then rmn_adjoint on device buffers, CUDA events on the stream"}
+
+
 def run_gpu(args, rank, world, dist):
     import torch
     from raym0nade_gb300 import api
@@ -213,8 +264,18 @@ def run_gpu(args, rank, world, dist):
     stream = torch.cuda.Stream()
     flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
 
+    tune = None
+    if args.autotune:
+        # project autotuner: slots per work unit x worker pool, timed on a
+        # 1/16-pixel proxy of the same batch (untimed here)
+        t0 = time.perf_counter()
+        tune = api.autotune(list(zip(models, argsl, photos)), 1.0 / 16, stream)
+        tune["tune_s"] = round(time.perf_counter() - t0, 2)
+        for a in argsl:
+            a.slots_per_unit = tune["slots_per_unit"]
     with torch.cuda.stream(stream):
-        batch = api.Batch(list(zip(models, argsl, photos)), use_graph=True, stream=stream)
+        batch = api.Batch(list(zip(models, argsl, photos)), use_graph=True, stream=stream,
+                          pool_workers=tune["pool_workers"] if tune else 0)
 
     def step_batched():
         batch.render(stream)
@@ -290,6 +351,8 @@ def run_gpu(args, rank, world, dist):
     d2h = npx * (4 * 16 + 20 * 4 + 12)
     h2d = len(insts) * 96 + npx * (4 * 16 + 20 * 4)
 
+    adj = adjoint_timing(args, stream, flush, barrier) if args.adjoint else None
+
     value = paths_per_step * world / (ms_b / 1e3) / 1e6
     plain = paths_per_step * world / (ms_p / 1e3) / 1e6
     if rank != 0:
@@ -323,7 +386,8 @@ def run_gpu(args, rank, world, dist):
         "e2e": {"value": paths_per_step * world / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "call": "rmn_render into pinned host buffers + rmn_compose(Full|gamma|FXAA) to a host image, per instance"},
-        "gpu_launches": 2 * args.steps,
+        # per batched step: G-buffer kernel, 3 kernels per wavefront iteration, finalize
+        "gpu_launches": args.steps * (2 + 3 * prof["iterations"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": None, "kernel": "qtrace_kernel (closest + shadow queues)", "peak_source": peak_src,
                      "bytes_model": "64 B per inner-node visit + 36 B per triangle test + 40 B per queued ray",
@@ -332,6 +396,10 @@ def run_gpu(args, rank, world, dist):
         "rays": {"closest": prof["closest_rays"], "shadow": prof["shadow_rays"], "Mrays_s": rays / ms_b / 1e3},
         "clocks": clocks,
     }
+    if tune:
+        out["config"]["autotune"] = tune
+    if adj:
+        out["adjoint"] = adj
     if base:
         out["cpu_baseline"] = base
     print(json.dumps(out))
@@ -345,6 +413,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="batch64", choices=["batch64", "cornell", "heightfield"])
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--no-autotune", dest="autotune", action="store_false")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("at least 3 warm-up steps")

@@ -267,7 +267,7 @@ __device__ __forceinline__ void push(int* q, unsigned int* qn, int w) { q[agg_in
 //   PH_NEE          next light sample of the terminating vertex
 //   PH_WAIT_NEE     shadow answer of that light sample
 template <bool COUNT>
-__global__ void __launch_bounds__(128) logic_kernel(const Job* __restrict__ jobs, int njobs, Pool P, Ctl* ctl,
+__global__ void __launch_bounds__(128, 8) logic_kernel(const Job* __restrict__ jobs, int njobs, Pool P, Ctl* ctl,
                                                     long long total_units, float4* __restrict__ parts, int* status,
                                                     Counters* ctr) {
   const int w = blockIdx.x * blockDim.x + threadIdx.x;

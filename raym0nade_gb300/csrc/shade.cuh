@@ -7,6 +7,10 @@
 #include "trace.cuh"
 
 #define RMN_LUM f3(0.3f, 0.6f, 0.1f)  // RGB_Weight, include/geometry.h:16
+// The three largest routines are real calls: inlined at their many call
+// sites they multiply the integrator kernels' code, and warps in different
+// phases then stall on instruction fetch.
+#define RMN_CALL static __device__ __noinline__
 #define RMN_MAX_TRYS 16                // src/sampling.cpp:201
 
 __constant__ int c_sample_count[17] = {0, 1, 2, 2, 3, 3, 3, 4, 4, 4, 4, 5, 5, 5, 5, 5, 6};  // src/render.cpp:126
@@ -114,7 +118,7 @@ RMN_D void lum_clamp(float3& v) {  // clamp(vec3&), src/sampling.cpp:238-243
 
 // BSDF::getBRDF, src/sampling.cpp:49-157 (subsurface, sheen, tints 0;
 // clearcoat 1.5, gloss 0.2). V = in, N = surfN.
-RMN_D float3 brdf(const Surf& s, float3 V, float3 L) {
+RMN_CALL float3 brdf(const Surf& s, float3 V, float3 L) {
   const float3 N = s.surfN;
   float nl = dot3(N, L), nv = dot3(N, V);
   if (nl <= 0.0f || nv <= 0.0f) return f3(0.0f);
@@ -200,7 +204,7 @@ RMN_D float dlog_gtr2(float c, float r) {
   float t = 1.0f + (r * r - 1.0f) * c * c;
   return 2.0f / r - 4.0f * r * c * c / t;
 }
-RMN_D void sample_reflect(const Surf& s, float3 in, RmnRng& rng, float3& dir, float3& w, int& fails,
+RMN_CALL void sample_reflect(const Surf& s, float3 in, RmnRng& rng, float3& dir, float3& w, int& fails,
                           ReflectAD* ad = nullptr) {
   float3 t, b;
   frame(s, in, t, b);
@@ -322,7 +326,7 @@ RMN_D bool light_weights(const DevScene& s, const Surf& sf, float3 V, float* w, 
 // if that ray is unoccluded (bsdf value clamped at luminance 64, light,
 // weight). Returns false when the sample is dropped before any shadow test.
 // Light weights `w` / `tot` come from light_weights (light mode only).
-RMN_D bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float* w, float tot, int cnt, RmnRng& rng,
+RMN_CALL bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float* w, float tot, int cnt, RmnRng& rng,
                      float3& dir, float& aim, LSample& out, int* light_index = nullptr) {
   const float3 pos = sf.pos;
   if (s.sky_w == 0) {
