@@ -12,17 +12,17 @@
 // Kernels, on one stream:
 //  1. primary_kernel  -- one thread per pixel of every job: camera ray (no
 //     jitter, as the reference), closest hit, hit shading -> G-buffer.
-//  2. per iteration, until no worker is left:
-//     logic_kernel    -- a pool of W workers; each advances its state machine
-//                        (take a unit, start a slot, consume the last trace
-//                        result, shade, sample, accumulate) until it needs a
-//                        ray traced, then appends itself to the closest-hit or
-//                        the shadow queue;
+//  2. per iteration, until no worker is left, over a pool of W workers
+//     (path state in HBM, structure of arrays):
+//     shade_kernel, nee_kernel, slot_kernel -- the integrator's logic, split
+//                        by phase so that each kernel runs over a compacted
+//                        list of the workers in its phase (see below); every
+//                        worker ends the iteration with one ray queued or
+//                        retired;
 //     qtrace_kernel<closest>, qtrace_kernel<shadow> -- persistent traversal
-//                        of the queues with per-lane dynamic ray fetch.
-//     Path state lives in HBM between the kernels, so traversal runs at the
-//     occupancy of a 60-register kernel and each kernel's warps execute one
-//     phase only.
+//                        of the ray queues with per-lane dynamic ray fetch.
+//     Traversal thus runs at the occupancy of a 64-register kernel, and the
+//     shading code runs on warps of one phase each.
 //  3. finalize_kernel -- per pixel, merges its units' partial accumulators
 //     in unit order and writes the four RadianceData buffers.
 //
@@ -61,14 +61,26 @@ struct Counters {
   unsigned long long closest, shadow, inner, leaves, tris, slots;
 };
 
-// Per-iteration control words. The first five are cleared before every
-// logic pass; next_unit runs over the whole render.
+// Queue lengths of one iteration parity; cleared when an iteration of that
+// parity starts.
+struct QLen {
+  unsigned int c, sn, sd;    // ray queues: closest, shadow (NEE), shadow (first vertex)
+  unsigned int nee, slot;    // hand-offs to nee_kernel / slot_kernel within the iteration
+  unsigned int c_next, s_next;  // fetch cursors of the trace kernels
+  unsigned int pad;
+};
 struct Ctl {
-  unsigned int qc, qs;            // queue lengths
-  unsigned int qc_next, qs_next;  // fetch cursors of the trace kernels
-  unsigned int live;              // workers not yet retired
-  unsigned int pad0;
-  unsigned long long next_unit;
+  QLen q[2];
+  unsigned long long next_unit;  // runs over the whole render
+};
+
+// Worker-id lists. The ray queues are double-buffered by iteration parity.
+struct Queues {
+  int* c[2];
+  int* sn[2];
+  int* sd[2];
+  int* nee;
+  int* slot;
 };
 
 // Worker pool in HBM (structure of arrays).
@@ -86,8 +98,6 @@ struct Pool {
   float4* lw;      // 2 per worker: light weights 0..7
   int4* nk;        // NEE sample k, count
   float4* pend;    // 2 per worker: pending sample bsdf|weight, light|-
-  int* qc;         // closest-hit queue (worker ids)
-  int* qs;         // shadow queue
 };
 
 // Partial accumulator of one unit: 7 float4.
@@ -257,40 +267,227 @@ __device__ __forceinline__ T agg_inc(T* ctr) {
 
 __device__ __forceinline__ void push(int* q, unsigned int* qn, int w) { q[agg_inc(qn)] = w; }
 
-// Advances worker w until it needs a ray traced (then it is queued) or no
-// unit is left. State machine over the reference's control flow:
-//   PH_FETCH        take the next unit (a pixel and a slot range)
-//   PH_SLOT         start slot j: a first-vertex light sample (shadow ray)
-//                   or the first bounce of an indirect path (closest-hit ray)
-//   PH_WAIT_DIRECT  shadow answer of a first-vertex light sample
-//   PH_WAIT_CLOSEST closest-hit answer of a path ray: sampleRay's body
-//   PH_NEE          next light sample of the terminating vertex
-//   PH_WAIT_NEE     shadow answer of that light sample
+// The logic of one iteration runs as three kernels, each over a compacted
+// list of the workers in its phase, so a warp executes one phase's code:
+//   shade_kernel  closest-hit answers (sampleRay's body): emit the sky or an
+//                 emitter, start the terminating vertex's light samples, or
+//                 sample the next bounce (closest-hit queue);
+//   nee_kernel    shadow answers of terminating-vertex light samples and the
+//                 workers shade_kernel handed over: emit, then draw the next
+//                 light sample (shadow queue) until the vertex is done;
+//   slot_kernel   shadow answers of first-vertex light samples and the
+//                 workers whose slot ended in the two kernels before: start
+//                 the next slot (fetching units) until one queues a ray, or
+//                 retire when no unit is left.
+// Ray queues are double-buffered by iteration parity: the queues filled in
+// iteration i are traced in iteration i and consumed in iteration i + 1.
+
+// Light samples of the terminating vertex from nk.x on, until one is queued
+// (true) or none is left (false).
+__device__ __forceinline__ bool nee_next(const Job* J, const Pool& P, int w, RmnRng& rng, int4& nk) {
+  const DevScene& s = J->s;
+  const float4* nv = P.nv + 5 * (size_t)w;
+  float4 a = nv[0], b = nv[1], c = nv[2], d = nv[3], e = nv[4];
+  Surf sf = default_surf();
+  sf.pos = f3(a.x, a.y, a.z);
+  sf.shapeN = f3(b.x, b.y, b.z);
+  sf.roughness = b.w;
+  sf.surfN = f3(c.x, c.y, c.z);
+  sf.metallic = c.w;
+  sf.base = f3(d.x, d.y, d.z);
+  sf.eta = d.w;
+  float4 l0 = P.lw[2 * w], l1 = P.lw[2 * w + 1];
+  float lwt[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
+  for (; nk.x < nk.y; ++nk.x) {
+    float3 dir;
+    float aim;
+    LSample ls;
+    if (!light_gen(s, sf, f3(e.x, e.y, e.z), lwt, e.w, nk.y, rng, dir, aim, ls)) continue;
+    ls.bsdf *= a.w;  // scaling(samples, factor), src/render.cpp:101-104
+    P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
+    P.rd[w] = make_float4(dir.x, dir.y, dir.z, aim);
+    P.pend[2 * w] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
+    P.pend[2 * w + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
+    return true;
+  }
+  return false;
+}
+
+__device__ __forceinline__ void store_worker(const Pool& P, int w, int4 ph, int phase, const RmnRng& rng, int4 un) {
+  ph.x = phase;
+  ph.y = (int)rng.ctr;
+  P.ph[w] = ph;
+  P.unit[w] = un;
+}
+
+__global__ void __launch_bounds__(128, 8) shade_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+                                                       int par, float4* __restrict__ parts, int* status) {
+  const unsigned n = ctl->q[par ^ 1].c;
+  const int* in = Q.c[par ^ 1];
+  QLen* out = &ctl->q[par];
+  for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const int w = in[idx];
+    int4 ph = P.ph[w];
+    int4 un = P.unit[w];
+    const Job* J = &jobs[un.x];
+    const Params& p = J->p;
+    const DevScene& s = J->s;
+    RmnRng rng;
+    rng.key = rmn_stream_key(p.seed, (uint32_t)un.y, (uint32_t)un.z);
+    rng.ctr = (unsigned)ph.y;
+    float4* part = parts + (size_t)P.uid[w] * RMN_PART_F4;
+    // sampleRay's body, src/render.cpp:121-312, opaque surfaces
+    float2 res = P.res[w];
+    int h = __float_as_int(res.x);
+    float4 o4 = P.ro[w], d4 = P.rd[w];
+    float3 o = f3(o4.x, o4.y, o4.z), dir = f3(d4.x, d4.y, d4.z);
+    int depth = ph.z;
+    bool exclude = (ph.w & FL_EXCLUDE) != 0;
+    int phase = PH_SLOT;  // unless set below, the slot ends here
+    if (h == -2) {
+      atomicExch(status, 1);
+    } else if (h < 0) {
+      float4 pb = P.pb[w];
+      if (!exclude && s.sky_w)
+        emit(part, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp, {f3(1.0f), sky_get(s, dir), 1.0f},
+             un.z * 8);
+    } else {
+      float4 pb = P.pb[w];
+      Surf sf = default_surf();
+      sf.pos = o + dir * res.y;
+      hit_info(s, h, dir, sf);
+      float rf = fmaxf(pb.w, 1.0f * sf.roughness);
+      sf.roughness = fmaxf(sf.roughness, rf);
+      const float p_rr = 1.0f + (0.5f - 1.0f) * sqrtf(sf.roughness);
+      bool nee = p_rr < 0.9f;
+      if (len3(sf.emis) > RMN_EPS) {
+        if (!exclude)
+          emit(part, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp, {f3(1.0f), sf.emis, 1.0f},
+               un.z * 8);
+      } else if (rng.next() <= 1.0f) {
+        nee = nee && sf.entering;
+        const float3 V = -dir;
+        if (nee && (depth >= p.maxd || rng.next() > p_rr)) {
+          int cnt = c_sample_count[depth < 16 ? depth : 16];
+          float k = 1.0f / 1.0f;
+          if (depth < p.maxd) k /= (1.0f - p_rr);
+          float lwt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+          float tot = 0.0f;
+          if (s.sky_w != 0 || light_weights(s, sf, V, lwt, tot)) {
+            float4* nv = P.nv + 5 * (size_t)w;
+            nv[0] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, k);
+            nv[1] = make_float4(sf.shapeN.x, sf.shapeN.y, sf.shapeN.z, sf.roughness);
+            nv[2] = make_float4(sf.surfN.x, sf.surfN.y, sf.surfN.z, sf.metallic);
+            nv[3] = make_float4(sf.base.x, sf.base.y, sf.base.z, sf.eta);
+            nv[4] = make_float4(V.x, V.y, V.z, tot);
+            P.lw[2 * w] = make_float4(lwt[0], lwt[1], lwt[2], lwt[3]);
+            P.lw[2 * w + 1] = make_float4(lwt[4], lwt[5], lwt[6], lwt[7]);
+            P.nk[w] = make_int4(0, cnt, 0, 0);
+            phase = PH_NEE;
+          }
+        } else {
+          float3 nd, wv;
+          int nf = 0;
+          sample_reflect(sf, V, rng, nd, wv, nf);
+          wv = wv / 1.0f;
+          if (nee) wv = wv / p_rr;
+          if (any_finite3(nd) && depth != p.maxd) {
+            float3 thr = f3(pb.x, pb.y, pb.z) * wv;
+            P.pb[w] = make_float4(thr.x, thr.y, thr.z, rf);
+            if (nf > 0) {
+              float4 pa = P.pa[w];
+              pa.w = pa.w * (1.0f / (float)(1 + nf));
+              P.pa[w] = pa;
+            }
+            P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
+            P.rd[w] = make_float4(nd.x, nd.y, nd.z, INFINITY);
+            ph.z = depth + 1;
+            ph.w = nee ? FL_EXCLUDE : 0;
+            phase = PH_WAIT_CLOSEST;
+          }
+        }
+      }
+    }
+    if (phase == PH_SLOT) un.z++;
+    store_worker(P, w, ph, phase, rng, un);
+    if (phase == PH_WAIT_CLOSEST) push(Q.c[par], &out->c, w);
+    else if (phase == PH_NEE) push(Q.nee, &out->nee, w);
+    else push(Q.slot, &out->slot, w);
+  }
+}
+
+__global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+                                                     int par, float4* __restrict__ parts) {
+  QLen* out = &ctl->q[par];
+  const unsigned a = ctl->q[par ^ 1].sn, n = a + out->nee;
+  const int* in = Q.sn[par ^ 1];
+  for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const int w = idx < a ? in[idx] : Q.nee[idx - a];
+    int4 ph = P.ph[w];
+    int4 un = P.unit[w];
+    const Job* J = &jobs[un.x];
+    RmnRng rng;
+    rng.key = rmn_stream_key(J->p.seed, (uint32_t)un.y, (uint32_t)un.z);
+    rng.ctr = (unsigned)ph.y;
+    int4 nk = P.nk[w];
+    if (ph.x == PH_WAIT_NEE) {
+      if (P.res[w].x == 0.0f) {
+        float4 pa4 = P.pend[2 * w], pb4 = P.pend[2 * w + 1];
+        float4 pb = P.pb[w];
+        emit(parts + (size_t)P.uid[w] * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), J->p.inv_spp,
+             {f3(pa4.x, pa4.y, pa4.z), f3(pb4.x, pb4.y, pb4.z), pa4.w}, un.z * 8 + nk.x);
+      }
+      nk.x++;
+    }
+    const bool queued = nee_next(J, P, w, rng, nk);
+    P.nk[w] = make_int4(nk.x, nk.y, 0, 0);
+    if (!queued) un.z++;
+    store_worker(P, w, ph, queued ? PH_WAIT_NEE : PH_SLOT, rng, un);
+    if (queued) push(Q.sn[par], &out->sn, w);
+    else push(Q.slot, &out->slot, w);
+  }
+}
+
 template <bool COUNT>
-__global__ void __launch_bounds__(128, 8) logic_kernel(const Job* __restrict__ jobs, int njobs, Pool P, Ctl* ctl,
-                                                    long long total_units, float4* __restrict__ parts, int* status,
-                                                    Counters* ctr) {
-  const int w = blockIdx.x * blockDim.x + threadIdx.x;
-  if (w >= P.W) return;
-  int4 ph = P.ph[w];
-  int phase = ph.x;
-  if (phase == PH_DONE) return;
-  int4 un = P.unit[w];
-  long long uid = P.uid[w];
+__global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jobs, int njobs, Pool P, Queues Q,
+                                                      Ctl* ctl, int par, long long total_units,
+                                                      float4* __restrict__ parts, Counters* ctr) {
+  QLen* out = &ctl->q[par];
+  const unsigned a = ctl->q[par ^ 1].sd, n = a + out->slot;
+  const int* in = Q.sd[par ^ 1];
   unsigned long long slots_done = 0;
-  const Job* J = phase == PH_FETCH ? nullptr : &jobs[un.x];
-  RmnRng rng;
-  rng.key = 0;
-  rng.ctr = (unsigned)ph.y;
-  if (J) rng.key = rmn_stream_key(J->p.seed, (uint32_t)un.y, (uint32_t)un.z);
-  bool stop = false;
-  for (int guard = 0; guard < 4096 && !stop; ++guard) {
-    switch (phase) {
-      case PH_FETCH: {
+  for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const int w = idx < a ? in[idx] : Q.slot[idx - a];
+    int4 ph = P.ph[w];
+    int phase = ph.x;
+    int4 un = P.unit[w];
+    long long uid = P.uid[w];
+    const Job* J = phase == PH_FETCH ? nullptr : &jobs[un.x];
+    RmnRng rng;
+    rng.key = 0;
+    rng.ctr = (unsigned)ph.y;
+    if (phase == PH_WAIT_DIRECT) {
+      if (P.res[w].x == 0.0f) {
+        float4 b0 = P.pend[2 * w], b1 = P.pend[2 * w + 1];
+        Rad4 d, sp;
+        demodulate(base_of(*J, un.y), f3(b0.x, b0.y, b0.z), f3(b1.x, b1.y, b1.z), b0.w, d, sp);
+        float4* part = parts + (size_t)uid * RMN_PART_F4;
+        Rad4 dd = r4(part[0]), ds = r4(part[1]);
+        radd(dd, d);
+        radd(ds, sp);
+        part[0] = f4(dd);
+        part[1] = f4(ds);
+      }
+      un.z++;
+      phase = PH_SLOT;
+    }
+    // Start slots until one queues a ray; every pass advances the slot or
+    // takes a new unit, so the loop ends within the units of the batch.
+    for (;;) {
+      if (phase == PH_FETCH) {
         unsigned long long u = agg_inc(&ctl->next_unit);
         if ((long long)u >= total_units) {
           phase = PH_DONE;
-          stop = true;
           break;
         }
         uid = (long long)u;
@@ -307,245 +504,82 @@ __global__ void __launch_bounds__(128, 8) logic_kernel(const Job* __restrict__ j
         bool hit = any_finite3(f3(gb[6], gb[7], gb[8]));
         un = make_int4(jb, pixel, hit ? j0 : j1, j1);
         phase = PH_SLOT;
-        break;
+        continue;
       }
-      case PH_SLOT: {
-        if (un.z >= un.w) {
-          phase = PH_FETCH;
-          break;
-        }
-        const Params& p = J->p;
-        const DevScene& s = J->s;
-        rng = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)un.z);
-        if (COUNT) slots_done++;
-        Surf g = load_first_vertex(*J, un.y);
-        if (un.z < p.spp_d) {
-          // sampleDirectLightFromFirstIntersection, src/render.cpp:425-437
-          if (len3(g.emis) > 0.0f) {
-            un.z++;
-            break;
-          }
-          float3 Vd = -norm3(g.pos - p.pos);
-          float lwt[8];
-          float tot = 0.0f;
-          if (s.sky_w == 0 && !light_weights(s, g, Vd, lwt, tot)) {
-            un.z++;
-            break;
-          }
-          float3 dir;
-          float aim;
-          LSample ls;
-          if (!light_gen(s, g, Vd, lwt, tot, p.spp_d, rng, dir, aim, ls)) {
-            un.z++;
-            break;
-          }
-          P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
-          P.rd[w] = make_float4(dir.x, dir.y, dir.z, aim);
-          P.pend[2 * w] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
-          P.pend[2 * w + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
-          push(P.qs, &ctl->qs, w);
-          phase = PH_WAIT_DIRECT;
-          stop = true;
-          break;
-        }
-        // sampleIndirectLightFromFirstIntersection, src/render.cpp:314-423
-        if (len3(g.emis) > 0.0f || !(rng.next() < 1.0f)) {
-          un.z++;
-          break;
-        }
-        float3 in = norm3(g.pos - p.pos);
-        Surf v0 = g;
-        v0.eta = 1.0f / v0.eta;
-        float3 dir, w0;
-        int f0 = 0;
-        sample_reflect(v0, -in, rng, dir, w0, f0);
-        if (!any_finite3(dir)) {
-          un.z++;
-          break;
-        }
-        P.pa[w] = make_float4(w0.x, w0.y, w0.z, f0 > 0 ? 1.0f / (float)(1 + f0) : 1.0f);
-        P.pb[w] = make_float4(1.0f, 1.0f, 1.0f, g.roughness * 1.0f);
-        P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
-        P.rd[w] = make_float4(dir.x, dir.y, dir.z, INFINITY);
-        ph.z = 1;           // depth of the vertex this ray will hit
-        ph.w = FL_EXCLUDE;  // the first bounce excludes direct light
-        push(P.qc, &ctl->qc, w);
-        phase = PH_WAIT_CLOSEST;
-        stop = true;
-        break;
+      if (un.z >= un.w) {
+        phase = PH_FETCH;
+        continue;
       }
-      case PH_WAIT_DIRECT: {
-        if (P.res[w].x == 0.0f) {
-          float4 a = P.pend[2 * w], b = P.pend[2 * w + 1];
-          Rad4 d, sp;
-          demodulate(base_of(*J, un.y), f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w, d, sp);
-          float4* part = parts + (size_t)uid * RMN_PART_F4;
-          Rad4 dd = r4(part[0]), ds = r4(part[1]);
-          radd(dd, d);
-          radd(ds, sp);
-          part[0] = f4(dd);
-          part[1] = f4(ds);
-        }
-        un.z++;
-        phase = PH_SLOT;
-        break;
-      }
-      case PH_WAIT_CLOSEST: {
-        // sampleRay's body, src/render.cpp:121-312, opaque surfaces
-        const Params& p = J->p;
-        const DevScene& s = J->s;
-        float2 res = P.res[w];
-        int h = __float_as_int(res.x);
-        float4 o4 = P.ro[w], d4 = P.rd[w];
-        float3 o = f3(o4.x, o4.y, o4.z), dir = f3(d4.x, d4.y, d4.z);
-        int depth = ph.z;
-        bool exclude = (ph.w & FL_EXCLUDE) != 0;
-        if (h == -2) {
-          atomicExch(status, 1);
+      const Params& p = J->p;
+      const DevScene& s = J->s;
+      rng = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)un.z);
+      if (COUNT) slots_done++;
+      Surf g = load_first_vertex(*J, un.y);
+      if (un.z < p.spp_d) {
+        // sampleDirectLightFromFirstIntersection, src/render.cpp:425-437
+        if (len3(g.emis) > 0.0f) {
           un.z++;
-          phase = PH_SLOT;
-          break;
+          continue;
         }
-        float4 pb = P.pb[w];
-        if (h < 0) {
-          if (!exclude && s.sky_w)
-            emit(parts + (size_t)uid * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp,
-                 {f3(1.0f), sky_get(s, dir), 1.0f}, un.z * 8);
+        float3 Vd = -norm3(g.pos - p.pos);
+        float lwt[8];
+        float tot = 0.0f;
+        if (s.sky_w == 0 && !light_weights(s, g, Vd, lwt, tot)) {
           un.z++;
-          phase = PH_SLOT;
-          break;
+          continue;
         }
-        Surf sf = default_surf();
-        sf.pos = o + dir * res.y;
-        hit_info(s, h, dir, sf);
-        float rf = fmaxf(pb.w, 1.0f * sf.roughness);
-        sf.roughness = fmaxf(sf.roughness, rf);
-        const float p_rr = 1.0f + (0.5f - 1.0f) * sqrtf(sf.roughness);
-        bool nee = p_rr < 0.9f;
-        if (len3(sf.emis) > RMN_EPS) {
-          if (!exclude)
-            emit(parts + (size_t)uid * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp,
-                 {f3(1.0f), sf.emis, 1.0f}, un.z * 8);
-          un.z++;
-          phase = PH_SLOT;
-          break;
-        }
-        if (!(rng.next() <= 1.0f)) {
-          un.z++;
-          phase = PH_SLOT;
-          break;
-        }
-        nee = nee && sf.entering;
-        const float3 V = -dir;
-        if (nee && (depth >= p.maxd || rng.next() > p_rr)) {
-          int cnt = c_sample_count[depth < 16 ? depth : 16];
-          float k = 1.0f / 1.0f;
-          if (depth < p.maxd) k /= (1.0f - p_rr);
-          float lwt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-          float tot = 0.0f;
-          if (s.sky_w == 0 && !light_weights(s, sf, V, lwt, tot)) {
-            un.z++;
-            phase = PH_SLOT;
-            break;
-          }
-          float4* nv = P.nv + 5 * (size_t)w;
-          nv[0] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, k);
-          nv[1] = make_float4(sf.shapeN.x, sf.shapeN.y, sf.shapeN.z, sf.roughness);
-          nv[2] = make_float4(sf.surfN.x, sf.surfN.y, sf.surfN.z, sf.metallic);
-          nv[3] = make_float4(sf.base.x, sf.base.y, sf.base.z, sf.eta);
-          nv[4] = make_float4(V.x, V.y, V.z, tot);
-          P.lw[2 * w] = make_float4(lwt[0], lwt[1], lwt[2], lwt[3]);
-          P.lw[2 * w + 1] = make_float4(lwt[4], lwt[5], lwt[6], lwt[7]);
-          P.nk[w] = make_int4(0, cnt, 0, 0);
-          phase = PH_NEE;
-          break;
-        }
-        float3 nd, wv;
-        int nf = 0;
-        sample_reflect(sf, V, rng, nd, wv, nf);
-        wv = wv / 1.0f;
-        if (nee) wv = wv / p_rr;
-        if (!any_finite3(nd) || depth == p.maxd) {
-          un.z++;
-          phase = PH_SLOT;
-          break;
-        }
-        float3 thr = f3(pb.x, pb.y, pb.z) * wv;
-        P.pb[w] = make_float4(thr.x, thr.y, thr.z, rf);
-        if (nf > 0) {
-          float4 pa = P.pa[w];
-          pa.w = pa.w * (1.0f / (float)(1 + nf));
-          P.pa[w] = pa;
-        }
-        P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
-        P.rd[w] = make_float4(nd.x, nd.y, nd.z, INFINITY);
-        ph.z = depth + 1;
-        ph.w = nee ? FL_EXCLUDE : 0;
-        push(P.qc, &ctl->qc, w);
-        stop = true;
-        break;
-      }
-      case PH_NEE: {
-        int4 nk = P.nk[w];
-        if (nk.x >= nk.y) {
-          un.z++;
-          phase = PH_SLOT;
-          break;
-        }
-        const DevScene& s = J->s;
-        const float4* nv = P.nv + 5 * (size_t)w;
-        float4 a = nv[0], b = nv[1], c = nv[2], d = nv[3], e = nv[4];
-        Surf sf = default_surf();
-        sf.pos = f3(a.x, a.y, a.z);
-        sf.shapeN = f3(b.x, b.y, b.z);
-        sf.roughness = b.w;
-        sf.surfN = f3(c.x, c.y, c.z);
-        sf.metallic = c.w;
-        sf.base = f3(d.x, d.y, d.z);
-        sf.eta = d.w;
-        float4 l0 = P.lw[2 * w], l1 = P.lw[2 * w + 1];
-        float lwt[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
         float3 dir;
         float aim;
         LSample ls;
-        if (!light_gen(s, sf, f3(e.x, e.y, e.z), lwt, e.w, nk.y, rng, dir, aim, ls)) {
-          P.nk[w] = make_int4(nk.x + 1, nk.y, 0, 0);
-          break;
+        if (!light_gen(s, g, Vd, lwt, tot, p.spp_d, rng, dir, aim, ls)) {
+          un.z++;
+          continue;
         }
-        ls.bsdf *= a.w;  // scaling(samples, factor), src/render.cpp:101-104
-        P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
+        P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
         P.rd[w] = make_float4(dir.x, dir.y, dir.z, aim);
         P.pend[2 * w] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
         P.pend[2 * w + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
-        push(P.qs, &ctl->qs, w);
-        phase = PH_WAIT_NEE;
-        stop = true;
+        phase = PH_WAIT_DIRECT;
         break;
       }
-      case PH_WAIT_NEE: {
-        if (P.res[w].x == 0.0f) {
-          float4 a = P.pend[2 * w], b = P.pend[2 * w + 1];
-          float4 pb = P.pb[w];
-          emit(parts + (size_t)uid * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), J->p.inv_spp,
-               {f3(a.x, a.y, a.z), f3(b.x, b.y, b.z), a.w}, un.z * 8 + P.nk[w].x);
-        }
-        int4 nk = P.nk[w];
-        P.nk[w] = make_int4(nk.x + 1, nk.y, 0, 0);
-        phase = PH_NEE;
-        break;
+      // sampleIndirectLightFromFirstIntersection, src/render.cpp:314-423
+      if (len3(g.emis) > 0.0f || !(rng.next() < 1.0f)) {
+        un.z++;
+        continue;
       }
-      default:
-        stop = true;
-        break;
+      float3 in0 = norm3(g.pos - p.pos);
+      Surf v0 = g;
+      v0.eta = 1.0f / v0.eta;
+      float3 dir, w0;
+      int f0 = 0;
+      sample_reflect(v0, -in0, rng, dir, w0, f0);
+      if (!any_finite3(dir)) {
+        un.z++;
+        continue;
+      }
+      P.pa[w] = make_float4(w0.x, w0.y, w0.z, f0 > 0 ? 1.0f / (float)(1 + f0) : 1.0f);
+      P.pb[w] = make_float4(1.0f, 1.0f, 1.0f, g.roughness * 1.0f);
+      P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
+      P.rd[w] = make_float4(dir.x, dir.y, dir.z, INFINITY);
+      ph.z = 1;           // depth of the vertex this ray will hit
+      ph.w = FL_EXCLUDE;  // the first bounce excludes direct light
+      phase = PH_WAIT_CLOSEST;
+      break;
     }
+    store_worker(P, w, ph, phase, rng, un);
+    P.uid[w] = uid;
+    if (phase == PH_WAIT_DIRECT) push(Q.sd[par], &out->sd, w);
+    else if (phase == PH_WAIT_CLOSEST) push(Q.c[par], &out->c, w);
   }
-  ph.x = phase;
-  ph.y = (int)rng.ctr;
-  P.ph[w] = ph;
-  P.unit[w] = un;
-  P.uid[w] = uid;
-  if (phase != PH_DONE) agg_inc(&ctl->live);
   if (COUNT && slots_done) atomicAdd(&ctr->slots, slots_done);
+}
+
+// Seeds the first iteration: every worker (in PH_FETCH) is listed as if it
+// had queued a first-vertex shadow ray in the iteration before.
+__global__ void seed_kernel(Queues Q, Ctl* ctl, int W) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < W) Q.sd[1][i] = i;
+  if (i == 0) ctl->q[1].sd = (unsigned)W;
 }
 
 constexpr int kFetchBudget = 16;  // node visits between refill checks
@@ -556,13 +590,17 @@ constexpr int kFetchBudget = 16;  // node visits between refill checks
 // longest ray. The rays of a batch belong to different scenes; each lane
 // traverses its own job's BVH.
 template <bool SHADOW, bool COUNT>
-__global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Ctl* ctl, int* status,
-                                                     Counters* ctr) {
+__global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+                                                     int par, int* status, Counters* ctr) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
-  const unsigned n = SHADOW ? ctl->qs : ctl->qc;
-  unsigned int* next = SHADOW ? &ctl->qs_next : &ctl->qc_next;
-  const int* q = SHADOW ? P.qs : P.qc;
+  QLen* ql = &ctl->q[par];
+  // the shadow kernel traces the NEE list, then the first-vertex list
+  const unsigned na = SHADOW ? ql->sn : ql->c;
+  const unsigned n = SHADOW ? na + ql->sd : na;
+  unsigned int* next = SHADOW ? &ql->s_next : &ql->c_next;
+  const int* qa = SHADOW ? Q.sn[par] : Q.c[par];
+  const int* qb = Q.sd[par];
   bool active = false, retired = false;
   int w = 0;
   TRay r;
@@ -580,7 +618,7 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
       if (!active && !retired) {
         unsigned i = base + __popc(need & lt);
         if (i < n) {
-          w = q[i];
+          w = i < na ? qa[i] : qb[i - na];
           float4 o = P.ro[w], d = P.rd[w];
           s = jobs[P.unit[w].x].s;
           r = make_tray(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
@@ -708,6 +746,7 @@ struct BatchState {
   int* d_status = nullptr;
   float4* d_parts = nullptr;
   Pool pool{};
+  Queues q{};
   std::vector<void*> allocs;
   cudaGraphExec_t init_exec = nullptr, chunk_exec = nullptr, fin_exec = nullptr;
   bool use_graph = false;
@@ -750,31 +789,41 @@ static cudaError_t launch_init(BatchState* b, cudaStream_t st, Counters* ctr) {
   if (e != cudaSuccess) return e;
   if (ctr) primary_kernel<true><<<(tp + 127) / 128, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
   else primary_kernel<false><<<(tp + 127) / 128, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
+  seed_kernel<<<(b->pool.W + 127) / 128, 128, 0, st>>>(b->q, b->d_ctl, b->pool.W);
   return cudaGetLastError();
 }
 
-static cudaError_t launch_iteration(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t* ev = nullptr) {
+// Iteration k of a chunk (parity k & 1): the three logic kernels, then the
+// two traversal kernels. ev (optional) records [0] before the logic, [1]
+// after it and [3] after the traversal.
+static cudaError_t launch_iteration(BatchState* b, cudaStream_t st, Counters* ctr, int k, cudaEvent_t* ev = nullptr) {
   const int nj = (int)b->table.jobs.size();
-  cudaError_t e = cudaMemsetAsync(b->d_ctl, 0, offsetof(Ctl, pad0), st);
+  const int par = k & 1;
+  cudaError_t e = cudaMemsetAsync(&b->d_ctl->q[par], 0, sizeof(QLen), st);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[0], st);
-  const int lb = (b->pool.W + 127) / 128;
-  if (ctr)
-    logic_kernel<true><<<lb, 128, 0, st>>>(b->d_jobs, nj, b->pool, b->d_ctl, b->table.total_units, b->d_parts,
-                                           b->d_status, ctr);
-  else
-    logic_kernel<false><<<lb, 128, 0, st>>>(b->d_jobs, nj, b->pool, b->d_ctl, b->table.total_units, b->d_parts,
-                                            b->d_status, ctr);
+  const int sms = device_sms();
+  const int gs = sms * blocks_per_sm(shade_kernel), gn = sms * blocks_per_sm(nee_kernel);
+  shade_kernel<<<gs, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_parts, b->d_status);
+  nee_kernel<<<gn, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_parts);
+  if (ctr) {
+    slot_kernel<true><<<sms * blocks_per_sm(slot_kernel<true>), 128, 0, st>>>(
+        b->d_jobs, nj, b->pool, b->q, b->d_ctl, par, b->table.total_units, b->d_parts, ctr);
+  } else {
+    slot_kernel<false><<<sms * blocks_per_sm(slot_kernel<false>), 128, 0, st>>>(
+        b->d_jobs, nj, b->pool, b->q, b->d_ctl, par, b->table.total_units, b->d_parts, ctr);
+  }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[1], st);
-  int tb = device_sms() * (ctr ? blocks_per_sm(qtrace_kernel<false, true>) : blocks_per_sm(qtrace_kernel<false, false>));
+  const int lb = (b->pool.W + 127) / 128;
+  int tb = sms * (ctr ? blocks_per_sm(qtrace_kernel<false, true>) : blocks_per_sm(qtrace_kernel<false, false>));
   if (tb > lb) tb = lb;
   if (ctr) {
-    qtrace_kernel<false, true><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->d_ctl, b->d_status, ctr);
-    qtrace_kernel<true, true><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->d_ctl, b->d_status, ctr);
+    qtrace_kernel<false, true><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_status, ctr);
+    qtrace_kernel<true, true><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_status, ctr);
   } else {
-    qtrace_kernel<false, false><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->d_ctl, b->d_status, ctr);
-    qtrace_kernel<true, false><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->d_ctl, b->d_status, ctr);
+    qtrace_kernel<false, false><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_status, ctr);
+    qtrace_kernel<true, false><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_status, ctr);
   }
   if (ev) cudaEventRecord(ev[3], st);
   return cudaGetLastError();
@@ -815,24 +864,28 @@ static rmn_status run(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t
   e = graph ? cudaGraphLaunch(b->init_exec, st) : launch_init(b, st, ctr);
   if (e != cudaSuccess) return cuda_fail(e, "render init");
   if (ev) cudaEventRecord(ev[1], st);
+  // Rays queued by the last iteration of a chunk (parity 1): the workers
+  // still alive. The chunk length is even, so parities repeat chunk to chunk.
+  static_assert(kIterationsPerChunk % 2 == 0, "iteration parity must repeat across chunks");
   Ctl h{};
-  h.live = 1;
+  unsigned int live = 1;
   unsigned int last_live = 0xffffffffu;
   unsigned long long last_next = 0;
   int stalled = 0;
   long long iters = 0;
-  while (h.live) {
+  while (live) {
     if (graph) {
       e = cudaGraphLaunch(b->chunk_exec, st);
     } else {
       for (int k = 0; k < kIterationsPerChunk && e == cudaSuccess; ++k)
-        e = launch_iteration(b, st, ctr, kt ? kt->e[k] : nullptr);
+        e = launch_iteration(b, st, ctr, k, kt ? kt->e[k] : nullptr);
     }
     if (e != cudaSuccess) return cuda_fail(e, "render iteration");
     iters += kIterationsPerChunk;
     e = cudaMemcpyAsync(&h, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "render iteration");
+    live = h.q[1].c + h.q[1].sn + h.q[1].sd;
     if (kt) {
       for (int k = 0; k < kIterationsPerChunk; ++k) {
         float a = 0.0f, c = 0.0f;
@@ -846,12 +899,12 @@ static rmn_status run(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t
     // Every iteration answers every queued ray, so a chunk that neither
     // retires a worker nor hands out a unit is only possible while paths are
     // long; 4096 such chunks in a row (>32k bounces) means no progress.
-    if (h.live == last_live && h.next_unit == last_next) {
+    if (live == last_live && h.next_unit == last_next) {
       if (++stalled > 4096) return fail(RMN_ERR_DEVICE_LIMIT, "render: no progress over 32768 iterations");
     } else {
       stalled = 0;
     }
-    last_live = h.live;
+    last_live = live;
     last_next = h.next_unit;
     if (iters > kMaxIterations) return fail(RMN_ERR_DEVICE_LIMIT, "render: iteration bound reached");
   }
@@ -904,8 +957,13 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
   alloc((void**)&P.lw, sizeof(float4) * 2 * W);
   alloc((void**)&P.nk, sizeof(int4) * W);
   alloc((void**)&P.pend, sizeof(float4) * 2 * W);
-  alloc((void**)&P.qc, sizeof(int) * W);
-  alloc((void**)&P.qs, sizeof(int) * W);
+  for (int k = 0; k < 2; ++k) {
+    alloc((void**)&b->q.c[k], sizeof(int) * W);
+    alloc((void**)&b->q.sn[k], sizeof(int) * W);
+    alloc((void**)&b->q.sd[k], sizeof(int) * W);
+  }
+  alloc((void**)&b->q.nee, sizeof(int) * W);
+  alloc((void**)&b->q.slot, sizeof(int) * W);
   if (e == cudaSuccess) e = cudaMemcpy(b->d_jobs, b->table.jobs.data(), jb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(b->d_status, 0, sizeof(int));
   if (e == cudaSuccess && use_graph) {
@@ -917,7 +975,7 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
         e = capture(cs,
                     [&] {
                       for (int k = 0; k < kIterationsPerChunk; ++k) {
-                        cudaError_t le = launch_iteration(b, cs, nullptr);
+                        cudaError_t le = launch_iteration(b, cs, nullptr, k);
                         if (le != cudaSuccess) return le;
                       }
                       return cudaSuccess;
