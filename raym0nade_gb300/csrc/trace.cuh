@@ -82,12 +82,14 @@ struct TraceCounters {
 };
 
 // Resumable traversal state: the deferred children (reference plus entry
-// distance) and the current node, so a warp can hand a lane a new ray while
-// its other lanes are still traversing.
+// distance), the current node and the position within the current leaf, so
+// a warp can hand a lane a new ray while its other lanes are still
+// traversing.
 struct Trav {
-  int cur;   // next node reference to visit
+  int cur;     // next node reference to visit
   int sp;
-  int hit;   // leaf-order triangle index of the closest hit so far, -1 none
+  int hit;     // leaf-order triangle index of the closest hit so far, -1 none
+  int ti, te;  // triangles [ti, te) of the current leaf still to test
   float tmax;
   int stack_ref[RMN_STACK];
   float stack_tl[RMN_STACK];
@@ -97,62 +99,73 @@ RMN_D void trav_begin(const DevScene& s, Trav& t, float tmax) {
   t.cur = s.root;
   t.sp = 0;
   t.hit = -1;
+  t.ti = t.te = 0;
   t.tmax = tmax;
 }
 
-// Visits up to `budget` nodes (an inner node or a whole leaf counts one).
-// Returns 1 when the query is answered (t.hit / t.tmax final), 0 when the
-// budget ran out first, -2 if the stack would overflow (never for trees the
-// builder accepts). With ANY set, answers as soon as a hit closer than `aim`
-// is recorded (Model::rayHit_test's question, after the same visits as the
+// Runs up to `budget` steps; a step is one inner node (both child boxes) or
+// one triangle of a leaf, so lanes of a warp at inner nodes and lanes in
+// leaves advance together instead of waiting for a whole leaf. Returns 1
+// when the query is answered (t.hit / t.tmax final), 0 when the budget ran
+// out first, -2 if the stack would overflow (never for trees the builder
+// accepts). With ANY set, answers as soon as a hit closer than `aim` is
+// recorded (Model::rayHit_test's question, after the same visits as the
 // closest-hit query up to that point).
 template <bool ANY, bool COUNT>
 RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav& t, int budget, TraceCounters* cnt) {
   for (;;) {
     if (budget-- <= 0) return 0;
-    int cur = t.cur;
-    if (cur >= 0) {
-      const DevNode* n = s.nodes + cur;
-      float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
-      int4 D = __ldg(&n->d);
-      if (COUNT) cnt->inner++;
-      float tl0, tl1;
-      bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, t.tmax, tl0);
-      bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, t.tmax, tl1);
-      int nref, fref;
-      bool hn, hf;
-      float tlf;
-      if (tl0 < tl1) {
-        nref = D.x; hn = h0; fref = D.y; hf = h1; tlf = tl1;
-      } else {
-        nref = D.y; hn = h1; fref = D.x; hf = h0; tlf = tl0;
+    if (t.ti < t.te) {  // next triangle of the current leaf, in leaf order
+      const int i = t.ti++;
+      const float4* tp = s.tri + 3 * i;
+      float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+      float th = tri_t(r, f3(a), f3(b), f3(c), b.w);
+      if (tmin < th && th < t.tmax) {
+        t.tmax = th;
+        t.hit = i;
+        if (ANY && th < aim) return 1;
       }
-      if (hn) {
-        if (hf) {
-          if (t.sp >= RMN_STACK) return -2;
-          t.stack_ref[t.sp] = fref;
-          t.stack_tl[t.sp] = tlf;
-          ++t.sp;
-        }
-        t.cur = nref;
-        continue;
-      }
-      if (hf && tlf < t.tmax) {
-        t.cur = fref;
-        continue;
-      }
+      if (t.ti < t.te) continue;
     } else {
-      int x = ~cur;
-      int first = x >> 4, count = x & 15;
-      if (COUNT) { cnt->leaves++; cnt->tris += count; }
-      for (int i = first; i < first + count; ++i) {
-        const float4* tp = s.tri + 3 * i;
-        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
-        float th = tri_t(r, f3(a), f3(b), f3(c), b.w);
-        if (tmin < th && th < t.tmax) {
-          t.tmax = th;
-          t.hit = i;
-          if (ANY && th < aim) return 1;
+      const int cur = t.cur;
+      if (cur >= 0) {
+        const DevNode* n = s.nodes + cur;
+        float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
+        int4 D = __ldg(&n->d);
+        if (COUNT) cnt->inner++;
+        float tl0, tl1;
+        bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, t.tmax, tl0);
+        bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, t.tmax, tl1);
+        int nref, fref;
+        bool hn, hf;
+        float tlf;
+        if (tl0 < tl1) {
+          nref = D.x; hn = h0; fref = D.y; hf = h1; tlf = tl1;
+        } else {
+          nref = D.y; hn = h1; fref = D.x; hf = h0; tlf = tl0;
+        }
+        if (hn) {
+          if (hf) {
+            if (t.sp >= RMN_STACK) return -2;
+            t.stack_ref[t.sp] = fref;
+            t.stack_tl[t.sp] = tlf;
+            ++t.sp;
+          }
+          t.cur = nref;
+          continue;
+        }
+        if (hf && tlf < t.tmax) {
+          t.cur = fref;
+          continue;
+        }
+      } else {
+        const int x = ~cur;
+        const int count = x & 15;
+        if (COUNT) { cnt->leaves++; cnt->tris += count; }
+        if (count > 0) {
+          t.ti = x >> 4;
+          t.te = t.ti + count;
+          continue;
         }
       }
     }
