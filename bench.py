@@ -275,7 +275,7 @@ def run_gpu(args, rank, world, dist):
             a.slots_per_unit = tune["slots_per_unit"]
     with torch.cuda.stream(stream):
         batch = api.Batch(list(zip(models, argsl, photos)), use_graph=True, stream=stream,
-                          pool_workers=tune["pool_workers"] if tune else 0)
+                          pool_workers=tune["pool_workers"] if tune else 0, lanes=tune["lanes"] if tune else 0)
 
     def step_batched():
         batch.render(stream)

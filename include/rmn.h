@@ -205,11 +205,12 @@ typedef struct rmn_batch_item {
   rmn_render_args args;
   rmn_image image;
 } rmn_batch_item;
-/* Launch knobs of a batch; NULL options = {1, 0}. */
+/* Launch knobs of a batch; NULL options = {1, 0, 0}. */
 typedef struct rmn_batch_options {
   int32_t use_graph;     /* replay the wavefront iterations from captured CUDA graphs */
-  int32_t pool_workers;  /* concurrent paths in flight (0: library default, 2^20) */
-  int32_t reserved[2];
+  int32_t pool_workers;  /* paths in flight per lane (0: library default, 2^20) */
+  int32_t lanes;         /* independent wavefronts run side by side, 1..4 (0: library default, 2) */
+  int32_t reserved;
 } rmn_batch_options;
 rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_batch_options* options, void* stream,
                             rmn_batch** out);
@@ -218,17 +219,18 @@ rmn_status rmn_batch_profile(rmn_batch* batch, rmn_render_profile* out, void* st
 rmn_status rmn_batch_destroy(rmn_batch* batch);
 
 /* Project-written autotuner for batches. Times candidate launch
- * configurations -- slots per work unit in {4, 8, 16, 32, 64} x worker pool
- * in {2^18, 2^19, 2^20, 2^21} -- on a proxy of the batch whose images keep
- * every item's scene, spp, depth and field of view but only `pixel_fraction`
- * (0 < f <= 1) of its pixels, and returns the fastest. Set each item's
- * slots_per_unit and the batch's pool_workers from the result. The images do
- * not depend on the choice beyond float summation order. */
+ * configurations -- slots per work unit in {4, 8, 16} x workers per lane in
+ * {2^19, 2^20, 2^21} x lanes in {1, 2, 3} -- on a proxy of the batch whose
+ * images keep every item's scene, spp, depth and field of view but only
+ * `pixel_fraction` (0 < f <= 1) of its pixels, and returns the fastest. Set
+ * each item's slots_per_unit and the batch's pool_workers and lanes from the
+ * result. The images do not depend on the choice beyond float summation
+ * order across units (slots_per_unit); pool size and lanes change nothing. */
 typedef struct rmn_tune_result {
   int32_t slots_per_unit, pool_workers;
   double best_ms, default_ms;  /* proxy render time: best and library default */
   int32_t candidates;
-  int32_t reserved;
+  int32_t lanes;
 } rmn_tune_result;
 rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixel_fraction, rmn_tune_result* out,
                               void* stream);

@@ -59,12 +59,12 @@ class BatchItem(C.Structure):
 
 
 class BatchOptions(C.Structure):
-    _fields_ = [("use_graph", C.c_int32), ("pool_workers", C.c_int32), ("reserved", C.c_int32 * 2)]
+    _fields_ = [("use_graph", C.c_int32), ("pool_workers", C.c_int32), ("lanes", C.c_int32), ("reserved", C.c_int32)]
 
 
 class TuneResult(C.Structure):
     _fields_ = [("slots_per_unit", C.c_int32), ("pool_workers", C.c_int32), ("best_ms", C.c_double),
-                ("default_ms", C.c_double), ("candidates", C.c_int32), ("reserved", C.c_int32)]
+                ("default_ms", C.c_double), ("candidates", C.c_int32), ("lanes", C.c_int32)]
 
 
 # name -> (restype, argtypes); every declaration of include/rmn.h.

@@ -312,19 +312,19 @@ def autotune(items, pixel_fraction: float = 1.0 / 16, stream=None) -> dict:
     res = _lib.TuneResult()
     _check(_lib.load().rmn_batch_autotune(_batch_items(items), len(items), float(pixel_fraction), C.byref(res),
                                           _stream(stream)), "rmn_batch_autotune")
-    return {k: getattr(res, k) for k, _ in res._fields_ if k != "reserved"}
+    return {k: getattr(res, k) for k, _ in res._fields_}
 
 
 class Batch:
     """rmn_batch: many renders in one persistent launch, optionally replayed
     from a captured CUDA graph. Photos must live on the device."""
 
-    def __init__(self, items, use_graph: bool = True, stream=None, pool_workers: int = 0):
-        """items: list of (Model, RenderArgs, Photo)."""
+    def __init__(self, items, use_graph: bool = True, stream=None, pool_workers: int = 0, lanes: int = 0):
+        """items: list of (Model, RenderArgs, Photo); pool_workers per lane."""
         lib = _lib.load()
         arr = _batch_items(items)
         h = C.c_void_p()
-        opt = _lib.BatchOptions(1 if use_graph else 0, int(pool_workers))
+        opt = _lib.BatchOptions(1 if use_graph else 0, int(pool_workers), int(lanes), 0)
         _check(lib.rmn_batch_create(arr, len(items), C.byref(opt), _stream(stream), C.byref(h)), "rmn_batch_create")
         self._h = h
         self.items = items

@@ -303,7 +303,7 @@ static rmn_status render_one(rmn_scene* scene, const rmn_render_args* args, cons
   if (r == RMN_OK) {
     RenderItem it{scene, a, static_cast<float*>(gb.dev), static_cast<float*>(dd.dev), static_cast<float*>(ds.dev),
                   static_cast<float*>(id.dev), static_cast<float*>(is.dev), static_cast<int*>(dr.dev)};
-    r = batch_create(&it, 1, false, 0, st, &b);
+    r = batch_create(&it, 1, false, 0, 0, st, &b);
   }
   if (r == RMN_OK) r = prof ? batch_profile(b, st, prof) : batch_launch(b, st);
   if (r == RMN_OK) r = finish_out(image->radiance_Dd, npx * 16, st, dd);
@@ -390,14 +390,16 @@ rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_ba
   clear_error();
   if (!items || n <= 0 || !out) return fail(RMN_ERR_INVALID_ARGUMENT, "a batch needs at least one item");
   *out = nullptr;
-  rmn_batch_options opt = options ? *options : rmn_batch_options{1, 0, {0, 0}};
+  rmn_batch_options opt = options ? *options : rmn_batch_options{1, 0, 0, 0};
   if (opt.pool_workers < 0) return fail(RMN_ERR_INVALID_ARGUMENT, "pool_workers must be >= 0");
+  if (opt.lanes < 0 || opt.lanes > 4) return fail(RMN_ERR_INVALID_ARGUMENT, "lanes must lie in [0, 4]");
   std::vector<RenderItem> its;
   rmn_status r = make_items(items, n, its, true);
   if (r != RMN_OK) return r;
   rmn_batch* bt = new (std::nothrow) rmn_batch();
   if (!bt) return fail(RMN_ERR_OUT_OF_MEMORY, "host allocation failed");
-  r = batch_create(its.data(), n, opt.use_graph != 0, opt.pool_workers, static_cast<cudaStream_t>(stream), &bt->state);
+  r = batch_create(its.data(), n, opt.use_graph != 0, opt.pool_workers, opt.lanes, static_cast<cudaStream_t>(stream),
+                   &bt->state);
   if (r != RMN_OK) {
     delete bt;
     return r;
@@ -470,34 +472,37 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
   if (e != cudaSuccess) r = cuda_fail(e, "autotune set-up");
-  const int slots[] = {4, 8, 16, 32, 64};
-  const int pools[] = {1 << 18, 1 << 19, 1 << 20, 1 << 21};
-  rmn_tune_result best{16, 1 << 20, 1e30, 0.0, 0, 0};
-  for (int si = 0; si < 5 && r == RMN_OK; ++si)
-    for (int pi = 0; pi < 4 && r == RMN_OK; ++pi) {
-      for (RenderItem& it : its) it.args.slots_per_unit = slots[si];
-      BatchState* b = nullptr;
-      r = batch_create(its.data(), n, true, pools[pi], st, &b);
-      if (r != RMN_OK) break;
-      r = batch_launch(b, st);  // warm-up
-      if (r == RMN_OK) {
-        cudaEventRecord(e0, st);
-        r = batch_launch(b, st);
-        cudaEventRecord(e1, st);
+  const int slots[] = {4, 8, 16};
+  const int pools[] = {1 << 19, 1 << 20, 1 << 21};
+  const int lanes[] = {1, 2, 3};
+  rmn_tune_result best{16, 1 << 20, 1e30, 0.0, 0, 2};
+  for (int si = 0; si < 3 && r == RMN_OK; ++si)
+    for (int pi = 0; pi < 3 && r == RMN_OK; ++pi)
+      for (int li = 0; li < 3 && r == RMN_OK; ++li) {
+        for (RenderItem& it : its) it.args.slots_per_unit = slots[si];
+        BatchState* b = nullptr;
+        r = batch_create(its.data(), n, true, pools[pi], lanes[li], st, &b);
+        if (r != RMN_OK) break;
+        r = batch_launch(b, st);  // warm-up
+        if (r == RMN_OK) {
+          cudaEventRecord(e0, st);
+          r = batch_launch(b, st);
+          cudaEventRecord(e1, st);
+        }
+        if (r == RMN_OK) r = batch_status(b, st);
+        float ms = 0.0f;
+        if (r == RMN_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(RMN_ERR_CUDA, "event timing");
+        batch_destroy(b);
+        if (r != RMN_OK) break;
+        best.candidates++;
+        if (slots[si] == 16 && pools[pi] == (1 << 20) && lanes[li] == 2) best.default_ms = ms;
+        if (ms < best.best_ms) {
+          best.best_ms = ms;
+          best.slots_per_unit = slots[si];
+          best.pool_workers = pools[pi];
+          best.lanes = lanes[li];
+        }
       }
-      if (r == RMN_OK) r = batch_status(b, st);
-      float ms = 0.0f;
-      if (r == RMN_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(RMN_ERR_CUDA, "event timing");
-      batch_destroy(b);
-      if (r != RMN_OK) break;
-      best.candidates++;
-      if (slots[si] == 16 && pools[pi] == (1 << 20)) best.default_ms = ms;
-      if (ms < best.best_ms) {
-        best.best_ms = ms;
-        best.slots_per_unit = slots[si];
-        best.pool_workers = pools[pi];
-      }
-    }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   cudaStreamSynchronize(st);

@@ -69,9 +69,16 @@ struct QLen {
   unsigned int c_next, s_next;  // fetch cursors of the trace kernels
   unsigned int pad;
 };
+// Control words of one lane (an independent wavefront over its own share of
+// the worker pool; a batch runs its lanes concurrently).
 struct Ctl {
   QLen q[2];
-  unsigned long long next_unit;  // runs over the whole render
+};
+constexpr int kMaxLanes = 4;
+struct CtlBlock {
+  unsigned long long next_unit;  // unit cursor shared by all lanes, runs over the whole render
+  unsigned long long pad;
+  Ctl lane[kMaxLanes];
 };
 
 // Worker-id lists. The ray queues are double-buffered by iteration parity.
@@ -450,8 +457,9 @@ __global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ job
 
 template <bool COUNT>
 __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jobs, int njobs, Pool P, Queues Q,
-                                                      Ctl* ctl, int par, long long total_units,
-                                                      float4* __restrict__ parts, Counters* ctr) {
+                                                      Ctl* ctl, unsigned long long* next_unit, int par,
+                                                      long long total_units, float4* __restrict__ parts,
+                                                      Counters* ctr) {
   QLen* out = &ctl->q[par];
   const unsigned a = ctl->q[par ^ 1].sd, n = a + out->slot;
   const int* in = Q.sd[par ^ 1];
@@ -485,7 +493,7 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
     // takes a new unit, so the loop ends within the units of the batch.
     for (;;) {
       if (phase == PH_FETCH) {
-        unsigned long long u = agg_inc(&ctl->next_unit);
+        unsigned long long u = agg_inc(next_unit);
         if ((long long)u >= total_units) {
           phase = PH_DONE;
           break;
@@ -729,7 +737,8 @@ int blocks_per_sm(K kernel) {
 
 namespace rmn {
 
-constexpr int kDefaultPoolWorkers = 1 << 20;
+constexpr int kDefaultPoolWorkers = 1 << 20;  // per lane
+constexpr int kDefaultLanes = 2;
 constexpr int kIterationsPerChunk = 8;
 constexpr long long kMaxIterations = 1LL << 22;  // bound on the iteration loop; a finite render never reaches it
 
@@ -742,14 +751,19 @@ struct JobTable {
 struct BatchState {
   JobTable table;
   Job* d_jobs = nullptr;
-  Ctl* d_ctl = nullptr;
+  CtlBlock* d_ctl = nullptr;
   int* d_status = nullptr;
   float4* d_parts = nullptr;
-  Pool pool{};
-  Queues q{};
+  int lanes = 1;
+  Pool pool[kMaxLanes] = {};  // each lane's share of the worker arrays
+  Queues q[kMaxLanes] = {};
   std::vector<void*> allocs;
   cudaGraphExec_t init_exec = nullptr, chunk_exec = nullptr, fin_exec = nullptr;
   bool use_graph = false;
+  // per-lane streams and fork/join events: graph capture, and direct
+  // launches of the lanes side by side
+  cudaStream_t ls[kMaxLanes] = {};
+  cudaEvent_t fork = nullptr, join[kMaxLanes] = {};
 };
 
 
@@ -784,46 +798,52 @@ static void build_jobs(const RenderItem* items, int n, JobTable* t) {
 
 static cudaError_t launch_init(BatchState* b, cudaStream_t st, Counters* ctr) {
   const int nj = (int)b->table.jobs.size(), tp = b->table.total_pix;
-  cudaError_t e = cudaMemsetAsync(b->d_ctl, 0, sizeof(Ctl), st);
-  if (e == cudaSuccess) e = cudaMemsetAsync(b->pool.ph, 0, sizeof(int4) * (size_t)b->pool.W, st);
+  cudaError_t e = cudaMemsetAsync(b->d_ctl, 0, sizeof(CtlBlock), st);
+  for (int l = 0; l < b->lanes && e == cudaSuccess; ++l)
+    e = cudaMemsetAsync(b->pool[l].ph, 0, sizeof(int4) * (size_t)b->pool[l].W, st);
   if (e != cudaSuccess) return e;
   if (ctr) primary_kernel<true><<<(tp + 127) / 128, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
   else primary_kernel<false><<<(tp + 127) / 128, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
-  seed_kernel<<<(b->pool.W + 127) / 128, 128, 0, st>>>(b->q, b->d_ctl, b->pool.W);
+  for (int l = 0; l < b->lanes; ++l)
+    seed_kernel<<<(b->pool[l].W + 127) / 128, 128, 0, st>>>(b->q[l], &b->d_ctl->lane[l], b->pool[l].W);
   return cudaGetLastError();
 }
 
-// Iteration k of a chunk (parity k & 1): the three logic kernels, then the
-// two traversal kernels. ev (optional) records [0] before the logic, [1]
-// after it and [3] after the traversal.
-static cudaError_t launch_iteration(BatchState* b, cudaStream_t st, Counters* ctr, int k, cudaEvent_t* ev = nullptr) {
+// Iteration k of a chunk (parity k & 1) of one lane: the three logic
+// kernels, then the two traversal kernels. ev (optional) records [0] before
+// the logic, [1] after it and [3] after the traversal.
+static cudaError_t launch_iteration(BatchState* b, int lane, cudaStream_t st, Counters* ctr, int k,
+                                    cudaEvent_t* ev = nullptr) {
   const int nj = (int)b->table.jobs.size();
   const int par = k & 1;
-  cudaError_t e = cudaMemsetAsync(&b->d_ctl->q[par], 0, sizeof(QLen), st);
+  const Pool& P = b->pool[lane];
+  const Queues& Q = b->q[lane];
+  Ctl* ctl = &b->d_ctl->lane[lane];
+  cudaError_t e = cudaMemsetAsync(&ctl->q[par], 0, sizeof(QLen), st);
   if (e != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[0], st);
   const int sms = device_sms();
   const int gs = sms * blocks_per_sm(shade_kernel), gn = sms * blocks_per_sm(nee_kernel);
-  shade_kernel<<<gs, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_parts, b->d_status);
-  nee_kernel<<<gn, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_parts);
+  shade_kernel<<<gs, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_parts, b->d_status);
+  nee_kernel<<<gn, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_parts);
   if (ctr) {
     slot_kernel<true><<<sms * blocks_per_sm(slot_kernel<true>), 128, 0, st>>>(
-        b->d_jobs, nj, b->pool, b->q, b->d_ctl, par, b->table.total_units, b->d_parts, ctr);
+        b->d_jobs, nj, P, Q, ctl, &b->d_ctl->next_unit, par, b->table.total_units, b->d_parts, ctr);
   } else {
     slot_kernel<false><<<sms * blocks_per_sm(slot_kernel<false>), 128, 0, st>>>(
-        b->d_jobs, nj, b->pool, b->q, b->d_ctl, par, b->table.total_units, b->d_parts, ctr);
+        b->d_jobs, nj, P, Q, ctl, &b->d_ctl->next_unit, par, b->table.total_units, b->d_parts, ctr);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[1], st);
-  const int lb = (b->pool.W + 127) / 128;
+  const int lb = (P.W + 127) / 128;
   int tb = sms * (ctr ? blocks_per_sm(qtrace_kernel<false, true>) : blocks_per_sm(qtrace_kernel<false, false>));
   if (tb > lb) tb = lb;
   if (ctr) {
-    qtrace_kernel<false, true><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_status, ctr);
-    qtrace_kernel<true, true><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_status, ctr);
+    qtrace_kernel<false, true><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+    qtrace_kernel<true, true><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
   } else {
-    qtrace_kernel<false, false><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_status, ctr);
-    qtrace_kernel<true, false><<<tb, 128, 0, st>>>(b->d_jobs, b->pool, b->q, b->d_ctl, par, b->d_status, ctr);
+    qtrace_kernel<false, false><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+    qtrace_kernel<true, false><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
   }
   if (ev) cudaEventRecord(ev[3], st);
   return cudaGetLastError();
@@ -851,10 +871,32 @@ static cudaError_t capture(cudaStream_t cs, F&& body, cudaGraphExec_t* out) {
 // The whole render: init (counters, pool, G-buffer), iterations in chunks
 // until every worker has retired, finalize. The host reads the live-worker
 // count after each chunk; kMaxIterations bounds the loop.
+// One chunk of iterations of every lane. Without counters or per-kernel
+// events the lanes run side by side on their own streams (forked from and
+// joined back into st); otherwise one after the other on st.
+static cudaError_t launch_lanes(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t (*ev)[kMaxLanes][4]) {
+  cudaError_t e = cudaSuccess;
+  if (ctr || ev || b->lanes == 1) {
+    for (int k = 0; k < kIterationsPerChunk && e == cudaSuccess; ++k)
+      for (int l = 0; l < b->lanes && e == cudaSuccess; ++l)
+        e = launch_iteration(b, l, st, ctr, k, ev ? ev[k][l] : nullptr);
+    return e;
+  }
+  e = cudaEventRecord(b->fork, st);
+  for (int l = 0; l < b->lanes && e == cudaSuccess; ++l) {
+    cudaStream_t ls = l == 0 ? st : b->ls[l];
+    if (l > 0) e = cudaStreamWaitEvent(ls, b->fork, 0);
+    for (int k = 0; k < kIterationsPerChunk && e == cudaSuccess; ++k) e = launch_iteration(b, l, ls, nullptr, k);
+    if (l > 0 && e == cudaSuccess) e = cudaEventRecord(b->join[l], ls);
+  }
+  for (int l = 1; l < b->lanes && e == cudaSuccess; ++l) e = cudaStreamWaitEvent(st, b->join[l], 0);
+  return e;
+}
+
 struct KernelTimes {
   double logic_ms = 0.0, trace_ms = 0.0;
   long long iterations = 0;
-  cudaEvent_t e[kIterationsPerChunk][4] = {};
+  cudaEvent_t e[kIterationsPerChunk][kMaxLanes][4] = {};
 };
 
 static rmn_status run(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t* ev, KernelTimes* kt = nullptr) {
@@ -867,7 +909,7 @@ static rmn_status run(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t
   // Rays queued by the last iteration of a chunk (parity 1): the workers
   // still alive. The chunk length is even, so parities repeat chunk to chunk.
   static_assert(kIterationsPerChunk % 2 == 0, "iteration parity must repeat across chunks");
-  Ctl h{};
+  CtlBlock h{};
   unsigned int live = 1;
   unsigned int last_live = 0xffffffffu;
   unsigned long long last_next = 0;
@@ -877,23 +919,24 @@ static rmn_status run(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t
     if (graph) {
       e = cudaGraphLaunch(b->chunk_exec, st);
     } else {
-      for (int k = 0; k < kIterationsPerChunk && e == cudaSuccess; ++k)
-        e = launch_iteration(b, st, ctr, k, kt ? kt->e[k] : nullptr);
+      e = launch_lanes(b, st, ctr, kt ? kt->e : nullptr);
     }
     if (e != cudaSuccess) return cuda_fail(e, "render iteration");
     iters += kIterationsPerChunk;
-    e = cudaMemcpyAsync(&h, b->d_ctl, sizeof(Ctl), cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(&h, b->d_ctl, sizeof(CtlBlock), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "render iteration");
-    live = h.q[1].c + h.q[1].sn + h.q[1].sd;
+    live = 0;
+    for (int l = 0; l < b->lanes; ++l) live += h.lane[l].q[1].c + h.lane[l].q[1].sn + h.lane[l].q[1].sd;
     if (kt) {
-      for (int k = 0; k < kIterationsPerChunk; ++k) {
-        float a = 0.0f, c = 0.0f;
-        cudaEventElapsedTime(&a, kt->e[k][0], kt->e[k][1]);
-        cudaEventElapsedTime(&c, kt->e[k][1], kt->e[k][3]);
-        kt->logic_ms += a;
-        kt->trace_ms += c;
-      }
+      for (int k = 0; k < kIterationsPerChunk; ++k)
+        for (int l = 0; l < b->lanes; ++l) {
+          float a = 0.0f, c = 0.0f;
+          cudaEventElapsedTime(&a, kt->e[k][l][0], kt->e[k][l][1]);
+          cudaEventElapsedTime(&c, kt->e[k][l][1], kt->e[k][l][3]);
+          kt->logic_ms += a;
+          kt->trace_ms += c;
+        }
       kt->iterations += kIterationsPerChunk;
     }
     // Every iteration answers every queued ray, so a chunk that neither
@@ -919,21 +962,29 @@ void batch_destroy(BatchState* b) {
   if (b->init_exec) cudaGraphExecDestroy(b->init_exec);
   if (b->chunk_exec) cudaGraphExecDestroy(b->chunk_exec);
   if (b->fin_exec) cudaGraphExecDestroy(b->fin_exec);
+  for (int l = 0; l < kMaxLanes; ++l) {
+    if (b->ls[l]) cudaStreamDestroy(b->ls[l]);
+    if (b->join[l]) cudaEventDestroy(b->join[l]);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
   for (void* p : b->allocs) cudaFree(p);
   delete b;
 }
 
-rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, cudaStream_t st,
-                        BatchState** out) {
+rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, int lanes,
+                        cudaStream_t st, BatchState** out) {
   *out = nullptr;
   BatchState* b = new BatchState();
   build_jobs(items, n, &b->table);
   b->use_graph = use_graph;
-  long long W = std::min<long long>(b->table.total_units, pool_workers > 0 ? pool_workers : kDefaultPoolWorkers);
-  if (W < 1) W = 1;
-  W = (W + 127) / 128 * 128;
-  Pool& P = b->pool;
-  P.W = (int)W;
+  b->lanes = lanes > 0 ? std::min(lanes, kMaxLanes) : kDefaultLanes;
+  // workers per lane; no more lanes and workers than there are units
+  long long per = pool_workers > 0 ? pool_workers : kDefaultPoolWorkers;
+  while (b->lanes > 1 && (long long)b->lanes * 128 > b->table.total_units) --b->lanes;
+  per = std::min<long long>(per, (b->table.total_units + b->lanes - 1) / b->lanes);
+  if (per < 1) per = 1;
+  per = (per + 127) / 128 * 128;
+  const long long W = per * b->lanes;
   cudaError_t e = cudaSuccess;
   auto alloc = [&](void** p, size_t bytes) {
     if (e != cudaSuccess) return;
@@ -942,9 +993,11 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
   };
   const size_t jb = sizeof(Job) * b->table.jobs.size();
   alloc((void**)&b->d_jobs, jb);
-  alloc((void**)&b->d_ctl, sizeof(Ctl));
+  alloc((void**)&b->d_ctl, sizeof(CtlBlock));
   alloc((void**)&b->d_status, sizeof(int));
   alloc((void**)&b->d_parts, sizeof(float4) * RMN_PART_F4 * (size_t)b->table.total_units);
+  Pool P{};
+  P.W = (int)W;
   alloc((void**)&P.unit, sizeof(int4) * W);
   alloc((void**)&P.ph, sizeof(int4) * W);
   alloc((void**)&P.uid, sizeof(long long) * W);
@@ -957,33 +1010,47 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
   alloc((void**)&P.lw, sizeof(float4) * 2 * W);
   alloc((void**)&P.nk, sizeof(int4) * W);
   alloc((void**)&P.pend, sizeof(float4) * 2 * W);
-  for (int k = 0; k < 2; ++k) {
-    alloc((void**)&b->q.c[k], sizeof(int) * W);
-    alloc((void**)&b->q.sn[k], sizeof(int) * W);
-    alloc((void**)&b->q.sd[k], sizeof(int) * W);
+  for (int l = 0; l < b->lanes; ++l) {
+    const size_t o = (size_t)l * per;
+    Pool& L = b->pool[l];
+    L.W = (int)per;
+    if (e == cudaSuccess) {
+      L.unit = P.unit + o;
+      L.ph = P.ph + o;
+      L.uid = P.uid + o;
+      L.ro = P.ro + o;
+      L.rd = P.rd + o;
+      L.res = P.res + o;
+      L.pa = P.pa + o;
+      L.pb = P.pb + o;
+      L.nv = P.nv + 5 * o;
+      L.lw = P.lw + 2 * o;
+      L.nk = P.nk + o;
+      L.pend = P.pend + 2 * o;
+    }
+    Queues& Q = b->q[l];
+    for (int k = 0; k < 2; ++k) {
+      alloc((void**)&Q.c[k], sizeof(int) * per);
+      alloc((void**)&Q.sn[k], sizeof(int) * per);
+      alloc((void**)&Q.sd[k], sizeof(int) * per);
+    }
+    alloc((void**)&Q.nee, sizeof(int) * per);
+    alloc((void**)&Q.slot, sizeof(int) * per);
   }
-  alloc((void**)&b->q.nee, sizeof(int) * W);
-  alloc((void**)&b->q.slot, sizeof(int) * W);
   if (e == cudaSuccess) e = cudaMemcpy(b->d_jobs, b->table.jobs.data(), jb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(b->d_status, 0, sizeof(int));
+  for (int l = 0; l < b->lanes && e == cudaSuccess; ++l) {
+    e = cudaStreamCreateWithFlags(&b->ls[l], cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->join[l], cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   if (e == cudaSuccess && use_graph) {
-    cudaStream_t cs;
-    e = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    if (e == cudaSuccess) {
-      e = capture(cs, [&] { return launch_init(b, cs, nullptr); }, &b->init_exec);
-      if (e == cudaSuccess)
-        e = capture(cs,
-                    [&] {
-                      for (int k = 0; k < kIterationsPerChunk; ++k) {
-                        cudaError_t le = launch_iteration(b, cs, nullptr, k);
-                        if (le != cudaSuccess) return le;
-                      }
-                      return cudaSuccess;
-                    },
-                    &b->chunk_exec);
-      if (e == cudaSuccess) e = capture(cs, [&] { return launch_finalize(b, cs); }, &b->fin_exec);
-      cudaStreamDestroy(cs);
-    }
+    // One chunk graph: the lanes' iterations as parallel branches (fork and
+    // join through events between the lane streams), so their kernels overlap.
+    cudaStream_t c0 = b->ls[0];
+    e = capture(c0, [&] { return launch_init(b, c0, nullptr); }, &b->init_exec);
+    if (e == cudaSuccess) e = capture(c0, [&] { return launch_lanes(b, c0, nullptr, nullptr); }, &b->chunk_exec);
+    if (e == cudaSuccess) e = capture(c0, [&] { return launch_finalize(b, c0); }, &b->fin_exec);
   }
   if (e != cudaSuccess) {
     batch_destroy(b);
@@ -1017,13 +1084,15 @@ rmn_status batch_profile(BatchState* b, cudaStream_t st, RenderProfileData* prof
   rmn_status r = e == cudaSuccess ? RMN_OK : cuda_fail(e, "render profile");
   KernelTimes kt;
   for (int k = 0; k < kIterationsPerChunk && r == RMN_OK; ++k)
-    for (int j = 0; j < 4 && r == RMN_OK; ++j)
-      if (cudaEventCreate(&kt.e[k][j]) != cudaSuccess) r = fail(RMN_ERR_CUDA, "cudaEventCreate");
+    for (int l = 0; l < b->lanes; ++l)
+      for (int j = 0; j < 4 && r == RMN_OK; ++j)
+        if (cudaEventCreate(&kt.e[k][l][j]) != cudaSuccess) r = fail(RMN_ERR_CUDA, "cudaEventCreate");
   if (r == RMN_OK) r = run(b, st, d_ctr, nullptr);
   if (r == RMN_OK) r = run(b, st, nullptr, ev, &kt);
   for (int k = 0; k < kIterationsPerChunk; ++k)
-    for (int j = 0; j < 4; ++j)
-      if (kt.e[k][j]) cudaEventDestroy(kt.e[k][j]);
+    for (int l = 0; l < kMaxLanes; ++l)
+      for (int j = 0; j < 4; ++j)
+        if (kt.e[k][l][j]) cudaEventDestroy(kt.e[k][l][j]);
   Counters h{};
   if (r == RMN_OK) {
     e = cudaMemcpyAsync(&h, d_ctr, sizeof(Counters), cudaMemcpyDeviceToHost, st);

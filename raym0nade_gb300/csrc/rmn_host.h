@@ -52,8 +52,8 @@ struct RenderProfileData {
 };
 struct BatchState;
 
-rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, cudaStream_t st,
-                        BatchState** out);
+rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, int lanes,
+                        cudaStream_t st, BatchState** out);
 rmn_status batch_launch(BatchState* b, cudaStream_t st);
 rmn_status batch_status(BatchState* b, cudaStream_t st);
 rmn_status batch_profile(BatchState* b, cudaStream_t st, RenderProfileData* prof);
