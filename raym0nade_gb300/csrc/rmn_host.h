@@ -12,6 +12,7 @@ struct rmn_scene {
   std::vector<void*> device_allocations;
   rmn_scene_info info{};
   int device = 0;
+  void* sky_share = nullptr;  // the sky's device tables, shared by every scene with the same sky map
 };
 
 namespace rmn {

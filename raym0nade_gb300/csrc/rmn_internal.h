@@ -114,6 +114,12 @@ struct DevScene {
   const float* light_prefix;
   const float4* sky;          // premultiplied texels (SkyBox::Init), w unused
   const float* sky_prefix;
+  // guide table of the sky prefix sums: bucket k covers draws x in
+  // [sky_gt[k], sky_gt[k+1]), whose lower_bound lies in [sky_gi[k], sky_gi[k+1]]
+  const float* sky_gt;
+  const int* sky_gi;
+  int sky_gk;                 // buckets (0: no table)
+  float sky_ginv;             // sky_gk / total, to guess the bucket
   int root;                   // root reference (inner index or leaf ref)
   int num_tris;
   int num_mats;

@@ -17,6 +17,8 @@
 #include <cmath>
 #include <cstring>
 #include <future>
+#include <memory>
+#include <mutex>
 #include <thread>
 
 #include "rmn_host.h"
@@ -150,6 +152,107 @@ rmn_status upload(rmn_scene* s, const std::vector<T>& v, const T** out) {
   s->info.device_bytes += (int64_t)(v.size() * sizeof(T));
   *out = static_cast<const T*>(p);
   return RMN_OK;
+}
+
+// Sky tables shared between scenes. A batch typically lights many scenes
+// with one environment; one copy of its texels, prefix sums and guide table
+// then stays in L2 instead of one per scene. Entries are keyed by device
+// and compared byte for byte; the last scene using an entry frees it.
+struct SkyShare {
+  int device = 0, w = 0, h = 0;
+  uint64_t hash = 0;
+  std::vector<float4> texels;  // host copy for the comparison
+  void* dev[4] = {};           // texels, prefix, guide thresholds, guide indices
+  int gk = 0;
+  float ginv = 0.0f;
+  int refs = 0;
+  int64_t bytes = 0;
+};
+std::mutex g_sky_mu;
+std::vector<SkyShare*> g_skies;
+
+uint64_t hash_bytes(const void* p, size_t n) {  // FNV-1a, 64 bit
+  const unsigned char* b = static_cast<const unsigned char*>(p);
+  uint64_t h = 1469598103934665603ULL;
+  for (size_t i = 0; i < n; ++i) h = (h ^ b[i]) * 1099511628211ULL;
+  return h;
+}
+
+// Guide table for lower_bound over a prefix-sum array p (non-decreasing):
+// K + 1 thresholds t_k = total * k / K and gi[k] = lower_bound(p, t_k).
+void build_guide(const std::vector<float>& p, std::vector<float>& gt, std::vector<int>& gi, int& K, float& inv) {
+  const int n = (int)p.size();
+  K = std::max(1, n / 8);
+  const float total = p[n - 1];
+  gt.resize(K + 1);
+  gi.resize(K + 1);
+  for (int k = 0; k <= K; ++k) {
+    gt[k] = (float)((double)total * k / K);
+    gi[k] = (int)(std::lower_bound(p.begin(), p.end(), gt[k]) - p.begin());
+    if (gi[k] > n - 1) gi[k] = n - 1;
+  }
+  inv = total > 0.0f ? (float)K / total : 0.0f;
+}
+
+rmn_status acquire_sky(rmn_scene* s, int W, int H, const std::vector<float4>& sky, const std::vector<float>& prefix) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  const uint64_t h = hash_bytes(sky.data(), sky.size() * sizeof(float4));
+  std::lock_guard<std::mutex> lock(g_sky_mu);
+  SkyShare* e = nullptr;
+  for (SkyShare* c : g_skies)
+    if (c->device == dev && c->w == W && c->h == H && c->hash == h &&
+        std::memcmp(c->texels.data(), sky.data(), sky.size() * sizeof(float4)) == 0)
+      e = c;
+  if (!e) {
+    std::unique_ptr<SkyShare> n(new SkyShare());
+    n->device = dev;
+    n->w = W;
+    n->h = H;
+    n->hash = h;
+    n->texels = sky;
+    std::vector<float> gt;
+    std::vector<int> gi;
+    build_guide(prefix, gt, gi, n->gk, n->ginv);
+    const void* src[4] = {sky.data(), prefix.data(), gt.data(), gi.data()};
+    const size_t bytes[4] = {sky.size() * sizeof(float4), prefix.size() * sizeof(float), gt.size() * sizeof(float),
+                             gi.size() * sizeof(int)};
+    for (int k = 0; k < 4; ++k) {
+      cudaError_t err = cudaMalloc(&n->dev[k], bytes[k]);
+      if (err == cudaSuccess) err = cudaMemcpy(n->dev[k], src[k], bytes[k], cudaMemcpyHostToDevice);
+      if (err != cudaSuccess) {
+        for (int j = 0; j <= k; ++j)
+          if (n->dev[j]) cudaFree(n->dev[j]);
+        return cuda_fail(err, "sky upload");
+      }
+      n->bytes += (int64_t)bytes[k];
+    }
+    e = n.release();
+    g_skies.push_back(e);
+  }
+  e->refs++;
+  s->sky_share = e;
+  DevScene& g = s->dev;
+  g.sky = static_cast<const float4*>(e->dev[0]);
+  g.sky_prefix = static_cast<const float*>(e->dev[1]);
+  g.sky_gt = static_cast<const float*>(e->dev[2]);
+  g.sky_gi = static_cast<const int*>(e->dev[3]);
+  g.sky_gk = e->gk;
+  g.sky_ginv = e->ginv;
+  s->info.device_bytes += e->bytes;
+  return RMN_OK;
+}
+
+void release_sky(rmn_scene* s) {
+  if (!s->sky_share) return;
+  std::lock_guard<std::mutex> lock(g_sky_mu);
+  SkyShare* e = static_cast<SkyShare*>(s->sky_share);
+  s->sky_share = nullptr;
+  if (--e->refs > 0) return;
+  for (void* p : e->dev)
+    if (p) cudaFree(p);
+  g_skies.erase(std::remove(g_skies.begin(), g_skies.end(), e), g_skies.end());
+  delete e;
 }
 
 }  // namespace
@@ -343,8 +446,7 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   if ((st = upload(s, lights, &g.lights)) != RMN_OK) return st;
   if ((st = upload(s, lfaces, &g.light_faces)) != RMN_OK) return st;
   if ((st = upload(s, lprefix, &g.light_prefix)) != RMN_OK) return st;
-  if ((st = upload(s, sky, &g.sky)) != RMN_OK) return st;
-  if ((st = upload(s, sky_prefix, &g.sky_prefix)) != RMN_OK) return st;
+  if (!sky.empty() && (st = acquire_sky(s, d->env_width, d->env_height, sky, sky_prefix)) != RMN_OK) return st;
   g.root = root;
   g.num_tris = nt;
   g.num_mats = d->num_materials;
@@ -356,6 +458,7 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
 }
 
 void free_scene(rmn_scene* s) {
+  release_sky(s);
   for (void* p : s->device_allocations) cudaFree(p);
   s->device_allocations.clear();
 }

@@ -283,6 +283,25 @@ RMN_D int prefix_draw(const float* p, int n, float x) {
   return lo;
 }
 
+// prefix_draw over the sky's prefix sums through its guide table: the same
+// index (the lower_bound is monotone in x, and the table brackets it), in a
+// few steps instead of log2(texels).
+RMN_D int sky_draw(const DevScene& s, int n, float x) {
+  const int K = s.sky_gk;
+  if (K <= 0) return prefix_draw(s.sky_prefix, n, x);
+  int k = (int)(x * s.sky_ginv);
+  k = k < 0 ? 0 : (k > K - 1 ? K - 1 : k);
+  while (k > 0 && __ldg(s.sky_gt + k) > x) --k;
+  while (k < K - 1 && __ldg(s.sky_gt + k + 1) <= x) ++k;
+  int lo = __ldg(s.sky_gi + k), hi = __ldg(s.sky_gi + k + 1);
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (__ldg(s.sky_prefix + mid) < x) lo = mid + 1;
+    else hi = mid;
+  }
+  return lo;
+}
+
 // SkyBox::get, src/component.cpp:120-140.
 RMN_D float3 sky_get(const DevScene& s, float3 dir) {
   if (s.sky_w == 0) return f3(0.0f);
@@ -383,7 +402,7 @@ RMN_CALL bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float
   const int npx = s.sky_w * s.sky_h;
   const float total = __ldg(s.sky_prefix + npx - 1);
   for (int T = 1; T <= RMN_MAX_TRYS; ++T) {
-    int p = prefix_draw(s.sky_prefix, npx, total * rng.next());
+    int p = sky_draw(s, npx, total * rng.next());
     if (p >= npx) p = npx - 1;
     int u = p % s.sky_w, v = p / s.sky_w;
     float phi = RMN_PI * (float(v) + 0.5f) / float(s.sky_h);

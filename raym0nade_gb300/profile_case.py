@@ -10,6 +10,9 @@ meaningful) while the whole process holds well under a few GB.
       under the synthetic sky: primary_kernel + path_kernel.
   python -m raym0nade_gb300.profile_case trace [--tris N] [--rays R]
       rmn_trace_closest and rmn_trace_shadow on a random soup: trace_kernel.
+  python -m raym0nade_gb300.profile_case batch [--lanes L]
+      rmn_batch of the 64-instance benchmark batch (slots per unit 4, 2^21
+      workers per lane), rendered twice: every wavefront kernel.
   python -m raym0nade_gb300.profile_case fxaa [--size WxH]
       rmn_compose(Full | gamma | FXAA): compose_kernel + fxaa_kernel.
 """
@@ -24,7 +27,8 @@ import numpy as np
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["render", "trace", "fxaa"])
+    ap.add_argument("case", choices=["render", "trace", "fxaa", "batch"])
+    ap.add_argument("--lanes", type=int, default=2)
     ap.add_argument("--tris", type=int, default=2_000_000)
     ap.add_argument("--size", default="256")
     ap.add_argument("--spp", type=int, default=16)
@@ -49,6 +53,18 @@ def main(argv=None):
             api.render(m, args, ph)
         torch.cuda.synchronize()
         print("render", m.info(), "pixels", side * side, "spp", a.spp)
+    elif a.case == "batch":
+        insts = scenes.batch_instances(64, seed=7)
+        models = [api.Model(i.scene) for i in insts]
+        argsl = [api.RenderArgs.from_camera(i.camera, seed=i.seed) for i in insts]
+        for r in argsl:
+            r.slots_per_unit = 4
+        photos = [api.Photo(i.camera.width, i.camera.height) for i in insts]
+        b = api.Batch(list(zip(models, argsl, photos)), use_graph=True, pool_workers=1 << 21, lanes=a.lanes)
+        for _ in range(2):
+            b.render()
+        torch.cuda.synchronize()
+        print("batch", len(insts), "instances, lanes", a.lanes)
     elif a.case == "trace":
         s = scenes.random_soup(a.tris, 1)
         m = api.Model(s)
