@@ -44,6 +44,39 @@ def test_struct_sizes_match_header():
     assert ctypes.sizeof(_lib.Image) == 6 * 8
 
 
+# ctypes mirror -> C struct of include/rmn.h
+ABI_STRUCTS = {"Material": "rmn_material", "SceneDesc": "rmn_scene_desc", "SceneInfo": "rmn_scene_info",
+               "RenderArgs": "rmn_render_args", "Image": "rmn_image", "RenderProfile": "rmn_render_profile",
+               "BatchItem": "rmn_batch_item", "BatchOptions": "rmn_batch_options", "TuneResult": "rmn_tune_result"}
+
+
+def test_ctypes_layouts_match_c_compiler(tmp_path):
+    """Every field offset and struct size of the ctypes mirror equals what a
+    C compiler makes of include/rmn.h."""
+    import shutil
+    import subprocess
+    from raym0nade_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    lines = ['#include <stdio.h>', '#include "rmn.h"', "int main(void) {"]
+    for py, c in ABI_STRUCTS.items():
+        lines.append(f'  printf("{py} size %zu\\n", sizeof({c}));')
+        for name, _ in getattr(_lib, py)._fields_:
+            lines.append(f'  printf("{py} {name} %zu\\n", offsetof({c}, {name}));')
+    lines.append("  return 0;\n}")
+    src = tmp_path / "abi.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "abi"
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split("\n")
+    for line in filter(None, out):
+        py, name, val = line.split()
+        cls = getattr(_lib, py)
+        got = ctypes.sizeof(cls) if name == "size" else getattr(cls, name).offset
+        assert got == int(val), (py, name, got, val)
+
+
 def test_parse_render_args_docs_block():
     from raym0nade_gb300.api import parse_render_args
     block = """0.96718 -0.2 -0.156768
