@@ -613,7 +613,10 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
   int w = 0;
   TRay r;
   float tmin = 0.0f, aim = 0.0f;
-  Trav t;
+  // the deferred-child stack in shared memory (launched with 128 threads)
+  __shared__ int2 sstack[RMN_STACK * 128];
+  TravT<SharedStack> t;
+  t.stack.base = sstack + threadIdx.x;
   DevScene s;
   TraceCounters tc = {0, 0, 0, 0, 0};
   for (;;) {

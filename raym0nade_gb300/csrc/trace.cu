@@ -25,7 +25,10 @@ __global__ void __launch_bounds__(128) trace_kernel(DevScene s, const float4* __
   int64_t i = 0;
   TRay r;
   float tmin = 0.0f, aim = 0.0f;
-  Trav t;
+  // the deferred-child stack in shared memory (launched with 128 threads)
+  __shared__ int2 sstack[RMN_STACK * 128];
+  TravT<SharedStack> t;
+  t.stack.base = sstack + threadIdx.x;
   for (;;) {
     // lanes without a ray take the next ones from the batch
     unsigned need = __ballot_sync(0xffffffffu, !active && !retired);

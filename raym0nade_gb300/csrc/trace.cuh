@@ -85,17 +85,33 @@ struct TraceCounters {
 // distance), the current node and the position within the current leaf, so
 // a warp can hand a lane a new ray while its other lanes are still
 // traversing.
-struct Trav {
+// Stack storage: per-thread local memory, or a slice of shared memory (the
+// persistent traversal kernels; entry e of thread i at base[e * 128 + i], so
+// a warp's accesses to one level fall in distinct banks).
+struct LocalStack {
+  int2 e[RMN_STACK];  // (reference, entry distance as float bits)
+  RMN_D void put(int i, int2 v) { e[i] = v; }
+  RMN_D int2 get(int i) const { return e[i]; }
+};
+struct SharedStack {
+  int2* base;
+  RMN_D void put(int i, int2 v) { base[i * 128] = v; }
+  RMN_D int2 get(int i) const { return base[i * 128]; }
+};
+
+template <class Stack>
+struct TravT {
   int cur;     // next node reference to visit
   int sp;
   int hit;     // leaf-order triangle index of the closest hit so far, -1 none
   int ti, te;  // triangles [ti, te) of the current leaf still to test
   float tmax;
-  int stack_ref[RMN_STACK];
-  float stack_tl[RMN_STACK];
+  Stack stack;
 };
+using Trav = TravT<LocalStack>;
 
-RMN_D void trav_begin(const DevScene& s, Trav& t, float tmax) {
+template <class Stack>
+RMN_D void trav_begin(const DevScene& s, TravT<Stack>& t, float tmax) {
   t.cur = s.root;
   t.sp = 0;
   t.hit = -1;
@@ -111,8 +127,9 @@ RMN_D void trav_begin(const DevScene& s, Trav& t, float tmax) {
 // accepts). With ANY set, answers as soon as a hit closer than `aim` is
 // recorded (Model::rayHit_test's question, after the same visits as the
 // closest-hit query up to that point).
-template <bool ANY, bool COUNT>
-RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav& t, int budget, TraceCounters* cnt) {
+template <bool ANY, bool COUNT, class Stack>
+RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, TravT<Stack>& t, int budget,
+                   TraceCounters* cnt) {
   for (;;) {
     if (budget-- <= 0) return 0;
     if (t.ti < t.te) {  // next triangle of the current leaf, in leaf order
@@ -147,8 +164,7 @@ RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav
         if (hn) {
           if (hf) {
             if (t.sp >= RMN_STACK) return -2;
-            t.stack_ref[t.sp] = fref;
-            t.stack_tl[t.sp] = tlf;
+            t.stack.put(t.sp, make_int2(fref, __float_as_int(tlf)));
             ++t.sp;
           }
           t.cur = nref;
@@ -174,8 +190,9 @@ RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav
     for (;;) {
       if (t.sp == 0) return 1;
       --t.sp;
-      if (t.stack_tl[t.sp] < t.tmax) {
-        t.cur = t.stack_ref[t.sp];
+      const int2 e = t.stack.get(t.sp);
+      if (__int_as_float(e.y) < t.tmax) {
+        t.cur = e.x;
         break;
       }
     }
