@@ -46,6 +46,10 @@ sys.path.insert(0, ROOT)
 METRIC = "Mpaths/s at rel-MSE≤1e-3 (batched vs per-scene launch); adjoint/forward time"
 UNIT = "Mpaths/s"
 FALLBACK_HBM_GBS = 6800.0
+# DRAM bytes (read + write) of all traversal launches of one batch64 render,
+# summed from an ncu capture of `python -m raym0nade_gb300.profile_case batch`
+# (profiles/launches_batch64.md); ncu cannot run inside the timed region.
+BATCH64_TRAVERSAL_DRAM_BYTES = 200.28e9 + 15.22e9
 
 
 def measured_peaks():
@@ -389,7 +393,11 @@ def run_gpu(args, rank, world, dist):
         # per batched step: G-buffer kernel, 3 kernels per wavefront iteration, finalize
         "gpu_launches": args.steps * (2 + 3 * prof["iterations"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": None, "kernel": "qtrace_kernel (closest + shadow queues)", "peak_source": peak_src,
+                     "traffic": BATCH64_TRAVERSAL_DRAM_BYTES if args.workload == "batch64" else None,
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over every qtrace_kernel "
+                                       "launch of one batch64 render (profiles/launches_batch64.md)",
+                     "per": "step (all traversal launches of one step)",
+                     "kernel": "qtrace_kernel (closest + shadow queues)", "peak_source": peak_src,
                      "bytes_model": "64 B per inner-node visit + 36 B per triangle test + 40 B per queued ray",
                      "algorithmic_bytes_per_step": alg_bytes, "trace_share": trace_share,
                      "logic_share": logic_share, "iterations": prof["iterations"]},
