@@ -185,15 +185,17 @@ def run_reference(args, rank, world):
         return
     insts, desc = workload(args.workload, 0)
     base, scs, block = cpu_baseline(insts, target_s=20.0 / (args.warmup + args.steps + 2))
-    vals = []
+    vals, secs = [], []
     for step in range(args.warmup + args.steps):
         p, s = cpu_sample_render(scs, insts, block, base["cores"])
         if step >= args.warmup:
             vals.append(p / s / 1e6)
+            secs.append(s)
     value = float(np.mean(vals))
     base["value"] = value
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+           "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)), "higher_is_better": True,
+           "scaling": "weak",
            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
            "config": {"workload": desc, "sample": base["sample"]}, "cpu_baseline": base,
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
