@@ -147,6 +147,22 @@ def dist_setup():
     return 0, 1, None
 
 
+def max_over_ranks(x, dist, device="cpu"):
+    """The largest of every rank's x (the job's time is its slowest rank's)."""
+    if dist is None:
+        return float(x)
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(paths_per_rank, world, seconds):
+    """Whole-job Mpaths/s: every rank renders paths_per_rank paths (weak
+    scaling) and the job takes the slowest rank's time."""
+    return paths_per_rank * world / seconds / 1e6
+
+
 def cpu_sample_render(scs, insts, block, threads):
     """Render a block x block pixel square at the centre of every instance
     with the CPU library's scenes `scs`; returns (paths, seconds)."""
@@ -314,11 +330,7 @@ def run_gpu(args, rank, world, dist):
             ms.append(e0.elapsed_time(e1))
         barrier()
         clocks = sampler.stop() if sampler else None
-        total = float(sum(ms))
-        if dist is not None:
-            t = torch.tensor([total], device="cuda")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            total = float(t.item())
+        total = max_over_ranks(float(sum(ms)), dist, "cuda")
         return total / steps, clocks
 
     # profile once (untimed): visit counters and per-kernel times of the batch
@@ -346,11 +358,7 @@ def run_gpu(args, rank, world, dist):
     for _ in range(e2e_steps):
         step_e2e()
     torch.cuda.synchronize()
-    e2e_s = (time.perf_counter() - t) / e2e_steps
-    if dist is not None:
-        tt = torch.tensor([e2e_s], device="cuda")
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e_s = float(tt.item())
+    e2e_s = max_over_ranks((time.perf_counter() - t) / e2e_steps, dist, "cuda")
     npx = sum(i.camera.width * i.camera.height for i in insts)
     # rmn_render copies the radiance buffers and G-buffer out; rmn_compose
     # stages them back in and copies the display image out
@@ -359,8 +367,8 @@ def run_gpu(args, rank, world, dist):
 
     adj = adjoint_timing(args, stream, flush, barrier) if args.adjoint else None
 
-    value = paths_per_step * world / (ms_b / 1e3) / 1e6
-    plain = paths_per_step * world / (ms_p / 1e3) / 1e6
+    value = job_rate(paths_per_step, world, ms_b / 1e3)
+    plain = job_rate(paths_per_step, world, ms_p / 1e3)
     if rank != 0:
         return
     peak, peak_src = measured_peaks()
@@ -389,7 +397,7 @@ def run_gpu(args, rank, world, dist):
                    "scene_build_s": round(build_s, 1)},
         "plain": {"value": plain, "unit": UNIT, "ms_per_step": ms_p, "launches_per_step": 2 * len(insts),
                   "batched_over_plain": value / plain},
-        "e2e": {"value": paths_per_step * world / e2e_s / 1e6, "unit": UNIT, "h2d_bytes_per_step": h2d,
+        "e2e": {"value": job_rate(paths_per_step, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "call": "rmn_render into pinned host buffers + rmn_compose(Full|gamma|FXAA) to a host image, per instance"},
         # per batched step: G-buffer kernel, 3 kernels per wavefront iteration, finalize
