@@ -105,6 +105,12 @@ struct Pool {
   float4* lw;      // 2 per worker: light weights 0..7
   int4* nk;        // NEE sample k, count
   float4* pend;    // 2 per worker: pending sample bsdf|weight, light|-
+  // first-vertex light samples, up to kDirectBatch per worker in flight
+  // (ray r of worker w at w * kDirectBatch + r); origin in ro
+  float4* drd;     // direction, aim depth
+  float4* dpend;   // 2 per ray: bsdf|weight, light|-
+  float* dres;     // 1: occluded
+  int2* dk;        // slots the batch covers, rays it queued
 };
 
 // Partial accumulator of one unit: 7 float4.
@@ -114,6 +120,10 @@ struct Pool {
 #define RMN_PART_F4 7
 
 enum Phase { PH_FETCH = 0, PH_SLOT, PH_WAIT_DIRECT, PH_WAIT_CLOSEST, PH_NEE, PH_WAIT_NEE, PH_DONE };
+
+// First-vertex light samples a worker draws at once: consecutive direct
+// slots of its unit, each with its own shadow ray in the same queue.
+constexpr int kDirectBatch = 8;
 enum Flags { FL_EXCLUDE = 1 };
 
 __device__ __forceinline__ int find_job_pix(const Job* jobs, int n, int v) {
@@ -430,6 +440,7 @@ __global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ job
   const int* in = Q.sn[par ^ 1];
   for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
     const int w = idx < a ? in[idx] : Q.nee[idx - a];
+    if (w < 0) continue;  // a first-vertex light-sample ray (slot_kernel consumes it)
     int4 ph = P.ph[w];
     int4 un = P.unit[w];
     const Job* J = &jobs[un.x];
@@ -475,18 +486,24 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
     rng.key = 0;
     rng.ctr = (unsigned)ph.y;
     if (phase == PH_WAIT_DIRECT) {
-      if (P.res[w].x == 0.0f) {
-        float4 b0 = P.pend[2 * w], b1 = P.pend[2 * w + 1];
-        Rad4 d, sp;
-        demodulate(base_of(*J, un.y), f3(b0.x, b0.y, b0.z), f3(b1.x, b1.y, b1.z), b0.w, d, sp);
-        float4* part = parts + (size_t)uid * RMN_PART_F4;
-        Rad4 dd = r4(part[0]), ds = r4(part[1]);
-        radd(dd, d);
-        radd(ds, sp);
-        part[0] = f4(dd);
-        part[1] = f4(ds);
+      // the answered light samples of the batch, added in slot order
+      const int2 dk = P.dk[w];
+      const float3 base = base_of(*J, un.y);
+      float4* part = parts + (size_t)uid * RMN_PART_F4;
+      Rad4 dd = r4(part[0]), ds = r4(part[1]);
+      for (int k = 0; k < dk.y; ++k) {
+        const size_t rid = (size_t)w * kDirectBatch + k;
+        if (P.dres[rid] == 0.0f) {
+          float4 b0 = P.dpend[2 * rid], b1 = P.dpend[2 * rid + 1];
+          Rad4 d, sp;
+          demodulate(base, f3(b0.x, b0.y, b0.z), f3(b1.x, b1.y, b1.z), b0.w, d, sp);
+          radd(dd, d);
+          radd(ds, sp);
+        }
       }
-      un.z++;
+      part[0] = f4(dd);
+      part[1] = f4(ds);
+      un.z += dk.x;
       phase = PH_SLOT;
     }
     // Start slots until one queues a ray; every pass advances the slot or
@@ -520,36 +537,56 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
       }
       const Params& p = J->p;
       const DevScene& s = J->s;
-      rng = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)un.z);
-      if (COUNT) slots_done++;
       Surf g = load_first_vertex(*J, un.y);
       if (un.z < p.spp_d) {
-        // sampleDirectLightFromFirstIntersection, src/render.cpp:425-437
-        if (len3(g.emis) > 0.0f) {
-          un.z++;
-          continue;
-        }
+        // sampleDirectLightFromFirstIntersection, src/render.cpp:425-437:
+        // up to kDirectBatch consecutive light-sample slots at once, each
+        // from its own stream; the samples without a shadow ray add nothing
+        const int c = min(min(un.w, p.spp_d) - un.z, kDirectBatch);
+        if (COUNT) slots_done += (unsigned long long)c;
         float3 Vd = -norm3(g.pos - p.pos);
         float lwt[8];
         float tot = 0.0f;
-        if (s.sky_w == 0 && !light_weights(s, g, Vd, lwt, tot)) {
-          un.z++;
-          continue;
+        int n = 0;
+        if (!(len3(g.emis) > 0.0f) && (s.sky_w != 0 || light_weights(s, g, Vd, lwt, tot))) {
+          for (int k = 0; k < c; ++k) {
+            RmnRng rk = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)(un.z + k));
+            float3 dir;
+            float aim;
+            LSample ls;
+            if (!light_gen(s, g, Vd, lwt, tot, p.spp_d, rk, dir, aim, ls)) continue;
+            const size_t rid = (size_t)w * kDirectBatch + n++;
+            P.drd[rid] = make_float4(dir.x, dir.y, dir.z, aim);
+            P.dpend[2 * rid] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
+            P.dpend[2 * rid + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
+          }
         }
-        float3 dir;
-        float aim;
-        LSample ls;
-        if (!light_gen(s, g, Vd, lwt, tot, p.spp_d, rng, dir, aim, ls)) {
-          un.z++;
+        if (n == 0) {
+          un.z += c;
           continue;
         }
         P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
-        P.rd[w] = make_float4(dir.x, dir.y, dir.z, aim);
-        P.pend[2 * w] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
-        P.pend[2 * w + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
+        P.dk[w] = make_int2(c, n);
+        // queue the n rays (ids ~(w * kDirectBatch + k)) in one reservation
+        {
+          namespace cg = cooperative_groups;
+          cg::coalesced_group grp = cg::coalesced_threads();
+          int incl = n;
+          for (int off = 1; off < (int)grp.size(); off <<= 1) {
+            int v = grp.shfl_up(incl, off);
+            if ((int)grp.thread_rank() >= off) incl += v;
+          }
+          unsigned base = 0;
+          if (grp.thread_rank() == grp.size() - 1) base = atomicAdd(&out->sn, (unsigned)incl);
+          base = grp.shfl(base, grp.size() - 1);
+          const unsigned first = base + (unsigned)(incl - n);
+          for (int k = 0; k < n; ++k) Q.sn[par][first + k] = ~(w * kDirectBatch + k);
+        }
         phase = PH_WAIT_DIRECT;
         break;
       }
+      rng = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)un.z);
+      if (COUNT) slots_done++;
       // sampleIndirectLightFromFirstIntersection, src/render.cpp:314-423
       if (len3(g.emis) > 0.0f || !(rng.next() < 1.0f)) {
         un.z++;
@@ -603,12 +640,11 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
   QLen* ql = &ctl->q[par];
-  // the shadow kernel traces the NEE list, then the first-vertex list
-  const unsigned na = SHADOW ? ql->sn : ql->c;
-  const unsigned n = SHADOW ? na + ql->sd : na;
+  // shadow queue entries: a worker id (its NEE sample) or ~(first-vertex
+  // light-sample ray id)
+  const unsigned n = SHADOW ? ql->sn : ql->c;
   unsigned int* next = SHADOW ? &ql->s_next : &ql->c_next;
-  const int* qa = SHADOW ? Q.sn[par] : Q.c[par];
-  const int* qb = Q.sd[par];
+  const int* q = SHADOW ? Q.sn[par] : Q.c[par];
   bool active = false, retired = false;
   int w = 0;
   TRay r;
@@ -629,9 +665,10 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
       if (!active && !retired) {
         unsigned i = base + __popc(need & lt);
         if (i < n) {
-          w = i < na ? qa[i] : qb[i - na];
-          float4 o = P.ro[w], d = P.rd[w];
-          s = jobs[P.unit[w].x].s;
+          w = q[i];
+          const int wk = (!SHADOW || w >= 0) ? w : (~w) / kDirectBatch;
+          float4 o = P.ro[wk], d = (!SHADOW || w >= 0) ? P.rd[wk] : P.drd[~w];
+          s = jobs[P.unit[wk].x].s;
           r = make_tray(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
           tmin = o.w;
           if (SHADOW) {
@@ -652,8 +689,13 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
     if (!active) continue;
     int st = trav_run<SHADOW, COUNT>(s, r, tmin, aim, t, kFetchBudget, &tc);
     if (st == 0) continue;
-    if (SHADOW) P.res[w] = make_float2(st == -2 ? 0.0f : ((t.tmax >= aim) ? 0.0f : 1.0f), 0.0f);
-    else P.res[w] = make_float2(__int_as_float(st == -2 ? -2 : t.hit), t.tmax);
+    if (SHADOW) {
+      const float occluded = st == -2 ? 0.0f : ((t.tmax >= aim) ? 0.0f : 1.0f);
+      if (w >= 0) P.res[w] = make_float2(occluded, 0.0f);
+      else P.dres[~w] = occluded;
+    } else {
+      P.res[w] = make_float2(__int_as_float(st == -2 ? -2 : t.hit), t.tmax);
+    }
     if (st == -2) atomicExch(status, 1);
     active = false;
   }
@@ -1013,6 +1055,10 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
   alloc((void**)&P.lw, sizeof(float4) * 2 * W);
   alloc((void**)&P.nk, sizeof(int4) * W);
   alloc((void**)&P.pend, sizeof(float4) * 2 * W);
+  alloc((void**)&P.drd, sizeof(float4) * kDirectBatch * W);
+  alloc((void**)&P.dpend, sizeof(float4) * 2 * kDirectBatch * W);
+  alloc((void**)&P.dres, sizeof(float) * kDirectBatch * W);
+  alloc((void**)&P.dk, sizeof(int2) * W);
   for (int l = 0; l < b->lanes; ++l) {
     const size_t o = (size_t)l * per;
     Pool& L = b->pool[l];
@@ -1030,11 +1076,15 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
       L.lw = P.lw + 2 * o;
       L.nk = P.nk + o;
       L.pend = P.pend + 2 * o;
+      L.drd = P.drd + kDirectBatch * o;
+      L.dpend = P.dpend + 2 * kDirectBatch * o;
+      L.dres = P.dres + kDirectBatch * o;
+      L.dk = P.dk + o;
     }
     Queues& Q = b->q[l];
     for (int k = 0; k < 2; ++k) {
       alloc((void**)&Q.c[k], sizeof(int) * per);
-      alloc((void**)&Q.sn[k], sizeof(int) * per);
+      alloc((void**)&Q.sn[k], sizeof(int) * kDirectBatch * per);
       alloc((void**)&Q.sd[k], sizeof(int) * per);
     }
     alloc((void**)&Q.nee, sizeof(int) * per);
