@@ -64,10 +64,10 @@ struct Counters {
 // Queue lengths of one iteration parity; cleared when an iteration of that
 // parity starts.
 struct QLen {
-  unsigned int c, sn, sd;    // ray queues: closest, shadow (NEE), shadow (first vertex)
-  unsigned int nee, slot;    // hand-offs to nee_kernel / slot_kernel within the iteration
+  unsigned int c, sn;           // ray queues: closest, shadow
+  unsigned int sd, nw;          // workers waiting for first-vertex / NEE shadow answers
+  unsigned int nee, slot;       // hand-offs to nee_kernel / slot_kernel within the iteration
   unsigned int c_next, s_next;  // fetch cursors of the trace kernels
-  unsigned int pad;
 };
 // Control words of one lane (an independent wavefront over its own share of
 // the worker pool; a batch runs its lanes concurrently).
@@ -83,9 +83,10 @@ struct CtlBlock {
 
 // Worker-id lists. The ray queues are double-buffered by iteration parity.
 struct Queues {
-  int* c[2];
-  int* sn[2];
-  int* sd[2];
+  int* c[2];   // closest-hit rays (worker ids)
+  int* sn[2];  // shadow rays (~ray ids, kDirectBatch per worker)
+  int* sd[2];  // workers waiting for first-vertex light samples (and the first iteration's seed)
+  int* nw[2];  // workers waiting for their terminating vertex's light samples
   int* nee;
   int* slot;
 };
@@ -104,11 +105,11 @@ struct Pool {
   float4* nv;      // 5 per worker: NEE vertex pos|kscale, shapeN|rough, surfN|metal, base|eta, V|tot
   float4* lw;      // 2 per worker: light weights 0..7
   int4* nk;        // NEE sample k, count
-  float4* pend;    // 2 per worker: pending sample bsdf|weight, light|-
-  // first-vertex light samples, up to kDirectBatch per worker in flight
-  // (ray r of worker w at w * kDirectBatch + r); origin in ro
+  // shadow rays, up to kDirectBatch per worker in flight: first-vertex or
+  // terminating-vertex light samples (ray r of worker w at
+  // w * kDirectBatch + r); origin in ro
   float4* drd;     // direction, aim depth
-  float4* dpend;   // 2 per ray: bsdf|weight, light|-
+  float4* dpend;   // 2 per ray: bsdf|weight, light|sample index
   float* dres;     // 1: occluded
   int2* dk;        // slots the batch covers, rays it queued
 };
@@ -123,7 +124,7 @@ enum Phase { PH_FETCH = 0, PH_SLOT, PH_WAIT_DIRECT, PH_WAIT_CLOSEST, PH_NEE, PH_
 
 // First-vertex light samples a worker draws at once: consecutive direct
 // slots of its unit, each with its own shadow ray in the same queue.
-constexpr int kDirectBatch = 8;
+constexpr int kDirectBatch = 8;  // also holds a terminating vertex's samples (sampleCount <= 6)
 enum Flags { FL_EXCLUDE = 1 };
 
 __device__ __forceinline__ int find_job_pix(const Job* jobs, int n, int v) {
@@ -299,9 +300,10 @@ __device__ __forceinline__ void push(int* q, unsigned int* qn, int w) { q[agg_in
 // Ray queues are double-buffered by iteration parity: the queues filled in
 // iteration i are traced in iteration i and consumed in iteration i + 1.
 
-// Light samples of the terminating vertex from nk.x on, until one is queued
-// (true) or none is left (false).
-__device__ __forceinline__ bool nee_next(const Job* J, const Pool& P, int w, RmnRng& rng, int4& nk) {
+// The light samples of a terminating vertex, drawn in order from the
+// path's stream: each that needs a shadow ray gets one of the worker's ray
+// slots (its sample index kept beside it). Returns the number queued.
+__device__ __forceinline__ int nee_draw(const Job* J, const Pool& P, int w, RmnRng& rng, int cnt) {
   const DevScene& s = J->s;
   const float4* nv = P.nv + 5 * (size_t)w;
   float4 a = nv[0], b = nv[1], c = nv[2], d = nv[3], e = nv[4];
@@ -315,19 +317,37 @@ __device__ __forceinline__ bool nee_next(const Job* J, const Pool& P, int w, Rmn
   sf.eta = d.w;
   float4 l0 = P.lw[2 * w], l1 = P.lw[2 * w + 1];
   float lwt[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
-  for (; nk.x < nk.y; ++nk.x) {
+  int n = 0;
+  for (int k = 0; k < cnt; ++k) {
     float3 dir;
     float aim;
     LSample ls;
-    if (!light_gen(s, sf, f3(e.x, e.y, e.z), lwt, e.w, nk.y, rng, dir, aim, ls)) continue;
+    if (!light_gen(s, sf, f3(e.x, e.y, e.z), lwt, e.w, cnt, rng, dir, aim, ls)) continue;
     ls.bsdf *= a.w;  // scaling(samples, factor), src/render.cpp:101-104
-    P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
-    P.rd[w] = make_float4(dir.x, dir.y, dir.z, aim);
-    P.pend[2 * w] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
-    P.pend[2 * w + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
-    return true;
+    const size_t rid = (size_t)w * kDirectBatch + n++;
+    P.drd[rid] = make_float4(dir.x, dir.y, dir.z, aim);
+    P.dpend[2 * rid] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
+    P.dpend[2 * rid + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, __int_as_float(k));
   }
-  return false;
+  if (n > 0) P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
+  return n;
+}
+
+// Appends the n shadow rays of worker w (ids ~(w * kDirectBatch + k)) to the
+// shadow queue with one atomic per warp.
+__device__ __forceinline__ void push_rays(int* q, unsigned int* qn, int w, int n) {
+  namespace cg = cooperative_groups;
+  cg::coalesced_group grp = cg::coalesced_threads();
+  int incl = n;
+  for (int off = 1; off < (int)grp.size(); off <<= 1) {
+    int v = grp.shfl_up(incl, off);
+    if ((int)grp.thread_rank() >= off) incl += v;
+  }
+  unsigned base = 0;
+  if (grp.thread_rank() == grp.size() - 1) base = atomicAdd(qn, (unsigned)incl);
+  base = grp.shfl(base, grp.size() - 1);
+  const unsigned first = base + (unsigned)(incl - n);
+  for (int k = 0; k < n; ++k) q[first + k] = ~(w * kDirectBatch + k);
 }
 
 __device__ __forceinline__ void store_worker(const Pool& P, int w, int4 ph, int phase, const RmnRng& rng, int4 un) {
@@ -436,33 +456,43 @@ __global__ void __launch_bounds__(128, 8) shade_kernel(const Job* __restrict__ j
 __global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
                                                      int par, float4* __restrict__ parts) {
   QLen* out = &ctl->q[par];
-  const unsigned a = ctl->q[par ^ 1].sn, n = a + out->nee;
-  const int* in = Q.sn[par ^ 1];
+  const unsigned a = ctl->q[par ^ 1].nw, n = a + out->nee;
+  const int* in = Q.nw[par ^ 1];
   for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
     const int w = idx < a ? in[idx] : Q.nee[idx - a];
-    if (w < 0) continue;  // a first-vertex light-sample ray (slot_kernel consumes it)
     int4 ph = P.ph[w];
     int4 un = P.unit[w];
     const Job* J = &jobs[un.x];
     RmnRng rng;
     rng.key = rmn_stream_key(J->p.seed, (uint32_t)un.y, (uint32_t)un.z);
     rng.ctr = (unsigned)ph.y;
-    int4 nk = P.nk[w];
+    int queued = 0;
     if (ph.x == PH_WAIT_NEE) {
-      if (P.res[w].x == 0.0f) {
-        float4 pa4 = P.pend[2 * w], pb4 = P.pend[2 * w + 1];
-        float4 pb = P.pb[w];
-        emit(parts + (size_t)P.uid[w] * RMN_PART_F4, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), J->p.inv_spp,
-             {f3(pa4.x, pa4.y, pa4.z), f3(pb4.x, pb4.y, pb4.z), pa4.w}, un.z * 8 + nk.x);
+      // the answered samples, emitted in sample order
+      const int2 dk = P.dk[w];
+      const float4 pa = P.pa[w], pb = P.pb[w];
+      const float3 base = base_of(*J, un.y);
+      float4* part = parts + (size_t)P.uid[w] * RMN_PART_F4;
+      for (int k = 0; k < dk.y; ++k) {
+        const size_t rid = (size_t)w * kDirectBatch + k;
+        if (P.dres[rid] != 0.0f) continue;
+        float4 b0 = P.dpend[2 * rid], b1 = P.dpend[2 * rid + 1];
+        emit(part, base, pa, f3(pb.x, pb.y, pb.z), J->p.inv_spp, {f3(b0.x, b0.y, b0.z), f3(b1.x, b1.y, b1.z), b0.w},
+             un.z * 8 + __float_as_int(b1.w));
       }
-      nk.x++;
+    } else {
+      const int cnt = P.nk[w].y;
+      queued = nee_draw(J, P, w, rng, cnt);
+      if (queued) P.dk[w] = make_int2(cnt, queued);
     }
-    const bool queued = nee_next(J, P, w, rng, nk);
-    P.nk[w] = make_int4(nk.x, nk.y, 0, 0);
     if (!queued) un.z++;
     store_worker(P, w, ph, queued ? PH_WAIT_NEE : PH_SLOT, rng, un);
-    if (queued) push(Q.sn[par], &out->sn, w);
-    else push(Q.slot, &out->slot, w);
+    if (queued) {
+      push_rays(Q.sn[par], &out->sn, w, queued);
+      push(Q.nw[par], &out->nw, w);
+    } else {
+      push(Q.slot, &out->slot, w);
+    }
   }
 }
 
@@ -567,21 +597,7 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
         }
         P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
         P.dk[w] = make_int2(c, n);
-        // queue the n rays (ids ~(w * kDirectBatch + k)) in one reservation
-        {
-          namespace cg = cooperative_groups;
-          cg::coalesced_group grp = cg::coalesced_threads();
-          int incl = n;
-          for (int off = 1; off < (int)grp.size(); off <<= 1) {
-            int v = grp.shfl_up(incl, off);
-            if ((int)grp.thread_rank() >= off) incl += v;
-          }
-          unsigned base = 0;
-          if (grp.thread_rank() == grp.size() - 1) base = atomicAdd(&out->sn, (unsigned)incl);
-          base = grp.shfl(base, grp.size() - 1);
-          const unsigned first = base + (unsigned)(incl - n);
-          for (int k = 0; k < n; ++k) Q.sn[par][first + k] = ~(w * kDirectBatch + k);
-        }
+        push_rays(Q.sn[par], &out->sn, w, n);
         phase = PH_WAIT_DIRECT;
         break;
       }
@@ -972,7 +988,7 @@ static rmn_status run(BatchState* b, cudaStream_t st, Counters* ctr, cudaEvent_t
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(e, "render iteration");
     live = 0;
-    for (int l = 0; l < b->lanes; ++l) live += h.lane[l].q[1].c + h.lane[l].q[1].sn + h.lane[l].q[1].sd;
+    for (int l = 0; l < b->lanes; ++l) live += h.lane[l].q[1].c + h.lane[l].q[1].sd + h.lane[l].q[1].nw;
     if (kt) {
       for (int k = 0; k < kIterationsPerChunk; ++k)
         for (int l = 0; l < b->lanes; ++l) {
@@ -1054,7 +1070,6 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
   alloc((void**)&P.nv, sizeof(float4) * 5 * W);
   alloc((void**)&P.lw, sizeof(float4) * 2 * W);
   alloc((void**)&P.nk, sizeof(int4) * W);
-  alloc((void**)&P.pend, sizeof(float4) * 2 * W);
   alloc((void**)&P.drd, sizeof(float4) * kDirectBatch * W);
   alloc((void**)&P.dpend, sizeof(float4) * 2 * kDirectBatch * W);
   alloc((void**)&P.dres, sizeof(float) * kDirectBatch * W);
@@ -1075,7 +1090,6 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
       L.nv = P.nv + 5 * o;
       L.lw = P.lw + 2 * o;
       L.nk = P.nk + o;
-      L.pend = P.pend + 2 * o;
       L.drd = P.drd + kDirectBatch * o;
       L.dpend = P.dpend + 2 * kDirectBatch * o;
       L.dres = P.dres + kDirectBatch * o;
@@ -1086,6 +1100,7 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
       alloc((void**)&Q.c[k], sizeof(int) * per);
       alloc((void**)&Q.sn[k], sizeof(int) * kDirectBatch * per);
       alloc((void**)&Q.sd[k], sizeof(int) * per);
+      alloc((void**)&Q.nw[k], sizeof(int) * per);
     }
     alloc((void**)&Q.nee, sizeof(int) * per);
     alloc((void**)&Q.slot, sizeof(int) * per);
