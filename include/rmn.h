@@ -163,6 +163,11 @@ rmn_status rmn_scene_create(const rmn_scene_desc* desc, rmn_scene** out);
 rmn_status rmn_scene_destroy(rmn_scene* scene);
 rmn_status rmn_scene_info_get(const rmn_scene* scene, rmn_scene_info* info);
 
+/* Renders keep the device memory of their worker pools and queues for the
+ * next render (up to 16 GiB per device); this frees it. No counterpart in the
+ * reference. */
+rmn_status rmn_release_cached_memory(void);
+
 /* Replaces Model::rayHit (src/model.cpp:332-341): closest hit per ray. */
 rmn_status rmn_trace_closest(rmn_scene* scene, const rmn_ray* rays, int64_t n, rmn_hit* hits, void* stream);
 

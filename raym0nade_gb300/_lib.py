@@ -77,6 +77,7 @@ SIGNATURES = {
     "rmn_trace_closest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "rmn_trace_shadow": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
     "rmn_render": (C.c_int, [C.c_void_p, C.POINTER(RenderArgs), C.POINTER(Image), C.c_void_p]),
+    "rmn_release_cached_memory": (C.c_int, []),
     "rmn_adjoint": (C.c_int, [C.c_void_p, C.POINTER(RenderArgs), C.POINTER(Image), C.c_void_p, C.c_void_p,
                               C.c_void_p]),
     "rmn_render_profile_get": (C.c_int, [C.c_void_p, C.POINTER(RenderArgs), C.POINTER(Image),

@@ -155,6 +155,12 @@ rmn_status rmn_scene_destroy(rmn_scene* scene) {
   return RMN_OK;
 }
 
+rmn_status rmn_release_cached_memory(void) {
+  clear_error();
+  release_cached_memory();
+  return RMN_OK;
+}
+
 rmn_status rmn_scene_info_get(const rmn_scene* scene, rmn_scene_info* info) {
   clear_error();
   if (!scene || !info) return fail(RMN_ERR_INVALID_ARGUMENT, "scene or info is NULL");

@@ -1028,7 +1028,10 @@ void batch_destroy(BatchState* b) {
     if (b->join[l]) cudaEventDestroy(b->join[l]);
   }
   if (b->fork) cudaEventDestroy(b->fork);
-  for (void* p : b->allocs) cudaFree(p);
+  // the blocks go back to the cache for the next batch: no work of this
+  // batch may still run on them (cudaFree would have waited likewise)
+  cudaDeviceSynchronize();
+  for (void* p : b->allocs) cached_free(p);
   delete b;
 }
 
@@ -1049,7 +1052,7 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
   cudaError_t e = cudaSuccess;
   auto alloc = [&](void** p, size_t bytes) {
     if (e != cudaSuccess) return;
-    e = cudaMalloc(p, bytes ? bytes : 16);
+    e = cached_malloc(p, bytes);
     if (e == cudaSuccess) b->allocs.push_back(*p);
   };
   const size_t jb = sizeof(Job) * b->table.jobs.size();

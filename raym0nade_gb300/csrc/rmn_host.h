@@ -53,6 +53,11 @@ struct RenderProfileData {
 };
 struct BatchState;
 
+// Device memory kept for reuse between batches (devmem.cpp).
+cudaError_t cached_malloc(void** p, size_t bytes);
+void cached_free(void* p);
+void release_cached_memory();
+
 rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, int lanes,
                         cudaStream_t st, BatchState** out);
 rmn_status batch_launch(BatchState* b, cudaStream_t st);
