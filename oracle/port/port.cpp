@@ -25,6 +25,7 @@
 #include <cstring>
 #include <random>
 #include <thread>
+#include <map>
 #include <vector>
 
 #include "../../raym0nade_gb300/csrc/rmn_rng.h"
@@ -406,8 +407,84 @@ struct Bsdf {
     ret += fs * ds * gs;
     return ret * nl;
   }
-  // BSDF::getBSDF, :194-199 (opaque surfaces always take the BRDF).
-  vec3 eval(const vec3& L) const { return brdf(L); }
+  // BSDF::getBTDF, src/sampling.cpp:159-192.
+  vec3 btdf(const vec3& L) const {
+    const vec3& N = s.surfN;
+    float nl = dot(s.surfN, L);
+    if (nl >= 0.0f) return vec3(0.0f);
+    const vec3& V = in;
+    vec3 H = normalize(L + s.eta * V);
+    float D = gtr2(dot(N, H), s.roughness);
+    float bt = D * (-nl);
+    float lh = dot(L, H), nv = dot(N, V), hv = dot(H, V);
+    bt *= std::abs(lh * hv) / (std::abs(nl * nv) + kEps);
+    float k = s.eta * hv + lh;
+    bt /= k * k;
+    return vec3(bt);
+  }
+  // BSDF::getBSDF, :194-199: the BTDF on the far side of a transmissive
+  // surface, the BRDF otherwise.
+  vec3 eval(const vec3& L) const {
+    if (s.opacity > 1.0f - kEps || s.entering) return brdf(L);
+    return btdf(L);
+  }
+  // BSDF::preciseRefraction, :285-308.
+  void precise_refraction(vec3& out, float& F) const {
+    const vec3& V = in;
+    const vec3& N = s.surfN;
+    float eta = s.eta;
+    float nv = dot(N, V);
+    if (nv < 0.0f) { F = 1.0f; out = vec3(NAN); return; }
+    float delta = 1.0f - eta * eta * (1.0f - nv * nv);
+    if (delta < 0.0f) { F = 1.0f; out = vec3(NAN); return; }
+    float k = eta * nv - std::sqrt(delta);
+    out = k * N - eta * V;
+    float ln = -dot(out, N);
+    float r0 = (1.0f - eta) / (1.0f + eta);
+    r0 = r0 * r0;
+    F = r0 + (1.0f - r0) * schlick(ln);
+  }
+  // refract, :342-349.
+  static vec3 refract(const vec3& V, const vec3& N, float eta) {
+    float nv = dot(N, V);
+    float delta = 1.0f - eta * eta * (1.0f - nv * nv);
+    if (delta < 0.0f) return vec3(NAN);
+    float k = eta * nv - std::sqrt(delta);
+    return k * N - eta * V;
+  }
+  // BSDF::sampleBTDF, :351-388 (GGX half vector, refracted; <= 16 tries).
+  template <class G>
+  void sample_btdf(G& gen, vec3& out, vec3& w, int& fails) const {
+    if (std::abs(s.eta - 1.0f) < kEps) {
+      out = -in;
+      w = vec3(1.0f);
+      return;
+    }
+    vec3 t, b;
+    frame(t, b);
+    const vec3& V = in;
+    for (int T = 1; T <= kMaxTrys; ++T) {
+      float u = gen(), phi = gen() * 2.0f * kPi;
+      float ct = std::sqrt((1.0f - u) / (1.0f + (s.roughness * s.roughness - 1.0f) * u));
+      float st = std::sqrt(1 - ct * ct);
+      vec3 H = st * std::cos(phi) * t + st * std::sin(phi) * b + ct * s.surfN;
+      out = refract(V, H, s.eta);
+      float weight;
+      if (!any_finite(out)) {
+        weight = 0.0f;
+      } else {
+        float vh = dot(V, H), vn = dot(V, s.surfN), hn = dot(H, s.surfN);
+        weight = std::abs(vh) / std::abs(vn * hn);
+      }
+      if (weight > 0.0f && dot(out, s.shapeN) < 0.0f) {
+        w = vec3(weight);
+        return;
+      }
+      fails++;
+    }
+    w = vec3(0.0f);
+    out = vec3(NAN);
+  }
 
   // getTangentSpaceWithInDir, src/geometry.cpp:114-124 (the fallback branch
   // needs dot(N, in) < -0.999, which hit shading rules out).
@@ -592,6 +669,59 @@ static void direct_light(const Scene& s, const Bsdf& bs, int cnt, GenOf&& gen_of
   }
 }
 
+// ------------------------------------------------------------- media -------
+// Medium, src/render.cpp:11-42: the media a path is inside, keyed by
+// material id (air: -1), as the reference's multimap.
+struct Medium {
+  std::multimap<int, std::pair<float, vec3>> m;
+  void init() {
+    m.clear();
+    m.emplace(-1, std::make_pair(1.0f, vec3(1.0f)));
+  }
+  void insert(int id, float ior, const vec3& absorb) { m.emplace(id, std::make_pair(ior, absorb)); }
+  void erase(int id) { m.erase(id); }
+  float ior() const {
+    float r = 1.0f;
+    for (const auto& e : m) r = std::max(r, e.second.first);
+    return r;
+  }
+  vec3 absorb() const {
+    vec3 a = vec3(1.0f);
+    for (const auto& e : m) a *= e.second.second;
+    return a;
+  }
+  int size() const { return (int)m.size(); }
+};
+
+static vec3 pow_s(vec3 v, float k) {  // src/geometry.cpp:22-27
+  if (v.x < 0.0f) v.x = 0.0f;
+  if (v.y < 0.0f) v.y = 0.0f;
+  if (v.z < 0.0f) v.z = 0.0f;
+  return vec3(std::pow(v.x, k), std::pow(v.y, k), std::pow(v.z, k));
+}
+
+// getAbsorb, src/render.cpp:83-87.
+static vec3 get_absorb(const vec3& absorb, float dis) {
+  const float omega = 32.0f;
+  float c = dot(absorb, kLum);
+  return (c < 1.0f - kEps) ? pow_s(absorb, omega * dis) : vec3(1.0f);
+}
+
+// calcEta, src/render.cpp:89-99: the relative index of refraction.
+static void calc_eta(Medium& med, Surf& h) {
+  float eta1 = med.ior(), eta2;
+  if (h.entering) {
+    eta2 = std::max(eta1, h.eta);
+  } else {
+    med.erase(h.id);
+    eta2 = med.ior();
+    med.insert(h.id, h.eta, h.base);
+  }
+  h.eta = eta1 / eta2;
+}
+
+constexpr float kP0Reflect = 0.24f;  // P0_reflect, src/render.cpp:118
+
 // ---------------------------------------------------------- integrator -----
 // One indirect sample from the first vertex: sampleIndirectLightFromFirst-
 // Intersection (src/render.cpp:314-423) followed by the sampleRay recursion
@@ -603,16 +733,31 @@ template <class G>
 static void indirect_path(const Scene& s, const Surf& g, const vec3& eye, int maxd, G& gen,
                           std::vector<LSample>& out) {
   if (length(g.emis) > 0) return;
+  Medium med;
+  med.init();
   vec3 in = normalize(g.pos - eye);
   Bsdf b0{-in, g};
   float rf = g.roughness * 1.0f;
-  b0.s.eta = 1.0f / b0.s.eta;
-  float p_reflect = 1.0f;  // opaque first vertex
+  const float ior0 = b0.s.eta;
+  b0.s.eta = 1.0f / b0.s.eta;  // from air into the surface
+  float p_reflect = 1.0f, F0 = 0.0f;
+  if (b0.s.opacity < kEps) {
+    vec3 rd;
+    b0.precise_refraction(rd, F0);
+    p_reflect = kP0Reflect + (1.0f - kP0Reflect) * F0;
+  }
   vec3 dir, w0 = vec3(NAN);
   int f0 = 0;
-  if (!(gen() < p_reflect)) return;  // refraction branch: glass is not restated
-  b0.sample_reflect(gen, dir, w0, f0);
-  w0 /= p_reflect;
+  if (gen() < p_reflect) {
+    b0.sample_reflect(gen, dir, w0, f0);
+    w0 /= p_reflect;
+  } else {
+    b0.sample_btdf(gen, dir, w0, f0);
+    w0 *= (1.0f - F0);
+    w0 /= (1.0f - p_reflect);
+    if (b0.s.entering) med.insert(b0.s.id, ior0, b0.s.base);
+    else med.erase(b0.s.id);
+  }
   if (!any_finite(dir)) return;
 
   vec3 fac[18];
@@ -631,31 +776,61 @@ static void indirect_path(const Scene& s, const Surf& g, const vec3& eye, int ma
     Bsdf bs{-ray.d, Surf()};
     bs.s.pos = ray.o + ray.d * h.tmax;
     hit_info(s, s.tris[h.face], ray, bs.s);
+    const float ior = bs.s.eta;
     rf = std::max(rf, 1.0f * bs.s.roughness);
     bs.s.roughness = std::max(bs.s.roughness, rf);
     const float p_rr = 1.0f + (0.5f - 1.0f) * std::sqrt(bs.s.roughness);
     bool nee = p_rr < 0.9f;
-    const vec3 absorb(1.0f);  // getAbsorb in air, :83-87
+    const vec3 absorb = get_absorb(med.absorb(), h.tmax);
     if (length(bs.s.emis) > kEps) {
       if (!exclude) term.push_back({absorb, bs.s.emis, 1.0f});
       break;
     }
-    float pr = 1.0f;
-    if (!(gen() <= pr)) break;  // opaque surfaces always reflect
-    nee = nee && bs.s.entering;
-    if (nee && (depth >= maxd || gen() > p_rr)) {
-      int cnt = kSampleCount[std::min(depth, 16)];
-      direct_light(s, bs, cnt, [&](int) -> G& { return gen; }, term);
-      float k = 1.0f / pr;
-      if (depth < maxd) k /= (1.0f - p_rr);
-      for (LSample& x : term) x.bsdf *= k;
-      break;
+    float pr = 1.0f, F = 0.0f;
+    if (bs.s.opacity < kEps) {
+      calc_eta(med, bs.s);
+      vec3 rd;
+      bs.precise_refraction(rd, F);
+      pr = (med.size() == 1) ? kP0Reflect + (1.0f - kP0Reflect) * F : F;
+      pr = std::max(pr - 1e-3f, 0.0f);
     }
+    const int cnt = kSampleCount[std::min(depth, 16)];
     vec3 nd, w;
     int nf = 0;
-    bs.sample_reflect(gen, nd, w, nf);
-    w /= pr;
-    if (nee) w /= p_rr;
+    if (gen() <= pr) {  // reflection
+      nee = nee && bs.s.entering && med.size() == 1;
+      if (nee && (depth >= maxd || gen() > p_rr)) {
+        direct_light(s, bs, cnt, [&](int) -> G& { return gen; }, term);
+        float k = 1.0f / pr;
+        if (depth < maxd) k /= (1.0f - p_rr);
+        for (LSample& x : term) x.bsdf *= k;
+        break;
+      }
+      bs.sample_reflect(gen, nd, w, nf);
+      w /= pr;
+      if (nee) w /= p_rr;
+    } else {  // refraction
+      nee = nee && !bs.s.entering && med.size() == 2;
+      if (nee && (depth >= maxd || gen() > p_rr)) {
+        direct_light(s, bs, cnt, [&](int) -> G& { return gen; }, term);
+        float k = 1.0f / (1.0f - pr);
+        if (depth < maxd) k /= (1.0f - p_rr);
+        for (LSample& x : term) x.bsdf *= k;
+        for (LSample& x : term) { x.light *= x.bsdf; x.bsdf = absorb; }  // passBsdf(samples, absorb)
+        break;
+      }
+      if (std::abs(bs.s.eta - 1.0f) < kEps) {
+        nd = ray.d;
+        w = vec3(1.0f);
+      } else {
+        bs.sample_btdf(gen, nd, w, nf);
+        w *= (1.0f - F);
+      }
+      w /= (1.0f - pr);
+      if (nee) w /= p_rr;
+      if (bs.s.entering) med.insert(bs.s.id, ior, bs.s.base);
+      else med.erase(bs.s.id);
+    }
     if (!any_finite(nd) || depth == maxd) { term.clear(); break; }
     w *= absorb;
     fac[depth] = w;

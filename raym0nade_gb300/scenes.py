@@ -206,6 +206,18 @@ def cornell(materials: list | None = None, wall_materials=None) -> Scene:
     return _assemble(meshes, materials, name="cornell")
 
 
+def cornell_glass() -> Scene:
+    """The Cornell box with a glass tall box (opacity 0, ior 1.5, roughness
+    0.05, faintly blue transmitting colour, which also tints the light inside
+    it) and a half-opaque short box (opacity 0.5): the reference's
+    transmissive and semi-opaque paths (refraction, media, Fresnel split)."""
+    mats = [material(CORNELL_GREY), material(CORNELL_RED), material(CORNELL_GREEN),
+            material((0.78, 0.78, 0.78), emission=CORNELL_LIGHT),
+            material((0.7, 0.6, 0.3), opacity=0.5, roughness=0.4),
+            material((1.0, 1.0, 1.0), roughness=0.05, opacity=0.0, ior=1.5, transmitting=(0.95, 0.98, 1.0))]
+    return cornell(mats)
+
+
 CORNELL16_LIGHT = 5  # material index of the emitter in cornell16
 
 

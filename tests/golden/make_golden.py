@@ -14,6 +14,9 @@ Fixtures (numpy .npz, compressed):
   render_cornell.npz 24 x 24 Cornell render, 16 spp, reference mt19937 stream.
   render_sky.npz     16 x 12 render of a small heightfield under a lat-long
                      sky (sky-mode light sampling, smooth normals).
+  render_glass.npz   20 x 20 render of the Cornell box with a glass box and a
+                     half-opaque box, 8 spp (refraction, media, Fresnel split).
+                     ``--glass`` writes this fixture alone.
   post.npz           Photo::shade(Full) + gammaCorrection of render records,
                      and Photo::FXAA of a 96 x 64 image with hard edges.
   cornell_4096spp.npz  the converged reference image of the Cornell workload
@@ -109,6 +112,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "render_sky.npz"), **scene_arrays(hf), args=hcam.packed(), seed=77,
                         records=hrec)
 
+    glass(R)
+
     rgb_lin = R.compose(rec, 1.0, gamma=False)
     rgb = R.compose(rec, 1.0, gamma=True)
     rng = np.random.default_rng(14)
@@ -122,6 +127,17 @@ def main():
     np.savez_compressed(os.path.join(HERE, "post.npz"), records=rec, linear=rgb_lin, display=rgb, fxaa_in=img,
                         fxaa_out=fx)
     print("fixtures written to", HERE)
+
+
+def glass(R=None):
+    if R is None:
+        bindings.build(with_reference=True)
+        R = bindings.OracleLib("ref")
+    g = scenes.cornell_glass()
+    cam = scenes.cornell_camera(20, 20, 8)
+    rec = R.scene(g).render(cam, seed=909)
+    np.savez_compressed(os.path.join(HERE, "render_glass.npz"), **scene_arrays(g), args=cam.packed(), seed=909,
+                        records=rec)
 
 
 def converged():
@@ -139,5 +155,8 @@ def converged():
 if __name__ == "__main__":
     if "--converged" in sys.argv:
         converged()
+    elif "--glass" in sys.argv:
+        glass()
+        print("glass fixture written to", HERE)
     else:
         main()

@@ -37,7 +37,7 @@ def test_golden_trace(port):
     assert same(ps.trace_shadow(z["shadow_rays"]), z["occluded"])
 
 
-@pytest.mark.parametrize("name", ["render_cornell", "render_sky"])
+@pytest.mark.parametrize("name", ["render_cornell", "render_sky", "render_glass"])
 def test_golden_render(port, name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     a = z["args"]
@@ -107,6 +107,18 @@ def test_render_cornell_matches_reference(port, ref, spp, p_direct):
     a = ps.render(cam, seed=5 + spp)
     b = rs.render(cam, seed=5 + spp)
     assert same(a[..., :38], b[..., :38])
+
+
+@pytest.mark.parametrize("spp,p_direct", [(8, 0.7), (4, 0.0)])
+def test_render_glass_matches_reference(port, ref, spp, p_direct):
+    """Transmissive and semi-opaque materials: refraction, media, Fresnel
+    split, the BTDF in light sampling, 16x indirect samples behind glass."""
+    ps, rs = _pair(port, ref, scenes.cornell_glass())
+    cam = scenes.cornell_camera(16, 16, spp, p_direct=p_direct)
+    a = ps.render(cam, seed=11 + spp)
+    b = rs.render(cam, seed=11 + spp)
+    assert same(a[..., :38], b[..., :38])
+    assert (a[..., 33] < 1e-4).sum() > 0  # some pixels see the glass
 
 
 def test_render_sky_matches_reference(port, ref):
