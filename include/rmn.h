@@ -130,10 +130,10 @@ typedef struct rmn_render_args {
 /* Caller-owned per-pixel outputs (width*height entries each, row-major).
  * radiance_*: 4 floats per pixel (RadianceData: rgb, Var) for
  * direct/indirect x diffuse/specular (Photo, include/image.h:36-39).
- * gbuffer: 20 floats per pixel, the HitInfo of the primary hit
+ * gbuffer: 21 floats per pixel, the HitInfo of the primary hit
  * (include/model.h:12-18) -- base colour[3], emission[3], position[3]
  * (NaN: the primary ray missed), shape normal[3], surface normal[3],
- * roughness, metallic, opacity, eta, material id. rmn_render needs the four
+ * roughness, metallic, opacity, eta, material id, entering (1/0). rmn_render needs the four
  * radiance buffers; gbuffer may be NULL (then it lives in scratch memory). */
 typedef struct rmn_image {
   float* radiance_Dd;
@@ -144,7 +144,7 @@ typedef struct rmn_image {
   int32_t* dropped; /* optional: per pixel, the indirect sample the firefly clamp
                        (src/render.cpp:532-547) dropped, as slot * 8 + sample, or -1 */
 } rmn_image;
-#define RMN_GBUFFER_FLOATS 20
+#define RMN_GBUFFER_FLOATS 21
 
 /* Photo::ShadeOption bits (include/image.h:17-34) used by rmn_compose. */
 enum {

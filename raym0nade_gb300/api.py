@@ -36,7 +36,7 @@ Full = 63
 Direct_Diffuse, Direct_Specular = DirectLight | Diffuse, DirectLight | Specular
 Indirect_Diffuse, Indirect_Specular = IndirectLight | Diffuse, IndirectLight | Specular
 GAMMA = 4096
-GBUFFER_FLOATS = 20
+GBUFFER_FLOATS = 21
 
 
 class RmnError(RuntimeError):

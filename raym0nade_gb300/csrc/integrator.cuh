@@ -12,6 +12,9 @@ struct Params {
   float3 pos, dir, up, right;
   float acc, exposure, p_direct, inv_spp;
   int W, H, spp, maxd, spp_d, slots;
+  int glass;      // the scene has transmissive or half-opaque materials
+  int slots16;    // slots of a pixel behind such a first vertex
+  float inv_spp16;
   int S;  // slots per unit
   int K;  // units per pixel
   uint64_t seed;
@@ -22,7 +25,7 @@ struct Params {
 // fewer partial records (112 B each).
 constexpr int kDefaultSlotsPerUnit = 16;
 
-inline Params make_params(const rmn_render_args& a) {
+inline Params make_params(const rmn_render_args& a, bool glass = false) {
   Params p;
   p.pos = f3(a.position[0], a.position[1], a.position[2]);
   p.dir = f3(a.direction[0], a.direction[1], a.direction[2]);
@@ -39,15 +42,19 @@ inline Params make_params(const rmn_render_args& a) {
   const int spp_i = (a.spp - p.spp_d) * 1;      // opaque first vertex
   p.inv_spp = 1.0f / (float)spp_i;
   p.slots = p.spp_d + spp_i;
+  p.glass = glass ? 1 : 0;
+  p.slots16 = p.spp_d + spp_i * 16;  // renderPixel's MultiSampleForRefraction
+  p.inv_spp16 = 1.0f / (float)(spp_i * 16);
+  const int layout = glass ? p.slots16 : p.slots;  // units are cut for the largest pixel
   // lanes_per_pixel > 0 fixes the number of units per pixel; 0 cuts the
   // slots into units of kDefaultSlotsPerUnit.
   if (a.lanes_per_pixel > 0) {
     p.K = a.lanes_per_pixel;
-    p.S = (p.slots + p.K - 1) / p.K;
+    p.S = (layout + p.K - 1) / p.K;
     if (p.S < 1) p.S = 1;
   } else {
     p.S = a.slots_per_unit > 0 ? a.slots_per_unit : kDefaultSlotsPerUnit;
-    p.K = (p.slots + p.S - 1) / p.S;
+    p.K = (layout + p.S - 1) / p.S;
     if (p.K < 1) p.K = 1;
   }
   p.seed = a.seed;

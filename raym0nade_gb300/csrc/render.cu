@@ -102,7 +102,7 @@ struct Pool {
   float2* res;     // closest: (leaf-order triangle, t); shadow: (occluded, -)
   float4* pa;      // first-vertex factor w0, weight product wf
   float4* pb;      // throughput product, roughness factor
-  float4* nv;      // 5 per worker: NEE vertex pos|kscale, shapeN|rough, surfN|metal, base|eta, V|tot
+  float4* nv;      // 6 per worker: NEE vertex pos|kscale, shapeN|rough, surfN|metal, base|eta, V|tot, absorb|opacity
   float4* lw;      // 2 per worker: light weights 0..7
   int4* nk;        // NEE sample k, count
   // shadow rays, up to kDirectBatch per worker in flight: first-vertex or
@@ -112,6 +112,10 @@ struct Pool {
   float4* dpend;   // 2 per ray: bsdf|weight, light|sample index
   float* dres;     // 1: occluded
   int2* dk;        // slots the batch covers, rays it queued
+  // the media a path is inside (scenes with transmissive materials)
+  int* mn;         // count
+  int* mid;        // RMN_MEDIA per worker: material id (air -1)
+  float4* mval;    // RMN_MEDIA per worker: ior, absorb
 };
 
 // Partial accumulator of one unit: 7 float4.
@@ -148,8 +152,8 @@ __device__ __forceinline__ int find_job_unit(const Job* jobs, int n, long long v
 
 
 
-// G-buffer record (RMN_GBUFFER_FLOATS = 20): base[3] emission[3] position[3]
-// shapeN[3] surfN[3] roughness metallic opacity eta material-id. The base
+// G-buffer record (RMN_GBUFFER_FLOATS = 21): base[3] emission[3] position[3]
+// shapeN[3] surfN[3] roughness metallic opacity eta material-id entering. The base
 // colour is stored untweaked; the integrator applies renderPixel's tweak for
 // its own use and finalize writes the tweaked colour back where the
 // reference leaves it.
@@ -181,7 +185,8 @@ __global__ void __launch_bounds__(128) primary_kernel(const Job* __restrict__ jo
   float* o = J.gbuf + (size_t)RMN_GBUFFER_FLOATS * i;
   float v[RMN_GBUFFER_FLOATS] = {g.base.x, g.base.y, g.base.z, g.emis.x, g.emis.y, g.emis.z, g.pos.x,
                                  g.pos.y, g.pos.z, g.shapeN.x, g.shapeN.y, g.shapeN.z, g.surfN.x, g.surfN.y,
-                                 g.surfN.z, g.roughness, g.metallic, g.opacity, g.eta, (float)g.id};
+                                 g.surfN.z, g.roughness, g.metallic, g.opacity, g.eta, (float)g.id,
+                                 g.entering ? 1.0f : 0.0f};
 #pragma unroll
   for (int k = 0; k < RMN_GBUFFER_FLOATS; ++k) o[k] = v[k];
   if (COUNT) {
@@ -225,6 +230,37 @@ __device__ __forceinline__ float3 base_of(const Job& J, int pixel) {
   const float* gb = gbuf_of(J, pixel);
   return tweak_base(f3(gb[0], gb[1], gb[2]));
 }
+// The base colour indirect samples are demodulated against: none behind a
+// transmissive first vertex (renderPixel, src/render.cpp:543-546).
+__device__ __forceinline__ float3 indirect_base_of(const Job& J, int pixel) {
+  const float* gb = gbuf_of(J, pixel);
+  if (J.p.glass && gb[17] < RMN_EPS) return f3(0.0f);
+  return tweak_base(f3(gb[0], gb[1], gb[2]));
+}
+// 1 / spp_indirect of the pixel: 16 times the samples behind a transmissive
+// or half-opaque first vertex (src/render.cpp:497-499).
+__device__ __forceinline__ float inv_spp_of(const Job& J, int pixel) {
+  if (!J.p.glass) return J.p.inv_spp;
+  return gbuf_of(J, pixel)[17] > 1.0f - RMN_EPS ? J.p.inv_spp : J.p.inv_spp16;
+}
+
+// The worker's media (scenes with transmissive materials only).
+__device__ __forceinline__ void load_media(const Pool& P, int w, Media& m) {
+  m.n = P.mn[w];
+  m.ok = true;
+  for (int i = 0; i < m.n && i < RMN_MEDIA; ++i) {
+    m.id[i] = P.mid[(size_t)w * RMN_MEDIA + i];
+    m.v[i] = P.mval[(size_t)w * RMN_MEDIA + i];
+  }
+}
+__device__ __forceinline__ void store_media(const Pool& P, int w, const Media& m) {
+  P.mn[w] = m.n;
+  for (int i = 0; i < m.n; ++i) {
+    P.mid[(size_t)w * RMN_MEDIA + i] = m.id[i];
+    P.mval[(size_t)w * RMN_MEDIA + i] = m.v[i];
+  }
+}
+
 __device__ __forceinline__ Surf load_first_vertex(const Job& J, int pixel) {
   const float* gb = gbuf_of(J, pixel);
   Surf g = default_surf();
@@ -238,6 +274,7 @@ __device__ __forceinline__ Surf load_first_vertex(const Job& J, int pixel) {
   g.opacity = gb[17];
   g.eta = gb[18];
   g.id = (int)gb[19];
+  g.entering = gb[20] != 0.0f;
   return g;
 }
 
@@ -305,8 +342,9 @@ __device__ __forceinline__ void push(int* q, unsigned int* qn, int w) { q[agg_in
 // slots (its sample index kept beside it). Returns the number queued.
 __device__ __forceinline__ int nee_draw(const Job* J, const Pool& P, int w, RmnRng& rng, int cnt) {
   const DevScene& s = J->s;
-  const float4* nv = P.nv + 5 * (size_t)w;
-  float4 a = nv[0], b = nv[1], c = nv[2], d = nv[3], e = nv[4];
+  const float4* nv = P.nv + 6 * (size_t)w;
+  float4 a = nv[0], b = nv[1], c = nv[2], d = nv[3], e = nv[4], f = nv[5];
+  const int4 nk = P.nk[w];
   Surf sf = default_surf();
   sf.pos = f3(a.x, a.y, a.z);
   sf.shapeN = f3(b.x, b.y, b.z);
@@ -315,6 +353,8 @@ __device__ __forceinline__ int nee_draw(const Job* J, const Pool& P, int w, RmnR
   sf.metallic = c.w;
   sf.base = f3(d.x, d.y, d.z);
   sf.eta = d.w;
+  sf.opacity = f.w;
+  sf.entering = nk.z != 0;
   float4 l0 = P.lw[2 * w], l1 = P.lw[2 * w + 1];
   float lwt[8] = {l0.x, l0.y, l0.z, l0.w, l1.x, l1.y, l1.z, l1.w};
   int n = 0;
@@ -324,6 +364,7 @@ __device__ __forceinline__ int nee_draw(const Job* J, const Pool& P, int w, RmnR
     LSample ls;
     if (!light_gen(s, sf, f3(e.x, e.y, e.z), lwt, e.w, cnt, rng, dir, aim, ls)) continue;
     ls.bsdf *= a.w;  // scaling(samples, factor), src/render.cpp:101-104
+    if (nk.w) ls.bsdf = ls.bsdf * f3(f.x, f.y, f.z);  // passBsdf(samples, absorb), :232
     const size_t rid = (size_t)w * kDirectBatch + n++;
     P.drd[rid] = make_float4(dir.x, dir.y, dir.z, aim);
     P.dpend[2 * rid] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
@@ -357,6 +398,122 @@ __device__ __forceinline__ void store_worker(const Pool& P, int w, int4 ph, int 
   P.unit[w] = un;
 }
 
+// sampleRay's body at a hit (src/render.cpp:121-312) for worker w: emit an
+// emitter, start the vertex's light samples, or sample the next bounce.
+// Returns the worker's next phase. GLASS: scenes with transmissive or
+// half-opaque materials (media, Fresnel split, refraction); without it the
+// opaque path compiles alone.
+template <bool GLASS>
+RMN_D int shade_hit(const Job* J, const Pool& P, int w, RmnRng& rng, int4& ph, const int4& un, float4* part,
+                    float2 res, float3 o, float3 dir, int* status) {
+  const Params& p = J->p;
+  const DevScene& s = J->s;
+  const int h = __float_as_int(res.x);
+  const int depth = ph.z;
+  const bool exclude = (ph.w & FL_EXCLUDE) != 0;
+  int phase = PH_SLOT;  // unless set below, the slot ends here
+  float4 pb = P.pb[w];
+  Surf sf = default_surf();
+  sf.pos = o + dir * res.y;
+  hit_info(s, h, dir, sf);
+  const float ior = sf.eta;  // absolute; calcEta makes sf.eta relative
+  float rf = fmaxf(pb.w, 1.0f * sf.roughness);
+  sf.roughness = fmaxf(sf.roughness, rf);
+  const float p_rr = 1.0f + (0.5f - 1.0f) * sqrtf(sf.roughness);
+  bool nee = p_rr < 0.9f;
+  Media med;
+  med.n = 1;
+  float3 absorb = f3(1.0f);
+  if (GLASS) {
+    load_media(P, w, med);
+    absorb = get_absorb(med.absorb(), res.y);  // getAbsorb over the segment just traced
+  }
+  if (len3(sf.emis) > RMN_EPS) {
+    if (!exclude)
+      emit(part, indirect_base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), inv_spp_of(*J, un.y),
+           {absorb, sf.emis, 1.0f}, un.z * 8);
+    return phase;
+  }
+  float pr = 1.0f, F = 0.0f;  // P_reflect and the Fresnel term
+  if (GLASS && sf.opacity < RMN_EPS) {
+    calc_eta(med, sf);
+    float3 rd;
+    precise_refraction(sf, -dir, rd, F);
+    pr = (med.n == 1) ? kP0Reflect + (1.0f - kP0Reflect) * F : F;
+    pr = (pr - 1e-3f < 0.0f) ? 0.0f : pr - 1e-3f;  // std::max(P_reflect - 1e-3f, 0.0f)
+  }
+  const float3 V = -dir;
+  const bool reflect = rng.next() <= pr;
+  if (!GLASS && !reflect) return phase;  // never: pr = 1 on opaque surfaces
+  // light sampling at this vertex: reflection in air, or refraction out of a
+  // medium into air
+  nee = nee && (reflect ? (sf.entering && med.n == 1) : (!sf.entering && med.n == 2));
+  if (nee && (depth >= p.maxd || rng.next() > p_rr)) {
+    int cnt = c_sample_count[depth < 16 ? depth : 16];
+    float k = 1.0f / (reflect ? pr : 1.0f - pr);
+    if (depth < p.maxd) k /= (1.0f - p_rr);
+    float lwt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+    float tot = 0.0f;
+    if (s.sky_w != 0 || light_weights(s, sf, V, lwt, tot)) {
+      float4* nv = P.nv + 6 * (size_t)w;
+      nv[0] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, k);
+      nv[1] = make_float4(sf.shapeN.x, sf.shapeN.y, sf.shapeN.z, sf.roughness);
+      nv[2] = make_float4(sf.surfN.x, sf.surfN.y, sf.surfN.z, sf.metallic);
+      nv[3] = make_float4(sf.base.x, sf.base.y, sf.base.z, sf.eta);
+      nv[4] = make_float4(V.x, V.y, V.z, tot);
+      nv[5] = make_float4(absorb.x, absorb.y, absorb.z, sf.opacity);
+      P.lw[2 * w] = make_float4(lwt[0], lwt[1], lwt[2], lwt[3]);
+      P.lw[2 * w + 1] = make_float4(lwt[4], lwt[5], lwt[6], lwt[7]);
+      P.nk[w] = make_int4(0, cnt, sf.entering ? 1 : 0, reflect ? 0 : 1);
+      phase = PH_NEE;
+    }
+  } else {
+    float3 nd, wv;
+    int nf = 0;
+    if (reflect) {
+      sample_reflect(sf, V, rng, nd, wv, nf);
+      wv = wv / pr;
+    } else if (GLASS) {
+      if (fabsf(sf.eta - 1.0f) < RMN_EPS) {  // inside a medium: straight on
+        nd = dir;
+        wv = f3(1.0f);
+      } else {
+        sample_btdf(sf, V, rng, nd, wv, nf);
+        wv = wv * (1.0f - F);
+      }
+      wv = wv / (1.0f - pr);
+      if (sf.entering) med.insert(sf.id, ior, sf.base);
+      else med.erase(sf.id);
+    }
+    if (nee) wv = wv / p_rr;
+    if (any_finite3(nd) && depth != p.maxd) {
+      wv = wv * absorb;
+      float3 thr = f3(pb.x, pb.y, pb.z) * wv;
+      P.pb[w] = make_float4(thr.x, thr.y, thr.z, rf);
+      if (nf > 0) {
+        float4 pa = P.pa[w];
+        pa.w = pa.w * (1.0f / (float)(1 + nf));
+        P.pa[w] = pa;
+      }
+      P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
+      P.rd[w] = make_float4(nd.x, nd.y, nd.z, INFINITY);
+      ph.z = depth + 1;
+      ph.w = nee ? FL_EXCLUDE : 0;
+      phase = PH_WAIT_CLOSEST;
+    }
+  }
+  if (GLASS) {
+    if (!med.ok) atomicExch(status, rmn::kDevMediaOverflow);
+    store_media(P, w, med);
+  }
+  return phase;
+}
+__device__ __noinline__ int shade_hit_glass(const Job* J, const Pool& P, int w, RmnRng& rng, int4& ph,
+                                            const int4& un, float4* part, float2 res, float3 o, float3 dir,
+                                            int* status) {
+  return shade_hit<true>(J, P, w, rng, ph, un, part, res, o, dir, status);
+}
+
 __global__ void __launch_bounds__(128, 8) shade_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
                                                        int par, float4* __restrict__ parts, int* status) {
   const unsigned n = ctl->q[par ^ 1].c;
@@ -373,77 +530,23 @@ __global__ void __launch_bounds__(128, 8) shade_kernel(const Job* __restrict__ j
     rng.key = rmn_stream_key(p.seed, (uint32_t)un.y, (uint32_t)un.z);
     rng.ctr = (unsigned)ph.y;
     float4* part = parts + (size_t)P.uid[w] * RMN_PART_F4;
-    // sampleRay's body, src/render.cpp:121-312, opaque surfaces
+    // sampleRay's body, src/render.cpp:121-312
     float2 res = P.res[w];
     int h = __float_as_int(res.x);
     float4 o4 = P.ro[w], d4 = P.rd[w];
     float3 o = f3(o4.x, o4.y, o4.z), dir = f3(d4.x, d4.y, d4.z);
-    int depth = ph.z;
-    bool exclude = (ph.w & FL_EXCLUDE) != 0;
+    const bool exclude = (ph.w & FL_EXCLUDE) != 0;
     int phase = PH_SLOT;  // unless set below, the slot ends here
     if (h == -2) {
       atomicExch(status, 1);
     } else if (h < 0) {
       float4 pb = P.pb[w];
       if (!exclude && s.sky_w)
-        emit(part, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp, {f3(1.0f), sky_get(s, dir), 1.0f},
-             un.z * 8);
+        emit(part, indirect_base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), inv_spp_of(*J, un.y),
+             {f3(1.0f), sky_get(s, dir), 1.0f}, un.z * 8);
     } else {
-      float4 pb = P.pb[w];
-      Surf sf = default_surf();
-      sf.pos = o + dir * res.y;
-      hit_info(s, h, dir, sf);
-      float rf = fmaxf(pb.w, 1.0f * sf.roughness);
-      sf.roughness = fmaxf(sf.roughness, rf);
-      const float p_rr = 1.0f + (0.5f - 1.0f) * sqrtf(sf.roughness);
-      bool nee = p_rr < 0.9f;
-      if (len3(sf.emis) > RMN_EPS) {
-        if (!exclude)
-          emit(part, base_of(*J, un.y), P.pa[w], f3(pb.x, pb.y, pb.z), p.inv_spp, {f3(1.0f), sf.emis, 1.0f},
-               un.z * 8);
-      } else if (rng.next() <= 1.0f) {
-        nee = nee && sf.entering;
-        const float3 V = -dir;
-        if (nee && (depth >= p.maxd || rng.next() > p_rr)) {
-          int cnt = c_sample_count[depth < 16 ? depth : 16];
-          float k = 1.0f / 1.0f;
-          if (depth < p.maxd) k /= (1.0f - p_rr);
-          float lwt[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-          float tot = 0.0f;
-          if (s.sky_w != 0 || light_weights(s, sf, V, lwt, tot)) {
-            float4* nv = P.nv + 5 * (size_t)w;
-            nv[0] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, k);
-            nv[1] = make_float4(sf.shapeN.x, sf.shapeN.y, sf.shapeN.z, sf.roughness);
-            nv[2] = make_float4(sf.surfN.x, sf.surfN.y, sf.surfN.z, sf.metallic);
-            nv[3] = make_float4(sf.base.x, sf.base.y, sf.base.z, sf.eta);
-            nv[4] = make_float4(V.x, V.y, V.z, tot);
-            P.lw[2 * w] = make_float4(lwt[0], lwt[1], lwt[2], lwt[3]);
-            P.lw[2 * w + 1] = make_float4(lwt[4], lwt[5], lwt[6], lwt[7]);
-            P.nk[w] = make_int4(0, cnt, 0, 0);
-            phase = PH_NEE;
-          }
-        } else {
-          float3 nd, wv;
-          int nf = 0;
-          sample_reflect(sf, V, rng, nd, wv, nf);
-          wv = wv / 1.0f;
-          if (nee) wv = wv / p_rr;
-          if (any_finite3(nd) && depth != p.maxd) {
-            float3 thr = f3(pb.x, pb.y, pb.z) * wv;
-            P.pb[w] = make_float4(thr.x, thr.y, thr.z, rf);
-            if (nf > 0) {
-              float4 pa = P.pa[w];
-              pa.w = pa.w * (1.0f / (float)(1 + nf));
-              P.pa[w] = pa;
-            }
-            P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
-            P.rd[w] = make_float4(nd.x, nd.y, nd.z, INFINITY);
-            ph.z = depth + 1;
-            ph.w = nee ? FL_EXCLUDE : 0;
-            phase = PH_WAIT_CLOSEST;
-          }
-        }
-      }
+      phase = p.glass ? shade_hit_glass(J, P, w, rng, ph, un, part, res, o, dir, status)
+                      : shade_hit<false>(J, P, w, rng, ph, un, part, res, o, dir, status);
     }
     if (phase == PH_SLOT) un.z++;
     store_worker(P, w, ph, phase, rng, un);
@@ -471,13 +574,14 @@ __global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ job
       // the answered samples, emitted in sample order
       const int2 dk = P.dk[w];
       const float4 pa = P.pa[w], pb = P.pb[w];
-      const float3 base = base_of(*J, un.y);
+      const float3 base = indirect_base_of(*J, un.y);
+      const float inv_spp = inv_spp_of(*J, un.y);
       float4* part = parts + (size_t)P.uid[w] * RMN_PART_F4;
       for (int k = 0; k < dk.y; ++k) {
         const size_t rid = (size_t)w * kDirectBatch + k;
         if (P.dres[rid] != 0.0f) continue;
         float4 b0 = P.dpend[2 * rid], b1 = P.dpend[2 * rid + 1];
-        emit(part, base, pa, f3(pb.x, pb.y, pb.z), J->p.inv_spp, {f3(b0.x, b0.y, b0.z), f3(b1.x, b1.y, b1.z), b0.w},
+        emit(part, base, pa, f3(pb.x, pb.y, pb.z), inv_spp, {f3(b0.x, b0.y, b0.z), f3(b1.x, b1.y, b1.z), b0.w},
              un.z * 8 + __float_as_int(b1.w));
       }
     } else {
@@ -494,6 +598,49 @@ __global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ job
       push(Q.slot, &out->slot, w);
     }
   }
+}
+
+// The first bounce of an indirect path from the first vertex g
+// (sampleIndirectLightFromFirstIntersection, src/render.cpp:314-423): the
+// reflection sample, or with GLASS the Fresnel split into reflection and
+// refraction, the refraction sample and the path's fresh media.
+template <bool GLASS>
+RMN_D void first_bounce(const Pool& P, int w, const Surf& g, float3 eye, RmnRng& rng, float3& dir, float3& w0,
+                        int& f0) {
+  float3 in0 = norm3(g.pos - eye);
+  Surf v0 = g;
+  const float ior0 = v0.eta;
+  v0.eta = 1.0f / v0.eta;  // from air into the surface
+  float p_reflect = 1.0f, F0 = 0.0f;
+  if (GLASS && v0.opacity < RMN_EPS) {
+    float3 rd;
+    precise_refraction(v0, -in0, rd, F0);
+    p_reflect = kP0Reflect + (1.0f - kP0Reflect) * F0;
+  }
+  if (rng.next() < p_reflect) {
+    sample_reflect(v0, -in0, rng, dir, w0, f0);
+    w0 = w0 / p_reflect;
+    if (GLASS) {
+      Media med;
+      med.init();  // Medium::Init: a fresh path starts in air
+      store_media(P, w, med);
+    }
+  } else if (GLASS) {
+    sample_btdf(v0, -in0, rng, dir, w0, f0);
+    w0 = w0 * (1.0f - F0);
+    w0 = w0 / (1.0f - p_reflect);
+    Media med;
+    med.init();
+    if (v0.entering) med.insert(v0.id, ior0, v0.base);
+    else med.erase(v0.id);
+    store_media(P, w, med);
+  } else {
+    dir = f3(NAN);  // never: p_reflect = 1 on opaque surfaces
+  }
+}
+__device__ __noinline__ void first_bounce_glass(const Pool& P, int w, const Surf& g, float3 eye, RmnRng& rng,
+                                                float3& dir, float3& w0, int& f0) {
+  first_bounce<true>(P, w, g, eye, rng, dir, w0, f0);
 }
 
 template <bool COUNT>
@@ -550,7 +697,12 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
         J = &jobs[jb];
         long long local = uid - J->unit_begin;
         int pixel = (int)(local / J->p.K), sub = (int)(local % J->p.K);
-        int j0 = sub * J->p.S, j1 = min(J->p.slots, j0 + J->p.S);
+        const float* gb0 = gbuf_of(*J, pixel);
+        // 16 times the indirect samples behind a transmissive or half-opaque
+        // first vertex (renderPixel, src/render.cpp:497-499); the units of a
+        // scene with such materials are laid out for that many
+        const int pix_slots = (J->p.glass && !(gb0[17] > 1.0f - RMN_EPS)) ? J->p.slots16 : J->p.slots;
+        int j1 = min(pix_slots, sub * J->p.S + J->p.S), j0 = min(sub * J->p.S, j1);
         float4* part = parts + (size_t)uid * RMN_PART_F4;
 #pragma unroll
         for (int k = 0; k < 6; ++k) part[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -604,16 +756,14 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
       rng = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)un.z);
       if (COUNT) slots_done++;
       // sampleIndirectLightFromFirstIntersection, src/render.cpp:314-423
-      if (len3(g.emis) > 0.0f || !(rng.next() < 1.0f)) {
+      if (len3(g.emis) > 0.0f) {
         un.z++;
         continue;
       }
-      float3 in0 = norm3(g.pos - p.pos);
-      Surf v0 = g;
-      v0.eta = 1.0f / v0.eta;
       float3 dir, w0;
       int f0 = 0;
-      sample_reflect(v0, -in0, rng, dir, w0, f0);
+      if (p.glass) first_bounce_glass(P, w, g, p.pos, rng, dir, w0, f0);
+      else first_bounce<false>(P, w, g, p.pos, rng, dir, w0, f0);
       if (!any_finite3(dir)) {
         un.z++;
         continue;
@@ -842,7 +992,7 @@ static void build_jobs(const RenderItem* items, int n, JobTable* t) {
     const RenderItem& it = items[i];
     Job j;
     j.s = it.scene->dev;
-    j.p = make_params(it.args);
+    j.p = make_params(it.args, it.scene->dev.has_glass != 0);
     j.gbuf = it.gbuf;
     j.dd = reinterpret_cast<float4*>(it.dd);
     j.ds = reinterpret_cast<float4*>(it.ds);
@@ -1070,13 +1220,20 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
   alloc((void**)&P.res, sizeof(float2) * W);
   alloc((void**)&P.pa, sizeof(float4) * W);
   alloc((void**)&P.pb, sizeof(float4) * W);
-  alloc((void**)&P.nv, sizeof(float4) * 5 * W);
+  alloc((void**)&P.nv, sizeof(float4) * 6 * W);
   alloc((void**)&P.lw, sizeof(float4) * 2 * W);
   alloc((void**)&P.nk, sizeof(int4) * W);
   alloc((void**)&P.drd, sizeof(float4) * kDirectBatch * W);
   alloc((void**)&P.dpend, sizeof(float4) * 2 * kDirectBatch * W);
   alloc((void**)&P.dres, sizeof(float) * kDirectBatch * W);
   alloc((void**)&P.dk, sizeof(int2) * W);
+  bool glass = false;
+  for (const Job& j : b->table.jobs) glass = glass || j.p.glass;
+  if (glass) {
+    alloc((void**)&P.mn, sizeof(int) * W);
+    alloc((void**)&P.mid, sizeof(int) * RMN_MEDIA * W);
+    alloc((void**)&P.mval, sizeof(float4) * RMN_MEDIA * W);
+  }
   for (int l = 0; l < b->lanes; ++l) {
     const size_t o = (size_t)l * per;
     Pool& L = b->pool[l];
@@ -1090,13 +1247,18 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
       L.res = P.res + o;
       L.pa = P.pa + o;
       L.pb = P.pb + o;
-      L.nv = P.nv + 5 * o;
+      L.nv = P.nv + 6 * o;
       L.lw = P.lw + 2 * o;
       L.nk = P.nk + o;
       L.drd = P.drd + kDirectBatch * o;
       L.dpend = P.dpend + 2 * kDirectBatch * o;
       L.dres = P.dres + kDirectBatch * o;
       L.dk = P.dk + o;
+      if (glass) {
+        L.mn = P.mn + o;
+        L.mid = P.mid + RMN_MEDIA * o;
+        L.mval = P.mval + RMN_MEDIA * o;
+      }
     }
     Queues& Q = b->q[l];
     for (int k = 0; k < 2; ++k) {
@@ -1139,6 +1301,8 @@ rmn_status batch_status(BatchState* b, cudaStream_t st) {
   cudaError_t e = cudaMemcpyAsync(&h, b->d_status, sizeof(int), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, "render");
+  if (h == kDevMediaOverflow) return fail(RMN_ERR_DEVICE_LIMIT, "render: a path entered more than %d nested media",
+                                          RMN_MEDIA - 1);
   if (h) return fail(RMN_ERR_DEVICE_LIMIT, "render: traversal stack bound reached");
   return RMN_OK;
 }

@@ -32,7 +32,7 @@ rmn_status build_scene(const rmn_scene_desc* desc, rmn_scene* scene);
 void free_scene(rmn_scene* scene);
 
 // Device-side status word written by kernels that hit one of their bounds.
-enum DeviceStatus { kDevOk = 0, kDevStackOverflow = 1, kDevBadIndex = 2 };
+enum DeviceStatus { kDevOk = 0, kDevStackOverflow = 1, kDevBadIndex = 2, kDevMediaOverflow = 3 };
 
 // Kernel launchers (trace.cu, render.cu, post.cu). All take device pointers.
 cudaError_t launch_trace_closest(const DevScene& s, const rmn_ray* rays, int64_t n, rmn_hit* hits, int* status,

@@ -126,4 +126,5 @@ struct DevScene {
   int num_lights;
   int sky_w, sky_h;
   int depth;
+  int has_glass;              // some material is transmissive or half-opaque (opacity <= 1 - 1e-4)
 };

@@ -275,12 +275,8 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
     if (d->indices[i] < 0 || d->indices[i] >= d->num_vertices)
       return fail(RMN_ERR_INVALID_ARGUMENT, "vertex index %d of triangle %lld out of range", d->indices[i],
                   (long long)(i / 3));
-  for (int m = 0; m < d->num_materials; ++m) {
-    const rmn_material& q = d->materials[m];
-    if (!(q.opacity > 1.0f - RMN_EPS))
-      return fail(RMN_ERR_UNSUPPORTED, "material %d is transmissive (opacity %g): glass and media are not on the GPU path",
-                  m, (double)q.opacity);
-  }
+  bool glass = false;
+  for (int m = 0; m < d->num_materials; ++m) glass = glass || !(d->materials[m].opacity > 1.0f - RMN_EPS);
   if (d->env_rgb && (d->env_width <= 0 || d->env_height <= 0))
     return fail(RMN_ERR_INVALID_ARGUMENT, "sky map needs positive width and height");
 
@@ -454,6 +450,7 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   g.sky_w = d->env_rgb ? d->env_width : 0;
   g.sky_h = d->env_rgb ? d->env_height : 0;
   g.depth = fl.max_depth;
+  g.has_glass = glass ? 1 : 0;
   return RMN_OK;
 }
 

@@ -78,7 +78,9 @@ RMN_D void hit_info(const DevScene& s, int i, float3 rd, Surf& h) {
   h.eta = mm.y;
   h.specular = 0.04f;
   if (h.opacity > 1.0f - RMN_EPS) h.entering = true;
-  h.base = f3(mb);  // opaque materials only reach the GPU path
+  // getHitMaterial, src/model.cpp:320-323: a transmissive surface takes its
+  // transmitting colour as base colour
+  h.base = h.opacity < RMN_EPS ? f3(__ldg(&m.trans)) : f3(mb);
   h.emis = f3(me);
   if (flags & RMN_TRI_RENORM) {  // calcSurfaceNormal with a zero normal-map texel
     float3 keep = h.surfN;
@@ -167,6 +169,28 @@ RMN_CALL float3 brdf(const Surf& s, float3 V, float3 L) {
   ret *= s.opacity;
   ret += fs * ds * gs;
   return ret * nl;
+}
+
+// BSDF::getBTDF, src/sampling.cpp:159-192 (eta relative, V = in).
+RMN_D float3 btdf(const Surf& s, float3 V, float3 L) {
+  const float3 N = s.surfN;
+  float nl = dot3(s.surfN, L);
+  if (nl >= 0.0f) return f3(0.0f);
+  float3 H = norm3(L + s.eta * V);
+  float D = gtr2(dot3(N, H), s.roughness);
+  float bt = D * (-nl);
+  float lh = dot3(L, H), nv = dot3(N, V), hv = dot3(H, V);
+  bt *= fabsf(lh * hv) / (fabsf(nl * nv) + RMN_EPS);
+  float k = s.eta * hv + lh;
+  bt /= k * k;
+  return f3(bt);
+}
+
+// BSDF::getBSDF, :194-199: the BTDF on the far side of a transmissive or
+// half-opaque surface, the BRDF otherwise.
+RMN_D float3 bsdf_eval(const Surf& s, float3 V, float3 L) {
+  if (s.opacity > 1.0f - RMN_EPS || s.entering) return brdf(s, V, L);
+  return btdf(s, V, L);
 }
 
 // getTangentSpaceWithInDir, src/geometry.cpp:105-124.
@@ -331,7 +355,7 @@ RMN_D bool light_weights(const DevScene& s, const Surf& sf, float3 V, float* w, 
     float4 c = __ldg(&s.lights[i].center);
     float3 ld = norm3(f3(c) - sf.pos);
     float dist = len3(f3(c) - sf.pos);
-    float3 f = brdf(sf, V, ld);
+    float3 f = bsdf_eval(sf, V, ld);
     w[i] = dot3(f, RMN_LUM) * c.w / (dist * dist + 1e-3f);
   }
   for (int i = 0; i < s.num_lights && i < 8; ++i) tot += w[i];
@@ -390,7 +414,7 @@ RMN_CALL bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float
     dir = norm3(lp - pos);
     float dist = len3(lp - pos);
     aim = dist - RMN_EPS;
-    float3 f = brdf(sf, V, dir);
+    float3 f = bsdf_eval(sf, V, dir);
     lum_clamp(f);
     out.bsdf = f;
     out.light = 2.0f * RMN_PI * lc.w * f3(lcol) / (dist * dist + 1e-3f) / pl;
@@ -415,7 +439,7 @@ RMN_CALL bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float
       float pdf = pr / total;
       dir = d;
       aim = INFINITY;
-      float3 f = brdf(sf, V, d);
+      float3 f = bsdf_eval(sf, V, d);
       lum_clamp(f);
       out.bsdf = f;
       out.light = f3(__ldg(s.sky + p)) / pdf;
@@ -424,6 +448,154 @@ RMN_CALL bool light_gen(const DevScene& s, const Surf& sf, float3 V, const float
     }
   }
   return false;
+}
+
+// ------------------------------------------------------------ glass -------
+// BSDF::preciseRefraction, src/sampling.cpp:285-308 (eta relative).
+RMN_D void precise_refraction(const Surf& s, float3 V, float3& out, float& F) {
+  const float3 N = s.surfN;
+  const float eta = s.eta;
+  float nv = dot3(N, V);
+  if (nv < 0.0f) {
+    F = 1.0f;
+    out = f3(NAN);
+    return;
+  }
+  float delta = 1.0f - eta * eta * (1.0f - nv * nv);
+  if (delta < 0.0f) {
+    F = 1.0f;
+    out = f3(NAN);
+    return;
+  }
+  float k = eta * nv - sqrtf(delta);
+  out = k * N - eta * V;
+  float ln = -dot3(out, N);
+  float r0 = (1.0f - eta) / (1.0f + eta);
+  r0 = r0 * r0;
+  F = r0 + (1.0f - r0) * schlick(ln);
+}
+
+// refract, :342-349.
+RMN_D float3 refract_dir(float3 V, float3 N, float eta) {
+  float nv = dot3(N, V);
+  float delta = 1.0f - eta * eta * (1.0f - nv * nv);
+  if (delta < 0.0f) return f3(NAN);
+  float k = eta * nv - sqrtf(delta);
+  return k * N - eta * V;
+}
+
+// BSDF::sampleBTDF, :351-388: a GGX half vector, refracted (<= 16 tries).
+RMN_CALL void sample_btdf(const Surf& s, float3 in, RmnRng& rng, float3& out, float3& w, int& fails) {
+  if (fabsf(s.eta - 1.0f) < RMN_EPS) {
+    out = -in;
+    w = f3(1.0f);
+    return;
+  }
+  float3 t, b;
+  frame(s, in, t, b);
+  const float3 V = in;
+  for (int T = 1; T <= RMN_MAX_TRYS; ++T) {
+    float u = rng.next(), phi = rng.next() * 2.0f * RMN_PI;
+    float ct = sqrtf((1.0f - u) / (1.0f + (s.roughness * s.roughness - 1.0f) * u));
+    float st = sqrtf(1 - ct * ct);
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    float3 H = st * cp * t + st * sp * b + ct * s.surfN;
+    out = refract_dir(V, H, s.eta);
+    float weight;
+    if (!any_finite3(out)) {
+      weight = 0.0f;
+    } else {
+      float vh = dot3(V, H), vn = dot3(V, s.surfN), hn = dot3(H, s.surfN);
+      weight = fabsf(vh) / fabsf(vn * hn);
+    }
+    if (weight > 0.0f && dot3(out, s.shapeN) < 0.0f) {
+      w = f3(weight);
+      return;
+    }
+    fails++;
+  }
+  w = f3(0.0f);
+  out = f3(NAN);
+}
+
+// getAbsorb, src/render.cpp:83-87, with pow_s (src/geometry.cpp:22-27).
+RMN_D float3 get_absorb(float3 a, float dis) {
+  float c = dot3(a, RMN_LUM);
+  if (!(c < 1.0f - RMN_EPS)) return f3(1.0f);
+  const float k = 32.0f * dis;
+  a.x = a.x < 0.0f ? 0.0f : a.x;
+  a.y = a.y < 0.0f ? 0.0f : a.y;
+  a.z = a.z < 0.0f ? 0.0f : a.z;
+  return f3(powf(a.x, k), powf(a.y, k), powf(a.z, k));
+}
+
+#define RMN_MEDIA 8  // media a path can be inside at once, air included
+constexpr float kP0Reflect = 0.24f;  // P0_reflect, src/render.cpp:118
+
+// Medium, src/render.cpp:11-42: the reference's multimap from material id
+// (air: -1) to (ior, absorb), as a sorted array: equal ids keep insertion
+// order, erase removes every entry of an id. ok turns false if a path would
+// be inside more than RMN_MEDIA media.
+struct Media {
+  int n;
+  bool ok;
+  int id[RMN_MEDIA];
+  float4 v[RMN_MEDIA];  // ior, absorb
+  RMN_D void init() {
+    n = 1;
+    ok = true;
+    id[0] = -1;
+    v[0] = make_float4(1.0f, 1.0f, 1.0f, 1.0f);
+  }
+  RMN_D void insert(int k, float ior, float3 ab) {
+    if (n >= RMN_MEDIA) {
+      ok = false;
+      return;
+    }
+    int i = n;
+    while (i > 0 && id[i - 1] > k) {
+      id[i] = id[i - 1];
+      v[i] = v[i - 1];
+      --i;
+    }
+    id[i] = k;
+    v[i] = make_float4(ior, ab.x, ab.y, ab.z);
+    ++n;
+  }
+  RMN_D void erase(int k) {
+    int j = 0;
+    for (int i = 0; i < n; ++i)
+      if (id[i] != k) {
+        id[j] = id[i];
+        v[j] = v[i];
+        ++j;
+      }
+    n = j;
+  }
+  RMN_D float ior() const {
+    float r = 1.0f;
+    for (int i = 0; i < n; ++i) r = r < v[i].x ? v[i].x : r;  // std::max
+    return r;
+  }
+  RMN_D float3 absorb() const {
+    float3 a = f3(1.0f);
+    for (int i = 0; i < n; ++i) a = a * f3(v[i].y, v[i].z, v[i].w);
+    return a;
+  }
+};
+
+// calcEta, src/render.cpp:89-99: sets s.eta to the relative index.
+RMN_D void calc_eta(Media& m, Surf& s) {
+  float eta1 = m.ior(), eta2;
+  if (s.entering) {
+    eta2 = eta1 < s.eta ? s.eta : eta1;  // std::max(eta1, eta)
+  } else {
+    m.erase(s.id);
+    eta2 = m.ior();
+    m.insert(s.id, s.eta, s.base);
+  }
+  s.eta = eta1 / eta2;
 }
 
 // ------------------------------------------------------------ derivatives --

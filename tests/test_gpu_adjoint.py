@@ -193,3 +193,9 @@ def test_adjoint_argument_errors():
     with pytest.raises(api.RmnError) as e:
         api.adjoint(m, a, ph, g)
     assert e.value.status == 1
+    ph.dropped = torch.full((16 * 16,), -1, dtype=torch.int32, device="cuda")
+    mg = api.Model(scenes.cornell_glass())
+    pg = api.render(mg, a)
+    with pytest.raises(api.RmnError) as e:
+        api.adjoint(mg, a, pg, g)
+    assert e.value.status == 4  # RMN_ERR_UNSUPPORTED

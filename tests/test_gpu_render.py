@@ -39,6 +39,7 @@ def gpu_records(model, cam, seed, lanes=0, host=False):
     rec[:, 8:12], rec[:, 12:16] = t(photo.radiance_Id), t(photo.radiance_Is)
     rec[:, 16:31] = g[:, 0:15]
     rec[:, 31], rec[:, 32], rec[:, 33], rec[:, 35], rec[:, 36] = g[:, 15], g[:, 16], g[:, 17], g[:, 18], g[:, 19]
+    rec[:, 37] = g[:, 20]
     return rec.reshape(cam.height, cam.width, 40), photo
 
 
@@ -55,6 +56,7 @@ def compare_paths(gpu, ora, frac=0.98):
     for a, b in [(16, 19), (22, 25), (25, 28), (28, 31)]:
         assert np.array_equal(gpu[..., a:b], ora[..., a:b], equal_nan=True), (a, b)
     assert np.array_equal(gpu[..., 31:34], ora[..., 31:34])
+    assert np.array_equal(gpu[..., 35:38], ora[..., 35:38])  # eta, material id, entering
     hit = ~np.isnan(ora[..., 22])
     assert np.array_equal(gpu[..., 19:22][hit], ora[..., 19:22][hit])
     em = np.isclose(gpu[..., 19:22], ora[..., 19:22], rtol=1e-5, atol=0).all(-1)
@@ -91,6 +93,35 @@ def test_sample_splits(port, spp, p_direct):
     g, _ = gpu_records(api.Model(c), cam, seed=3)
     o = port.scene(c).render(cam, seed=3, mode=1)
     compare_paths(g, o)
+
+
+@pytest.mark.parametrize("p_direct", [0.7, 0.0])
+def test_glass_paths_match_oracle(port, p_direct):
+    """Transmissive and half-opaque boxes: refraction, the Fresnel split,
+    media and absorption, the BTDF in light sampling, 16x samples behind
+    glass -- against the oracle on the same random streams."""
+    c = scenes.cornell_glass()
+    cam = scenes.cornell_camera(40, 40, 8, p_direct=p_direct)
+    g, _ = gpu_records(api.Model(c), cam, seed=17)
+    o = port.scene(c).render(cam, seed=17, mode=1)
+    assert (o[..., 33] < 1e-4).sum() > 50
+    compare_paths(g, o, frac=0.95)
+
+
+def test_glass_mean_matches_reference_stream(port):
+    """Statistical: the GPU's counter streams against the reference's own
+    mt19937 stream (the oracle in mode 0, pinned to the reference) at 1024 spp:
+    mean luminance of the whole image (seed-to-seed spread 0.3 %) and of the
+    glass box's pixels (spread 3.5 %: paths through glass to the light are
+    rare and bright)."""
+    c = scenes.cornell_glass()
+    cam = scenes.cornell_camera(32, 32, 1024)
+    g, _ = gpu_records(api.Model(c), cam, seed=23)
+    o = port.scene(c).render(cam, seed=23, mode=0)
+    lg, lo = linear_image(g) @ LUM, linear_image(o) @ LUM
+    glass = o[..., 33] < 1e-4
+    assert abs(lg.mean() - lo.mean()) <= 0.02 * lo.mean()
+    assert abs(lg[glass].mean() - lo[glass].mean()) <= 0.12 * lo[glass].mean()
 
 
 def test_lane_split_invariance():
@@ -194,8 +225,10 @@ def test_batch_equals_individual_renders(use_graph):
     hf.env = scenes.sky_env(64, 32, sun_radiance=100.0, sun_diameter_deg=8.0)
     sky = api.Model(hf)
     skycam = scenes.Camera((0.3, 2.0, -0.8), (0.35, -0.45, 0.82), (0.0, -1.0, 0.0), (-1.0, 0.0, 0.0), 0.03, 33, 21, 9)
+    gl = api.Model(scenes.cornell_glass())
     specs = [(cor, scenes.cornell_camera(40, 40, 16), 1, 4), (sky, skycam, 2, 0),
-             (cor, scenes.cornell_camera(17, 29, 5, max_depth=6), 3, 1), (sky, skycam, 4, 32)]
+             (cor, scenes.cornell_camera(17, 29, 5, max_depth=6), 3, 1), (sky, skycam, 4, 32),
+             (gl, scenes.cornell_camera(24, 24, 6), 5, 0)]
     items, solo = [], []
     for m, cam, seed, k in specs:
         a = api.RenderArgs.from_camera(cam, seed=seed, lanes_per_pixel=k)

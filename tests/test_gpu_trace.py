@@ -114,12 +114,12 @@ def test_scene_errors():
     with pytest.raises(api.RmnError) as e:
         api.Model(c)
     assert e.value.status == 1 and "out of range" in str(e.value)
-    g = scenes.cornell()
-    g.materials = g.materials.copy()
-    g.materials[0, 11] = 0.0  # glass
+    m = scenes.cornell()
+    m.mesh_material = m.mesh_material.copy()
+    m.mesh_material[2] = 99  # no such material
     with pytest.raises(api.RmnError) as e:
-        api.Model(g)
-    assert e.value.status == 4
+        api.Model(m)
+    assert e.value.status == 1
 
 
 @pytest.mark.parametrize("shape", [(64, 96), (61, 173), (1080, 1920), (7, 5)])
@@ -151,7 +151,7 @@ def _photo_from_records(rec):
     g = torch.zeros((h * w, api.GBUFFER_FLOATS), device="cuda")
     g[:, 0:3] = r[:, 16:19]; g[:, 3:6] = r[:, 19:22]; g[:, 6:9] = r[:, 22:25]
     g[:, 9:12] = r[:, 25:28]; g[:, 12:15] = r[:, 28:31]; g[:, 15] = r[:, 31]
-    g[:, 16] = r[:, 32]; g[:, 17] = r[:, 33]; g[:, 18] = r[:, 35]; g[:, 19] = r[:, 36]
+    g[:, 16] = r[:, 32]; g[:, 17] = r[:, 33]; g[:, 18] = r[:, 35]; g[:, 19] = r[:, 36]; g[:, 20] = r[:, 37]
     p.Gbuffer.copy_(g)
     return p
 
