@@ -269,6 +269,75 @@ def adjoint_timing(args, stream, flush, barrier):
             "call": "rmn_render then rmn_adjoint on device buffers, CUDA events on the stream"}
 
 
+def config_timings(args, stream, flush, barrier):
+    """The reference's other configurations, each timed on its own (CUDA
+    events on the stream, W warm-ups, L2 flushed before each step, device
+    buffers):
+      cornell     -- Cornell box (36 triangles), 256x256, 64 spp, depth 8;
+      traversal   -- 1M-triangle random soup, 4M closest-hit + 4M shadow rays;
+      heightfield -- 2048^2 heightfield (8,380,418 triangles) under a
+                     2048x1024 sky, 1920x1080, 256 spp, depth 16, composed
+                     with gamma and FXAA."""
+    import torch
+    from raym0nade_gb300 import api, scenes
+
+    def timeit(fn, steps=None):
+        for _ in range(args.warmup):
+            fn()
+        barrier()
+        ms = []
+        for _ in range(steps or args.steps):
+            flush.fill_(1)
+            torch.cuda.current_stream().wait_stream(stream)
+            stream.wait_stream(torch.cuda.current_stream())
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ms.append(e0.elapsed_time(e1))
+        return float(sum(ms)) / len(ms)
+
+    out = {}
+    cm = api.Model(scenes.cornell())
+    cam = scenes.cornell_camera(256, 256, 64, max_depth=8)
+    ca = api.RenderArgs.from_camera(cam, seed=1)
+    cp = api.Photo(256, 256)
+    ms = timeit(lambda: api.render(cm, ca, cp, stream))
+    out["cornell"] = {"Mpaths_s": 256 * 256 * 64 / ms / 1e3, "ms": ms,
+                      "workload": "Cornell box 36 tris, 256x256, 64 spp, max depth 8 (rmn_render)"}
+
+    soup = api.Model(scenes.random_soup(1_000_000, 1))
+    rays = torch.from_numpy(scenes.random_rays(4_000_000, 2)).cuda()
+    srays = torch.from_numpy(scenes.random_rays(4_000_000, 3, shadow=True)).cuda()
+    hits = soup.rayHit(rays, stream=stream)
+    occ = soup.rayHit_test(srays, stream=stream)
+    mc = timeit(lambda: soup.rayHit(rays, hits, stream))
+    msh = timeit(lambda: soup.rayHit_test(srays, occ, stream))
+    out["traversal"] = {"closest_Mrays_s": 4e6 / mc / 1e3, "shadow_Mrays_s": 4e6 / msh / 1e3,
+                        "closest_ms": mc, "shadow_ms": msh,
+                        "workload": "1M-triangle soup, 4M closest-hit + 4M shadow rays (rmn_trace_closest / _shadow)"}
+    del soup, rays, srays, hits, occ
+
+    hf = scenes.heightfield(2048, seed=3)
+    hf.env = scenes.sky_env(2048, 1024)
+    hm = api.Model(hf)
+    hcam = scenes.heightfield_camera(1920, 1080, 256)
+    ha = api.RenderArgs.from_camera(hcam, seed=1)
+    hp = api.Photo(1920, 1080)
+    rgb = torch.empty((1080, 1920, 3), dtype=torch.float32, device="cuda")
+
+    def step_hf():
+        api.render(hm, ha, hp, stream)
+        hp.shade(api.Full | api.GAMMA | api.DoFXAA, out=rgb, stream=stream)
+
+    ms = timeit(step_hf, steps=max(1, min(args.steps, 2)))
+    out["heightfield"] = {"Mpaths_s": 1920 * 1080 * 256 / ms / 1e3, "ms": ms,
+                          "workload": "2048^2 heightfield (8,380,418 tris), sky 2048x1024, 1920x1080, 256 spp, "
+                                      "max depth 16, gamma + FXAA (rmn_render + rmn_compose)"}
+    return out
+
+
 def run_gpu(args, rank, world, dist):
     import torch
     from raym0nade_gb300 import api
@@ -295,6 +364,7 @@ def run_gpu(args, rank, world, dist):
         tune["tune_s"] = round(time.perf_counter() - t0, 2)
         for a in argsl:
             a.slots_per_unit = tune["slots_per_unit"]
+    lanes = tune["lanes"] if tune else 2
     with torch.cuda.stream(stream):
         batch = api.Batch(list(zip(models, argsl, photos)), use_graph=True, stream=stream,
                           pool_workers=tune["pool_workers"] if tune else 0, lanes=tune["lanes"] if tune else 0)
@@ -366,6 +436,7 @@ def run_gpu(args, rank, world, dist):
     h2d = len(insts) * 96 + npx * (4 * 16 + 20 * 4)
 
     adj = adjoint_timing(args, stream, flush, barrier) if args.adjoint else None
+    per_config = config_timings(args, stream, flush, barrier) if args.configs else None
 
     value = job_rate(paths_per_step, world, ms_b / 1e3)
     plain = job_rate(paths_per_step, world, ms_p / 1e3)
@@ -393,15 +464,17 @@ def run_gpu(args, rank, world, dist):
         "config": {"workload": desc, "instances": len(insts), "triangles": int(sum(i.scene.num_triangles for i in insts)),
                    "pixels": npx, "paths_per_step": paths_per_step, "parallelism": f"replicas x{world}",
                    "l2": f"scene data {scene_bytes / 1e9:.2f} GB > L2, and a 256 MiB buffer is overwritten between steps",
-                   "launch": "rmn_batch: 1 G-buffer + 1 persistent path kernel per step, replayed CUDA graph",
+                   "launch": "rmn_batch: G-buffer kernel, then wavefront iterations (shade, NEE, slot, closest and "
+                             "shadow traversal kernels) of every lane as parallel branches of a replayed CUDA graph",
                    "scene_build_s": round(build_s, 1)},
         "plain": {"value": plain, "unit": UNIT, "ms_per_step": ms_p, "launches_per_step": 2 * len(insts),
                   "batched_over_plain": value / plain},
         "e2e": {"value": job_rate(paths_per_step, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
                 "call": "rmn_render into pinned host buffers + rmn_compose(Full|gamma|FXAA) to a host image, per instance"},
-        # per batched step: G-buffer kernel, 3 kernels per wavefront iteration, finalize
-        "gpu_launches": args.steps * (2 + 3 * prof["iterations"]),
+        # per batched step: G-buffer kernel, one seed kernel per lane, 5 kernels
+        # per wavefront iteration and lane, finalize
+        "gpu_launches": args.steps * (2 + lanes + 5 * lanes * prof["iterations"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": BATCH64_TRAVERSAL_DRAM_BYTES if args.workload == "batch64" else None,
                      "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over every qtrace_kernel "
@@ -418,6 +491,8 @@ def run_gpu(args, rank, world, dist):
         out["config"]["autotune"] = tune
     if adj:
         out["adjoint"] = adj
+    if per_config:
+        out["configs"] = per_config
     if base:
         out["cpu_baseline"] = base
     print(json.dumps(out))
@@ -433,6 +508,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false")
+    ap.add_argument("--no-configs", dest="configs", action="store_false")
     args = ap.parse_args()
     if args.warmup < 3:
         raise SystemExit("at least 3 warm-up steps")
