@@ -6,7 +6,9 @@ ctypes bindings for the two CPU checker libraries built by oracle/Makefile:
   hot path (oracle/port/port.cpp);
 * ``ref``:  oracle/_ref/libref.so, the reference's own sources compiled with
   shims (oracle/ref/harness.cpp); only present where the reference checkout
-  was available at build time.
+  was available at build time;
+* ``ref_tex``: oracle/_ref/libref_tex.so, the same with the reference's own
+  src/material.cpp (8-bit textures, mip chains) instead of constant texels.
 
 Both export the same functions (prefix ``port_`` / ``ref_``), wrapped here by
 ``OracleLib``. Only tests/, __graft_entry__.smoke() and bench.py's CPU
@@ -23,6 +25,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libport.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
+REF_TEX_SO = os.path.join(HERE, "_ref", "libref_tex.so")
 REFERENCE_DIR = "/root/reference"
 PIX_FLOATS = 40
 
@@ -34,6 +37,7 @@ class _SceneIn(C.Structure):
         ("num_meshes", C.c_int32), ("mesh_first", C.c_void_p), ("mesh_material", C.c_void_p),
         ("num_materials", C.c_int32), ("materials", C.c_void_p),
         ("env_width", C.c_int32), ("env_height", C.c_int32), ("env_rgb", C.c_void_p),
+        ("num_textures", C.c_int32), ("tex_dims", C.c_void_p), ("tex_data", C.c_void_p), ("mat_tex", C.c_void_p),
     ]
 
 
@@ -58,10 +62,15 @@ class OracleScene:
         env = None if scene.env is None else np.ascontiguousarray(scene.env, np.float32)
         self._keep.append(env)
         p, n, u, i, mf, mm, mat = self._keep[:7]
+        dims, texs, mtex = scene.texture_arrays()
+        ptrs = (C.c_void_p * max(len(texs), 1))(*[t.ctypes.data for t in texs])
+        self._keep += [dims, texs, mtex, ptrs]
         d = _SceneIn(p.shape[0], _ptr(p), _ptr(n), _ptr(u), i.shape[0], _ptr(i), mm.shape[0], _ptr(mf), _ptr(mm),
                      mat.shape[0], _ptr(mat), 0 if env is None else env.shape[1], 0 if env is None else env.shape[0],
-                     _ptr(env))
+                     _ptr(env), len(texs), _ptr(dims), C.cast(ptrs, C.c_void_p).value if texs else None, _ptr(mtex))
         self.handle = lib.fn("scene_create")(C.byref(d))
+        if not self.handle:
+            raise ValueError(f"{lib.kind}: scene refused")
         self.num_triangles = int(i.shape[0])
 
     def close(self):
@@ -123,7 +132,8 @@ class OracleScene:
 class OracleLib:
     def __init__(self, kind: str = "port"):
         self.kind = kind
-        path = PORT_SO if kind == "port" else REF_SO
+        path = {"port": PORT_SO, "ref": REF_SO, "ref_tex": REF_TEX_SO}[kind]
+        prefix = "port" if kind == "port" else "ref"
         if not os.path.exists(path):
             raise FileNotFoundError(f"{path} is not built (oracle.bindings.build())")
         self.lib = C.CDLL(path)
@@ -145,7 +155,7 @@ class OracleLib:
             "fxaa": (None, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
         }
         for name, (res, args) in sig.items():
-            f = getattr(self.lib, f"{kind}_{name}", None)
+            f = getattr(self.lib, f"{prefix}_{name}", None)
             if f is None:
                 continue
             f.restype = res
@@ -182,3 +192,7 @@ class OracleLib:
 
 def have_ref() -> bool:
     return os.path.exists(REF_SO)
+
+
+def have_ref_tex() -> bool:
+    return os.path.exists(REF_TEX_SO)

@@ -34,6 +34,15 @@ typedef struct orc_scene_in {
   const float* materials;  // ORC_MAT_FLOATS per material
   int32_t env_width, env_height;
   const float* env_rgb;  // 3 per texel, row-major from the top row; NULL if none
+  // 8-bit textures, row-major as the reference's loaders deliver them:
+  // tex_dims 3 per texture (width, height, channels), tex_data one pointer
+  // per texture; mat_tex 4 per material (diffuse, specular, emissive, normal
+  // map texture index, -1 none), or NULL for no textures at all. A texture
+  // slot takes precedence over the record's constant texel.
+  int32_t num_textures;
+  const int32_t* tex_dims;
+  const uint8_t* const* tex_data;
+  const int32_t* mat_tex;
 } orc_scene_in;
 
 // RenderArgs (include/render.h:8-15) packed as 24 floats:

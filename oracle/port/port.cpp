@@ -55,17 +55,127 @@ static bool any_finite(const vec3& v) { return std::isfinite(v.x) || std::isfini
 static float fmix(float a, float b, float t) { return a * (1 - t) + b * t; }  // src/sampling.cpp:16-18
 static float fclampf(float x, float a, float b) { return x < a ? a : (x > b ? b : x); }  // :12-14
 
+// ---------------------------------------------------------------- textures -
+constexpr int kMipLevels = 8;  // MAX_MIPMAP_LEVEL, include/material.h:10
+
+// ImageData, src/material.cpp:26-118: 8-bit texels, a mip chain of 2x2 box
+// averages (integer division), bilinear lookups with wrap-around and a blend
+// of two levels.
+struct Image {
+  int w = 0, h = 0, ch = 0, depth = 0;
+  std::vector<uint8_t> lv[kMipLevels];
+
+  void mips() {  // ImageData::generateMipmaps, :100-129
+    depth = kMipLevels;
+    for (int level = 1; level < kMipLevels; ++level) {
+      int pw = w >> (level - 1), ph = h >> (level - 1), cw = w >> level, chh = h >> level;
+      if (cw == 0 || chh == 0) { depth = level; break; }
+      lv[level].resize((size_t)cw * chh * ch);
+      for (int y = 0; y < chh; ++y)
+        for (int x = 0; x < cw; ++x)
+          for (int c = 0; c < ch; ++c) {
+            int sum = 0;
+            for (int dy = 0; dy < 2; ++dy)
+              for (int dx = 0; dx < 2; ++dx) {
+                int px = (x * 2 + dx) % pw, py = (y * 2 + dy) % ph;
+                sum += lv[level - 1][((size_t)py * pw + px) * ch + c];
+              }
+            lv[level][((size_t)y * cw + x) * ch + c] = (uint8_t)(sum / 4);
+          }
+    }
+  }
+  // get_basic<vec3/vec4>: N bytes from index, / 255.
+  template <int N>
+  static vec4 basic(const std::vector<uint8_t>& d, int i) {
+    vec4 v(static_cast<float>(d[i]), static_cast<float>(d[i + 1]), static_cast<float>(d[i + 2]),
+           N == 4 ? static_cast<float>(d[i + 3]) : 0.0f);
+    return v / 255.0f;
+  }
+  // get_bilinear, :48-80 (the element stride follows the requested type).
+  template <int N>
+  static vec4 bilinear(const std::vector<uint8_t>& d, int width, int height, float u, float v) {
+    auto wrap = [](int& x, int m) {
+      if (x < 0 || x >= m) {
+        x %= m;
+        if (x < 0) x += m;
+      }
+    };
+    float x = u * float(width), y = v * float(height);
+    int x0 = int(floorf(x)), y0 = int(floorf(y));
+    float dx = x - float(x0), dy = y - float(y0);
+    wrap(x0, width);
+    wrap(y0, height);
+    int x1 = (x0 + 1) % width, y1 = (y0 + 1) % height;
+    vec4 c00 = basic<N>(d, (y0 * width + x0) * N), c01 = basic<N>(d, (y0 * width + x1) * N);
+    vec4 c10 = basic<N>(d, (y1 * width + x0) * N), c11 = basic<N>(d, (y1 * width + x1) * N);
+    vec4 c0 = c00 * (1.0f - dx) + c01 * dx;
+    vec4 c1 = c10 * (1.0f - dx) + c11 * dx;
+    return c0 * (1.0f - dy) + c1 * dy;
+  }
+  // ImageData::get, :82-94.
+  template <int N>
+  vec4 get(float u, float v, float dep) const {
+    v = 1.0f - v;
+    dep = std::max(std::min(dep, static_cast<float>(depth - 1)), 0.0f);
+    int level = static_cast<int>(dep);
+    int next = std::min(level + 1, depth - 1);
+    float blend = dep - float(level);
+    vec4 a = bilinear<N>(lv[level], w >> level, h >> level, u, v);
+    vec4 b = bilinear<N>(lv[next], w >> next, h >> next, u, v);
+    return a * (1.0f - blend) + b * blend;
+  }
+  bool has_transparent_part() const {  // ImageData::hasTransparentPart, :100-105
+    for (size_t i = 3; i < lv[0].size(); i += 4)
+      if (lv[0][i] < 255) return true;
+    return false;
+  }
+};
+
+static void gamma_pow(vec4& v) {  // gammaPow, src/material.cpp:335-346
+  const float g = 2.2f;
+  v[0] = std::pow(v[0], g);
+  v[1] = std::pow(v[1], g);
+  v[2] = std::pow(v[2], g);
+}
+
 // ---------------------------------------------------------------- scene ----
 struct Mat {
   vec3 base, emis, trans;
   bool has_base, has_emis, has_surf;
   float roughness, metallic, opacity, ior;
   int id;
-  // Material::getDiffuseColor / getEmissiveColor / getSurfaceData with one
-  // constant texel (src/material.cpp:349-383).
-  vec3 diffuse() const { return has_base ? base : vec3(1.0f); }
-  vec3 emission() const { return has_emis ? emis : vec3(0.0f); }
-  void surface(float& r, float& m) const {
+  const Image* tex[4] = {nullptr, nullptr, nullptr, nullptr};  // diffuse, specular, emissive, normal map
+  bool transparent = false;  // Material::hasFullyTransparentPart
+  // Material::getDiffuseColor / getNormal / getEmissiveColor /
+  // getSurfaceData, src/material.cpp:349-383: a texture when the slot has
+  // one (mip level log2(duv * width), duv = NaN: level 0), else the record's
+  // constant texel.
+  static float level_of(const Image* t, float duv) { return std::isnan(duv) ? 0.0f : std::log2(duv * float(t->w)); }
+  vec4 diffuse4(float u, float v, float duv) const {
+    if (!tex[0]) return has_base ? vec4(base.x, base.y, base.z, 1.0f) : vec4(1.0f);
+    vec4 c = tex[0]->get<4>(u, v, level_of(tex[0], duv));
+    gamma_pow(c);
+    return c;
+  }
+  vec3 diffuse(float u = 0.0f, float v = 0.0f, float duv = NAN) const { return vec3(diffuse4(u, v, duv)); }
+  vec3 normal_map(float u, float v, float duv) const {
+    if (!tex[3]) return vec3(0.0f);
+    return vec3(tex[3]->get<3>(u, v, level_of(tex[3], duv))) * 2.0f - 1.0f;
+  }
+  vec3 emission(float u = 0.0f, float v = 0.0f, float duv = NAN) const {
+    if (!tex[2]) return has_emis ? emis : vec3(0.0f);
+    vec4 c = tex[2]->get<4>(u, v, level_of(tex[2], duv));
+    gamma_pow(c);
+    return vec3(c);
+  }
+  bool emissive() const { return tex[2] != nullptr || has_emis; }
+  void surface(float& r, float& m, float u = 0.0f, float v = 0.0f) const {
+    if (tex[1]) {
+      vec4 d = tex[1]->get<4>(u, v, 0);
+      m = std::min(d[2], 0.99f);
+      r = std::max(d[1], 1e-3f);
+      return;
+    }
     if (!has_surf) { m = 0.0f; r = roughness; return; }
     m = std::min(metallic, 0.99f);
     r = std::max(roughness, 1e-3f);
@@ -113,6 +223,7 @@ struct Stats { uint64_t inner = 0, leaves = 0, tris = 0; };
 struct Scene {
   std::vector<vec3> nrm;
   std::vector<vec2> uv;
+  std::vector<Image> images;
   std::vector<Mat> mats;
   std::vector<Tri> tris;   // permuted in place by the builder, like Model::faces
   std::vector<Node> nodes; // heap-indexed, children 2u and 2u+1
@@ -236,18 +347,41 @@ static void traverse(const Scene& s, const Ray& r, Hit& h, Stats* st) {
   if (s.tris.empty()) return;  // the reference indexes past its node array here
   visit(s, 1, r, h, st);
 }
-// Model::rayHit, src/model.cpp:332-341. Constant-texel materials have no
-// fully transparent texels, so the alpha-test retry never fires.
+static vec3 bary(const vec3& v0, const vec3& v1, const vec3& v2, const vec3& p);
+// TransparentTest, src/model.cpp:217-230: the hit is cut away when its
+// material's diffuse texture has texels of alpha < 1 and the level-0 alpha at
+// the hit is below eps.
+static bool alpha_cut(const Scene& s, const Ray& r, const Hit& h) {
+  const Tri& f = s.tris[h.face];
+  const Mat& m = s.mats[f.mat];
+  if (!m.transparent) return false;
+  vec3 p = r.o + r.d * h.tmax;
+  vec3 b = bary(f.v[0], f.v[1], f.v[2], p);
+  vec2 uv = b[0] * s.uv[f.vid[0]] + b[1] * s.uv[f.vid[1]] + b[2] * s.uv[f.vid[2]];
+  return m.diffuse4(uv[0], uv[1], NAN)[3] < kEps;
+}
+constexpr int kAlphaRetries = 8;  // maxRayDepth_hit, src/model.cpp:330
+// Model::rayHit, src/model.cpp:332-341: a cut-away hit restarts the search
+// eps beyond it, at most 8 times.
 static Hit closest(const Scene& s, const Ray& r, Stats* st = nullptr) {
   Hit h{kEps, INFINITY, -1};
-  traverse(s, r, h, st);
+  for (int k = 0; k < kAlphaRetries; ++k) {
+    traverse(s, r, h, st);
+    if (h.tmax == INFINITY || !alpha_cut(s, r, h)) return h;
+    h = Hit{h.tmax + kEps, INFINITY, -1};
+  }
   return h;
 }
 // Model::rayHit_test, src/model.cpp:343-354.
 static bool occluded(const Scene& s, const Ray& r, float aim, Stats* st = nullptr) {
   Hit h{kEps, aim + kEps, -1};
-  traverse(s, r, h, st);
-  return !(h.tmax >= aim);
+  for (int k = 0; k < kAlphaRetries; ++k) {
+    traverse(s, r, h, st);
+    if (h.tmax >= aim) return false;
+    if (!alpha_cut(s, r, h)) return true;
+    h = Hit{h.tmax + kEps, aim + kEps, -1};
+  }
+  return true;
 }
 
 // barycentric, src/geometry.cpp:89-103 -> (gamma, alpha, beta).
@@ -293,10 +427,9 @@ static void hit_normals(const Scene& s, const Tri& f, const vec3& in, const vec3
   if (!any_finite(surfN)) surfN = shapeN;
 }
 
-// calcSurfaceNormal with the zero normal-map texel that getNormal returns
-// without a normal texture (src/model.cpp:279-298, src/material.cpp:358-363).
-static void surface_normal(const Scene& s, const Tri& f, const vec3& shapeN, vec3& surfN) {
-  const vec3 nm(0.0f);
+// calcSurfaceNormal, src/model.cpp:279-298: the normal-map texel (zero
+// without a normal map) in the uv tangent frame.
+static void surface_normal(const Scene& s, const Tri& f, const vec3& nm, const vec3& shapeN, vec3& surfN) {
   vec3 e1 = f.v[1] - f.v[0], e2 = f.v[2] - f.v[0];
   vec2 d1 = s.uv[f.vid[1]] - s.uv[f.vid[0]], d2 = s.uv[f.vid[2]] - s.uv[f.vid[0]];
   float k = 1.0f / (d1.x * d2.y - d2.x * d1.y);
@@ -308,24 +441,58 @@ static void surface_normal(const Scene& s, const Tri& f, const vec3& shapeN, vec
   if (!any_finite(surfN)) surfN = keep;
 }
 
-// getHitInfo + getHitMaterial for constant-texel materials,
-// src/render.cpp:62-79 and src/model.cpp:300-328. Ray differentials only feed
-// texture LOD, which constant texels ignore.
-static void hit_info(const Scene& s, const Tri& f, const Ray& r, Surf& h) {
+// RayDifferential, include/render.h:29-33.
+struct Diff { vec3 dPdx = vec3(0.0f), dPdy = vec3(0.0f), dDdx = vec3(0.0f), dDdy = vec3(0.0f); };
+
+// calc_dPdxy, src/render.cpp:44-50.
+static void calc_dPdxy(const Ray& r, float t, const vec3& n, const Diff& d, vec3& px, vec3& py) {
+  float dtdx = -dot(d.dPdx + t * d.dDdx, n) / dot(r.d, n);
+  float dtdy = -dot(d.dPdy + t * d.dDdy, n) / dot(r.d, n);
+  px = d.dPdx + dtdx * r.d + t * d.dDdx;
+  py = d.dPdy + dtdy * r.d + t * d.dDdy;
+}
+// calc_dDdxy, src/render.cpp:52-60 (the normal's derivatives are zero).
+static void calc_dDdxy(const Ray& r, const vec3& n, const Diff& d, vec3& dx, vec3& dy) {
+  const vec3 dN(0.0f);
+  float dDNdx = dot(dN, r.d) + dot(d.dDdx, n);
+  float dDNdy = dot(dN, r.d) + dot(d.dDdy, n);
+  dx = d.dDdx - 2.0f * (dot(r.d, n) * dN + dDNdx * n);
+  dy = d.dDdy - 2.0f * (dot(r.d, n) * dN + dDNdy * n);
+}
+static bool any_finite2(const vec2& v) { return std::isfinite(v.x) || std::isfinite(v.y); }
+// getDuv, src/model.cpp:272-277.
+static vec2 get_duv(const Scene& s, const Tri& f, const vec3& dP) {
+  vec3 b = bary(f.v[0], f.v[1], f.v[2], f.v[0] + dP);
+  return (b[0] - 1.0f) * s.uv[f.vid[0]] + b[1] * s.uv[f.vid[1]] + b[2] * s.uv[f.vid[2]];
+}
+
+// getHitInfo + getHitMaterial, src/render.cpp:62-79 and src/model.cpp:
+// 300-328: t is the hit distance along r, d the ray's differential (texture
+// level of detail); hit_dPdx / hit_dPdy receive the hit point's.
+static void hit_info(const Scene& s, const Tri& f, const Ray& r, float t, const Diff& d, Surf& h, vec3* hit_dPdx = nullptr,
+                     vec3* hit_dPdy = nullptr) {
   vec3 b = bary(f.v[0], f.v[1], f.v[2], h.pos);
   hit_normals(s, f, r.d, b, h.shapeN, h.surfN, h.entering);
   vec3 raw = h.surfN;
+  vec3 px, py;
+  calc_dPdxy(r, t, h.shapeN, d, px, py);
+  vec2 uv = b[0] * s.uv[f.vid[0]] + b[1] * s.uv[f.vid[1]] + b[2] * s.uv[f.vid[2]];
   const Mat& m = s.mats[f.mat];
   h.id = m.id;
-  m.surface(h.roughness, h.metallic);
+  m.surface(h.roughness, h.metallic, uv[0], uv[1]);
   h.opacity = m.opacity;
   h.eta = m.ior;
   if (h.opacity > 1.0f - kEps) h.entering = true;
-  h.base = (h.opacity < kEps) ? m.trans : m.diffuse();
-  h.emis = m.emission();
-  surface_normal(s, f, h.shapeN, h.surfN);
+  vec2 ux = get_duv(s, f, px), uy = get_duv(s, f, py);
+  float duv = (any_finite2(ux) && any_finite2(ux)) ? (length(ux) + length(uy)) / 2.0f : NAN;
+  h.base = (h.opacity < kEps) ? m.trans : m.diffuse(uv[0], uv[1], duv);
+  h.emis = m.emission(uv[0], uv[1], duv);
+  vec3 nm = m.normal_map(uv[0], uv[1], duv);
+  surface_normal(s, f, nm, h.shapeN, h.surfN);
   if (dot(h.surfN, r.d) >= 0.0f) h.surfN = raw;
   if (dot(h.surfN, r.d) >= 0.0f) h.surfN = h.shapeN;
+  if (hit_dPdx) *hit_dPdx = px;
+  if (hit_dPdy) *hit_dPdy = py;
 }
 
 // ---------------------------------------------------------------- BSDF -----
@@ -730,7 +897,7 @@ constexpr float kP0Reflect = 0.24f;  // P0_reflect, src/render.cpp:118
 // mulWeight, :101-116); the loop keeps the per-depth factors and applies them
 // in that order so the float products match.
 template <class G>
-static void indirect_path(const Scene& s, const Surf& g, const vec3& eye, int maxd, G& gen,
+static void indirect_path(const Scene& s, const Surf& g, const vec3& eye, const Diff& d0, int maxd, G& gen,
                           std::vector<LSample>& out) {
   if (length(g.emis) > 0) return;
   Medium med;
@@ -748,7 +915,11 @@ static void indirect_path(const Scene& s, const Surf& g, const vec3& eye, int ma
   }
   vec3 dir, w0 = vec3(NAN);
   int f0 = 0;
+  Diff diff = d0;  // the refracted ray keeps the camera ray's differential
   if (gen() < p_reflect) {
+    const Ray cam{eye, in};
+    calc_dPdxy(cam, length(g.pos - eye), b0.s.shapeN, d0, diff.dPdx, diff.dPdy);
+    calc_dDdxy(cam, b0.s.surfN, d0, diff.dDdx, diff.dDdy);
     b0.sample_reflect(gen, dir, w0, f0);
     w0 /= p_reflect;
   } else {
@@ -775,7 +946,8 @@ static void indirect_path(const Scene& s, const Surf& g, const vec3& eye, int ma
     }
     Bsdf bs{-ray.d, Surf()};
     bs.s.pos = ray.o + ray.d * h.tmax;
-    hit_info(s, s.tris[h.face], ray, bs.s);
+    vec3 hpx, hpy;
+    hit_info(s, s.tris[h.face], ray, h.tmax, diff, bs.s, &hpx, &hpy);
     const float ior = bs.s.eta;
     rf = std::max(rf, 1.0f * bs.s.roughness);
     bs.s.roughness = std::max(bs.s.roughness, rf);
@@ -809,6 +981,9 @@ static void indirect_path(const Scene& s, const Surf& g, const vec3& eye, int ma
       bs.sample_reflect(gen, nd, w, nf);
       w /= pr;
       if (nee) w /= p_rr;
+      vec3 ddx, ddy;
+      calc_dDdxy(ray, bs.s.surfN, diff, ddx, ddy);
+      diff = Diff{hpx, hpy, ddx, ddy};
     } else {  // refraction
       nee = nee && !bs.s.entering && med.size() == 2;
       if (nee && (depth >= maxd || gen() > p_rr)) {
@@ -900,6 +1075,17 @@ struct CtrGen {
   float operator()() { return r.next(); }
 };
 
+// initRayDiff, src/render.cpp:439-446: the camera ray's differential for
+// the unnormalised pixel direction d.
+static Diff ray_diff(const vec3& d, const Args& a) {
+  Diff r;
+  const vec3 ddx = a.accuracy * a.right, ddy = a.accuracy * a.up;
+  float dd = dot(d, d), dx = dot(d, ddx), dy = dot(d, ddy);
+  r.dDdx = (dd * ddx - d * dx) / (std::sqrt(dd) * dd);
+  r.dDdy = (dd * ddy - d * dy) / (std::sqrt(dd) * dd);
+  return r;
+}
+
 // renderPixel, src/render.cpp:448-551. mode 0: one mt19937 per pixel seeded
 // with orc_pixel_seed (reference stream); mode 1: the library's counter
 // stream, one per (pixel, sample slot).
@@ -908,6 +1094,7 @@ static void render_pixel(const Scene& s, const Args& a, uint64_t seed, int mode,
   const int id = y * a.w + x;
   float rx = float(x) - float(a.w) / 2.0f, ry = float(y) - float(a.h) / 2.0f;
   vec3 d = a.dir + a.accuracy * (rx * a.right + ry * a.up);
+  const Diff d0 = ray_diff(d, a);
   vec3 dir = normalize(d);
   Ray ray{a.pos, dir};
   Surf g;
@@ -921,7 +1108,7 @@ static void render_pixel(const Scene& s, const Args& a, uint64_t seed, int mode,
     base_out = g.base;
   } else {
     g.pos = ray.o + h.tmax * ray.d;
-    hit_info(s, s.tris[h.face], ray, g);
+    hit_info(s, s.tris[h.face], ray, h.tmax, d0, g);
     bool opaque = g.opacity > 1.0f - kEps;
     vec3 keep = g.base;
     float c0 = dot(g.base, kLum);
@@ -950,10 +1137,10 @@ static void render_pixel(const Scene& s, const Args& a, uint64_t seed, int mode,
     std::vector<LSample> samples;
     for (int T = 0; T < spp_i; ++T) {
       if (mode == 0) {
-        indirect_path(s, g, a.pos, a.maxd, mt, samples);
+        indirect_path(s, g, a.pos, d0, a.maxd, mt, samples);
       } else {
         CtrGen c{rmn_rng(seed, (uint32_t)id, (uint32_t)(spp_d + T))};
-        indirect_path(s, g, a.pos, a.maxd, c, samples);
+        indirect_path(s, g, a.pos, d0, a.maxd, c, samples);
       }
     }
     nsamples = (int)samples.size();
@@ -1084,9 +1271,23 @@ void* port_scene_create(const orc_scene_in* in) {
     s->nrm[i] = in->normals ? vec3(in->normals[3 * i], in->normals[3 * i + 1], in->normals[3 * i + 2]) : vec3(0.0f);
     s->uv[i] = in->uvs ? vec2(in->uvs[2 * i], in->uvs[2 * i + 1]) : vec2(0.0f);
   }
+  s->images.resize(in->num_textures > 0 ? in->num_textures : 0);
+  for (int i = 0; i < in->num_textures; ++i) {
+    Image& im = s->images[i];
+    im.w = in->tex_dims[3 * i];
+    im.h = in->tex_dims[3 * i + 1];
+    im.ch = in->tex_dims[3 * i + 2];
+    im.lv[0].assign(in->tex_data[i], in->tex_data[i] + (size_t)im.w * im.h * im.ch);
+    im.mips();
+  }
   for (int m = 0; m < in->num_materials; ++m) {
     const float* p = in->materials + ORC_MAT_FLOATS * m;
     Mat q;
+    for (int k = 0; k < 4; ++k) {
+      int t = in->mat_tex ? in->mat_tex[4 * m + k] : -1;
+      q.tex[k] = t >= 0 ? &s->images[t] : nullptr;
+    }
+    q.transparent = q.tex[0] && q.tex[0]->has_transparent_part();
     q.base = vec3(p[0], p[1], p[2]); q.has_base = p[3] != 0.0f;
     q.emis = vec3(p[4], p[5], p[6]); q.has_emis = p[7] != 0.0f;
     q.roughness = p[8]; q.metallic = p[9]; q.has_surf = p[10] != 0.0f;
@@ -1110,16 +1311,23 @@ void* port_scene_create(const orc_scene_in* in) {
       s->tris.push_back(f);
     }
     const Mat& M = s->mats[mat];
-    if (!M.has_emis) continue;
-    // checkLightObject: the average emissive colour of a constant texel over
-    // the 8x8 grid is 64 equal adds divided by 64.
+    if (!M.emissive()) continue;
+    // checkLightObject, src/model.cpp:44-82, with getAverageEmissiveColor
+    // (:23-42): the emission averaged over an 8x8 grid of barycentric points.
     Light lo;
     vec3 col(0.0f);
     std::vector<float> fw;
     for (size_t j = off; j < s->tris.size(); ++j) {
       const Tri& f = s->tris[j];
       vec3 avg(0.0f);
-      for (int i = 0; i < 64; ++i) avg += M.emission();
+      for (int gi = 0; gi < 8; ++gi)
+        for (int gj = 0; gj < 8; ++gj) {
+          float ga = static_cast<float>(gi) / 7.0f, gb = static_cast<float>(gj) / 7.0f;
+          if (ga + gb > 1.0f) { ga = 1.0f - ga; gb = 1.0f - gb; }
+          float gc = 1.0f - ga - gb;
+          vec2 uv = ga * s->uv[f.vid[0]] + gb * s->uv[f.vid[1]] + gc * s->uv[f.vid[2]];
+          avg += M.emission(uv[0], uv[1], NAN);
+        }
       avg = avg / static_cast<float>(64);
       float cl = dot(avg, kLum), area = length(cross(f.v[1] - f.v[0], f.v[2] - f.v[0])) / 2.0f;
       if (cl < kEps || area < kEps) continue;
@@ -1196,7 +1404,8 @@ void port_trace_closest(void* h, const float* rays, int64_t n, int32_t* face, fl
     const float* r = rays + 8 * i;
     Ray ray{vec3(r[0], r[1], r[2]), vec3(r[4], r[5], r[6])};
     Hit hh{r[3], r[7], -1};
-    traverse(s, ray, hh, nullptr);
+    if (r[3] == kEps && std::isinf(r[7]) && r[7] > 0) hh = closest(s, ray);  // Model::rayHit, alpha test included
+    else traverse(s, ray, hh, nullptr);
     if (hh.face < 0) {
       face[i] = -1; t[i] = hh.tmax; bc[3 * i] = bc[3 * i + 1] = bc[3 * i + 2] = 0.0f;
       return;

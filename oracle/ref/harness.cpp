@@ -9,12 +9,20 @@
 // (oracle/port) against the reference itself.
 //
 // What the harness supplies in place of the reference's asset layer:
-//  * src/material.cpp is replaced by the definitions below: a material holds
+//  * libref.so: src/material.cpp is replaced by the definitions below
+//    (ORC_REAL_MATERIAL undefined): a material holds
 //    at most one constant float texel per texture slot (diffuse, specular,
 //    emissive), stored as four floats in the slot's level-0 byte vector;
 //    getDiffuseColor / getEmissiveColor / getSurfaceData return that texel
 //    (with getSurfaceData's clamps) and getNormal returns the zero texel of a
 //    missing normal map, as src/material.cpp:349-383 does without textures.
+//  * libref_tex.so (ORC_REAL_MATERIAL): the reference's own src/material.cpp
+//    is linked; texture slots receive the scene's 8-bit textures (what
+//    Material::loadImageFromFile leaves in ImageData after a DDS load),
+//    ImageData::generateMipmaps builds their mip chains and
+//    hasFullyTransparentPart is set as Material::loadMaterialProperties
+//    sets it. A constant texel cannot be expressed there, so a material
+//    record that asks for one without a texture in that slot is refused.
 //  * Model's public members are filled directly (what Model::Model does
 //    through assimp, src/model.cpp:172-215), including the per-mesh
 //    checkLightObject call, SkyBox::Init and BVH::build.
@@ -62,6 +70,7 @@
 
 #include "../port/oracle_api.h"
 
+#ifndef ORC_REAL_MATERIAL
 // ---------------------------------------------------------------------------
 // src/material.cpp replacement (constant texels).
 static void put_texel(ImageData& img, float a, float b, float c, float d) {
@@ -109,6 +118,7 @@ void Material::getSurfaceData(float, float, float& r, float& m) const {
   m = std::min(t[2], 0.99f);
   r = std::max(t[1], 1e-3f);
 }
+#endif
 
 // ---------------------------------------------------------------------------
 // libpng entry points: PNG output is not on the checked path.
@@ -175,10 +185,35 @@ void* ref_scene_create(const orc_scene_in* in) {
     const float* p = in->materials + ORC_MAT_FLOATS * i;
     Material& q = m->materials[i];
     q.id = i;
+#ifdef ORC_REAL_MATERIAL
+    static const int slot[4] = {aiTextureType_DIFFUSE, aiTextureType_SPECULAR, aiTextureType_EMISSIVE,
+                                aiTextureType_NORMALS};
+    static const int flag[4] = {3, 10, 7, -1};
+    for (int k = 0; k < 4; ++k) {
+      int t = in->mat_tex ? in->mat_tex[4 * i + k] : -1;
+      if (t < 0) {
+        if (flag[k] >= 0 && p[flag[k]] != 0.0f) {
+          std::cerr << "libref_tex: material " << i << " asks for a constant texel" << std::endl;
+          delete m;
+          return nullptr;
+        }
+        continue;
+      }
+      ImageData& img = q.texture[slot[k]];
+      img.width = in->tex_dims[3 * t];
+      img.height = in->tex_dims[3 * t + 1];
+      img.channels = in->tex_dims[3 * t + 2];
+      img.data[0].assign(in->tex_data[t], in->tex_data[t] + (size_t)img.width * img.height * img.channels);
+      img.generateMipmaps();
+    }
+    if (q.texture[aiTextureType_DIFFUSE].hasTransparentPart()) q.hasFullyTransparentPart = true;
+    q.roughness = p[8];
+#else
     if (p[3] != 0.0f) put_texel(q.texture[aiTextureType_DIFFUSE], p[0], p[1], p[2], 1.0f);
     if (p[7] != 0.0f) put_texel(q.texture[aiTextureType_EMISSIVE], p[4], p[5], p[6], 1.0f);
     if (p[10] != 0.0f) put_texel(q.texture[aiTextureType_SPECULAR], 0.0f, p[8], p[9], 1.0f);
     else q.roughness = p[8];
+#endif
     q.opacity = p[11];
     q.ior = p[12];
     q.transmittingColor = vec3(p[13], p[14], p[15]);

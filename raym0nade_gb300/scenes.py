@@ -66,6 +66,12 @@ class Scene:
     materials: np.ndarray            # (nmat, 16) float32
     env: np.ndarray | None = None    # (h, w, 3) float32, row 0 = zenith
     name: str = "scene"
+    # 8-bit RGBA textures, (h, w, 4) uint8 each, row 0 = the image's top row
+    # (texture v = 1); mat_tex (nmat, 4) int32: per material the diffuse,
+    # specular, emissive and normal-map texture index, -1 for none (the
+    # record's constant texel, or none).
+    textures: list | None = None
+    mat_tex: np.ndarray | None = None
 
     @property
     def num_triangles(self) -> int:
@@ -77,6 +83,21 @@ class Scene:
         assert self.indices.dtype == np.int32 and self.indices.shape[1] == 3
         assert self.mesh_first[0] == 0 and self.mesh_first[-1] == self.indices.shape[0]
         assert self.materials.dtype == np.float32 and self.materials.shape[1] == MAT_FLOATS
+        if self.mat_tex is not None:
+            n = len(self.textures or [])
+            assert self.mat_tex.dtype == np.int32 and self.mat_tex.shape == (self.materials.shape[0], 4)
+            assert ((self.mat_tex >= -1) & (self.mat_tex < n)).all()
+            for t in self.textures or []:
+                assert t.dtype == np.uint8 and t.ndim == 3 and t.shape[2] == 4
+
+    def texture_arrays(self):
+        """(dims (n, 3) int32 of width, height, channels; contiguous byte
+        arrays; mat_tex) for a C scene description, or Nones."""
+        if self.mat_tex is None:
+            return None, [], None
+        texs = [np.ascontiguousarray(t, np.uint8) for t in self.textures or []]
+        dims = np.array([[t.shape[1], t.shape[0], t.shape[2]] for t in texs], np.int32).reshape(-1, 3)
+        return dims, texs, np.ascontiguousarray(self.mat_tex, np.int32)
 
 
 @dataclass
@@ -425,6 +446,156 @@ def heightfield_camera(width=1920, height=1080, spp=256, extent=200.0) -> Camera
     up_img /= np.linalg.norm(up_img)
     acc = math.tan(math.radians(30.0)) / (width / 2.0)
     return Camera(tuple(eye), tuple(f), tuple(up_img), tuple(r), acc, width, height, spp, max_depth=16)
+
+
+def _tex_material(roughness=0.8, opacity=1.0, ior=1.0, transmitting=(0.0, 0.0, 0.0)) -> np.ndarray:
+    """A material record whose colour slots all come from textures (or their
+    defaults: white diffuse, no emission, roughness from the record)."""
+    m = material(roughness=roughness, opacity=opacity, ior=ior, transmitting=transmitting)
+    m[3] = 0.0
+    return m
+
+
+def _rgba(rgb, alpha=None) -> np.ndarray:
+    rgb = np.clip(np.rint(np.asarray(rgb) * 255.0), 0, 255).astype(np.uint8)
+    a = np.full(rgb.shape[:2] + (1,), 255, np.uint8) if alpha is None else \
+        np.clip(np.rint(np.asarray(alpha) * 255.0), 0, 255).astype(np.uint8)[..., None]
+    return np.concatenate([rgb, a], -1)
+
+
+def texture_checker(w, h, cells, seed) -> np.ndarray:
+    """RGBA8 checkerboard of two seeded colours with per-texel noise."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.15, 0.95, (2, 3))
+    y, x = np.mgrid[0:h, 0:w]
+    k = ((x * cells // w) + (y * cells // h)) % 2
+    rgb = c[k] * rng.uniform(0.85, 1.0, (h, w, 1))
+    return _rgba(rgb)
+
+
+def texture_normals(w, h, seed, amp=0.35) -> np.ndarray:
+    """RGBA8 tangent-space normal map (n * 0.5 + 0.5) of a sum of sines."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w] / np.array([h, w])[:, None, None]
+    gx = np.zeros((h, w))
+    gy = np.zeros((h, w))
+    for _ in range(3):
+        fx, fy = rng.integers(1, 6, 2)
+        ph = rng.uniform(0, 2 * np.pi)
+        arg = 2 * np.pi * (fx * x + fy * y) + ph
+        gx += amp * fx * np.cos(arg) / 3
+        gy += amp * fy * np.cos(arg) / 3
+    n = np.stack([-gx, -gy, np.ones_like(gx)], -1)
+    n /= np.linalg.norm(n, axis=-1, keepdims=True)
+    return _rgba(n * 0.5 + 0.5)
+
+
+def texture_surface(w, h, seed) -> np.ndarray:
+    """RGBA8 specular texture: G roughness in [0.05, 0.9] in smooth bands,
+    B metallic 0 or 0.8 in blocks (Material::getSurfaceData's channels)."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w]
+    rough = 0.05 + 0.85 * (0.5 + 0.5 * np.sin(2 * np.pi * (x / w * 2 + y / h) + rng.uniform(0, 6)))
+    metal = np.where(((x * 4 // w) + (y * 4 // h)) % 3 == 0, 0.8, 0.0)
+    return _rgba(np.stack([np.zeros_like(rough), rough, metal], -1))
+
+
+def texture_cutout(w, h, seed, holes=5) -> np.ndarray:
+    """RGBA8 leaf-like cutout: seeded colour, alpha 0 inside ``holes`` discs
+    (the alpha test cuts them away) and 0.5 in a ring around each."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:h, 0:w] + 0.5
+    alpha = np.ones((h, w))
+    for _ in range(holes):
+        cx, cy = rng.uniform(0, w), rng.uniform(0, h)
+        r = rng.uniform(0.08, 0.2) * w
+        d = np.hypot(x - cx, y - cy)
+        alpha = np.where(d < 1.3 * r, np.minimum(alpha, 0.5), alpha)
+        alpha = np.where(d < r, 0.0, alpha)
+    rgb = rng.uniform(0.2, 0.8, 3) * rng.uniform(0.8, 1.0, (h, w, 1))
+    return _rgba(rgb, alpha)
+
+
+def texture_emissive(w, h, seed) -> np.ndarray:
+    """RGBA8 emissive stripes of seeded colours."""
+    rng = np.random.default_rng(seed)
+    c = rng.uniform(0.3, 1.0, (4, 3))
+    x = np.arange(w)
+    rgb = np.broadcast_to(c[(x * 4 // w) % 4][None], (h, w, 3))
+    return _rgba(rgb)
+
+
+def textured_room(seed: int = 5, sky: bool = True) -> Scene:
+    """A room open to the sky exercising the reference's texture layer
+    (src/material.cpp, src/model.cpp:217-330):
+
+    * floor, 4 x 6, uvs tiled over [-3, 3] x [0, 9] (wrap-around): diffuse
+      checker 128x128, specular texture 64x64, normal map 64x64;
+    * back wall: diffuse 96x80 (non-power-of-two mip chain), normal map;
+    * left wall: no texture (white diffuse), roughness 0.6;
+    * right-hand emissive panel with a 32x16 striped emissive texture (a
+      light object averaged over its 8x8 grid);
+    * an alpha-tested fence (cutout discs) across the room, and a stack of
+      ten cutout layers 1 cm apart whose holes line up, past the eight
+      retries of Model::rayHit;
+    * lit by a 64x32 sky without sun (``sky``), else by the panel alone
+      (light-object sampling).
+    """
+    rng = np.random.default_rng(seed)
+    texs = [texture_checker(128, 128, 8, seed + 1), texture_surface(64, 64, seed + 2),
+            texture_normals(64, 64, seed + 3), texture_checker(96, 80, 6, seed + 4),
+            texture_normals(32, 32, seed + 5, amp=0.6), texture_emissive(32, 16, seed + 6),
+            texture_cutout(64, 64, seed + 7)]
+    stack = np.zeros((16, 16, 4), np.uint8)
+    stack[..., :3] = np.array([200, 120, 60], np.uint8)
+    stack[..., 3] = 255
+    stack[4:12, 4:12, 3] = 0
+    texs.append(stack)
+    mats = [_tex_material(0.8), _tex_material(0.7), _tex_material(0.6), _tex_material(0.8),
+            _tex_material(0.5), _tex_material(0.7)]
+    mat_tex = np.array([[0, 1, -1, 2],     # floor
+                        [3, -1, -1, 4],    # back wall
+                        [-1, -1, -1, -1],  # left wall
+                        [-1, -1, 5, -1],   # emissive panel
+                        [6, -1, -1, -1],   # fence
+                        [7, -1, -1, -1]],  # stacked layers
+                       np.int32)
+    meshes = []
+
+    def quad(a, b, c, d, uv, mat):
+        q, n = _quad(a, b, c, d)
+        ua, ub, uc, ud = uv
+        meshes.append((q, n, np.array([ua, ub, uc, ua, uc, ud], np.float32), mat))
+
+    quad((-2, 0, 0), (-2, 0, 6), (2, 0, 6), (2, 0, 0), [(-3, 0), (-3, 9), (3, 9), (3, 0)], 0)
+    quad((-2, 0, 6), (-2, 3, 6), (2, 3, 6), (2, 0, 6), [(0, 0), (0, 1), (1, 1), (1, 0)], 1)
+    quad((-2, 0, 0), (-2, 3, 0), (-2, 3, 6), (-2, 0, 6), [(0, 0), (0, 1), (1, 1), (1, 0)], 2)
+    quad((1.9, 0.5, 2), (1.9, 0.5, 4), (1.9, 2.0, 4), (1.9, 2.0, 2), [(0, 0), (1, 0), (1, 1), (0, 1)], 3)
+    quad((-1.5, 0, 2.5), (-1.5, 1.5, 2.5), (0.5, 1.5, 2.5), (0.5, 0, 2.5), [(0, 0), (0, 1.5), (2, 1.5), (2, 0)], 4)
+    jitter = rng.uniform(-1e-3, 1e-3, 10)
+    for k in range(10):
+        z = 1.0 + 0.01 * k + jitter[k] * 0.1
+        quad((0.6, 0.2, z), (0.6, 0.6, z), (1.0, 0.6, z), (1.0, 0.2, z), [(0, 0), (0, 1), (1, 1), (1, 0)], 5)
+    sc = _assemble(meshes, mats, env=sky_env(64, 32, sun_radiance=0.0) if sky else None, name="textured_room")
+    sc.textures = texs
+    sc.mat_tex = mat_tex
+    sc.check()
+    return sc
+
+
+def textured_camera(width=96, height=64, spp=16, max_depth=16, p_direct=0.7) -> Camera:
+    """Inside the room at (0.3, 0.9, -0.4) looking at (0.2, 0.5, 4) across the
+    floor, 70 degree field of view across the width."""
+    eye = np.array([0.3, 0.9, -0.4])
+    f = np.array([0.2, 0.5, 4.0]) - eye
+    f /= np.linalg.norm(f)
+    r = np.cross(f, [0.0, 1.0, 0.0])
+    r /= np.linalg.norm(r)
+    up_img = np.cross(f, r)
+    up_img /= np.linalg.norm(up_img)
+    acc = math.tan(math.radians(35.0)) / (width / 2.0)
+    return Camera(tuple(eye), tuple(f), tuple(up_img), tuple(r), acc, width, height, spp, p_direct,
+                  max_depth=max_depth)
 
 
 @dataclass

@@ -30,3 +30,14 @@ def ref():
         else:
             pytest.skip("the reference checkout is not on this machine; parity is carried by tests/golden")
     return bindings.OracleLib("ref")
+
+
+@pytest.fixture(scope="session")
+def ref_tex():
+    from oracle import bindings
+    if not bindings.have_ref_tex():
+        if os.path.isdir(os.path.join(bindings.REFERENCE_DIR, "src")):
+            bindings.build(with_reference=True)
+        else:
+            pytest.skip("the reference checkout is not on this machine; parity is carried by tests/golden")
+    return bindings.OracleLib("ref_tex")

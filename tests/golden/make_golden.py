@@ -17,6 +17,12 @@ Fixtures (numpy .npz, compressed):
   render_glass.npz   20 x 20 render of the Cornell box with a glass box and a
                      half-opaque box, 8 spp (refraction, media, Fresnel split).
                      ``--glass`` writes this fixture alone.
+  render_textured.npz  48 x 32 render of the textured room (diffuse,
+                     specular, emissive and normal-map textures, mip chains,
+                     alpha-tested cutouts), 16 spp, from the reference built
+                     with its own src/material.cpp (oracle/_ref/libref_tex.so);
+                     plus 4,096 closest-hit and 4,096 shadow rays through the
+                     room (alpha-test retries). ``--textured`` writes it alone.
   post.npz           Photo::shade(Full) + gammaCorrection of render records,
                      and Photo::FXAA of a 96 x 64 image with hard edges.
   cornell_4096spp.npz  the converged reference image of the Cornell workload
@@ -42,14 +48,38 @@ def scene_arrays(s):
              mesh_material=s.mesh_material, materials=s.materials)
     if s.env is not None:
         d["env"] = s.env
+    if s.mat_tex is not None:
+        d["mat_tex"] = s.mat_tex
+        for i, t in enumerate(s.textures):
+            d["tex%d" % i] = t
     return d
 
 
 def scene_from(z, prefix=""):
     g = lambda k: z[prefix + k]
     env = z[prefix + "env"] if (prefix + "env") in z else None
-    return scenes.Scene(g("positions"), g("normals"), g("uvs"), g("indices"), g("mesh_first"), g("mesh_material"),
-                        g("materials"), env)
+    sc = scenes.Scene(g("positions"), g("normals"), g("uvs"), g("indices"), g("mesh_first"), g("mesh_material"),
+                      g("materials"), env)
+    if (prefix + "mat_tex") in z:
+        sc.mat_tex = g("mat_tex")
+        n = 0
+        while (prefix + "tex%d" % n) in z:
+            n += 1
+        sc.textures = [g("tex%d" % i) for i in range(n)]
+    return sc
+
+
+def room_rays(n, seed, shadow=False):
+    """Rays through the textured room: origins in its volume, uniform
+    directions; shadow rays aim U(0, 6) ahead."""
+    rng = np.random.default_rng(seed)
+    r = np.empty((n, 8), np.float32)
+    r[:, 0:3] = rng.uniform((-1.9, 0.05, 0.1), (1.8, 2.9, 5.9), (n, 3))
+    r[:, 3] = np.float32(1e-4)
+    d = rng.standard_normal((n, 3))
+    r[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    r[:, 7] = rng.uniform(0.0, 6.0, n) if shadow else np.inf
+    return r
 
 
 def reachable(ranges):
@@ -113,6 +143,7 @@ def main():
                         records=hrec)
 
     glass(R)
+    textured()
 
     rgb_lin = R.compose(rec, 1.0, gamma=False)
     rgb = R.compose(rec, 1.0, gamma=True)
@@ -140,6 +171,21 @@ def glass(R=None):
                         records=rec)
 
 
+def textured():
+    bindings.build(with_reference=True)
+    T = bindings.OracleLib("ref_tex")
+    room = scenes.textured_room()
+    cam = scenes.textured_camera(48, 32, 16)
+    ts = T.scene(room)
+    rec = ts.render(cam, seed=515)
+    rays = room_rays(4096, 516)
+    srays = room_rays(4096, 517, shadow=True)
+    face, t, bc = ts.trace_closest(rays)
+    occ = ts.trace_shadow(srays)
+    np.savez_compressed(os.path.join(HERE, "render_textured.npz"), **scene_arrays(room), args=cam.packed(),
+                        seed=515, records=rec, rays=rays, face=face, t=t, bary=bc, shadow_rays=srays, occluded=occ)
+
+
 def converged():
     bindings.build(with_reference=True)
     R = bindings.OracleLib("ref")
@@ -158,5 +204,8 @@ if __name__ == "__main__":
     elif "--glass" in sys.argv:
         glass()
         print("glass fixture written to", HERE)
+    elif "--textured" in sys.argv:
+        textured()
+        print("textured fixture written to", HERE)
     else:
         main()

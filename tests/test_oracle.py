@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 from raym0nade_gb300 import scenes
-from tests.golden.make_golden import edge_rays, reachable, scene_from, tie_soup
+from tests.golden.make_golden import edge_rays, reachable, room_rays, scene_from, tie_soup
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -37,7 +37,7 @@ def test_golden_trace(port):
     assert same(ps.trace_shadow(z["shadow_rays"]), z["occluded"])
 
 
-@pytest.mark.parametrize("name", ["render_cornell", "render_sky", "render_glass"])
+@pytest.mark.parametrize("name", ["render_cornell", "render_sky", "render_glass", "render_textured"])
 def test_golden_render(port, name):
     z = np.load(os.path.join(GOLDEN, name + ".npz"))
     a = z["args"]
@@ -46,6 +46,14 @@ def test_golden_render(port, name):
     rec = port.scene(scene_from(z)).render(cam, seed=int(z["seed"]), mode=0)
     ref = z["records"]
     assert same(rec[..., :38], ref[..., :38])
+
+
+def test_golden_textured_trace(port):
+    z = np.load(os.path.join(GOLDEN, "render_textured.npz"))
+    ps = port.scene(scene_from(z))
+    face, t, bc = ps.trace_closest(z["rays"])
+    assert same(face, z["face"]) and same(t, z["t"]) and same(bc, z["bary"])
+    assert same(ps.trace_shadow(z["shadow_rays"]), z["occluded"])
 
 
 def test_golden_post(port):
@@ -138,3 +146,42 @@ def test_post_matches_reference(port, ref):
     rec = rng.random((500, 40)).astype(np.float32)
     for g in (False, True):
         assert same(port.compose(rec, 1.3, gamma=g), ref.compose(rec, 1.3, gamma=g))
+
+
+# ------------------------------------------------ textures (f2) -----------
+def test_textured_lights_match_reference(port, ref_tex):
+    for sky in (True, False):
+        room = scenes.textured_room(sky=sky)
+        assert same(port.scene(room).lights(), ref_tex.scene(room).lights())
+
+
+def test_textured_trace_matches_reference(port, ref_tex):
+    room = scenes.textured_room()
+    ps, rs = port.scene(room), ref_tex.scene(room)
+    rays = room_rays(20000, 41)
+    a, b = ps.trace_closest(rays), rs.trace_closest(rays)
+    assert all(same(x, y) for x, y in zip(a, b))
+    srays = room_rays(20000, 42, shadow=True)
+    assert same(ps.trace_shadow(srays), rs.trace_shadow(srays))
+    # the cutouts matter: without the alpha test (a t_min other than eps
+    # takes the bare BVH query) some rays stop at a cut-away texel instead
+    raw = rays.copy()
+    raw[:, 3] = np.float32(1.5e-4)
+    assert (ps.trace_closest(raw)[0] != a[0]).sum() > 20
+
+
+@pytest.mark.parametrize("sky,spp,p_direct", [(True, 16, 0.7), (False, 12, 0.7), (True, 6, 0.0)])
+def test_render_textured_matches_reference(port, ref_tex, sky, spp, p_direct):
+    room = scenes.textured_room(sky=sky)
+    cam = scenes.textured_camera(64, 40, spp, p_direct=p_direct)
+    a = port.scene(room).render(cam, seed=31)
+    b = ref_tex.scene(room).render(cam, seed=31)
+    assert same(a[..., :38], b[..., :38])
+    assert set(np.unique(a[..., 36]).astype(int)) == set(range(6))
+
+
+def test_ref_tex_refuses_constant_texels(ref_tex):
+    room = scenes.textured_room()
+    room.materials[2, 3] = 1.0  # a constant diffuse texel without a texture
+    with pytest.raises(ValueError):
+        ref_tex.scene(room)
