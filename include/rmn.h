@@ -48,11 +48,10 @@ typedef enum rmn_status {
   RMN_ERR_INTERNAL = 6
 } rmn_status;
 
-/* Constant-texel material, 16 floats. The reference's Material
- * (include/material.h:26-50) samples textures; a material here holds at most
- * one constant texel per slot, resolved exactly as Material::getDiffuseColor,
- * getEmissiveColor and getSurfaceData resolve a texel (src/material.cpp:
- * 349-383). */
+/* Material record, 16 floats: per slot a constant texel, resolved exactly
+ * as Material::getDiffuseColor, getEmissiveColor and getSurfaceData resolve
+ * a texel (src/material.cpp:349-383), unless rmn_scene_desc gives the slot a
+ * texture (rmn_texture), which then takes precedence. */
 typedef struct rmn_material {
   float base_color[3];   /* diffuse texel, linear RGB */
   float has_base;        /* 0: no diffuse texture -> white */
@@ -65,6 +64,25 @@ typedef struct rmn_material {
   float ior;
   float transmitting_color[3];
 } rmn_material;
+
+/* 8-bit texture as the reference's DDS loader leaves it in ImageData
+ * (Material::loadImageFromDDS, src/material.cpp:61-95): width x height
+ * texels of `channels` bytes, row-major, row 0 = the image's top row
+ * (texture v = 1). channels must be 4 (RGBA): the reference reads every
+ * diffuse, specular and emissive lookup with a 4-byte stride and normal-map
+ * lookups with a 3-byte stride whatever the channel count
+ * (get_bilinear, src/material.cpp:48-80). The library builds the mip chain
+ * of ImageData::generateMipmaps (src/material.cpp:107-129). */
+typedef struct rmn_texture {
+  int32_t width, height, channels;
+  const uint8_t* texels;
+} rmn_texture;
+
+/* Texture slots of material_textures (4 per material). */
+#define RMN_TEX_DIFFUSE 0   /* aiTextureType_DIFFUSE: base colour (gamma 2.2) and alpha test */
+#define RMN_TEX_SPECULAR 1  /* aiTextureType_SPECULAR: G roughness, B metallic, level 0 */
+#define RMN_TEX_EMISSIVE 2  /* aiTextureType_EMISSIVE: emission (gamma 2.2); makes the mesh a light object */
+#define RMN_TEX_NORMALS 3   /* aiTextureType_NORMALS: tangent-space normal map */
 
 /* Scene arrays; what Model::Model builds from an assimp scene
  * (src/model.cpp:84-123,172-215). Triangles are grouped in meshes with one
@@ -84,6 +102,15 @@ typedef struct rmn_scene_desc {
   const rmn_material* materials;
   int32_t env_width, env_height;  /* lat-long sky (SkyBox, include/component.h:56-67) */
   const float* env_rgb;           /* 3 per texel, row 0 = zenith; NULL: no sky */
+  /* Textures (zero / NULL for an untextured scene). material_textures holds
+   * 4 texture indices per material (RMN_TEX_*), -1 for none. A diffuse
+   * texture with a texel of alpha < 255 makes its material alpha-tested
+   * (Material::hasFullyTransparentPart; TransparentTest, src/model.cpp:
+   * 217-230). Texels are copied; the caller's arrays may be freed after
+   * rmn_scene_create returns. */
+  int32_t num_textures;
+  const rmn_texture* textures;
+  const int32_t* material_textures;
 } rmn_scene_desc;
 
 typedef struct rmn_scene rmn_scene;
@@ -158,7 +185,9 @@ const char* rmn_last_error(void);
 const char* rmn_version(void);
 
 /* Scene construction: replaces Model::Model's geometry/BVH/light/sky steps
- * (src/model.cpp:172-215). */
+ * (src/model.cpp:172-215) and Material's texture loading and mip chains
+ * (src/material.cpp:107-129, 291-302). The arrays of rmn_scene_desc are read
+ * on the host (host memory). */
 rmn_status rmn_scene_create(const rmn_scene_desc* desc, rmn_scene** out);
 rmn_status rmn_scene_destroy(rmn_scene* scene);
 rmn_status rmn_scene_info_get(const rmn_scene* scene, rmn_scene_info* info);

@@ -25,7 +25,12 @@ class SceneDesc(C.Structure):
                 ("uvs", C.c_void_p), ("num_triangles", C.c_int32), ("indices", C.c_void_p),
                 ("num_meshes", C.c_int32), ("mesh_first", C.c_void_p), ("mesh_material", C.c_void_p),
                 ("num_materials", C.c_int32), ("materials", C.c_void_p), ("env_width", C.c_int32),
-                ("env_height", C.c_int32), ("env_rgb", C.c_void_p)]
+                ("env_height", C.c_int32), ("env_rgb", C.c_void_p), ("num_textures", C.c_int32),
+                ("textures", C.c_void_p), ("material_textures", C.c_void_p)]
+
+
+class Texture(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("channels", C.c_int32), ("texels", C.c_void_p)]
 
 
 class SceneInfo(C.Structure):

@@ -79,9 +79,14 @@ class Model:
         env = None if scene.env is None else np.ascontiguousarray(scene.env, np.float32)
         self._keep.append(env)
         p, n, u, i, mf, mm, mat = self._keep[:7]
+        _, texs, mtex = scene.texture_arrays()
+        tarr = (_lib.Texture * max(len(texs), 1))(*[_lib.Texture(t.shape[1], t.shape[0], t.shape[2], t.ctypes.data)
+                                                     for t in texs])
+        self._keep += [texs, mtex, tarr]
         d = _lib.SceneDesc(p.shape[0], _ptr(p), _ptr(n), _ptr(u), i.shape[0], _ptr(i), mm.shape[0], _ptr(mf),
                            _ptr(mm), mat.shape[0], _ptr(mat), 0 if env is None else env.shape[1],
-                           0 if env is None else env.shape[0], _ptr(env))
+                           0 if env is None else env.shape[0], _ptr(env), len(texs),
+                           C.cast(tarr, C.c_void_p).value if texs else None, _ptr(mtex))
         h = C.c_void_p()
         _check(lib.rmn_scene_create(C.byref(d), C.byref(h)), "rmn_scene_create")
         self._h = h

@@ -138,7 +138,7 @@ struct PathAdj {
 
 __device__ __forceinline__ bool occluded(const DevScene& s, float3 pos, float3 dir, float aim, int* status) {
   float tm = aim + RMN_EPS;  // HitRecord(eps, aimDepth + eps), Model::rayHit_test
-  int st = trace<true, false>(s, make_tray(pos, dir), RMN_EPS, tm, aim, nullptr);
+  int st = trace<true, false, false>(s, make_tray(pos, dir), RMN_EPS, tm, aim, nullptr);  // no textured scenes here
   if (st == -2) {
     atomicExch(status, 1);
     return false;
@@ -251,7 +251,7 @@ __device__ void adjoint_slot(const AdjJob& J, int pixel, int j, GradSink& G, int
   };
   for (;;) {
     float tm = INFINITY;
-    int h = trace<false, false>(s, make_tray(o, dir), RMN_EPS, tm, 0.0f, nullptr);
+    int h = trace<false, false, false>(s, make_tray(o, dir), RMN_EPS, tm, 0.0f, nullptr);
     if (h == -2) {
       atomicExch(status, 1);
       return;

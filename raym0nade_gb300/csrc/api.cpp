@@ -337,6 +337,8 @@ rmn_status rmn_adjoint(const rmn_scene* scene, const rmn_render_args* args, cons
     return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_adjoint needs the forward's G-buffer and dropped-sample record");
   if (scene->dev.has_glass)
     return fail(RMN_ERR_UNSUPPORTED, "rmn_adjoint: transmissive and half-opaque materials are not differentiated");
+  if (scene->dev.has_tex)
+    return fail(RMN_ERR_UNSUPPORTED, "rmn_adjoint: textured materials are not differentiated");
   const rmn_render_args& a = *args;
   rmn_status r = check_args(a);
   if (r != RMN_OK) return r;

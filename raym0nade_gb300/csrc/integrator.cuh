@@ -61,6 +61,25 @@ inline Params make_params(const rmn_render_args& a, bool glass = false) {
   return p;
 }
 
+// The camera ray's unnormalised direction for pixel (x, y) (renderPixel,
+// src/render.cpp:463-467; no jitter).
+__device__ __forceinline__ float3 pixel_dir(const Params& p, int x, int y) {
+  float rx = float(x) - float(p.W) / 2.0f, ry = float(y) - float(p.H) / 2.0f;
+  return p.dir + p.acc * (rx * p.right + ry * p.up);
+}
+
+// initRayDiff, src/render.cpp:439-446: the camera ray's differential.
+__device__ __forceinline__ RayDiff init_ray_diff(const Params& p, float3 d) {
+  RayDiff r;
+  r.dPdx = f3(0.0f);
+  r.dPdy = f3(0.0f);
+  const float3 ddx = p.acc * p.right, ddy = p.acc * p.up;
+  float dd = dot3(d, d), dx = dot3(d, ddx), dy = dot3(d, ddy);
+  r.dDdx = (dd * ddx - d * dx) / (sqrtf(dd) * dd);
+  r.dDdy = (dd * ddy - d * dy) / (sqrtf(dd) * dd);
+  return r;
+}
+
 // renderPixel's demodulation tweak, src/render.cpp:492-495: a faint red is
 // added to black or grey base colours (double-precision literals as there).
 __device__ __forceinline__ float3 tweak_base(float3 b) {

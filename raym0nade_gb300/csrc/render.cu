@@ -116,7 +116,20 @@ struct Pool {
   int* mn;         // count
   int* mid;        // RMN_MEDIA per worker: material id (air -1)
   float4* mval;    // RMN_MEDIA per worker: ior, absorb
+  // the differential of the path's current ray (scenes with textures):
+  // 3 per worker, (dPdx, dPdy.x), (dPdy.yz, dDdx.xy), (dDdx.z, dDdy)
+  float4* rdiff;
 };
+
+__device__ __forceinline__ RayDiff load_diff(const Pool& P, int w) {
+  const float4 a = P.rdiff[3 * (size_t)w], b = P.rdiff[3 * (size_t)w + 1], c = P.rdiff[3 * (size_t)w + 2];
+  return {f3(a.x, a.y, a.z), f3(a.w, b.x, b.y), f3(b.z, b.w, c.x), f3(c.y, c.z, c.w)};
+}
+__device__ __forceinline__ void store_diff(const Pool& P, int w, const RayDiff& d) {
+  P.rdiff[3 * (size_t)w] = make_float4(d.dPdx.x, d.dPdx.y, d.dPdx.z, d.dPdy.x);
+  P.rdiff[3 * (size_t)w + 1] = make_float4(d.dPdy.y, d.dPdy.z, d.dDdx.x, d.dDdx.y);
+  P.rdiff[3 * (size_t)w + 2] = make_float4(d.dDdx.z, d.dDdy.x, d.dDdy.y, d.dDdy.z);
+}
 
 // Partial accumulator of one unit: 7 float4.
 //   [0] Dd  [1] Ds  [2] Id without the largest sample  [3] Is likewise
@@ -156,8 +169,9 @@ __device__ __forceinline__ int find_job_unit(const Job* jobs, int n, long long v
 // shapeN[3] surfN[3] roughness metallic opacity eta material-id entering. The base
 // colour is stored untweaked; the integrator applies renderPixel's tweak for
 // its own use and finalize writes the tweaked colour back where the
-// reference leaves it.
-template <bool COUNT>
+// reference leaves it. TEX: the batch has textured scenes (a separate build,
+// so untextured batches keep the lean kernel).
+template <bool COUNT, bool TEX>
 __global__ void __launch_bounds__(128) primary_kernel(const Job* __restrict__ jobs, int njobs, int total_pix,
                                                       int* status, Counters* ctr) {
   int gi = blockIdx.x * blockDim.x + threadIdx.x;
@@ -167,20 +181,24 @@ __global__ void __launch_bounds__(128) primary_kernel(const Job* __restrict__ jo
   const Params& p = J.p;
   int i = gi - J.pix_begin;
   int x = i % p.W, y = i / p.W;
-  float rx = float(x) - float(p.W) / 2.0f, ry = float(y) - float(p.H) / 2.0f;
-  float3 d = p.dir + p.acc * (rx * p.right + ry * p.up);
+  float3 d = pixel_dir(p, x, y);
   float3 D = norm3(d);
   TRay r = make_tray(p.pos, D);
   float tmax = INFINITY;
   TraceCounters tc = {0, 0, 0, 0, 0};
-  int h = trace<false, COUNT>(s, r, RMN_EPS, tmax, 0.0f, &tc);
+  int h = trace<false, COUNT, TEX>(s, r, RMN_EPS, tmax, 0.0f, &tc);
   if (h == -2) atomicExch(status, 1);
   Surf g = default_surf();
   if (h < 0) {
     if (s.sky_w) g.emis = sky_get(s, D);
   } else {
     g.pos = p.pos + tmax * D;
-    hit_info(s, h, D, g);
+    if (TEX && s.has_tex) {
+      float3 px, py;
+      hit_info_tex(s, h, D, tmax, init_ray_diff(p, d), g, px, py);
+    } else {
+      hit_info(s, h, D, g);
+    }
   }
   float* o = J.gbuf + (size_t)RMN_GBUFFER_FLOATS * i;
   float v[RMN_GBUFFER_FLOATS] = {g.base.x, g.base.y, g.base.z, g.emis.x, g.emis.y, g.emis.z, g.pos.x,
@@ -415,7 +433,14 @@ RMN_D int shade_hit(const Job* J, const Pool& P, int w, RmnRng& rng, int4& ph, c
   float4 pb = P.pb[w];
   Surf sf = default_surf();
   sf.pos = o + dir * res.y;
-  hit_info(s, h, dir, sf);
+  RayDiff diff;
+  float3 hpx, hpy;  // the hit point's differential (scenes with textures)
+  if (s.has_tex) {
+    diff = load_diff(P, w);
+    hit_info_tex(s, h, dir, res.y, diff, sf, hpx, hpy);
+  } else {
+    hit_info(s, h, dir, sf);
+  }
   const float ior = sf.eta;  // absolute; calcEta makes sf.eta relative
   float rf = fmaxf(pb.w, 1.0f * sf.roughness);
   sf.roughness = fmaxf(sf.roughness, rf);
@@ -497,6 +522,13 @@ RMN_D int shade_hit(const Job* J, const Pool& P, int w, RmnRng& rng, int4& ph, c
       }
       P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
       P.rd[w] = make_float4(nd.x, nd.y, nd.z, INFINITY);
+      if (s.has_tex && reflect) {  // a refracted ray keeps its differential
+        RayDiff nx;
+        nx.dPdx = hpx;
+        nx.dPdy = hpy;
+        calc_dDdxy(dir, sf.surfN, diff, nx.dDdx, nx.dDdy);
+        store_diff(P, w, nx);
+      }
       ph.z = depth + 1;
       ph.w = nee ? FL_EXCLUDE : 0;
       phase = PH_WAIT_CLOSEST;
@@ -604,9 +636,11 @@ __global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ job
 // (sampleIndirectLightFromFirstIntersection, src/render.cpp:314-423): the
 // reflection sample, or with GLASS the Fresnel split into reflection and
 // refraction, the refraction sample and the path's fresh media.
+// With textures (d0: the camera ray's differential) the path's ray
+// differential is set too: the reflection's, or d0 for a refraction.
 template <bool GLASS>
 RMN_D void first_bounce(const Pool& P, int w, const Surf& g, float3 eye, RmnRng& rng, float3& dir, float3& w0,
-                        int& f0) {
+                        int& f0, const RayDiff* d0) {
   float3 in0 = norm3(g.pos - eye);
   Surf v0 = g;
   const float ior0 = v0.eta;
@@ -618,6 +652,12 @@ RMN_D void first_bounce(const Pool& P, int w, const Surf& g, float3 eye, RmnRng&
     p_reflect = kP0Reflect + (1.0f - kP0Reflect) * F0;
   }
   if (rng.next() < p_reflect) {
+    if (d0) {
+      RayDiff nx;
+      calc_dPdxy(in0, len3(g.pos - eye), v0.shapeN, *d0, nx.dPdx, nx.dPdy);
+      calc_dDdxy(in0, v0.surfN, *d0, nx.dDdx, nx.dDdy);
+      store_diff(P, w, nx);
+    }
     sample_reflect(v0, -in0, rng, dir, w0, f0);
     w0 = w0 / p_reflect;
     if (GLASS) {
@@ -626,6 +666,7 @@ RMN_D void first_bounce(const Pool& P, int w, const Surf& g, float3 eye, RmnRng&
       store_media(P, w, med);
     }
   } else if (GLASS) {
+    if (d0) store_diff(P, w, *d0);
     sample_btdf(v0, -in0, rng, dir, w0, f0);
     w0 = w0 * (1.0f - F0);
     w0 = w0 / (1.0f - p_reflect);
@@ -639,8 +680,8 @@ RMN_D void first_bounce(const Pool& P, int w, const Surf& g, float3 eye, RmnRng&
   }
 }
 __device__ __noinline__ void first_bounce_glass(const Pool& P, int w, const Surf& g, float3 eye, RmnRng& rng,
-                                                float3& dir, float3& w0, int& f0) {
-  first_bounce<true>(P, w, g, eye, rng, dir, w0, f0);
+                                                float3& dir, float3& w0, int& f0, const RayDiff* d0) {
+  first_bounce<true>(P, w, g, eye, rng, dir, w0, f0, d0);
 }
 
 template <bool COUNT>
@@ -762,8 +803,10 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
       }
       float3 dir, w0;
       int f0 = 0;
-      if (p.glass) first_bounce_glass(P, w, g, p.pos, rng, dir, w0, f0);
-      else first_bounce<false>(P, w, g, p.pos, rng, dir, w0, f0);
+      RayDiff d0;
+      if (s.has_tex) d0 = init_ray_diff(p, pixel_dir(p, un.y % p.W, un.y / p.W));
+      if (p.glass) first_bounce_glass(P, w, g, p.pos, rng, dir, w0, f0, s.has_tex ? &d0 : nullptr);
+      else first_bounce<false>(P, w, g, p.pos, rng, dir, w0, f0, s.has_tex ? &d0 : nullptr);
       if (!any_finite3(dir)) {
         un.z++;
         continue;
@@ -799,8 +842,10 @@ constexpr int kFetchBudget = 16;  // node visits between refill checks
 // every 16 node visits, lanes whose ray is answered take the next queue
 // entries (one warp-aggregated atomic), so a warp does not wait for its
 // longest ray. The rays of a batch belong to different scenes; each lane
-// traverses its own job's BVH.
-template <bool SHADOW, bool COUNT>
+// traverses its own job's BVH. ALPHA: the batch has scenes with alpha-tested
+// materials, whose queries retry past cut-away texels (a separate build, so
+// the common case keeps its register budget).
+template <bool SHADOW, bool COUNT, bool ALPHA>
 __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
                                                      int par, int* status, Counters* ctr) {
   const int lane = threadIdx.x & 31;
@@ -815,6 +860,9 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
   int w = 0;
   TRay r;
   float tmin = 0.0f, aim = 0.0f;
+  int searches = 0;  // alpha-test searches finished for the lane's ray
+  int jb = 0;        // the lane's job
+  bool alpha = false;
   // the deferred-child stack in shared memory (launched with 128 threads)
   __shared__ int2 sstack[RMN_STACK * 128];
   TravT<SharedStack> t;
@@ -834,7 +882,9 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
           w = q[i];
           const int wk = (!SHADOW || w >= 0) ? w : (~w) / kDirectBatch;
           float4 o = P.ro[wk], d = (!SHADOW || w >= 0) ? P.rd[wk] : P.drd[~w];
-          s = jobs[P.unit[wk].x].s;
+          jb = P.unit[wk].x;
+          s = jobs[jb].s;
+          alpha = ALPHA && s.has_alpha != 0;
           r = make_tray(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
           tmin = o.w;
           if (SHADOW) {
@@ -845,6 +895,7 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
             trav_begin(s, t, d.w);
             if (COUNT) tc.closest++;
           }
+          searches = 0;
           active = true;
         } else {
           retired = true;
@@ -853,8 +904,13 @@ __global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ job
     }
     if (__ballot_sync(0xffffffffu, active) == 0) break;
     if (!active) continue;
-    int st = trav_run<SHADOW, COUNT>(s, r, tmin, aim, t, kFetchBudget, &tc);
+    int st = trav_run<SHADOW, COUNT>(s, r, tmin, aim, t, kFetchBudget, &tc, !alpha);
     if (st == 0) continue;
+    // Model::rayHit / rayHit_test retry past cut-away texels (the texture
+    // tables are read through the job table, not kept in registers)
+    if (ALPHA && st == 1 && alpha && !(SHADOW && t.tmax >= aim) &&
+        alpha_again(jobs[jb].s, r, t, tmin, SHADOW ? aim + RMN_EPS : INFINITY, searches, !SHADOW))
+      continue;
     if (SHADOW) {
       const float occluded = st == -2 ? 0.0f : ((t.tmax >= aim) ? 0.0f : 1.0f);
       if (w >= 0) P.res[w] = make_float2(occluded, 0.0f);
@@ -966,6 +1022,8 @@ struct BatchState {
   int* d_status = nullptr;
   float4* d_parts = nullptr;
   int lanes = 1;
+  bool alpha = false;         // some job's scene has alpha-tested materials
+  bool tex = false;           // some job's scene has textures
   Pool pool[kMaxLanes] = {};  // each lane's share of the worker arrays
   Queues q[kMaxLanes] = {};
   std::vector<void*> allocs;
@@ -1013,11 +1071,28 @@ static cudaError_t launch_init(BatchState* b, cudaStream_t st, Counters* ctr) {
   for (int l = 0; l < b->lanes && e == cudaSuccess; ++l)
     e = cudaMemsetAsync(b->pool[l].ph, 0, sizeof(int4) * (size_t)b->pool[l].W, st);
   if (e != cudaSuccess) return e;
-  if (ctr) primary_kernel<true><<<(tp + 127) / 128, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
-  else primary_kernel<false><<<(tp + 127) / 128, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
+  const int pb = (tp + 127) / 128;
+  if (ctr) {
+    if (b->tex) primary_kernel<true, true><<<pb, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
+    else primary_kernel<true, false><<<pb, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
+  } else {
+    if (b->tex) primary_kernel<false, true><<<pb, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
+    else primary_kernel<false, false><<<pb, 128, 0, st>>>(b->d_jobs, nj, tp, b->d_status, ctr);
+  }
   for (int l = 0; l < b->lanes; ++l)
     seed_kernel<<<(b->pool[l].W + 127) / 128, 128, 0, st>>>(b->q[l], &b->d_ctl->lane[l], b->pool[l].W);
   return cudaGetLastError();
+}
+
+// The two traversal kernels of an iteration (closest, then shadow), on as
+// many persistent blocks as fit, at most one lane's worth of rays.
+template <bool COUNT, bool ALPHA>
+static void launch_qtrace(BatchState* b, const Pool& P, const Queues& Q, Ctl* ctl, int par, Counters* ctr, int lb,
+                          cudaStream_t st) {
+  int tb = device_sms() * blocks_per_sm(qtrace_kernel<false, COUNT, ALPHA>);
+  if (tb > lb) tb = lb;
+  qtrace_kernel<false, COUNT, ALPHA><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+  qtrace_kernel<true, COUNT, ALPHA><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
 }
 
 // Iteration k of a chunk (parity k & 1) of one lane: the three logic
@@ -1047,14 +1122,12 @@ static cudaError_t launch_iteration(BatchState* b, int lane, cudaStream_t st, Co
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[1], st);
   const int lb = (P.W + 127) / 128;
-  int tb = sms * (ctr ? blocks_per_sm(qtrace_kernel<false, true>) : blocks_per_sm(qtrace_kernel<false, false>));
-  if (tb > lb) tb = lb;
   if (ctr) {
-    qtrace_kernel<false, true><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
-    qtrace_kernel<true, true><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+    if (b->alpha) launch_qtrace<true, true>(b, P, Q, ctl, par, ctr, lb, st);
+    else launch_qtrace<true, false>(b, P, Q, ctl, par, ctr, lb, st);
   } else {
-    qtrace_kernel<false, false><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
-    qtrace_kernel<true, false><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+    if (b->alpha) launch_qtrace<false, true>(b, P, Q, ctl, par, ctr, lb, st);
+    else launch_qtrace<false, false>(b, P, Q, ctl, par, ctr, lb, st);
   }
   if (ev) cudaEventRecord(ev[3], st);
   return cudaGetLastError();
@@ -1234,6 +1307,12 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
     alloc((void**)&P.mid, sizeof(int) * RMN_MEDIA * W);
     alloc((void**)&P.mval, sizeof(float4) * RMN_MEDIA * W);
   }
+  for (const Job& j : b->table.jobs) {
+    b->tex = b->tex || j.s.has_tex;
+    b->alpha = b->alpha || j.s.has_alpha;
+  }
+  const bool tex = b->tex;
+  if (tex) alloc((void**)&P.rdiff, sizeof(float4) * 3 * W);
   for (int l = 0; l < b->lanes; ++l) {
     const size_t o = (size_t)l * per;
     Pool& L = b->pool[l];
@@ -1259,6 +1338,7 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
         L.mid = P.mid + RMN_MEDIA * o;
         L.mval = P.mval + RMN_MEDIA * o;
       }
+      if (tex) L.rdiff = P.rdiff + 3 * o;
     }
     Queues& Q = b->q[l];
     for (int k = 0; k < 2; ++k) {

@@ -84,13 +84,25 @@ RMN_HD int leaf_ref(int first, int count) { return ~((first << 4) | count); }
 // Shading data, 3 float4 each: vertex normals n0, n1, n2; [0].w = material.
 #define RMN_TRI_SMOOTH 1  // area <= 1e-2: interpolated vertex normals (src/model.cpp:250-265)
 #define RMN_TRI_RENORM 2  // calcSurfaceNormal's tangent frame is finite (src/model.cpp:279-298)
+#define RMN_TRI_ALPHA 4   // the material is alpha-tested (Material::hasFullyTransparentPart)
+// Texture coordinates of a scene with textures, 2 float4 per triangle in
+// leaf order: (u0, v0, u1, v1), (u2, v2, -, -).
 
-// Resolved constant-texel material (64 B).
+// Material (80 B): constant texels resolved, plus texture indices.
 struct __align__(16) DevMat {
   float4 base;   // diffuse colour (white without a texel), w = roughness
   float4 emis;   // emission (0 without a texel), w = metallic
   float4 misc;   // opacity, ior, has emission, material id
   float4 trans;  // transmitting colour
+  int4 tex;      // texture index per slot (diffuse, specular, emissive, normal map), -1 none
+};
+
+// Texture (ImageData, include/material.h:12-24): RGBA8 texels of all mip
+// levels in one array; level l is (w >> l) x (h >> l) texels at byte off[l].
+#define RMN_MIP_LEVELS 8  // MAX_MIPMAP_LEVEL, include/material.h:10
+struct __align__(16) DevTex {
+  int w, h, depth, pad;
+  long long off[RMN_MIP_LEVELS];
 };
 
 // Light object (LightObject, include/component.h:47-54) and its faces.
@@ -127,4 +139,10 @@ struct DevScene {
   int sky_w, sky_h;
   int depth;
   int has_glass;              // some material is transmissive or half-opaque (opacity <= 1 - 1e-4)
+  // textures (scenes without any: null / 0)
+  const float4* uv;           // 2 per triangle, leaf order
+  const DevTex* texs;
+  const uint8_t* texels;
+  int has_tex;                // some material has a texture: textured shading with ray differentials
+  int has_alpha;              // some material is alpha-tested: traversal retries past cut-away texels
 };

@@ -22,6 +22,7 @@
 #include <thread>
 
 #include "rmn_host.h"
+#include "texture.h"
 
 namespace rmn {
 namespace {
@@ -122,6 +123,11 @@ float bits_float(int32_t i) {
   float f;
   std::memcpy(&f, &i, 4);
   return f;
+}
+int32_t float_bits(float f) {
+  int32_t i;
+  std::memcpy(&i, &f, 4);
+  return i;
 }
 
 // The tangent frame of calcSurfaceNormal (src/model.cpp:279-298). With the
@@ -243,6 +249,48 @@ rmn_status acquire_sky(rmn_scene* s, int W, int H, const std::vector<float4>& sk
   return RMN_OK;
 }
 
+// ImageData after Material::loadImageFromFile: level 0 as loaded and the mip
+// chain of ImageData::generateMipmaps (src/material.cpp:107-129): level l
+// halves the previous one with 2x2 integer box averages (texel coordinates
+// wrapped, sum / 4 truncated) until a side would reach 0, at most 8 levels.
+struct HostTex {
+  int w = 0, h = 0, depth = 0;
+  std::vector<uint8_t> lv[RMN_MIP_LEVELS];
+};
+void build_mips(const rmn_texture& in, HostTex& t) {
+  const int ch = 4;
+  t.w = in.width;
+  t.h = in.height;
+  t.lv[0].assign(in.texels, in.texels + (size_t)in.width * in.height * ch);
+  t.depth = RMN_MIP_LEVELS;
+  for (int level = 1; level < RMN_MIP_LEVELS; ++level) {
+    const int pw = t.w >> (level - 1), ph = t.h >> (level - 1), cw = t.w >> level, chh = t.h >> level;
+    if (cw == 0 || chh == 0) {
+      t.depth = level;
+      break;
+    }
+    std::vector<uint8_t>& out = t.lv[level];
+    const std::vector<uint8_t>& prev = t.lv[level - 1];
+    out.resize((size_t)cw * chh * ch);
+    for (int y = 0; y < chh; ++y)
+      for (int x = 0; x < cw; ++x)
+        for (int c = 0; c < ch; ++c) {
+          int sum = 0;
+          for (int dy = 0; dy < 2; ++dy)
+            for (int dx = 0; dx < 2; ++dx)
+              sum += prev[((size_t)((y * 2 + dy) % ph) * pw + (x * 2 + dx) % pw) * ch + c];
+          out[((size_t)y * cw + x) * ch + c] = (uint8_t)(sum / 4);
+        }
+  }
+}
+// ImageData::hasTransparentPart, src/material.cpp:102-107: some level-0
+// alpha below 255.
+bool has_transparent_part(const HostTex& t) {
+  for (size_t i = 3; i < t.lv[0].size(); i += 4)
+    if (t.lv[0][i] < 255) return true;
+  return false;
+}
+
 void release_sky(rmn_scene* s) {
   if (!s->sky_share) return;
   std::lock_guard<std::mutex> lock(g_sky_mu);
@@ -279,6 +327,27 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   for (int m = 0; m < d->num_materials; ++m) glass = glass || !(d->materials[m].opacity > 1.0f - RMN_EPS);
   if (d->env_rgb && (d->env_width <= 0 || d->env_height <= 0))
     return fail(RMN_ERR_INVALID_ARGUMENT, "sky map needs positive width and height");
+  if (d->num_textures < 0 || (d->num_textures > 0 && !d->textures))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "num_textures must be >= 0, with a texture array when positive");
+  for (int i = 0; i < d->num_textures; ++i) {
+    const rmn_texture& t = d->textures[i];
+    if (t.width <= 0 || t.height <= 0 || t.width > 32768 || t.height > 32768 || !t.texels)
+      return fail(RMN_ERR_INVALID_ARGUMENT, "texture %d needs 1..32768 x 1..32768 texels", i);
+    if (t.channels != 4)
+      return fail(RMN_ERR_UNSUPPORTED,
+                  "texture %d has %d channels: textures are RGBA8 (the reference reads 4-byte texels)", i,
+                  t.channels);
+  }
+  bool textured = false;
+  if (d->material_textures) {
+    for (int k = 0; k < 4 * d->num_materials; ++k) {
+      const int t = d->material_textures[k];
+      if (t < -1 || t >= d->num_textures)
+        return fail(RMN_ERR_INVALID_ARGUMENT, "material %d slot %d has texture %d out of range", k / 4, k % 4, t);
+      textured = textured || t >= 0;
+    }
+  }
+  auto mat_tex = [&](int m, int slot) { return d->material_textures ? d->material_textures[4 * m + slot] : -1; };
 
   const int nt = d->num_triangles;
   std::vector<float3> pos(d->num_vertices);
@@ -328,6 +397,59 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
     }
   }
 
+  // ---- textures: mip chains, packed level after level ----
+  std::vector<HostTex> htex(textured ? d->num_textures : 0);
+  std::vector<DevTex> dtex(htex.size());
+  std::vector<uint8_t> texels;
+  for (size_t i = 0; i < htex.size(); ++i) {
+    build_mips(d->textures[i], htex[i]);
+    DevTex& t = dtex[i];
+    t = DevTex{};
+    t.w = htex[i].w;
+    t.h = htex[i].h;
+    t.depth = htex[i].depth;
+    for (int l = 0; l < t.depth; ++l) {
+      t.off[l] = (long long)texels.size();
+      texels.insert(texels.end(), htex[i].lv[l].begin(), htex[i].lv[l].end());
+    }
+  }
+  std::vector<char> alpha_mat(d->num_materials, 0);
+  bool has_alpha = false;
+  for (int m = 0; m < d->num_materials; ++m) {
+    const int t = mat_tex(m, RMN_TEX_DIFFUSE);
+    alpha_mat[m] = (textured && t >= 0 && has_transparent_part(htex[t])) ? 1 : 0;
+    has_alpha = has_alpha || alpha_mat[m];
+  }
+  if (has_alpha)
+    for (int i = 0; i < nt; ++i) {
+      int flags = float_bits(tri[3 * i + 2].w);
+      if (alpha_mat[tri_mesh_mat[b.items[i].id]]) flags |= RMN_TRI_ALPHA;
+      tri[3 * i + 2].w = bits_float(flags);
+    }
+  std::vector<float4> uvs;
+  if (textured) {
+    uvs.resize(2 * (size_t)nt);
+    for (int i = 0; i < nt; ++i) {
+      int t = b.items[i].id;
+      float w[6];
+      for (int k = 0; k < 3; ++k) {
+        int v = d->indices[3 * t + k];
+        w[2 * k] = d->uvs ? d->uvs[2 * v] : 0.0f;
+        w[2 * k + 1] = d->uvs ? d->uvs[2 * v + 1] : 0.0f;
+      }
+      uvs[2 * i] = make_float4(w[0], w[1], w[2], w[3]);
+      uvs[2 * i + 1] = make_float4(w[4], w[5], 0.0f, 0.0f);
+    }
+  }
+  // Material::getEmissiveColor(u, v, NaN): level 0 of the emissive texture,
+  // gamma 2.2, or the constant texel.
+  auto emissive_at = [&](int m, float u, float v) -> float3 {
+    const int t = textured ? mat_tex(m, RMN_TEX_EMISSIVE) : -1;
+    if (t >= 0) return tex_gamma(tex_get<4>(dtex[t], texels.data(), u, v, 0.0f));
+    const rmn_material& q = d->materials[m];
+    return q.has_emission != 0.0f ? f3(q.emission[0], q.emission[1], q.emission[2]) : f3(0.0f);
+  };
+
   // ---- materials (Material::get*, src/material.cpp:349-383) ----
   std::vector<DevMat> mats(d->num_materials);
   for (int m = 0; m < d->num_materials; ++m) {
@@ -343,29 +465,49 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
     mats[m].emis = make_float4(emis.x, emis.y, emis.z, metal);
     mats[m].misc = make_float4(q.opacity, q.ior, q.has_emission != 0.0f ? 1.0f : 0.0f, (float)m);
     mats[m].trans = make_float4(q.transmitting_color[0], q.transmitting_color[1], q.transmitting_color[2], 0.0f);
+    mats[m].tex = make_int4(-1, -1, -1, -1);
+    if (textured)
+      mats[m].tex = make_int4(mat_tex(m, 0), mat_tex(m, 1), mat_tex(m, 2), mat_tex(m, 3));
   }
 
   // ---- light objects (Model::checkLightObject, src/model.cpp:44-82) ----
-  // One per mesh with an emissive texel, built before the sky is loaded as
-  // in the reference (so also when a sky map is present, where they stay
-  // unused by light sampling). The average emissive colour of a constant
-  // texel over the reference's 8x8 grid is 64 equal adds divided by 64.
+  // One per mesh with an emissive texel or texture, built before the sky is
+  // loaded as in the reference (so also when a sky map is present, where
+  // they stay unused by light sampling). Each face's colour is its emission
+  // averaged over an 8x8 grid of barycentric points
+  // (getAverageEmissiveColor, src/model.cpp:23-42).
   std::vector<DevLight> lights;
   std::vector<float4> lfaces;
   std::vector<float> lprefix;
   for (int m = 0; m < d->num_meshes; ++m) {
-    const rmn_material& q = d->materials[d->mesh_material[m]];
-    if (q.has_emission == 0.0f) continue;
-    float3 e = f3(q.emission[0], q.emission[1], q.emission[2]);
-    float3 avg = f3(0.0f);
-    for (int i = 0; i < 64; ++i) avg += e;
-    avg = avg / (float)64;
-    float cl = dot3(avg, f3(0.3f, 0.6f, 0.1f));
+    const int mi = d->mesh_material[m];
+    const rmn_material& q = d->materials[mi];
+    if (q.has_emission == 0.0f && !(textured && mat_tex(mi, RMN_TEX_EMISSIVE) >= 0)) continue;
     float3 color = f3(0.0f), center = f3(0.0f);
     float power = 0.0f;
     std::vector<float> w;
     std::vector<int> faces;
     for (int t = d->mesh_first[m]; t < d->mesh_first[m + 1]; ++t) {
+      float uv[3][2] = {};
+      for (int k = 0; k < 3 && d->uvs; ++k) {
+        uv[k][0] = d->uvs[2 * d->indices[3 * t + k]];
+        uv[k][1] = d->uvs[2 * d->indices[3 * t + k] + 1];
+      }
+      float3 avg = f3(0.0f);
+      for (int gi = 0; gi < 8; ++gi)
+        for (int gj = 0; gj < 8; ++gj) {
+          float ga = static_cast<float>(gi) / 7.0f, gb = static_cast<float>(gj) / 7.0f;
+          if (ga + gb > 1.0f) {
+            ga = 1.0f - ga;
+            gb = 1.0f - gb;
+          }
+          float gc = 1.0f - ga - gb;
+          float u = ga * uv[0][0] + gb * uv[1][0] + gc * uv[2][0];
+          float v = ga * uv[0][1] + gb * uv[1][1] + gc * uv[2][1];
+          avg += emissive_at(mi, u, v);
+        }
+      avg = avg / static_cast<float>(64);
+      float cl = dot3(avg, f3(0.3f, 0.6f, 0.1f));
       float3 v0 = pos[d->indices[3 * t]], v1 = pos[d->indices[3 * t + 1]], v2 = pos[d->indices[3 * t + 2]];
       float area = len3(cross3(v1 - v0, v2 - v0)) / 2.0f;
       if (cl < RMN_EPS || area < RMN_EPS) continue;
@@ -443,6 +585,9 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   if ((st = upload(s, lfaces, &g.light_faces)) != RMN_OK) return st;
   if ((st = upload(s, lprefix, &g.light_prefix)) != RMN_OK) return st;
   if (!sky.empty() && (st = acquire_sky(s, d->env_width, d->env_height, sky, sky_prefix)) != RMN_OK) return st;
+  if ((st = upload(s, uvs, &g.uv)) != RMN_OK) return st;
+  if ((st = upload(s, dtex, &g.texs)) != RMN_OK) return st;
+  if ((st = upload(s, texels, &g.texels)) != RMN_OK) return st;
   g.root = root;
   g.num_tris = nt;
   g.num_mats = d->num_materials;
@@ -451,6 +596,8 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   g.sky_h = d->env_rgb ? d->env_height : 0;
   g.depth = fl.max_depth;
   g.has_glass = glass ? 1 : 0;
+  g.has_tex = textured ? 1 : 0;
+  g.has_alpha = has_alpha ? 1 : 0;
   return RMN_OK;
 }
 

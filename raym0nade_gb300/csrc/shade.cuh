@@ -91,6 +91,117 @@ RMN_D void hit_info(const DevScene& s, int i, float3 rd, Surf& h) {
   if (dot3(h.surfN, rd) >= 0.0f) h.surfN = h.shapeN;
 }
 
+// ---------------------------------------------------------- textures ------
+// RayDifferential, include/render.h:29-33.
+struct RayDiff {
+  float3 dPdx, dPdy, dDdx, dDdy;
+};
+
+// calc_dPdxy, src/render.cpp:44-50: the hit point's differential for a ray
+// of direction rd hitting a plane of normal n at distance t.
+RMN_D void calc_dPdxy(float3 rd, float t, float3 n, const RayDiff& d, float3& px, float3& py) {
+  float dtdx = -dot3(d.dPdx + t * d.dDdx, n) / dot3(rd, n);
+  float dtdy = -dot3(d.dPdy + t * d.dDdy, n) / dot3(rd, n);
+  px = d.dPdx + dtdx * rd + t * d.dDdx;
+  py = d.dPdy + dtdy * rd + t * d.dDdy;
+}
+// calc_dDdxy, src/render.cpp:52-60: the reflected direction's differential
+// (the normal's derivatives are zero).
+RMN_D void calc_dDdxy(float3 rd, float3 n, const RayDiff& d, float3& dx, float3& dy) {
+  const float3 dN = f3(0.0f);
+  float dDNdx = dot3(dN, rd) + dot3(d.dDdx, n);
+  float dDNdy = dot3(dN, rd) + dot3(d.dDdy, n);
+  dx = d.dDdx - 2.0f * (dot3(rd, n) * dN + dDNdx * n);
+  dy = d.dDdy - 2.0f * (dot3(rd, n) * dN + dDNdy * n);
+}
+// getDuv, src/model.cpp:272-277: the texture-space step of a surface step dP.
+RMN_D float2 get_duv(float3 v0, float3 e1, float3 e2, float4 u01, float4 u2, float3 dP) {
+  float3 b = bary(v0, e1, e2, v0 + dP);
+  return make_float2((b.x - 1.0f) * u01.x + b.y * u01.z + b.z * u2.x, (b.x - 1.0f) * u01.y + b.y * u01.w + b.z * u2.y);
+}
+RMN_D bool any_finite2(float2 v) { return finite1(v.x) || finite1(v.y); }  // isfinite(vec2), any component
+RMN_D float len2(float2 v) { return sqrtf(v.x * v.x + v.y * v.y); }
+
+// getHitInfo + getHitMaterial + calcSurfaceNormal of a scene with textures
+// (src/render.cpp:62-79, src/model.cpp:279-328) for a hit at distance t
+// along rd on leaf-order triangle i, reached by a ray of differential d:
+// texture coordinates, level of detail duv from the hit point's
+// differential (returned in px, py), textured diffuse, emission and
+// specular data, and the normal map in the uv tangent frame. Slots without
+// a texture take the material's constant texel. h.pos must hold the hit.
+RMN_CALL void hit_info_tex(const DevScene& s, int i, float3 rd, float t, const RayDiff& d, Surf& h, float3& px,
+                           float3& py) {
+  const float4* tp = s.tri + 3 * i;
+  float4 A = __ldg(tp), B = __ldg(tp + 1), C = __ldg(tp + 2);
+  int flags = __float_as_int(C.w);
+  float3 v0 = f3(A), e1 = f3(B), e2 = f3(C);
+  float3 b = bary(v0, e1, e2, h.pos);
+  const float4* sh = s.shade + 3 * i;
+  float4 N0 = __ldg(sh);
+  int mat = __float_as_int(N0.w);
+  float3 n0 = f3(N0), n1 = f3(0.0f), n2 = f3(0.0f);
+  bool smooth = (flags & RMN_TRI_SMOOTH) != 0;
+  if (smooth) {
+    n1 = f3(__ldg(sh + 1));
+    n2 = f3(__ldg(sh + 2));
+  }
+  hit_normals(e1, e2, smooth, n0, n1, n2, rd, b, h.shapeN, h.surfN, h.entering);
+  float3 raw = h.surfN;
+  calc_dPdxy(rd, t, h.shapeN, d, px, py);
+  const float4 u01 = __ldg(s.uv + 2 * i), u2 = __ldg(s.uv + 2 * i + 1);
+  const float u = b.x * u01.x + b.y * u01.z + b.z * u2.x;
+  const float v = b.x * u01.y + b.y * u01.w + b.z * u2.y;
+  const DevMat& m = s.mats[mat];
+  float4 mb = __ldg(&m.base), me = __ldg(&m.emis), mm = __ldg(&m.misc);
+  int4 tx = __ldg(&m.tex);
+  h.id = (int)mm.w;
+  if (tx.y >= 0) {  // getSurfaceData: level 0 of the specular texture
+    float4 sd = tex_get<4>(s.texs[tx.y], s.texels, u, v, 0.0f);
+    h.metallic = 0.99f < sd.z ? 0.99f : sd.z;
+    h.roughness = sd.y < 1e-3f ? 1e-3f : sd.y;
+  } else {
+    h.roughness = mb.w;
+    h.metallic = me.w;
+  }
+  h.opacity = mm.x;
+  h.eta = mm.y;
+  h.specular = 0.04f;
+  if (h.opacity > 1.0f - RMN_EPS) h.entering = true;
+  const float2 ux = get_duv(v0, e1, e2, u01, u2, px), uy = get_duv(v0, e1, e2, u01, u2, py);
+  // the reference tests dUVdx twice (src/model.cpp:316)
+  const float duv = (any_finite2(ux) && any_finite2(ux)) ? (len2(ux) + len2(uy)) / 2.0f : NAN;
+  if (h.opacity < RMN_EPS) {
+    h.base = f3(__ldg(&m.trans));
+  } else if (tx.x >= 0) {
+    const DevTex& tt = s.texs[tx.x];
+    h.base = tex_gamma(tex_get<4>(tt, s.texels, u, v, tex_level(tt, duv)));
+  } else {
+    h.base = f3(mb);
+  }
+  if (tx.z >= 0) {
+    const DevTex& tt = s.texs[tx.z];
+    h.emis = tex_gamma(tex_get<4>(tt, s.texels, u, v, tex_level(tt, duv)));
+  } else {
+    h.emis = f3(me);
+  }
+  float3 nm = f3(0.0f);
+  if (tx.w >= 0) {
+    const DevTex& tt = s.texs[tx.w];
+    nm = f3(tex_get<3>(tt, s.texels, u, v, tex_level(tt, duv))) * 2.0f - f3(1.0f);
+  }
+  // calcSurfaceNormal, src/model.cpp:279-298
+  const float d1x = u01.z - u01.x, d1y = u01.w - u01.y, d2x = u2.x - u01.x, d2y = u2.y - u01.y;
+  const float k = 1.0f / (d1x * d2y - d2x * d1y);
+  const float3 tu = k * (d2y * e1 - d1y * e2), tv = k * (-d2x * e1 + d1x * e2);
+  const float3 tg = norm3(tu - h.shapeN * dot3(h.shapeN, tu));
+  const float3 bt = norm3(tv - h.shapeN * dot3(h.shapeN, tv) - tg * dot3(tg, tv));
+  const float3 keep = h.surfN;
+  h.surfN = norm3(tg * nm.x + bt * nm.y + h.surfN);
+  if (!any_finite3(h.surfN)) h.surfN = keep;
+  if (dot3(h.surfN, rd) >= 0.0f) h.surfN = raw;
+  if (dot3(h.surfN, rd) >= 0.0f) h.surfN = h.shapeN;
+}
+
 // ------------------------------------------------------------------ BSDF --
 RMN_D float pow5f(float x) { float x2 = x * x; return x2 * x2 * x; }
 RMN_D float schlick(float u) {

@@ -1,6 +1,8 @@
 // Ray-query kernels: closest hit (Model::rayHit, src/model.cpp:332-341) and
 // occlusion (Model::rayHit_test, src/model.cpp:343-354) over ray batches in
-// HBM.
+// HBM. In scenes with alpha-tested materials, occlusion queries and closest
+// queries over (eps, inf) -- Model::rayHit's interval -- retry past cut-away
+// hits as the reference does; other intervals are bare BVH queries.
 //
 // Work distribution: a persistent grid (a multiple of the SM count). Each
 // lane owns one ray at a time; every 16 node visits the lanes whose ray is
@@ -24,7 +26,9 @@ __global__ void __launch_bounds__(128) trace_kernel(DevScene s, const float4* __
   bool active = false, retired = false;
   int64_t i = 0;
   TRay r;
-  float tmin = 0.0f, aim = 0.0f;
+  float tmin = 0.0f, aim = 0.0f, restart = 0.0f;
+  int searches = 0;
+  bool retry = false;
   // the deferred-child stack in shared memory (launched with 128 threads)
   __shared__ int2 sstack[RMN_STACK * 128];
   TravT<SharedStack> t;
@@ -46,11 +50,15 @@ __global__ void __launch_bounds__(128) trace_kernel(DevScene s, const float4* __
             // HitRecord(eps, aimDepth + eps); occluded iff nearer than aimDepth.
             tmin = RMN_EPS;
             aim = r1.w;
-            trav_begin(s, t, aim + RMN_EPS);
+            restart = aim + RMN_EPS;
+            retry = s.has_alpha != 0;
           } else {
             tmin = r0.w;
-            trav_begin(s, t, r1.w);
+            restart = r1.w;
+            retry = s.has_alpha && r0.w == RMN_EPS && isinf(r1.w) && r1.w > 0.0f;
           }
+          trav_begin(s, t, restart);
+          searches = 0;
           active = true;
         } else {
           retired = true;
@@ -59,9 +67,10 @@ __global__ void __launch_bounds__(128) trace_kernel(DevScene s, const float4* __
     }
     if (__ballot_sync(0xffffffffu, active) == 0) return;
     if (!active) continue;
-    int st = trav_run<SHADOW, false>(s, r, tmin, aim, t, kFetchBudget, nullptr);
+    int st = trav_run<SHADOW, false>(s, r, tmin, aim, t, kFetchBudget, nullptr, !retry);
     if (st == 0) continue;
     if (st == -2) atomicExch(status, (int)rmn::kDevStackOverflow);
+    else if (retry && !(SHADOW && t.tmax >= aim) && alpha_again(s, r, t, tmin, restart, searches, !SHADOW)) continue;
     if (SHADOW) {
       occ[i] = (t.tmax >= aim) ? 0 : 1;
     } else if (t.hit < 0) {

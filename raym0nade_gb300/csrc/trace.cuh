@@ -15,6 +15,7 @@
 //    t_min < t < t_max (first hit wins ties).
 #pragma once
 #include "rmn_internal.h"
+#include "texture.h"
 
 struct TRay {
   float3 o, d, inv;
@@ -124,12 +125,13 @@ RMN_D void trav_begin(const DevScene& s, TravT<Stack>& t, float tmax) {
 // leaves advance together instead of waiting for a whole leaf. Returns 1
 // when the query is answered (t.hit / t.tmax final), 0 when the budget ran
 // out first, -2 if the stack would overflow (never for trees the builder
-// accepts). With ANY set, answers as soon as a hit closer than `aim` is
-// recorded (Model::rayHit_test's question, after the same visits as the
-// closest-hit query up to that point).
+// accepts). With ANY and `early` set, answers as soon as a hit closer than
+// `aim` is recorded (Model::rayHit_test's question, after the same visits
+// as the closest-hit query up to that point); scenes with alpha-tested
+// materials clear `early`, since their occlusion test needs the closest hit.
 template <bool ANY, bool COUNT, class Stack>
 RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, TravT<Stack>& t, int budget,
-                   TraceCounters* cnt) {
+                   TraceCounters* cnt, bool early = true) {
   for (;;) {
     if (budget-- <= 0) return 0;
     if (t.ti < t.te) {  // next triangle of the current leaf, in leaf order
@@ -140,7 +142,7 @@ RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav
       if (tmin < th && th < t.tmax) {
         t.tmax = th;
         t.hit = i;
-        if (ANY && th < aim) return 1;
+        if (ANY && early && th < aim) return 1;
       }
       if (t.ti < t.te) continue;
     } else {
@@ -199,21 +201,6 @@ RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav
   }
 }
 
-// One whole query: closest hit in (tmin, tmax). Returns the leaf-order
-// triangle index or -1 (tmax becomes the hit distance), -2 on stack overflow.
-template <bool ANY, bool COUNT>
-RMN_D int trace(const DevScene& s, const TRay& r, float tmin, float& tmax, float aim, TraceCounters* cnt) {
-  Trav t;
-  trav_begin(s, t, tmax);
-  if (COUNT) {
-    if (ANY) cnt->shadow++;
-    else cnt->closest++;
-  }
-  int st = trav_run<ANY, COUNT>(s, r, tmin, aim, t, 0x7fffffff, cnt);
-  tmax = t.tmax;
-  return st == -2 ? -2 : t.hit;
-}
-
 // barycentric(v0, v1, v2, P), src/geometry.cpp:89-103, with e1 = v1 - v0 and
 // e2 = v2 - v0 precomputed. Returns (gamma, alpha, beta).
 RMN_D float3 bary(float3 v0, float3 e1, float3 e2, float3 p) {
@@ -223,4 +210,81 @@ RMN_D float3 bary(float3 v0, float3 e1, float3 e2, float3 p) {
   float al = dot3(cross3(vp, e2), n) / den;
   float be = dot3(cross3(e1, vp), n) / den;
   return f3(1.0f - al - be, al, be);
+}
+
+// TransparentTest, src/model.cpp:217-230: a hit at distance t on triangle i
+// (leaf order) of an alpha-tested material is cut away where the level-0
+// diffuse alpha at the hit is below eps (getDiffuseColor(u, v, NaN); gamma
+// leaves alpha alone). The scene's arrays come as plain pointers so that a
+// caller's scene copy can stay in registers.
+RMN_D bool alpha_cut_at(const float4* __restrict__ tri, const float4* __restrict__ uv,
+                        const float4* __restrict__ shade, const DevMat* __restrict__ mats,
+                        const DevTex* __restrict__ texs, const uint8_t* __restrict__ texels,
+                        float3 o, float3 d, int i, float t) {
+  const float4* tp = tri + 3 * i;
+  const float4 C = __ldg(tp + 2);
+  if (!(__float_as_int(C.w) & RMN_TRI_ALPHA)) return false;
+  const float4 A = __ldg(tp), B = __ldg(tp + 1);
+  const float3 b = bary(f3(A), f3(B), f3(C), o + d * t);
+  const float4 u01 = __ldg(uv + 2 * i), u2 = __ldg(uv + 2 * i + 1);
+  const float u = b.x * u01.x + b.y * u01.z + b.z * u2.x;
+  const float v = b.x * u01.y + b.y * u01.w + b.z * u2.y;
+  const int mat = __float_as_int(__ldg(&shade[3 * i].w));
+  const int tx = __ldg(&mats[mat].tex.x);
+  return tex_get<4>(texs[tx], texels, u, v, 0.0f).w < RMN_EPS;
+}
+RMN_D bool alpha_cut(const DevScene& s, const TRay& r, int i, float t) {
+  return alpha_cut_at(s.tri, s.uv, s.shade, s.mats, s.texs, s.texels, r.o, r.d, i, t);
+}
+
+// The retry loop of Model::rayHit / rayHit_test (src/model.cpp:330-354)
+// after an answered search: if the closest hit is cut away and fewer than 8
+// searches ran, begins the next search from eps beyond it (up to
+// `restart_tmax`) and returns true. `searches` counts the finished searches.
+// When the eighth hit is cut away too, the reference leaves its loop with
+// the record reset for a next search: Model::rayHit (`closest`) then
+// answers a miss, rayHit_test answers occluded (t stays below the aim).
+template <class Stack>
+RMN_D bool alpha_again(const DevScene& s, const TRay& r, TravT<Stack>& t, float& tmin, float restart_tmax,
+                       int& searches, bool closest) {
+  if (t.hit < 0 || !alpha_cut(s, r, t.hit, t.tmax)) return false;
+  if (++searches >= 8) {
+    if (closest) {
+      t.hit = -1;
+      t.tmax = restart_tmax;
+    }
+    return false;
+  }
+  tmin = t.tmax + RMN_EPS;
+  trav_begin(s, t, restart_tmax);
+  return true;
+}
+
+// One whole query: closest hit in (tmin, tmax) (with ANY: whether a hit is
+// nearer than aim). In a scene with alpha-tested materials the query is
+// Model::rayHit's (tmin = eps, tmax = inf) or rayHit_test's (tmax = aim +
+// eps), retried past cut-away hits; ALPHA = false builds the query for
+// scenes known to have none. Returns the leaf-order triangle index or -1
+// (tmax becomes the hit distance), -2 on stack overflow.
+template <bool ANY, bool COUNT, bool ALPHA = true>
+RMN_D int trace(const DevScene& s, const TRay& r, float tmin, float& tmax, float aim, TraceCounters* cnt) {
+  Trav t;
+  const float tmax0 = tmax;
+  trav_begin(s, t, tmax);
+  if (COUNT) {
+    if (ANY) cnt->shadow++;
+    else cnt->closest++;
+  }
+  int searches = 0;
+  for (;;) {
+    const bool alpha = ALPHA && s.has_alpha;
+    int st = trav_run<ANY, COUNT>(s, r, tmin, aim, t, 0x7fffffff, cnt, !alpha);
+    if (st == -2) {
+      tmax = t.tmax;
+      return -2;
+    }
+    if (alpha && !(ANY && t.tmax >= aim) && alpha_again(s, r, t, tmin, tmax0, searches, !ANY)) continue;
+    tmax = t.tmax;
+    return t.hit;
+  }
 }

@@ -47,7 +47,8 @@ def test_struct_sizes_match_header():
 # ctypes mirror -> C struct of include/rmn.h
 ABI_STRUCTS = {"Material": "rmn_material", "SceneDesc": "rmn_scene_desc", "SceneInfo": "rmn_scene_info",
                "RenderArgs": "rmn_render_args", "Image": "rmn_image", "RenderProfile": "rmn_render_profile",
-               "BatchItem": "rmn_batch_item", "BatchOptions": "rmn_batch_options", "TuneResult": "rmn_tune_result"}
+               "BatchItem": "rmn_batch_item", "BatchOptions": "rmn_batch_options", "TuneResult": "rmn_tune_result",
+               "Texture": "rmn_texture"}
 
 
 def test_ctypes_layouts_match_c_compiler(tmp_path):
