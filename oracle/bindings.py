@@ -153,6 +153,7 @@ class OracleLib:
             "compose": (None, [C.c_void_p, C.c_int64, C.c_float, C.c_int, C.c_void_p]),
             "gamma": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
             "fxaa": (None, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
+            "photo": (None, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(self.lib, f"{prefix}_{name}", None)
@@ -181,6 +182,19 @@ class OracleLib:
         out = np.empty_like(rgb)
         self.fn("gamma")(_ptr(rgb), rgb.size // 3, _ptr(out))
         return out
+
+    def photo(self, recs: np.ndarray, stages: int, options: int = 0, exposure: float = 1.0, focus: float = 1.0,
+              coc: float = 0.0, camera=(0.0, 0.0, 0.0)):
+        """Photo's post passes on render records (h, w, 40): stages 1
+        spatialClamp, 2 filter (both update the records' radiance, returned
+        as a new array), 4 postProcessing(options), 8 the same without gamma
+        and FXAA. Returns (records, rgb (h, w, 3) or None)."""
+        recs = np.array(recs, np.float32, copy=True, order="C")
+        h, w = recs.shape[:2]
+        rgb = np.zeros((h, w, 3), np.float32)
+        post = np.array([exposure, focus, coc, *camera], np.float32)
+        self.fn("photo")(_ptr(recs), w, h, stages, options, _ptr(post), _ptr(rgb))
+        return recs, (rgb if stages & 12 else None)
 
     def fxaa(self, rgb: np.ndarray) -> np.ndarray:
         rgb = np.ascontiguousarray(rgb, np.float32)

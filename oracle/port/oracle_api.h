@@ -59,6 +59,18 @@ typedef struct orc_scene_in {
 //  [36] material id [37] entering [38] indirect sample count [39] spp_indirect
 #define ORC_PIX_FLOATS 40
 
+// Photo's post passes (src/image.cpp:30-356, 454-479) on a W x H render
+// given as records (radiance with Var, G-buffer fields; in place):
+//   stages bit 1  Photo::spatialClamp of the four radiance buffers;
+//          bit 2  Photo::filter (filterVar + five a-trous passes);
+//          bit 4  Photo::postProcessing(options) into rgb (3 per pixel):
+//                 shade, depth-of-field blur (1024), bloom (256), gamma,
+//                 FXAA (512);
+//          bit 8  the same without gamma and FXAA (linear).
+// post: exposure, focus, CoC, camera position (3).
+void port_photo(float* recs, int w, int h, int stages, int options, const float* post, float* rgb);
+void ref_photo(float* recs, int w, int h, int stages, int options, const float* post, float* rgb);
+
 #ifdef __cplusplus
 }
 #endif

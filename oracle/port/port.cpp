@@ -1237,6 +1237,251 @@ static void fxaa(const float* in, float* out, int W, int H) {
     }
 }
 
+// ------------------------------------------------------ photo passes -----
+// Photo's post passes (src/image.cpp:30-356, 454-479) on the records of a
+// render: radiance buffers with their Var, the G-buffer, and the pixel array.
+struct PhotoBuf {
+  int w = 0, h = 0;
+  float exposure = 1.0f, focus = 1.0f, coc = 0.0f;
+  vec3 cam = vec3(0.0f);
+  std::vector<Surf> g;
+  std::vector<Rad> buf[4];  // Dd, Ds, Id, Is
+  std::vector<vec3> px;
+};
+
+// clamp(RadianceData*, ...), src/image.cpp:30-75: luminance blurred by a
+// separable 7-tap kernel (taps outside the image dropped); a pixel brighter
+// than 36x its neighbourhood (its own tap removed) is scaled down to it.
+static void spatial_clamp_buf(std::vector<Rad>& r, int W, int H) {
+  const float h[7] = {0.03125f, 0.109375f, 0.21875f, 0.28125f, 0.21875f, 0.109375f, 0.03125f};
+  const size_t n = (size_t)W * H;
+  std::vector<float> lum(n), b1(n), b2(n);
+  for (size_t i = 0; i < n; ++i) lum[i] = dot(r[i].r, kLum);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      float sum = 0.0f;
+      for (int dx = -3; dx <= 3; ++dx) {
+        int nx = x + dx;
+        if (nx >= 0 && nx < W) sum += lum[(size_t)y * W + nx] * h[dx + 3];
+      }
+      b1[(size_t)y * W + x] = sum;
+    }
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      float sum = 0.0f;
+      for (int dy = -3; dy <= 3; ++dy) {
+        int ny = y + dy;
+        if (ny >= 0 && ny < H) sum += b1[(size_t)ny * W + x] * h[dy + 3];
+      }
+      b2[(size_t)y * W + x] = sum;
+    }
+  for (size_t i = 0; i < n; ++i) {
+    float l = lum[i];
+    float bl = b2[i] - h[3] * h[3] * l;
+    if (l > 36.0f * bl) r[i].r *= bl / (l + kEps) / (1.0f - h[3] * h[3]);
+  }
+}
+
+// filterVar, src/image.cpp:84-108: Var of a 3x3 binomial neighbourhood.
+static void filter_var(std::vector<Rad>& r, int W, int H) {
+  const float h[3] = {0.25f, 0.5f, 0.25f};
+  std::vector<float> v((size_t)W * H);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      vec3 E(0.0f);
+      float E2 = 0.0f, V = 0.0f;
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) {
+          int nx = x + dx, ny = y + dy;
+          if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+          const Rad& q = r[(size_t)ny * W + nx];
+          float wt = h[dx + 1] * h[dy + 1];
+          E += q.r * wt;
+          E2 += dot(q.r, q.r) * wt;
+          V += q.var * wt;
+        }
+      v[(size_t)y * W + x] = V + E2 - dot(E, E);
+    }
+  for (size_t i = 0; i < v.size(); ++i) r[i].var = v[i];
+}
+
+// getWeight, src/image.cpp:110-158: edge-stopping weight of tap q for p.
+static float edge_weight(const Surf& P, const Surf& Q, const Rad& Lp, const Rad& Lq, bool specular) {
+  if (!any_finite(Q.pos)) return 0.0f;
+  float w = std::pow(std::max(0.0f, dot(P.surfN, Q.surfN)), 1024.0f);
+  if (w < 1e-6f) return 0.0f;
+  float k = 0.0f;
+  vec3 dir = normalize(Q.pos - P.pos);
+  float st = std::abs(dot(P.shapeN, dir));
+  float tt = st / (std::sqrt(1.0f - st * st) + kEps);
+  k += -tt / 1.0f;
+  float rd = length(Lp.r - Lq.r) / (1.0f * std::sqrt(Lp.var) + 1e-2f);
+  k += -rd;
+  float md = length(vec3(P.metallic - Q.metallic, P.specular - Q.specular, P.opacity - Q.opacity));
+  k += -md / 1.0f;
+  if (k < -7.5f) return 0.0f;
+  w *= std::exp(k);
+  if (specular) w *= std::max(P.roughness, 4e-2f);
+  if (!std::isfinite(w)) return 0.0f;
+  return w;
+}
+
+// filterRadiance(..., step), src/image.cpp:160-199: one a-trous pass.
+static void filter_pass(std::vector<Rad>& r, const std::vector<Surf>& G, int W, int H, bool specular, int step) {
+  const float h[5] = {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f};
+  const size_t n = (size_t)W * H;
+  std::vector<vec3> rb(n, vec3(0.0f));
+  std::vector<float> vb(n, 0.0f);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) {
+      const size_t i = (size_t)y * W + x;
+      float ws = 0.0f;
+      const Rad& Lp = r[i];
+      const Surf& P = G[i];
+      if (!any_finite(P.pos)) continue;
+      for (int dy = -2; dy <= 2; ++dy)
+        for (int dx = -2; dx <= 2; ++dx) {
+          int nx = x + dx * step, ny = y + dy * step;
+          if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+          float wt = h[dx + 2] * h[dy + 2];
+          const size_t j = (size_t)ny * W + nx;
+          if (dx != 0 || dy != 0) wt *= edge_weight(P, G[j], Lp, r[j], specular);
+          ws += wt;
+          rb[i] += r[j].r * wt;
+          vb[i] += r[j].var * wt * wt;
+        }
+      rb[i] /= ws;
+      vb[i] /= ws * ws;
+    }
+  for (size_t i = 0; i < n; ++i) {
+    r[i].r = rb[i];
+    r[i].var = vb[i];
+  }
+}
+
+// Photo::filter, src/image.cpp:201-213: filterVar, then passes of step 1, 2,
+// 4, 8, 16; the specular buffers weight by roughness.
+static void filter_photo(PhotoBuf& ph) {
+  for (int b = 0; b < 4; ++b) {
+    const bool spec = (b & 1) != 0;
+    filter_var(ph.buf[b], ph.w, ph.h);
+    for (int step = 1; step <= 16; step *= 2) filter_pass(ph.buf[b], ph.g, ph.w, ph.h, spec, step);
+  }
+}
+
+// Photo::shade, src/image.cpp:215-246.
+static void shade_photo(PhotoBuf& ph, int opt) {
+  for (size_t i = 0; i < ph.px.size(); ++i) {
+    const Surf& G = ph.g[i];
+    if (opt & 64) { ph.px[i] = (G.shapeN + vec3(1.0f)) / 2.0f; continue; }
+    if (opt & 128) { ph.px[i] = (G.surfN + vec3(1.0f)) / 2.0f; continue; }
+    vec3 rd(0.0f), rs(0.0f);
+    if (opt & 4) {
+      if (opt & 16) rd += ph.buf[0][i].r;
+      if (opt & 32) rs += ph.buf[1][i].r;
+    }
+    if (opt & 8) {
+      if (opt & 16) rd += ph.buf[2][i].r;
+      if (opt & 32) rs += ph.buf[3][i].r;
+    }
+    if (!(opt & (4 | 8))) rd = vec3(1.0f);
+    vec3 dc = (opt & 1) ? G.base : vec3(1.0f);
+    ph.px[i] = dc * rd + rs;
+    if (opt & 2) ph.px[i] += G.emis * ph.exposure;
+  }
+}
+
+// Photo::bloom, src/image.cpp:248-280: the part above luminance 1 (scaled
+// by lum^-0.65, minus 1 per channel) blurred by five a-trous passes, each
+// pass's result added at 1/6.
+static void bloom_photo(PhotoBuf& ph) {
+  const float h[5] = {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f};
+  const int W = ph.w, H = ph.h;
+  std::vector<vec3> bc((size_t)W * H, vec3(0.0f));
+  for (size_t i = 0; i < bc.size(); ++i) {
+    float c = dot(ph.px[i], kLum);
+    if (c < 1.0f) continue;
+    bc[i] = ph.px[i] / std::pow(c, 0.65f);
+    for (int k = 0; k < 3; ++k) bc[i][k] = std::max(bc[i][k] - 1.0f, 0.0f);
+  }
+  for (int step = 1; step <= 16; step *= 2) {
+    std::vector<vec3> t = bc;
+    for (int y = 0; y < H; ++y)
+      for (int x = 0; x < W; ++x) {
+        vec3& col = bc[(size_t)y * W + x];
+        col = vec3(0.0f);
+        for (int ky = -2; ky <= 2; ++ky)
+          for (int kx = -2; kx <= 2; ++kx) {
+            int nx = x + kx * step, ny = y + ky * step;
+            if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+            col += t[(size_t)ny * W + nx] * h[ky + 2] * h[kx + 2];
+          }
+      }
+    for (size_t i = 0; i < bc.size(); ++i) ph.px[i] += bc[i] / 6.0f;
+  }
+}
+
+// float -> int of the depth-of-field radii: truncation, 0 for NaN (what
+// aarch64 and CUDA give; the conversion is undefined in C++ and x86 gives
+// INT_MIN, on which the reference's loops run for 2^31 steps).
+static int dof_int(float v) {
+  if (v != v) return 0;
+  if (v >= 2147483647.0f) return 2147483647;
+  if (v <= -2147483648.0f) return (-2147483647 - 1);
+  return (int)v;
+}
+
+// Photo::depthFeildBlur, src/image.cpp:282-356: pixels in stable depth
+// order scatter their colour over a disc of radius CoC0 (weights normalised
+// per pixel); a receiving pixel stops taking weight at 0.99.
+static void dof_photo(PhotoBuf& ph) {
+  struct PixelPos { int x, y; float depth; };
+  const int W = ph.w, H = ph.h;
+  std::vector<PixelPos> pix;
+  pix.reserve((size_t)W * H);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) pix.push_back({x, y, length(ph.g[(size_t)y * W + x].pos - ph.cam)});
+  std::stable_sort(pix.begin(), pix.end(), [](const PixelPos& a, const PixelPos& b) { return a.depth < b.depth; });
+  std::vector<vec3> blur((size_t)W * H, vec3(0.0f));
+  std::vector<float> gained((size_t)W * H, 0.0f);
+  for (const PixelPos& p : pix) {
+    const float coc0 = std::min(ph.coc * std::abs(1.0f - ph.focus / p.depth) + kEps, 96.0f);
+    const int radius = dof_int(coc0);
+    const vec3 color = ph.px[(size_t)p.y * W + p.x];
+    float tw = 0.0f;
+    for (int dy = -radius; dy <= radius; ++dy) {
+      int xl, xr;
+      const int xlen = dof_int(std::sqrt(coc0 * coc0 - dy * dy));
+      for (xl = -xlen; xl <= 0; xl++) {
+        float wt = std::min(coc0 - std::sqrt(float(xl * xl + dy * dy)), 1.0f);
+        if (wt == 1.0f) break;
+        tw += wt;
+      }
+      for (xr = xlen; xr > 0; xr--) {
+        float wt = std::min(coc0 - std::sqrt(float(xr * xr + dy * dy)), 1.0f);
+        if (wt == 1.0f) break;
+        tw += wt;
+      }
+      tw += xr - xl + 1;
+    }
+    for (int dy = -radius; dy <= radius; ++dy) {
+      const int xlen = dof_int(std::sqrt(coc0 * coc0 - dy * dy));
+      for (int dx = -xlen; dx <= xlen; ++dx) {
+        int nx = p.x + dx, ny = p.y + dy;
+        if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+        float wt = std::min(coc0 - std::sqrt(float(dx * dx + dy * dy)), 1.0f) / tw;
+        if (wt < kEps) continue;
+        const size_t id = (size_t)ny * W + nx;
+        if (gained[id] + wt > 0.99f) wt = 0.99f - gained[id];
+        if (wt < kEps) continue;
+        blur[id] += color * wt;
+        gained[id] += wt;
+      }
+    }
+  }
+  for (size_t i = 0; i < blur.size(); ++i) ph.px[i] = blur[i] / gained[i];
+}
+
 template <class F>
 static void parallel_for(long n, int threads, F&& f, long chunk = 64) {
   if (threads <= 1 || n <= chunk) { for (long i = 0; i < n; ++i) f(i); return; }
@@ -1482,5 +1727,59 @@ void port_gamma(const float* in, int64_t n, float* out) {
 }
 
 void port_fxaa(const float* in, float* out, int w, int h) { fxaa(in, out, w, h); }
+
+void port_photo(float* recs, int w, int h, int stages, int options, const float* post, float* rgb) {
+  PhotoBuf ph;
+  ph.w = w;
+  ph.h = h;
+  ph.exposure = post[0];
+  ph.focus = post[1];
+  ph.coc = post[2];
+  ph.cam = vec3(post[3], post[4], post[5]);
+  const size_t n = (size_t)w * h;
+  ph.g.resize(n);
+  ph.px.assign(n, vec3(0.0f));
+  for (int b = 0; b < 4; ++b) ph.buf[b].resize(n);
+  for (size_t i = 0; i < n; ++i) {
+    const float* r = recs + ORC_PIX_FLOATS * i;
+    for (int b = 0; b < 4; ++b) {
+      ph.buf[b][i].r = vec3(r[4 * b], r[4 * b + 1], r[4 * b + 2]);
+      ph.buf[b][i].var = r[4 * b + 3];
+    }
+    Surf& G = ph.g[i];
+    G.base = vec3(r[16], r[17], r[18]);
+    G.emis = vec3(r[19], r[20], r[21]);
+    G.pos = vec3(r[22], r[23], r[24]);
+    G.shapeN = vec3(r[25], r[26], r[27]);
+    G.surfN = vec3(r[28], r[29], r[30]);
+    G.roughness = r[31]; G.metallic = r[32]; G.opacity = r[33]; G.specular = r[34]; G.eta = r[35];
+    G.id = (int)r[36]; G.entering = r[37] != 0.0f;
+  }
+  if (stages & 1)
+    for (int b = 0; b < 4; ++b) spatial_clamp_buf(ph.buf[b], w, h);
+  if (stages & 2) filter_photo(ph);
+  if (stages & (4 | 8)) {  // Photo::postProcessing, src/image.cpp:470-479 (8: without gamma and FXAA)
+    shade_photo(ph, options);
+    if (options & 1024) dof_photo(ph);
+    if (options & 256) bloom_photo(ph);
+    if (stages & 4) {
+      for (vec3& p : ph.px) p = gamma(p);
+      if (options & 512) {
+        std::vector<float> a(3 * n), o(3 * n);
+        for (size_t i = 0; i < n; ++i) { a[3 * i] = ph.px[i].x; a[3 * i + 1] = ph.px[i].y; a[3 * i + 2] = ph.px[i].z; }
+        fxaa(a.data(), o.data(), w, h);
+        for (size_t i = 0; i < n; ++i) ph.px[i] = vec3(o[3 * i], o[3 * i + 1], o[3 * i + 2]);
+      }
+    }
+    for (size_t i = 0; i < n; ++i) { rgb[3 * i] = ph.px[i].x; rgb[3 * i + 1] = ph.px[i].y; rgb[3 * i + 2] = ph.px[i].z; }
+  }
+  for (size_t i = 0; i < n; ++i) {
+    float* r = recs + ORC_PIX_FLOATS * i;
+    for (int b = 0; b < 4; ++b) {
+      r[4 * b] = ph.buf[b][i].r.x; r[4 * b + 1] = ph.buf[b][i].r.y; r[4 * b + 2] = ph.buf[b][i].r.z;
+      r[4 * b + 3] = ph.buf[b][i].var;
+    }
+  }
+}
 
 }  // extern "C"

@@ -388,6 +388,50 @@ void ref_gamma(const float* in, int64_t n, float* out) {
   }
 }
 
+void ref_photo(float* recs, int w, int h, int stages, int options, const float* post, float* rgb) {
+  Photo ph(w, h);
+  ph.exposure = post[0];
+  ph.focus = post[1];
+  ph.CoC = post[2];
+  ph.cameraPosition = vec3(post[3], post[4], post[5]);
+  const long n = (long)w * h;
+  RadianceData* bufs[4] = {ph.radiance_Dd, ph.radiance_Ds, ph.radiance_Id, ph.radiance_Is};
+  for (long i = 0; i < n; ++i) {
+    const float* r = recs + ORC_PIX_FLOATS * i;
+    for (int b = 0; b < 4; ++b) {
+      bufs[b][i].radiance = vec3(r[4 * b], r[4 * b + 1], r[4 * b + 2]);
+      bufs[b][i].Var = r[4 * b + 3];
+    }
+    HitInfo& G = ph.Gbuffer[i];
+    G.baseColor = vec3(r[16], r[17], r[18]);
+    G.emission = vec3(r[19], r[20], r[21]);
+    G.position = vec3(r[22], r[23], r[24]);
+    G.shapeNormal = vec3(r[25], r[26], r[27]);
+    G.surfaceNormal = vec3(r[28], r[29], r[30]);
+    G.roughness = r[31]; G.metallic = r[32]; G.opacity = r[33]; G.specular = r[34]; G.eta = r[35];
+    G.id = (int)r[36]; G.entering = r[37] != 0.0f;
+  }
+  if (stages & 1) ph.spatialClamp();
+  if (stages & 2) ph.filter();
+  if (stages & 4) ph.postProcessing(options);
+  if (stages & 8) {  // postProcessing without gammaCorrection and FXAA
+    ph.shade(options);
+    if (options & Photo::DoDepthFieldBlur) ph.depthFeildBlur();
+    if (options & Photo::DoBloom) ph.bloom();
+  }
+  if (stages & (4 | 8))
+    for (long i = 0; i < n; ++i) {
+      rgb[3 * i] = ph.pixelarray[i].x; rgb[3 * i + 1] = ph.pixelarray[i].y; rgb[3 * i + 2] = ph.pixelarray[i].z;
+    }
+  for (long i = 0; i < n; ++i) {
+    float* r = recs + ORC_PIX_FLOATS * i;
+    for (int b = 0; b < 4; ++b) {
+      r[4 * b] = bufs[b][i].radiance.x; r[4 * b + 1] = bufs[b][i].radiance.y; r[4 * b + 2] = bufs[b][i].radiance.z;
+      r[4 * b + 3] = bufs[b][i].Var;
+    }
+  }
+}
+
 void ref_fxaa(const float* in, float* out, int w, int h) {
   Photo ph(w, h);
   for (long i = 0; i < (long)w * h; ++i) ph.pixelarray[i] = vec3(in[3 * i], in[3 * i + 1], in[3 * i + 2]);

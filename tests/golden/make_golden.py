@@ -25,6 +25,10 @@ Fixtures (numpy .npz, compressed):
                      room (alpha-test retries). ``--textured`` writes it alone.
   post.npz           Photo::shade(Full) + gammaCorrection of render records,
                      and Photo::FXAA of a 96 x 64 image with hard edges.
+  photo.npz          Photo's post passes on 32 x 20 synthetic records
+                     (``photo_records``): spatialClamp, filter, bloom, depth
+                     of field, postProcessing with and without them (the
+                     cases of PHOTO_CASES). ``--photo`` writes it alone.
   cornell_4096spp.npz  the converged reference image of the Cornell workload
                      (256 x 256, 4096 spp, max depth 16, P_Direct 0.7):
                      Photo::shade(Full) before gamma, float16. Made by
@@ -67,6 +71,72 @@ def scene_from(z, prefix=""):
             n += 1
         sc.textures = [g("tex%d" % i) for i in range(n)]
     return sc
+
+
+def photo_records(w, h, seed, miss=0.0):
+    """Synthetic render records (h, w, 40) for the post passes: a tilted,
+    bumpy surface seen from (0, 0, -1) (positions, jittered shape and
+    surface normals), random roughness / metallic / opacity patches, noisy
+    radiance with Var, fireflies planted in every buffer, an emitter patch
+    bright enough to bloom; a fraction ``miss`` of pixels without a hit."""
+    rng = np.random.default_rng(seed)
+    r = np.zeros((h, w, 40), np.float32)
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float64)
+    u, v = xx / w - 0.5, yy / h - 0.5
+    z = 1.0 + 0.6 * u + 0.3 * v + 0.05 * np.sin(9 * u) * np.cos(7 * v)
+    pos = np.stack([u * z, v * z, z], -1)
+    n = np.stack([-0.6 + 0.2 * rng.standard_normal((h, w)), -0.3 + 0.2 * rng.standard_normal((h, w)),
+                  -np.ones((h, w))], -1)
+    sn = n / np.linalg.norm(n, axis=-1, keepdims=True)
+    n2 = sn + 0.02 * rng.standard_normal((h, w, 3))
+    n2 /= np.linalg.norm(n2, axis=-1, keepdims=True)
+    for b in range(4):
+        rad = rng.gamma(2.0, 0.15, (h, w, 3)) * (1.0 + 0.5 * np.sin(5 * u + b))[..., None]
+        spikes = rng.random((h, w)) < 0.01
+        rad[spikes] *= rng.uniform(20, 400, (spikes.sum(), 1))
+        r[..., 4 * b:4 * b + 3] = rad
+        r[..., 4 * b + 3] = rng.gamma(1.0, 0.05, (h, w))
+    r[..., 16:19] = rng.uniform(0.05, 0.95, (h, w, 3))
+    em = (np.abs(u - 0.2) < 0.06) & (np.abs(v + 0.1) < 0.08)
+    r[..., 19:22][em] = rng.uniform(2.0, 8.0, (em.sum(), 3))
+    r[..., 22:25] = pos
+    r[..., 25:28] = sn
+    r[..., 28:31] = n2
+    patch = ((xx // 8) + 3 * (yy // 8)).astype(np.int64) % 7
+    r[..., 31] = np.array([0.01, 0.03, 0.1, 0.3, 0.5, 0.8, 1.0])[patch]
+    r[..., 32] = np.where(patch % 3 == 0, 0.8, 0.0)
+    r[..., 33] = np.where(patch == 5, 0.0, 1.0)
+    r[..., 34] = 0.04
+    r[..., 35] = 1.0
+    r[..., 36] = patch
+    r[..., 37] = 1.0
+    if miss > 0:
+        m = rng.random((h, w)) < miss
+        r[..., 22:25][m] = np.nan
+        r[..., 25:31][m] = np.nan
+    return r
+
+
+# (stages, options) of the photo.npz cases; post arguments exposure 1,
+# focus 0.9, CoC 8, camera (0, 0, -1)
+PHOTO_CASES = [(1, 0), (2, 0), (3, 0), (8, 63 | 256), (8, 63 | 1024), (8, 63 | 1024 | 256), (4, 63 | 1024 | 256 | 512),
+               (3 | 4, 63 | 512), (4, 64), (4, 128), (4, 1 | 512)]
+PHOTO_POST = dict(exposure=1.0, focus=0.9, coc=8.0, camera=(0.0, 0.0, -1.0))
+
+
+def photo(R=None):
+    if R is None:
+        bindings.build(with_reference=True)
+        R = bindings.OracleLib("ref")
+    rec = photo_records(32, 20, 3)
+    out = {"records": rec}
+    for k, (stages, opt) in enumerate(PHOTO_CASES):
+        r2, rgb = R.photo(rec, stages, opt, **PHOTO_POST)
+        if stages & 3:  # the passes that change the radiance buffers
+            out["rec%d" % k] = r2[..., :16]
+        if rgb is not None:
+            out["rgb%d" % k] = rgb
+    np.savez_compressed(os.path.join(HERE, "photo.npz"), **out)
 
 
 def room_rays(n, seed, shadow=False):
@@ -144,6 +214,7 @@ def main():
 
     glass(R)
     textured()
+    photo(R)
 
     rgb_lin = R.compose(rec, 1.0, gamma=False)
     rgb = R.compose(rec, 1.0, gamma=True)
@@ -204,6 +275,9 @@ if __name__ == "__main__":
     elif "--glass" in sys.argv:
         glass()
         print("glass fixture written to", HERE)
+    elif "--photo" in sys.argv:
+        photo()
+        print("photo fixture written to", HERE)
     elif "--textured" in sys.argv:
         textured()
         print("textured fixture written to", HERE)

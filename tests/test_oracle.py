@@ -15,7 +15,8 @@ import numpy as np
 import pytest
 
 from raym0nade_gb300 import scenes
-from tests.golden.make_golden import edge_rays, reachable, room_rays, scene_from, tie_soup
+from tests.golden.make_golden import (PHOTO_CASES, PHOTO_POST, edge_rays, photo_records, reachable, room_rays,
+                                      scene_from, tie_soup)
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
@@ -54,6 +55,15 @@ def test_golden_textured_trace(port):
     face, t, bc = ps.trace_closest(z["rays"])
     assert same(face, z["face"]) and same(t, z["t"]) and same(bc, z["bary"])
     assert same(ps.trace_shadow(z["shadow_rays"]), z["occluded"])
+
+
+def test_golden_photo(port):
+    z = np.load(os.path.join(GOLDEN, "photo.npz"))
+    for k, (stages, opt) in enumerate(PHOTO_CASES):
+        r2, rgb = port.photo(z["records"], stages, opt, **PHOTO_POST)
+        assert same(r2[..., :16], z["rec%d" % k] if stages & 3 else z["records"][..., :16]), (stages, opt)
+        if rgb is not None:
+            assert same(rgb, z["rgb%d" % k]), (stages, opt)
 
 
 def test_golden_post(port):
@@ -185,3 +195,40 @@ def test_ref_tex_refuses_constant_texels(ref_tex):
     room.materials[2, 3] = 1.0  # a constant diffuse texel without a texture
     with pytest.raises(ValueError):
         ref_tex.scene(room)
+
+
+# ------------------------------------------------ post passes (f3) ---------
+def _inside_camera(w, h, spp):
+    import math
+    acc = math.tan(math.radians(30.0)) / (w / 2.0)
+    return scenes.Camera((0.5, 0.5, 0.3), (0.0, 0.0, 1.0), (0.0, -1.0, 0.0), (-1.0, 0.0, 0.0), acc, w, h, spp)
+
+
+@pytest.mark.parametrize("stages,opt", PHOTO_CASES)
+def test_photo_passes_match_reference(port, ref, stages, opt):
+    """spatialClamp, filter, bloom, depth of field and postProcessing on a
+    Cornell render seen from inside the box (every pixel a hit) and on
+    synthetic records with fireflies, bumpy normals and material patches."""
+    rec = ref.scene(scenes.cornell()).render(_inside_camera(48, 32, 16), seed=5)
+    for r, post in [(rec, dict(exposure=1.0, focus=0.5, coc=6.0, camera=(0.5, 0.5, 0.3))),
+                    (photo_records(56, 36, 9), PHOTO_POST)]:
+        a = port.photo(r, stages, opt, **post)
+        b = ref.photo(r, stages, opt, **post)
+        assert same(a[0], b[0])
+        if a[1] is not None:
+            assert same(a[1], b[1])
+
+
+def test_photo_passes_change_the_image(port):
+    """The cases are not vacuous: the clamp scales fireflies, the filter
+    smooths, bloom adds light, depth of field blurs."""
+    rec = photo_records(64, 40, 3)
+    c, _ = port.photo(rec, 1)
+    assert (c[..., :16] != rec[..., :16]).sum() > 30
+    f, _ = port.photo(rec, 2)
+    assert np.abs(f[..., 8:11] - rec[..., 8:11]).mean() > 0.01
+    _, base = port.photo(rec, 8, 63, **PHOTO_POST)
+    _, bl = port.photo(rec, 8, 63 | 256, **PHOTO_POST)
+    _, dof = port.photo(rec, 8, 63 | 1024, **PHOTO_POST)
+    assert (bl - base).min() >= 0.0 and (bl - base).max() > 0.1
+    assert np.abs(dof - base).mean() > 0.01
