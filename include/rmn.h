@@ -173,13 +173,25 @@ typedef struct rmn_image {
 } rmn_image;
 #define RMN_GBUFFER_FLOATS 21
 
-/* Photo::ShadeOption bits (include/image.h:17-34) used by rmn_compose. */
+/* Photo::ShadeOption bits (include/image.h:17-34) used by rmn_compose and
+ * rmn_post_process. */
 enum {
   RMN_SHADE_BASECOLOR = 1, RMN_SHADE_EMISSION = 2, RMN_SHADE_DIRECT = 4, RMN_SHADE_INDIRECT = 8,
   RMN_SHADE_DIFFUSE = 16, RMN_SHADE_SPECULAR = 32, RMN_SHADE_FULL = 63,
-  RMN_SHADE_GAMMA = 4096, /* apply Photo::gammaCorrection */
-  RMN_SHADE_FXAA = 512    /* then Photo::FXAA (display-referred, as postProcessing does) */
+  RMN_SHADE_SHAPE_NORMAL = 64, RMN_SHADE_SURFACE_NORMAL = 128,
+  RMN_SHADE_BLOOM = 256,           /* Photo::bloom (rmn_post_process only) */
+  RMN_SHADE_FXAA = 512,            /* then Photo::FXAA (display-referred, as postProcessing does) */
+  RMN_SHADE_DEPTH_OF_FIELD = 1024, /* Photo::depthFeildBlur (rmn_post_process only) */
+  RMN_SHADE_GAMMA = 4096           /* apply Photo::gammaCorrection */
 };
+
+/* Photo's post-processing state (include/image.h:36-38). */
+typedef struct rmn_post_args {
+  int32_t width, height;
+  float exposure;
+  float focus, CoC;          /* depth of field: focus distance, circle-of-confusion scale (finite, >= 0) */
+  float camera_position[3];  /* depth is measured from here */
+} rmn_post_args;
 
 const char* rmn_last_error(void);
 const char* rmn_version(void);
@@ -309,6 +321,42 @@ rmn_status rmn_compose_noalloc(const rmn_image* image, int32_t width, int32_t he
 
 /* Photo::FXAA (src/image.cpp:363-452) on an rgb image (3 floats per pixel). */
 rmn_status rmn_fxaa(const float* rgb_in, float* rgb_out, int32_t width, int32_t height, void* stream);
+
+/* Photo::postProcessing (src/image.cpp:470-479) over rmn_render's buffers:
+ * Photo::shade(options), then the depth-of-field blur (RMN_SHADE_DEPTH_OF_FIELD,
+ * src/image.cpp:282-356) and bloom (RMN_SHADE_BLOOM, :248-280) when asked,
+ * gammaCorrection when RMN_SHADE_GAMMA is set (postProcessing always applies
+ * it), FXAA last -> rgb (3 floats per pixel). The depth-of-field blur sorts
+ * the pixels' depths on the host (std::stable_sort, as the reference) and
+ * synchronises the stream once. */
+rmn_status rmn_post_process(const rmn_image* image, const rmn_post_args* args, int32_t options, float* rgb,
+                            void* stream);
+
+/* Photo::spatialClamp (src/image.cpp:30-82): clamps fireflies of the four
+ * radiance buffers in place. */
+rmn_status rmn_spatial_clamp(const rmn_image* image, int32_t width, int32_t height, void* stream);
+
+/* Photo::filter (src/image.cpp:84-213): the G-buffer-guided a-trous filter
+ * (filterVar, then passes of step 1..16) of the four radiance buffers, in
+ * place (the specular buffers weight by roughness). */
+rmn_status rmn_filter(const rmn_image* image, int32_t width, int32_t height, void* stream);
+
+/* The export set of render_multiThread (src/render.cpp:641-674): images
+ * k = 0..count-1 (tags from rmn_export_tag) into rgb + 3 * width * height * k,
+ * each through Photo::postProcessing (gamma applied): RMN_EXPORTS images, plus
+ * RMN_EXPORTS_DOF more when args->CoC > 1e-4 (the depth-of-field exports).
+ * As in the reference the radiance buffers are modified on the way:
+ * spatialClamp after export 3, filter after export 11. `rgb` holds
+ * (RMN_EXPORTS + RMN_EXPORTS_DOF) images; *count receives how many were
+ * written. */
+#define RMN_EXPORTS 20
+#define RMN_EXPORTS_DOF 5
+rmn_status rmn_export_set(const rmn_image* image, const rmn_post_args* args, float* rgb, int32_t* count,
+                          void* stream);
+/* The file tag of export k ("DiffuseColor", ..., "Filter_DepthFieldBlur_Bloom_FXAA") and its shade
+ * options; NULL / -1 out of range. */
+const char* rmn_export_tag(int32_t k);
+int32_t rmn_export_options(int32_t k);
 
 #ifdef __cplusplus
 }

@@ -29,6 +29,11 @@ class SceneDesc(C.Structure):
                 ("textures", C.c_void_p), ("material_textures", C.c_void_p)]
 
 
+class PostArgs(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("exposure", C.c_float), ("focus", C.c_float),
+                ("CoC", C.c_float), ("camera_position", C.c_float * 3)]
+
+
 class Texture(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("channels", C.c_int32), ("texels", C.c_void_p)]
 
@@ -98,6 +103,13 @@ SIGNATURES = {
     "rmn_compose_noalloc": (C.c_int, [C.POINTER(Image), C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p,
                                       C.c_void_p]),
     "rmn_fxaa": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_void_p]),
+    "rmn_post_process": (C.c_int, [C.POINTER(Image), C.POINTER(PostArgs), C.c_int32, C.c_void_p, C.c_void_p]),
+    "rmn_spatial_clamp": (C.c_int, [C.POINTER(Image), C.c_int32, C.c_int32, C.c_void_p]),
+    "rmn_filter": (C.c_int, [C.POINTER(Image), C.c_int32, C.c_int32, C.c_void_p]),
+    "rmn_export_set": (C.c_int, [C.POINTER(Image), C.POINTER(PostArgs), C.c_void_p, C.POINTER(C.c_int32),
+                                 C.c_void_p]),
+    "rmn_export_tag": (C.c_char_p, [C.c_int32]),
+    "rmn_export_options": (C.c_int32, [C.c_int32]),
 }
 
 _lib = None

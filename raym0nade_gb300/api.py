@@ -36,6 +36,7 @@ Full = 63
 Direct_Diffuse, Direct_Specular = DirectLight | Diffuse, DirectLight | Specular
 Indirect_Diffuse, Indirect_Specular = IndirectLight | Diffuse, IndirectLight | Specular
 GAMMA = 4096
+EXPORTS, EXPORTS_DOF = 20, 5  # RMN_EXPORTS, RMN_EXPORTS_DOF
 GBUFFER_FLOATS = 21
 
 
@@ -239,12 +240,52 @@ class Photo:
                                        _ptr(out), _stream(stream)), "rmn_compose")
         return out
 
-    def postProcessing(self, options: int):
-        """Photo::postProcessing without bloom / depth of field: shade,
-        gammaCorrection, then FXAA if requested (src/image.cpp:470-479)."""
-        if options & (DoBloom | DoDepthFieldBlur):
-            raise RmnError(4, "Photo.postProcessing: bloom and depth of field are not on the GPU path")
-        return self.shade(options | GAMMA)
+    # Photo's depth-of-field state (include/image.h:36-38)
+    focus, CoC, cameraPosition = 1.0, 0.0, (0.0, 0.0, 0.0)
+
+    def _post_args(self) -> "_lib.PostArgs":
+        return _lib.PostArgs(self.width, self.height, float(self.exposure), float(self.focus), float(self.CoC),
+                             (C.c_float * 3)(*self.cameraPosition))
+
+    def post_process(self, options: int, out=None, stream=None):
+        """rmn_post_process: Photo::shade(options), depth of field
+        (DoDepthFieldBlur) and bloom (DoBloom), gammaCorrection with GAMMA,
+        FXAA with DoFXAA."""
+        if out is None:
+            out = _empty_like_device(self.Gbuffer, (self.height, self.width, 3), np.float32)
+        img, a = self.c_image(), self._post_args()
+        _check(_lib.load().rmn_post_process(C.byref(img), C.byref(a), int(options), _ptr(out), _stream(stream)),
+               "rmn_post_process")
+        return out
+
+    def postProcessing(self, options: int, out=None, stream=None):
+        """Photo::postProcessing (src/image.cpp:470-479): shade, depth of
+        field, bloom, gammaCorrection, FXAA, as `options` asks."""
+        return self.post_process(options | GAMMA, out, stream)
+
+    def spatialClamp(self, stream=None):
+        """Photo::spatialClamp (src/image.cpp:77-82), in place."""
+        img = self.c_image()
+        _check(_lib.load().rmn_spatial_clamp(C.byref(img), self.width, self.height, _stream(stream)),
+               "rmn_spatial_clamp")
+
+    def filter(self, stream=None):
+        """Photo::filter (src/image.cpp:201-213), in place."""
+        img = self.c_image()
+        _check(_lib.load().rmn_filter(C.byref(img), self.width, self.height, _stream(stream)), "rmn_filter")
+
+    def export_set(self, out=None, stream=None):
+        """rmn_export_set: the images render_multiThread exports
+        (src/render.cpp:641-674) as {tag: (h, w, 3)}; the radiance buffers are
+        clamped and filtered on the way, as there."""
+        lib = _lib.load()
+        n = EXPORTS + EXPORTS_DOF
+        if out is None:
+            out = _empty_like_device(self.Gbuffer, (n, self.height, self.width, 3), np.float32)
+        img, a, cnt = self.c_image(), self._post_args(), C.c_int32(0)
+        _check(lib.rmn_export_set(C.byref(img), C.byref(a), _ptr(out), C.byref(cnt), _stream(stream)),
+               "rmn_export_set")
+        return {lib.rmn_export_tag(k).decode(): out[k] for k in range(cnt.value)}
 
     @staticmethod
     def save(rgb, path: str) -> None:

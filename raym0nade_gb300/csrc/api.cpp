@@ -117,6 +117,112 @@ void clear_error() { g_error[0] = 0; }
 
 using namespace rmn;
 
+namespace {
+
+// Photo::postProcessing(options) on device buffers into `out` (device,
+// 3 floats per pixel): shade, depth of field, bloom, gamma, FXAA.
+rmn_status post_device(const float* dd, const float* ds, const float* id, const float* is, const float* gb,
+                       const rmn_post_args& a, int options, float* out, cudaStream_t st) {
+  const int W = a.width, H = a.height;
+  const size_t npx = (size_t)W * H;
+  const bool fx = (options & RMN_SHADE_FXAA) != 0;
+  const bool dof = (options & RMN_SHADE_DEPTH_OF_FIELD) != 0, bloom = (options & RMN_SHADE_BLOOM) != 0;
+  float* tmp = nullptr;
+  if (fx) {
+    cudaError_t e = cudaMallocAsync(&tmp, npx * 12, st);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (post)");
+  }
+  float* target = fx ? tmp : out;
+  // the gamma of compose itself only when nothing runs between shade and gamma
+  const int copt = (dof || bloom) ? (options & ~RMN_SHADE_GAMMA) : options;
+  cudaError_t e = launch_compose(dd, ds, id, is, gb, W, H, a.exposure, copt, target, st);
+  if (e == cudaSuccess && dof) e = launch_dof(target, gb, W, H, a.focus, a.CoC, a.camera_position, st);
+  if (e == cudaSuccess && bloom) e = launch_bloom(target, W, H, st);
+  if (e == cudaSuccess && (dof || bloom) && (options & RMN_SHADE_GAMMA)) e = launch_gamma(target, (int)npx, st);
+  if (e == cudaSuccess && fx) e = launch_fxaa(target, out, W, H, st);
+  if (tmp) cudaFreeAsync(tmp, st);
+  if (e != cudaSuccess) return cuda_fail(e, "post-processing launch");
+  return RMN_OK;
+}
+
+// The radiance buffers and G-buffer of an rmn_image, staged in (and, for
+// the in-place passes, back out).
+struct ImageArgs {
+  Arg b[4], gb;
+  rmn_status stage(const rmn_image* img, size_t npx, cudaStream_t st, bool need_gbuffer) {
+    const float* src[4] = {img->radiance_Dd, img->radiance_Ds, img->radiance_Id, img->radiance_Is};
+    rmn_status r = RMN_OK;
+    for (int k = 0; k < 4 && r == RMN_OK; ++k) r = stage_in(src[k], npx * 16, st, &b[k]);
+    if (r == RMN_OK && need_gbuffer) r = stage_in(img->gbuffer, npx * RMN_GBUFFER_FLOATS * 4, st, &gb);
+    return r;
+  }
+  rmn_status write_back(const rmn_image* img, size_t npx, cudaStream_t st) {
+    float* dst[4] = {img->radiance_Dd, img->radiance_Ds, img->radiance_Id, img->radiance_Is};
+    rmn_status r = RMN_OK;
+    for (int k = 0; k < 4 && r == RMN_OK; ++k) r = finish_out(dst[k], npx * 16, st, b[k]);
+    return r;
+  }
+  float* const* bufs() {
+    for (int k = 0; k < 4; ++k) p[k] = static_cast<float*>(b[k].dev);
+    return p;
+  }
+  void release_all(cudaStream_t st) {
+    for (Arg& a : b) release(a, st);
+    release(gb, st);
+  }
+  float* p[4] = {};
+};
+
+bool image_complete(const rmn_image* img, bool need_gbuffer) {
+  return img && img->radiance_Dd && img->radiance_Ds && img->radiance_Id && img->radiance_Is &&
+         (!need_gbuffer || img->gbuffer);
+}
+
+// render_multiThread's exports (src/render.cpp:641-674), in order.
+struct ExportSpec {
+  const char* tag;
+  int options;
+};
+constexpr int kFull = RMN_SHADE_FULL, kFX = RMN_SHADE_FXAA, kBl = RMN_SHADE_BLOOM, kDoF = RMN_SHADE_DEPTH_OF_FIELD;
+const ExportSpec kExports[RMN_EXPORTS + RMN_EXPORTS_DOF] = {
+    {"DiffuseColor", RMN_SHADE_BASECOLOR},
+    {"DiffuseColor_FXAA", RMN_SHADE_BASECOLOR | kFX},
+    {"shapeNormal", RMN_SHADE_SHAPE_NORMAL},
+    {"surfaceNormal", RMN_SHADE_SURFACE_NORMAL},
+    {"Direct_Diffuse", RMN_SHADE_DIRECT | RMN_SHADE_DIFFUSE},  // after spatialClamp
+    {"Direct_Specular", RMN_SHADE_DIRECT | RMN_SHADE_SPECULAR},
+    {"Indirect_Diffuse", RMN_SHADE_INDIRECT | RMN_SHADE_DIFFUSE},
+    {"Indirect_Specular", RMN_SHADE_INDIRECT | RMN_SHADE_SPECULAR},
+    {"Raw", kFull},
+    {"Raw_Bloom", kFull | kBl},
+    {"Raw_FXAA", kFull | kFX},
+    {"Raw_Bloom_FXAA", kFull | kBl | kFX},
+    {"Direct_Diffuse_Filter", RMN_SHADE_DIRECT | RMN_SHADE_DIFFUSE},  // after filter
+    {"Direct_Specular_Filter", RMN_SHADE_DIRECT | RMN_SHADE_SPECULAR},
+    {"Indirect_Diffuse_Filter", RMN_SHADE_INDIRECT | RMN_SHADE_DIFFUSE},
+    {"Indirect_Specular_Filter", RMN_SHADE_INDIRECT | RMN_SHADE_SPECULAR},
+    {"Filter", kFull},
+    {"Filter_Bloom", kFull | kBl},
+    {"Filter_FXAA", kFull | kFX},
+    {"Filter_Bloom_FXAA", kFull | kBl | kFX},
+    {"BaseColor_DepthFieldBlur", RMN_SHADE_BASECOLOR | kDoF},  // when CoC > eps
+    {"Filter_DepthFieldBlur", kFull | kDoF},
+    {"Filter_DepthFieldBlur_Bloom", kFull | kDoF | kBl},
+    {"Filter_DepthFieldBlur_FXAA", kFull | kDoF | kFX},
+    {"Filter_DepthFieldBlur_Bloom_FXAA", kFull | kDoF | kBl | kFX},
+};
+
+rmn_status check_post(const rmn_post_args* a) {
+  if (!a || a->width <= 0 || a->height <= 0 || a->height > 65535 || (int64_t)a->width * a->height > (1LL << 30))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "post arguments: image size out of range (height <= 65535)");
+  // a finite, non-negative CoC keeps every blur radius in [0, 96]
+  if (!(a->CoC >= 0.0f) || !std::isfinite(a->CoC))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "post arguments: CoC must be finite and >= 0");
+  return RMN_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 const char* rmn_last_error(void) { return g_error; }
@@ -226,9 +332,119 @@ rmn_status rmn_fxaa(const float* rgb_in, float* rgb_out, int32_t width, int32_t 
   return r;
 }
 
+rmn_status rmn_post_process(const rmn_image* image, const rmn_post_args* args, int32_t options, float* rgb,
+                            void* stream) {
+  clear_error();
+  rmn_status r = check_post(args);
+  if (r != RMN_OK) return r;
+  if (!rgb || !image_complete(image, true))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_post_process needs all four radiance buffers, the G-buffer and rgb");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t npx = (size_t)args->width * args->height;
+  ImageArgs in;
+  Arg o;
+  r = in.stage(image, npx, st, true);
+  if (r == RMN_OK) r = stage_out(rgb, npx * 12, st, &o);
+  if (r == RMN_OK) {
+    float* const* b = in.bufs();
+    r = post_device(b[0], b[1], b[2], b[3], static_cast<const float*>(in.gb.dev), *args, options,
+                    static_cast<float*>(o.dev), st);
+  }
+  if (r == RMN_OK) r = finish_out(rgb, npx * 12, st, o);
+  in.release_all(st);
+  release(o, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
+  return r;
+}
+
+rmn_status rmn_spatial_clamp(const rmn_image* image, int32_t width, int32_t height, void* stream) {
+  clear_error();
+  if (!image_complete(image, false) || width <= 0 || height <= 0 || height > 65535)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_spatial_clamp needs the four radiance buffers and a size");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t npx = (size_t)width * height;
+  ImageArgs in;
+  rmn_status r = in.stage(image, npx, st, false);
+  if (r == RMN_OK) {
+    cudaError_t e = launch_spatial_clamp(in.bufs(), width, height, st);
+    if (e != cudaSuccess) r = cuda_fail(e, "spatial clamp launch");
+  }
+  if (r == RMN_OK) r = in.write_back(image, npx, st);
+  in.release_all(st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
+  return r;
+}
+
+rmn_status rmn_filter(const rmn_image* image, int32_t width, int32_t height, void* stream) {
+  clear_error();
+  if (!image_complete(image, true) || width <= 0 || height <= 0 || height > 65535)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_filter needs the four radiance buffers, the G-buffer and a size");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t npx = (size_t)width * height;
+  ImageArgs in;
+  rmn_status r = in.stage(image, npx, st, true);
+  if (r == RMN_OK) {
+    cudaError_t e = launch_filter(in.bufs(), static_cast<const float*>(in.gb.dev), width, height, st);
+    if (e != cudaSuccess) r = cuda_fail(e, "filter launch");
+  }
+  if (r == RMN_OK) r = in.write_back(image, npx, st);
+  in.release_all(st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
+  return r;
+}
+
+rmn_status rmn_export_set(const rmn_image* image, const rmn_post_args* args, float* rgb, int32_t* count,
+                          void* stream) {
+  clear_error();
+  rmn_status r = check_post(args);
+  if (r != RMN_OK) return r;
+  if (!rgb || !count || !image_complete(image, true))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_export_set needs the radiance buffers, the G-buffer, rgb and count");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const size_t npx = (size_t)args->width * args->height;
+  const int n = RMN_EXPORTS + (args->CoC > RMN_EPS ? RMN_EXPORTS_DOF : 0);
+  ImageArgs in;
+  Arg o;
+  r = in.stage(image, npx, st, true);
+  if (r == RMN_OK) r = stage_out(rgb, npx * 12 * n, st, &o);
+  float* const* b = in.bufs();
+  const float* gb = static_cast<const float*>(in.gb.dev);
+  for (int k = 0; k < n && r == RMN_OK; ++k) {
+    cudaError_t e = cudaSuccess;
+    if (k == 4) e = launch_spatial_clamp(b, args->width, args->height, st);  // photo.spatialClamp()
+    if (k == 12) e = launch_filter(b, gb, args->width, args->height, st);    // photo.filter()
+    if (e != cudaSuccess) {
+      r = cuda_fail(e, "export pass launch");
+      break;
+    }
+    r = post_device(b[0], b[1], b[2], b[3], gb, *args, kExports[k].options | RMN_SHADE_GAMMA,
+                    static_cast<float*>(o.dev) + 3 * npx * k, st);
+  }
+  if (r == RMN_OK) r = finish_out(rgb, npx * 12 * n, st, o);
+  if (r == RMN_OK) r = in.write_back(image, npx, st);
+  in.release_all(st);
+  release(o, st);
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (r == RMN_OK && e != cudaSuccess) r = cuda_fail(e, "stream synchronize");
+  *count = r == RMN_OK ? n : 0;
+  return r;
+}
+
+const char* rmn_export_tag(int32_t k) {
+  return (k >= 0 && k < RMN_EXPORTS + RMN_EXPORTS_DOF) ? kExports[k].tag : nullptr;
+}
+
+int32_t rmn_export_options(int32_t k) {
+  return (k >= 0 && k < RMN_EXPORTS + RMN_EXPORTS_DOF) ? (kExports[k].options | RMN_SHADE_GAMMA) : -1;
+}
+
 rmn_status rmn_compose(const rmn_image* image, int32_t width, int32_t height, float exposure, int32_t options,
                        float* rgb, void* stream) {
   clear_error();
+  options &= ~(RMN_SHADE_BLOOM | RMN_SHADE_DEPTH_OF_FIELD);  // rmn_post_process's passes
   if (!image || !rgb || width <= 0 || height <= 0 || !image->gbuffer || !image->radiance_Dd || !image->radiance_Ds ||
       !image->radiance_Id || !image->radiance_Is)
     return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_compose needs all four radiance buffers and the G-buffer");

@@ -1,0 +1,464 @@
+// Photo's post passes beside compose and FXAA (src/image.cpp:30-356):
+// spatialClamp, the a-trous filter, bloom and the depth-of-field blur, on
+// the device, each pass restating the reference's float operations in the
+// reference's order.
+//
+//  * spatialClamp: a row kernel (7-tap blur of luminance) and a column kernel
+//    (7-tap blur, clamp in place), the four buffers in one grid (z).
+//  * filter: filterVar and five a-trous passes, ping-ponging between the
+//    caller's buffers and a scratch copy (the sixth write lands back in the
+//    caller's); the G-buffer fields the edge-stopping weight reads are packed
+//    once into 48 bytes per pixel.
+//  * bloom: the bright part, then five a-trous passes, each adding its
+//    result to the image (ping-pong scratch).
+//  * depth of field: the reference scatters pixels in stable depth order and
+//    every receiving pixel stops taking weight at 0.99, so what a pixel
+//    receives depends on the order of its senders. That order is per
+//    receiver: the blur is a gather in which each receiver folds its
+//    senders in the reference's order. The host sorts the depths with the
+//    same std::stable_sort (ties and all) and lists the pixels of each tile
+//    of T x T pixels (T >= the largest radius) in that order; a receiver
+//    merges the lists of its 3 x 3 tiles by rank, so it meets every sender
+//    that can reach it, in order.
+#include <algorithm>
+#include <cmath>
+#include <vector>
+
+#include "rmn_host.h"
+
+namespace {
+
+constexpr float kLumR = 0.3f, kLumG = 0.6f, kLumB = 0.1f;
+__device__ __forceinline__ float lum3(float3 v) { return dot3(v, f3(kLumR, kLumG, kLumB)); }
+__device__ __forceinline__ float3 xyz(float4 v) { return f3(v.x, v.y, v.z); }
+
+// ------------------------------------------------------- spatialClamp -----
+__constant__ float c_h7[7] = {0.03125f, 0.109375f, 0.21875f, 0.28125f, 0.21875f, 0.109375f, 0.03125f};
+
+struct Bufs {
+  float4* b[4];  // Dd, Ds, Id, Is (radiance, Var)
+};
+
+__global__ void clamp_rows_kernel(Bufs in, float* __restrict__ b1, int W, int H) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  if (x >= W) return;
+  const float4* r = in.b[z] + (size_t)y * W;
+  float sum = 0.0f;
+  for (int dx = -3; dx <= 3; ++dx) {
+    int nx = x + dx;
+    if (nx >= 0 && nx < W) sum += lum3(xyz(r[nx])) * c_h7[dx + 3];
+  }
+  b1[(size_t)z * W * H + (size_t)y * W + x] = sum;
+}
+
+__global__ void clamp_cols_kernel(Bufs io, const float* __restrict__ b1, int W, int H) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  if (x >= W) return;
+  const float* c = b1 + (size_t)z * W * H;
+  float sum = 0.0f;
+  for (int dy = -3; dy <= 3; ++dy) {
+    int ny = y + dy;
+    if (ny >= 0 && ny < H) sum += c[(size_t)ny * W + x] * c_h7[dy + 3];
+  }
+  float4& p = io.b[z][(size_t)y * W + x];
+  const float l = lum3(xyz(p));
+  const float h3 = c_h7[3];
+  const float bl = sum - h3 * h3 * l;
+  if (l > 36.0f * bl) {
+    const float s = bl / (l + RMN_EPS) / (1.0f - h3 * h3);
+    p.x *= s;
+    p.y *= s;
+    p.z *= s;
+  }
+}
+
+// ------------------------------------------------------------- filter -----
+// Guide record of a pixel for the edge-stopping weight (48 B):
+// (position, metallic), (surface normal, opacity), (shape normal, roughness).
+__global__ void guide_kernel(const float* __restrict__ gbuf, float4* __restrict__ guide, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* g = gbuf + (size_t)RMN_GBUFFER_FLOATS * i;
+  guide[3 * (size_t)i] = make_float4(g[6], g[7], g[8], g[16]);
+  guide[3 * (size_t)i + 1] = make_float4(g[12], g[13], g[14], g[17]);
+  guide[3 * (size_t)i + 2] = make_float4(g[9], g[10], g[11], g[15]);
+}
+
+// filterVar, src/image.cpp:84-108.
+__global__ void filter_var_kernel(Bufs in, Bufs out, int W, int H) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  if (x >= W) return;
+  const float h[3] = {0.25f, 0.5f, 0.25f};
+  const float4* r = in.b[z];
+  float3 E = f3(0.0f);
+  float E2 = 0.0f, V = 0.0f;
+  for (int dy = -1; dy <= 1; ++dy)
+    for (int dx = -1; dx <= 1; ++dx) {
+      int nx = x + dx, ny = y + dy;
+      if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+      const float4 q = r[(size_t)ny * W + nx];
+      const float wt = h[dx + 1] * h[dy + 1];
+      E += xyz(q) * wt;
+      E2 += dot3(xyz(q), xyz(q)) * wt;
+      V += q.w * wt;
+    }
+  const size_t i = (size_t)y * W + x;
+  const float4 p = r[i];
+  out.b[z][i] = make_float4(p.x, p.y, p.z, V + E2 - dot3(E, E));
+}
+
+// getWeight, src/image.cpp:110-158 (sigma_z = sigma_l = sigma_m = 1,
+// sigma_n = 1024, eps 1e-2, eps_r 4e-2; every pixel's specular is the
+// HitInfo default 0.04, so its difference is 0).
+__device__ __forceinline__ float edge_weight(const float4* __restrict__ guide, size_t ip, size_t iq, float4 Lp,
+                                             float4 Lq, bool specular) {
+  const float4 q0 = guide[3 * iq], q1 = guide[3 * iq + 1];
+  if (!any_finite3(xyz(q0))) return 0.0f;
+  const float4 p0 = guide[3 * ip], p1 = guide[3 * ip + 1], p2 = guide[3 * ip + 2];
+  const float d = dot3(xyz(p1), xyz(q1));
+  float w = powf(0.0f < d ? d : 0.0f, 1024.0f);
+  if (w < 1e-6f) return 0.0f;
+  float k = 0.0f;
+  const float3 dir = norm3(xyz(q0) - xyz(p0));
+  const float st = fabsf(dot3(xyz(p2), dir));
+  const float tt = st / (sqrtf(1.0f - st * st) + RMN_EPS);
+  k += -tt / 1.0f;
+  const float rd = len3(xyz(Lp) - xyz(Lq)) / (1.0f * sqrtf(Lp.w) + 1e-2f);
+  k += -rd;
+  const float md = len3(f3(p0.w - q0.w, 0.04f - 0.04f, p1.w - q1.w));
+  k += -md / 1.0f;
+  if (k < -7.5f) return 0.0f;
+  w *= expf(k);
+  if (specular) w *= p2.w < 4e-2f ? 4e-2f : p2.w;
+  if (!isfinite(w)) return 0.0f;
+  return w;
+}
+
+// filterRadiance(..., step), src/image.cpp:160-199.
+__global__ void filter_pass_kernel(Bufs in, Bufs out, const float4* __restrict__ guide, int W, int H, int step) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y, z = blockIdx.z;
+  if (x >= W) return;
+  const float h[5] = {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f};
+  const bool specular = (z & 1) != 0;  // Ds, Is
+  const float4* r = in.b[z];
+  const size_t i = (size_t)y * W + x;
+  float3 rb = f3(0.0f);
+  float vb = 0.0f;
+  if (any_finite3(xyz(guide[3 * i]))) {
+    const float4 Lp = r[i];
+    float ws = 0.0f;
+    for (int dy = -2; dy <= 2; ++dy)
+      for (int dx = -2; dx <= 2; ++dx) {
+        int nx = x + dx * step, ny = y + dy * step;
+        if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+        float wt = h[dx + 2] * h[dy + 2];
+        const size_t j = (size_t)ny * W + nx;
+        const float4 Lq = r[j];
+        if (dx != 0 || dy != 0) wt *= edge_weight(guide, i, j, Lp, Lq, specular);
+        ws += wt;
+        rb += xyz(Lq) * wt;
+        vb += Lq.w * wt * wt;
+      }
+    rb = rb / ws;
+    vb /= ws * ws;
+  }
+  out.b[z][i] = make_float4(rb.x, rb.y, rb.z, vb);
+}
+
+// --------------------------------------------------------------- bloom ----
+__global__ void bloom_init_kernel(const float* __restrict__ rgb, float3* __restrict__ bc, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float3 p = f3(rgb[3 * (size_t)i], rgb[3 * (size_t)i + 1], rgb[3 * (size_t)i + 2]);
+  const float c = lum3(p);
+  float3 b = f3(0.0f);
+  if (!(c < 1.0f)) {
+    b = p / powf(c, 0.65f);
+    b.x = b.x - 1.0f < 0.0f ? 0.0f : b.x - 1.0f;  // std::max(v - 1, 0)
+    b.y = b.y - 1.0f < 0.0f ? 0.0f : b.y - 1.0f;
+    b.z = b.z - 1.0f < 0.0f ? 0.0f : b.z - 1.0f;
+  }
+  bc[i] = b;
+}
+
+// One bloom pass: out = blur(in, step); rgb += out / 6.
+__global__ void bloom_pass_kernel(const float3* __restrict__ in, float3* __restrict__ out, float* __restrict__ rgb,
+                                  int W, int H, int step) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= W) return;
+  const float h[5] = {0.0625f, 0.25f, 0.375f, 0.25f, 0.0625f};
+  float3 col = f3(0.0f);
+  for (int ky = -2; ky <= 2; ++ky)
+    for (int kx = -2; kx <= 2; ++kx) {
+      int nx = x + kx * step, ny = y + ky * step;
+      if (nx < 0 || nx >= W || ny < 0 || ny >= H) continue;
+      col += in[(size_t)ny * W + nx] * h[ky + 2] * h[kx + 2];
+    }
+  const size_t i = (size_t)y * W + x;
+  out[i] = col;
+  const float3 a = col / 6.0f;
+  rgb[3 * i] += a.x;
+  rgb[3 * i + 1] += a.y;
+  rgb[3 * i + 2] += a.z;
+}
+
+// ----------------------------------------------------- depth of field -----
+// float -> int of the radii: truncation, 0 for NaN (CUDA's and aarch64's
+// conversion; in C++ the conversion of NaN is undefined).
+__host__ __device__ __forceinline__ int dof_int(float v) {
+  if (v != v) return 0;
+  if (v >= 2147483647.0f) return 2147483647;
+  if (v <= -2147483648.0f) return (-2147483647 - 1);
+  return (int)v;
+}
+__host__ __device__ __forceinline__ float dof_coc(float coc, float focus, float depth) {
+  const float c = coc * fabsf(1.0f - focus / depth) + RMN_EPS;
+  return 96.0f < c ? 96.0f : c;  // std::min(..., MaxCoC)
+}
+
+__global__ void depth_kernel(const float* __restrict__ gbuf, float3 cam, float* __restrict__ depth, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* g = gbuf + (size_t)RMN_GBUFFER_FLOATS * i;
+  depth[i] = len3(f3(g[6], g[7], g[8]) - cam);
+}
+
+// Per sending pixel: CoC0, its total weight (the reference's two loops per
+// row, inwards from the disc's edge until a weight reaches 1), radius.
+__global__ void dof_source_kernel(const float* __restrict__ depth, float coc, float focus, float4* __restrict__ src,
+                                  int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float c0 = dof_coc(coc, focus, depth[i]);
+  const int radius = dof_int(c0);
+  float tw = 0.0f;
+  for (int dy = -radius; dy <= radius; ++dy) {
+    const int xlen = dof_int(sqrtf(c0 * c0 - (float)(dy * dy)));
+    int xl, xr;
+    for (xl = -xlen; xl <= 0; xl++) {
+      float w = c0 - sqrtf((float)(xl * xl + dy * dy));
+      w = 1.0f < w ? 1.0f : w;
+      if (w == 1.0f) break;
+      tw += w;
+    }
+    for (xr = xlen; xr > 0; xr--) {
+      float w = c0 - sqrtf((float)(xr * xr + dy * dy));
+      w = 1.0f < w ? 1.0f : w;
+      if (w == 1.0f) break;
+      tw += w;
+    }
+    tw += (float)(xr - xl + 1);
+  }
+  src[i] = make_float4(c0, tw, __int_as_float(radius), 0.0f);
+}
+
+// The receiving pixel (x, y): its senders, in rank order, from the rank lists
+// of its 3 x 3 tiles.
+__global__ void dof_gather_kernel(const float* __restrict__ rgb, const float4* __restrict__ src,
+                                  const int* __restrict__ order, const int* __restrict__ tile_start,
+                                  const int* __restrict__ tile_rank, int W, int H, int T, int TW, int TH,
+                                  float* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= W) return;
+  const int tx = x / T, ty = y / T;
+  int head[9], end[9], cur[9];
+  int nl = 0;
+  for (int j = ty - 1; j <= ty + 1; ++j)
+    for (int i = tx - 1; i <= tx + 1; ++i) {
+      if (i < 0 || i >= TW || j < 0 || j >= TH) continue;
+      const int t = j * TW + i;
+      head[nl] = tile_start[t];
+      end[nl] = tile_start[t + 1];
+      cur[nl] = head[nl] < end[nl] ? tile_rank[head[nl]] : 0x7fffffff;
+      ++nl;
+    }
+  float3 blur = f3(0.0f);
+  float gained = 0.0f;
+  for (;;) {
+    int best = -1, br = 0x7fffffff;
+    for (int k = 0; k < nl; ++k)
+      if (cur[k] < br) {
+        br = cur[k];
+        best = k;
+      }
+    if (best < 0) break;
+    ++head[best];
+    cur[best] = head[best] < end[best] ? tile_rank[head[best]] : 0x7fffffff;
+    const int s = order[br];
+    const int sx = s % W, sy = s / W;
+    const int dx = x - sx, dy = y - sy;
+    const float4 sv = src[s];
+    const int radius = __float_as_int(sv.z);
+    if (dy < -radius || dy > radius) continue;
+    const float c0 = sv.x;
+    const int xlen = dof_int(sqrtf(c0 * c0 - (float)(dy * dy)));
+    if (dx < -xlen || dx > xlen) continue;
+    float w = c0 - sqrtf((float)(dx * dx + dy * dy));
+    w = (1.0f < w ? 1.0f : w) / sv.y;
+    if (w < RMN_EPS) continue;
+    if (gained + w > 0.99f) w = 0.99f - gained;
+    if (w < RMN_EPS) continue;
+    blur += f3(rgb[3 * (size_t)s], rgb[3 * (size_t)s + 1], rgb[3 * (size_t)s + 2]) * w;
+    gained += w;
+  }
+  const float3 o = blur / gained;
+  const size_t i = (size_t)y * W + x;
+  out[3 * i] = o.x;
+  out[3 * i + 1] = o.y;
+  out[3 * i + 2] = o.z;
+}
+
+__global__ void gamma_kernel(float* __restrict__ rgb, int n) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float3 p = f3(rgb[3 * (size_t)i], rgb[3 * (size_t)i + 1], rgb[3 * (size_t)i + 2]);
+  p = max3(p, f3(0.0f));
+  const float c = lum3(p);
+  if (c > 0.75f) p = p / c * (tanhf(3.0f * (c - 0.75f)) / 3.0f + 0.75f);
+  p = min3(p, f3(1.0f));
+  const float e = 1.0f / 2.2f;
+  rgb[3 * (size_t)i] = powf(p.x, e);
+  rgb[3 * (size_t)i + 1] = powf(p.y, e);
+  rgb[3 * (size_t)i + 2] = powf(p.z, e);
+}
+
+struct DevScratch {
+  std::vector<void*> ptrs;
+  cudaStream_t st;
+  cudaError_t err = cudaSuccess;
+  template <class T>
+  T* get(size_t count) {
+    void* p = nullptr;
+    if (err != cudaSuccess) return nullptr;
+    err = cudaMallocAsync(&p, count * sizeof(T) + 16, st);
+    if (err != cudaSuccess) return nullptr;
+    ptrs.push_back(p);
+    return static_cast<T*>(p);
+  }
+  ~DevScratch() {
+    for (void* p : ptrs) cudaFreeAsync(p, st);
+  }
+};
+
+dim3 row_grid(int W, int H, int z = 1) { return dim3((W + 127) / 128, H, z); }
+
+}  // namespace
+
+namespace rmn {
+
+cudaError_t launch_spatial_clamp(float* const bufs[4], int W, int H, cudaStream_t st) {
+  DevScratch sc{{}, st};
+  float* b1 = sc.get<float>((size_t)4 * W * H);
+  if (sc.err != cudaSuccess) return sc.err;
+  Bufs b;
+  for (int k = 0; k < 4; ++k) b.b[k] = reinterpret_cast<float4*>(bufs[k]);
+  clamp_rows_kernel<<<row_grid(W, H, 4), 128, 0, st>>>(b, b1, W, H);
+  clamp_cols_kernel<<<row_grid(W, H, 4), 128, 0, st>>>(b, b1, W, H);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_filter(float* const bufs[4], const float* gbuf, int W, int H, cudaStream_t st) {
+  const size_t n = (size_t)W * H;
+  DevScratch sc{{}, st};
+  float4* guide = sc.get<float4>(3 * n);
+  float4* tmp = sc.get<float4>(4 * n);
+  if (sc.err != cudaSuccess) return sc.err;
+  Bufs A, B;
+  for (int k = 0; k < 4; ++k) {
+    A.b[k] = reinterpret_cast<float4*>(bufs[k]);
+    B.b[k] = tmp + k * n;
+  }
+  guide_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(gbuf, guide, (int)n);
+  filter_var_kernel<<<row_grid(W, H, 4), 128, 0, st>>>(A, B, W, H);
+  // passes of step 1, 2, 4, 8, 16: B -> A -> B -> A -> B -> A
+  bool toA = true;
+  for (int step = 1; step <= 16; step *= 2) {
+    if (toA) filter_pass_kernel<<<row_grid(W, H, 4), 128, 0, st>>>(B, A, guide, W, H, step);
+    else filter_pass_kernel<<<row_grid(W, H, 4), 128, 0, st>>>(A, B, guide, W, H, step);
+    toA = !toA;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bloom(float* rgb, int W, int H, cudaStream_t st) {
+  const size_t n = (size_t)W * H;
+  DevScratch sc{{}, st};
+  float3* a = sc.get<float3>(n);
+  float3* b = sc.get<float3>(n);
+  if (sc.err != cudaSuccess) return sc.err;
+  bloom_init_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(rgb, a, (int)n);
+  for (int step = 1; step <= 16; step *= 2) {
+    bloom_pass_kernel<<<row_grid(W, H), 128, 0, st>>>(a, b, rgb, W, H, step);
+    std::swap(a, b);
+  }
+  return cudaGetLastError();
+}
+
+// Depth of field in place on rgb (device). Synchronises `st` once: the
+// depth order is sorted on the host.
+cudaError_t launch_dof(float* rgb, const float* gbuf, int W, int H, float focus, float coc, const float cam[3],
+                       cudaStream_t st) {
+  const int n = W * H;
+  DevScratch sc{{}, st};
+  float* depth = sc.get<float>(n);
+  if (sc.err != cudaSuccess) return sc.err;
+  depth_kernel<<<(n + 255) / 256, 256, 0, st>>>(gbuf, f3(cam[0], cam[1], cam[2]), depth, n);
+  std::vector<float> hd(n);
+  cudaError_t e = cudaMemcpyAsync(hd.data(), depth, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  // Photo::depthFeildBlur's order: std::stable_sort of (x, y, depth) records
+  // in raster order by depth, with the reference's comparator.
+  struct PixelPos {
+    int x, y;
+    float depth;
+  };
+  std::vector<PixelPos> pix;
+  pix.reserve(n);
+  for (int y = 0; y < H; ++y)
+    for (int x = 0; x < W; ++x) pix.push_back({x, y, hd[(size_t)y * W + x]});
+  std::stable_sort(pix.begin(), pix.end(), [](const PixelPos& a, const PixelPos& b) { return a.depth < b.depth; });
+  int rmax = 0;
+  for (int i = 0; i < n; ++i) rmax = std::max(rmax, dof_int(dof_coc(coc, focus, hd[i])));
+  const int T = std::max(rmax, 8), TW = (W + T - 1) / T, TH = (H + T - 1) / T;
+  std::vector<int> order(n), tile_start((size_t)TW * TH + 1, 0), tile_rank(n);
+  for (int r = 0; r < n; ++r) {
+    const PixelPos& p = pix[r];
+    order[r] = p.y * W + p.x;
+    tile_start[(size_t)(p.y / T) * TW + p.x / T + 1]++;
+  }
+  for (size_t t = 0; t < (size_t)TW * TH; ++t) tile_start[t + 1] += tile_start[t];
+  {
+    std::vector<int> fill(tile_start.begin(), tile_start.end() - 1);
+    for (int r = 0; r < n; ++r) {
+      const PixelPos& p = pix[r];
+      tile_rank[fill[(size_t)(p.y / T) * TW + p.x / T]++] = r;  // ranks ascend within a tile
+    }
+  }
+  float4* src = sc.get<float4>(n);
+  int* d_order = sc.get<int>(n);
+  int* d_start = sc.get<int>(tile_start.size());
+  int* d_rank = sc.get<int>(n);
+  float* out = sc.get<float>((size_t)3 * n);
+  if (sc.err != cudaSuccess) return sc.err;
+  e = cudaMemcpyAsync(d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_start, tile_start.data(), sizeof(int) * tile_start.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_rank, tile_rank.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+  if (e != cudaSuccess) return e;
+  dof_source_kernel<<<(n + 255) / 256, 256, 0, st>>>(depth, coc, focus, src, n);
+  dof_gather_kernel<<<row_grid(W, H), 128, 0, st>>>(rgb, src, d_order, d_start, d_rank, W, H, T, TW, TH, out);
+  e = cudaMemcpyAsync(rgb, out, sizeof(float) * 3 * n, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return e;
+  // the host vectors above are read by the copies: wait for them
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) return e;
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gamma(float* rgb, int n, cudaStream_t st) {
+  gamma_kernel<<<(n + 255) / 256, 256, 0, st>>>(rgb, n);
+  return cudaGetLastError();
+}
+
+}  // namespace rmn

@@ -70,6 +70,13 @@ void batch_destroy(BatchState* b);
 rmn_status launch_adjoint(const rmn_scene* scene, const rmn_render_args& args, const float* gbuf, const int* dropped,
                           const float* dimg, float* dmat, cudaStream_t st);
 cudaError_t launch_fxaa(const float* in, float* out, int w, int h, cudaStream_t stream);
+// Post passes (photo.cu); bufs = Dd, Ds, Id, Is (4 floats per pixel).
+cudaError_t launch_spatial_clamp(float* const bufs[4], int w, int h, cudaStream_t st);
+cudaError_t launch_filter(float* const bufs[4], const float* gbuf, int w, int h, cudaStream_t st);
+cudaError_t launch_bloom(float* rgb, int w, int h, cudaStream_t st);
+cudaError_t launch_dof(float* rgb, const float* gbuf, int w, int h, float focus, float coc, const float cam[3],
+                       cudaStream_t st);
+cudaError_t launch_gamma(float* rgb, int n, cudaStream_t st);
 cudaError_t launch_compose(const float* dd, const float* ds, const float* id, const float* is, const float* gbuf,
                            int w, int h, float exposure, int options, float* rgb, cudaStream_t stream);
 
