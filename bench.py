@@ -335,7 +335,93 @@ def config_timings(args, stream, flush, barrier):
     out["heightfield"] = {"Mpaths_s": 1920 * 1080 * 256 / ms / 1e3, "ms": ms,
                           "workload": "2048^2 heightfield (8,380,418 tris), sky 2048x1024, 1920x1080, 256 spp, "
                                       "max depth 16, gamma + FXAA (rmn_render + rmn_compose)"}
+
+    # the export set of render_multiThread on the heightfield's buffers, with
+    # depth of field (25 images); the CPU restatement timed on a crop
+    hp.focus, hp.CoC, hp.cameraPosition = 120.0, 6.0, tuple(hcam.position)
+    keep = [x.clone() for x in (hp.radiance_Dd, hp.radiance_Ds, hp.radiance_Id, hp.radiance_Is)]
+    recs = records_from_photo(hp, 1920, 1080)
+    exports = torch.empty((25, 1080, 1920, 3), dtype=torch.float32, device="cuda")
+
+    def step_post():
+        for dst, src in zip((hp.radiance_Dd, hp.radiance_Ds, hp.radiance_Id, hp.radiance_Is), keep):
+            dst.copy_(src)
+        hp.export_set(out=exports, stream=stream)
+
+    ms = timeit(step_post, steps=max(1, min(args.steps, 3)))
+    cpu = post_cpu_sample(recs, hp, 240, 136)
+    out["post_exports"] = {"ms": ms, "Mpixels_s": 1920 * 1080 / ms / 1e3, "images": 25,
+                           "cpu_port_ms_per_Mpixel": cpu["ms_per_Mpixel"], "cpu_sample": cpu["sample"],
+                           "gpu_over_cpu": cpu["ms_per_Mpixel"] * 1920 * 1080 / 1e6 / ms,
+                           "workload": "render_multiThread's 25 exports of the 1920x1080 heightfield render "
+                                       "(spatialClamp, filter, bloom, depth of field CoC 6, gamma, FXAA; "
+                                       "rmn_export_set)"}
+    del hm, hp, exports, keep
+
+    room = api.Model(scenes.textured_room())
+    tcam = scenes.textured_camera(1024, 768, 64)
+    ta = api.RenderArgs.from_camera(tcam, seed=1)
+    tp = api.Photo(1024, 768)
+    ms = timeit(lambda: api.render(room, ta, tp, stream))
+    cpu = textured_cpu_sample()
+    out["textured"] = {"Mpaths_s": 1024 * 768 * 64 / ms / 1e3, "ms": ms,
+                       "cpu_port_Mpaths_s": cpu["Mpaths_s"], "cpu_sample": cpu["sample"],
+                       "workload": "textured room (diffuse / specular / emissive / normal-map textures with mip "
+                                   "chains, alpha-tested cutouts), 1024x768, 64 spp, max depth 16 (rmn_render)"}
     return out
+
+
+GB_TO_REC = [16, 17, 18, 19, 20, 21, 22, 23, 24, 25, 26, 27, 28, 29, 30, 31, 32, 33, 35, 36, 37]
+
+
+def records_from_photo(ph, w, h):
+    """The oracle's per-pixel records (h, w, 40) of a GPU Photo."""
+    import numpy as np
+    r = np.zeros((h * w, 40), np.float32)
+    for k, b in enumerate((ph.radiance_Dd, ph.radiance_Ds, ph.radiance_Id, ph.radiance_Is)):
+        r[:, 4 * k:4 * k + 4] = b.cpu().numpy()
+    r[:, GB_TO_REC] = ph.Gbuffer.cpu().numpy()
+    r[:, 34] = 0.04  # HitInfo::specular
+    return r.reshape(h, w, 40)
+
+
+def post_cpu_sample(recs, ph, cw, ch):
+    """The export sequence of the CPU restatement (single thread, as the
+    reference's Photo passes except filter's four threads) on a cw x ch crop."""
+    from oracle.bindings import OracleLib
+    from raym0nade_gb300 import api
+    port = OracleLib("port")
+    y0, x0 = (recs.shape[0] - ch) // 2, (recs.shape[1] - cw) // 2
+    crop = recs[y0:y0 + ch, x0:x0 + cw].copy()
+    post = dict(exposure=1.0, focus=ph.focus, coc=ph.CoC, camera=ph.cameraPosition)
+    lib = api._lib.load()
+    opts = [lib.rmn_export_options(k) & ~api.GAMMA for k in range(api.EXPORTS + api.EXPORTS_DOF)]
+    t0 = time.perf_counter()
+    r = crop
+    for k, o in enumerate(opts):
+        if k == 4:
+            r, _ = port.photo(r, 1)
+        if k == 12:
+            r, _ = port.photo(r, 2)
+        port.photo(r, 4, o, **post)
+    dt = (time.perf_counter() - t0) * 1e3
+    return {"ms_per_Mpixel": dt / (cw * ch / 1e6), "sample": f"{cw}x{ch} centre crop, 25 exports, 1 thread"}
+
+
+def textured_cpu_sample():
+    """The CPU restatement (all host threads) of the textured room on a
+    256x192 image at 64 spp."""
+    import os as _os
+    from oracle.bindings import OracleLib
+    from raym0nade_gb300 import scenes
+    port = OracleLib("port")
+    sc = port.scene(scenes.textured_room())
+    cam = scenes.textured_camera(256, 192, 64)
+    th = _os.cpu_count() or 8
+    t0 = time.perf_counter()
+    sc.render(cam, seed=1, mode=0, threads=th)
+    dt = time.perf_counter() - t0
+    return {"Mpaths_s": 256 * 192 * 64 / dt / 1e6, "sample": f"256x192, 64 spp, {th} threads"}
 
 
 def run_gpu(args, rank, world, dist):

@@ -120,9 +120,11 @@ using namespace rmn;
 namespace {
 
 // Photo::postProcessing(options) on device buffers into `out` (device,
-// 3 floats per pixel): shade, depth of field, bloom, gamma, FXAA.
+// 3 floats per pixel): shade, depth of field, bloom, gamma, FXAA. `plan`:
+// the depth-of-field plan of this G-buffer, or null to make one.
 rmn_status post_device(const float* dd, const float* ds, const float* id, const float* is, const float* gb,
-                       const rmn_post_args& a, int options, float* out, cudaStream_t st) {
+                       const rmn_post_args& a, int options, float* out, cudaStream_t st,
+                       const DofPlan* plan = nullptr) {
   const int W = a.width, H = a.height;
   const size_t npx = (size_t)W * H;
   const bool fx = (options & RMN_SHADE_FXAA) != 0;
@@ -136,7 +138,8 @@ rmn_status post_device(const float* dd, const float* ds, const float* id, const 
   // the gamma of compose itself only when nothing runs between shade and gamma
   const int copt = (dof || bloom) ? (options & ~RMN_SHADE_GAMMA) : options;
   cudaError_t e = launch_compose(dd, ds, id, is, gb, W, H, a.exposure, copt, target, st);
-  if (e == cudaSuccess && dof) e = launch_dof(target, gb, W, H, a.focus, a.CoC, a.camera_position, st);
+  if (e == cudaSuccess && dof)
+    e = plan ? dof_apply(plan, target, st) : launch_dof(target, gb, W, H, a.focus, a.CoC, a.camera_position, st);
   if (e == cudaSuccess && bloom) e = launch_bloom(target, W, H, st);
   if (e == cudaSuccess && (dof || bloom) && (options & RMN_SHADE_GAMMA)) e = launch_gamma(target, (int)npx, st);
   if (e == cudaSuccess && fx) e = launch_fxaa(target, out, W, H, st);
@@ -412,17 +415,21 @@ rmn_status rmn_export_set(const rmn_image* image, const rmn_post_args* args, flo
   if (r == RMN_OK) r = stage_out(rgb, npx * 12 * n, st, &o);
   float* const* b = in.bufs();
   const float* gb = static_cast<const float*>(in.gb.dev);
+  DofPlan* plan = nullptr;  // one depth order for the five depth-of-field exports
   for (int k = 0; k < n && r == RMN_OK; ++k) {
     cudaError_t e = cudaSuccess;
     if (k == 4) e = launch_spatial_clamp(b, args->width, args->height, st);  // photo.spatialClamp()
     if (k == 12) e = launch_filter(b, gb, args->width, args->height, st);    // photo.filter()
+    if (e == cudaSuccess && !plan && (kExports[k].options & RMN_SHADE_DEPTH_OF_FIELD))
+      e = dof_plan_create(gb, args->width, args->height, args->focus, args->CoC, args->camera_position, st, &plan);
     if (e != cudaSuccess) {
       r = cuda_fail(e, "export pass launch");
       break;
     }
     r = post_device(b[0], b[1], b[2], b[3], gb, *args, kExports[k].options | RMN_SHADE_GAMMA,
-                    static_cast<float*>(o.dev) + 3 * npx * k, st);
+                    static_cast<float*>(o.dev) + 3 * npx * k, st, plan);
   }
+  dof_plan_destroy(plan, st);
   if (r == RMN_OK) r = finish_out(rgb, npx * 12 * n, st, o);
   if (r == RMN_OK) r = in.write_back(image, npx, st);
   in.release_all(st);

@@ -15,11 +15,16 @@
 //    every receiving pixel stops taking weight at 0.99, so what a pixel
 //    receives depends on the order of its senders. That order is per
 //    receiver: the blur is a gather in which each receiver folds its
-//    senders in the reference's order. The host sorts the depths with the
-//    same std::stable_sort (ties and all) and lists the pixels of each tile
-//    of T x T pixels (T >= the largest radius) in that order; a receiver
-//    merges the lists of its 3 x 3 tiles by rank, so it meets every sender
-//    that can reach it, in order.
+//    senders in the reference's order. The pixels of each tile of T x T
+//    pixels (T >= the largest radius) are listed in that order with a sort
+//    key; a receiver merges the lists of its 3 x 3 tiles by key, so it meets
+//    every sender that can reach it, in order. Without NaN depths a stable
+//    sort by depth is the order by (depth, raster index), whose key is
+//    (depth bits, index): each tile ranks its own pixels on the device. A
+//    NaN depth (a pixel without a hit) compares false both ways in the
+//    reference's comparator, so its place depends on std::stable_sort's
+//    algorithm: then the host runs that very sort and the key is the rank.
+//    A plan (order, radii, weights) serves every blur of the same G-buffer.
 #include <algorithm>
 #include <cmath>
 #include <vector>
@@ -216,21 +221,27 @@ __host__ __device__ __forceinline__ float dof_coc(float coc, float focus, float 
   return 96.0f < c ? 96.0f : c;  // std::min(..., MaxCoC)
 }
 
-__global__ void depth_kernel(const float* __restrict__ gbuf, float3 cam, float* __restrict__ depth, int n) {
+// depth = length(position - camera); flags[0] |= a NaN depth.
+__global__ void depth_kernel(const float* __restrict__ gbuf, float3 cam, float* __restrict__ depth, int n,
+                             int* __restrict__ flags) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float* g = gbuf + (size_t)RMN_GBUFFER_FLOATS * i;
-  depth[i] = len3(f3(g[6], g[7], g[8]) - cam);
+  const float d = len3(f3(g[6], g[7], g[8]) - cam);
+  depth[i] = d;
+  if (d != d) atomicOr(&flags[0], 1);
 }
 
 // Per sending pixel: CoC0, its total weight (the reference's two loops per
 // row, inwards from the disc's edge until a weight reaches 1), radius.
+// flags[1] = max radius.
 __global__ void dof_source_kernel(const float* __restrict__ depth, float coc, float focus, float4* __restrict__ src,
-                                  int n) {
+                                  int n, int* __restrict__ flags) {
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float c0 = dof_coc(coc, focus, depth[i]);
   const int radius = dof_int(c0);
+  atomicMax(&flags[1], radius);
   float tw = 0.0f;
   for (int dy = -radius; dy <= radius; ++dy) {
     const int xlen = dof_int(sqrtf(c0 * c0 - (float)(dy * dy)));
@@ -252,16 +263,40 @@ __global__ void dof_source_kernel(const float* __restrict__ depth, float coc, fl
   src[i] = make_float4(c0, tw, __int_as_float(radius), 0.0f);
 }
 
-// The receiving pixel (x, y): its senders, in rank order, from the rank lists
-// of its 3 x 3 tiles.
-__global__ void dof_gather_kernel(const float* __restrict__ rgb, const float4* __restrict__ src,
-                                  const int* __restrict__ order, const int* __restrict__ tile_start,
-                                  const int* __restrict__ tile_rank, int W, int H, int T, int TW, int TH,
-                                  float* __restrict__ out) {
+// Tile t = (tx, ty) of a T-grid covers x in [tx T, min(W, tx T + T)) and
+// likewise y; its list occupies [tile_start[t], tile_start[t + 1]).
+__global__ void dof_rank_kernel(const float* __restrict__ depth, const int* __restrict__ tile_start, int W, int H,
+                                int T, int TW, unsigned long long* __restrict__ key, int* __restrict__ pix) {
   const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
   if (x >= W) return;
   const int tx = x / T, ty = y / T;
-  int head[9], end[9], cur[9];
+  const int x0 = tx * T, y0 = ty * T, x1 = min(W, x0 + T), y1 = min(H, y0 + T);
+  const int p = y * W + x;
+  const unsigned long long kp = ((unsigned long long)__float_as_uint(depth[p]) << 32) | (unsigned)p;
+  int rank = 0;
+  for (int qy = y0; qy < y1; ++qy)
+    for (int qx = x0; qx < x1; ++qx) {
+      const int q = qy * W + qx;
+      const unsigned long long kq = ((unsigned long long)__float_as_uint(depth[q]) << 32) | (unsigned)q;
+      rank += kq < kp ? 1 : 0;
+    }
+  const int slot = tile_start[ty * TW + tx] + rank;
+  key[slot] = kp;
+  pix[slot] = p;
+}
+
+// The receiving pixel (x, y): its senders, in the reference's order, from the
+// key-sorted lists of its 3 x 3 tiles.
+__global__ void dof_gather_kernel(const float* __restrict__ rgb, const float4* __restrict__ src,
+                                  const int* __restrict__ tile_start, const unsigned long long* __restrict__ key,
+                                  const int* __restrict__ pix, int W, int H, int T, int TW, int TH,
+                                  float* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
+  if (x >= W) return;
+  const unsigned long long kNone = ~0ull;
+  const int tx = x / T, ty = y / T;
+  int head[9], end[9];
+  unsigned long long cur[9];
   int nl = 0;
   for (int j = ty - 1; j <= ty + 1; ++j)
     for (int i = tx - 1; i <= tx + 1; ++i) {
@@ -269,22 +304,23 @@ __global__ void dof_gather_kernel(const float* __restrict__ rgb, const float4* _
       const int t = j * TW + i;
       head[nl] = tile_start[t];
       end[nl] = tile_start[t + 1];
-      cur[nl] = head[nl] < end[nl] ? tile_rank[head[nl]] : 0x7fffffff;
+      cur[nl] = head[nl] < end[nl] ? key[head[nl]] : kNone;
       ++nl;
     }
   float3 blur = f3(0.0f);
   float gained = 0.0f;
   for (;;) {
-    int best = -1, br = 0x7fffffff;
+    int best = -1;
+    unsigned long long bk = kNone;
     for (int k = 0; k < nl; ++k)
-      if (cur[k] < br) {
-        br = cur[k];
+      if (cur[k] < bk) {
+        bk = cur[k];
         best = k;
       }
     if (best < 0) break;
+    const int s = pix[head[best]];
     ++head[best];
-    cur[best] = head[best] < end[best] ? tile_rank[head[best]] : 0x7fffffff;
-    const int s = order[br];
+    cur[best] = head[best] < end[best] ? key[head[best]] : kNone;
     const int sx = s % W, sy = s / W;
     const int dx = x - sx, dy = y - sy;
     const float4 sv = src[s];
@@ -394,66 +430,130 @@ cudaError_t launch_bloom(float* rgb, int W, int H, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-// Depth of field in place on rgb (device). Synchronises `st` once: the
-// depth order is sorted on the host.
-cudaError_t launch_dof(float* rgb, const float* gbuf, int W, int H, float focus, float coc, const float cam[3],
-                       cudaStream_t st) {
+struct DofPlan {
+  int W = 0, H = 0, T = 0, TW = 0, TH = 0;
+  float4* src = nullptr;
+  int* tile_start = nullptr;
+  unsigned long long* key = nullptr;
+  int* pix = nullptr;
+  float* out = nullptr;
+  std::vector<void*> allocs;
+};
+
+void dof_plan_destroy(DofPlan* p, cudaStream_t st) {
+  if (!p) return;
+  for (void* a : p->allocs) cudaFreeAsync(a, st);
+  delete p;
+}
+
+// Order, radii and weights of the depth-of-field blur of one G-buffer and
+// camera. Synchronises `st` (the tile size depends on the largest radius).
+cudaError_t dof_plan_create(const float* gbuf, int W, int H, float focus, float coc, const float cam[3],
+                            cudaStream_t st, DofPlan** out) {
+  *out = nullptr;
   const int n = W * H;
-  DevScratch sc{{}, st};
-  float* depth = sc.get<float>(n);
-  if (sc.err != cudaSuccess) return sc.err;
-  depth_kernel<<<(n + 255) / 256, 256, 0, st>>>(gbuf, f3(cam[0], cam[1], cam[2]), depth, n);
-  std::vector<float> hd(n);
-  cudaError_t e = cudaMemcpyAsync(hd.data(), depth, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return e;
-  // Photo::depthFeildBlur's order: std::stable_sort of (x, y, depth) records
-  // in raster order by depth, with the reference's comparator.
-  struct PixelPos {
-    int x, y;
-    float depth;
+  DofPlan* p = new DofPlan();
+  p->W = W;
+  p->H = H;
+  cudaError_t e = cudaSuccess;
+  auto alloc = [&](size_t bytes) -> void* {
+    void* q = nullptr;
+    if (e == cudaSuccess) e = cudaMallocAsync(&q, bytes + 16, st);
+    if (e == cudaSuccess) p->allocs.push_back(q);
+    return e == cudaSuccess ? q : nullptr;
   };
-  std::vector<PixelPos> pix;
-  pix.reserve(n);
-  for (int y = 0; y < H; ++y)
-    for (int x = 0; x < W; ++x) pix.push_back({x, y, hd[(size_t)y * W + x]});
-  std::stable_sort(pix.begin(), pix.end(), [](const PixelPos& a, const PixelPos& b) { return a.depth < b.depth; });
-  int rmax = 0;
-  for (int i = 0; i < n; ++i) rmax = std::max(rmax, dof_int(dof_coc(coc, focus, hd[i])));
-  const int T = std::max(rmax, 8), TW = (W + T - 1) / T, TH = (H + T - 1) / T;
-  std::vector<int> order(n), tile_start((size_t)TW * TH + 1, 0), tile_rank(n);
-  for (int r = 0; r < n; ++r) {
-    const PixelPos& p = pix[r];
-    order[r] = p.y * W + p.x;
-    tile_start[(size_t)(p.y / T) * TW + p.x / T + 1]++;
+  float* depth = static_cast<float*>(alloc(sizeof(float) * n));
+  int* flags = static_cast<int*>(alloc(2 * sizeof(int)));
+  p->src = static_cast<float4*>(alloc(sizeof(float4) * n));
+  p->key = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long) * n));
+  p->pix = static_cast<int*>(alloc(sizeof(int) * n));
+  p->out = static_cast<float*>(alloc(sizeof(float) * 3 * n));
+  int hflags[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 2 * sizeof(int), st);
+  if (e == cudaSuccess) {
+    depth_kernel<<<(n + 255) / 256, 256, 0, st>>>(gbuf, f3(cam[0], cam[1], cam[2]), depth, n, flags);
+    dof_source_kernel<<<(n + 255) / 256, 256, 0, st>>>(depth, coc, focus, p->src, n, flags);
+    e = cudaGetLastError();
   }
-  for (size_t t = 0; t < (size_t)TW * TH; ++t) tile_start[t + 1] += tile_start[t];
-  {
-    std::vector<int> fill(tile_start.begin(), tile_start.end() - 1);
-    for (int r = 0; r < n; ++r) {
-      const PixelPos& p = pix[r];
-      tile_rank[fill[(size_t)(p.y / T) * TW + p.x / T]++] = r;  // ranks ascend within a tile
+  if (e == cudaSuccess) e = cudaMemcpyAsync(hflags, flags, sizeof hflags, cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    dof_plan_destroy(p, st);
+    return e;
+  }
+  p->T = std::max(hflags[1], 8);
+  p->TW = (W + p->T - 1) / p->T;
+  p->TH = (H + p->T - 1) / p->T;
+  std::vector<int> tile_start((size_t)p->TW * p->TH + 1, 0);
+  for (int ty = 0; ty < p->TH; ++ty)
+    for (int tx = 0; tx < p->TW; ++tx) {
+      const int w = std::min(W, tx * p->T + p->T) - tx * p->T, h = std::min(H, ty * p->T + p->T) - ty * p->T;
+      tile_start[(size_t)ty * p->TW + tx + 1] = w * h;
+    }
+  for (size_t t = 0; t + 1 < tile_start.size(); ++t) tile_start[t + 1] += tile_start[t];
+  p->tile_start = static_cast<int*>(alloc(sizeof(int) * tile_start.size()));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(p->tile_start, tile_start.data(), sizeof(int) * tile_start.size(), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess && !hflags[0]) {
+    dof_rank_kernel<<<row_grid(W, H), 128, 0, st>>>(depth, p->tile_start, W, H, p->T, p->TW, p->key, p->pix);
+    e = cudaGetLastError();
+  } else if (e == cudaSuccess) {
+    // NaN depths: the reference's own std::stable_sort decides the order
+    std::vector<float> hd(n);
+    e = cudaMemcpyAsync(hd.data(), depth, sizeof(float) * n, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) {
+      struct PixelPos {
+        int x, y;
+        float depth;
+      };
+      std::vector<PixelPos> pixs;
+      pixs.reserve(n);
+      for (int y = 0; y < H; ++y)
+        for (int x = 0; x < W; ++x) pixs.push_back({x, y, hd[(size_t)y * W + x]});
+      std::stable_sort(pixs.begin(), pixs.end(),
+                       [](const PixelPos& a, const PixelPos& b) { return a.depth < b.depth; });
+      std::vector<unsigned long long> hkey(n);
+      std::vector<int> hpix(n);
+      std::vector<int> fill(tile_start.begin(), tile_start.end() - 1);
+      for (int r = 0; r < n; ++r) {  // ranks ascend within each tile
+        const PixelPos& q = pixs[r];
+        const int slot = fill[(size_t)(q.y / p->T) * p->TW + q.x / p->T]++;
+        hkey[slot] = (unsigned long long)r;
+        hpix[slot] = q.y * W + q.x;
+      }
+      e = cudaMemcpyAsync(p->key, hkey.data(), sizeof(unsigned long long) * n, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(p->pix, hpix.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host vectors go out of scope
     }
   }
-  float4* src = sc.get<float4>(n);
-  int* d_order = sc.get<int>(n);
-  int* d_start = sc.get<int>(tile_start.size());
-  int* d_rank = sc.get<int>(n);
-  float* out = sc.get<float>((size_t)3 * n);
-  if (sc.err != cudaSuccess) return sc.err;
-  e = cudaMemcpyAsync(d_order, order.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // tile_start (host) was copied from
+  if (e != cudaSuccess) {
+    dof_plan_destroy(p, st);
+    return e;
+  }
+  *out = p;
+  return cudaSuccess;
+}
+
+// Photo::depthFeildBlur in place on rgb (device) with a plan of its G-buffer.
+cudaError_t dof_apply(const DofPlan* p, float* rgb, cudaStream_t st) {
+  dof_gather_kernel<<<row_grid(p->W, p->H), 128, 0, st>>>(rgb, p->src, p->tile_start, p->key, p->pix, p->W, p->H,
+                                                           p->T, p->TW, p->TH, p->out);
+  cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(d_start, tile_start.data(), sizeof(int) * tile_start.size(), cudaMemcpyHostToDevice, st);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(d_rank, tile_rank.data(), sizeof(int) * n, cudaMemcpyHostToDevice, st);
+    e = cudaMemcpyAsync(rgb, p->out, sizeof(float) * 3 * (size_t)p->W * p->H, cudaMemcpyDeviceToDevice, st);
+  return e;
+}
+
+cudaError_t launch_dof(float* rgb, const float* gbuf, int W, int H, float focus, float coc, const float cam[3],
+                       cudaStream_t st) {
+  DofPlan* p = nullptr;
+  cudaError_t e = dof_plan_create(gbuf, W, H, focus, coc, cam, st, &p);
   if (e != cudaSuccess) return e;
-  dof_source_kernel<<<(n + 255) / 256, 256, 0, st>>>(depth, coc, focus, src, n);
-  dof_gather_kernel<<<row_grid(W, H), 128, 0, st>>>(rgb, src, d_order, d_start, d_rank, W, H, T, TW, TH, out);
-  e = cudaMemcpyAsync(rgb, out, sizeof(float) * 3 * n, cudaMemcpyDeviceToDevice, st);
-  if (e != cudaSuccess) return e;
-  // the host vectors above are read by the copies: wait for them
-  e = cudaStreamSynchronize(st);
-  if (e != cudaSuccess) return e;
-  return cudaGetLastError();
+  e = dof_apply(p, rgb, st);
+  dof_plan_destroy(p, st);
+  return e;
 }
 
 cudaError_t launch_gamma(float* rgb, int n, cudaStream_t st) {

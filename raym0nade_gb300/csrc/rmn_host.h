@@ -76,6 +76,12 @@ cudaError_t launch_filter(float* const bufs[4], const float* gbuf, int w, int h,
 cudaError_t launch_bloom(float* rgb, int w, int h, cudaStream_t st);
 cudaError_t launch_dof(float* rgb, const float* gbuf, int w, int h, float focus, float coc, const float cam[3],
                        cudaStream_t st);
+// A depth-of-field plan serves every blur of the same G-buffer and camera.
+struct DofPlan;
+cudaError_t dof_plan_create(const float* gbuf, int w, int h, float focus, float coc, const float cam[3],
+                            cudaStream_t st, DofPlan** out);
+cudaError_t dof_apply(const DofPlan* plan, float* rgb, cudaStream_t st);
+void dof_plan_destroy(DofPlan* plan, cudaStream_t st);
 cudaError_t launch_gamma(float* rgb, int n, cudaStream_t st);
 cudaError_t launch_compose(const float* dd, const float* ds, const float* id, const float* is, const float* gbuf,
                            int w, int h, float exposure, int options, float* rgb, cudaStream_t stream);

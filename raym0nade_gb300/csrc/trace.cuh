@@ -275,6 +275,11 @@ RMN_D int trace(const DevScene& s, const TRay& r, float tmin, float& tmax, float
     if (ANY) cnt->shadow++;
     else cnt->closest++;
   }
+  if (!ALPHA) {
+    int st = trav_run<ANY, COUNT>(s, r, tmin, aim, t, 0x7fffffff, cnt);
+    tmax = t.tmax;
+    return st == -2 ? -2 : t.hit;
+  }
   int searches = 0;
   for (;;) {
     const bool alpha = ALPHA && s.has_alpha;
