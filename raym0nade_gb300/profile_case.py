@@ -15,6 +15,13 @@ meaningful) while the whole process holds well under a few GB.
       workers per lane), rendered twice: every wavefront kernel.
   python -m raym0nade_gb300.profile_case fxaa [--size WxH]
       rmn_compose(Full | gamma | FXAA): compose_kernel + fxaa_kernel.
+  python -m raym0nade_gb300.profile_case post [--size WxH] [--spp K]
+      a render of the textured room (every pixel a hit), then the export set
+      of render_multiThread (rmn_export_set: spatialClamp, filter, bloom,
+      depth of field, gamma, FXAA) twice.
+  python -m raym0nade_gb300.profile_case textured [--size WxH] [--spp K]
+      rmn_render of the textured room: the wavefront kernels with textures
+      and alpha-tested traversal.
 """
 from __future__ import annotations
 
@@ -27,7 +34,7 @@ import numpy as np
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["render", "trace", "fxaa", "batch"])
+    ap.add_argument("case", choices=["render", "trace", "fxaa", "batch", "post", "textured"])
     ap.add_argument("--lanes", type=int, default=2)
     ap.add_argument("--tris", type=int, default=2_000_000)
     ap.add_argument("--size", default="256")
@@ -75,6 +82,22 @@ def main(argv=None):
             m.rayHit_test(sr)
         torch.cuda.synchronize()
         print("trace", m.info(), "rays", a.rays)
+    elif a.case in ("post", "textured"):
+        w, h = (int(x) for x in a.size.split("x")) if "x" in a.size else (1920, 1080)
+        m = api.Model(scenes.textured_room())
+        cam = scenes.textured_camera(w, h, a.spp)
+        args = api.RenderArgs.from_camera(cam, seed=1)
+        ph = api.Photo(w, h)
+        api.render(m, args, ph)
+        if a.case == "textured":
+            api.render(m, args, ph)
+        else:
+            ph.focus, ph.CoC, ph.cameraPosition = 3.0, 6.0, tuple(cam.position)
+            out = torch.empty((api.EXPORTS + api.EXPORTS_DOF, h, w, 3), dtype=torch.float32, device="cuda")
+            for _ in range(2):
+                ph.export_set(out)
+        torch.cuda.synchronize()
+        print(a.case, w, h, "spp", a.spp)
     else:
         w, h = (int(x) for x in a.size.split("x")) if "x" in a.size else (1920, 1080)
         rng = np.random.default_rng(1)
