@@ -495,19 +495,20 @@ def run_gpu(args, rank, world, dist):
     ms_b, clocks = timed(step_batched, args.steps, args.warmup, sampler)
     ms_p, _ = timed(step_plain, args.steps, 1)
 
-    # end to end through the host-buffer ABI: render + display image per instance
-    host_photos = [api.Photo(i.camera.width, i.camera.height, device=False) for i in insts]
-    for ph in host_photos:
-        for k in ("radiance_Dd", "radiance_Ds", "radiance_Id", "radiance_Is", "Gbuffer"):
-            setattr(ph, k, torch.zeros(getattr(ph, k).shape, dtype=torch.float32).pin_memory())
+    # End to end through the C ABI, host in and host out, wall clock: every
+    # step uploads the 64 cameras and seeds from pinned host memory
+    # (rmn_batch_update), renders the batch (rmn_batch_render) and brings
+    # every instance's display image back to pinned host memory
+    # (rmn_compose(Full | gamma | FXAA) into a host array).
     disp = [torch.empty((i.camera.height, i.camera.width, 3), dtype=torch.float32).pin_memory() for i in insts]
 
     def step_e2e():
-        for m, a, ph, d in zip(models, argsl, host_photos, disp):
-            api.render(m, a, ph, stream)
+        batch.update(argsl, stream)
+        batch.render(stream)
+        for ph, d in zip(photos, disp):
             ph.shade(api.Full | api.GAMMA | api.DoFXAA, out=d, stream=stream)
 
-    e2e_steps = max(1, min(args.steps, 2))
+    e2e_steps = max(1, min(args.steps, 3))
     step_e2e()
     barrier()
     t = time.perf_counter()
@@ -516,10 +517,8 @@ def run_gpu(args, rank, world, dist):
     torch.cuda.synchronize()
     e2e_s = max_over_ranks((time.perf_counter() - t) / e2e_steps, dist, "cuda")
     npx = sum(i.camera.width * i.camera.height for i in insts)
-    # rmn_render copies the radiance buffers and G-buffer out; rmn_compose
-    # stages them back in and copies the display image out
-    d2h = npx * (4 * 16 + 20 * 4 + 12)
-    h2d = len(insts) * 96 + npx * (4 * 16 + 20 * 4)
+    d2h = npx * 12 + 4  # display images, and the batch's status word
+    h2d = batch.update_bytes
 
     adj = adjoint_timing(args, stream, flush, barrier) if args.adjoint else None
     per_config = config_timings(args, stream, flush, barrier) if args.configs else None
@@ -557,7 +556,8 @@ def run_gpu(args, rank, world, dist):
                   "batched_over_plain": value / plain},
         "e2e": {"value": job_rate(paths_per_step, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h,
-                "call": "rmn_render into pinned host buffers + rmn_compose(Full|gamma|FXAA) to a host image, per instance"},
+                "call": "rmn_batch_update (cameras and seeds from pinned host memory) + rmn_batch_render + "
+                        "rmn_compose(Full|gamma|FXAA) of every instance into pinned host memory; wall clock"},
         # per batched step: G-buffer kernel, one seed kernel per lane, 5 kernels
         # per wavefront iteration and lane, finalize
         "gpu_launches": args.steps * (2 + lanes + 5 * lanes * prof["iterations"]),

@@ -261,6 +261,14 @@ typedef struct rmn_batch_options {
 rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_batch_options* options, void* stream,
                             rmn_batch** out);
 rmn_status rmn_batch_render(rmn_batch* batch, void* stream);
+/* New camera poses, seeds and exposures for the items of a batch (args[i]
+ * for items[i] of rmn_batch_create), e.g. per frame of an animation; the
+ * next rmn_batch_render on `stream` uses them. Image size, spp, P_Direct,
+ * max_depth, lanes_per_pixel and slots_per_unit must stay as the batch was
+ * built (RMN_ERR_INVALID_ARGUMENT otherwise). The library uploads its job
+ * table, rmn_batch_update_bytes(batch) bytes, from pinned host memory. */
+rmn_status rmn_batch_update(rmn_batch* batch, const rmn_render_args* args, int32_t n, void* stream);
+int64_t rmn_batch_update_bytes(const rmn_batch* batch);
 rmn_status rmn_batch_profile(rmn_batch* batch, rmn_render_profile* out, void* stream);
 rmn_status rmn_batch_destroy(rmn_batch* batch);
 

@@ -96,6 +96,8 @@ SIGNATURES = {
                                    C.POINTER(C.c_void_p)]),
     "rmn_batch_autotune": (C.c_int, [C.POINTER(BatchItem), C.c_int32, C.c_float, C.POINTER(TuneResult), C.c_void_p]),
     "rmn_batch_render": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "rmn_batch_update": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
+    "rmn_batch_update_bytes": (C.c_int64, [C.c_void_p]),
     "rmn_batch_profile": (C.c_int, [C.c_void_p, C.POINTER(RenderProfile), C.c_void_p]),
     "rmn_batch_destroy": (C.c_int, [C.c_void_p]),
     "rmn_compose": (C.c_int, [C.POINTER(Image), C.c_int32, C.c_int32, C.c_float, C.c_int32, C.c_void_p,

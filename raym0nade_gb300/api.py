@@ -378,6 +378,17 @@ class Batch:
     def render(self, stream=None):
         _check(_lib.load().rmn_batch_render(self._h, _stream(stream)), "rmn_batch_render")
 
+    def update(self, args_list, stream=None):
+        """rmn_batch_update: new RenderArgs (camera, seed, exposure) per item,
+        same image sizes, spp, P_Direct and depth as at creation."""
+        arr = (_lib.RenderArgs * len(args_list))(*[a.c() for a in args_list])
+        _check(_lib.load().rmn_batch_update(self._h, arr, len(args_list), _stream(stream)), "rmn_batch_update")
+
+    @property
+    def update_bytes(self) -> int:
+        """Bytes rmn_batch_update uploads (the library's job table)."""
+        return int(_lib.load().rmn_batch_update_bytes(self._h))
+
     def profile(self, stream=None) -> dict:
         prof = _lib.RenderProfile()
         _check(_lib.load().rmn_batch_profile(self._h, C.byref(prof), _stream(stream)), "rmn_batch_profile")

@@ -744,6 +744,20 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
   return r;
 }
 
+rmn_status rmn_batch_update(rmn_batch* batch, const rmn_render_args* args, int32_t n, void* stream) {
+  clear_error();
+  if (!batch || !batch->state || !args) return fail(RMN_ERR_INVALID_ARGUMENT, "NULL batch or arguments");
+  for (int i = 0; i < n; ++i) {
+    rmn_status r = check_args(args[i]);
+    if (r != RMN_OK) return fail(r, "rmn_batch_update item %d: %s", i, rmn_last_error());
+  }
+  return batch_update(batch->state, args, n, static_cast<cudaStream_t>(stream));
+}
+
+int64_t rmn_batch_update_bytes(const rmn_batch* batch) {
+  return (batch && batch->state) ? (int64_t)batch_job_bytes() * batch_items(batch->state) : 0;
+}
+
 rmn_status rmn_batch_render(rmn_batch* batch, void* stream) {
   clear_error();
   if (!batch || !batch->state) return fail(RMN_ERR_INVALID_ARGUMENT, "NULL batch");

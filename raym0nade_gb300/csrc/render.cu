@@ -36,6 +36,7 @@
 
 #include <algorithm>
 #include <cstddef>
+#include <cstring>
 #include <vector>
 
 #include "rmn_host.h"
@@ -1011,6 +1012,7 @@ constexpr long long kMaxIterations = 1LL << 22;  // bound on the iteration loop;
 
 struct JobTable {
   std::vector<Job> jobs;
+  std::vector<int> item;  // job k renders item item[k] of the caller's list
   int total_pix = 0;
   long long total_units = 0;
 };
@@ -1033,6 +1035,10 @@ struct BatchState {
   // launches of the lanes side by side
   cudaStream_t ls[kMaxLanes] = {};
   cudaEvent_t fork = nullptr, join[kMaxLanes] = {};
+  // rmn_batch_update: the job table's pinned host copy and the event after
+  // its last upload
+  Job* h_jobs = nullptr;
+  cudaEvent_t upd = nullptr;
 };
 
 
@@ -1044,6 +1050,7 @@ static void build_jobs(const RenderItem* items, int n, JobTable* t) {
   std::stable_sort(order.begin(), order.end(),
                    [&](int a, int b) { return items[a].args.max_depth > items[b].args.max_depth; });
   t->jobs.clear();
+  t->item = order;
   t->total_pix = 0;
   t->total_units = 0;
   for (int i : order) {
@@ -1251,9 +1258,11 @@ void batch_destroy(BatchState* b) {
     if (b->join[l]) cudaEventDestroy(b->join[l]);
   }
   if (b->fork) cudaEventDestroy(b->fork);
+  if (b->upd) cudaEventDestroy(b->upd);
   // the blocks go back to the cache for the next batch: no work of this
   // batch may still run on them (cudaFree would have waited likewise)
   cudaDeviceSynchronize();
+  if (b->h_jobs) cudaFreeHost(b->h_jobs);
   for (void* p : b->allocs) cached_free(p);
   delete b;
 }
@@ -1375,6 +1384,45 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
 }
 
 rmn_status batch_launch(BatchState* b, cudaStream_t st) { return run(b, st, nullptr, nullptr); }
+
+// New camera poses, seeds and exposures for the items of a batch: the job
+// table is rewritten and uploaded (on `st`, before the next render on it).
+// Everything that shapes the work -- image size, spp, P_Direct, max depth,
+// the unit split -- must stay as the batch was built.
+rmn_status batch_update(BatchState* b, const rmn_render_args* args, int n, cudaStream_t st) {
+  const int nj = (int)b->table.jobs.size();
+  if (n != nj) return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_batch_update: %d arguments for a batch of %d", n, nj);
+  cudaError_t e = cudaSuccess;
+  if (!b->h_jobs) {
+    e = cudaMallocHost(&b->h_jobs, sizeof(Job) * nj);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->upd, cudaEventDisableTiming);
+    if (e != cudaSuccess) return cuda_fail(e, "rmn_batch_update (pinned job table)");
+  } else {
+    e = cudaEventSynchronize(b->upd);  // the previous upload has read the pinned copy
+    if (e != cudaSuccess) return cuda_fail(e, "rmn_batch_update");
+  }
+  std::vector<Job> next = b->table.jobs;
+  for (int k = 0; k < nj; ++k) {
+    Job& j = next[k];
+    const Params q = make_params(args[b->table.item[k]], j.p.glass != 0);
+    const Params& p = j.p;
+    if (q.W != p.W || q.H != p.H || q.spp != p.spp || q.maxd != p.maxd || q.spp_d != p.spp_d || q.S != p.S ||
+        q.K != p.K || q.slots != p.slots || q.slots16 != p.slots16)
+      return fail(RMN_ERR_INVALID_ARGUMENT,
+                  "rmn_batch_update: item %d changes the image size, spp, P_Direct, max depth or unit split",
+                  b->table.item[k]);
+    j.p = q;
+  }
+  b->table.jobs = next;
+  std::memcpy(b->h_jobs, next.data(), sizeof(Job) * nj);
+  e = cudaMemcpyAsync(b->d_jobs, b->h_jobs, sizeof(Job) * nj, cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) e = cudaEventRecord(b->upd, st);
+  if (e != cudaSuccess) return cuda_fail(e, "rmn_batch_update (upload)");
+  return RMN_OK;
+}
+
+size_t batch_job_bytes() { return sizeof(Job); }
+int batch_items(const BatchState* b) { return (int)b->table.jobs.size(); }
 
 rmn_status batch_status(BatchState* b, cudaStream_t st) {
   int h = 0;

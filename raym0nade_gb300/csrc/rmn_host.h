@@ -61,6 +61,9 @@ void release_cached_memory();
 rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, int lanes,
                         cudaStream_t st, BatchState** out);
 rmn_status batch_launch(BatchState* b, cudaStream_t st);
+rmn_status batch_update(BatchState* b, const rmn_render_args* args, int n, cudaStream_t st);
+size_t batch_job_bytes();
+int batch_items(const BatchState* b);
 rmn_status batch_status(BatchState* b, cudaStream_t st);
 rmn_status batch_profile(BatchState* b, cudaStream_t st, RenderProfileData* prof);
 void batch_destroy(BatchState* b);

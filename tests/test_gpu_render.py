@@ -258,3 +258,32 @@ def test_render_profile_counts():
     assert prof["pixels"] == 32 * 32
     assert prof["sample_slots"] > 0 and prof["shadow_rays"] > 0 and prof["inner_visits"] > 0
     assert prof["triangle_tests"] >= prof["leaf_visits"] > 0
+
+
+def test_batch_update_moves_cameras():
+    """rmn_batch_update: new cameras and seeds for a built batch (its graph
+    replayed) give the images of rmn_render with those arguments; a change of
+    image size is refused."""
+    import dataclasses
+    cor = api.Model(scenes.cornell())
+    gl = api.Model(scenes.cornell_glass())
+    cams = [scenes.cornell_camera(32, 32, 8), scenes.cornell_camera(24, 20, 6)]
+    models = [cor, gl]
+    args = [api.RenderArgs.from_camera(c, seed=3 + k) for k, c in enumerate(cams)]
+    items = [(m, a, api.Photo(c.width, c.height)) for m, a, c in zip(models, args, cams)]
+    b = api.Batch(items, use_graph=True)
+    b.render()
+    moved = [dataclasses.replace(c, position=(0.45, 0.55, -1.3)) for c in cams]
+    new_args = [api.RenderArgs.from_camera(c, seed=11 + k) for k, c in enumerate(moved)]
+    b.update(new_args)
+    b.render()
+    torch.cuda.synchronize()
+    for (m, a, ph), na in zip(items, new_args):
+        ref = _photo_np(api.render(m, na))
+        for x, y in zip(_photo_np(ph), ref):
+            assert np.array_equal(x, y, equal_nan=True)
+    assert b.update_bytes > 0
+    bad = [api.RenderArgs.from_camera(scenes.cornell_camera(40, 40, 8), seed=1), new_args[1]]
+    with pytest.raises(api.RmnError) as e:
+        b.update(bad)
+    assert e.value.status == 1
