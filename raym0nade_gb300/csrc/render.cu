@@ -847,7 +847,7 @@ constexpr int kFetchBudget = 16;  // node visits between refill checks
 // materials, whose queries retry past cut-away texels (a separate build, so
 // the common case keeps its register budget).
 template <bool SHADOW, bool COUNT, bool ALPHA>
-__global__ void __launch_bounds__(128) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+__global__ void __launch_bounds__(128, 8) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
                                                      int par, int* status, Counters* ctr) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;

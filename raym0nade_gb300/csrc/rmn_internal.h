@@ -62,7 +62,10 @@ RMN_HD float3 mix3(float3 x, float3 y, float a) { return x * (1.0f - a) + y * a;
 #define RMN_EPS 1e-4f                 // eps_zero, include/geometry.h:13
 #define RMN_PI 3.14159265358979323846f
 #define RMN_LEAF_MAX 10               // LeafBagSize, src/bvh.cpp:16
-#define RMN_STACK 32                  // traversal stack entries (tree depth <= 31; median splits of < 2^27 triangles stay below 26)
+// traversal stack entries: trees up to depth 26 (median splits of < 2^27
+// triangles stay below 26 levels); 27 x 8 B x 128 threads of shared memory
+// lets 8 persistent traversal blocks share an SM
+#define RMN_STACK 27
 
 // ------------------------------------------------------------ layout ------
 // Two-child node (64 B): the boxes of both children plus their references,
