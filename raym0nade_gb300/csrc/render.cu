@@ -845,9 +845,11 @@ constexpr int kFetchBudget = 16;  // node visits between refill checks
 // longest ray. The rays of a batch belong to different scenes; each lane
 // traverses its own job's BVH. ALPHA: the batch has scenes with alpha-tested
 // materials, whose queries retry past cut-away texels (a separate build, so
-// the common case keeps its register budget).
-template <bool SHADOW, bool COUNT, bool ALPHA>
-__global__ void __launch_bounds__(128, 8) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+// the common case keeps its register budget). STACK: the shared stack's
+// entries (RMN_STACK, or RMN_STACK_SMALL for batches of shallower trees, with
+// 9 instead of 8 blocks per SM).
+template <bool SHADOW, bool COUNT, bool ALPHA, int STACK>
+__global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
                                                      int par, int* status, Counters* ctr) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -865,8 +867,8 @@ __global__ void __launch_bounds__(128, 8) qtrace_kernel(const Job* __restrict__ 
   int jb = 0;        // the lane's job
   bool alpha = false;
   // the deferred-child stack in shared memory (launched with 128 threads)
-  __shared__ int2 sstack[RMN_STACK * 128];
-  TravT<SharedStack> t;
+  __shared__ int2 sstack[STACK * 128];
+  TravT<SharedStackN<STACK>> t;
   t.stack.base = sstack + threadIdx.x;
   DevScene s;
   TraceCounters tc = {0, 0, 0, 0, 0};
@@ -1026,6 +1028,7 @@ struct BatchState {
   int lanes = 1;
   bool alpha = false;         // some job's scene has alpha-tested materials
   bool tex = false;           // some job's scene has textures
+  bool shallow = true;        // every job's tree fits the small traversal stack
   Pool pool[kMaxLanes] = {};  // each lane's share of the worker arrays
   Queues q[kMaxLanes] = {};
   std::vector<void*> allocs;
@@ -1093,13 +1096,13 @@ static cudaError_t launch_init(BatchState* b, cudaStream_t st, Counters* ctr) {
 
 // The two traversal kernels of an iteration (closest, then shadow), on as
 // many persistent blocks as fit, at most one lane's worth of rays.
-template <bool COUNT, bool ALPHA>
+template <bool COUNT, bool ALPHA, int STACK>
 static void launch_qtrace(BatchState* b, const Pool& P, const Queues& Q, Ctl* ctl, int par, Counters* ctr, int lb,
                           cudaStream_t st) {
-  int tb = device_sms() * blocks_per_sm(qtrace_kernel<false, COUNT, ALPHA>);
+  int tb = device_sms() * blocks_per_sm(qtrace_kernel<false, COUNT, ALPHA, STACK>);
   if (tb > lb) tb = lb;
-  qtrace_kernel<false, COUNT, ALPHA><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
-  qtrace_kernel<true, COUNT, ALPHA><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+  qtrace_kernel<false, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+  qtrace_kernel<true, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
 }
 
 // Iteration k of a chunk (parity k & 1) of one lane: the three logic
@@ -1130,11 +1133,13 @@ static cudaError_t launch_iteration(BatchState* b, int lane, cudaStream_t st, Co
   if (ev) cudaEventRecord(ev[1], st);
   const int lb = (P.W + 127) / 128;
   if (ctr) {
-    if (b->alpha) launch_qtrace<true, true>(b, P, Q, ctl, par, ctr, lb, st);
-    else launch_qtrace<true, false>(b, P, Q, ctl, par, ctr, lb, st);
+    if (b->alpha) launch_qtrace<true, true, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
+    else if (b->shallow) launch_qtrace<true, false, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
+    else launch_qtrace<true, false, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
   } else {
-    if (b->alpha) launch_qtrace<false, true>(b, P, Q, ctl, par, ctr, lb, st);
-    else launch_qtrace<false, false>(b, P, Q, ctl, par, ctr, lb, st);
+    if (b->alpha) launch_qtrace<false, true, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
+    else if (b->shallow) launch_qtrace<false, false, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
+    else launch_qtrace<false, false, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
   }
   if (ev) cudaEventRecord(ev[3], st);
   return cudaGetLastError();
@@ -1319,6 +1324,7 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
   for (const Job& j : b->table.jobs) {
     b->tex = b->tex || j.s.has_tex;
     b->alpha = b->alpha || j.s.has_alpha;
+    b->shallow = b->shallow && j.s.depth + 1 <= RMN_STACK_SMALL;
   }
   const bool tex = b->tex;
   if (tex) alloc((void**)&P.rdiff, sizeof(float4) * 3 * W);

@@ -17,8 +17,10 @@ namespace {
 
 constexpr int kFetchBudget = 16;  // node visits between refill checks
 
-template <bool SHADOW>
-__global__ void __launch_bounds__(128) trace_kernel(DevScene s, const float4* __restrict__ rays, int64_t n,
+// STACK: shared stack entries (RMN_STACK_SMALL for trees that fit it: one
+// more block per SM).
+template <bool SHADOW, int STACK>
+__global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) trace_kernel(DevScene s, const float4* __restrict__ rays, int64_t n,
                                                     float4* __restrict__ hits, uint8_t* __restrict__ occ,
                                                     unsigned long long* __restrict__ next, int* status) {
   const int lane = threadIdx.x & 31;
@@ -30,8 +32,8 @@ __global__ void __launch_bounds__(128) trace_kernel(DevScene s, const float4* __
   int searches = 0;
   bool retry = false;
   // the deferred-child stack in shared memory (launched with 128 threads)
-  __shared__ int2 sstack[RMN_STACK * 128];
-  TravT<SharedStack> t;
+  __shared__ int2 sstack[STACK * 128];
+  TravT<SharedStackN<STACK>> t;
   t.stack.base = sstack + threadIdx.x;
   for (;;) {
     // lanes without a ray take the next ones from the batch
@@ -94,6 +96,16 @@ int persistent_blocks(const void* kernel, int threads) {
   return sms * per_sm;
 }
 
+template <bool SHADOW, int STACK>
+void launch_kernel(const DevScene& s, const float4* rays, int64_t n, float4* hits, uint8_t* occ,
+                   unsigned long long* next, int* status, cudaStream_t stream) {
+  const int threads = 128;
+  int blocks = persistent_blocks((const void*)trace_kernel<SHADOW, STACK>, threads);
+  int64_t need = (n + threads - 1) / threads;
+  if (need < blocks) blocks = (int)need;
+  trace_kernel<SHADOW, STACK><<<blocks, threads, 0, stream>>>(s, rays, n, hits, occ, next, status);
+}
+
 cudaError_t launch(bool shadow, const DevScene& s, const rmn_ray* rays, int64_t n, rmn_hit* hits, uint8_t* occ,
                    int* status, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
@@ -102,19 +114,15 @@ cudaError_t launch(bool shadow, const DevScene& s, const rmn_ray* rays, int64_t 
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(next, 0, sizeof(unsigned long long), stream);
   if (e == cudaSuccess) {
-    const int threads = 128;
+    const float4* r = reinterpret_cast<const float4*>(rays);
+    float4* h = reinterpret_cast<float4*>(hits);
+    const bool shallow = s.depth + 1 <= RMN_STACK_SMALL;
     if (shadow) {
-      int blocks = persistent_blocks((const void*)trace_kernel<true>, threads);
-      int64_t need = (n + threads - 1) / threads;
-      if (need < blocks) blocks = (int)need;
-      trace_kernel<true><<<blocks, threads, 0, stream>>>(s, reinterpret_cast<const float4*>(rays), n, nullptr, occ,
-                                                         next, status);
+      if (shallow) launch_kernel<true, RMN_STACK_SMALL>(s, r, n, nullptr, occ, next, status, stream);
+      else launch_kernel<true, RMN_STACK>(s, r, n, nullptr, occ, next, status, stream);
     } else {
-      int blocks = persistent_blocks((const void*)trace_kernel<false>, threads);
-      int64_t need = (n + threads - 1) / threads;
-      if (need < blocks) blocks = (int)need;
-      trace_kernel<false><<<blocks, threads, 0, stream>>>(s, reinterpret_cast<const float4*>(rays), n,
-                                                          reinterpret_cast<float4*>(hits), nullptr, next, status);
+      if (shallow) launch_kernel<false, RMN_STACK_SMALL>(s, r, n, h, nullptr, next, status, stream);
+      else launch_kernel<false, RMN_STACK>(s, r, n, h, nullptr, next, status, stream);
     }
     e = cudaGetLastError();
   }

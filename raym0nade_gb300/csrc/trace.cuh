@@ -88,17 +88,25 @@ struct TraceCounters {
 // traversing.
 // Stack storage: per-thread local memory, or a slice of shared memory (the
 // persistent traversal kernels; entry e of thread i at base[e * 128 + i], so
-// a warp's accesses to one level fall in distinct banks).
+// a warp's accesses to one level fall in distinct banks). kCap entries.
 struct LocalStack {
+  static constexpr int kCap = RMN_STACK;
   int2 e[RMN_STACK];  // (reference, entry distance as float bits)
   RMN_D void put(int i, int2 v) { e[i] = v; }
   RMN_D int2 get(int i) const { return e[i]; }
 };
-struct SharedStack {
+template <int N = RMN_STACK>
+struct SharedStackN {
+  static constexpr int kCap = N;
   int2* base;
   RMN_D void put(int i, int2 v) { base[i * 128] = v; }
   RMN_D int2 get(int i) const { return base[i * 128]; }
 };
+using SharedStack = SharedStackN<RMN_STACK>;
+// A shallower shared stack for batches whose trees are at most
+// RMN_STACK_SMALL - 1 deep: less shared memory, one more persistent block
+// per SM.
+#define RMN_STACK_SMALL 23
 
 template <class Stack>
 struct TravT {
@@ -165,7 +173,7 @@ RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav
         }
         if (hn) {
           if (hf) {
-            if (t.sp >= RMN_STACK) return -2;
+            if (t.sp >= Stack::kCap) return -2;
             t.stack.put(t.sp, make_int2(fref, __float_as_int(tlf)));
             ++t.sp;
           }
