@@ -19,7 +19,7 @@ def lib():
 
 def declared_functions():
     text = open(os.path.join(ROOT, "include", "rmn.h")).read()
-    return sorted(set(re.findall(r"^\s*(?:const char\*|rmn_status)\s+(rmn_\w+)\s*\(", text, re.M)))
+    return sorted(set(re.findall(r"^\s*(?:const char\*|rmn_status|int32_t|int64_t)\s+(rmn_\w+)\s*\(", text, re.M)))
 
 
 def test_header_declares_entry_points():
@@ -106,3 +106,55 @@ def test_scene_generators_shapes():
     assert h.num_triangles == 2 * 32 * 32
     e = scenes.sky_env(64, 32)
     assert e.shape == (32, 64, 3) and e.max() >= 5e4
+
+
+def test_argument_checks_need_no_gpu(lib):
+    """The new entry points refuse bad arguments before any device work."""
+    import ctypes as C
+    from raym0nade_gb300 import _lib, scenes
+    img = _lib.Image()
+    rgb = (C.c_float * 12)()
+    pa = _lib.PostArgs(2, 2, 1.0, 1.0, 0.0, (C.c_float * 3)())
+    # incomplete image, or no rgb
+    assert lib.rmn_post_process(C.byref(img), C.byref(pa), 63, rgb, None) == 1
+    assert lib.rmn_spatial_clamp(C.byref(img), 2, 2, None) == 1
+    assert lib.rmn_filter(C.byref(img), 2, 2, None) == 1
+    cnt = C.c_int32(-1)
+    assert lib.rmn_export_set(C.byref(img), C.byref(pa), rgb, C.byref(cnt), None) == 1
+    # a negative or non-finite CoC, a zero size
+    for bad in (_lib.PostArgs(2, 2, 1.0, 1.0, -1.0, (C.c_float * 3)()),
+                _lib.PostArgs(2, 2, 1.0, 1.0, float("inf"), (C.c_float * 3)()),
+                _lib.PostArgs(0, 2, 1.0, 1.0, 0.0, (C.c_float * 3)())):
+        assert lib.rmn_post_process(C.byref(img), C.byref(bad), 63, rgb, None) == 1
+    assert b"CoC" in lib.rmn_last_error() or b"size" in lib.rmn_last_error()
+    # export table
+    assert lib.rmn_export_tag(0) == b"DiffuseColor" and lib.rmn_export_tag(25) is None
+    assert lib.rmn_export_options(-1) == -1
+    assert lib.rmn_batch_update(None, None, 0, None) == 1 and lib.rmn_batch_update_bytes(None) == 0
+
+
+def test_texture_scene_checks_need_no_gpu(lib):
+    """rmn_scene_create refuses RGB textures (the reference's 4-byte lookups
+    read past them) and out-of-range texture indices before uploading."""
+    import ctypes as C
+    from raym0nade_gb300 import _lib, scenes
+    room = scenes.textured_room()
+
+    def create(textures, mat_tex):
+        keep = [np.ascontiguousarray(x) for x in (room.positions, room.normals, room.uvs, room.indices,
+                                                  room.mesh_first, room.mesh_material, room.materials)]
+        p, n, u, i, mf, mm, mat = keep
+        tarr = (_lib.Texture * len(textures))(*[_lib.Texture(t.shape[1], t.shape[0], t.shape[2], t.ctypes.data)
+                                                for t in textures])
+        d = _lib.SceneDesc(p.shape[0], p.ctypes.data, n.ctypes.data, u.ctypes.data, i.shape[0], i.ctypes.data,
+                           mm.shape[0], mf.ctypes.data, mm.ctypes.data, mat.shape[0], mat.ctypes.data, 0, 0, None,
+                           len(textures), C.cast(tarr, C.c_void_p).value, mat_tex.ctypes.data)
+        h = C.c_void_p()
+        return lib.rmn_scene_create(C.byref(d), C.byref(h)), textures
+    rgb = [np.ascontiguousarray(t[..., :3]) for t in room.textures]
+    st, _ = create(rgb, np.ascontiguousarray(room.mat_tex))
+    assert st == 4 and b"channels" in lib.rmn_last_error()
+    bad = room.mat_tex.copy()
+    bad[0, 0] = len(room.textures)
+    st, _ = create(list(room.textures), np.ascontiguousarray(bad))
+    assert st == 1 and b"out of range" in lib.rmn_last_error()
