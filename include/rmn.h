@@ -361,6 +361,13 @@ rmn_status rmn_filter(const rmn_image* image, int32_t width, int32_t height, voi
 #define RMN_EXPORTS_DOF 5
 rmn_status rmn_export_set(const rmn_image* image, const rmn_post_args* args, float* rgb, int32_t* count,
                           void* stream);
+/* Photo::save (src/image.cpp:481-532) without libpng: rgb (3 floats per
+ * pixel, host or device memory) as an 8-bit RGB PNG at `path`, each byte
+ * static_cast<uint8_t>(value * 255) as the reference writes it (values
+ * outside [0, 1] clamp; the reference leaves them undefined). The image data
+ * are stored uncompressed (deflate stored blocks). */
+rmn_status rmn_save_png(const float* rgb, int32_t width, int32_t height, const char* path);
+
 /* The file tag of export k ("DiffuseColor", ..., "Filter_DepthFieldBlur_Bloom_FXAA") and its shade
  * options; NULL / -1 out of range. */
 const char* rmn_export_tag(int32_t k);

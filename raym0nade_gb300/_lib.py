@@ -111,6 +111,7 @@ SIGNATURES = {
     "rmn_export_set": (C.c_int, [C.POINTER(Image), C.POINTER(PostArgs), C.c_void_p, C.POINTER(C.c_int32),
                                  C.c_void_p]),
     "rmn_export_tag": (C.c_char_p, [C.c_int32]),
+    "rmn_save_png": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_char_p]),
     "rmn_export_options": (C.c_int32, [C.c_int32]),
 }
 

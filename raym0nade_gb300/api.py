@@ -289,13 +289,20 @@ class Photo:
 
     @staticmethod
     def save(rgb, path: str) -> None:
-        """Photo::save as binary PPM: each channel * 255 truncated to a byte
-        (src/image.cpp:588-594); PNG output needs libpng, absent here."""
-        a = rgb.cpu().numpy() if (torch is not None and isinstance(rgb, torch.Tensor)) else np.asarray(rgb)
-        b = np.clip(a * 255.0, 0, 255).astype(np.uint8)
-        with open(path, "wb") as f:
-            f.write(b"P6\n%d %d\n255\n" % (b.shape[1], b.shape[0]))
-            f.write(b.tobytes())
+        """Photo::save (src/image.cpp:481-532): an 8-bit RGB PNG through
+        rmn_save_png, each channel * 255 truncated to a byte; a path ending in
+        .ppm writes binary PPM with the same bytes."""
+        if path.lower().endswith(".ppm"):
+            a = rgb.cpu().numpy() if (torch is not None and isinstance(rgb, torch.Tensor)) else np.asarray(rgb)
+            b = np.clip(a * np.float32(255.0), 0, 255).astype(np.uint8)
+            with open(path, "wb") as f:
+                f.write(b"P6\n%d %d\n255\n" % (b.shape[1], b.shape[0]))
+                f.write(b.tobytes())
+            return
+        if not (torch is not None and isinstance(rgb, torch.Tensor)):
+            rgb = np.ascontiguousarray(rgb, np.float32)
+        h, w = int(rgb.shape[0]), int(rgb.shape[1])
+        _check(_lib.load().rmn_save_png(_ptr(rgb), w, h, path.encode()), "rmn_save_png")
 
 
 def render(model: Model, args: RenderArgs, photo: Photo | None = None, stream=None) -> Photo:

@@ -440,6 +440,20 @@ rmn_status rmn_export_set(const rmn_image* image, const rmn_post_args* args, flo
   return r;
 }
 
+rmn_status rmn_save_png(const float* rgb, int32_t width, int32_t height, const char* path) {
+  clear_error();
+  if (!rgb || !path || width <= 0 || height <= 0 || (int64_t)width * height > (1LL << 30))
+    return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_save_png needs an image, a size and a path");
+  const size_t n = (size_t)width * height * 3;
+  if (is_device_ptr(rgb)) {
+    std::vector<float> h(n);
+    cudaError_t e = cudaMemcpy(h.data(), rgb, n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy (rmn_save_png)");
+    return write_png(h.data(), width, height, path);
+  }
+  return write_png(rgb, width, height, path);
+}
+
 const char* rmn_export_tag(int32_t k) {
   return (k >= 0 && k < RMN_EXPORTS + RMN_EXPORTS_DOF) ? kExports[k].tag : nullptr;
 }

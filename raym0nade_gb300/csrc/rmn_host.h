@@ -53,6 +53,9 @@ struct RenderProfileData {
 };
 struct BatchState;
 
+// Photo::save as an 8-bit RGB PNG (png.cpp); rgb in host memory.
+rmn_status write_png(const float* rgb, int w, int h, const char* path);
+
 // Device memory kept for reuse between batches (devmem.cpp).
 cudaError_t cached_malloc(void** p, size_t bytes);
 void cached_free(void* p);

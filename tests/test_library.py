@@ -158,3 +158,44 @@ def test_texture_scene_checks_need_no_gpu(lib):
     bad[0, 0] = len(room.textures)
     st, _ = create(list(room.textures), np.ascontiguousarray(bad))
     assert st == 1 and b"out of range" in lib.rmn_last_error()
+
+
+def _read_png(path):
+    """A minimal PNG reader (8-bit RGB, filter 0) that checks every CRC."""
+    import struct
+    import zlib
+    data = open(path, "rb").read()
+    assert data[:8] == b"\x89PNG\r\n\x1a\n"
+    pos, chunks = 8, []
+    while pos < len(data):
+        n, = struct.unpack(">I", data[pos:pos + 4])
+        typ, body = data[pos + 4:pos + 8], data[pos + 8:pos + 8 + n]
+        crc, = struct.unpack(">I", data[pos + 8 + n:pos + 12 + n])
+        assert crc == zlib.crc32(typ + body) & 0xffffffff, typ
+        chunks.append((typ, body))
+        pos += 12 + n
+    assert chunks[0][0] == b"IHDR" and chunks[-1][0] == b"IEND"
+    w, h, depth, ctype, comp, filt, inter = struct.unpack(">IIBBBBB", chunks[0][1])
+    assert (depth, ctype, comp, filt, inter) == (8, 2, 0, 0, 0)
+    raw = zlib.decompress(b"".join(b for t, b in chunks if t == b"IDAT"))
+    rows = np.frombuffer(raw, np.uint8).reshape(h, 1 + 3 * w)
+    assert (rows[:, 0] == 0).all()
+    return rows[:, 1:].reshape(h, w, 3)
+
+
+@pytest.mark.parametrize("w,h", [(1, 1), (37, 5), (300, 260)])
+def test_save_png_bytes_are_the_references(lib, tmp_path, w, h):
+    """Photo::save's bytes, static_cast<png_byte>(v * 255), in a PNG any
+    reader decodes (the 300 x 260 image spans several stored blocks)."""
+    from raym0nade_gb300 import api
+    rng = np.random.default_rng(w * h)
+    img = rng.random((h, w, 3), dtype=np.float32)
+    img[0, 0] = (0.0, 1.0, 0.999)
+    path = str(tmp_path / "x.png")
+    api.Photo.save(img, path)
+    got = _read_png(path)
+    want = (img * np.float32(255)).astype(np.uint8)  # truncation, as the reference's cast
+    assert np.array_equal(got, want)
+    ppm = str(tmp_path / "x.ppm")
+    api.Photo.save(img, ppm)
+    assert open(ppm, "rb").read().endswith(want.tobytes())
