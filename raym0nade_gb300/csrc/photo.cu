@@ -18,7 +18,9 @@
 //    senders in the reference's order. The pixels of each tile of T x T
 //    pixels (T >= the largest radius) are listed in that order with a sort
 //    key; a receiver merges the lists of its 3 x 3 tiles by key, so it meets
-//    every sender that can reach it, in order. Without NaN depths a stable
+//    every sender that can reach it, in order (a block per tile first keeps
+//    the senders whose square reaches the tile and merges them once, so a
+//    receiver only walks its tile's candidates). Without NaN depths a stable
 //    sort by depth is the order by (depth, raster index), whose key is
 //    (depth bits, index): each tile ranks its own pixels on the device. A
 //    NaN depth (a pixel without a hit) compares false both ways in the
@@ -285,42 +287,114 @@ __global__ void dof_rank_kernel(const float* __restrict__ depth, const int* __re
   pix[slot] = p;
 }
 
-// The receiving pixel (x, y): its senders, in the reference's order, from the
-// key-sorted lists of its 3 x 3 tiles.
-__global__ void dof_gather_kernel(const float* __restrict__ rgb, const float4* __restrict__ src,
-                                  const int* __restrict__ tile_start, const unsigned long long* __restrict__ key,
-                                  const int* __restrict__ pix, int W, int H, int T, int TW, int TH,
-                                  float* __restrict__ out) {
-  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y;
-  if (x >= W) return;
-  const unsigned long long kNone = ~0ull;
-  const int tx = x / T, ty = y / T;
-  int head[9], end[9];
-  unsigned long long cur[9];
-  int nl = 0;
+// Per receiving tile: the senders of its 3 x 3 tiles whose square of
+// half-width radius touches the tile, in the reference's order. A block per
+// tile compacts each neighbour list (order kept) into `tmp`, then places every
+// survivor at its rank in the merged order: its index in its own list plus,
+// for every other list, the number of survivors with a smaller key.
+constexpr int kCandThreads = 256;
+
+__device__ int block_exclusive_scan(int v, int* warp_sums, int& total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int x = v;
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) warp_sums[wid] = x;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < kCandThreads / 32 ? warp_sums[lane] : 0;
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    if (lane < kCandThreads / 32) warp_sums[lane] = w;  // inclusive
+  }
+  __syncthreads();
+  const int before = (wid > 0 ? warp_sums[wid - 1] : 0) + x - v;
+  total = warp_sums[kCandThreads / 32 - 1];
+  __syncthreads();
+  return before;
+}
+
+__global__ void __launch_bounds__(kCandThreads) dof_candidates_kernel(
+    const float4* __restrict__ src, const int* __restrict__ tile_start, const unsigned long long* __restrict__ key,
+    const int* __restrict__ pix, const long long* __restrict__ cand_off, int W, int H, int T, int TW, int TH,
+    unsigned long long* __restrict__ tmp_key, int* __restrict__ tmp_pix, int* __restrict__ cand,
+    int* __restrict__ cand_count) {
+  __shared__ int warp_sums[kCandThreads / 32];
+  __shared__ int lst_begin[9], lst_len[9];
+  const int t = blockIdx.x, tx = t % TW, ty = t / TW;
+  const int x0 = tx * T, y0 = ty * T, x1 = min(W, x0 + T) - 1, y1 = min(H, y0 + T) - 1;
+  const long long base = cand_off[t];
+  int nl = 0, filled = 0;
   for (int j = ty - 1; j <= ty + 1; ++j)
     for (int i = tx - 1; i <= tx + 1; ++i) {
       if (i < 0 || i >= TW || j < 0 || j >= TH) continue;
-      const int t = j * TW + i;
-      head[nl] = tile_start[t];
-      end[nl] = tile_start[t + 1];
-      cur[nl] = head[nl] < end[nl] ? key[head[nl]] : kNone;
+      const int u = j * TW + i, b = tile_start[u], len = tile_start[u + 1] - b;
+      int kept = 0;
+      for (int c0 = 0; c0 < len; c0 += kCandThreads) {
+        const int c = c0 + threadIdx.x;
+        bool keep = false;
+        int s = 0;
+        if (c < len) {
+          s = pix[b + c];
+          const int sx = s % W, sy = s / W, r = __float_as_int(src[s].z);
+          keep = sx - r <= x1 && sx + r >= x0 && sy - r <= y1 && sy + r >= y0;
+        }
+        int total;
+        const int at = block_exclusive_scan(keep ? 1 : 0, warp_sums, total);
+        if (keep) {
+          tmp_key[base + filled + kept + at] = key[b + c];
+          tmp_pix[base + filled + kept + at] = s;
+        }
+        kept += total;
+      }
+      if (threadIdx.x == 0) {
+        lst_begin[nl] = filled;
+        lst_len[nl] = kept;
+      }
+      filled += kept;
       ++nl;
     }
+  __syncthreads();
+  for (int c = threadIdx.x; c < filled; c += kCandThreads) {
+    const unsigned long long k = tmp_key[base + c];
+    int rank = 0;
+    for (int l = 0; l < nl; ++l) {
+      const int b = lst_begin[l], len = lst_len[l];
+      if (c >= b && c < b + len) {
+        rank += c - b;
+        continue;
+      }
+      int lo = 0, hi = len;  // survivors of list l with a smaller key
+      while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (tmp_key[base + b + mid] < k) lo = mid + 1;
+        else hi = mid;
+      }
+      rank += lo;
+    }
+    cand[base + rank] = tmp_pix[base + c];
+  }
+  if (threadIdx.x == 0) cand_count[t] = filled;
+}
+
+// The receiving pixel (x, y): its tile's candidates, in order.
+__global__ void dof_fold_kernel(const float* __restrict__ rgb, const float4* __restrict__ src,
+                                const long long* __restrict__ cand_off, const int* __restrict__ cand,
+                                const int* __restrict__ cand_count, int W, int H, int T, int TW,
+                                float* __restrict__ out) {
+  const int x = blockIdx.x * blockDim.x + threadIdx.x, y = blockIdx.y * blockDim.y + threadIdx.y;
+  if (x >= W || y >= H) return;
+  const int t = (y / T) * TW + x / T;
+  const int* c = cand + cand_off[t];
+  const int n = cand_count[t];
   float3 blur = f3(0.0f);
   float gained = 0.0f;
-  for (;;) {
-    int best = -1;
-    unsigned long long bk = kNone;
-    for (int k = 0; k < nl; ++k)
-      if (cur[k] < bk) {
-        bk = cur[k];
-        best = k;
-      }
-    if (best < 0) break;
-    const int s = pix[head[best]];
-    ++head[best];
-    cur[best] = head[best] < end[best] ? key[head[best]] : kNone;
+  for (int k = 0; k < n; ++k) {
+    const int s = c[k];
     const int sx = s % W, sy = s / W;
     const int dx = x - sx, dy = y - sy;
     const float4 sv = src[s];
@@ -436,6 +510,10 @@ struct DofPlan {
   int* tile_start = nullptr;
   unsigned long long* key = nullptr;
   int* pix = nullptr;
+  // per receiving tile: its candidate senders in order
+  long long* cand_off = nullptr;
+  int* cand = nullptr;
+  int* cand_count = nullptr;
   float* out = nullptr;
   std::vector<void*> allocs;
 };
@@ -527,7 +605,36 @@ cudaError_t dof_plan_create(const float* gbuf, int W, int H, float focus, float 
       if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // the host vectors go out of scope
     }
   }
-  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // tile_start (host) was copied from
+  // candidate lists: capacity of tile t = the pixels of its 3 x 3 tiles
+  const size_t ntiles = (size_t)p->TW * p->TH;
+  std::vector<long long> cand_off(ntiles + 1, 0);
+  for (int ty = 0; ty < p->TH; ++ty)
+    for (int tx = 0; tx < p->TW; ++tx) {
+      long long cap = 0;
+      for (int j = ty - 1; j <= ty + 1; ++j)
+        for (int i = tx - 1; i <= tx + 1; ++i)
+          if (i >= 0 && i < p->TW && j >= 0 && j < p->TH) {
+            const size_t u = (size_t)j * p->TW + i;
+            cap += tile_start[u + 1] - tile_start[u];
+          }
+      cand_off[(size_t)ty * p->TW + tx + 1] = cap;
+    }
+  for (size_t t = 0; t < ntiles; ++t) cand_off[t + 1] += cand_off[t];
+  const size_t total = (size_t)cand_off[ntiles];
+  p->cand_off = static_cast<long long*>(alloc(sizeof(long long) * (ntiles + 1)));
+  p->cand = static_cast<int*>(alloc(sizeof(int) * total));
+  p->cand_count = static_cast<int*>(alloc(sizeof(int) * ntiles));
+  unsigned long long* tmp_key = static_cast<unsigned long long*>(alloc(sizeof(unsigned long long) * total));
+  int* tmp_pix = static_cast<int*>(alloc(sizeof(int) * total));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(p->cand_off, cand_off.data(), sizeof(long long) * (ntiles + 1), cudaMemcpyHostToDevice, st);
+  if (e == cudaSuccess) {
+    dof_candidates_kernel<<<(unsigned)ntiles, kCandThreads, 0, st>>>(p->src, p->tile_start, p->key, p->pix,
+                                                                     p->cand_off, W, H, p->T, p->TW, p->TH, tmp_key,
+                                                                     tmp_pix, p->cand, p->cand_count);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);  // host arrays were copied from
   if (e != cudaSuccess) {
     dof_plan_destroy(p, st);
     return e;
@@ -538,8 +645,9 @@ cudaError_t dof_plan_create(const float* gbuf, int W, int H, float focus, float 
 
 // Photo::depthFeildBlur in place on rgb (device) with a plan of its G-buffer.
 cudaError_t dof_apply(const DofPlan* p, float* rgb, cudaStream_t st) {
-  dof_gather_kernel<<<row_grid(p->W, p->H), 128, 0, st>>>(rgb, p->src, p->tile_start, p->key, p->pix, p->W, p->H,
-                                                           p->T, p->TW, p->TH, p->out);
+  dim3 grid((p->W + 15) / 16, (p->H + 15) / 16), block(16, 16);
+  dof_fold_kernel<<<grid, block, 0, st>>>(rgb, p->src, p->cand_off, p->cand, p->cand_count, p->W, p->H, p->T, p->TW,
+                                          p->out);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(rgb, p->out, sizeof(float) * 3 * (size_t)p->W * p->H, cudaMemcpyDeviceToDevice, st);
