@@ -273,8 +273,8 @@ rmn_status rmn_batch_profile(rmn_batch* batch, rmn_render_profile* out, void* st
 rmn_status rmn_batch_destroy(rmn_batch* batch);
 
 /* Project-written autotuner for batches. Times candidate launch
- * configurations -- slots per work unit in {4, 8, 16} x workers per lane in
- * {2^19, 2^20, 2^21} x lanes in {1, 2, 3} -- on a proxy of the batch whose
+ * configurations -- slots per work unit in {2, 4, 8, 16} x workers per lane
+ * in {2^20, 2^21, 2^22} x lanes in {2, 3, 4} -- on a proxy of the batch whose
  * images keep every item's scene, spp, depth and field of view but only
  * `pixel_fraction` (0 < f <= 1) of its pixels, and returns the fastest. Set
  * each item's slots_per_unit and the batch's pool_workers and lanes from the

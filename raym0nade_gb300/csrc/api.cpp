@@ -719,11 +719,11 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
   if (e == cudaSuccess) e = cudaEventCreate(&e0);
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
   if (e != cudaSuccess) r = cuda_fail(e, "autotune set-up");
-  const int slots[] = {4, 8, 16};
-  const int pools[] = {1 << 19, 1 << 20, 1 << 21};
-  const int lanes[] = {1, 2, 3};
+  const int slots[] = {2, 4, 8, 16};
+  const int pools[] = {1 << 20, 1 << 21, 1 << 22};
+  const int lanes[] = {2, 3, 4};
   rmn_tune_result best{16, 1 << 20, 1e30, 0.0, 0, 2};
-  for (int si = 0; si < 3 && r == RMN_OK; ++si)
+  for (int si = 0; si < 4 && r == RMN_OK; ++si)
     for (int pi = 0; pi < 3 && r == RMN_OK; ++pi)
       for (int li = 0; li < 3 && r == RMN_OK; ++li) {
         for (RenderItem& it : its) it.args.slots_per_unit = slots[si];
