@@ -274,7 +274,9 @@ rmn_status rmn_batch_destroy(rmn_batch* batch);
 
 /* Project-written autotuner for batches. Times candidate launch
  * configurations -- slots per work unit in {2, 4, 8, 16} x workers per lane
- * in {2^20, 2^21, 2^22} x lanes in {2, 3, 4} -- on a proxy of the batch whose
+ * in {2^20, ..., 2^23} x lanes in {2, 3, 4}, leaving out those whose
+ * full-size batch would take more than half of the free device memory (the
+ * library default, 16 x 2^20 x 2, is always timed) -- on a proxy of the batch whose
  * images keep every item's scene, spp, depth and field of view but only
  * `pixel_fraction` (0 < f <= 1) of its pixels, and returns the fastest. Set
  * each item's slots_per_unit and the batch's pool_workers and lanes from the

@@ -690,6 +690,19 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
   rmn_status r = make_items(items, n, its, false);
   if (r != RMN_OK) return r;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
+  // Candidates whose full-size batch would take more than half of the free
+  // device memory are not tried.
+  const std::vector<RenderItem> full = its;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess) {
+    cudaGetLastError();
+    free_b = 0;
+  }
+  auto fits = [&](int slots, int pool, int lanes) {
+    std::vector<RenderItem> f = full;
+    for (RenderItem& it : f) it.args.slots_per_unit = slots;
+    return batch_device_bytes(f.data(), n, pool, lanes) <= free_b / 2;
+  };
   // Proxy renders: the same scenes, spp, depth and field of view at a
   // fraction of the pixels, into buffers owned by the tuner.
   const float scale = std::sqrt(pixel_fraction);
@@ -720,12 +733,14 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
   if (e == cudaSuccess) e = cudaEventCreate(&e1);
   if (e != cudaSuccess) r = cuda_fail(e, "autotune set-up");
   const int slots[] = {2, 4, 8, 16};
-  const int pools[] = {1 << 20, 1 << 21, 1 << 22};
+  const int pools[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
   const int lanes[] = {2, 3, 4};
   rmn_tune_result best{16, 1 << 20, 1e30, 0.0, 0, 2};
   for (int si = 0; si < 4 && r == RMN_OK; ++si)
-    for (int pi = 0; pi < 3 && r == RMN_OK; ++pi)
+    for (int pi = 0; pi < 4 && r == RMN_OK; ++pi)
       for (int li = 0; li < 3 && r == RMN_OK; ++li) {
+        const bool is_default = slots[si] == 16 && pools[pi] == (1 << 20) && lanes[li] == 2;
+        if (!is_default && !fits(slots[si], pools[pi], lanes[li])) continue;
         for (RenderItem& it : its) it.args.slots_per_unit = slots[si];
         BatchState* b = nullptr;
         r = batch_create(its.data(), n, true, pools[pi], lanes[li], st, &b);

@@ -1428,6 +1428,27 @@ rmn_status batch_update(BatchState* b, const rmn_render_args* args, int n, cudaS
 }
 
 size_t batch_job_bytes() { return sizeof(Job); }
+
+// Device bytes batch_create would take for these items: the unit partials,
+// and per worker its state, shadow-ray slots and queue entries (media and
+// ray differentials where a scene needs them).
+size_t batch_device_bytes(const RenderItem* items, int n, int pool_workers, int lanes) {
+  JobTable t;
+  build_jobs(items, n, &t);
+  bool glass = false, tex = false;
+  for (const Job& j : t.jobs) {
+    glass = glass || j.p.glass;
+    tex = tex || j.s.has_tex;
+  }
+  const int nl = lanes > 0 ? std::min(lanes, kMaxLanes) : kDefaultLanes;
+  long long per = pool_workers > 0 ? pool_workers : kDefaultPoolWorkers;
+  per = std::min<long long>(per, (t.total_units + nl - 1) / nl);
+  const size_t worker = 4 * sizeof(int4) + sizeof(long long) + 2 * sizeof(float4) + sizeof(float2) + 8 * sizeof(float4) +
+                        sizeof(int4) + kDirectBatch * (3 * sizeof(float4) + sizeof(float)) + sizeof(int2) +
+                        sizeof(int) * (2 * (3 + kDirectBatch) + 2) + (glass ? RMN_MEDIA * 20 + 4 : 0) +
+                        (tex ? 3 * sizeof(float4) : 0);
+  return sizeof(float4) * RMN_PART_F4 * (size_t)t.total_units + worker * (size_t)per * nl;
+}
 int batch_items(const BatchState* b) { return (int)b->table.jobs.size(); }
 
 rmn_status batch_status(BatchState* b, cudaStream_t st) {
