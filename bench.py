@@ -450,7 +450,7 @@ def run_gpu(args, rank, world, dist):
         tune["tune_s"] = round(time.perf_counter() - t0, 2)
         for a in argsl:
             a.slots_per_unit = tune["slots_per_unit"]
-    lanes = tune["lanes"] if tune else 2
+    lanes = (tune["lanes"] if tune else 0) or 3  # 0: the library default, 3 lanes
     with torch.cuda.stream(stream):
         batch = api.Batch(list(zip(models, argsl, photos)), use_graph=True, stream=stream,
                           pool_workers=tune["pool_workers"] if tune else 0, lanes=tune["lanes"] if tune else 0)

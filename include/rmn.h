@@ -150,7 +150,9 @@ typedef struct rmn_render_args {
   int32_t max_depth;                   /* 16 in the reference (src/render.cpp:125); 1..16 */
   uint64_t seed;                       /* counter-based random stream key */
   int32_t lanes_per_pixel;             /* work units per pixel (0: from slots_per_unit); 1..64 */
-  int32_t slots_per_unit;              /* sample slots per work unit (0: library default 16) */
+  int32_t slots_per_unit;              /* sample slots per work unit (0: library default: 2 for renders of up to
+                                          2^26 sample slots, else 4, more when the per-unit records would take
+                                          over a quarter of the free device memory) */
   int32_t reserved[2];
 } rmn_render_args;
 
@@ -254,8 +256,9 @@ typedef struct rmn_batch_item {
 /* Launch knobs of a batch; NULL options = {1, 0, 0}. */
 typedef struct rmn_batch_options {
   int32_t use_graph;     /* replay the wavefront iterations from captured CUDA graphs */
-  int32_t pool_workers;  /* paths in flight per lane (0: library default, 2^20) */
-  int32_t lanes;         /* independent wavefronts run side by side, 1..4 (0: library default, 2) */
+  int32_t pool_workers;  /* paths in flight per lane (0: library default, 2^22, halved while the workers
+                            would take over a quarter of the free device memory) */
+  int32_t lanes;         /* independent wavefronts run side by side, 1..4 (0: library default, 3) */
   int32_t reserved;
 } rmn_batch_options;
 rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_batch_options* options, void* stream,
@@ -276,17 +279,17 @@ rmn_status rmn_batch_destroy(rmn_batch* batch);
  * configurations -- slots per work unit in {2, 4, 8, 16} x workers per lane
  * in {2^20, ..., 2^23} x lanes in {2, 3, 4}, leaving out those whose
  * full-size batch would take more than half of the free device memory (the
- * library default, 16 x 2^20 x 2, is always timed) -- on a proxy of the batch whose
+ * library's own choice is always timed) -- on a proxy of the batch whose
  * images keep every item's scene, spp, depth and field of view but only
  * `pixel_fraction` (0 < f <= 1) of its pixels, and returns the fastest. Set
  * each item's slots_per_unit and the batch's pool_workers and lanes from the
  * result. The images do not depend on the choice beyond float summation
  * order across units (slots_per_unit); pool size and lanes change nothing. */
 typedef struct rmn_tune_result {
-  int32_t slots_per_unit, pool_workers;
+  int32_t slots_per_unit, pool_workers;  /* 0: the library's default won */
   double best_ms, default_ms;  /* proxy render time: best and library default */
   int32_t candidates;
-  int32_t lanes;
+  int32_t lanes;               /* 0: the library's default won */
 } rmn_tune_result;
 rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixel_fraction, rmn_tune_result* out,
                               void* stream);

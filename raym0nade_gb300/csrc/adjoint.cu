@@ -136,9 +136,11 @@ struct PathAdj {
   float3 A_light, A_w0, dbase;
 };
 
-__device__ __forceinline__ bool occluded(const DevScene& s, float3 pos, float3 dir, float aim, int* status) {
+// stk: the thread's deferred-child stack in shared memory.
+__device__ __forceinline__ bool occluded(const DevScene& s, float3 pos, float3 dir, float aim, int* status,
+                                         int2* stk) {
   float tm = aim + RMN_EPS;  // HitRecord(eps, aimDepth + eps), Model::rayHit_test
-  int st = trace<true, false, false>(s, make_tray(pos, dir), RMN_EPS, tm, aim, nullptr);  // no textured scenes here
+  int st = trace_shared<true>(s, make_tray(pos, dir), RMN_EPS, tm, aim, stk);  // no textured scenes here
   if (st == -2) {
     atomicExch(status, 1);
     return false;
@@ -160,7 +162,7 @@ struct Record {
   float3 l, q, lr;
 };
 
-__device__ void adjoint_slot(const AdjJob& J, int pixel, int j, GradSink& G, int* status) {
+__device__ void adjoint_slot(const AdjJob& J, int pixel, int j, GradSink& G, int* status, int2* stk) {
   const Params& p = J.p;
   const DevScene& s = J.s;
   const float* gb = J.gbuf + (size_t)RMN_GBUFFER_FLOATS * pixel;
@@ -197,7 +199,7 @@ __device__ void adjoint_slot(const AdjJob& J, int pixel, int j, GradSink& G, int
     LSample ls;
     int li = -1;
     if (!light_gen(s, g, Vd, lwt, tot, p.spp_d, rng, dir, aim, ls, &li)) return;
-    if (occluded(s, g.pos, dir, aim, status)) return;
+    if (occluded(s, g.pos, dir, aim, status, stk)) return;
     DemodAdj d = demod_adj(g.base, sav, ls.bsdf, ls.light, ls.weight, gpx, E);
     if (!finite1(d.S) || d.S == 0.0f) return;
     float3 l, q, lr;
@@ -251,7 +253,7 @@ __device__ void adjoint_slot(const AdjJob& J, int pixel, int j, GradSink& G, int
   };
   for (;;) {
     float tm = INFINITY;
-    int h = trace<false, false, false>(s, make_tray(o, dir), RMN_EPS, tm, 0.0f, nullptr);
+    int h = trace_shared<false>(s, make_tray(o, dir), RMN_EPS, tm, 0.0f, stk);
     if (h == -2) {
       atomicExch(status, 1);
       return;
@@ -296,7 +298,7 @@ __device__ void adjoint_slot(const AdjJob& J, int pixel, int j, GradSink& G, int
         int li = -1;
         if (!light_gen(s, sf, V, lwt, tot, cnt, rng, ld, aim, ls, &li)) continue;
         ls.bsdf *= k;
-        if (occluded(s, sf.pos, ld, aim, status)) continue;
+        if (occluded(s, sf.pos, ld, aim, status, stk)) continue;
         if (drop == sid0 + n) continue;
         const float3 light = (ls.light * ls.bsdf) * thr;
         DemodAdj d = add_sample(light, ls.weight * paw * p.inv_spp);
@@ -341,7 +343,7 @@ __device__ void adjoint_slot(const AdjJob& J, int pixel, int j, GradSink& G, int
   G.add(m0, 3, dot3(acc.A_w0, lr0));
 }
 
-__global__ void __launch_bounds__(128) adjoint_kernel(AdjJob J, long long total, int nmats, double* gout,
+__global__ void __launch_bounds__(128, 8) adjoint_kernel(AdjJob J, long long total, int nmats, double* gout,
                                                       int* status) {
   extern __shared__ float sg[];
   const bool use_sh = nmats <= kSharedMats;
@@ -350,13 +352,14 @@ __global__ void __launch_bounds__(128) adjoint_kernel(AdjJob J, long long total,
     __syncthreads();
   }
   GradSink G{sg, gout, use_sh};
+  __shared__ int2 sstack[RMN_STACK * 128];  // traversal stacks (launched with 128 threads)
   // Slot-major order: the lanes of a warp replay the same slot of 32
   // neighbouring pixels, so they run the same kind of work (a first-vertex
   // light sample or a path) on nearby surfaces.
   const long long npx = (long long)J.p.W * J.p.H;
   for (long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x; t < total;
        t += (long long)gridDim.x * blockDim.x)
-    adjoint_slot(J, (int)(t % npx), (int)(t / npx), G, status);
+    adjoint_slot(J, (int)(t % npx), (int)(t / npx), G, status, sstack + threadIdx.x);
   if (use_sh) {
     __syncthreads();
     for (int i = threadIdx.x; i < nmats * kGradPerMat; i += blockDim.x)

@@ -735,36 +735,40 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
   const int slots[] = {2, 4, 8, 16};
   const int pools[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
   const int lanes[] = {2, 3, 4};
-  rmn_tune_result best{16, 1 << 20, 1e30, 0.0, 0, 2};
-  for (int si = 0; si < 4 && r == RMN_OK; ++si)
-    for (int pi = 0; pi < 4 && r == RMN_OK; ++pi)
-      for (int li = 0; li < 3 && r == RMN_OK; ++li) {
-        const bool is_default = slots[si] == 16 && pools[pi] == (1 << 20) && lanes[li] == 2;
-        if (!is_default && !fits(slots[si], pools[pi], lanes[li])) continue;
-        for (RenderItem& it : its) it.args.slots_per_unit = slots[si];
-        BatchState* b = nullptr;
-        r = batch_create(its.data(), n, true, pools[pi], lanes[li], st, &b);
-        if (r != RMN_OK) break;
-        r = batch_launch(b, st);  // warm-up
-        if (r == RMN_OK) {
-          cudaEventRecord(e0, st);
-          r = batch_launch(b, st);
-          cudaEventRecord(e1, st);
-        }
-        if (r == RMN_OK) r = batch_status(b, st);
-        float ms = 0.0f;
-        if (r == RMN_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(RMN_ERR_CUDA, "event timing");
-        batch_destroy(b);
-        if (r != RMN_OK) break;
-        best.candidates++;
-        if (slots[si] == 16 && pools[pi] == (1 << 20) && lanes[li] == 2) best.default_ms = ms;
-        if (ms < best.best_ms) {
-          best.best_ms = ms;
-          best.slots_per_unit = slots[si];
-          best.pool_workers = pools[pi];
-          best.lanes = lanes[li];
-        }
-      }
+  // candidate 0: the library's own choice (the items' slots_per_unit, pool
+  // and lanes left at 0); then the grid
+  rmn_tune_result best{0, 0, 1e30, 0.0, 0, 0};
+  std::vector<int> proxy_slots(its.size());
+  for (size_t i = 0; i < its.size(); ++i) proxy_slots[i] = its[i].args.slots_per_unit;
+  for (int ci = -1; ci < 4 * 4 * 3 && r == RMN_OK; ++ci) {
+    const int si = ci < 0 ? 0 : ci / 12, pi = ci < 0 ? 0 : (ci / 3) % 4, li = ci < 0 ? 0 : ci % 3;
+    const bool is_default = ci < 0;
+    const int cs = is_default ? 0 : slots[si], cp = is_default ? 0 : pools[pi], cl = is_default ? 0 : lanes[li];
+    if (!is_default && !fits(cs, cp, cl)) continue;
+    for (size_t i = 0; i < its.size(); ++i) its[i].args.slots_per_unit = is_default ? proxy_slots[i] : cs;
+    BatchState* b = nullptr;
+    r = batch_create(its.data(), n, true, cp, cl, st, &b);
+    if (r != RMN_OK) break;
+    r = batch_launch(b, st);  // warm-up
+    if (r == RMN_OK) {
+      cudaEventRecord(e0, st);
+      r = batch_launch(b, st);
+      cudaEventRecord(e1, st);
+    }
+    if (r == RMN_OK) r = batch_status(b, st);
+    float ms = 0.0f;
+    if (r == RMN_OK && cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) r = fail(RMN_ERR_CUDA, "event timing");
+    batch_destroy(b);
+    if (r != RMN_OK) break;
+    best.candidates++;
+    if (is_default) best.default_ms = ms;
+    if (ms < best.best_ms) {
+      best.best_ms = ms;
+      best.slots_per_unit = cs;
+      best.pool_workers = cp;
+      best.lanes = cl;
+    }
+  }
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);
   cudaStreamSynchronize(st);

@@ -1007,14 +1007,15 @@ int blocks_per_sm(K kernel) {
 
 namespace rmn {
 
-constexpr int kDefaultPoolWorkers = 1 << 20;  // per lane
-constexpr int kDefaultLanes = 2;
+constexpr int kDefaultPoolWorkers = 1 << 22;  // per lane, fewer when device memory is short
+constexpr int kDefaultLanes = 3;
 constexpr int kIterationsPerChunk = 8;
 constexpr long long kMaxIterations = 1LL << 22;  // bound on the iteration loop; a finite render never reaches it
 
 struct JobTable {
   std::vector<Job> jobs;
   std::vector<int> item;  // job k renders item item[k] of the caller's list
+  std::vector<int> slots; // slots per unit chosen for an item that left it to the library (else 0)
   int total_pix = 0;
   long long total_units = 0;
 };
@@ -1272,15 +1273,83 @@ void batch_destroy(BatchState* b) {
   delete b;
 }
 
-rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, int lanes,
+// Bytes of one worker's state, shadow-ray slots and queue entries (media and
+// ray differentials where a scene needs them).
+static size_t worker_bytes(bool glass, bool tex) {
+  return 4 * sizeof(int4) + sizeof(long long) + 2 * sizeof(float4) + sizeof(float2) + 8 * sizeof(float4) +
+         sizeof(int4) + kDirectBatch * (3 * sizeof(float4) + sizeof(float)) + sizeof(int2) +
+         sizeof(int) * (2 * (3 + kDirectBatch) + 2) + (glass ? RMN_MEDIA * 20 + 4 : 0) + (tex ? 3 * sizeof(float4) : 0);
+}
+
+static size_t free_device_bytes() {
+  size_t f = 0, t = 0;
+  if (cudaMemGetInfo(&f, &t) != cudaSuccess) {
+    cudaGetLastError();
+    return 0;
+  }
+  return f;
+}
+
+// The library's unit split for the items that leave it open
+// (slots_per_unit = lanes_per_pixel = 0; others get 0 in S): 2 slots per
+// unit for an item of up to 2^26 sample slots, 4 above -- a choice of the
+// item alone, so its images do not depend on the batch around it -- all
+// doubled while the unit partials (112 B each) of those items would take
+// more than a quarter of the free device memory. Short units drain the
+// wavefront evenly; the partials are the price.
+void default_slots_per_unit(const RenderItem* items, int n, int* S) {
+  std::vector<long long> slots(n, 0);
+  for (int i = 0; i < n; ++i) {
+    S[i] = 0;
+    if (items[i].args.slots_per_unit != 0 || items[i].args.lanes_per_pixel != 0) continue;
+    rmn_render_args a = items[i].args;
+    a.slots_per_unit = 1;
+    const Params p = make_params(a, items[i].scene->dev.has_glass != 0);
+    slots[i] = (long long)p.W * p.H * p.K;
+    S[i] = slots[i] <= (1LL << 26) ? 2 : 4;
+  }
+  const size_t budget = free_device_bytes() / 4;
+  for (int f = 1; f < (1 << 18); f *= 2) {
+    size_t bytes = 0;
+    for (int i = 0; i < n; ++i)
+      if (S[i]) bytes += (size_t)(slots[i] / ((long long)S[i] * f) + 1) * sizeof(float4) * RMN_PART_F4;
+    if (bytes <= budget) {
+      for (int i = 0; i < n; ++i) S[i] *= f;
+      return;
+    }
+  }
+  for (int i = 0; i < n; ++i)
+    if (S[i]) S[i] = 1 << 20;
+}
+
+rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int pool_workers, int lanes,
                         cudaStream_t st, BatchState** out) {
   *out = nullptr;
+  // items that leave the unit split to the library take its default
+  std::vector<RenderItem> items_v(items_in, items_in + n);
+  std::vector<int> S_def(n, 0);
+  default_slots_per_unit(items_in, n, S_def.data());
+  for (int i = 0; i < n; ++i)
+    if (S_def[i]) items_v[i].args.slots_per_unit = S_def[i];
+  const RenderItem* items = items_v.data();
   BatchState* b = new BatchState();
   build_jobs(items, n, &b->table);
+  b->table.slots = S_def;
   b->use_graph = use_graph;
   b->lanes = lanes > 0 ? std::min(lanes, kMaxLanes) : kDefaultLanes;
-  // workers per lane; no more lanes and workers than there are units
+  // workers per lane; no more lanes and workers than there are units; the
+  // default pool halves while the workers would take more than a quarter of
+  // the free device memory
   long long per = pool_workers > 0 ? pool_workers : kDefaultPoolWorkers;
+  if (pool_workers <= 0) {
+    bool glass = false, tex = false;
+    for (const Job& j : b->table.jobs) {
+      glass = glass || j.p.glass;
+      tex = tex || j.s.has_tex;
+    }
+    const size_t budget = free_device_bytes() / 4;
+    while (per > 4096 && worker_bytes(glass, tex) * (size_t)per * b->lanes > budget) per /= 2;
+  }
   while (b->lanes > 1 && (long long)b->lanes * 128 > b->table.total_units) --b->lanes;
   per = std::min<long long>(per, (b->table.total_units + b->lanes - 1) / b->lanes);
   if (per < 1) per = 1;
@@ -1410,7 +1479,10 @@ rmn_status batch_update(BatchState* b, const rmn_render_args* args, int n, cudaS
   std::vector<Job> next = b->table.jobs;
   for (int k = 0; k < nj; ++k) {
     Job& j = next[k];
-    const Params q = make_params(args[b->table.item[k]], j.p.glass != 0);
+    rmn_render_args a = args[b->table.item[k]];
+    const int S_def = b->table.slots[b->table.item[k]];
+    if (S_def && a.slots_per_unit == 0 && a.lanes_per_pixel == 0) a.slots_per_unit = S_def;
+    const Params q = make_params(a, j.p.glass != 0);
     const Params& p = j.p;
     if (q.W != p.W || q.H != p.H || q.spp != p.spp || q.maxd != p.maxd || q.spp_d != p.spp_d || q.S != p.S ||
         q.K != p.K || q.slots != p.slots || q.slots16 != p.slots16)
@@ -1443,11 +1515,7 @@ size_t batch_device_bytes(const RenderItem* items, int n, int pool_workers, int 
   const int nl = lanes > 0 ? std::min(lanes, kMaxLanes) : kDefaultLanes;
   long long per = pool_workers > 0 ? pool_workers : kDefaultPoolWorkers;
   per = std::min<long long>(per, (t.total_units + nl - 1) / nl);
-  const size_t worker = 4 * sizeof(int4) + sizeof(long long) + 2 * sizeof(float4) + sizeof(float2) + 8 * sizeof(float4) +
-                        sizeof(int4) + kDirectBatch * (3 * sizeof(float4) + sizeof(float)) + sizeof(int2) +
-                        sizeof(int) * (2 * (3 + kDirectBatch) + 2) + (glass ? RMN_MEDIA * 20 + 4 : 0) +
-                        (tex ? 3 * sizeof(float4) : 0);
-  return sizeof(float4) * RMN_PART_F4 * (size_t)t.total_units + worker * (size_t)per * nl;
+  return sizeof(float4) * RMN_PART_F4 * (size_t)t.total_units + worker_bytes(glass, tex) * (size_t)per * nl;
 }
 int batch_items(const BatchState* b) { return (int)b->table.jobs.size(); }
 

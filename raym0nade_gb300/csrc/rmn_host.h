@@ -67,6 +67,7 @@ rmn_status batch_launch(BatchState* b, cudaStream_t st);
 rmn_status batch_update(BatchState* b, const rmn_render_args* args, int n, cudaStream_t st);
 size_t batch_job_bytes();
 size_t batch_device_bytes(const RenderItem* items, int n, int pool_workers, int lanes);
+void default_slots_per_unit(const RenderItem* items, int n, int* S);
 int batch_items(const BatchState* b);
 rmn_status batch_status(BatchState* b, cudaStream_t st);
 rmn_status batch_profile(BatchState* b, cudaStream_t st, RenderProfileData* prof);

@@ -209,6 +209,19 @@ RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav
   }
 }
 
+// One whole query without the alpha retry (scenes without alpha-tested
+// materials), its deferred-child stack in shared memory at `stk` (entry e
+// at stk[e * 128], see SharedStackN). Same answer as trace().
+template <bool ANY>
+RMN_D int trace_shared(const DevScene& s, const TRay& r, float tmin, float& tmax, float aim, int2* stk) {
+  TravT<SharedStackN<RMN_STACK>> t;
+  t.stack.base = stk;
+  trav_begin(s, t, tmax);
+  int st = trav_run<ANY, false>(s, r, tmin, aim, t, 0x7fffffff, nullptr);
+  tmax = t.tmax;
+  return st == -2 ? -2 : t.hit;
+}
+
 // barycentric(v0, v1, v2, P), src/geometry.cpp:89-103, with e1 = v1 - v0 and
 // e2 = v2 - v0 precomputed. Returns (gamma, alpha, beta).
 RMN_D float3 bary(float3 v0, float3 e1, float3 e2, float3 p) {
