@@ -685,6 +685,31 @@ __device__ __noinline__ void first_bounce_glass(const Pool& P, int w, const Surf
   first_bounce<true>(P, w, g, eye, rng, dir, w0, f0, d0);
 }
 
+// Fetch order of a job's units: tiles of kFetchTile pixels, within a tile
+// first every pixel's units that start with a light-sample slot, then its
+// path units, so the 32 lanes of a warp fetching together start the same
+// kind of slot. The record of unit (pixel, sub) stays at pixel * K + sub:
+// results do not depend on the order.
+constexpr int kFetchTile = 32;
+__device__ __forceinline__ void unit_of_fetch(const Params& p, long long local, int& pixel, int& sub) {
+  const int K = p.K;
+  const int Kd = min(K, (p.spp_d + p.S - 1) / p.S);  // units starting with a light-sample slot
+  const long long per_tile = (long long)kFetchTile * K;
+  const long long tile = local / per_tile;
+  const int r = (int)(local - tile * per_tile);
+  const int npx = p.W * p.H;
+  const int first = (int)(tile * kFetchTile);
+  const int pt = min(kFetchTile, npx - first);
+  if (r < pt * Kd) {
+    pixel = first + r / Kd;
+    sub = r % Kd;
+  } else {
+    const int r2 = r - pt * Kd, Ki = K - Kd;
+    pixel = first + r2 / Ki;
+    sub = Kd + r2 % Ki;
+  }
+}
+
 template <bool COUNT>
 __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jobs, int njobs, Pool P, Queues Q,
                                                       Ctl* ctl, unsigned long long* next_unit, int par,
@@ -737,8 +762,9 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
         uid = (long long)u;
         int jb = find_job_unit(jobs, njobs, uid);
         J = &jobs[jb];
-        long long local = uid - J->unit_begin;
-        int pixel = (int)(local / J->p.K), sub = (int)(local % J->p.K);
+        int pixel, sub;
+        unit_of_fetch(J->p, uid - J->unit_begin, pixel, sub);
+        uid = J->unit_begin + (long long)pixel * J->p.K + sub;  // the unit's record, in pixel order
         const float* gb0 = gbuf_of(*J, pixel);
         // 16 times the indirect samples behind a transmissive or half-opaque
         // first vertex (renderPixel, src/render.cpp:497-499); the units of a
