@@ -49,7 +49,7 @@ FALLBACK_HBM_GBS = 6800.0
 # DRAM bytes (read + write) of all traversal launches of one batch64 render,
 # summed from an ncu capture of `python -m raym0nade_gb300.profile_case batch`
 # (profiles/launches_batch64.md); ncu cannot run inside the timed region.
-BATCH64_TRAVERSAL_DRAM_BYTES = 136.94e9 + 15.10e9
+BATCH64_TRAVERSAL_DRAM_BYTES = 136.05e9 + 14.83e9
 
 
 def measured_peaks():
