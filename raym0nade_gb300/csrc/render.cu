@@ -1160,11 +1160,13 @@ static cudaError_t launch_iteration(BatchState* b, int lane, cudaStream_t st, Co
   if (ev) cudaEventRecord(ev[1], st);
   const int lb = (P.W + 127) / 128;
   if (ctr) {
-    if (b->alpha) launch_qtrace<true, true, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
+    if (b->alpha && b->shallow) launch_qtrace<true, true, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
+    else if (b->alpha) launch_qtrace<true, true, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
     else if (b->shallow) launch_qtrace<true, false, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
     else launch_qtrace<true, false, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
   } else {
-    if (b->alpha) launch_qtrace<false, true, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
+    if (b->alpha && b->shallow) launch_qtrace<false, true, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
+    else if (b->alpha) launch_qtrace<false, true, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
     else if (b->shallow) launch_qtrace<false, false, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
     else launch_qtrace<false, false, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
   }
