@@ -13,21 +13,21 @@
 
 namespace {
 
-uint32_t crc_table[256];
-bool crc_ready = false;
-
-void crc_init() {
-  for (uint32_t n = 0; n < 256; ++n) {
-    uint32_t c = n;
-    for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-    crc_table[n] = c;
+struct CrcTable {
+  uint32_t t[256];
+  CrcTable() {
+    for (uint32_t n = 0; n < 256; ++n) {
+      uint32_t c = n;
+      for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
+      t[n] = c;
+    }
   }
-  crc_ready = true;
-}
+};
 
 uint32_t crc32(uint32_t crc, const uint8_t* p, size_t n) {
+  static const CrcTable table;  // initialised once, thread-safe
   crc = ~crc;
-  for (size_t i = 0; i < n; ++i) crc = crc_table[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
+  for (size_t i = 0; i < n; ++i) crc = table.t[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
   return ~crc;
 }
 
@@ -61,7 +61,6 @@ uint8_t to_byte(float v) {
 namespace rmn {
 
 rmn_status write_png(const float* rgb, int w, int h, const char* path) {
-  if (!crc_ready) crc_init();
   // scanlines: filter byte 0, then RGB bytes
   const size_t row = 1 + 3 * (size_t)w;
   std::vector<uint8_t> raw(row * h);
