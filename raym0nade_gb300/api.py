@@ -414,21 +414,19 @@ class Batch:
 
 
 def render_multiThread(model: Model, args: RenderArgs) -> Photo:
-    """render_multiThread (include/render.h:43): render, then export the
-    images the reference exports before its denoiser runs
-    (src/render.cpp:641-653, minus spatialClamp/bloom) to savePath + '(tag).ppm'."""
+    """render_multiThread (include/render.h:43, src/render.cpp:593-677):
+    render, then write the reference's export set (src/render.cpp:641-674:
+    spatialClamp, filter, bloom, depth of field when CoC > eps, FXAA) to
+    savePath + '(tag).png'; the radiance buffers end clamped and filtered,
+    as the reference's Photo does."""
     photo = render(model, args)
     if args.savePath:
         d = os.path.dirname(args.savePath)
         if d:
             os.makedirs(d, exist_ok=True)
-        exports = [("DiffuseColor", BaseColor), ("DiffuseColor_FXAA", BaseColor | DoFXAA),
-                   ("shapeNormal", shapeNormal), ("surfaceNormal", surfaceNormal),
-                   ("Direct_Diffuse", Direct_Diffuse), ("Direct_Specular", Direct_Specular),
-                   ("Indirect_Diffuse", Indirect_Diffuse), ("Indirect_Specular", Indirect_Specular),
-                   ("Raw", Full), ("Raw_FXAA", Full | DoFXAA)]
-        for tag, opt in exports:
-            Photo.save(photo.postProcessing(opt), f"{args.savePath}({tag}).ppm")
+        photo.focus, photo.CoC, photo.cameraPosition = args.focus, args.CoC, tuple(args.position)
+        for tag, rgb in photo.export_set().items():
+            Photo.save(rgb, f"{args.savePath}({tag}).png")
     return photo
 
 

@@ -134,3 +134,18 @@ def test_export_set_matches_oracle_sequence(port):
     assert close_frac(radiance(ph), r.reshape(-1, 40)[:, :16]) >= 0.999
     ph2 = photo_from_records(rec, dict(post, coc=0.0))
     assert len(ph2.export_set()) == api.EXPORTS
+
+
+def test_render_multithread_writes_the_export_set(tmp_path):
+    """The render_multiThread mirror: a render, then the reference's 25
+    exports (depth of field on) as PNG files named savePath(tag).png."""
+    from tests.test_library import _read_png
+    cam = scenes.cornell_camera(32, 24, 8)
+    a = api.RenderArgs.from_camera(cam, seed=2, savePath=str(tmp_path / "out" / "img"))
+    a.focus, a.CoC = 1.5, 2.0
+    api.render_multiThread(api.Model(scenes.cornell()), a)
+    lib = api._lib.load()
+    for k in range(api.EXPORTS + api.EXPORTS_DOF):
+        tag = lib.rmn_export_tag(k).decode()
+        img = _read_png(str(tmp_path / "out" / f"img({tag}).png"))
+        assert img.shape == (24, 32, 3)
