@@ -368,6 +368,46 @@ def config_timings(args, stream, flush, barrier):
                        "cpu_port_Mpaths_s": cpu["Mpaths_s"], "cpu_sample": cpu["sample"],
                        "workload": "textured room (diffuse / specular / emissive / normal-map textures with mip "
                                    "chains, alpha-tested cutouts), 1024x768, 64 spp, max depth 16 (rmn_render)"}
+    out["asset_decode"] = asset_decode_timings(max(1, min(args.steps, 3)))
+    return out
+
+
+def asset_decode_timings(repeats):
+    """rmn_image_load (host, one thread) on full-size asset files written
+    here: a 2048x1024 run-length-encoded Radiance sky, a 2048x2048 DXT5 DDS
+    texture and a 2048x2048 RGB PNG (zlib level 6, Sub / Up / Paeth rows).
+    Best of `repeats` wall-clock decodes each."""
+    import shutil
+    import tempfile
+    from raym0nade_gb300 import assets, scenes
+    from tests.golden import image_files as F
+    d = tempfile.mkdtemp()
+    rng = np.random.default_rng(9)
+    files = {}
+    p = os.path.join(d, "sky.hdr")
+    with open(p, "wb") as f:
+        f.write(F.encode_hdr(F.float_to_rgbe(scenes.sky_env(2048, 1024))))
+    files["hdr_2048x1024_rle"] = (p, assets.HDR)
+    p = os.path.join(d, "tex.dds")
+    with open(p, "wb") as f:
+        f.write(F.encode_dds(2048, 2048, rng.integers(0, 256, 512 * 512 * 16, dtype=np.uint8).tobytes(), b"DXT5"))
+    files["dds_dxt5_2048x2048"] = (p, assets.DDS)
+    yy, xx = np.mgrid[0:2048, 0:2048]
+    img = np.stack([(xx // 8) % 256, (yy // 8) % 256, ((xx + yy) // 16) % 256], -1) + rng.integers(0, 4, (2048, 2048, 3))
+    p = os.path.join(d, "tex.png")
+    with open(p, "wb") as f:
+        f.write(F.encode_png(np.minimum(img, 255), 2, 8, filters=(1, 2, 4), level=6))
+    files["png_rgb8_2048x2048"] = (p, assets.PNG)
+    out = {}
+    for name, (p, kind) in files.items():
+        best, nbytes = float("inf"), 0
+        for _ in range(repeats):
+            t0 = time.perf_counter()
+            a = assets.load_image(p, kind)
+            best = min(best, time.perf_counter() - t0)
+            nbytes = a.nbytes
+        out[name] = {"ms": best * 1e3, "decoded_MB_s": nbytes / best / 1e6, "file_MB": os.path.getsize(p) / 1e6}
+    shutil.rmtree(d)
     return out
 
 

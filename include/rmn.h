@@ -373,6 +373,35 @@ rmn_status rmn_export_set(const rmn_image* image, const rmn_post_args* args, flo
  * are stored uncompressed (deflate stored blocks). */
 rmn_status rmn_save_png(const float* rgb, int32_t width, int32_t height, const char* path);
 
+/* Image decoders of the asset front-end (host memory, no GPU involved). */
+#define RMN_IMAGE_PNG 0 /* Material::loadImageFromPNG (src/material.cpp:217-285): 8-bit RGB,
+                           16-bit samples keep their high byte, gray and palette expand to RGB,
+                           alpha is dropped (libpng's strip_16 / expand / palette_to_rgb /
+                           gray_to_rgb / strip_alpha); Adam7-interlaced files are de-interlaced */
+#define RMN_IMAGE_DDS 1 /* scripts/dds_to_array.py as Material::loadImageFromDDS
+                           (src/material.cpp:190-215) takes it: DXT1/DXT3/DXT5 -> 8-bit RGBA,
+                           uncompressed 32-bit -> RGBA, 24-bit -> RGB */
+#define RMN_IMAGE_HDR 2 /* scripts/hdr_to_array.py as SkyBox::load (src/component.cpp:69-114)
+                           takes it: Radiance RGBE (flat or run-length encoded, "-Y H +X W")
+                           -> float32 RGB */
+
+typedef struct rmn_image_desc {
+  int32_t width, height, channels;
+  int32_t bytes_per_channel;   /* 1 (uint8) or 4 (float32) */
+} rmn_image_desc;
+
+/* Decode the image file `path` of the given kind into `data` (capacity
+ * bytes, host memory): width x height pixels of `channels` samples,
+ * row-major, row 0 = the image's top row. With data == NULL only `info` is
+ * filled (the header is read, the pixels are not decoded). Replaces the
+ * libpng call of Material::loadImageFromPNG and the embedded-Python calls of
+ * call_image_to_array (src/material.cpp:150-188). A malformed file, a
+ * missing file or a capacity below width*height*channels*bytes_per_channel
+ * gives RMN_ERR_INVALID_ARGUMENT; a valid variant outside the list above
+ * (DX10/BC4-BC7 DDS, XYZE or rotated HDR, unknown critical PNG chunks)
+ * gives RMN_ERR_UNSUPPORTED. */
+rmn_status rmn_image_load(const char* path, int32_t kind, rmn_image_desc* info, void* data, size_t capacity);
+
 /* The file tag of export k ("DiffuseColor", ..., "Filter_DepthFieldBlur_Bloom_FXAA") and its shade
  * options; NULL / -1 out of range. */
 const char* rmn_export_tag(int32_t k);

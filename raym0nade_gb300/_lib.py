@@ -77,6 +77,11 @@ class TuneResult(C.Structure):
                 ("default_ms", C.c_double), ("candidates", C.c_int32), ("lanes", C.c_int32)]
 
 
+class ImageDesc(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("channels", C.c_int32),
+                ("bytes_per_channel", C.c_int32)]
+
+
 # name -> (restype, argtypes); every declaration of include/rmn.h.
 SIGNATURES = {
     "rmn_last_error": (C.c_char_p, []),
@@ -113,6 +118,7 @@ SIGNATURES = {
     "rmn_export_tag": (C.c_char_p, [C.c_int32]),
     "rmn_save_png": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_char_p]),
     "rmn_export_options": (C.c_int32, [C.c_int32]),
+    "rmn_image_load": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(ImageDesc), C.c_void_p, C.c_size_t]),
 }
 
 _lib = None

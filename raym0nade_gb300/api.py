@@ -72,8 +72,14 @@ class Model:
     """A scene resident in HBM; what the reference's Model holds after
     Model::Model (faces, materials, light objects, sky map, BVH)."""
 
-    def __init__(self, scene: "_scenes.Scene"):
+    def __init__(self, scene, model_name: str | None = None, skyMap_name: str = "null"):
+        """Model(scene) from arrays, or Model(model_folder, model_name,
+        skyMap_name) as the reference's constructor (src/model.cpp:172):
+        an OBJ/MTL model imported by raym0nade_gb300.assets.load_model."""
         lib = _lib.load()
+        if isinstance(scene, str):
+            from . import assets
+            scene = assets.load_model(scene, model_name, skyMap_name)
         scene.check()
         self._keep = [np.ascontiguousarray(x) for x in (scene.positions, scene.normals, scene.uvs, scene.indices,
                                                         scene.mesh_first, scene.mesh_material, scene.materials)]

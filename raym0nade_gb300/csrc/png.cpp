@@ -24,13 +24,6 @@ struct CrcTable {
   }
 };
 
-uint32_t crc32(uint32_t crc, const uint8_t* p, size_t n) {
-  static const CrcTable table;  // initialised once, thread-safe
-  crc = ~crc;
-  for (size_t i = 0; i < n; ++i) crc = table.t[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
-  return ~crc;
-}
-
 void put32(std::vector<uint8_t>& v, uint32_t x) {
   v.push_back((uint8_t)(x >> 24));
   v.push_back((uint8_t)(x >> 16));
@@ -43,7 +36,7 @@ void chunk(std::vector<uint8_t>& out, const char* type, const std::vector<uint8_
   const size_t start = out.size();
   out.insert(out.end(), type, type + 4);
   out.insert(out.end(), data.begin(), data.end());
-  put32(out, crc32(0, out.data() + start, out.size() - start));
+  put32(out, rmn::png_crc32(0, out.data() + start, out.size() - start));
 }
 
 // The reference's byte: static_cast<png_byte>(v * 255). Defined here for
@@ -59,6 +52,13 @@ uint8_t to_byte(float v) {
 }  // namespace
 
 namespace rmn {
+
+uint32_t png_crc32(uint32_t crc, const uint8_t* p, size_t n) {
+  static const CrcTable table;  // initialised once, thread-safe
+  crc = ~crc;
+  for (size_t i = 0; i < n; ++i) crc = table.t[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
+  return ~crc;
+}
 
 rmn_status write_png(const float* rgb, int w, int h, const char* path) {
   // scanlines: filter byte 0, then RGB bytes

@@ -55,6 +55,8 @@ struct BatchState;
 
 // Photo::save as an 8-bit RGB PNG (png.cpp); rgb in host memory.
 rmn_status write_png(const float* rgb, int w, int h, const char* path);
+// CRC-32 of PNG chunks (ISO 3309 polynomial), shared by the writer and the reader.
+uint32_t png_crc32(uint32_t crc, const uint8_t* p, size_t n);
 
 // Device memory kept for reuse between batches (devmem.cpp).
 cudaError_t cached_malloc(void** p, size_t bytes);

@@ -29,6 +29,13 @@ Fixtures (numpy .npz, compressed):
                      (``photo_records``): spatialClamp, filter, bloom, depth
                      of field, postProcessing with and without them (the
                      cases of PHOTO_CASES). ``--photo`` writes it alone.
+  images/, images.npz  small PNG, Radiance HDR and DDS files (every PNG
+                     colour type family, Adam7, all filters, stored / fixed /
+                     dynamic deflate; flat and run-length HDR scanlines;
+                     BC1-BC3 and uncompressed DDS) and their decoded arrays:
+                     the written samples through libpng's transforms, RGBE
+                     m * 2^(e - 136), BC blocks through oracle/image_codecs.py.
+                     Needs no reference; ``--images`` writes them alone.
   cornell_4096spp.npz  the converged reference image of the Cornell workload
                      (256 x 256, 4096 spp, max depth 16, P_Direct 0.7):
                      Photo::shade(Full) before gamma, float16. Made by
@@ -215,6 +222,7 @@ def main():
     glass(R)
     textured()
     photo(R)
+    images()
 
     rgb_lin = R.compose(rec, 1.0, gamma=False)
     rgb = R.compose(rec, 1.0, gamma=True)
@@ -257,6 +265,61 @@ def textured():
                         seed=515, records=rec, rays=rays, face=face, t=t, bary=bc, shadow_rays=srays, occluded=occ)
 
 
+def images():
+    import shutil
+    import zlib
+
+    from oracle import image_codecs
+    from tests.golden import image_files as F
+    d = os.path.join(HERE, "images")
+    if os.path.isdir(d):
+        shutil.rmtree(d)
+    os.makedirs(d)
+    rng = np.random.default_rng(2718)
+    out = {}
+
+    def png(name, h, w, ctype, depth, **kw):
+        pal = kw.pop("palette", None)
+        s = rng.integers(0, 1 << depth, (h, w, F.PNG_CHANNELS[ctype]))
+        open(os.path.join(d, name), "wb").write(F.encode_png(s, ctype, depth, palette=pal, **kw))
+        out[name] = F.png_expected_rgb(s, ctype, depth, pal)
+
+    png("gray2_adam7.png", 9, 11, 0, 2, interlace=True, level=1, strategy=zlib.Z_FIXED, filters=(1, 2, 3, 4))
+    png("rgb16_paeth.png", 6, 10, 2, 16, filters=(4, 3), level=9)
+    png("palette4.png", 7, 9, 3, 4, palette=rng.integers(0, 256, (12, 3)), trns=bytes([0, 128]),
+        filters=(0, 1))
+    png("rgba8_stored.png", 5, 8, 6, 8, level=0, filters=(2, 4, 1))
+    png("graya16.png", 5, 5, 4, 16, interlace=True, filters=(3,))
+
+    def hdr(name, h, w, **kw):
+        rgbe = F.float_to_rgbe(np.exp(rng.normal(0.0, 3.0, (h, w, 3))))
+        rgbe[h // 2, :] = rgbe[h // 2, 0]
+        open(os.path.join(d, name), "wb").write(F.encode_hdr(rgbe, **kw))
+        out[name] = F.rgbe_expected(rgbe)
+
+    hdr("sky_rle.hdr", 12, 40, flat_from=9)
+    hdr("narrow_flat.hdr", 5, 4)
+
+    def bc(name, h, w, kind):
+        size = 8 if kind == 1 else 16
+        pay = rng.integers(0, 256, ((w + 3) // 4) * ((h + 3) // 4) * size).astype(np.uint8).tobytes()
+        open(os.path.join(d, name), "wb").write(F.encode_dds(w, h, pay, b"DXT%d" % (2 * kind - 1)))
+        out[name] = image_codecs.bc_decode(pay, w, h, kind)
+
+    bc("bc1.dds", 6, 10, 1)
+    bc("bc2.dds", 8, 8, 2)
+    bc("bc3.dds", 7, 13, 3)
+    px = rng.integers(0, 256, (5, 6, 4)).astype(np.uint8)
+    masks = (0x00FF0000, 0x0000FF00, 0x000000FF, 0xFF000000)
+    open(os.path.join(d, "bgra32.dds"), "wb").write(
+        F.encode_dds(6, 5, px.tobytes(), bitcount=32, masks=masks, alpha_flag=True))
+    out["bgra32.dds"] = px[..., [2, 1, 0, 3]]
+    open(os.path.join(d, "bgr24.dds"), "wb").write(
+        F.encode_dds(6, 5, px[..., :3].tobytes(), bitcount=24, masks=masks[:3] + (0,)))
+    out["bgr24.dds"] = px[..., [2, 1, 0]]
+    np.savez_compressed(os.path.join(HERE, "images.npz"), **out)
+
+
 def converged():
     bindings.build(with_reference=True)
     R = bindings.OracleLib("ref")
@@ -278,6 +341,9 @@ if __name__ == "__main__":
     elif "--photo" in sys.argv:
         photo()
         print("photo fixture written to", HERE)
+    elif "--images" in sys.argv:
+        images()
+        print("image files written to", os.path.join(HERE, "images"))
     elif "--textured" in sys.argv:
         textured()
         print("textured fixture written to", HERE)

@@ -48,7 +48,7 @@ def test_struct_sizes_match_header():
 ABI_STRUCTS = {"Material": "rmn_material", "SceneDesc": "rmn_scene_desc", "SceneInfo": "rmn_scene_info",
                "RenderArgs": "rmn_render_args", "Image": "rmn_image", "RenderProfile": "rmn_render_profile",
                "BatchItem": "rmn_batch_item", "BatchOptions": "rmn_batch_options", "TuneResult": "rmn_tune_result",
-               "Texture": "rmn_texture", "PostArgs": "rmn_post_args"}
+               "Texture": "rmn_texture", "PostArgs": "rmn_post_args", "ImageDesc": "rmn_image_desc"}
 
 
 def test_ctypes_layouts_match_c_compiler(tmp_path):
