@@ -408,6 +408,19 @@ def asset_decode_timings(repeats):
             nbytes = a.nbytes
         out[name] = {"ms": best * 1e3, "decoded_MB_s": nbytes / best / 1e6, "file_MB": os.path.getsize(p) / 1e6}
     shutil.rmtree(d)
+    # rmn_scene_create of the textured room with its eight textures replaced
+    # by 2048x2048 RGBA ones: level-0 upload (128 MiB) and the device-built
+    # mip chains, beside the BVH and tables of a 30-triangle scene
+    from raym0nade_gb300 import api
+    room = scenes.textured_room()
+    room.textures = [rng.integers(0, 256, (2048, 2048, 4), dtype=np.uint8) for _ in room.textures]
+    best = float("inf")
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        m = api.Model(room)
+        best = min(best, time.perf_counter() - t0)
+        del m
+    out["scene_create_8_textures_2048sq"] = {"ms": best * 1e3, "texture_MB": 8 * 2048 * 2048 * 4 / 1e6}
     return out
 
 

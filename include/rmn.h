@@ -60,13 +60,13 @@ typedef struct rmn_material {
   float roughness;       /* specular texel G, or Material::roughness without one */
   float metallic;        /* specular texel B (clamped to <= 0.99); 0 without one */
   float has_specular;    /* 1: roughness/metallic come from a specular texel */
-  float opacity;         /* 1 opaque; < 1e-4 transmissive (not on the GPU path) */
+  float opacity;         /* 1 opaque; < 1e-4 transmissive (refraction, media); between: half-opaque */
   float ior;
   float transmitting_color[3];
 } rmn_material;
 
 /* 8-bit texture as the reference's DDS loader leaves it in ImageData
- * (Material::loadImageFromDDS, src/material.cpp:61-95): width x height
+ * (Material::loadImageFromDDS, src/material.cpp:190-215): width x height
  * texels of `channels` bytes, row-major, row 0 = the image's top row
  * (texture v = 1). channels must be 4 (RGBA): the reference reads every
  * diffuse, specular and emissive lookup with a 4-byte stride and normal-map
@@ -401,6 +401,15 @@ typedef struct rmn_image_desc {
  * (DX10/BC4-BC7 DDS, XYZE or rotated HDR, unknown critical PNG chunks)
  * gives RMN_ERR_UNSUPPORTED. */
 rmn_status rmn_image_load(const char* path, int32_t kind, rmn_image_desc* info, void* data, size_t capacity);
+
+/* Copy mip level `level` of scene texture `texture` (RGBA8, built by
+ * rmn_scene_create as ImageData::generateMipmaps builds it,
+ * src/material.cpp:107-129) from the device into host memory `out`
+ * (capacity bytes); `info` receives its size (channels 4, 1 byte each).
+ * With out == NULL only `info` is filled. A texture or level the scene does
+ * not hold gives RMN_ERR_INVALID_ARGUMENT. */
+rmn_status rmn_scene_texture_get(const rmn_scene* scene, int32_t texture, int32_t level, rmn_image_desc* info,
+                                 uint8_t* out, size_t capacity);
 
 /* The file tag of export k ("DiffuseColor", ..., "Filter_DepthFieldBlur_Bloom_FXAA") and its shade
  * options; NULL / -1 out of range. */

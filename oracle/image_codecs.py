@@ -1,7 +1,12 @@
-"""Oracle for the DDS block decoder: a numpy restatement of the S3TC block
-formats that scripts/dds_to_array.py's reader (imageio, absent here; the
-reference pins no version) decodes. TEST INFRASTRUCTURE ONLY: imported by
-tests/ as the checker of rmn_image_load, never by the library.
+"""Oracle for the texture front-end. TEST INFRASTRUCTURE ONLY: imported by
+tests/ as the checker of rmn_image_load and of the device mip chains, never
+by the library.
+
+``mip_chain`` restates ImageData::generateMipmaps (src/material.cpp:107-129)
+with its wrapped coordinates and truncating division.
+
+``bc_decode`` restates the S3TC block formats that scripts/dds_to_array.py's
+reader (imageio, absent here; the reference pins no version) decodes.
 
 Formats (DirectX "Block compression" documentation, BC1-BC3):
 * colour block: two RGB565 endpoints, bit-replicated to 8 bits, and 16
@@ -67,3 +72,25 @@ def bc_decode(payload: bytes, width: int, height: int, kind: int) -> np.ndarray:
         tex[:, :, 3] = np.take_along_axis(pal, sel, 1)
     img = tex.reshape(bh, bw, 4, 4, 4).transpose(0, 2, 1, 3, 4).reshape(bh * 4, bw * 4, 4)
     return img[:height, :width].astype(np.uint8)
+
+
+def mip_chain(tex: np.ndarray, max_levels: int = 8) -> list:
+    """ImageData::generateMipmaps: level l is (h >> l, w >> l) texels, each
+    channel the truncated mean of the 2 x 2 box of level l-1 at
+    ((2y + dy) mod ph, (2x + dx) mod pw); it stops before a side would be 0,
+    after at most 8 levels."""
+    levels = [np.asarray(tex, np.uint8)]
+    h, w = levels[0].shape[:2]
+    for level in range(1, max_levels):
+        cw, chh = w >> level, h >> level
+        if cw == 0 or chh == 0:
+            break
+        prev = levels[-1].astype(np.int64)
+        ph, pw = prev.shape[:2]
+        ys, xs = np.arange(chh), np.arange(cw)
+        s = 0
+        for dy in range(2):
+            for dx in range(2):
+                s = s + prev[((2 * ys + dy) % ph)[:, None], ((2 * xs + dx) % pw)[None, :]]
+        levels.append((s // 4).astype(np.uint8))
+    return levels

@@ -121,6 +121,17 @@ class Model:
         _check(_lib.load().rmn_scene_info_get(self._h, C.byref(s)), "rmn_scene_info_get")
         return {k: getattr(s, k) for k, _ in s._fields_}
 
+    def texture(self, index: int, level: int = 0) -> np.ndarray:
+        """Mip level `level` of scene texture `index` as the device holds it
+        (ImageData::data[level]): (h, w, 4) uint8 (rmn_scene_texture_get)."""
+        lib = _lib.load()
+        info = _lib.ImageDesc()
+        _check(lib.rmn_scene_texture_get(self._h, index, level, C.byref(info), None, 0), "rmn_scene_texture_get")
+        out = np.empty((info.height, info.width, 4), np.uint8)
+        _check(lib.rmn_scene_texture_get(self._h, index, level, C.byref(info), out.ctypes.data, out.nbytes),
+               "rmn_scene_texture_get")
+        return out
+
     def rayHit(self, rays, hits=None, stream=None):
         """Model::rayHit over a batch. rays: (n, 8) float32 (origin, t_min,
         dir, t_max). Returns hits (n, 4): face id (int32 bits), t, alpha, beta."""

@@ -277,6 +277,27 @@ rmn_status rmn_scene_info_get(const rmn_scene* scene, rmn_scene_info* info) {
   return RMN_OK;
 }
 
+rmn_status rmn_scene_texture_get(const rmn_scene* scene, int32_t texture, int32_t level, rmn_image_desc* info,
+                                 uint8_t* out, size_t capacity) {
+  clear_error();
+  if (!scene || !info) return fail(RMN_ERR_INVALID_ARGUMENT, "scene or info is NULL");
+  if (texture < 0 || texture >= (int32_t)scene->textures.size())
+    return fail(RMN_ERR_INVALID_ARGUMENT, "texture %d: the scene holds %zu textures", texture, scene->textures.size());
+  const DevTex& t = scene->textures[texture];
+  if (level < 0 || level >= t.depth)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "level %d: texture %d has %d levels", level, texture, t.depth);
+  info->width = t.w >> level;
+  info->height = t.h >> level;
+  info->channels = 4;
+  info->bytes_per_channel = 1;
+  if (!out) return RMN_OK;
+  const size_t n = (size_t)info->width * info->height * 4;
+  if (capacity < n) return fail(RMN_ERR_INVALID_ARGUMENT, "%zu bytes needed, %zu given", n, capacity);
+  cudaError_t e = cudaMemcpy(out, scene->dev.texels + t.off[level], n, cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy (rmn_scene_texture_get)");
+  return RMN_OK;
+}
+
 static rmn_status trace_common(rmn_scene* scene, const rmn_ray* rays, int64_t n, void* out, size_t out_bytes,
                                bool shadow, void* stream) {
   clear_error();

@@ -13,6 +13,7 @@ struct rmn_scene {
   rmn_scene_info info{};
   int device = 0;
   void* sky_share = nullptr;  // the sky's device tables, shared by every scene with the same sky map
+  std::vector<DevTex> textures;  // host copy of dev.texs (sizes, depths, level offsets)
 };
 
 namespace rmn {
@@ -52,6 +53,11 @@ struct RenderProfileData {
   unsigned long long closest, shadow, inner, leaves, tris, slots, pixels;
 };
 struct BatchState;
+
+// The mip chains of ImageData::generateMipmaps (mips.cu): level 0 of every
+// texture already in `texels` at tex[t].off[0]; levels 1.. are written at
+// their offsets. Synchronises `stream`.
+cudaError_t launch_build_mips(uint8_t* texels, const DevTex* tex, int ntex, cudaStream_t stream);
 
 // Photo::save as an 8-bit RGB PNG (png.cpp); rgb in host memory.
 rmn_status write_png(const float* rgb, int w, int h, const char* path);

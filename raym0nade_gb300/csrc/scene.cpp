@@ -249,45 +249,32 @@ rmn_status acquire_sky(rmn_scene* s, int W, int H, const std::vector<float4>& sk
   return RMN_OK;
 }
 
-// ImageData after Material::loadImageFromFile: level 0 as loaded and the mip
-// chain of ImageData::generateMipmaps (src/material.cpp:107-129): level l
-// halves the previous one with 2x2 integer box averages (texel coordinates
-// wrapped, sum / 4 truncated) until a side would reach 0, at most 8 levels.
-struct HostTex {
-  int w = 0, h = 0, depth = 0;
-  std::vector<uint8_t> lv[RMN_MIP_LEVELS];
-};
-void build_mips(const rmn_texture& in, HostTex& t) {
-  const int ch = 4;
+// ImageData after Material::loadImageFromFile and generateMipmaps
+// (src/material.cpp:107-129): level l is (w >> l) x (h >> l) texels, until a
+// side would reach 0, at most 8 levels; the levels of every texture are
+// packed one after the other. Level 0 is the caller's array; the device
+// builds the rest (mips.cu).
+DevTex texture_layout(const rmn_texture& in, long long& bytes) {
+  DevTex t{};
   t.w = in.width;
   t.h = in.height;
-  t.lv[0].assign(in.texels, in.texels + (size_t)in.width * in.height * ch);
   t.depth = RMN_MIP_LEVELS;
-  for (int level = 1; level < RMN_MIP_LEVELS; ++level) {
-    const int pw = t.w >> (level - 1), ph = t.h >> (level - 1), cw = t.w >> level, chh = t.h >> level;
-    if (cw == 0 || chh == 0) {
-      t.depth = level;
+  for (int l = 0; l < RMN_MIP_LEVELS; ++l) {
+    if (l > 0 && ((t.w >> l) == 0 || (t.h >> l) == 0)) {
+      t.depth = l;
       break;
     }
-    std::vector<uint8_t>& out = t.lv[level];
-    const std::vector<uint8_t>& prev = t.lv[level - 1];
-    out.resize((size_t)cw * chh * ch);
-    for (int y = 0; y < chh; ++y)
-      for (int x = 0; x < cw; ++x)
-        for (int c = 0; c < ch; ++c) {
-          int sum = 0;
-          for (int dy = 0; dy < 2; ++dy)
-            for (int dx = 0; dx < 2; ++dx)
-              sum += prev[((size_t)((y * 2 + dy) % ph) * pw + (x * 2 + dx) % pw) * ch + c];
-          out[((size_t)y * cw + x) * ch + c] = (uint8_t)(sum / 4);
-        }
+    t.off[l] = bytes;
+    bytes += 4LL * (t.w >> l) * (t.h >> l);
   }
+  return t;
 }
 // ImageData::hasTransparentPart, src/material.cpp:102-107: some level-0
 // alpha below 255.
-bool has_transparent_part(const HostTex& t) {
-  for (size_t i = 3; i < t.lv[0].size(); i += 4)
-    if (t.lv[0][i] < 255) return true;
+bool has_transparent_part(const rmn_texture& t) {
+  const size_t n = (size_t)t.width * t.height * 4;
+  for (size_t i = 3; i < n; i += 4)
+    if (t.texels[i] < 255) return true;
   return false;
 }
 
@@ -333,6 +320,8 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
     const rmn_texture& t = d->textures[i];
     if (t.width <= 0 || t.height <= 0 || t.width > 32768 || t.height > 32768 || !t.texels)
       return fail(RMN_ERR_INVALID_ARGUMENT, "texture %d needs 1..32768 x 1..32768 texels", i);
+    if (is_device_pointer(t.texels))
+      return fail(RMN_ERR_INVALID_ARGUMENT, "texture %d: texels must be in host memory", i);
     if (t.channels != 4)
       return fail(RMN_ERR_UNSUPPORTED,
                   "texture %d has %d channels: textures are RGBA8 (the reference reads 4-byte texels)", i,
@@ -398,26 +387,14 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   }
 
   // ---- textures: mip chains, packed level after level ----
-  std::vector<HostTex> htex(textured ? d->num_textures : 0);
-  std::vector<DevTex> dtex(htex.size());
-  std::vector<uint8_t> texels;
-  for (size_t i = 0; i < htex.size(); ++i) {
-    build_mips(d->textures[i], htex[i]);
-    DevTex& t = dtex[i];
-    t = DevTex{};
-    t.w = htex[i].w;
-    t.h = htex[i].h;
-    t.depth = htex[i].depth;
-    for (int l = 0; l < t.depth; ++l) {
-      t.off[l] = (long long)texels.size();
-      texels.insert(texels.end(), htex[i].lv[l].begin(), htex[i].lv[l].end());
-    }
-  }
+  std::vector<DevTex> dtex(textured ? d->num_textures : 0);
+  long long texel_bytes = 0;
+  for (size_t i = 0; i < dtex.size(); ++i) dtex[i] = texture_layout(d->textures[i], texel_bytes);
   std::vector<char> alpha_mat(d->num_materials, 0);
   bool has_alpha = false;
   for (int m = 0; m < d->num_materials; ++m) {
     const int t = mat_tex(m, RMN_TEX_DIFFUSE);
-    alpha_mat[m] = (textured && t >= 0 && has_transparent_part(htex[t])) ? 1 : 0;
+    alpha_mat[m] = (textured && t >= 0 && has_transparent_part(d->textures[t])) ? 1 : 0;
     has_alpha = has_alpha || alpha_mat[m];
   }
   if (has_alpha)
@@ -445,7 +422,11 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   // gamma 2.2, or the constant texel.
   auto emissive_at = [&](int m, float u, float v) -> float3 {
     const int t = textured ? mat_tex(m, RMN_TEX_EMISSIVE) : -1;
-    if (t >= 0) return tex_gamma(tex_get<4>(dtex[t], texels.data(), u, v, 0.0f));
+    if (t >= 0) {  // level 0 only (level of detail 0): read from the caller's texels
+      DevTex level0 = dtex[t];
+      level0.off[0] = 0;
+      return tex_gamma(tex_get<4>(level0, d->textures[t].texels, u, v, 0.0f));
+    }
     const rmn_material& q = d->materials[m];
     return q.has_emission != 0.0f ? f3(q.emission[0], q.emission[1], q.emission[2]) : f3(0.0f);
   };
@@ -587,7 +568,24 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   if (!sky.empty() && (st = acquire_sky(s, d->env_width, d->env_height, sky, sky_prefix)) != RMN_OK) return st;
   if ((st = upload(s, uvs, &g.uv)) != RMN_OK) return st;
   if ((st = upload(s, dtex, &g.texs)) != RMN_OK) return st;
-  if ((st = upload(s, texels, &g.texels)) != RMN_OK) return st;
+  s->textures = dtex;
+  g.texels = nullptr;
+  if (texel_bytes > 0) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, (size_t)texel_bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "cudaMalloc (textures)");
+    s->device_allocations.push_back(p);
+    uint8_t* tx = static_cast<uint8_t*>(p);
+    for (size_t i = 0; i < dtex.size(); ++i) {
+      const rmn_texture& t = d->textures[i];
+      e = cudaMemcpy(tx + dtex[i].off[0], t.texels, (size_t)t.width * t.height * 4, cudaMemcpyHostToDevice);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy (textures)");
+    }
+    e = launch_build_mips(tx, dtex.data(), (int)dtex.size(), nullptr);
+    if (e != cudaSuccess) return cuda_fail(e, "mip chains");
+    s->info.device_bytes += texel_bytes;
+    g.texels = tx;
+  }
   g.root = root;
   g.num_tris = nt;
   g.num_mats = d->num_materials;

@@ -149,3 +149,24 @@ def test_adjoint_rejects_textured_scenes():
     with pytest.raises(api.RmnError) as e:
         api.adjoint(room, args, photo, torch.ones(16 * 16, 3, device="cuda"))
     assert e.value.status == 4
+
+
+def test_mip_chains_match_oracle():
+    """The device-built chains (rmn_scene_texture_get) level for level
+    against ImageData::generateMipmaps restated in numpy, for the room's
+    textures and for odd, thin and long sizes (depths 1 to 8)."""
+    from oracle.image_codecs import mip_chain
+    room = scenes.textured_room()
+    rng = np.random.default_rng(12)
+    extra = [rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+             for h, w in [(21, 37), (1, 64), (3, 300), (16, 2048), (255, 257), (1, 1), (600, 5)]]
+    room.textures = list(room.textures) + extra
+    m = api.Model(room)
+    for i, tex in enumerate(room.textures):
+        want = mip_chain(tex)
+        for level, w in enumerate(want):
+            assert np.array_equal(m.texture(i, level), w), (i, level)
+        with pytest.raises(api.RmnError):
+            m.texture(i, len(want))
+    with pytest.raises(api.RmnError):
+        m.texture(len(room.textures), 0)

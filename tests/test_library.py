@@ -121,6 +121,8 @@ def test_argument_checks_need_no_gpu(lib):
     assert lib.rmn_filter(C.byref(img), 2, 2, None) == 1
     cnt = C.c_int32(-1)
     assert lib.rmn_export_set(C.byref(img), C.byref(pa), rgb, C.byref(cnt), None) == 1
+    info = _lib.ImageDesc()
+    assert lib.rmn_scene_texture_get(None, 0, 0, C.byref(info), None, 0) == 1
     # a negative or non-finite CoC, a zero size
     for bad in (_lib.PostArgs(2, 2, 1.0, 1.0, -1.0, (C.c_float * 3)()),
                 _lib.PostArgs(2, 2, 1.0, 1.0, float("inf"), (C.c_float * 3)()),
