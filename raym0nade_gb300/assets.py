@@ -197,7 +197,7 @@ def parse_mtl(path: str) -> list:
             line = raw.strip()
             if not line or line.startswith("#"):
                 continue
-            key, _, rest = line.partition(" ")
+            key, rest = (line.split(None, 1) + [""])[:2]
             k = key.lower()
             rest = rest.strip()
             if k == "newmtl":
@@ -249,18 +249,21 @@ def load_obj(path: str):
         return i - 1 if i > 0 else n + i
 
     with open(path, "r", errors="replace") as f:
-        for raw in f:
+        lines = f.read().replace("\\\n", " ").splitlines()  # a trailing backslash continues the line
+    for lineno, raw in enumerate(lines, 1):
+        try:
             line = raw.strip()
             if not line or line[0] == "#":
                 continue
-            key, _, rest = line.partition(" ")
-            if key == "v":
-                v.append([float(x) for x in rest.split()[:3]])
+            key, rest = (line.split(None, 1) + [""])[:2]
+            if key in ("v", "vn"):
+                xyz = [float(x) for x in rest.split()[:3]]
+                if len(xyz) != 3:
+                    raise ValueError("three coordinates expected")
+                (v if key == "v" else vn).append(xyz)
             elif key == "vt":
                 t = rest.split()
                 vt.append([float(t[0]), float(t[1]) if len(t) > 1 else 0.0])
-            elif key == "vn":
-                vn.append([float(x) for x in rest.split()[:3]])
             elif key == "f":
                 corners = []
                 for tok in rest.split():
@@ -283,6 +286,8 @@ def load_obj(path: str):
                 close()
             elif key == "mtllib":
                 mtllibs.extend(rest.split())
+        except (ValueError, IndexError) as e:
+            raise ValueError(f"{path}:{lineno}: cannot read {raw.strip()[:60]!r} ({e})") from None
     close()
     P = np.asarray(v, np.float32).reshape(-1, 3)
     T = np.asarray(vt, np.float32).reshape(-1, 2)
@@ -292,6 +297,8 @@ def load_obj(path: str):
         c = np.asarray(corners, np.int64)
         if (c[:, 0] < 0).any() or (c[:, 0] >= len(P)).any():
             raise ValueError(f"{path}: a face refers to a vertex that does not exist")
+        if (c[:, 1] >= len(T)).any() or (c[:, 2] >= len(N)).any() or (c[:, 1] < -1).any() or (c[:, 2] < -1).any():
+            raise ValueError(f"{path}: a face refers to a texture coordinate or normal that does not exist")
         pos = P[c[:, 0]]
         nrm = None if (c[:, 2] < 0).any() else N[c[:, 2]]
         uv = None if (c[:, 1] < 0).any() else T[c[:, 1]]

@@ -352,6 +352,17 @@ def test_load_model_without_mtl_or_normals(tmp_path):
     write(tmp_path, "e.obj", b"v 0 0 0\nl 1 1\n")
     with pytest.raises(ValueError):
         assets.load_model(str(tmp_path) + "/", "e.obj")
+    # tabs, a continued line, and the errors a broken file gives (with its line)
+    write(tmp_path, "t.obj", b"v\t0 0 0\nv 1 0 0\nv 0 1 \\\n 0\nf\t1 2 3\n")
+    sc = assets.load_model(str(tmp_path) + "/", "t.obj")
+    assert sc.num_triangles == 1 and np.allclose(sc.positions[2], [0, 1, 0])
+    for bad, where in [(b"v 0 0\n", ":1:"), (b"v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 x\n", ":4:")]:
+        write(tmp_path, "b.obj", bad)
+        with pytest.raises(ValueError, match=where):
+            assets.load_model(str(tmp_path) + "/", "b.obj")
+    write(tmp_path, "c.obj", b"v 0 0 0\nv 1 0 0\nv 0 1 0\nvn 0 0 1\nf 1//1 2//2 3//1\n")
+    with pytest.raises(ValueError, match="does not exist"):
+        assets.load_model(str(tmp_path) + "/", "c.obj")
 
 
 def test_imported_model_oracle_matches_reference(port, ref_tex, tmp_path):

@@ -78,6 +78,47 @@ def test_ctypes_layouts_match_c_compiler(tmp_path):
         assert got == int(val), (py, name, got, val)
 
 
+def test_c_program_links_and_decodes(lib, tmp_path):
+    """A plain C program against include/rmn.h and librmn.so: it decodes a
+    committed PNG with rmn_image_load (host work, no GPU) and reports the
+    library's error text for a missing file."""
+    import shutil
+    import subprocess
+    from raym0nade_gb300 import _lib
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "use.c"
+    src.write_text(r"""
+#include <stdio.h>
+#include <stdlib.h>
+#include "rmn.h"
+int main(int argc, char **argv) {
+  rmn_image_desc d;
+  if (rmn_image_load(argv[1], RMN_IMAGE_PNG, &d, NULL, 0) != RMN_OK) return 1;
+  size_t n = (size_t)d.width * d.height * d.channels;
+  unsigned char *px = malloc(n);
+  if (rmn_image_load(argv[1], RMN_IMAGE_PNG, &d, px, n) != RMN_OK) return 2;
+  unsigned long sum = 0;
+  for (size_t i = 0; i < n; i++) sum += px[i];
+  printf("%d %d %d %lu\n", d.width, d.height, d.channels, sum);
+  if (rmn_image_load("/nonexistent.png", RMN_IMAGE_PNG, &d, NULL, 0) != RMN_ERR_INVALID_ARGUMENT) return 3;
+  printf("%s\n", rmn_last_error());
+  free(px);
+  return 0;
+}
+""")
+    exe = tmp_path / "use"
+    libdir = os.path.dirname(_lib.LIB_PATH)
+    subprocess.run([cc, "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe), "-L", libdir, "-lrmn",
+                    "-Wl,-rpath," + libdir], check=True)
+    png = os.path.join(ROOT, "tests", "golden", "images", "rgb16_paeth.png")
+    out = subprocess.run([str(exe), png], check=True, capture_output=True, text=True).stdout.split("\n")
+    want = np.load(os.path.join(ROOT, "tests", "golden", "images.npz"))["rgb16_paeth.png"]
+    assert out[0].split() == [str(want.shape[1]), str(want.shape[0]), "3", str(int(want.astype(np.int64).sum()))]
+    assert "could not read" in out[1]
+
+
 def test_parse_render_args_docs_block():
     from raym0nade_gb300.api import parse_render_args
     block = """0.96718 -0.2 -0.156768
