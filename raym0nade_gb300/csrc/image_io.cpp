@@ -480,11 +480,12 @@ rmn_status decode_png(const std::vector<uint8_t>& f, bool header_only, Decoded& 
 
 rmn_status decode_hdr(const std::vector<uint8_t>& f, bool header_only, Decoded& img) {
   size_t at = 0;
-  auto line = [&](std::string& s) {
+  auto line = [&](std::string& s) {  // one header line, without its "\n" (or "\r\n")
     s.clear();
     while (at < f.size() && f[at] != '\n') s.push_back((char)f[at++]);
     if (at >= f.size()) return false;
     ++at;
+    if (!s.empty() && s.back() == '\r') s.pop_back();
     return true;
   };
   std::string s;

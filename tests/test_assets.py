@@ -153,6 +153,8 @@ def test_hdr_flat_and_run_length(tmp_path, h, w):
 def test_hdr_rejects_and_unsupported(tmp_path):
     rgbe = F.float_to_rgbe(np.ones((4, 16, 3), np.float32))
     assert status_of(write(tmp_path, "ok.hdr", F.encode_hdr(rgbe)), assets.HDR) == 0
+    crlf = F.encode_hdr(rgbe, header=b"#?RADIANCE\r\nFORMAT=32-bit_rle_rgbe\r\n\r\n").replace(b"+X 16\n", b"+X 16\r\n")
+    assert status_of(write(tmp_path, "crlf.hdr", crlf), assets.HDR) == 0
     xyze = F.encode_hdr(rgbe, header=b"#?RADIANCE\nFORMAT=32-bit_rle_xyze\n\n")
     assert status_of(write(tmp_path, "xyze.hdr", xyze), assets.HDR) == 4
     rot = F.encode_hdr(rgbe).replace(b"-Y 4 +X 16", b"+Y 4 +X 16")
