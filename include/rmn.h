@@ -411,6 +411,25 @@ rmn_status rmn_image_load(const char* path, int32_t kind, rmn_image_desc* info, 
 rmn_status rmn_scene_texture_get(const rmn_scene* scene, int32_t texture, int32_t level, rmn_image_desc* info,
                                  uint8_t* out, size_t capacity);
 
+/* A model read from disk as Model::Model(model_folder, model_name,
+ * skyMap_name) reads it (src/model.cpp:124-215): a Wavefront OBJ file
+ * (model_folder + model_name) with its MTL libraries, the textures they name
+ * decoded (PNG / DDS, RGB expanded to RGBA) and the sky map
+ * (model_folder + skyMap_name, Radiance HDR; "null" or NULL: none). Meshes,
+ * materials and texture slots follow assimp's OBJ import and
+ * Material::loadMaterialProperties: name, opacity and textures only.
+ * rmn_model_desc lays it out for rmn_scene_create; the arrays stay owned by
+ * the model until rmn_model_free. A file that cannot be read or parsed gives
+ * RMN_ERR_INVALID_ARGUMENT (the message names file and line); a texture of
+ * another type, a DDS that does not decode or a sky map that does not decode
+ * is left out with a message on stderr, as the reference goes on without it. */
+typedef struct rmn_model rmn_model;
+rmn_status rmn_model_read(const char* model_folder, const char* model_name, const char* skyMap_name,
+                          rmn_model** out);
+rmn_status rmn_model_desc(const rmn_model* model, rmn_scene_desc* desc);
+const char* rmn_model_material_name(const rmn_model* model, int32_t material);  /* NULL out of range */
+rmn_status rmn_model_free(rmn_model* model);
+
 /* The file tag of export k ("DiffuseColor", ..., "Filter_DepthFieldBlur_Bloom_FXAA") and its shade
  * options; NULL / -1 out of range. */
 const char* rmn_export_tag(int32_t k);

@@ -119,6 +119,10 @@ SIGNATURES = {
     "rmn_save_png": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_char_p]),
     "rmn_export_options": (C.c_int32, [C.c_int32]),
     "rmn_image_load": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(ImageDesc), C.c_void_p, C.c_size_t]),
+    "rmn_model_read": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "rmn_model_desc": (C.c_int, [C.c_void_p, C.POINTER(SceneDesc)]),
+    "rmn_model_material_name": (C.c_char_p, [C.c_void_p, C.c_int32]),
+    "rmn_model_free": (C.c_int, [C.c_void_p]),
     "rmn_scene_texture_get": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.POINTER(ImageDesc), C.c_void_p,
                                         C.c_size_t]),
 }

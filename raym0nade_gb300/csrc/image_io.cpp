@@ -345,10 +345,7 @@ void unfilter_row(int ft, const uint8_t* src, const uint8_t* up, uint8_t* out, s
   }
 }
 
-struct Decoded {
-  int w = 0, h = 0, channels = 0, bytes_per_channel = 1;
-  std::vector<uint8_t> bytes;  // uint8 samples or float32, row 0 = top
-};
+using Decoded = rmn::DecodedImage;
 
 rmn_status decode_png(const std::vector<uint8_t>& f, bool header_only, Decoded& img) {
   static const uint8_t kSig[8] = {137, 80, 78, 71, 13, 10, 26, 10};
@@ -695,19 +692,27 @@ bool read_file(const char* path, std::vector<uint8_t>& out) {
 
 }  // namespace
 
-extern "C" rmn_status rmn_image_load(const char* path, int32_t kind, rmn_image_desc* info, void* data,
-                                     size_t capacity) {
-  rmn::clear_error();
-  if (!path || !info) return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_image_load needs a path and an info record");
+namespace rmn {
+
+rmn_status decode_image_file(const char* path, int kind, bool header_only, DecodedImage& img) {
   if (kind != RMN_IMAGE_PNG && kind != RMN_IMAGE_DDS && kind != RMN_IMAGE_HDR)
     return fail(RMN_ERR_INVALID_ARGUMENT, "unknown image kind %d", kind);
   std::vector<uint8_t> file;
   if (!read_file(path, file)) return fail(RMN_ERR_INVALID_ARGUMENT, "could not read %s", path);
+  return kind == RMN_IMAGE_PNG   ? decode_png(file, header_only, img)
+         : kind == RMN_IMAGE_DDS ? decode_dds(file, header_only, img)
+                                 : decode_hdr(file, header_only, img);
+}
+
+}  // namespace rmn
+
+extern "C" rmn_status rmn_image_load(const char* path, int32_t kind, rmn_image_desc* info, void* data,
+                                     size_t capacity) {
+  rmn::clear_error();
+  if (!path || !info) return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_image_load needs a path and an info record");
   Decoded img;
   const bool header_only = data == nullptr;
-  rmn_status st = kind == RMN_IMAGE_PNG   ? decode_png(file, header_only, img)
-                  : kind == RMN_IMAGE_DDS ? decode_dds(file, header_only, img)
-                                          : decode_hdr(file, header_only, img);
+  rmn_status st = rmn::decode_image_file(path, kind, header_only, img);
   if (st != RMN_OK) return st;
   info->width = img.w;
   info->height = img.h;

@@ -61,6 +61,15 @@ cudaError_t launch_build_mips(uint8_t* texels, const DevTex* tex, int ntex, cuda
 
 // Photo::save as an 8-bit RGB PNG (png.cpp); rgb in host memory.
 rmn_status write_png(const float* rgb, int w, int h, const char* path);
+// A decoded image file (image_io.cpp): uint8 samples or float32 values,
+// row-major, row 0 = the image's top row.
+struct DecodedImage {
+  int w = 0, h = 0, channels = 0, bytes_per_channel = 1;
+  std::vector<uint8_t> bytes;
+};
+// Decode `path` as RMN_IMAGE_PNG / _DDS / _HDR (the size only with header_only).
+rmn_status decode_image_file(const char* path, int kind, bool header_only, DecodedImage& img);
+
 // CRC-32 of PNG chunks (ISO 3309 polynomial), shared by the writer and the reader.
 uint32_t png_crc32(uint32_t crc, const uint8_t* p, size_t n);
 

@@ -14,7 +14,7 @@ import zlib
 import numpy as np
 import pytest
 
-from oracle import image_codecs
+from oracle import image_codecs, obj_import
 from raym0nade_gb300 import _lib, assets, build, scenes
 from tests.golden import image_files as F
 from tests.golden import model_files
@@ -277,15 +277,15 @@ def test_load_texture_dispatch(tmp_path, capsys):
     write(tmp_path, "a.jpg", b"\xff\xd8")
     assert assets.load_texture(str(tmp_path / "a.jpg")) is None
     assert "Unsupported file format: " in capsys.readouterr().out
-    assert assets.url_decode("a%20b\\c%2f%41") == "a b\\c/A"
+    assert obj_import.url_decode("a%20b\\c%2f%41") == "a b\\c/A"
 
 
-def test_load_model_obj_room(tmp_path, capsys):
+def test_load_model_obj_room(tmp_path, capfd):
     folder = str(tmp_path) + "/"
     exp = model_files.write_room(folder)
     sc = assets.load_model(folder, "room.obj", "sky.hdr")
     sc.check()
-    assert "Unsupported file format: " in capsys.readouterr().out  # the .tga
+    assert "Unsupported file format: " in capfd.readouterr().err  # the .tga
     assert sc.material_names == exp["materials"]
     # one mesh per run of faces with the same object and material
     want_mats = [m for m, _ in exp["meshes"]]
@@ -341,7 +341,7 @@ def test_load_model_obj_room(tmp_path, capsys):
     assert assets.load_model(folder, "room.obj").env is None
     write(tmp_path, "bad.hdr", b"#?RADIANCE\n")
     assert assets.load_model(folder, "room.obj", "bad.hdr").env is None
-    assert "Conversion failed" in capsys.readouterr().out
+    assert "Conversion failed" in capfd.readouterr().err
 
 
 def test_load_model_without_mtl_or_normals(tmp_path):
@@ -382,3 +382,77 @@ def test_imported_model_oracle_matches_reference(port, ref_tex, tmp_path):
         assert np.array_equal(a[..., :38], b[..., :38], equal_nan=True)
         ids = set(np.unique(a[..., 36][~np.isnan(a[..., 36])]).astype(int))
         assert {1, 3, 4, 5} <= ids  # walls, glass, cut-out leaf, box in view
+
+
+def same_scene(a, b):
+    for k in ("positions", "normals", "uvs", "indices", "mesh_first", "mesh_material", "materials"):
+        x, y = getattr(a, k), getattr(b, k)
+        assert x.dtype == y.dtype and np.array_equal(x, y, equal_nan=True), k
+    assert a.material_names == b.material_names
+    assert (a.env is None) == (b.env is None) and (a.env is None or np.array_equal(a.env, b.env))
+    assert (a.textures is None) == (b.textures is None)
+    if a.textures is not None:
+        assert len(a.textures) == len(b.textures) and np.array_equal(a.mat_tex, b.mat_tex)
+        assert all(np.array_equal(x, y) for x, y in zip(a.textures, b.textures))
+
+
+def test_native_importer_matches_oracle(tmp_path, capfd):
+    """rmn_model_read against the oracle's restatement (oracle/obj_import.py,
+    with the oracle's own image readers): identical arrays."""
+    folder = str(tmp_path) + "/"
+    model_files.write_room(folder)
+    for sky in ("sky.hdr", "null"):
+        same_scene(assets.load_model(folder, "room.obj", sky), obj_import.load_model(folder, "room.obj", sky))
+
+
+def _random_obj(rng, path):
+    """Random OBJ text: objects, groups, material switches, polygons of 3-6
+    corners with every corner form and negative indices, degenerate faces,
+    normals pointing anywhere (the infacing test), comments, tabs, CRLF line
+    ends, continued lines, lines and points."""
+    out = ["mtllib lib.mtl", "# random model"]
+    nv = nt = nn = 0
+    mats = ["A", "B", "Glass", "Water", "Nope"]
+    for k in range(int(rng.integers(3, 8))):
+        out.append(("o" if rng.random() < 0.5 else "g") + f" part{k}")
+        for _ in range(int(rng.integers(4, 12))):
+            out.append("v %.7g %.7g %.7g" % tuple(rng.normal(0, 2, 3) * 10.0 ** int(rng.integers(-2, 3))))
+            nv += 1
+            out.append("vt\t%.5f %.5f" % tuple(rng.uniform(-1, 2, 2)))
+            nt += 1
+            if rng.random() < 0.8:
+                out.append("vn %.6f %.6f %.6f" % tuple(rng.normal(0, 1, 3)))
+                nn += 1
+        form = int(rng.integers(0, 4))
+        for f in range(int(rng.integers(2, 9))):
+            if rng.random() < 0.3:
+                out.append("usemtl " + mats[int(rng.integers(0, len(mats)))])
+            n = int(rng.integers(3, 7))
+            toks = []
+            for _ in range(n):
+                vi = int(rng.integers(1, nv + 1))
+                ti = int(rng.integers(1, nt + 1))
+                ni = int(rng.integers(1, nn + 1)) if nn else 0
+                if rng.random() < 0.3:
+                    vi, ti = vi - nv - 1, ti - nt - 1
+                toks.append([f"{vi}", f"{vi}/{ti}", f"{vi}//{ni}" if ni else f"{vi}/{ti}",
+                             f"{vi}/{ti}/{ni}" if ni else f"{vi}/{ti}"][form])
+            out.append("f " + " ".join(toks))
+            if rng.random() < 0.1:
+                out.append("l 1 2")
+            if rng.random() < 0.1:
+                out[-1] = out[-1] + " \\"
+                out.append("")
+    text = "\r\n".join(out) if rng.random() < 0.5 else "\n".join(out)
+    with open(path, "w", newline="") as f:
+        f.write(text + "\n")
+
+
+def test_native_importer_matches_oracle_random_models(tmp_path):
+    rng = np.random.default_rng(77)
+    folder = str(tmp_path) + "/"
+    with open(folder + "lib.mtl", "w") as f:
+        f.write("newmtl A\nd 1\nnewmtl B\nTr 0.5\nnewmtl Glass\n  d\t0.2\nnewmtl Water\nd 0.995\n")
+    for k in range(40):
+        _random_obj(rng, folder + f"m{k}.obj")
+        same_scene(assets.load_model(folder, f"m{k}.obj"), obj_import.load_model(folder, f"m{k}.obj"))
