@@ -421,6 +421,25 @@ def asset_decode_timings(repeats):
         best = min(best, time.perf_counter() - t0)
         del m
     out["scene_create_8_textures_2048sq"] = {"ms": best * 1e3, "texture_MB": 8 * 2048 * 2048 * 4 / 1e6}
+    # rmn_model_read of a Wavefront OBJ: a 256x256 heightfield (130,050
+    # triangles, v/vt/vn per corner), through assets.load_model
+    hf = scenes.heightfield(256, seed=3)
+    d = tempfile.mkdtemp()
+    with open(os.path.join(d, "hf.obj"), "w") as f:
+        for key, a in (("v", hf.positions), ("vn", hf.normals), ("vt", hf.uvs)):
+            np.savetxt(f, a, fmt=key + " %.6f" * a.shape[1])
+        i = hf.indices.astype(np.int64) + 1
+        np.savetxt(f, np.repeat(i, 3, axis=1), fmt="f %d/%d/%d %d/%d/%d %d/%d/%d")
+    size = os.path.getsize(os.path.join(d, "hf.obj"))
+    best = float("inf")
+    for _ in range(repeats):
+        t0 = time.perf_counter()
+        sc = assets.load_model(d + "/", "hf.obj")
+        best = min(best, time.perf_counter() - t0)
+    assert sc.num_triangles == hf.num_triangles
+    shutil.rmtree(d)
+    out["obj_import_heightfield_256"] = {"ms": best * 1e3, "file_MB": size / 1e6, "triangles": hf.num_triangles,
+                                         "MB_s": size / best / 1e6}
     return out
 
 

@@ -25,12 +25,14 @@
 // reference leaves ImageData::channels unset for PNG files).
 #include <array>
 #include <cerrno>
+#include <charconv>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <map>
 #include <string>
+#include <string_view>
 #include <vector>
 
 #include "rmn_host.h"
@@ -122,22 +124,38 @@ void key_rest(const std::string& line, std::string& key, std::string& rest) {
   rest = strip(line.substr(i));
 }
 
-// A decimal number (strtod, whole token; hexadecimal and "nan(...)" forms are
-// not numbers here), rounded to double first as a text reader does.
-bool parse_double(const std::string& t, double* v) {
-  if (t.empty() || t.find_first_of("xX(") != std::string::npos) return false;
-  char* end = nullptr;
-  *v = std::strtod(t.c_str(), &end);
-  return end == t.c_str() + t.size();
+using sv = std::string_view;
+
+// A sign '+' is allowed before a number, as a text reader allows it.
+sv drop_plus(sv t) {
+  if (t.size() > 1 && t[0] == '+' && t[1] != '+' && t[1] != '-') t.remove_prefix(1);
+  return t;
 }
 
-bool parse_long(const std::string& t, long long* v) {
-  if (t.empty()) return false;
-  errno = 0;
-  char* end = nullptr;
-  *v = std::strtoll(t.c_str(), &end, 10);
-  return end == t.c_str() + t.size() && errno == 0;
+// A decimal number, the whole token (std::from_chars: correctly rounded to
+// double; hexadecimal and "nan(...)" forms are not numbers here; a value
+// beyond double's range is +-inf or 0 as strtod gives it).
+bool sv_double(sv t, double* v) {
+  if (t.empty() || t.find_first_of("xX(") != sv::npos) return false;
+  t = drop_plus(t);
+  const auto r = std::from_chars(t.data(), t.data() + t.size(), *v);
+  if (r.ptr != t.data() + t.size()) return false;
+  if (r.ec == std::errc::result_out_of_range) {
+    const std::string z(t);
+    *v = std::strtod(z.c_str(), nullptr);
+    return true;
+  }
+  return r.ec == std::errc();
 }
+
+bool sv_long(sv t, long long* v) {
+  t = drop_plus(t);
+  if (t.empty()) return false;
+  const auto r = std::from_chars(t.data(), t.data() + t.size(), *v);
+  return r.ec == std::errc() && r.ptr == t.data() + t.size();
+}
+
+bool parse_double(const std::string& t, double* v) { return sv_double(sv(t), v); }
 
 std::string lower(std::string s) {
   for (char& c : s)
@@ -240,60 +258,115 @@ struct MeshRun {
   std::vector<int32_t> tris;  // 3 corner indices per triangle
 };
 
+// The OBJ parse works on views into the normalised text: no allocation per
+// line or token.
+
+bool sv_space(char c) { return is_space(c); }
+
+sv sv_strip(sv s) {
+  while (!s.empty() && sv_space(s.front())) s.remove_prefix(1);
+  while (!s.empty() && sv_space(s.back())) s.remove_suffix(1);
+  return s;
+}
+
+// The next whitespace-separated token of s (s advances past it); empty at the end.
+sv next_token(sv& s) {
+  while (!s.empty() && sv_space(s.front())) s.remove_prefix(1);
+  size_t j = 0;
+  while (j < s.size() && !sv_space(s[j])) ++j;
+  sv t = s.substr(0, j);
+  s.remove_prefix(j);
+  return t;
+}
+
+
 rmn_status parse_obj(const std::string& path, std::vector<float>& P, std::vector<float>& T, std::vector<float>& N,
                      std::vector<MeshRun>& meshes, std::vector<std::string>& mtllibs) {
-  std::string text;
-  if (!read_text(path, text)) return fail(RMN_ERR_INVALID_ARGUMENT, "could not read %s", path.c_str());
-  const std::vector<std::string> lines = split_lines(text, true);
+  std::string raw;
+  if (!read_text(path, raw)) return fail(RMN_ERR_INVALID_ARGUMENT, "could not read %s", path.c_str());
+  // the text with "\r\n" / "\r" as "\n" and continued lines joined
+  std::string t;
+  if (raw.find('\r') == std::string::npos && raw.find("\\\n") == std::string::npos) {
+    t.swap(raw);
+  } else {
+    t.reserve(raw.size());
+    for (size_t i = 0; i < raw.size(); ++i) {
+      char c = raw[i];
+      if (c == '\r') {
+        if (i + 1 < raw.size() && raw[i + 1] == '\n') continue;
+        c = '\n';
+      }
+      if (c == '\n' && !t.empty() && t.back() == '\\') {
+        t.back() = ' ';
+        continue;
+      }
+      t.push_back(c);
+    }
+    std::string().swap(raw);
+  }
   MeshRun cur{kDefaultMaterial, {}, {}};
   auto close = [&]() {
-    if (!cur.tris.empty()) meshes.push_back(cur);
+    if (!cur.tris.empty()) {
+      const std::string mat = cur.mat;
+      meshes.push_back(std::move(cur));
+      cur = MeshRun{mat, {}, {}};
+    }
     cur.corners.clear();
     cur.tris.clear();
   };
-  for (size_t ln = 0; ln < lines.size(); ++ln) {
-    const std::string line = strip(lines[ln]);
+  std::vector<Corner> cs;
+  size_t ln = 0, start = 0;
+  for (size_t i = 0; i <= t.size(); ++i) {
+    const char ch = i < t.size() ? t[i] : '\n';
+    if (!(ch == '\n' || ch == '\v' || ch == '\f' || ch == '\x1c' || ch == '\x1d' || ch == '\x1e')) continue;
+    if (i == t.size() && start >= t.size()) break;
+    ++ln;
+    const sv line = sv_strip(sv(t).substr(start, i - start));
+    start = i + 1;
     if (line.empty() || line[0] == '#') continue;
-    std::string key, rest;
-    key_rest(line, key, rest);
     auto bad = [&]() {
-      return fail(RMN_ERR_INVALID_ARGUMENT, "%s:%zu: cannot read '%.60s'", path.c_str(), ln + 1, line.c_str());
+      const std::string l(line.substr(0, 60));
+      return fail(RMN_ERR_INVALID_ARGUMENT, "%s:%zu: cannot read '%s'", path.c_str(), ln, l.c_str());
     };
+    sv rest = line;
+    const sv key = next_token(rest);
+    rest = sv_strip(rest);
     if (key == "v" || key == "vn") {
-      const std::vector<std::string> t = tokens(rest);
-      if (t.size() < 3) return bad();
       std::vector<float>& dst = key == "v" ? P : N;
       for (int k = 0; k < 3; ++k) {
         double d;
-        if (!parse_double(t[k], &d)) return bad();
+        if (!sv_double(next_token(rest), &d)) return bad();
         dst.push_back((float)d);
       }
     } else if (key == "vt") {
-      const std::vector<std::string> t = tokens(rest);
       double u, v = 0.0;
-      if (t.empty() || !parse_double(t[0], &u) || (t.size() > 1 && !parse_double(t[1], &v))) return bad();
+      if (!sv_double(next_token(rest), &u)) return bad();
+      const sv second = next_token(rest);
+      if (!second.empty() && !sv_double(second, &v)) return bad();
       T.push_back((float)u);
       T.push_back((float)v);
     } else if (key == "f") {
-      std::vector<Corner> cs;
-      for (const std::string& tok : tokens(rest)) {
-        std::vector<std::string> parts;
+      cs.clear();
+      for (sv tok = next_token(rest); !tok.empty(); tok = next_token(rest)) {
+        sv parts[3];
+        int np = 0;
         size_t a = 0;
         for (size_t b = 0; b <= tok.size(); ++b)
           if (b == tok.size() || tok[b] == '/') {
-            parts.emplace_back(tok, a, b - a);
+            if (np < 3) parts[np] = tok.substr(a, b - a);
+            ++np;
             a = b + 1;
           }
-        auto index = [](const std::string& s, size_t n, long long* out) {
+        auto index = [](sv s, size_t n, long long* out) {
           long long i;
-          if (!parse_long(s, &i)) return false;
+          if (!sv_long(s, &i)) return false;
           *out = i > 0 ? i - 1 : (long long)n + i;
           return true;
         };
         Corner c{0, -1, -1};
         if (!index(parts[0], P.size() / 3, &c.v)) return bad();
-        if (parts.size() > 1 && !parts[1].empty() && !index(parts[1], T.size() / 2, &c.t)) return bad();
-        if (parts.size() > 2 && !parts[2].empty() && !index(parts[2], N.size() / 3, &c.n)) return bad();
+        if (np > 1 && !parts[1].empty() && !index(parts[1], T.size() / 2, &c.t)) return bad();
+        if (np > 2 && !parts[2].empty() && !index(parts[2], N.size() / 3, &c.n)) return bad();
         cs.push_back(c);
       }
       if (cs.size() < 3) continue;
@@ -305,12 +378,12 @@ rmn_status parse_obj(const std::string& path, std::vector<float>& P, std::vector
         cur.tris.push_back(base + k + 1);
       }
     } else if (key == "usemtl") {
-      if (rest != cur.mat) close();
-      cur.mat = rest;
+      if (rest != sv(cur.mat)) close();
+      cur.mat = std::string(rest);
     } else if (key == "o" || key == "g") {
       close();
     } else if (key == "mtllib") {
-      for (const std::string& t : tokens(rest)) mtllibs.push_back(t);
+      for (sv m = next_token(rest); !m.empty(); m = next_token(rest)) mtllibs.emplace_back(m);
     }
   }
   close();
