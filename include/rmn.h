@@ -369,8 +369,9 @@ rmn_status rmn_export_set(const rmn_image* image, const rmn_post_args* args, flo
 /* Photo::save (src/image.cpp:481-532) without libpng: rgb (3 floats per
  * pixel, host or device memory) as an 8-bit RGB PNG at `path`, each byte
  * static_cast<uint8_t>(value * 255) as the reference writes it (values
- * outside [0, 1] clamp; the reference leaves them undefined). The image data
- * are stored uncompressed (deflate stored blocks). */
+ * outside [0, 1] clamp; the reference leaves them undefined). Rows are
+ * filtered adaptively and deflated (LZ77 + dynamic Huffman; stored blocks for
+ * incompressible data), as libpng writes by default. */
 rmn_status rmn_save_png(const float* rgb, int32_t width, int32_t height, const char* path);
 
 /* Image decoders of the asset front-end (host memory, no GPU involved). */

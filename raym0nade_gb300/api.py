@@ -442,8 +442,16 @@ def render_multiThread(model: Model, args: RenderArgs) -> Photo:
         if d:
             os.makedirs(d, exist_ok=True)
         photo.focus, photo.CoC, photo.cameraPosition = args.focus, args.CoC, tuple(args.position)
-        for tag, rgb in photo.export_set().items():
-            Photo.save(rgb, f"{args.savePath}({tag}).png")
+        exports = photo.export_set()
+        host = {tag: (rgb.cpu().numpy() if (torch is not None and isinstance(rgb, torch.Tensor)) else rgb)
+                for tag, rgb in exports.items()}
+        # the PNG files are independent: encode them on several host threads
+        # (the library call releases the interpreter lock)
+        from concurrent.futures import ThreadPoolExecutor
+        with ThreadPoolExecutor(max_workers=max(1, min(8, os.cpu_count() or 1))) as pool:
+            jobs = [pool.submit(Photo.save, rgb, f"{args.savePath}({tag}).png") for tag, rgb in host.items()]
+            for j in jobs:
+                j.result()
     return photo
 
 

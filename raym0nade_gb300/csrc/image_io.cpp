@@ -21,6 +21,7 @@
 // length against the bytes present and returns RMN_ERR_INVALID_ARGUMENT for
 // a malformed file and RMN_ERR_UNSUPPORTED for a valid variant it does not
 // decode.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -302,6 +303,222 @@ const char* zlib_decompress(const uint8_t* p, size_t n, std::vector<uint8_t>& ou
   }
   if (check != adler32(out.data(), out.size())) return "zlib checksum mismatch";
   return nullptr;
+}
+
+// ---------------------------------------------------------------- deflate
+
+struct BitWriter {
+  std::vector<uint8_t>& out;
+  uint64_t buf = 0;
+  int cnt = 0;
+  explicit BitWriter(std::vector<uint8_t>& o) : out(o) {}
+  void put(uint32_t bits, int n) {  // n <= 32, first bit in the least significant position
+    buf |= (uint64_t)bits << cnt;
+    cnt += n;
+    while (cnt >= 8) {
+      out.push_back((uint8_t)buf);
+      buf >>= 8;
+      cnt -= 8;
+    }
+  }
+  void flush() {
+    if (cnt > 0) out.push_back((uint8_t)buf);
+    buf = 0;
+    cnt = 0;
+  }
+};
+
+// Huffman code lengths for the frequencies, at most max_len bits: the
+// optimal tree (two lightest nodes merged first, ties to the lower index);
+// while it is too deep, the frequencies are halved (kept >= 1) and the tree
+// rebuilt. A single used symbol gets length 1.
+void huffman_lengths(const uint32_t* freq, int n, int max_len, uint8_t* len) {
+  std::vector<uint32_t> f(freq, freq + n);
+  for (;;) {
+    std::fill(len, len + n, 0);
+    std::vector<std::pair<uint64_t, int>> heap;  // (weight, node), a min-heap
+    std::vector<int> parent;
+    for (int i = 0; i < n; ++i)
+      if (f[i]) {
+        heap.push_back({((uint64_t)f[i] << 20) | (uint64_t)parent.size(), (int)parent.size()});
+        parent.push_back(-1);
+      }
+    if (parent.empty()) return;
+    if (parent.size() == 1) {
+      for (int i = 0; i < n; ++i)
+        if (f[i]) len[i] = 1;
+      return;
+    }
+    auto cmp = [](const std::pair<uint64_t, int>& a, const std::pair<uint64_t, int>& b) { return a.first > b.first; };
+    std::make_heap(heap.begin(), heap.end(), cmp);
+    while (heap.size() > 1) {
+      std::pop_heap(heap.begin(), heap.end(), cmp);
+      const auto a = heap.back();
+      heap.pop_back();
+      std::pop_heap(heap.begin(), heap.end(), cmp);
+      const auto b = heap.back();
+      heap.pop_back();
+      const int node = (int)parent.size();
+      parent.push_back(-1);
+      parent[a.second] = parent[b.second] = node;
+      const uint64_t w = ((a.first >> 20) + (b.first >> 20)) << 20 | (uint64_t)node;
+      heap.push_back({w, node});
+      std::push_heap(heap.begin(), heap.end(), cmp);
+    }
+    int leaf = 0, deepest = 0;
+    for (int i = 0; i < n; ++i) {
+      if (!f[i]) continue;
+      int d = 0;
+      for (int v = leaf; parent[v] >= 0; v = parent[v]) ++d;
+      len[i] = (uint8_t)std::min(d, 255);
+      deepest = std::max(deepest, d);
+      ++leaf;
+    }
+    if (deepest <= max_len) return;
+    for (int i = 0; i < n; ++i)
+      if (f[i]) f[i] = (f[i] + 1) >> 1;
+  }
+}
+
+// Canonical codes of the lengths (RFC 1951 section 3.2.2), bit-reversed for
+// writing first bit first.
+void canonical_codes(const uint8_t* len, int n, uint32_t* code) {
+  int count[16] = {0};
+  for (int i = 0; i < n; ++i) count[len[i]]++;
+  count[0] = 0;
+  uint32_t next[16] = {0};
+  uint32_t c = 0;
+  for (int l = 1; l < 16; ++l) {
+    c = (c + count[l - 1]) << 1;
+    next[l] = c;
+  }
+  for (int i = 0; i < n; ++i) {
+    if (!len[i]) continue;
+    uint32_t v = next[len[i]]++, r = 0;
+    for (int b = 0; b < len[i]; ++b) r |= ((v >> b) & 1u) << (len[i] - 1 - b);
+    code[i] = r;
+  }
+}
+
+struct Symbol {
+  uint16_t litlen;  // literal byte, or match length 3..258
+  uint16_t dist;    // 0: literal
+};
+
+// Length 3..258 -> symbol 257..285 and distance 1..32768 -> code 0..29,
+// from tables built once (distances above 256 by (d - 1) >> 7).
+struct CodeTables {
+  uint16_t len_sym[259];
+  uint8_t dist_lo[257], dist_hi[256];
+  CodeTables() {
+    for (int l = 3; l <= 258; ++l) {
+      int s = 28;
+      while (kLenBase[s] > l) --s;
+      len_sym[l] = (uint16_t)(257 + s);
+    }
+    auto slow = [](int d) {
+      int s = 29;
+      while (kDistBase[s] > d) --s;
+      return s;
+    };
+    for (int d = 1; d <= 256; ++d) dist_lo[d] = (uint8_t)slow(d);
+    for (int q = 2; q < 256; ++q) dist_hi[q] = (uint8_t)slow((q << 7) + 1);
+  }
+};
+const CodeTables& code_tables() {
+  static const CodeTables t;  // initialised once, thread-safe
+  return t;
+}
+int length_symbol(int len) { return code_tables().len_sym[len]; }
+int distance_symbol(int d) { return d <= 256 ? code_tables().dist_lo[d] : code_tables().dist_hi[(d - 1) >> 7]; }
+
+// One dynamic-Huffman block of symbols.
+void write_block(BitWriter& bw, const std::vector<Symbol>& sy, bool last) {
+  uint32_t lf[286] = {0}, df[30] = {0};
+  for (const Symbol& s : sy) {
+    if (!s.dist) {
+      lf[s.litlen]++;
+    } else {
+      lf[length_symbol(s.litlen)]++;
+      df[distance_symbol(s.dist)]++;
+    }
+  }
+  lf[256] = 1;
+  bool any_dist = false;
+  for (uint32_t x : df) any_dist = any_dist || x;
+  if (!any_dist) df[0] = 1;  // one distance code of one bit
+  uint8_t ll[286], dl[30];
+  huffman_lengths(lf, 286, 15, ll);
+  huffman_lengths(df, 30, 15, dl);
+  int hlit = 286, hdist = 30;
+  while (hlit > 257 && !ll[hlit - 1]) --hlit;
+  while (hdist > 1 && !dl[hdist - 1]) --hdist;
+  // the code lengths, run-length coded with 16 / 17 / 18
+  std::vector<uint8_t> lens(ll, ll + hlit);
+  lens.insert(lens.end(), dl, dl + hdist);
+  std::vector<std::pair<uint8_t, uint8_t>> rle;  // (symbol, extra value)
+  for (size_t i = 0; i < lens.size();) {
+    size_t j = i;
+    while (j < lens.size() && lens[j] == lens[i]) ++j;
+    size_t run = j - i;
+    if (lens[i] == 0) {
+      while (run >= 11) {
+        const size_t k = std::min<size_t>(run, 138);
+        rle.push_back({18, (uint8_t)(k - 11)});
+        run -= k;
+      }
+      if (run >= 3) {
+        rle.push_back({17, (uint8_t)(run - 3)});
+        run = 0;
+      }
+    } else {
+      rle.push_back({lens[i], 0});
+      --run;
+      while (run >= 3) {
+        const size_t k = std::min<size_t>(run, 6);
+        rle.push_back({16, (uint8_t)(k - 3)});
+        run -= k;
+      }
+    }
+    while (run--) rle.push_back({lens[i], 0});
+    i = j;
+  }
+  uint32_t cf[19] = {0};
+  for (const auto& r : rle) cf[r.first]++;
+  uint8_t cl[19];
+  huffman_lengths(cf, 19, 7, cl);
+  int hclen = 19;
+  while (hclen > 4 && !cl[kCodeLengthOrder[hclen - 1]]) --hclen;
+  uint32_t ccode[19] = {0}, lcode[286] = {0}, dcode[30] = {0};
+  canonical_codes(cl, 19, ccode);
+  canonical_codes(ll, 286, lcode);
+  canonical_codes(dl, 30, dcode);
+
+  bw.put(last ? 1 : 0, 1);
+  bw.put(2, 2);
+  bw.put((uint32_t)(hlit - 257), 5);
+  bw.put((uint32_t)(hdist - 1), 5);
+  bw.put((uint32_t)(hclen - 4), 4);
+  for (int i = 0; i < hclen; ++i) bw.put(cl[kCodeLengthOrder[i]], 3);
+  for (const auto& r : rle) {
+    bw.put(ccode[r.first], cl[r.first]);
+    if (r.first == 16) bw.put(r.second, 2);
+    if (r.first == 17) bw.put(r.second, 3);
+    if (r.first == 18) bw.put(r.second, 7);
+  }
+  for (const Symbol& s : sy) {
+    if (!s.dist) {
+      bw.put(lcode[s.litlen], ll[s.litlen]);
+      continue;
+    }
+    const int ls = length_symbol(s.litlen) - 257;
+    bw.put(lcode[257 + ls], ll[257 + ls]);
+    bw.put((uint32_t)(s.litlen - kLenBase[ls]), kLenExtra[ls]);
+    const int ds = distance_symbol(s.dist);
+    bw.put(dcode[ds], dl[ds]);
+    bw.put((uint32_t)(s.dist - kDistBase[ds]), kDistExtra[ds]);
+  }
+  bw.put(lcode[256], ll[256]);
 }
 
 // ---------------------------------------------------------------- PNG
@@ -693,6 +910,86 @@ bool read_file(const char* path, std::vector<uint8_t>& out) {
 }  // namespace
 
 namespace rmn {
+
+// zlib stream (RFC 1950) of `data`: greedy LZ77 over a 32 KiB window (hash
+// chains on 3-byte prefixes, at most kChain candidates per position, a match
+// of kNice bytes taken at once) and
+// dynamic-Huffman blocks of up to 2^16 symbols; stored blocks when that
+// would not be smaller.
+std::vector<uint8_t> zlib_compress(const uint8_t* data, size_t n) {
+  constexpr int kHashBits = 15, kWindow = 32768, kChain = 8, kNice = 64, kMaxMatch = 258;
+  std::vector<uint8_t> out = {0x78, 0x9C};
+  std::vector<int32_t> head(1 << kHashBits, -1), prev(kWindow, -1);
+  auto hash = [&](size_t i) {
+    const uint32_t v = (uint32_t)data[i] | (uint32_t)data[i + 1] << 8 | (uint32_t)data[i + 2] << 16;
+    return (v * 2654435761u) >> (32 - kHashBits);
+  };
+  auto insert = [&](size_t i) {
+    if (i + 2 >= n) return;
+    const uint32_t h = hash(i);
+    prev[i & (kWindow - 1)] = head[h];
+    head[h] = (int32_t)i;
+  };
+  BitWriter bw(out);
+  std::vector<Symbol> sy;
+  sy.reserve(1 << 16);
+  size_t i = 0;
+  while (i < n) {
+    int best = 0, best_d = 0;
+    if (i + 2 < n) {
+      const size_t limit = std::min<size_t>(kMaxMatch, n - i);
+      int32_t cand = head[hash(i)];
+      for (int c = 0; c < kChain && cand >= 0 && i - (size_t)cand <= (size_t)kWindow; ++c) {
+        const uint8_t* a = data + cand;
+        const uint8_t* b = data + i;
+        if (a[best] == b[best]) {
+          size_t l = 0;
+          while (l < limit && a[l] == b[l]) ++l;
+          if ((int)l > best) {
+            best = (int)l;
+            best_d = (int)(i - (size_t)cand);
+            if (l == limit || best >= kNice) break;  // long enough
+          }
+        }
+        const int32_t nx = prev[cand & (kWindow - 1)];
+        if (nx >= cand) break;  // the slot was reused by a newer position
+        cand = nx;
+      }
+    }
+    if (best >= 3) {
+      sy.push_back({(uint16_t)best, (uint16_t)best_d});
+      for (int k = 0; k < best; ++k) insert(i + k);
+      i += best;
+    } else {
+      sy.push_back({data[i], 0});
+      insert(i);
+      ++i;
+    }
+    if (sy.size() == (1u << 16) || i == n) {
+      write_block(bw, sy, i == n);
+      sy.clear();
+    }
+  }
+  if (n == 0) write_block(bw, sy, true);
+  bw.flush();
+  if (out.size() > n + n / 65535 * 5 + 16) {  // incompressible: stored blocks
+    out.assign({0x78, 0x01});
+    size_t pos = 0;
+    do {
+      const size_t k = std::min<size_t>(65535, n - pos);
+      out.push_back(pos + k == n ? 1 : 0);
+      out.push_back((uint8_t)(k & 0xff));
+      out.push_back((uint8_t)(k >> 8));
+      out.push_back((uint8_t)(~k & 0xff));
+      out.push_back((uint8_t)((~k >> 8) & 0xff));
+      out.insert(out.end(), data + pos, data + pos + k);
+      pos += k;
+    } while (pos < n);
+  }
+  const uint32_t a = adler32(data, n);
+  for (int k = 3; k >= 0; --k) out.push_back((uint8_t)(a >> (8 * k)));
+  return out;
+}
 
 rmn_status decode_image_file(const char* path, int kind, bool header_only, DecodedImage& img) {
   if (kind != RMN_IMAGE_PNG && kind != RMN_IMAGE_DDS && kind != RMN_IMAGE_HDR)

@@ -1,10 +1,12 @@
 // Photo::save (src/image.cpp:481-532) without libpng: an 8-bit RGB PNG whose
 // bytes are static_cast<png_byte>(value * 255) per channel, as the reference
-// writes them. The image data go into zlib "stored" deflate blocks (no
-// compression), which every PNG reader accepts; CRC-32 (chunks) and Adler-32
-// (zlib stream) are computed here.
+// writes them. Rows are filtered adaptively and the stream deflated
+// (zlib_compress, image_io.cpp) as libpng does by default; the decoded
+// pixels, not the file bytes, are what matches the reference's file.
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -61,37 +63,59 @@ uint32_t png_crc32(uint32_t crc, const uint8_t* p, size_t n) {
 }
 
 rmn_status write_png(const float* rgb, int w, int h, const char* path) {
-  // scanlines: filter byte 0, then RGB bytes
-  const size_t row = 1 + 3 * (size_t)w;
-  std::vector<uint8_t> raw(row * h);
+  // scanlines, each with the filter whose bytes have the smallest sum of
+  // magnitudes (bytes read as signed), as libpng's adaptive filtering picks
+  const size_t stride = 3 * (size_t)w;
+  std::vector<uint8_t> raw((stride + 1) * h), cur(stride), prev(stride, 0), best(stride), trial(stride);
+  auto magnitude = [](uint8_t v) -> uint32_t { return v < 128 ? v : 256u - v; };
   for (int y = 0; y < h; ++y) {
-    uint8_t* r = &raw[row * y];
-    r[0] = 0;
-    for (size_t k = 0; k < 3 * (size_t)w; ++k) r[1 + k] = to_byte(rgb[3 * (size_t)w * y + k]);
+    for (size_t k = 0; k < stride; ++k) cur[k] = to_byte(rgb[stride * y + k]);
+    uint64_t best_sum = UINT64_MAX;
+    int best_ft = 0;
+    for (int ft = 0; ft < 5; ++ft) {  // one loop per filter type (bpp = 3)
+      uint8_t* t = trial.data();
+      const uint8_t* x = cur.data();
+      const uint8_t* up = prev.data();
+      const size_t k = std::min<size_t>(3, stride);
+      switch (ft) {
+        case 0:
+          std::memcpy(t, x, stride);
+          break;
+        case 1:
+          std::memcpy(t, x, k);
+          for (size_t i = k; i < stride; ++i) t[i] = (uint8_t)(x[i] - x[i - 3]);
+          break;
+        case 2:
+          for (size_t i = 0; i < stride; ++i) t[i] = (uint8_t)(x[i] - up[i]);
+          break;
+        case 3:
+          for (size_t i = 0; i < k; ++i) t[i] = (uint8_t)(x[i] - (up[i] >> 1));
+          for (size_t i = k; i < stride; ++i) t[i] = (uint8_t)(x[i] - ((x[i - 3] + up[i]) >> 1));
+          break;
+        default:
+          for (size_t i = 0; i < k; ++i) t[i] = (uint8_t)(x[i] - up[i]);  // a = c = 0: Paeth picks b
+          for (size_t i = k; i < stride; ++i) {
+            const int a = x[i - 3], b = up[i], c = up[i - 3];
+            const int pa = std::abs(b - c), pb = std::abs(a - c), pc = std::abs(a + b - 2 * c);
+            const int bc = pc < pb ? c : b;
+            t[i] = (uint8_t)(x[i] - ((pc < pb ? pc : pb) < pa ? bc : a));
+          }
+          break;
+      }
+      uint64_t sum = 0;
+      for (size_t i = 0; i < stride; ++i) sum += magnitude(t[i]);
+      if (sum < best_sum) {
+        best_sum = sum;
+        best_ft = ft;
+        best.swap(trial);
+      }
+    }
+    uint8_t* r = &raw[(stride + 1) * y];
+    r[0] = (uint8_t)best_ft;
+    std::memcpy(r + 1, best.data(), stride);
+    prev.swap(cur);
   }
-  // zlib stream of stored blocks
-  std::vector<uint8_t> z;
-  z.reserve(raw.size() + raw.size() / 65535 * 5 + 16);
-  z.push_back(0x78);
-  z.push_back(0x01);
-  size_t pos = 0;
-  do {
-    const size_t n = std::min<size_t>(65535, raw.size() - pos);
-    const bool last = pos + n == raw.size();
-    z.push_back(last ? 1 : 0);
-    z.push_back((uint8_t)(n & 0xff));
-    z.push_back((uint8_t)(n >> 8));
-    z.push_back((uint8_t)(~n & 0xff));
-    z.push_back((uint8_t)((~n >> 8) & 0xff));
-    z.insert(z.end(), raw.begin() + pos, raw.begin() + pos + n);
-    pos += n;
-  } while (pos < raw.size());
-  uint32_t a = 1, b = 0;  // Adler-32
-  for (uint8_t c : raw) {
-    a = (a + c) % 65521;
-    b = (b + a) % 65521;
-  }
-  put32(z, (b << 16) | a);
+  const std::vector<uint8_t> z = zlib_compress(raw.data(), raw.size());
 
   std::vector<uint8_t> out = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};
   std::vector<uint8_t> ihdr;

@@ -70,6 +70,9 @@ struct DecodedImage {
 // Decode `path` as RMN_IMAGE_PNG / _DDS / _HDR (the size only with header_only).
 rmn_status decode_image_file(const char* path, int kind, bool header_only, DecodedImage& img);
 
+// A zlib stream of n bytes (image_io.cpp): LZ77 + dynamic Huffman blocks.
+std::vector<uint8_t> zlib_compress(const uint8_t* data, size_t n);
+
 // CRC-32 of PNG chunks (ISO 3309 polynomial), shared by the writer and the reader.
 uint32_t png_crc32(uint32_t crc, const uint8_t* p, size_t n);
 

@@ -456,3 +456,38 @@ def test_native_importer_matches_oracle_random_models(tmp_path):
     for k in range(40):
         _random_obj(rng, folder + f"m{k}.obj")
         same_scene(assets.load_model(folder, f"m{k}.obj"), obj_import.load_model(folder, f"m{k}.obj"))
+
+
+@pytest.mark.parametrize("kind", ["smooth", "noise", "tiles", "tiny", "flat"])
+def test_save_png_compresses_and_round_trips(tmp_path, kind):
+    """rmn_save_png's deflate stream: read back by Python's zlib (through
+    the oracle's reader) and by the library's own decoder, pixel for pixel;
+    smooth and repetitive images shrink, noise falls back to stored blocks."""
+    lib = _lib.load()
+    rng = np.random.default_rng(5)
+    h, w = {"tiny": (1, 2), "tiles": (300, 700)}.get(kind, (240, 320))
+    yy, xx = np.mgrid[0:h, 0:w].astype(np.float32)
+    if kind == "smooth":
+        img = np.stack([xx / w, yy / h, (xx + yy) / (w + h)], -1)
+    elif kind == "noise":
+        img = rng.random((h, w, 3), dtype=np.float32)
+    elif kind == "tiles":
+        tile = rng.random((20, 37, 3), dtype=np.float32)
+        img = np.tile(tile, (h // 20 + 1, w // 37 + 1, 1))[:h, :w]
+    elif kind == "flat":
+        img = np.full((h, w, 3), 0.25, np.float32)
+    else:
+        img = rng.random((h, w, 3), dtype=np.float32)
+    img = np.ascontiguousarray(img, np.float32)
+    p = str(tmp_path / f"{kind}.png")
+    assert lib.rmn_save_png(img.ctypes.data, w, h, p.encode()) == 0
+    want = np.clip(img * np.float32(255), 0, 255).astype(np.uint8)
+    assert np.array_equal(image_codecs.png_read(p), want)
+    assert np.array_equal(assets.load_png(p), want)
+    size, raw = os.path.getsize(p), h * (1 + 3 * w)
+    if kind in ("smooth", "flat"):
+        assert size < 0.1 * raw
+    if kind == "tiles":
+        assert size < 0.2 * raw
+    if kind == "noise":
+        assert size < raw * 1.01 + 200

@@ -248,7 +248,8 @@ def test_texture_scene_checks_need_no_gpu(lib):
 
 
 def _read_png(path):
-    """A minimal PNG reader (8-bit RGB, filter 0) that checks every CRC."""
+    """Check every chunk CRC and the header of an 8-bit RGB PNG, then decode
+    it with the oracle's reader (Python's zlib, all five filters)."""
     import struct
     import zlib
     data = open(path, "rb").read()
@@ -265,15 +266,15 @@ def _read_png(path):
     w, h, depth, ctype, comp, filt, inter = struct.unpack(">IIBBBBB", chunks[0][1])
     assert (depth, ctype, comp, filt, inter) == (8, 2, 0, 0, 0)
     raw = zlib.decompress(b"".join(b for t, b in chunks if t == b"IDAT"))
-    rows = np.frombuffer(raw, np.uint8).reshape(h, 1 + 3 * w)
-    assert (rows[:, 0] == 0).all()
-    return rows[:, 1:].reshape(h, w, 3)
+    assert len(raw) == h * (1 + 3 * w)
+    from oracle.image_codecs import png_read
+    return png_read(path)
 
 
 @pytest.mark.parametrize("w,h", [(1, 1), (37, 5), (300, 260)])
 def test_save_png_bytes_are_the_references(lib, tmp_path, w, h):
     """Photo::save's bytes, static_cast<png_byte>(v * 255), in a PNG any
-    reader decodes (the 300 x 260 image spans several stored blocks)."""
+    reader decodes (adaptive row filters, deflate by the library)."""
     from raym0nade_gb300 import api
     rng = np.random.default_rng(w * h)
     img = rng.random((h, w, 3), dtype=np.float32)
