@@ -154,6 +154,8 @@ class OracleLib:
             "gamma": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
             "fxaa": (None, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
             "photo": (None, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
+            "mip_chain": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
+            "url_decode": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int]),
         }
         for name, (res, args) in sig.items():
             f = getattr(self.lib, f"{prefix}_{name}", None)
@@ -168,6 +170,28 @@ class OracleLib:
 
     def scene(self, scene) -> OracleScene:
         return OracleScene(self, scene)
+
+    def mip_chain(self, tex: np.ndarray) -> list:
+        """ImageData::generateMipmaps of the reference (ref_tex only): the
+        levels of an (h, w, c) uint8 image."""
+        tex = np.ascontiguousarray(tex, np.uint8)
+        h, w, c = tex.shape
+        out = np.zeros(tex.nbytes * 2, np.uint8)
+        depth = self.fn("mip_chain")(_ptr(tex), w, h, c, _ptr(out), out.nbytes)
+        assert depth > 0
+        levels, at = [], 0
+        for lv in range(depth):
+            n = (h >> lv) * (w >> lv) * c
+            levels.append(out[at:at + n].reshape(h >> lv, w >> lv, c).copy())
+            at += n
+        return levels
+
+    def url_decode(self, s: str) -> str:
+        """urlDecode of the reference (ref_tex only)."""
+        buf = C.create_string_buffer(4 * len(s) + 8)
+        n = self.fn("url_decode")(s.encode("latin-1"), buf, len(buf))
+        assert n >= 0
+        return buf.raw[:n].decode("latin-1")
 
     def compose(self, recs: np.ndarray, exposure: float = 1.0, gamma: bool = True) -> np.ndarray:
         recs = np.ascontiguousarray(recs, np.float32)

@@ -432,6 +432,38 @@ void ref_photo(float* recs, int w, int h, int stages, int options, const float* 
   }
 }
 
+#ifdef ORC_REAL_MATERIAL
+// ImageData::generateMipmaps (src/material.cpp:107-129) on an 8-bit image:
+// the levels packed one after the other into out (capacity bytes). Returns
+// the number of levels, or -1 when out is too small.
+int ref_mip_chain(const uint8_t* texels, int w, int h, int channels, uint8_t* out, size_t capacity) {
+  ImageData img;
+  img.width = w;
+  img.height = h;
+  img.channels = channels;
+  img.data[0].assign(texels, texels + (size_t)w * h * channels);
+  img.generateMipmaps();
+  size_t at = 0;
+  for (int l = 0; l < img.map_depth; ++l) {
+    const size_t n = img.data[l].size();
+    if (at + n > capacity) return -1;
+    std::memcpy(out + at, img.data[l].data(), n);
+    at += n;
+  }
+  return img.map_depth;
+}
+
+// urlDecode (src/material.cpp:9-24) into out (NUL-terminated); returns the
+// decoded length or -1 when out is too small.
+int ref_url_decode(const char* in, char* out, int capacity) {
+  const std::string s = urlDecode(in);
+  if ((int)s.size() + 1 > capacity) return -1;
+  std::memcpy(out, s.data(), s.size());
+  out[s.size()] = 0;
+  return (int)s.size();
+}
+#endif
+
 void ref_fxaa(const float* in, float* out, int w, int h) {
   Photo ph(w, h);
   for (long i = 0; i < (long)w * h; ++i) ph.pixelarray[i] = vec3(in[3 * i], in[3 * i + 1], in[3 * i + 2]);

@@ -29,6 +29,8 @@ Fixtures (numpy .npz, compressed):
                      (``photo_records``): spatialClamp, filter, bloom, depth
                      of field, postProcessing with and without them (the
                      cases of PHOTO_CASES). ``--photo`` writes it alone.
+  mips.npz           ImageData::generateMipmaps of the reference on five
+                     textures of odd, thin and long sizes (``--mips``).
   images/, images.npz  small PNG, Radiance HDR and DDS files (every PNG
                      colour type family, Adam7, all filters, stored / fixed /
                      dynamic deflate; flat and run-length HDR scanlines;
@@ -223,6 +225,7 @@ def main():
     textured()
     photo(R)
     images()
+    mips()
 
     rgb_lin = R.compose(rec, 1.0, gamma=False)
     rgb = R.compose(rec, 1.0, gamma=True)
@@ -320,6 +323,25 @@ def images():
     np.savez_compressed(os.path.join(HERE, "images.npz"), **out)
 
 
+def mips():
+    """ImageData::generateMipmaps of the reference on textures of odd, thin
+    and long sizes -> tests/golden/mips.npz."""
+    bindings.build(with_reference=True)
+    T = bindings.OracleLib("ref_tex")
+    rng = np.random.default_rng(4242)
+    out = {}
+    sizes = [(21, 37), (3, 300), (63, 65), (1, 64), (300, 5)]
+    for k, (h, w) in enumerate(sizes):
+        tex = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+        levels = T.mip_chain(tex)
+        out[f"tex{k}"] = tex
+        out[f"tex{k}_depth"] = np.int64(len(levels))
+        for lv, a in enumerate(levels):
+            out[f"tex{k}_level{lv}"] = a
+    out["count"] = np.int64(len(sizes))
+    np.savez_compressed(os.path.join(HERE, "mips.npz"), **out)
+
+
 def converged():
     bindings.build(with_reference=True)
     R = bindings.OracleLib("ref")
@@ -341,6 +363,9 @@ if __name__ == "__main__":
     elif "--photo" in sys.argv:
         photo()
         print("photo fixture written to", HERE)
+    elif "--mips" in sys.argv:
+        mips()
+        print("mip chains written to", HERE)
     elif "--images" in sys.argv:
         images()
         print("image files written to", os.path.join(HERE, "images"))

@@ -232,3 +232,36 @@ def test_photo_passes_change_the_image(port):
     _, dof = port.photo(rec, 8, 63 | 1024, **PHOTO_POST)
     assert (bl - base).min() >= 0.0 and (bl - base).max() > 0.1
     assert np.abs(dof - base).mean() > 0.01
+
+
+# ------------------------------------------------------------- textures ----
+MIP_SIZES = [(21, 37), (1, 64), (3, 300), (16, 2048), (255, 257), (1, 1), (600, 5), (64, 64)]
+
+
+def test_mip_chain_matches_reference(ref_tex):
+    """oracle/image_codecs.mip_chain (the checker of the device-built chains)
+    against the reference's own ImageData::generateMipmaps, level for level."""
+    from oracle.image_codecs import mip_chain
+    rng = np.random.default_rng(31)
+    for h, w in MIP_SIZES:
+        tex = rng.integers(0, 256, (h, w, 4)).astype(np.uint8)
+        want = ref_tex.mip_chain(tex)
+        got = mip_chain(tex)
+        assert len(got) == len(want) and all(np.array_equal(a, b) for a, b in zip(got, want)), (h, w)
+
+
+def test_golden_mip_chains():
+    """The same pin carried by tests/golden/mips.npz (made from the
+    reference by make_golden.py --mips)."""
+    from oracle.image_codecs import mip_chain
+    z = np.load(os.path.join(GOLDEN, "mips.npz"))
+    for k in range(int(z["count"])):
+        got = mip_chain(z[f"tex{k}"])
+        want = [z[f"tex{k}_level{lv}"] for lv in range(int(z[f"tex{k}_depth"]))]
+        assert len(got) == len(want) and all(np.array_equal(a, b) for a, b in zip(got, want)), k
+
+
+def test_url_decode_matches_reference(ref_tex):
+    from oracle.obj_import import url_decode
+    for s in ["a%20b", "tex\\leaf.dds", "%41%42c", "x%4", "%2F%2f", "plain.dds", "100%25", "%e9t%C3%A9.png", ""]:
+        assert url_decode(s) == ref_tex.url_decode(s), s
