@@ -156,6 +156,7 @@ class OracleLib:
             "photo": (None, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
             "mip_chain": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
             "url_decode": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int]),
+            "material_properties": (None, [C.c_char_p, C.c_float, C.c_int, C.c_void_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(self.lib, f"{prefix}_{name}", None)
@@ -185,6 +186,14 @@ class OracleLib:
             levels.append(out[at:at + n].reshape(h >> lv, w >> lv, c).copy())
             at += n
         return levels
+
+    def material_properties(self, name: str, opacity=None) -> np.ndarray:
+        """Material::loadMaterialProperties of the reference (ref_tex only):
+        (opacity, ior, roughness, transmitting rgb, hasFullyTransparentPart)."""
+        out = np.zeros(7, np.float32)
+        self.fn("material_properties")(name.encode(), 1.0 if opacity is None else float(opacity),
+                                       0 if opacity is None else 1, _ptr(out))
+        return out
 
     def url_decode(self, s: str) -> str:
         """urlDecode of the reference (ref_tex only)."""

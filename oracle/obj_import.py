@@ -128,13 +128,13 @@ def parse_mtl(path: str) -> list:
         rest = rest.strip()
         try:
             if k == "newmtl":
-                mats.append({"name": rest, "opacity": 1.0, "textures": {}})
+                mats.append({"name": rest, "opacity": np.float32(1.0), "textures": {}})
             elif not mats:
                 continue
-            elif k == "d":
-                mats[-1]["opacity"] = float(rest.split()[-1])
+            elif k == "d":  # an ai_real (float), as assimp hands the opacity over
+                mats[-1]["opacity"] = np.float32(float(rest.split()[-1]))
             elif k == "tr":
-                mats[-1]["opacity"] = 1.0 - float(rest.split()[-1])
+                mats[-1]["opacity"] = np.float32(1.0) - np.float32(float(rest.split()[-1]))
             elif k in MTL_TEXTURES:
                 mats[-1]["textures"][MTL_TEXTURES[k]] = _texture_path(rest)
         except (ValueError, IndexError) as e:
@@ -258,7 +258,7 @@ def load_model(model_folder: str, model_name: str, skyMap_name: str = "null") ->
     cache, textures = {}, []
     mat_rows, mat_tex = [], []
     for name in names:
-        spec = by_name.get(name, {"name": name, "opacity": 1.0, "textures": {}})
+        spec = by_name.get(name, {"name": name, "opacity": np.float32(1.0), "textures": {}})
         slots = [-1, -1, -1, -1]
         for slot in sorted(spec["textures"]):
             p = url_decode((model_folder + spec["textures"][slot]).replace("\\", "/"))
@@ -268,7 +268,7 @@ def load_model(model_folder: str, model_name: str, skyMap_name: str = "null") ->
                 if tex is not None:
                     textures.append(tex)
             slots[slot] = cache[p]
-        if spec["opacity"] < 0.99:
+        if spec["opacity"] < np.float32(0.99):  # loadMaterialProperties compares floats
             op, ior, rough, trans = glass_properties(name)
             row = scenes.material(roughness=rough, opacity=op, ior=ior, transmitting=trans)
         else:

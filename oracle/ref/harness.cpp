@@ -453,6 +453,26 @@ int ref_mip_chain(const uint8_t* texels, int w, int h, int channels, uint8_t* ou
   return img.map_depth;
 }
 
+// Material::loadMaterialProperties (src/material.cpp:300-336) for a material
+// of this name and (when has_opacity) opacity, without textures: out =
+// opacity, ior, roughness, transmitting colour (3), hasFullyTransparentPart.
+void ref_material_properties(const char* name, float opacity, int has_opacity, float* out) {
+  aiMaterial am;
+  am.has_name = true;
+  am.name = name;
+  am.has_opacity = has_opacity != 0;
+  am.opacity = opacity;
+  Material m;
+  m.loadMaterialProperties(&am);
+  out[0] = m.opacity;
+  out[1] = m.ior;
+  out[2] = m.roughness;
+  out[3] = m.transmittingColor.x;
+  out[4] = m.transmittingColor.y;
+  out[5] = m.transmittingColor.z;
+  out[6] = m.hasFullyTransparentPart ? 1.0f : 0.0f;
+}
+
 // urlDecode (src/material.cpp:9-24) into out (NUL-terminated); returns the
 // decoded length or -1 when out is too small.
 int ref_url_decode(const char* in, char* out, int capacity) {

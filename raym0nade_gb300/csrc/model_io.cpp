@@ -211,7 +211,7 @@ std::string texture_path(const std::string& rest) {
 
 struct MtlSpec {
   std::string name;
-  double opacity = 1.0;
+  float opacity = 1.0f;  // ai_real, as assimp hands AI_MATKEY_OPACITY over
   std::map<int, std::string> textures;  // slot -> file name
 };
 
@@ -226,7 +226,7 @@ rmn_status parse_mtl(const std::string& path, std::vector<MtlSpec>& mats) {
     key_rest(line, key, rest);
     const std::string k = lower(key);
     if (k == "newmtl") {
-      mats.push_back(MtlSpec{rest, 1.0, {}});
+      mats.push_back(MtlSpec{rest, 1.0f, {}});
       continue;
     }
     if (mats.empty()) continue;
@@ -235,7 +235,7 @@ rmn_status parse_mtl(const std::string& path, std::vector<MtlSpec>& mats) {
       double v;
       if (t.empty() || !parse_double(t.back(), &v))
         return fail(RMN_ERR_INVALID_ARGUMENT, "%s:%zu: cannot read '%.60s'", path.c_str(), ln + 1, line.c_str());
-      mats.back().opacity = k == "d" ? v : 1.0 - v;
+      mats.back().opacity = k == "d" ? (float)v : 1.0f - (float)v;
     } else if (k == "map_kd") {
       mats.back().textures[RMN_TEX_DIFFUSE] = texture_path(rest);
     } else if (k == "map_ks") {
@@ -471,7 +471,7 @@ rmn_status read_model(const std::string& folder, const std::string& name, const 
   std::map<std::string, int> cache;  // texture path -> index, -1 = not loaded
   for (const std::string& n : names) {
     auto it = by_name.find(n);
-    const MtlSpec empty{n, 1.0, {}};
+    const MtlSpec empty{n, 1.0f, {}};
     const MtlSpec& spec = it != by_name.end() ? *it->second : empty;
     int32_t slots[4] = {-1, -1, -1, -1};
     for (const auto& kv : spec.textures) {  // slots in increasing order
@@ -494,7 +494,7 @@ rmn_status read_model(const std::string& folder, const std::string& name, const 
       }
       slots[kv.first] = c->second;
     }
-    M.materials.push_back(spec.opacity < 0.99 ? glass_material(n) : default_material());
+    M.materials.push_back(spec.opacity < 0.99f ? glass_material(n) : default_material());  // float test
     M.material_textures.insert(M.material_textures.end(), slots, slots + 4);
   }
   std::map<std::string, int> index_of;

@@ -265,3 +265,30 @@ def test_url_decode_matches_reference(ref_tex):
     from oracle.obj_import import url_decode
     for s in ["a%20b", "tex\\leaf.dds", "%41%42c", "x%4", "%2F%2f", "plain.dds", "100%25", "%e9t%C3%A9.png", ""]:
         assert url_decode(s) == ref_tex.url_decode(s), s
+
+
+def test_imported_materials_match_reference(ref_tex, tmp_path):
+    """The importer's materials (native rmn_model_read and the oracle's
+    restatement) against the reference's own Material::loadMaterialProperties
+    for the same names and opacities, including opacities within float
+    rounding of the 0.99 threshold."""
+    from oracle import obj_import
+    from raym0nade_gb300 import assets
+    cases = [("Ice", "d 0.5"), ("Water", "d 0.98"), ("White_Wine", "d 0.99"), ("Beer", "Tr 0.8"),
+             ("Red_Wine", "d 0.98999999"), ("TransparentGlassWine", "d 0.9899999"), ("TransparentGlass", "d 0"),
+             ("Other", "Tr 0.0"), ("Opaque", None), ("Half", "d 0.5"), ("Neg", "d -1")]
+    mtl = "".join(f"newmtl {n}\n" + (f"{d}\n" if d else "") for n, d in cases)
+    obj = "mtllib m.mtl\nv 0 0 0\nv 1 0 0\nv 0 1 0\n" + "".join(f"usemtl {n}\nf 1 2 3\n" for n, _ in cases)
+    (tmp_path / "m.mtl").write_text(mtl)
+    (tmp_path / "m.obj").write_text(obj)
+    folder = str(tmp_path) + "/"
+    for sc in (assets.load_model(folder, "m.obj"), obj_import.load_model(folder, "m.obj")):
+        for name, d in cases:
+            op = None
+            if d is not None:
+                key, v = d.split()
+                op = np.float32(float(v)) if key == "d" else np.float32(1.0) - np.float32(float(v))
+            ref = ref_tex.material_properties(name, op)
+            row = sc.materials[sc.material_names.index(name)]
+            got = np.array([row[11], row[12], row[8], row[13], row[14], row[15]], np.float32)
+            assert np.array_equal(got, ref[:6]), (name, d, got, ref)
