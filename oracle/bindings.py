@@ -157,6 +157,7 @@ class OracleLib:
             "mip_chain": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
             "url_decode": (C.c_int, [C.c_char_p, C.c_char_p, C.c_int]),
             "material_properties": (None, [C.c_char_p, C.c_float, C.c_int, C.c_void_p]),
+            "save_rows": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_char_p, C.c_void_p]),
         }
         for name, (res, args) in sig.items():
             f = getattr(self.lib, f"{prefix}_{name}", None)
@@ -193,6 +194,15 @@ class OracleLib:
         out = np.zeros(7, np.float32)
         self.fn("material_properties")(name.encode(), 1.0 if opacity is None else float(opacity),
                                        0 if opacity is None else 1, _ptr(out))
+        return out
+
+    def save_rows(self, rgb: np.ndarray, path: str) -> np.ndarray:
+        """The 8-bit rows the reference's Photo::save hands to libpng for an
+        (h, w, 3) float32 image (ref / ref_tex only)."""
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        h, w = rgb.shape[:2]
+        out = np.zeros((h, w, 3), np.uint8)
+        assert self.fn("save_rows")(_ptr(rgb), w, h, path.encode(), _ptr(out)) == 0
         return out
 
     def url_decode(self, s: str) -> str:

@@ -121,8 +121,12 @@ void Material::getSurfaceData(float, float, float& r, float& m) const {
 #endif
 
 // ---------------------------------------------------------------------------
-// libpng entry points: PNG output is not on the checked path.
+// libpng entry points. Writing records the IHDR size and the rows handed to
+// png_write_row (ref_save_rows reads them back: the bytes Photo::save
+// produces); nothing is compressed or read.
 static jmp_buf g_png_jmp;
+static unsigned g_png_w = 0, g_png_h = 0;
+static std::vector<png_byte> g_png_rows;
 jmp_buf* oracle_png_jmpbuf(png_structp) { return &g_png_jmp; }
 png_structp png_create_write_struct(const char*, void*, void*, void*) { return nullptr; }
 png_structp png_create_read_struct(const char*, void*, void*, void*) { return nullptr; }
@@ -130,9 +134,13 @@ png_infop png_create_info_struct(png_structp) { return nullptr; }
 void png_destroy_write_struct(png_structp*, png_infop*) {}
 void png_destroy_read_struct(png_structp*, png_infop*, png_infop*) {}
 void png_init_io(png_structp, FILE*) {}
-void png_set_IHDR(png_structp, png_infop, unsigned, unsigned, int, int, int, int, int) {}
+void png_set_IHDR(png_structp, png_infop, unsigned w, unsigned h, int, int, int, int, int) {
+  g_png_w = w;
+  g_png_h = h;
+  g_png_rows.clear();
+}
 void png_write_info(png_structp, png_infop) {}
-void png_write_row(png_structp, png_bytep) {}
+void png_write_row(png_structp, png_bytep row) { g_png_rows.insert(g_png_rows.end(), row, row + 3 * g_png_w); }
 void png_write_end(png_structp, png_infop) {}
 void png_read_info(png_structp, png_infop) {}
 unsigned png_get_image_width(png_structp, png_infop) { return 0; }
@@ -483,6 +491,19 @@ int ref_url_decode(const char* in, char* out, int capacity) {
   return (int)s.size();
 }
 #endif
+
+// Photo::save (src/image.cpp:481-532) of an RGB image: the 8-bit rows it
+// hands to libpng, into out (w * h * 3 bytes). Returns 0, or -1 when the
+// rows did not arrive (path not writable).
+int ref_save_rows(const float* rgb, int w, int h, const char* path, uint8_t* out) {
+  Photo ph(w, h);
+  for (long i = 0; i < (long)w * h; ++i) ph.pixelarray[i] = vec3(rgb[3 * i], rgb[3 * i + 1], rgb[3 * i + 2]);
+  g_png_rows.clear();
+  ph.save(path);
+  if (g_png_rows.size() != (size_t)w * h * 3) return -1;
+  std::memcpy(out, g_png_rows.data(), g_png_rows.size());
+  return 0;
+}
 
 void ref_fxaa(const float* in, float* out, int w, int h) {
   Photo ph(w, h);

@@ -292,3 +292,22 @@ def test_imported_materials_match_reference(ref_tex, tmp_path):
             row = sc.materials[sc.material_names.index(name)]
             got = np.array([row[11], row[12], row[8], row[13], row[14], row[15]], np.float32)
             assert np.array_equal(got, ref[:6]), (name, d, got, ref)
+
+
+def test_save_png_pixels_match_reference(ref, tmp_path):
+    """rmn_save_png's decoded pixels against the rows the reference's own
+    Photo::save hands to libpng (static_cast<png_byte>(v * 255)), on values
+    in [0, 1] including every k / 255 boundary and its float neighbours."""
+    from raym0nade_gb300 import _lib, build
+    build.build()
+    lib = _lib.load()
+    k = np.arange(256, dtype=np.float32) / np.float32(255)
+    edges = np.concatenate([k, np.nextafter(k, np.float32(0)), np.nextafter(k, np.float32(1))]).clip(0, 1)
+    rng = np.random.default_rng(8)
+    vals = np.concatenate([edges, rng.random(3 * 64 * 40 - edges.size, dtype=np.float32)])
+    img = vals[:3 * 64 * 40].reshape(40, 64, 3)
+    want = ref.save_rows(img, str(tmp_path / "ref.png"))
+    p = str(tmp_path / "ours.png")
+    assert lib.rmn_save_png(np.ascontiguousarray(img).ctypes.data, 64, 40, p.encode()) == 0
+    from oracle.image_codecs import png_read
+    assert np.array_equal(png_read(p), want)
