@@ -205,6 +205,35 @@ class OracleLib:
         assert self.fn("save_rows")(_ptr(rgb), w, h, path.encode(), _ptr(out)) == 0
         return out
 
+    def python_loaders(self):
+        """(sky_load, dds_load): the reference's SkyBox::load and
+        Material::loadImageFromDDS, which call the Python functions
+        hdr_to_array / dds_to_array of ./scripts through the embedded
+        interpreter -- here the running one, so they are called with the GIL
+        held (ref_tex only)."""
+        lib = C.PyDLL(REF_TEX_SO)
+        sky = lib.ref_sky_load
+        sky.restype, sky.argtypes = C.c_int, [C.c_char_p, C.c_void_p, C.c_long, C.c_void_p, C.c_void_p]
+        dds = lib.ref_dds_load
+        dds.restype, dds.argtypes = C.c_int, [C.c_char_p, C.c_void_p, C.c_long, C.c_void_p]
+
+        def sky_load(path, capacity=1 << 24):
+            out = np.zeros(capacity, np.float32)
+            w, h = C.c_int(), C.c_int()
+            if sky(path.encode(), _ptr(out), capacity, C.byref(w), C.byref(h)) != 0:
+                return None
+            return out[:w.value * h.value * 3].reshape(h.value, w.value, 3).copy()
+
+        def dds_load(path, capacity=1 << 24):
+            out = np.zeros(capacity, np.uint8)
+            dims = np.zeros(3, np.int32)
+            if dds(path.encode(), _ptr(out), capacity, _ptr(dims)) != 0:
+                return None
+            w, h, c = (int(x) for x in dims)
+            return out[:w * h * c].reshape(h, w, c).copy()
+
+        return sky_load, dds_load
+
     def url_decode(self, s: str) -> str:
         """urlDecode of the reference (ref_tex only)."""
         buf = C.create_string_buffer(4 * len(s) + 8)

@@ -461,6 +461,35 @@ int ref_mip_chain(const uint8_t* texels, int w, int h, int channels, uint8_t* ou
   return img.map_depth;
 }
 
+// SkyBox::load (src/component.cpp:69-114) as the reference runs it: through
+// call_image_to_array and the Python function hdr_to_array of module
+// hdr_to_array on the interpreter's path (./scripts). Call with the GIL held.
+// out receives the SkyBox's texels after SkyBox::Init (premultiplied by the
+// texel solid angle). Returns 0, or -1 for an empty sky or a small buffer.
+int ref_sky_load(const char* path, float* out, long capacity, int* w, int* h) {
+  SkyBox sky;
+  sky.load(path);
+  if (sky.empty() || (long)sky.data.size() * 3 > capacity) return -1;
+  *w = sky.width;
+  *h = sky.height;
+  for (size_t i = 0; i < sky.data.size(); ++i)
+    for (int c = 0; c < 3; ++c) out[3 * i + c] = sky.data[i][c];
+  return 0;
+}
+
+// Material::loadImageFromDDS (src/material.cpp:190-215) through the Python
+// function dds_to_array, as above: level 0 of the ImageData it fills.
+int ref_dds_load(const char* path, uint8_t* out, long capacity, int* dims) {
+  ImageData img;
+  if (!Material::loadImageFromDDS(img, path) || img.data[0].empty()) return -1;
+  if ((long)img.data[0].size() > capacity) return -1;
+  dims[0] = img.width;
+  dims[1] = img.height;
+  dims[2] = img.channels;
+  std::memcpy(out, img.data[0].data(), img.data[0].size());
+  return 0;
+}
+
 // Material::loadMaterialProperties (src/material.cpp:300-336) for a material
 // of this name and (when has_opacity) opacity, without textures: out =
 // opacity, ior, roughness, transmitting colour (3), hasFullyTransparentPart.

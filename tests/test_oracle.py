@@ -311,3 +311,31 @@ def test_save_png_pixels_match_reference(ref, tmp_path):
     assert lib.rmn_save_png(np.ascontiguousarray(img).ctypes.data, 64, 40, p.encode()) == 0
     from oracle.image_codecs import png_read
     assert np.array_equal(png_read(p), want)
+
+
+def test_script_mirrors_feed_the_references_loaders(ref_tex, tmp_path, monkeypatch):
+    """The reference's own SkyBox::load and Material::loadImageFromDDS,
+    calling scripts/hdr_to_array.py and scripts/dds_to_array.py through
+    their embedded-Python path, with those scripts being this package's
+    mirrors: the reference ends up with the texels the library decodes."""
+    from raym0nade_gb300 import assets, build
+    from tests.golden import image_files as F
+    build.build()
+    (tmp_path / "scripts").mkdir()
+    (tmp_path / "scripts" / "hdr_to_array.py").write_text("from raym0nade_gb300.assets import hdr_to_array\n")
+    (tmp_path / "scripts" / "dds_to_array.py").write_text("from raym0nade_gb300.assets import dds_to_array\n")
+    rng = np.random.default_rng(17)
+    rgbe = F.float_to_rgbe(np.exp(rng.normal(0, 2, (12, 40, 3))))
+    (tmp_path / "sky.hdr").write_bytes(F.encode_hdr(rgbe))
+    pay = rng.integers(0, 256, 3 * 4 * 16).astype(np.uint8).tobytes()
+    (tmp_path / "t.dds").write_bytes(F.encode_dds(13, 10, pay, b"DXT5"))
+    monkeypatch.chdir(tmp_path)
+    sky_load, dds_load = ref_tex.python_loaders()
+    got = sky_load(str(tmp_path / "sky.hdr"))
+    raw = assets.load_image(str(tmp_path / "sky.hdr"), assets.HDR)
+    h, w = raw.shape[:2]
+    phi = np.float32(np.pi) * (np.arange(h, dtype=np.float32) + np.float32(0.5)) / np.float32(h)
+    area = np.sin(phi) * np.float32(2 * np.pi) / np.float32(w * h)
+    np.testing.assert_allclose(got, raw * area[:, None, None], rtol=2e-6, atol=0)
+    tex = dds_load(str(tmp_path / "t.dds"))
+    assert np.array_equal(tex, assets.load_image(str(tmp_path / "t.dds"), assets.DDS))
