@@ -24,6 +24,7 @@
 // assimp's missing arrays). RGB images become RGBA with opaque alpha (the
 // reference leaves ImageData::channels unset for PNG files).
 #include <array>
+#include <atomic>
 #include <cerrno>
 #include <charconv>
 #include <cmath>
@@ -33,6 +34,7 @@
 #include <map>
 #include <string>
 #include <string_view>
+#include <thread>
 #include <vector>
 
 #include "rmn_host.h"
@@ -468,33 +470,70 @@ rmn_status read_model(const std::string& folder, const std::string& name, const 
     names.push_back(m.name);
     by_name[m.name] = &m;
   }
-  std::map<std::string, int> cache;  // texture path -> index, -1 = not loaded
+  // texture files in order of first use, decoded on several threads; the
+  // results are taken in that order, so indices and the first error are
+  // those of one-by-one loading
+  struct TexJob {
+    std::string path;
+    rmn::DecodedImage img;
+    bool loaded = false;
+    rmn_status st = RMN_OK;
+    std::string err;
+  };
+  std::vector<TexJob> jobs;
+  std::map<std::string, int> job_of;
+  std::vector<std::array<int, 4>> mat_jobs;
+  std::vector<const MtlSpec*> specs;
+  std::vector<MtlSpec> defaults;
+  defaults.reserve(names.size());
   for (const std::string& n : names) {
     auto it = by_name.find(n);
-    const MtlSpec empty{n, 1.0f, {}};
-    const MtlSpec& spec = it != by_name.end() ? *it->second : empty;
-    int32_t slots[4] = {-1, -1, -1, -1};
-    for (const auto& kv : spec.textures) {  // slots in increasing order
+    if (it == by_name.end()) defaults.push_back(MtlSpec{n, 1.0f, {}});
+    const MtlSpec& spec = it != by_name.end() ? *it->second : defaults.back();
+    specs.push_back(&spec);
+    std::array<int, 4> js = {-1, -1, -1, -1};
+    for (const auto& kv : spec.textures) {
       std::string p = folder + kv.second;
       for (char& c : p)
         if (c == '\\') c = '/';
       p = url_decode(p);
-      auto c = cache.find(p);
-      if (c == cache.end()) {
-        rmn::DecodedImage img;
-        bool loaded = false;
-        if ((st = load_texture(p, img, &loaded)) != RMN_OK) return st;
-        int idx = -1;
-        if (loaded) {
-          idx = (int)M.texels.size();
-          M.texels.push_back(std::move(img.bytes));
-          M.textures.push_back(rmn_texture{img.w, img.h, 4, nullptr});
-        }
-        c = cache.emplace(p, idx).first;
+      auto j = job_of.find(p);
+      if (j == job_of.end()) {
+        j = job_of.emplace(p, (int)jobs.size()).first;
+        jobs.emplace_back();
+        jobs.back().path = p;
       }
-      slots[kv.first] = c->second;
+      js[kv.first] = j->second;
     }
-    M.materials.push_back(spec.opacity < 0.99f ? glass_material(n) : default_material());  // float test
+    mat_jobs.push_back(js);
+  }
+  {
+    std::atomic<size_t> next{0};
+    auto work = [&]() {
+      for (size_t j; (j = next.fetch_add(1)) < jobs.size();) {
+        TexJob& t = jobs[j];
+        t.st = load_texture(t.path, t.img, &t.loaded);
+        if (t.st != RMN_OK) t.err = rmn_last_error();
+      }
+    };
+    const size_t nthreads = std::min<size_t>(jobs.size(), std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+    std::vector<std::thread> pool;
+    for (size_t k = 1; k < nthreads; ++k) pool.emplace_back(work);
+    work();
+    for (std::thread& t : pool) t.join();
+  }
+  std::vector<int> tex_of(jobs.size(), -1);
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    if (jobs[j].st != RMN_OK) return fail(jobs[j].st, "%s", jobs[j].err.c_str());
+    if (!jobs[j].loaded) continue;
+    tex_of[j] = (int)M.texels.size();
+    M.texels.push_back(std::move(jobs[j].img.bytes));
+    M.textures.push_back(rmn_texture{jobs[j].img.w, jobs[j].img.h, 4, nullptr});
+  }
+  for (size_t i = 0; i < names.size(); ++i) {
+    int32_t slots[4];
+    for (int k = 0; k < 4; ++k) slots[k] = mat_jobs[i][k] < 0 ? -1 : tex_of[mat_jobs[i][k]];
+    M.materials.push_back(specs[i]->opacity < 0.99f ? glass_material(names[i]) : default_material());  // float test
     M.material_textures.insert(M.material_textures.end(), slots, slots + 4);
   }
   std::map<std::string, int> index_of;

@@ -491,3 +491,23 @@ def test_save_png_compresses_and_round_trips(tmp_path, kind):
         assert size < 0.2 * raw
     if kind == "noise":
         assert size < raw * 1.01 + 200
+
+
+def test_native_importer_many_textures(tmp_path, capfd):
+    """Texture files decoded on several threads: indices in order of first
+    use, shared files once, a missing DDS and an unsupported type left out
+    with the reference's messages -- as the oracle's one-by-one loading."""
+    rng = np.random.default_rng(2)
+    folder = str(tmp_path) + "/"
+    mtl = []
+    for k in range(24):
+        pay = rng.integers(0, 256, (64 // 4) * (48 // 4) * 16).astype(np.uint8).tobytes()
+        (tmp_path / f"t{k}.dds").write_bytes(F.encode_dds(64, 48, pay, b"DXT5"))
+        mtl.append(f"newmtl m{k}\nmap_Kd t{k}.dds\nmap_Ks t{(k * 7) % 24}.dds\n")
+    mtl.append("newmtl bad\nmap_Kd missing.dds\nmap_Ks x.tga\n")
+    (tmp_path / "m.mtl").write_text("".join(mtl))
+    obj = "mtllib m.mtl\nv 0 0 0\nv 1 0 0\nv 0 1 0\n" + "".join(f"usemtl m{k}\nf 1 2 3\n" for k in range(24))
+    (tmp_path / "m.obj").write_text(obj + "usemtl bad\nf 1 2 3\n")
+    same_scene(assets.load_model(folder, "m.obj"), obj_import.load_model(folder, "m.obj"))
+    err = capfd.readouterr().err
+    assert "Unsupported file format: " in err and "Conversion failed: " in err
