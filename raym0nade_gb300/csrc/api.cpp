@@ -466,13 +466,17 @@ rmn_status rmn_save_png(const float* rgb, int32_t width, int32_t height, const c
   if (!rgb || !path || width <= 0 || height <= 0 || (int64_t)width * height > (1LL << 30))
     return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_save_png needs an image, a size and a path");
   const size_t n = (size_t)width * height * 3;
-  if (is_device_ptr(rgb)) {
-    std::vector<float> h(n);
-    cudaError_t e = cudaMemcpy(h.data(), rgb, n * sizeof(float), cudaMemcpyDeviceToHost);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy (rmn_save_png)");
-    return write_png(h.data(), width, height, path);
+  try {  // no C++ exception crosses the ABI
+    if (is_device_ptr(rgb)) {
+      std::vector<float> h(n);
+      cudaError_t e = cudaMemcpy(h.data(), rgb, n * sizeof(float), cudaMemcpyDeviceToHost);
+      if (e != cudaSuccess) return cuda_fail(e, "cudaMemcpy (rmn_save_png)");
+      return write_png(h.data(), width, height, path);
+    }
+    return write_png(rgb, width, height, path);
+  } catch (const std::bad_alloc&) {
+    return fail(RMN_ERR_OUT_OF_MEMORY, "out of host memory writing %s", path);
   }
-  return write_png(rgb, width, height, path);
 }
 
 const char* rmn_export_tag(int32_t k) {

@@ -26,6 +26,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <stdexcept>
 #include <string>
 #include <vector>
 
@@ -1009,7 +1010,14 @@ extern "C" rmn_status rmn_image_load(const char* path, int32_t kind, rmn_image_d
   if (!path || !info) return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_image_load needs a path and an info record");
   Decoded img;
   const bool header_only = data == nullptr;
-  rmn_status st = rmn::decode_image_file(path, kind, header_only, img);
+  rmn_status st;
+  try {  // no C++ exception crosses the ABI
+    st = rmn::decode_image_file(path, kind, header_only, img);
+  } catch (const std::bad_alloc&) {
+    return fail(RMN_ERR_OUT_OF_MEMORY, "out of host memory decoding %s", path);
+  } catch (const std::exception& e) {
+    return fail(RMN_ERR_INTERNAL, "decoding %s: %s", path, e.what());
+  }
   if (st != RMN_OK) return st;
   info->width = img.w;
   info->height = img.h;

@@ -31,6 +31,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <map>
 #include <string>
 #include <string_view>
@@ -661,6 +662,8 @@ rmn_status rmn_model_read(const char* model_folder, const char* model_name, cons
     st = read_model(model_folder, model_name, skyMap_name ? skyMap_name : "null", *m);
   } catch (const std::bad_alloc&) {
     st = fail(RMN_ERR_OUT_OF_MEMORY, "out of host memory reading %s%s", model_folder, model_name);
+  } catch (const std::exception& e) {  // e.g. no thread for the texture decoders
+    st = fail(RMN_ERR_INTERNAL, "reading %s%s: %s", model_folder, model_name, e.what());
   }
   if (st != RMN_OK) {
     delete m;
