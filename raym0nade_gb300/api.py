@@ -78,8 +78,8 @@ class Model:
         an OBJ/MTL model imported by raym0nade_gb300.assets.load_model."""
         lib = _lib.load()
         if isinstance(scene, str):
-            from . import assets
-            scene = assets.load_model(scene, model_name, skyMap_name)
+            self._from_file(lib, scene, model_name, skyMap_name)
+            return
         scene.check()
         self._keep = [np.ascontiguousarray(x) for x in (scene.positions, scene.normals, scene.uvs, scene.indices,
                                                         scene.mesh_first, scene.mesh_material, scene.materials)]
@@ -100,6 +100,26 @@ class Model:
         self.name = scene.name
         self.num_triangles = int(i.shape[0])
         self._keep = None  # the library copied everything it needs
+
+    def _from_file(self, lib, model_folder: str, model_name: str, skyMap_name: str) -> None:
+        """rmn_model_read -> rmn_model_desc -> rmn_scene_create: the arrays
+        go from the reader to the scene without a copy in Python."""
+        mh = C.c_void_p()
+        st = lib.rmn_model_read(os.fsencode(model_folder), os.fsencode(model_name or ""),
+                                os.fsencode(skyMap_name), C.byref(mh))
+        if st != 0:
+            raise ValueError(lib.rmn_last_error().decode(errors="replace"))
+        try:
+            d = _lib.SceneDesc()
+            _check(lib.rmn_model_desc(mh, C.byref(d)), "rmn_model_desc")
+            h = C.c_void_p()
+            _check(lib.rmn_scene_create(C.byref(d), C.byref(h)), "rmn_scene_create")
+            self._h = h
+            self.name = os.path.splitext(model_name or "")[0]
+            self.num_triangles = int(d.num_triangles)
+            self._keep = None
+        finally:
+            lib.rmn_model_free(mh)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:
@@ -417,6 +437,26 @@ class Batch:
         prof = _lib.RenderProfile()
         _check(_lib.load().rmn_batch_profile(self._h, C.byref(prof), _stream(stream)), "rmn_batch_profile")
         return {k: getattr(prof, k) for k, _ in prof._fields_}
+
+    def _from_file(self, lib, model_folder: str, model_name: str, skyMap_name: str) -> None:
+        """rmn_model_read -> rmn_model_desc -> rmn_scene_create: the arrays
+        go from the reader to the scene without a copy in Python."""
+        mh = C.c_void_p()
+        st = lib.rmn_model_read(os.fsencode(model_folder), os.fsencode(model_name or ""),
+                                os.fsencode(skyMap_name), C.byref(mh))
+        if st != 0:
+            raise ValueError(lib.rmn_last_error().decode(errors="replace"))
+        try:
+            d = _lib.SceneDesc()
+            _check(lib.rmn_model_desc(mh, C.byref(d)), "rmn_model_desc")
+            h = C.c_void_p()
+            _check(lib.rmn_scene_create(C.byref(d), C.byref(h)), "rmn_scene_create")
+            self._h = h
+            self.name = os.path.splitext(model_name or "")[0]
+            self.num_triangles = int(d.num_triangles)
+            self._keep = None
+        finally:
+            lib.rmn_model_free(mh)
 
     def close(self):
         if getattr(self, "_h", None) is not None and self._h.value:

@@ -511,3 +511,22 @@ def test_native_importer_many_textures(tmp_path, capfd):
     same_scene(assets.load_model(folder, "m.obj"), obj_import.load_model(folder, "m.obj"))
     err = capfd.readouterr().err
     assert "Unsupported file format: " in err and "Conversion failed: " in err
+
+
+def test_model_from_file_goes_native_to_scene_create(tmp_path):
+    """api.Model(folder, name, sky) hands rmn_model_read's description
+    straight to rmn_scene_create: it builds on a GPU, and without one it gets
+    as far as the first device allocation (the description passes every
+    argument check)."""
+    from raym0nade_gb300 import api
+    folder = str(tmp_path) + "/"
+    model_files.write_room(folder)
+    try:
+        m = api.Model(folder, "room.obj", "sky.hdr")
+    except api.RmnError as e:
+        assert e.status == 2, str(e)  # RMN_ERR_CUDA: no device here
+    else:
+        assert m.num_triangles == assets.load_model(folder, "room.obj").num_triangles
+        assert m.info()["num_lights"] == 1
+    with pytest.raises(ValueError, match="could not read"):
+        api.Model(folder, "missing.obj")
