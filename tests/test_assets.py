@@ -530,3 +530,62 @@ def test_model_from_file_goes_native_to_scene_create(tmp_path):
         assert m.info()["num_lights"] == 1
     with pytest.raises(ValueError, match="could not read"):
         api.Model(folder, "missing.obj")
+
+
+def test_decoders_and_importer_survive_mutated_files(tmp_path):
+    """Malformed files give a status, never a crash: truncated, bit-flipped
+    and spliced copies of the committed images (PNG chunk CRCs repaired so
+    the damage reaches inflate and the filters), and of the OBJ/MTL room."""
+    import zlib as _z
+    rng = np.random.default_rng(99)
+    d = os.path.join(GOLDEN, "images")
+    kinds = {"png": assets.PNG, "dds": assets.DDS, "hdr": assets.HDR}
+
+    def fix_crcs(b):
+        at = 8
+        while at + 12 <= len(b):
+            n = int.from_bytes(b[at:at + 4], "big")
+            if n > len(b) - at - 12:
+                break
+            b[at + 8 + n:at + 12 + n] = (_z.crc32(bytes(b[at + 4:at + 8 + n])) & 0xFFFFFFFF).to_bytes(4, "big")
+            at += 12 + n
+
+    statuses = set()
+    for name in sorted(os.listdir(d)):
+        kind = kinds[name.rsplit(".", 1)[1]]
+        base = open(os.path.join(d, name), "rb").read()
+        for _ in range(150):
+            b = bytearray(base)
+            if rng.random() < 0.3:
+                b = b[:int(rng.integers(0, len(b)))]
+            for _ in range(int(rng.integers(1, 6))):
+                if b:
+                    b[int(rng.integers(0, len(b)))] = int(rng.integers(0, 256))
+            if kind == assets.PNG and rng.random() < 0.8:
+                fix_crcs(b)
+            p = write(tmp_path, "m.bin", bytes(b))
+            statuses.add(status_of(p, kind))
+    assert statuses <= {0, 1, 4} and 1 in statuses
+    folder = str(tmp_path) + "/"
+    model_files.write_room(folder)
+    obj = open(folder + "room.obj").read()
+    alphabet = "0123456789 -+./\\\n\tvfnt#%eE"
+    for _ in range(150):
+        t = list(obj)
+        for _ in range(int(rng.integers(1, 8))):
+            at = int(rng.integers(0, len(t)))
+            op = rng.integers(0, 3)
+            if op == 0:
+                t[at] = alphabet[int(rng.integers(0, len(alphabet)))]
+            elif op == 1:
+                del t[at:at + int(rng.integers(1, 20))]
+            else:
+                t.insert(at, alphabet[int(rng.integers(0, len(alphabet)))])
+        with open(folder + "m.obj", "w") as f:
+            f.write("".join(t))
+        try:
+            sc = assets.load_model(folder, "m.obj")
+        except ValueError:
+            continue
+        sc.check()
+        assert (sc.indices >= 0).all() and (sc.indices < sc.positions.shape[0]).all()
