@@ -277,7 +277,9 @@ def config_timings(args, stream, flush, barrier):
       traversal   -- 1M-triangle random soup, 4M closest-hit + 4M shadow rays;
       heightfield -- 2048^2 heightfield (8,380,418 triangles) under a
                      2048x1024 sky, 1920x1080, 256 spp, depth 16, composed
-                     with gamma and FXAA."""
+                     with gamma and FXAA;
+    then the post passes' export set, the textured room, the glass Cornell
+    box and the host-side asset front-end."""
     import torch
     from raym0nade_gb300 import api, scenes
 
@@ -368,6 +370,19 @@ def config_timings(args, stream, flush, barrier):
                        "cpu_port_Mpaths_s": cpu["Mpaths_s"], "cpu_sample": cpu["sample"],
                        "workload": "textured room (diffuse / specular / emissive / normal-map textures with mip "
                                    "chains, alpha-tested cutouts), 1024x768, 64 spp, max depth 16 (rmn_render)"}
+    try:  # glass and media; a failure here is reported, not fatal to the line
+        gm = api.Model(scenes.cornell_glass())
+        ga = api.RenderArgs.from_camera(scenes.cornell_camera(512, 512, 64), seed=1)
+        gp = api.Photo(512, 512)
+        ms = timeit(lambda: api.render(gm, ga, gp, stream))
+        cpu = glass_cpu_sample()
+        out["glass"] = {"Mpaths_s": 512 * 512 * 64 / ms / 1e3, "ms": ms,
+                        "cpu_port_Mpaths_s": cpu["Mpaths_s"], "cpu_sample": cpu["sample"],
+                        "workload": "Cornell box with a glass tall box and a half-opaque short box, 512x512, "
+                                    "64 spp (x16 indirect paths behind glass), max depth 16 (rmn_render)"}
+        del gm, gp
+    except Exception as e:  # pragma: no cover
+        out["glass"] = {"error": f"{type(e).__name__}: {e}"[:300]}
     try:  # host-side asset front-end; a failure here is reported, not fatal to the line
         out["asset_decode"] = asset_decode_timings(max(1, min(args.steps, 3)))
     except Exception as e:  # pragma: no cover
@@ -497,6 +512,22 @@ def textured_cpu_sample():
     sc.render(cam, seed=1, mode=0, threads=th)
     dt = time.perf_counter() - t0
     return {"Mpaths_s": 256 * 192 * 64 / dt / 1e6, "sample": f"256x192, 64 spp, {th} threads"}
+
+
+def glass_cpu_sample():
+    """The CPU restatement (all host threads) of the glass Cornell box on a
+    96x96 image at 64 spp."""
+    import os as _os
+    from oracle.bindings import OracleLib
+    from raym0nade_gb300 import scenes
+    port = OracleLib("port")
+    sc = port.scene(scenes.cornell_glass())
+    cam = scenes.cornell_camera(96, 96, 64)
+    th = _os.cpu_count() or 8
+    t0 = time.perf_counter()
+    sc.render(cam, seed=1, mode=0, threads=th)
+    dt = time.perf_counter() - t0
+    return {"Mpaths_s": 96 * 96 * 64 / dt / 1e6, "sample": f"96x96, 64 spp, {th} threads"}
 
 
 def run_gpu(args, rank, world, dist):
