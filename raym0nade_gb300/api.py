@@ -325,6 +325,24 @@ class Photo:
         return {lib.rmn_export_tag(k).decode(): out[k] for k in range(cnt.value)}
 
     @staticmethod
+    def load(file_name: str):
+        """Photo(const char* file_name) / Photo::load (src/image.cpp:18,
+        534-607): the PNG's RGB, every colour type and depth brought to 8
+        bits as libpng's transforms there do (rmn_image_load), divided by
+        255 -> (h, w, 3) float32 on the host."""
+        from . import assets
+        return assets.load_png(file_name).astype(np.float32) / np.float32(255.0)
+
+    @staticmethod
+    def reverseGammaCorrection(rgb):
+        """Photo::reverseGammaCorrection (src/image.cpp:610-613): every
+        channel to the power 2.2 (host; the step before FXAA in the
+        reference's fxaa.cpp tool)."""
+        if torch is not None and isinstance(rgb, torch.Tensor):
+            return torch.pow(rgb, 2.2)
+        return np.power(np.asarray(rgb, np.float32), np.float32(2.2))
+
+    @staticmethod
     def save(rgb, path: str) -> None:
         """Photo::save (src/image.cpp:481-532): an 8-bit RGB PNG through
         rmn_save_png, each channel * 255 truncated to a byte; a path ending in

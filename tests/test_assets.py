@@ -589,3 +589,23 @@ def test_decoders_and_importer_survive_mutated_files(tmp_path):
             continue
         sc.check()
         assert (sc.indices >= 0).all() and (sc.indices < sc.positions.shape[0]).all()
+
+
+def test_photo_load_and_reverse_gamma(tmp_path):
+    """Photo::load (the PNG's RGB / 255) and reverseGammaCorrection, the
+    first steps of the reference's fxaa.cpp tool, on a saved image and on a
+    16-bit gray-alpha PNG."""
+    from raym0nade_gb300 import api
+    rng = np.random.default_rng(4)
+    img = rng.random((9, 14, 3), dtype=np.float32)
+    p = str(tmp_path / "a.png")
+    api.Photo.save(img, p)
+    got = api.Photo.load(p)
+    want = (img * np.float32(255)).astype(np.uint8).astype(np.float32) / np.float32(255)
+    assert got.dtype == np.float32 and np.array_equal(got, want)
+    s = rng.integers(0, 65536, (5, 6, 2))
+    q = write(tmp_path, "g.png", F.encode_png(s, 4, 16))
+    g = api.Photo.load(q)
+    assert np.array_equal(g[..., 0], (s[..., 0] >> 8).astype(np.float32) / np.float32(255))
+    r = api.Photo.reverseGammaCorrection(got)
+    assert np.array_equal(r, np.power(got, np.float32(2.2)))
