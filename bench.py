@@ -163,22 +163,40 @@ def job_rate(paths_per_rank, world, seconds):
     return paths_per_rank * world / seconds / 1e6
 
 
-def cpu_sample_render(scs, insts, block, threads):
-    """Render a block x block pixel square at the centre of every instance
-    with the CPU library's scenes `scs`; returns (paths, seconds)."""
+# CPU sample of every instance: one pixel drawn uniformly (seeded) from each
+# cell of a CPU_GRID x CPU_GRID grid laid over the whole image, so the sample
+# spans sky-miss and hit regions in proportion; the same pixels in both the
+# reference arm and the GPU line's cpu_baseline.
+CPU_GRID = 48
+
+
+def cpu_sample_pixels(inst, grid=CPU_GRID):
+    """Row-major pixel indices of the stratified sample of one instance."""
+    c = inst.camera
+    gx, gy = min(grid, c.width), min(grid, c.height)
+    rng = np.random.default_rng(1_000_003 * (inst.seed + 1) + c.width * 7919 + c.height)
+    xe = np.linspace(0, c.width, gx + 1).astype(np.int64)
+    ye = np.linspace(0, c.height, gy + 1).astype(np.int64)
+    xs = xe[:-1] + (rng.random(gx) * (xe[1:] - xe[:-1])).astype(np.int64)
+    ys = ye[:-1, None] + (rng.random((gy, gx)) * (ye[1:] - ye[:-1])[:, None]).astype(np.int64)
+    return (ys * c.width + xs[None, :]).ravel()
+
+
+def cpu_sample_render(scs, insts, threads):
+    """Render the stratified pixel sample of every instance with the CPU
+    library's scenes `scs` (reference mt19937 stream, per-pixel seeds);
+    returns (paths, seconds)."""
     paths, secs = 0, 0.0
     for sc, inst in zip(scs, insts):
-        c = inst.camera
-        b = min(block, c.width, c.height)
-        x0, y0 = (c.width - b) // 2, (c.height - b) // 2
+        px = cpu_sample_pixels(inst)
         t = time.perf_counter()
-        sc.render(c, seed=inst.seed, mode=0, rect=(x0, y0, x0 + b, y0 + b), threads=threads)
+        sc.render_pixels(inst.camera, inst.seed, px, mode=0, threads=threads)
         secs += time.perf_counter() - t
-        paths += b * b * c.spp
+        paths += px.size * inst.camera.spp
     return paths, secs
 
 
-def cpu_baseline(insts, target_s=15.0):
+def cpu_baseline(insts):
     from oracle import bindings
     if not os.path.exists(bindings.PORT_SO):
         bindings.build(with_reference=False)
@@ -186,24 +204,31 @@ def cpu_baseline(insts, target_s=15.0):
     lib = bindings.OracleLib("ref" if kind == "reference" else "port")
     threads = os.cpu_count() or 8
     scs = [lib.scene(i.scene) for i in insts]
-    # probe the rate on a small block, then size the block for ~target_s
-    p0, s0 = cpu_sample_render(scs, insts, 6, threads)
-    rate = p0 / max(s0, 1e-6)
-    block = int(max(6, min(512, math.sqrt(max(1.0, rate * target_s / max(1, sum(i.camera.spp for i in insts)))))))
-    paths, secs = cpu_sample_render(scs, insts, block, threads)
+    paths, secs = cpu_sample_render(scs, insts, threads)
+    npx = sum(cpu_sample_pixels(i).size for i in insts)
     return {"value": paths / secs / 1e6, "unit": UNIT, "cores": threads, "kind": kind,
-            "sample": f"{block}x{block} centre pixels of each of the {len(insts)} instances at their own spp/depth "
-                      f"({paths} paths, {secs:.1f} s, reference mt19937 stream)"}, scs, block
+            "sample": f"{npx} pixels: in each of the {len(insts)} instances one seeded uniform pixel per cell of a "
+                      f"{CPU_GRID}x{CPU_GRID} grid over the whole image, at the instance's own spp and depth "
+                      f"({paths} paths, {secs:.1f} s, reference mt19937 stream)"}, scs
+
+
+def workload_config(insts, desc, world):
+    """The workload's `config` object, identical in both arms."""
+    return {"workload": desc, "instances": len(insts),
+            "triangles": int(sum(i.scene.num_triangles for i in insts)),
+            "pixels": int(sum(i.camera.width * i.camera.height for i in insts)),
+            "paths_per_step": int(sum(instance_paths(i) for i in insts)), "parallelism": f"replicas x{world}",
+            "l2": "scene data > L2 (129 MB), and a 256 MiB buffer is overwritten between GPU steps"}
 
 
 def run_reference(args, rank, world):
     if rank != 0:
         return
     insts, desc = workload(args.workload, 0)
-    base, scs, block = cpu_baseline(insts, target_s=20.0 / (args.warmup + args.steps + 2))
+    base, scs = cpu_baseline(insts)
     vals, secs = [], []
     for step in range(args.warmup + args.steps):
-        p, s = cpu_sample_render(scs, insts, block, base["cores"])
+        p, s = cpu_sample_render(scs, insts, base["cores"])
         if step >= args.warmup:
             vals.append(p / s / 1e6)
             secs.append(s)
@@ -212,8 +237,8 @@ def run_reference(args, rank, world):
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": 1e3 * float(np.mean(secs)), "higher_is_better": True,
            "scaling": "weak",
-           "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-           "config": {"workload": desc, "sample": base["sample"]}, "cpu_baseline": base,
+           "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded procedural scenes; no dataset)",
+           "config": workload_config(insts, desc, world), "cpu_baseline": base,
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(out))
 
@@ -549,8 +574,9 @@ def run_gpu(args, rank, world, dist):
 
     tune = None
     if args.autotune:
-        # project autotuner: slots per work unit x worker pool, timed on a
-        # 1/16-pixel proxy of the same batch (untimed here)
+        # project autotuner: slots per work unit x worker pool x lanes, then
+        # the traversal stack, timed on a 1/16-pixel proxy of the same batch
+        # (untimed here)
         t0 = time.perf_counter()
         tune = api.autotune(list(zip(models, argsl, photos)), 1.0 / 16, stream)
         tune["tune_s"] = round(time.perf_counter() - t0, 2)
@@ -559,7 +585,8 @@ def run_gpu(args, rank, world, dist):
     lanes = (tune["lanes"] if tune else 0) or 3  # 0: the library default, 3 lanes
     with torch.cuda.stream(stream):
         batch = api.Batch(list(zip(models, argsl, photos)), use_graph=True, stream=stream,
-                          pool_workers=tune["pool_workers"] if tune else 0, lanes=tune["lanes"] if tune else 0)
+                          pool_workers=tune["pool_workers"] if tune else 0, lanes=tune["lanes"] if tune else 0,
+                          stack_entries=tune["stack_entries"] if tune else 0)
 
     def step_batched():
         batch.render(stream)
@@ -647,17 +674,15 @@ def run_gpu(args, rank, world, dist):
     logic_share = prof["logic_ms"] / max(1e-9, total_ms)
     trace_ms_live = ms_b * trace_share
     achieved = alg_bytes / (trace_ms_live / 1e3) / 1e9
-    base, _, _ = cpu_baseline(insts) if args.cpu_baseline else (None, None, None)
+    base, _ = cpu_baseline(insts) if args.cpu_baseline else (None, None)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": ms_b, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded procedural scenes; no dataset)",
-        "config": {"workload": desc, "instances": len(insts), "triangles": int(sum(i.scene.num_triangles for i in insts)),
-                   "pixels": npx, "paths_per_step": paths_per_step, "parallelism": f"replicas x{world}",
-                   "l2": f"scene data {scene_bytes / 1e9:.2f} GB > L2, and a 256 MiB buffer is overwritten between steps",
-                   "launch": "rmn_batch: G-buffer kernel, then wavefront iterations (shade, NEE, slot, closest and "
-                             "shadow traversal kernels) of every lane as parallel branches of a replayed CUDA graph",
-                   "scene_build_s": round(build_s, 1)},
+        "config": workload_config(insts, desc, world),
+        "setup": {"launch": "rmn_batch: G-buffer kernel, then wavefront iterations (shade, NEE, slot, closest and "
+                            "shadow traversal kernels) of every lane as parallel branches of a replayed CUDA graph",
+                  "scene_bytes": scene_bytes, "scene_build_s": round(build_s, 1)},
         "plain": {"value": plain, "unit": UNIT, "ms_per_step": ms_p, "launches_per_step": 2 * len(insts),
                   "batched_over_plain": value / plain},
         "e2e": {"value": job_rate(paths_per_step, world, e2e_s), "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -680,7 +705,7 @@ def run_gpu(args, rank, world, dist):
         "clocks": clocks,
     }
     if tune:
-        out["config"]["autotune"] = tune
+        out["setup"]["autotune"] = tune
     if adj:
         out["adjoint"] = adj
     if per_config:
@@ -688,6 +713,111 @@ def run_gpu(args, rank, world, dist):
     if base:
         out["cpu_baseline"] = base
     print(json.dumps(out))
+
+
+def profile_case(a):
+    """One small, self-contained case per kernel for ncu (``--profile-case``):
+    each builds its scene, runs the work once as a warm-up and once more, and
+    exits, so ``ncu --clock-control none -k regex:<kernel> -s <n> -c 1``
+    captures a warm launch. Scene data is sized above the 129 MB L2 where the
+    case allows, while the process holds a few GB at most (the batch case: the
+    64-instance workload at the given launch configuration).
+
+      render    rmn_render of a heightfield (--tris) under the synthetic sky,
+                --size square, --spp
+      trace     rmn_trace_closest / rmn_trace_shadow on a random soup (--tris,
+                --rays)
+      batch     the batch64 workload as one rmn_batch (--slots per unit,
+                --pool workers per lane, --lanes, --stack entries), rendered
+                twice
+      adjoint   rmn_render then rmn_adjoint of the 16-material Cornell box,
+                --size square, --spp, depth 16, twice
+      fxaa      rmn_compose(Full | gamma | FXAA) of a --size WxH image
+      post      the textured room at --size WxH, then rmn_export_set twice
+      textured  rmn_render of the textured room at --size WxH, twice
+    """
+    import torch
+
+    from raym0nade_gb300 import api, scenes
+
+    torch.cuda.init()
+    t0 = time.time()
+    if a.profile_case == "render":
+        n = max(3, int(round(math.sqrt(a.tris / 2.0))) + 1)
+        s = scenes.heightfield(n, seed=3)
+        s.env = scenes.sky_env(1024, 512)
+        side = int(a.size)
+        cam = scenes.heightfield_camera(side, side, a.spp)
+        m = api.Model(s)
+        args = api.RenderArgs.from_camera(cam, seed=1)
+        ph = api.Photo(side, side)
+        for _ in range(2):
+            api.render(m, args, ph)
+        torch.cuda.synchronize()
+        print("render", m.info(), "pixels", side * side, "spp", a.spp)
+    elif a.profile_case == "batch":
+        insts = scenes.batch_instances(64, seed=7)
+        models = [api.Model(i.scene) for i in insts]
+        argsl = [api.RenderArgs.from_camera(i.camera, seed=i.seed) for i in insts]
+        for r in argsl:
+            r.slots_per_unit = a.slots
+        photos = [api.Photo(i.camera.width, i.camera.height) for i in insts]
+        b = api.Batch(list(zip(models, argsl, photos)), use_graph=True, pool_workers=a.pool, lanes=a.lanes,
+                      stack_entries=a.stack)
+        for _ in range(2):
+            b.render()
+        torch.cuda.synchronize()
+        print("batch", len(insts), "instances: slots", a.slots, "pool", a.pool, "lanes", a.lanes, "stack", a.stack)
+    elif a.profile_case == "adjoint":
+        side = int(a.size)
+        cam = scenes.cornell_camera(side, side, a.spp, max_depth=16)
+        m = api.Model(scenes.cornell16())
+        args = api.RenderArgs.from_camera(cam, seed=1)
+        ph = api.render(m, args)
+        g = torch.ones((side * side, 3), dtype=torch.float32, device="cuda")
+        for _ in range(2):
+            api.adjoint(m, args, ph, g)
+        torch.cuda.synchronize()
+        print("adjoint", side, "spp", a.spp)
+    elif a.profile_case == "trace":
+        s = scenes.random_soup(a.tris, 1)
+        m = api.Model(s)
+        rays = torch.from_numpy(scenes.random_rays(a.rays, 2)).cuda()
+        sr = torch.from_numpy(scenes.random_rays(a.rays, 3, shadow=True)).cuda()
+        for _ in range(2):
+            m.rayHit(rays)
+            m.rayHit_test(sr)
+        torch.cuda.synchronize()
+        print("trace", m.info(), "rays", a.rays)
+    elif a.profile_case in ("post", "textured"):
+        w, h = (int(x) for x in a.size.split("x")) if "x" in a.size else (1920, 1080)
+        m = api.Model(scenes.textured_room())
+        cam = scenes.textured_camera(w, h, a.spp)
+        args = api.RenderArgs.from_camera(cam, seed=1)
+        ph = api.Photo(w, h)
+        api.render(m, args, ph)
+        if a.profile_case == "textured":
+            api.render(m, args, ph)
+        else:
+            ph.focus, ph.CoC, ph.cameraPosition = 3.0, 6.0, tuple(cam.position)
+            out = torch.empty((api.EXPORTS + api.EXPORTS_DOF, h, w, 3), dtype=torch.float32, device="cuda")
+            for _ in range(2):
+                ph.export_set(out)
+        torch.cuda.synchronize()
+        print(a.profile_case, w, h, "spp", a.spp)
+    else:
+        w, h = (int(x) for x in a.size.split("x")) if "x" in a.size else (1920, 1080)
+        rng = np.random.default_rng(1)
+        ph = api.Photo(w, h)
+        n = w * h
+        for k in ("radiance_Dd", "radiance_Ds", "radiance_Id", "radiance_Is"):
+            getattr(ph, k).copy_(torch.from_numpy(rng.random((n, 4), dtype=np.float32)))
+        ph.Gbuffer.copy_(torch.from_numpy(rng.random((n, api.GBUFFER_FLOATS), dtype=np.float32)))
+        for _ in range(2):
+            ph.shade(api.Full | api.GAMMA | api.DoFXAA)
+        torch.cuda.synchronize()
+        print("fxaa", w, h)
+    print(f"done in {time.time() - t0:.1f} s")
 
 
 def main():
@@ -701,7 +831,20 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false")
     ap.add_argument("--no-configs", dest="configs", action="store_false")
+    ap.add_argument("--profile-case", choices=["render", "trace", "batch", "adjoint", "fxaa", "post", "textured"],
+                    help="run one small case for a profiler instead of the benchmark (see profile_case)")
+    ap.add_argument("--tris", type=int, default=2_000_000)
+    ap.add_argument("--size", default="256")
+    ap.add_argument("--spp", type=int, default=16)
+    ap.add_argument("--rays", type=int, default=1_000_000)
+    ap.add_argument("--slots", type=int, default=2)
+    ap.add_argument("--pool", type=int, default=1 << 23)
+    ap.add_argument("--lanes", type=int, default=3)
+    ap.add_argument("--stack", type=int, default=0)
     args = ap.parse_args()
+    if args.profile_case:
+        profile_case(args)
+        return
     if args.warmup < 3:
         raise SystemExit("at least 3 warm-up steps")
     rank, world, dist = (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), None)

@@ -151,8 +151,9 @@ typedef struct rmn_render_args {
   uint64_t seed;                       /* counter-based random stream key */
   int32_t lanes_per_pixel;             /* work units per pixel (0: from slots_per_unit); 1..64 */
   int32_t slots_per_unit;              /* sample slots per work unit (0: library default: 2 for renders of up to
-                                          2^26 sample slots, else 4, more when the per-unit records would take
-                                          over a quarter of the free device memory) */
+                                          2^26 sample slots, else 4, doubled while the render's own per-unit
+                                          records, 112 B each, would exceed 16 GiB -- a choice of the render
+                                          alone, so its image does not depend on the batch or free memory) */
   int32_t reserved[2];
 } rmn_render_args;
 
@@ -207,8 +208,9 @@ rmn_status rmn_scene_destroy(rmn_scene* scene);
 rmn_status rmn_scene_info_get(const rmn_scene* scene, rmn_scene_info* info);
 
 /* Renders keep the device memory of their worker pools and queues for the
- * next render (up to 16 GiB per device); this frees it. No counterpart in the
- * reference. */
+ * next render (up to 16 GiB per device); this frees it, and makes
+ * rmn_compose_noalloc resolve its array's device address again (call it
+ * after a cudaDeviceReset). No counterpart in the reference. */
 rmn_status rmn_release_cached_memory(void);
 
 /* Replaces Model::rayHit (src/model.cpp:332-341): closest hit per ray. */
@@ -259,7 +261,9 @@ typedef struct rmn_batch_options {
   int32_t pool_workers;  /* paths in flight per lane (0: library default, 2^22, halved while the workers
                             would take over a quarter of the free device memory) */
   int32_t lanes;         /* independent wavefronts run side by side, 1..4 (0: library default, 3) */
-  int32_t reserved;
+  int32_t stack_entries; /* traversal stack, 23 or 27 entries (0: library default, the smallest that holds
+                            every item's tree: 23 when all trees are at most 22 levels deep); a stack too
+                            small for a tree is RMN_ERR_INVALID_ARGUMENT */
 } rmn_batch_options;
 rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_batch_options* options, void* stream,
                             rmn_batch** out);
@@ -274,6 +278,16 @@ rmn_status rmn_batch_update(rmn_batch* batch, const rmn_render_args* args, int32
 int64_t rmn_batch_update_bytes(const rmn_batch* batch);
 rmn_status rmn_batch_profile(rmn_batch* batch, rmn_render_profile* out, void* stream);
 rmn_status rmn_batch_destroy(rmn_batch* batch);
+/* Device bytes rmn_batch_create would take for these items with these
+ * options, the scenes and caller-owned images excluded: the per-unit records
+ * (112 B per unit of every item, at its slots_per_unit or the library's
+ * default split) and the worker pool (per worker its path state, shadow-ray
+ * slots and queue entries, times pool_workers per lane -- at most one
+ * worker per unit -- times lanes; the library's default pool counted at its
+ * full 2^22 per lane). No counterpart in the reference; for callers that
+ * plan device memory, and the autotuner's memory cap. */
+rmn_status rmn_batch_device_bytes(const rmn_batch_item* items, int32_t n, const rmn_batch_options* options,
+                                  int64_t* out);
 
 /* Project-written autotuner for batches. Times candidate launch
  * configurations -- slots per work unit in {2, 4, 8, 16} x workers per lane
@@ -281,15 +295,23 @@ rmn_status rmn_batch_destroy(rmn_batch* batch);
  * full-size batch would take more than half of the free device memory (the
  * library's own choice is always timed) -- on a proxy of the batch whose
  * images keep every item's scene, spp, depth and field of view but only
- * `pixel_fraction` (0 < f <= 1) of its pixels, and returns the fastest. Set
- * each item's slots_per_unit and the batch's pool_workers and lanes from the
- * result. The images do not depend on the choice beyond float summation
- * order across units (slots_per_unit); pool size and lanes change nothing. */
+ * `pixel_fraction` (0 < f <= 1) of its pixels (rmn_batch_device_bytes
+ * gives a candidate's full size); then the fastest of those
+ * once more with the other traversal stack build where the batch's trees
+ * allow both (27 entries instead of 23). Returns the fastest. Set each
+ * item's slots_per_unit and the batch's pool_workers, lanes and
+ * stack_entries from the result. The images do not depend on the choice
+ * beyond float summation order across units (slots_per_unit); pool size,
+ * lanes and stack change nothing. RMN_ERR_OUT_OF_MEMORY when not even the
+ * library's default split with the smallest pool (4096 workers, one lane)
+ * fits in the free device memory. */
 typedef struct rmn_tune_result {
   int32_t slots_per_unit, pool_workers;  /* 0: the library's default won */
   double best_ms, default_ms;  /* proxy render time: best and library default */
-  int32_t candidates;
+  int32_t candidates;          /* configurations timed */
   int32_t lanes;               /* 0: the library's default won */
+  int32_t stack_entries;       /* 23 or 27 (the value to pass in rmn_batch_options) */
+  int32_t reserved;
 } rmn_tune_result;
 rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixel_fraction, rmn_tune_result* out,
                               void* stream);
@@ -326,8 +348,11 @@ rmn_status rmn_compose(const rmn_image* image, int32_t width, int32_t height, fl
  * pixels (24 MiB, held by every GPU that loads the library); larger images
  * are rejected with RMN_ERR_INVALID_ARGUMENT. All buffers must be device
  * memory. The first call on each device resolves the array's address
- * (cudaGetSymbolAddress) and must come before any stream capture. Calls share
- * the array: calls whose work overlaps on the GPU race. */
+ * (cudaGetSymbolAddress) and must come before any stream capture; after a
+ * cudaDeviceReset, call rmn_release_cached_memory before the next call, so
+ * that it resolves the address anew. Calls share the array: calls whose
+ * work overlaps on the GPU race. The call returns once its work on `stream`
+ * has finished (it synchronises the stream). */
 #define RMN_NOALLOC_MAX_PIXELS (1 << 21)
 rmn_status rmn_compose_noalloc(const rmn_image* image, int32_t width, int32_t height, float exposure,
                                int32_t options, float* rgb, void* stream);
@@ -373,6 +398,12 @@ rmn_status rmn_export_set(const rmn_image* image, const rmn_post_args* args, flo
  * filtered adaptively and deflated (LZ77 + dynamic Huffman; stored blocks for
  * incompressible data), as libpng writes by default. */
 rmn_status rmn_save_png(const float* rgb, int32_t width, int32_t height, const char* path);
+
+/* Photo::reverseGammaCorrection (src/image.cpp:610-613) on the host: every
+ * channel of n rgb pixels to the power 2.2f with the C library's powf, as
+ * the reference's glm::pow of floats computes it (the step before FXAA in
+ * the reference's fxaa.cpp tool). In place when in == out. */
+rmn_status rmn_reverse_gamma(const float* in, int64_t n, float* out);
 
 /* Image decoders of the asset front-end (host memory, no GPU involved). */
 #define RMN_IMAGE_PNG 0 /* Material::loadImageFromPNG (src/material.cpp:217-285): 8-bit RGB,

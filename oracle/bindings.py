@@ -26,7 +26,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "_build", "libport.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
 REF_TEX_SO = os.path.join(HERE, "_ref", "libref_tex.so")
-REFERENCE_DIR = "/root/reference"
+# the reference checkout, where one is present: from the environment
+REFERENCE_DIR = os.environ.get("RMN_REFERENCE_DIR", "")
 PIX_FLOATS = 40
 
 
@@ -47,7 +48,8 @@ def build(with_reference: bool | None = None) -> None:
     targets = ["port"]
     if with_reference or (with_reference is None and os.path.isdir(os.path.join(REFERENCE_DIR, "src"))):
         targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE, "-j8"] + targets, check=True)
+    env = dict(os.environ, RMN_REFERENCE_DIR=REFERENCE_DIR)
+    subprocess.run(["make", "-s", "-C", HERE, "-j8"] + targets, check=True, env=env)
 
 
 def _ptr(a):
@@ -128,6 +130,16 @@ class OracleScene:
         self.lib.fn("render")(self.handle, _ptr(args), C.c_uint64(seed), mode, x0, y0, x1, y1, _ptr(out), threads)
         return out
 
+    def render_pixels(self, camera, seed: int, pixels, mode: int = 0, threads: int = 8) -> np.ndarray:
+        """Per-pixel records (n, 40) of the listed pixels (row-major indices
+        y * width + x), each rendered as in a whole-image render."""
+        px = np.ascontiguousarray(pixels, np.int32)
+        out = np.zeros((px.shape[0], PIX_FLOATS), np.float32)
+        args = camera.packed(threads)
+        self.lib.fn("render_pixels")(self.handle, _ptr(args), C.c_uint64(seed), mode, _ptr(px), px.shape[0],
+                                     _ptr(out), threads)
+        return out
+
 
 class OracleLib:
     def __init__(self, kind: str = "port"):
@@ -146,12 +158,15 @@ class OracleLib:
             "light_count": (C.c_int, [C.c_void_p]),
             "light_export": (None, [C.c_void_p, C.c_void_p]),
             "trace_closest": (None, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int]),
+            "render_pixels": (None, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_void_p, C.c_int64, C.c_void_p,
+                                     C.c_int]),
             "trace_shadow": (None, [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_int]),
             "trace_stats": (None, [C.c_void_p, C.c_void_p, C.c_int64, C.c_int, C.c_void_p]),
             "render": (None, [C.c_void_p, C.c_void_p, C.c_uint64, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                               C.c_void_p, C.c_int]),
             "compose": (None, [C.c_void_p, C.c_int64, C.c_float, C.c_int, C.c_void_p]),
             "gamma": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
+            "reverse_gamma": (None, [C.c_void_p, C.c_int64, C.c_void_p]),
             "fxaa": (None, [C.c_void_p, C.c_void_p, C.c_int, C.c_int]),
             "photo": (None, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_void_p]),
             "mip_chain": (C.c_int, [C.c_void_p, C.c_int, C.c_int, C.c_int, C.c_void_p, C.c_size_t]),
@@ -253,6 +268,13 @@ class OracleLib:
         rgb = np.ascontiguousarray(rgb, np.float32)
         out = np.empty_like(rgb)
         self.fn("gamma")(_ptr(rgb), rgb.size // 3, _ptr(out))
+        return out
+
+    def reverse_gamma(self, rgb: np.ndarray) -> np.ndarray:
+        """Photo::reverseGammaCorrection (reference build only)."""
+        rgb = np.ascontiguousarray(rgb, np.float32)
+        out = np.empty_like(rgb)
+        self.fn("reverse_gamma")(_ptr(rgb), rgb.size // 3, _ptr(out))
         return out
 
     def photo(self, recs: np.ndarray, stages: int, options: int = 0, exposure: float = 1.0, focus: float = 1.0,

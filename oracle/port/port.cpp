@@ -1710,6 +1710,17 @@ void port_render(void* h, const float* args, uint64_t seed, int mode, int x0, in
   }, 1);
 }
 
+// Renders the listed pixels (row-major indices y * width + x) of the image
+// described by args; out holds ORC_PIX_FLOATS per listed pixel.
+void port_render_pixels(void* h, const float* args, uint64_t seed, int mode, const int32_t* pixels, int64_t n,
+                        float* out, int threads) {
+  const Scene& s = *static_cast<Scene*>(h);
+  Args a = unpack_args(args);
+  parallel_for((long)n, threads, [&](long i) {
+    render_pixel(s, a, seed, mode, pixels[i] % a.w, pixels[i] / a.w, out + ORC_PIX_FLOATS * i);
+  }, 1);
+}
+
 // Photo::shade(Full) [+ gammaCorrection] over pixel records -> rgb.
 void port_compose(const float* recs, int64_t n, float exposure, int apply_gamma, float* rgb) {
   for (int64_t i = 0; i < n; ++i) {

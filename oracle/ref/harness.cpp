@@ -368,6 +368,23 @@ void ref_render(void* h, const float* args, uint64_t seed, int mode, int x0, int
   }, 1);
 }
 
+// renderPixel for the listed pixels (row-major indices), each with its
+// per-pixel seeded Generator; out holds ORC_PIX_FLOATS per listed pixel.
+void ref_render_pixels(void* h, const float* args, uint64_t seed, int mode, const int32_t* pixels, int64_t n,
+                       float* out, int threads) {
+  if (mode != 0) return;
+  const Model& m = *static_cast<Model*>(h);
+  RenderArgs a = unpack(args);
+  Photo ph(a.width, a.height);
+  ph.exposure = a.exposure;
+  for_each_index((long)n, threads, [&](long i) {
+    const int id = pixels[i];
+    RenderData rd((int)orc_pixel_seed(seed, (uint32_t)id));
+    renderPixel(m, a, rd, ph, id % a.width, id / a.width);
+    put_pixel(ph, id, out + ORC_PIX_FLOATS * i);
+  }, 1);
+}
+
 void ref_compose(const float* recs, int64_t n, float exposure, int apply_gamma, float* rgb) {
   Photo ph((int)n, 1);
   ph.exposure = exposure;
@@ -384,6 +401,16 @@ void ref_compose(const float* recs, int64_t n, float exposure, int apply_gamma, 
   if (apply_gamma) ph.gammaCorrection();
   for (int64_t i = 0; i < n; ++i) {
     rgb[3 * i] = ph.pixelarray[i].x; rgb[3 * i + 1] = ph.pixelarray[i].y; rgb[3 * i + 2] = ph.pixelarray[i].z;
+  }
+}
+
+// Photo::reverseGammaCorrection (src/image.cpp:610-613) over n rgb pixels.
+void ref_reverse_gamma(const float* in, int64_t n, float* out) {
+  Photo ph((int)n, 1);
+  for (int64_t i = 0; i < n; ++i) ph.pixelarray[i] = vec3(in[3 * i], in[3 * i + 1], in[3 * i + 2]);
+  ph.reverseGammaCorrection();
+  for (int64_t i = 0; i < n; ++i) {
+    out[3 * i] = ph.pixelarray[i].x; out[3 * i + 1] = ph.pixelarray[i].y; out[3 * i + 2] = ph.pixelarray[i].z;
   }
 }
 

@@ -69,12 +69,14 @@ class BatchItem(C.Structure):
 
 
 class BatchOptions(C.Structure):
-    _fields_ = [("use_graph", C.c_int32), ("pool_workers", C.c_int32), ("lanes", C.c_int32), ("reserved", C.c_int32)]
+    _fields_ = [("use_graph", C.c_int32), ("pool_workers", C.c_int32), ("lanes", C.c_int32),
+                ("stack_entries", C.c_int32)]
 
 
 class TuneResult(C.Structure):
     _fields_ = [("slots_per_unit", C.c_int32), ("pool_workers", C.c_int32), ("best_ms", C.c_double),
-                ("default_ms", C.c_double), ("candidates", C.c_int32), ("lanes", C.c_int32)]
+                ("default_ms", C.c_double), ("candidates", C.c_int32), ("lanes", C.c_int32),
+                ("stack_entries", C.c_int32), ("reserved", C.c_int32)]
 
 
 class ImageDesc(C.Structure):
@@ -100,6 +102,8 @@ SIGNATURES = {
     "rmn_batch_create": (C.c_int, [C.POINTER(BatchItem), C.c_int32, C.POINTER(BatchOptions), C.c_void_p,
                                    C.POINTER(C.c_void_p)]),
     "rmn_batch_autotune": (C.c_int, [C.POINTER(BatchItem), C.c_int32, C.c_float, C.POINTER(TuneResult), C.c_void_p]),
+    "rmn_batch_device_bytes": (C.c_int, [C.POINTER(BatchItem), C.c_int32, C.POINTER(BatchOptions),
+                                         C.POINTER(C.c_int64)]),
     "rmn_batch_render": (C.c_int, [C.c_void_p, C.c_void_p]),
     "rmn_batch_update": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
     "rmn_batch_update_bytes": (C.c_int64, [C.c_void_p]),
@@ -117,6 +121,7 @@ SIGNATURES = {
                                  C.c_void_p]),
     "rmn_export_tag": (C.c_char_p, [C.c_int32]),
     "rmn_save_png": (C.c_int, [C.c_void_p, C.c_int32, C.c_int32, C.c_char_p]),
+    "rmn_reverse_gamma": (C.c_int, [C.c_void_p, C.c_int64, C.c_void_p]),
     "rmn_export_options": (C.c_int32, [C.c_int32]),
     "rmn_image_load": (C.c_int, [C.c_char_p, C.c_int32, C.POINTER(ImageDesc), C.c_void_p, C.c_size_t]),
     "rmn_model_read": (C.c_int, [C.c_char_p, C.c_char_p, C.c_char_p, C.POINTER(C.c_void_p)]),

@@ -329,18 +329,26 @@ class Photo:
         """Photo(const char* file_name) / Photo::load (src/image.cpp:18,
         534-607): the PNG's RGB, every colour type and depth brought to 8
         bits as libpng's transforms there do (rmn_image_load), divided by
-        255 -> (h, w, 3) float32 on the host."""
+        255 -> (h, w, 3) float32 on the host. An interlaced (Adam7) PNG comes
+        back as its whole image; the reference reads it with png_read_row
+        without png_set_interlace_handling, so libpng hands it the rows of
+        the separate interlace passes instead."""
         from . import assets
         return assets.load_png(file_name).astype(np.float32) / np.float32(255.0)
 
     @staticmethod
     def reverseGammaCorrection(rgb):
         """Photo::reverseGammaCorrection (src/image.cpp:610-613): every
-        channel to the power 2.2 (host; the step before FXAA in the
-        reference's fxaa.cpp tool)."""
-        if torch is not None and isinstance(rgb, torch.Tensor):
+        channel to the power 2.2f (the step before FXAA in the reference's
+        fxaa.cpp tool). Host arrays go through rmn_reverse_gamma (the C
+        library's powf, as the reference); a device tensor is raised with
+        torch.pow on the GPU (CUDA's powf: within an ulp or two)."""
+        if torch is not None and isinstance(rgb, torch.Tensor) and rgb.is_cuda:
             return torch.pow(rgb, 2.2)
-        return np.power(np.asarray(rgb, np.float32), np.float32(2.2))
+        a = np.ascontiguousarray(np.asarray(rgb, np.float32))
+        out = np.empty_like(a)
+        _check(_lib.load().rmn_reverse_gamma(_ptr(a), a.size // 3, _ptr(out)), "rmn_reverse_gamma")
+        return out
 
     @staticmethod
     def save(rgb, path: str) -> None:
@@ -415,24 +423,38 @@ def _batch_items(items):
 
 def autotune(items, pixel_fraction: float = 1.0 / 16, stream=None) -> dict:
     """rmn_batch_autotune over (Model, RenderArgs, Photo) items: the fastest
-    slots per unit and pool size on a proxy with `pixel_fraction` of the
-    pixels."""
+    slots per unit, pool size, lanes and traversal stack on a proxy with
+    `pixel_fraction` of the pixels. Pass slots_per_unit to the items'
+    RenderArgs and pool_workers / lanes / stack_entries to Batch."""
     res = _lib.TuneResult()
     _check(_lib.load().rmn_batch_autotune(_batch_items(items), len(items), float(pixel_fraction), C.byref(res),
                                           _stream(stream)), "rmn_batch_autotune")
     return {k: getattr(res, k) for k, _ in res._fields_}
 
 
+def batch_device_bytes(items, pool_workers: int = 0, lanes: int = 0) -> int:
+    """rmn_batch_device_bytes: device bytes a Batch of these (Model,
+    RenderArgs, Photo) items would take with these options (unit records and
+    worker pool; scenes and images excluded)."""
+    out = C.c_int64()
+    opt = _lib.BatchOptions(1, int(pool_workers), int(lanes), 0)
+    _check(_lib.load().rmn_batch_device_bytes(_batch_items(items), len(items), C.byref(opt), C.byref(out)),
+           "rmn_batch_device_bytes")
+    return int(out.value)
+
+
 class Batch:
     """rmn_batch: many renders in one persistent launch, optionally replayed
     from a captured CUDA graph. Photos must live on the device."""
 
-    def __init__(self, items, use_graph: bool = True, stream=None, pool_workers: int = 0, lanes: int = 0):
-        """items: list of (Model, RenderArgs, Photo); pool_workers per lane."""
+    def __init__(self, items, use_graph: bool = True, stream=None, pool_workers: int = 0, lanes: int = 0,
+                 stack_entries: int = 0):
+        """items: list of (Model, RenderArgs, Photo); pool_workers per lane;
+        stack_entries 0 (library default), 23 or 27."""
         lib = _lib.load()
         arr = _batch_items(items)
         h = C.c_void_p()
-        opt = _lib.BatchOptions(1 if use_graph else 0, int(pool_workers), int(lanes), 0)
+        opt = _lib.BatchOptions(1 if use_graph else 0, int(pool_workers), int(lanes), int(stack_entries))
         _check(lib.rmn_batch_create(arr, len(items), C.byref(opt), _stream(stream), C.byref(h)), "rmn_batch_create")
         self._h = h
         self.items = items

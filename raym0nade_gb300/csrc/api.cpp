@@ -267,6 +267,7 @@ rmn_status rmn_scene_destroy(rmn_scene* scene) {
 rmn_status rmn_release_cached_memory(void) {
   clear_error();
   release_cached_memory();
+  noalloc_forget_addresses();
   return RMN_OK;
 }
 
@@ -461,6 +462,13 @@ rmn_status rmn_export_set(const rmn_image* image, const rmn_post_args* args, flo
   return r;
 }
 
+rmn_status rmn_reverse_gamma(const float* in, int64_t n, float* out) {
+  clear_error();
+  if (!in || !out || n < 0) return fail(RMN_ERR_INVALID_ARGUMENT, "rmn_reverse_gamma needs host arrays and n >= 0");
+  for (int64_t i = 0; i < 3 * n; ++i) out[i] = powf(in[i], 2.2f);
+  return RMN_OK;
+}
+
 rmn_status rmn_save_png(const float* rgb, int32_t width, int32_t height, const char* path) {
   clear_error();
   if (!rgb || !path || width <= 0 || height <= 0 || (int64_t)width * height > (1LL << 30))
@@ -571,7 +579,7 @@ static rmn_status render_one(rmn_scene* scene, const rmn_render_args* args, cons
   if (r == RMN_OK) {
     RenderItem it{scene, a, static_cast<float*>(gb.dev), static_cast<float*>(dd.dev), static_cast<float*>(ds.dev),
                   static_cast<float*>(id.dev), static_cast<float*>(is.dev), static_cast<int*>(dr.dev)};
-    r = batch_create(&it, 1, false, 0, 0, st, &b);
+    r = batch_create(&it, 1, false, 0, 0, 0, st, &b);
   }
   if (r == RMN_OK) r = prof ? batch_profile(b, st, prof) : batch_launch(b, st);
   if (r == RMN_OK) r = finish_out(image->radiance_Dd, npx * 16, st, dd);
@@ -665,13 +673,15 @@ rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_ba
   rmn_batch_options opt = options ? *options : rmn_batch_options{1, 0, 0, 0};
   if (opt.pool_workers < 0) return fail(RMN_ERR_INVALID_ARGUMENT, "pool_workers must be >= 0");
   if (opt.lanes < 0 || opt.lanes > 4) return fail(RMN_ERR_INVALID_ARGUMENT, "lanes must lie in [0, 4]");
+  if (opt.stack_entries != 0 && opt.stack_entries != RMN_STACK_SMALL && opt.stack_entries != RMN_STACK)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "stack_entries must be 0, %d or %d", RMN_STACK_SMALL, RMN_STACK);
   std::vector<RenderItem> its;
   rmn_status r = make_items(items, n, its, true);
   if (r != RMN_OK) return r;
   rmn_batch* bt = new (std::nothrow) rmn_batch();
   if (!bt) return fail(RMN_ERR_OUT_OF_MEMORY, "host allocation failed");
-  r = batch_create(its.data(), n, opt.use_graph != 0, opt.pool_workers, opt.lanes, static_cast<cudaStream_t>(stream),
-                   &bt->state);
+  r = batch_create(its.data(), n, opt.use_graph != 0, opt.pool_workers, opt.lanes, opt.stack_entries,
+                   static_cast<cudaStream_t>(stream), &bt->state);
   if (r != RMN_OK) {
     delete bt;
     return r;
@@ -705,6 +715,20 @@ static rmn_status make_items(const rmn_batch_item* items, int32_t n, std::vector
   return RMN_OK;
 }
 
+rmn_status rmn_batch_device_bytes(const rmn_batch_item* items, int32_t n, const rmn_batch_options* options,
+                                  int64_t* out) {
+  clear_error();
+  if (!items || n <= 0 || !out) return fail(RMN_ERR_INVALID_ARGUMENT, "a batch needs at least one item and an output");
+  const rmn_batch_options opt = options ? *options : rmn_batch_options{1, 0, 0, 0};
+  if (opt.pool_workers < 0 || opt.lanes < 0 || opt.lanes > 4)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "pool_workers must be >= 0 and lanes lie in [0, 4]");
+  std::vector<RenderItem> its;
+  rmn_status r = make_items(items, n, its, false);
+  if (r != RMN_OK) return r;
+  *out = (int64_t)batch_device_bytes(its.data(), n, opt.pool_workers, opt.lanes);
+  return RMN_OK;
+}
+
 rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixel_fraction, rmn_tune_result* out,
                               void* stream) {
   clear_error();
@@ -728,6 +752,11 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
     for (RenderItem& it : f) it.args.slots_per_unit = slots;
     return batch_device_bytes(f.data(), n, pool, lanes) <= free_b / 2;
   };
+  // the batch cannot be built at all when its default unit records and the
+  // smallest pool exceed what is free
+  if (batch_device_bytes(full.data(), n, 4096, 1) > free_b)
+    return fail(RMN_ERR_OUT_OF_MEMORY, "autotune: no configuration of this batch fits in the %zu free device bytes",
+                free_b);
   // Proxy renders: the same scenes, spp, depth and field of view at a
   // fraction of the pixels, into buffers owned by the tuner.
   const float scale = std::sqrt(pixel_fraction);
@@ -760,19 +789,34 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
   const int slots[] = {2, 4, 8, 16};
   const int pools[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
   const int lanes[] = {2, 3, 4};
-  // candidate 0: the library's own choice (the items' slots_per_unit, pool
-  // and lanes left at 0); then the grid
-  rmn_tune_result best{0, 0, 1e30, 0.0, 0, 0};
+  // candidate 0: the library's own choice (the items' slots_per_unit, pool,
+  // lanes and stack left at 0); then the grid at the default stack; last, the
+  // fastest so far with the deeper stack build, where the default is the
+  // shallow one (the stack must hold every tree, so only larger stacks are
+  // admissible; they cost shared memory and so persistent blocks per SM)
+  const int stack_def = default_stack_entries(its.data(), n);
+  rmn_tune_result best{0, 0, 1e30, 0.0, 0, 0, stack_def, 0};
   std::vector<int> proxy_slots(its.size());
   for (size_t i = 0; i < its.size(); ++i) proxy_slots[i] = its[i].args.slots_per_unit;
-  for (int ci = -1; ci < 4 * 4 * 3 && r == RMN_OK; ++ci) {
-    const int si = ci < 0 ? 0 : ci / 12, pi = ci < 0 ? 0 : (ci / 3) % 4, li = ci < 0 ? 0 : ci % 3;
-    const bool is_default = ci < 0;
-    const int cs = is_default ? 0 : slots[si], cp = is_default ? 0 : pools[pi], cl = is_default ? 0 : lanes[li];
-    if (!is_default && !fits(cs, cp, cl)) continue;
-    for (size_t i = 0; i < its.size(); ++i) its[i].args.slots_per_unit = is_default ? proxy_slots[i] : cs;
+  const int grid = 4 * 4 * 3;
+  for (int ci = -1; ci <= grid && r == RMN_OK; ++ci) {
+    const bool is_default = ci < 0, stack_pass = ci == grid;
+    if (stack_pass && stack_def == RMN_STACK) break;
+    const int si = ci < 0 || stack_pass ? 0 : ci / 12, pi = ci < 0 || stack_pass ? 0 : (ci / 3) % 4,
+              li = ci < 0 || stack_pass ? 0 : ci % 3;
+    int cs = is_default ? 0 : slots[si], cp = is_default ? 0 : pools[pi], cl = is_default ? 0 : lanes[li];
+    int ck = stack_def;
+    if (stack_pass) {
+      cs = best.slots_per_unit;
+      cp = best.pool_workers;
+      cl = best.lanes;
+      ck = RMN_STACK;
+    } else if (!is_default && !fits(cs, cp, cl)) {
+      continue;
+    }
+    for (size_t i = 0; i < its.size(); ++i) its[i].args.slots_per_unit = cs == 0 ? proxy_slots[i] : cs;
     BatchState* b = nullptr;
-    r = batch_create(its.data(), n, true, cp, cl, st, &b);
+    r = batch_create(its.data(), n, true, cp, cl, ck, st, &b);
     if (r != RMN_OK) break;
     r = batch_launch(b, st);  // warm-up
     if (r == RMN_OK) {
@@ -792,6 +836,7 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
       best.slots_per_unit = cs;
       best.pool_workers = cp;
       best.lanes = cl;
+      best.stack_entries = ck;
     }
   }
   if (e0) cudaEventDestroy(e0);

@@ -15,8 +15,12 @@
 // the host it names a host-side stand-in). The first call on each device
 // resolves the array's device address with cudaGetSymbolAddress, with that
 // device current, and caches it; make that first call before any stream
-// capture. All calls share the one array, so calls whose work overlaps on
-// the GPU (different streams, or different host threads) race on it.
+// capture. A device reset (cudaDeviceReset) invalidates that address with the
+// rest of the device's state: rmn_release_cached_memory, called after the
+// reset, makes the next call resolve it again. All calls share the one
+// array, so calls whose work overlaps on the GPU (different streams, or
+// different host threads) race on it. A call returns once its work on
+// `stream` has finished (it synchronises the stream).
 #include <mutex>
 
 #include "rmn_host.h"
@@ -47,6 +51,13 @@ rmn_status scratch_for_current_device(float** out) {
 }
 
 }  // namespace
+
+namespace rmn {
+void noalloc_forget_addresses() {
+  std::lock_guard<std::mutex> lock(g_mu);
+  for (float*& p : g_scratch) p = nullptr;
+}
+}  // namespace rmn
 
 extern "C" rmn_status rmn_compose_noalloc(const rmn_image* image, int32_t width, int32_t height, float exposure,
                                           int32_t options, float* rgb, void* stream) {

@@ -1055,7 +1055,7 @@ struct BatchState {
   int lanes = 1;
   bool alpha = false;         // some job's scene has alpha-tested materials
   bool tex = false;           // some job's scene has textures
-  bool shallow = true;        // every job's tree fits the small traversal stack
+  bool shallow = true;        // the traversal runs its RMN_STACK_SMALL-entry build
   Pool pool[kMaxLanes] = {};  // each lane's share of the worker arrays
   Queues q[kMaxLanes] = {};
   std::vector<void*> allocs;
@@ -1318,41 +1318,55 @@ static size_t free_device_bytes() {
   return f;
 }
 
+// Unit records one item may take under the library's default split.
+constexpr long long kItemPartBytes = 1LL << 34;  // 16 GiB
+
 // The library's unit split for the items that leave it open
 // (slots_per_unit = lanes_per_pixel = 0; others get 0 in S): 2 slots per
-// unit for an item of up to 2^26 sample slots, 4 above -- a choice of the
-// item alone, so its images do not depend on the batch around it -- all
-// doubled while the unit partials (112 B each) of those items would take
-// more than a quarter of the free device memory. Short units drain the
-// wavefront evenly; the partials are the price.
+// unit for an item of up to 2^26 sample slots, 4 above, doubled while that
+// item's own unit records (112 B each) would exceed kItemPartBytes. The
+// choice depends on the item alone -- not on the batch around it, nor on the
+// device memory free at the call -- so an item's images, whose float sums
+// run over its units in unit order, are the same wherever it is rendered.
+// Short units drain the wavefront evenly; the records are the price. A
+// batch whose records do not fit fails with RMN_ERR_OUT_OF_MEMORY rather
+// than changing the split.
 void default_slots_per_unit(const RenderItem* items, int n, int* S) {
-  std::vector<long long> slots(n, 0);
   for (int i = 0; i < n; ++i) {
     S[i] = 0;
     if (items[i].args.slots_per_unit != 0 || items[i].args.lanes_per_pixel != 0) continue;
     rmn_render_args a = items[i].args;
+    const bool glass = items[i].scene->dev.has_glass != 0;
     a.slots_per_unit = 1;
-    const Params p = make_params(a, items[i].scene->dev.has_glass != 0);
-    slots[i] = (long long)p.W * p.H * p.K;
-    S[i] = slots[i] <= (1LL << 26) ? 2 : 4;
-  }
-  const size_t budget = free_device_bytes() / 4;
-  for (int f = 1; f < (1 << 18); f *= 2) {
-    size_t bytes = 0;
-    for (int i = 0; i < n; ++i)
-      if (S[i]) bytes += (size_t)(slots[i] / ((long long)S[i] * f) + 1) * sizeof(float4) * RMN_PART_F4;
-    if (bytes <= budget) {
-      for (int i = 0; i < n; ++i) S[i] *= f;
-      return;
+    const Params p1 = make_params(a, glass);
+    int s = (long long)p1.W * p1.H * p1.K <= (1LL << 26) ? 2 : 4;
+    for (;; s *= 2) {
+      a.slots_per_unit = s;
+      const Params p = make_params(a, glass);
+      if (s >= (1 << 20) ||
+          (long long)p.W * p.H * p.K * (long long)(sizeof(float4) * RMN_PART_F4) <= kItemPartBytes)
+        break;
     }
+    S[i] = s;
   }
+}
+
+int default_stack_entries(const RenderItem* items, int n) {
   for (int i = 0; i < n; ++i)
-    if (S[i]) S[i] = 1 << 20;
+    if (items[i].scene->dev.depth + 1 > RMN_STACK_SMALL) return RMN_STACK;
+  return RMN_STACK_SMALL;
 }
 
 rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int pool_workers, int lanes,
-                        cudaStream_t st, BatchState** out) {
+                        int stack_entries, cudaStream_t st, BatchState** out) {
   *out = nullptr;
+  // the traversal stack must hold every item's deepest path of deferred
+  // children; a larger one only costs occupancy
+  const int stack_min = default_stack_entries(items_in, n);
+  if (stack_entries == 0) stack_entries = stack_min;
+  if (stack_entries < stack_min)
+    return fail(RMN_ERR_INVALID_ARGUMENT, "a traversal stack of %d entries is too small for a tree of this batch",
+                stack_entries);
   // items that leave the unit split to the library take its default
   std::vector<RenderItem> items_v(items_in, items_in + n);
   std::vector<int> S_def(n, 0);
@@ -1421,8 +1435,8 @@ rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int p
   for (const Job& j : b->table.jobs) {
     b->tex = b->tex || j.s.has_tex;
     b->alpha = b->alpha || j.s.has_alpha;
-    b->shallow = b->shallow && j.s.depth + 1 <= RMN_STACK_SMALL;
   }
+  b->shallow = stack_entries == RMN_STACK_SMALL;
   const bool tex = b->tex;
   if (tex) alloc((void**)&P.rdiff, sizeof(float4) * 3 * W);
   for (int l = 0; l < b->lanes; ++l) {
@@ -1532,9 +1546,15 @@ size_t batch_job_bytes() { return sizeof(Job); }
 // Device bytes batch_create would take for these items: the unit partials,
 // and per worker its state, shadow-ray slots and queue entries (media and
 // ray differentials where a scene needs them).
-size_t batch_device_bytes(const RenderItem* items, int n, int pool_workers, int lanes) {
+size_t batch_device_bytes(const RenderItem* items_in, int n, int pool_workers, int lanes) {
+  // items that leave the unit split open take the library's default
+  std::vector<RenderItem> items(items_in, items_in + n);
+  std::vector<int> S(n, 0);
+  default_slots_per_unit(items_in, n, S.data());
+  for (int i = 0; i < n; ++i)
+    if (S[i]) items[i].args.slots_per_unit = S[i];
   JobTable t;
-  build_jobs(items, n, &t);
+  build_jobs(items.data(), n, &t);
   bool glass = false, tex = false;
   for (const Job& j : t.jobs) {
     glass = glass || j.p.glass;

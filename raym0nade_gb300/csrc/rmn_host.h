@@ -80,9 +80,17 @@ uint32_t png_crc32(uint32_t crc, const uint8_t* p, size_t n);
 cudaError_t cached_malloc(void** p, size_t bytes);
 void cached_free(void* p);
 void release_cached_memory();
+// Forgets the device addresses rmn_compose_noalloc resolved (after a device
+// reset they name nothing); the next call on each device resolves them anew.
+void noalloc_forget_addresses();
 
+// stack_entries: the traversal kernels' deferred-child stack, RMN_STACK_SMALL
+// or RMN_STACK entries (0: the smallest that holds every item's tree).
 rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, int lanes,
-                        cudaStream_t st, BatchState** out);
+                        int stack_entries, cudaStream_t st, BatchState** out);
+// The traversal stack the library picks for these items (RMN_STACK_SMALL when
+// every tree is at most RMN_STACK_SMALL - 1 deep, else RMN_STACK).
+int default_stack_entries(const RenderItem* items, int n);
 rmn_status batch_launch(BatchState* b, cudaStream_t st);
 rmn_status batch_update(BatchState* b, const rmn_render_args* args, int n, cudaStream_t st);
 size_t batch_job_bytes();

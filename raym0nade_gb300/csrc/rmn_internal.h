@@ -66,6 +66,9 @@ RMN_HD float3 mix3(float3 x, float3 y, float a) { return x * (1.0f - a) + y * a;
 // triangles stay below 26 levels); 27 x 8 B x 128 threads of shared memory
 // lets 8 persistent traversal blocks share an SM
 #define RMN_STACK 27
+// A shallower stack for batches whose trees are at most RMN_STACK_SMALL - 1
+// deep: less shared memory, one more persistent traversal block per SM.
+#define RMN_STACK_SMALL 23
 
 // ------------------------------------------------------------ layout ------
 // Two-child node (64 B): the boxes of both children plus their references,

@@ -103,10 +103,6 @@ struct SharedStackN {
   RMN_D int2 get(int i) const { return base[i * 128]; }
 };
 using SharedStack = SharedStackN<RMN_STACK>;
-// A shallower shared stack for batches whose trees are at most
-// RMN_STACK_SMALL - 1 deep: less shared memory, one more persistent block
-// per SM.
-#define RMN_STACK_SMALL 23
 
 template <class Stack>
 struct TravT {

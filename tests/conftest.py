@@ -6,6 +6,9 @@ import pytest
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
+# where the reference checkout lies on the machine that builds the oracle
+# from it (absent elsewhere: the tests then use tests/golden)
+os.environ.setdefault("RMN_REFERENCE_DIR", "/root/reference")
 
 
 def pytest_configure(config):

@@ -38,10 +38,15 @@ Fixtures (numpy .npz, compressed):
                      the written samples through libpng's transforms, RGBE
                      m * 2^(e - 136), BC blocks through oracle/image_codecs.py.
                      Needs no reference; ``--images`` writes them alone.
-  cornell_4096spp.npz  the converged reference image of the Cornell workload
-                     (256 x 256, 4096 spp, max depth 16, P_Direct 0.7):
-                     Photo::shade(Full) before gamma, float16. Made by
-                     ``python tests/golden/make_golden.py --converged``.
+  converged_<case>.npz  converged reference images for the image-parity
+                     tests: Photo::shade(Full) before gamma (float16) of two
+                     independent 4096-spp renders (per-pixel seeds 4096 and
+                     8192) of each case of CONVERGED_CASES -- the Cornell
+                     workload (256 x 256, depth 16, P_Direct 0.7), a
+                     heightfield under the synthetic sun in sky mode
+                     (192 x 108) and the glass Cornell box (128 x 128).
+                     Made by ``python tests/golden/make_golden.py
+                     --converged [case ...]``.
 """
 import os
 import sys
@@ -51,6 +56,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, ROOT)
+os.environ.setdefault("RMN_REFERENCE_DIR", "/root/reference")  # the reference checkout these fixtures come from
 
 from oracle import bindings  # noqa: E402
 from raym0nade_gb300 import scenes  # noqa: E402
@@ -342,21 +348,58 @@ def mips():
     np.savez_compressed(os.path.join(HERE, "mips.npz"), **out)
 
 
-def converged():
+CONVERGED_CASES = ("cornell", "sky", "glass")
+CONVERGED_SEEDS = (4096, 8192)
+
+
+def converged_case(name):
+    """Scene and camera of a converged-image case (4096 spp).
+
+    cornell: the Cornell workload, 256 x 256, depth 16.
+    sky:     a 256 x 256-vertex heightfield with 0.1-wide cells (smooth
+             normals, the 50/50 Lambertian / GGX-conductor patches) under
+             the 2048 x 1024 synthetic sky with its 0.5-degree sun of
+             radiance 5e4 -- sky-mode light sampling -- seen from the
+             heightfield workload's camera at 192 x 108.
+    glass:   the Cornell box with the glass tall box and the half-opaque
+             short box, 128 x 128 (16x the indirect paths behind glass)."""
+    if name == "cornell":
+        return scenes.cornell(), scenes.cornell_camera(256, 256, 4096)
+    if name == "sky":
+        ext = 25.6
+        hf = scenes.heightfield(256, seed=3, extent=ext, patch=16)
+        hf.env = scenes.sky_env(2048, 1024)
+        return hf, scenes.heightfield_camera(192, 108, 4096, extent=ext)
+    if name == "glass":
+        return scenes.cornell_glass(), scenes.cornell_camera(128, 128, 4096)
+    raise ValueError(name)
+
+
+def converged(names=CONVERGED_CASES):
+    """Two independent 4096-spp renders of each case by the reference's own
+    renderer (per-pixel mt19937 seeds differ between the two), on all host
+    threads; the linear composite of each is stored as float16."""
+    import time
     bindings.build(with_reference=True)
     R = bindings.OracleLib("ref")
-    cor = scenes.cornell()
-    cam = scenes.cornell_camera(256, 256, 4096)
-    rec = R.scene(cor).render(cam, seed=4096, threads=os.cpu_count() or 8)
-    lin = R.compose(rec, 1.0, gamma=False)
-    np.savez_compressed(os.path.join(HERE, "cornell_4096spp.npz"), linear=lin.astype(np.float16),
-                        args=cam.packed(), seed=4096, mean=np.float64(lin.astype(np.float64).mean()))
-    print("converged Cornell reference written")
+    for name in names:
+        sc, cam = converged_case(name)
+        rs = R.scene(sc)
+        out = dict(args=cam.packed(), seeds=np.asarray(CONVERGED_SEEDS, np.int64))
+        for tag, seed in zip("ab", CONVERGED_SEEDS):
+            t0 = time.time()
+            rec = rs.render(cam, seed=seed, threads=os.cpu_count() or 8)
+            lin = R.compose(rec, 1.0, gamma=False)
+            assert np.isfinite(lin).all() and np.abs(lin).max() < 6e4, name
+            out["linear_" + tag] = lin.astype(np.float16)
+            print(f"{name} seed {seed}: {time.time() - t0:.1f} s", flush=True)
+        np.savez_compressed(os.path.join(HERE, f"converged_{name}.npz"), **out)
+    print("converged references written")
 
 
 if __name__ == "__main__":
     if "--converged" in sys.argv:
-        converged()
+        converged([a for a in sys.argv[1:] if not a.startswith("--")] or CONVERGED_CASES)
     elif "--glass" in sys.argv:
         glass()
         print("glass fixture written to", HERE)

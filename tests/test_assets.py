@@ -608,4 +608,4 @@ def test_photo_load_and_reverse_gamma(tmp_path):
     g = api.Photo.load(q)
     assert np.array_equal(g[..., 0], (s[..., 0] >> 8).astype(np.float32) / np.float32(255))
     r = api.Photo.reverseGammaCorrection(got)
-    assert np.array_equal(r, np.power(got, np.float32(2.2)))
+    np.testing.assert_allclose(r, np.power(got, np.float32(2.2)), rtol=3e-7, atol=0)

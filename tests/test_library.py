@@ -119,24 +119,11 @@ int main(int argc, char **argv) {
     assert "could not read" in out[1]
 
 
-def _cpp_blocks(md):
-    blocks, cur = [], None
-    for line in open(md).read().splitlines():
-        if line.startswith("```cpp"):
-            cur = []
-        elif line.startswith("```") and cur is not None:
-            blocks.append("\n".join(cur))
-            cur = None
-        elif cur is not None:
-            cur.append(line)
-    return blocks
-
-
 def test_integration_binding_compiles_against_reference_headers(tmp_path):
-    """The reference-side C++ of INTEGRATION.md (the render_multiThread
-    replacement, the image loaders, the model creation) compiles against the
-    reference's own headers (with the oracle's glm / assimp / libpng
-    stand-ins) and include/rmn.h."""
+    """The reference-side C++ binding (tests/golden/reference_binding.cpp:
+    the render_multiThread replacement, the image loaders, the model
+    creation) compiles against the reference's own headers (with the
+    oracle's glm / assimp / libpng stand-ins) and include/rmn.h."""
     import shutil
     import subprocess
     from oracle import bindings
@@ -146,16 +133,7 @@ def test_integration_binding_compiles_against_reference_headers(tmp_path):
     cxx = shutil.which("g++")
     if cxx is None:
         pytest.skip("no C++ compiler")
-    blocks = _cpp_blocks(os.path.join(ROOT, "INTEGRATION.md"))
-    render, loaders, console = blocks[0], blocks[1], blocks[2]
-    # what src/render.cpp, src/material.cpp and src/component.cpp include
-    head = "\n".join(['#include <mutex>', '#include <thread>', '#include <iostream>', '#include <stdexcept>',
-                      '#include "render.h"', '#include "geometry.h"', '#include "image.h"', '#include "sampling.h"',
-                      '#include "material.h"', '#include "component.h"'])
-    src = tmp_path / "binding.cpp"
-    src.write_text(head + "\n" + render + "\n" + loaders + "\n"
-                   + "void create_model(const std::string &folder, const std::string &name, "
-                   + "const std::string &sky) {\n" + console + "\n}\n")
+    src = os.path.join(ROOT, "tests", "golden", "reference_binding.cpp")
     import sysconfig
     cmd = [cxx, "-std=c++17", "-fsyntax-only", "-w", "-I", os.path.join(ROOT, "oracle", "shim"), "-I", ref_inc,
            "-I", sysconfig.get_paths()["include"], "-I", os.path.join(ROOT, "include"), str(src)]

@@ -127,6 +127,19 @@ def test_render_cornell_matches_reference(port, ref, spp, p_direct):
     assert same(a[..., :38], b[..., :38])
 
 
+def test_render_pixels_match_whole_renders(port, ref):
+    """The pixel-list render (the benchmark's stratified CPU sample) gives each
+    listed pixel exactly its record of a whole-image render."""
+    c = scenes.cornell()
+    cam = scenes.cornell_camera(20, 16, 6)
+    rng = np.random.default_rng(3)
+    px = rng.choice(20 * 16, 50, replace=False).astype(np.int32)
+    for lib in (port, ref):
+        whole = lib.scene(c).render(cam, seed=12).reshape(-1, 40)
+        part = lib.scene(c).render_pixels(cam, 12, px)
+        assert np.array_equal(part, whole[px], equal_nan=True)
+
+
 @pytest.mark.parametrize("spp,p_direct", [(8, 0.7), (4, 0.0)])
 def test_render_glass_matches_reference(port, ref, spp, p_direct):
     """Transmissive and semi-opaque materials: refraction, media, Fresnel
@@ -339,3 +352,14 @@ def test_script_mirrors_feed_the_references_loaders(ref_tex, tmp_path, monkeypat
     np.testing.assert_allclose(got, raw * area[:, None, None], rtol=2e-6, atol=0)
     tex = dds_load(str(tmp_path / "t.dds"))
     assert np.array_equal(tex, assets.load_image(str(tmp_path / "t.dds"), assets.DDS))
+
+
+def test_reverse_gamma_matches_reference(ref):
+    """Photo.reverseGammaCorrection of the mirror against the reference's
+    Photo::reverseGammaCorrection (glm::pow of floats), bit for bit, on every
+    k / 255 a loaded PNG yields and on random values."""
+    from raym0nade_gb300 import api
+    rng = np.random.default_rng(6)
+    k255 = (np.arange(256, dtype=np.float32) / np.float32(255.0))
+    x = np.concatenate([np.repeat(k255, 3), rng.random(3 * 4000, dtype=np.float32)]).reshape(-1, 3)
+    assert np.array_equal(api.Photo.reverseGammaCorrection(x), ref.reverse_gamma(x))

@@ -5,10 +5,14 @@ let cudaMalloc/cudaFree synchronise the device). Its intermediate image lives
 in a fixed device array of RMN_NOALLOC_MAX_PIXELS pixels.
 
 Checked through the C ABI against rmn_compose, the allocating entry point,
-on two calls in a row (the shared array keeps the previous call's contents).
-This file is collected last on purpose.
+on two calls in a row (the shared array keeps the previous call's contents),
+and checked to allocate nothing: after a first call (which loads the array's
+module), further calls leave the device's free memory and the stream-ordered
+allocator's default pool unchanged. This file is collected last on purpose.
 """
 import ctypes
+import glob
+import os
 
 import numpy as np
 import pytest
@@ -45,6 +49,66 @@ def test_compose_noalloc_matches_compose(w, h, opts):
         st = lib.rmn_compose_noalloc(ctypes.byref(img), w, h, 1.0, opts, ctypes.c_void_p(out.data_ptr()), None)
         assert st == 0, lib.rmn_last_error()
         np.testing.assert_allclose(out.cpu().numpy(), ref, rtol=2e-6, atol=1e-7)
+
+
+def _cudart():
+    """The CUDA runtime torch loaded (for the default memory pool's counters),
+    or None."""
+    import torch.cuda
+    names = ["libcudart.so.13", "libcudart.so.12", "libcudart.so"]
+    here = os.path.dirname(torch.__file__)
+    names += glob.glob(os.path.join(here, "..", "nvidia", "cu*", "lib", "libcudart.so*"))
+    names += glob.glob(os.path.join(here, "..", "nvidia", "cuda_runtime", "lib", "libcudart.so*"))
+    for n in names:
+        try:
+            return ctypes.CDLL(n)
+        except OSError:
+            continue
+    return None
+
+
+def _pool_counters(rt):
+    """(reserved, used) bytes of the current device's default memory pool."""
+    if rt is None:
+        return None
+    dev = ctypes.c_int()
+    pool = ctypes.c_void_p()
+    if rt.cudaGetDevice(ctypes.byref(dev)) or rt.cudaDeviceGetDefaultMemPool(ctypes.byref(pool), dev):
+        return None
+    out = []
+    for attr in (5, 7):  # cudaMemPoolAttrReservedMemCurrent, cudaMemPoolAttrUsedMemCurrent
+        v = ctypes.c_uint64()
+        if rt.cudaMemPoolGetAttribute(pool, attr, ctypes.byref(v)):
+            return None
+        out.append(v.value)
+    return tuple(out)
+
+
+def test_compose_noalloc_allocates_nothing():
+    """1920 x 1080 with FXAA (near the 2^21-pixel limit): once the first call
+    has run, two more calls change neither the device's free memory nor the
+    default memory pool's reserved and used bytes."""
+    lib = _lib.load()
+    w, h = 1920, 1080
+    opts = api.Full | api.GAMMA | api.DoFXAA
+    ph = _photo(w, h, 11)
+    out = torch.empty((h, w, 3), device="cuda")
+    img = ph.c_image()
+    call = lambda: lib.rmn_compose_noalloc(ctypes.byref(img), w, h, 1.0, opts, ctypes.c_void_p(out.data_ptr()), None)
+    assert call() == 0, lib.rmn_last_error()
+    torch.cuda.synchronize()
+    rt = _cudart()
+    free0, pool0 = torch.cuda.mem_get_info()[0], _pool_counters(rt)
+    for _ in range(2):
+        assert call() == 0, lib.rmn_last_error()
+    torch.cuda.synchronize()
+    free1, pool1 = torch.cuda.mem_get_info()[0], _pool_counters(rt)
+    assert free1 == free0
+    assert pool1 == pool0
+    # after rmn_release_cached_memory the address is resolved again
+    assert lib.rmn_release_cached_memory() == 0
+    assert call() == 0, lib.rmn_last_error()
+    np.testing.assert_allclose(out.cpu().numpy(), ph.shade(opts).cpu().numpy(), rtol=2e-6, atol=1e-7)
 
 
 def test_compose_noalloc_limits():
