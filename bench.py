@@ -46,10 +46,16 @@ sys.path.insert(0, ROOT)
 METRIC = "Mpaths/s at rel-MSE≤1e-3 (batched vs per-scene launch); adjoint/forward time"
 UNIT = "Mpaths/s"
 FALLBACK_HBM_GBS = 6800.0
-# DRAM bytes (read + write) of all traversal launches of one batch64 render,
-# summed from an ncu capture of `python -m raym0nade_gb300.profile_case batch`
-# (profiles/launches_batch64.md); ncu cannot run inside the timed region.
-BATCH64_TRAVERSAL_DRAM_BYTES = 136.05e9 + 14.83e9
+# DRAM and L2 bytes (read + write) of the traversal launches (closest and
+# shadow queues) of one batch64 render at the launch configuration given
+# beside them, summed from an ncu capture (metrics dram__bytes_read.sum,
+# dram__bytes_write.sum, lts__t_bytes.sum) of
+#   python bench.py --profile-case batch --slots 2 --pool 8388608 --lanes 3
+# (ncu cannot run inside the timed region). The line reports whether the
+# timed configuration is this one.
+BATCH64_TRAVERSAL_BYTES = {
+    "config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 3, "stack_entries": 23, "ray_order": 0},
+    "dram": 216.8e9, "l2": 2449.1e9}
 
 
 def measured_peaks():
@@ -59,6 +65,26 @@ def measured_peaks():
         return float(d["hbm_gbs"]), "measured"
     except Exception:
         return FALLBACK_HBM_GBS, "fallback"
+
+
+def l2_copy_gbs(stream):
+    """Bytes moved per second (read + write) by a device copy of a 24 MiB
+    buffer into another, both resident in the 129 MB L2, repeated: a
+    reference figure for L2 bandwidth on this GPU (measured here; there is
+    no published number)."""
+    import torch
+    a = torch.empty(24 << 20, dtype=torch.uint8, device="cuda")
+    b = torch.empty_like(a)
+    with torch.cuda.stream(stream):
+        for _ in range(20):
+            b.copy_(a)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(200):
+            b.copy_(a)
+        e1.record(stream)
+    e1.synchronize()
+    return 2.0 * a.numel() * 200 / (e0.elapsed_time(e1) / 1e3) / 1e9
 
 
 def instance_paths(inst):
@@ -586,7 +612,8 @@ def run_gpu(args, rank, world, dist):
     with torch.cuda.stream(stream):
         batch = api.Batch(list(zip(models, argsl, photos)), use_graph=True, stream=stream,
                           pool_workers=tune["pool_workers"] if tune else 0, lanes=tune["lanes"] if tune else 0,
-                          stack_entries=tune["stack_entries"] if tune else 0)
+                          stack_entries=tune["stack_entries"] if tune else 0,
+                          ray_order=tune["ray_order"] if tune else 0)
 
     def step_batched():
         batch.render(stream)
@@ -674,6 +701,27 @@ def run_gpu(args, rank, world, dist):
     logic_share = prof["logic_ms"] / max(1e-9, total_ms)
     trace_ms_live = ms_b * trace_share
     achieved = alg_bytes / (trace_ms_live / 1e3) / 1e9
+    # measured traffic of the traversal launches, where a capture of this
+    # workload at this launch configuration exists
+    traffic, traffic_src, l2 = None, None, None
+    if args.workload == "batch64":
+        cfg = BATCH64_TRAVERSAL_BYTES["config"]
+        timed = {"slots_per_unit": tune["slots_per_unit"] if tune else 0,
+                 "pool_workers": tune["pool_workers"] if tune else 0, "lanes": tune["lanes"] if tune else 0,
+                 "stack_entries": tune["stack_entries"] if tune else 0, "ray_order": tune["ray_order"] if tune else 0}
+        same = timed == cfg
+        traffic = BATCH64_TRAVERSAL_BYTES["dram"]
+        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum over every qtrace_kernel launch of one "
+                       "batch64 render at " + json.dumps(cfg) + ("" if same else "; NOT the timed configuration"))
+        l2_peak = l2_copy_gbs(stream)
+        l2_gbs = BATCH64_TRAVERSAL_BYTES["l2"] / (trace_ms_live / 1e3) / 1e9
+        l2 = {"bytes_per_step": BATCH64_TRAVERSAL_BYTES["l2"], "achieved": l2_gbs, "unit": "GB/s",
+              "copy_rate": l2_peak, "frac_of_copy_rate": l2_gbs / l2_peak, "same_config": same,
+              "source": "ncu lts__t_bytes.sum over the same launches; copy_rate: a device copy between two "
+                        "L2-resident 24 MiB buffers, measured here"}
+    limiter = ("dependent-fetch latency and SIMT divergence: measured DRAM traffic is a small share of the "
+               "algorithmic bytes (L1/L2 hits) and neither DRAM nor L2 runs near its rate (ncu: long-scoreboard "
+               "stalls dominate the traversal's issue slots)")
     base, _ = cpu_baseline(insts) if args.cpu_baseline else (None, None)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -690,17 +738,17 @@ def run_gpu(args, rank, world, dist):
                 "call": "rmn_batch_update (cameras and seeds from pinned host memory) + rmn_batch_render + "
                         "rmn_compose(Full|gamma|FXAA) of every instance into pinned host memory; wall clock"},
         # per batched step: G-buffer kernel, one seed kernel per lane, 5 kernels
-        # per wavefront iteration and lane, finalize
-        "gpu_launches": args.steps * (2 + lanes + 5 * lanes * prof["iterations"]),
+        # per wavefront iteration and lane (11 with binned ray queues), finalize
+        "gpu_launches": args.steps * (2 + lanes + (11 if tune and tune["ray_order"] else 5) * lanes *
+                                      prof["iterations"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                     "traffic": BATCH64_TRAVERSAL_DRAM_BYTES if args.workload == "batch64" else None,
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum over every qtrace_kernel "
-                                       "launch of one batch64 render (profiles/launches_batch64.md)",
+                     "traffic": traffic, "traffic_source": traffic_src,
                      "per": "step (all traversal launches of one step)",
                      "kernel": "qtrace_kernel (closest + shadow queues)", "peak_source": peak_src,
                      "bytes_model": "64 B per inner-node visit + 36 B per triangle test + 40 B per queued ray",
                      "algorithmic_bytes_per_step": alg_bytes, "trace_share": trace_share,
-                     "logic_share": logic_share, "iterations": prof["iterations"]},
+                     "logic_share": logic_share, "iterations": prof["iterations"],
+                     "l2": l2, "limiter": limiter},
         "rays": {"closest": prof["closest_rays"], "shadow": prof["shadow_rays"], "Mrays_s": rays / ms_b / 1e3},
         "clocks": clocks,
     }
@@ -723,8 +771,11 @@ def profile_case(a):
     case allows, while the process holds a few GB at most (the batch case: the
     64-instance workload at the given launch configuration).
 
-      render    rmn_render of a heightfield (--tris) under the synthetic sky,
-                --size square, --spp
+      render    a heightfield (--tris) under the synthetic sky, --size square,
+                --spp, rendered twice as a one-item rmn_batch at --slots per
+                unit, --pool workers per lane, --lanes, --stack, --order (0:
+                library defaults) -- small pools over many units give a
+                steady state
       trace     rmn_trace_closest / rmn_trace_shadow on a random soup (--tris,
                 --rays)
       batch     the batch64 workload as one rmn_batch (--slots per unit,
@@ -750,11 +801,16 @@ def profile_case(a):
         cam = scenes.heightfield_camera(side, side, a.spp)
         m = api.Model(s)
         args = api.RenderArgs.from_camera(cam, seed=1)
+        args.slots_per_unit = a.slots
         ph = api.Photo(side, side)
+        b = api.Batch([(m, args, ph)], use_graph=False, pool_workers=a.pool, lanes=a.lanes, stack_entries=a.stack,
+                      ray_order=a.order)
         for _ in range(2):
-            api.render(m, args, ph)
+            b.render()
         torch.cuda.synchronize()
-        print("render", m.info(), "pixels", side * side, "spp", a.spp)
+        prof = b.profile()
+        print("render", m.info(), "pixels", side * side, "spp", a.spp, "slots", a.slots, "pool", a.pool,
+              "lanes", a.lanes, "iterations", prof["iterations"])
     elif a.profile_case == "batch":
         insts = scenes.batch_instances(64, seed=7)
         models = [api.Model(i.scene) for i in insts]
@@ -763,7 +819,7 @@ def profile_case(a):
             r.slots_per_unit = a.slots
         photos = [api.Photo(i.camera.width, i.camera.height) for i in insts]
         b = api.Batch(list(zip(models, argsl, photos)), use_graph=True, pool_workers=a.pool, lanes=a.lanes,
-                      stack_entries=a.stack)
+                      stack_entries=a.stack, ray_order=a.order)
         for _ in range(2):
             b.render()
         torch.cuda.synchronize()
@@ -837,10 +893,11 @@ def main():
     ap.add_argument("--size", default="256")
     ap.add_argument("--spp", type=int, default=16)
     ap.add_argument("--rays", type=int, default=1_000_000)
-    ap.add_argument("--slots", type=int, default=2)
-    ap.add_argument("--pool", type=int, default=1 << 23)
-    ap.add_argument("--lanes", type=int, default=3)
+    ap.add_argument("--slots", type=int, default=0)
+    ap.add_argument("--pool", type=int, default=0)
+    ap.add_argument("--lanes", type=int, default=0)
     ap.add_argument("--stack", type=int, default=0)
+    ap.add_argument("--order", type=int, default=0)
     args = ap.parse_args()
     if args.profile_case:
         profile_case(args)

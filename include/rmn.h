@@ -149,11 +149,13 @@ typedef struct rmn_render_args {
   int32_t width, height, spp, threads; /* threads: ignored on the GPU */
   int32_t max_depth;                   /* 16 in the reference (src/render.cpp:125); 1..16 */
   uint64_t seed;                       /* counter-based random stream key */
-  int32_t lanes_per_pixel;             /* work units per pixel (0: from slots_per_unit); 1..64 */
-  int32_t slots_per_unit;              /* sample slots per work unit (0: library default: 2 for renders of up to
+  int32_t lanes_per_pixel;             /* work units per pixel, each of consecutive sample slots (0: from
+                                          slots_per_unit); 1..64 */
+  int32_t slots_per_unit;              /* sample slots per path unit; the light-sample slots go in units of
+                                          max(slots_per_unit, 8). 0: library default: 2 for renders of up to
                                           2^26 sample slots, else 4, doubled while the render's own per-unit
                                           records, 112 B each, would exceed 16 GiB -- a choice of the render
-                                          alone, so its image does not depend on the batch or free memory) */
+                                          alone, so its image does not depend on the batch or free memory */
   int32_t reserved[2];
 } rmn_render_args;
 
@@ -264,6 +266,11 @@ typedef struct rmn_batch_options {
   int32_t stack_entries; /* traversal stack, 23 or 27 entries (0: library default, the smallest that holds
                             every item's tree: 23 when all trees are at most 22 levels deep); a stack too
                             small for a tree is RMN_ERR_INVALID_ARGUMENT */
+  int32_t ray_order;     /* 1: before each traversal launch, reorder its ray queue by bucket (the ray's render,
+                            the octant of its direction, the cell of its origin in an 8^3 grid over the scene
+                            box) so that a warp traces rays that start close and head alike; 0: as queued.
+                            Images do not depend on it. */
+  int32_t reserved;
 } rmn_batch_options;
 rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_batch_options* options, void* stream,
                             rmn_batch** out);
@@ -298,9 +305,10 @@ rmn_status rmn_batch_device_bytes(const rmn_batch_item* items, int32_t n, const 
  * `pixel_fraction` (0 < f <= 1) of its pixels (rmn_batch_device_bytes
  * gives a candidate's full size); then the fastest of those
  * once more with the other traversal stack build where the batch's trees
- * allow both (27 entries instead of 23). Returns the fastest. Set each
- * item's slots_per_unit and the batch's pool_workers, lanes and
- * stack_entries from the result. The images do not depend on the choice
+ * allow both (27 entries instead of 23), then the fastest with its ray
+ * queues binned (ray_order 1). Returns the fastest. Set each item's
+ * slots_per_unit and the batch's pool_workers, lanes, stack_entries and
+ * ray_order from the result. The images do not depend on the choice
  * beyond float summation order across units (slots_per_unit); pool size,
  * lanes and stack change nothing. RMN_ERR_OUT_OF_MEMORY when not even the
  * library's default split with the smallest pool (4096 workers, one lane)
@@ -311,7 +319,7 @@ typedef struct rmn_tune_result {
   int32_t candidates;          /* configurations timed */
   int32_t lanes;               /* 0: the library's default won */
   int32_t stack_entries;       /* 23 or 27 (the value to pass in rmn_batch_options) */
-  int32_t reserved;
+  int32_t ray_order;           /* 0 or 1 (likewise) */
 } rmn_tune_result;
 rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixel_fraction, rmn_tune_result* out,
                               void* stream);

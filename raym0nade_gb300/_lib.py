@@ -70,13 +70,13 @@ class BatchItem(C.Structure):
 
 class BatchOptions(C.Structure):
     _fields_ = [("use_graph", C.c_int32), ("pool_workers", C.c_int32), ("lanes", C.c_int32),
-                ("stack_entries", C.c_int32)]
+                ("stack_entries", C.c_int32), ("ray_order", C.c_int32), ("reserved", C.c_int32)]
 
 
 class TuneResult(C.Structure):
     _fields_ = [("slots_per_unit", C.c_int32), ("pool_workers", C.c_int32), ("best_ms", C.c_double),
                 ("default_ms", C.c_double), ("candidates", C.c_int32), ("lanes", C.c_int32),
-                ("stack_entries", C.c_int32), ("reserved", C.c_int32)]
+                ("stack_entries", C.c_int32), ("ray_order", C.c_int32)]
 
 
 class ImageDesc(C.Structure):

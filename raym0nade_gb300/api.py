@@ -437,7 +437,7 @@ def batch_device_bytes(items, pool_workers: int = 0, lanes: int = 0) -> int:
     RenderArgs, Photo) items would take with these options (unit records and
     worker pool; scenes and images excluded)."""
     out = C.c_int64()
-    opt = _lib.BatchOptions(1, int(pool_workers), int(lanes), 0)
+    opt = _lib.BatchOptions(1, int(pool_workers), int(lanes), 0, 0, 0)
     _check(_lib.load().rmn_batch_device_bytes(_batch_items(items), len(items), C.byref(opt), C.byref(out)),
            "rmn_batch_device_bytes")
     return int(out.value)
@@ -448,13 +448,15 @@ class Batch:
     from a captured CUDA graph. Photos must live on the device."""
 
     def __init__(self, items, use_graph: bool = True, stream=None, pool_workers: int = 0, lanes: int = 0,
-                 stack_entries: int = 0):
+                 stack_entries: int = 0, ray_order: int = 0):
         """items: list of (Model, RenderArgs, Photo); pool_workers per lane;
-        stack_entries 0 (library default), 23 or 27."""
+        stack_entries 0 (library default), 23 or 27; ray_order 1 bins the
+        ray queues before each traversal launch."""
         lib = _lib.load()
         arr = _batch_items(items)
         h = C.c_void_p()
-        opt = _lib.BatchOptions(1 if use_graph else 0, int(pool_workers), int(lanes), int(stack_entries))
+        opt = _lib.BatchOptions(1 if use_graph else 0, int(pool_workers), int(lanes), int(stack_entries),
+                                int(ray_order), 0)
         _check(lib.rmn_batch_create(arr, len(items), C.byref(opt), _stream(stream), C.byref(h)), "rmn_batch_create")
         self._h = h
         self.items = items

@@ -79,7 +79,8 @@ struct DemodAdj {
   float S;
   float3 df, dlight, dbase;
 };
-__device__ DemodAdj demod_adj(float3 bt, float3 sav, float3 f, float3 light, float w, float3 g, float E) {
+__device__ __noinline__ DemodAdj demod_adj(float3 bt, float3 sav, float3 f, float3 light, float w, float3 g,
+                                           float E) {
   DemodAdj r;
   r.S = 0.0f;
   r.df = r.dlight = r.dbase = f3(0.0f);
@@ -136,8 +137,10 @@ struct PathAdj {
   float3 A_light, A_w0, dbase;
 };
 
-// stk: the thread's deferred-child stack in shared memory.
-__device__ __forceinline__ bool occluded(const DevScene& s, float3 pos, float3 dir, float aim, int* status,
+// stk: the thread's deferred-child stack in shared memory. A real call, as
+// are brdf_logd and demod_adj: inlined at each of their call sites they
+// multiplied the replay's code, and its warps stalled on instruction fetch.
+__device__ __noinline__ bool occluded(const DevScene& s, float3 pos, float3 dir, float aim, int* status,
                                          int2* stk) {
   float tm = aim + RMN_EPS;  // HitRecord(eps, aimDepth + eps), Model::rayHit_test
   int st = trace_shared<true>(s, make_tray(pos, dir), RMN_EPS, tm, aim, stk);  // no textured scenes here
@@ -149,7 +152,7 @@ __device__ __forceinline__ bool occluded(const DevScene& s, float3 pos, float3 d
 }
 
 // Log-derivatives of a factor clamp64(brdf(V, L)) * k of surface sf.
-__device__ __forceinline__ void brdf_logd(const Surf& sf, float3 V, float3 L, int clamp_mode, float3& l, float3& q,
+__device__ __noinline__ void brdf_logd(const Surf& sf, float3 V, float3 L, int clamp_mode, float3& l, float3& q,
                                           float3& lr) {
   float3 db, dr;
   float3 f = brdf_d(sf, V, L, db, dr);

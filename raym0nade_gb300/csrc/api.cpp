@@ -579,7 +579,7 @@ static rmn_status render_one(rmn_scene* scene, const rmn_render_args* args, cons
   if (r == RMN_OK) {
     RenderItem it{scene, a, static_cast<float*>(gb.dev), static_cast<float*>(dd.dev), static_cast<float*>(ds.dev),
                   static_cast<float*>(id.dev), static_cast<float*>(is.dev), static_cast<int*>(dr.dev)};
-    r = batch_create(&it, 1, false, 0, 0, 0, st, &b);
+    r = batch_create(&it, 1, false, 0, 0, 0, 0, st, &b);
   }
   if (r == RMN_OK) r = prof ? batch_profile(b, st, prof) : batch_launch(b, st);
   if (r == RMN_OK) r = finish_out(image->radiance_Dd, npx * 16, st, dd);
@@ -670,8 +670,9 @@ rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_ba
   clear_error();
   if (!items || n <= 0 || !out) return fail(RMN_ERR_INVALID_ARGUMENT, "a batch needs at least one item");
   *out = nullptr;
-  rmn_batch_options opt = options ? *options : rmn_batch_options{1, 0, 0, 0};
+  rmn_batch_options opt = options ? *options : rmn_batch_options{1, 0, 0, 0, 0, 0};
   if (opt.pool_workers < 0) return fail(RMN_ERR_INVALID_ARGUMENT, "pool_workers must be >= 0");
+  if (opt.ray_order != 0 && opt.ray_order != 1) return fail(RMN_ERR_INVALID_ARGUMENT, "ray_order must be 0 or 1");
   if (opt.lanes < 0 || opt.lanes > 4) return fail(RMN_ERR_INVALID_ARGUMENT, "lanes must lie in [0, 4]");
   if (opt.stack_entries != 0 && opt.stack_entries != RMN_STACK_SMALL && opt.stack_entries != RMN_STACK)
     return fail(RMN_ERR_INVALID_ARGUMENT, "stack_entries must be 0, %d or %d", RMN_STACK_SMALL, RMN_STACK);
@@ -681,7 +682,7 @@ rmn_status rmn_batch_create(const rmn_batch_item* items, int32_t n, const rmn_ba
   rmn_batch* bt = new (std::nothrow) rmn_batch();
   if (!bt) return fail(RMN_ERR_OUT_OF_MEMORY, "host allocation failed");
   r = batch_create(its.data(), n, opt.use_graph != 0, opt.pool_workers, opt.lanes, opt.stack_entries,
-                   static_cast<cudaStream_t>(stream), &bt->state);
+                   opt.ray_order, static_cast<cudaStream_t>(stream), &bt->state);
   if (r != RMN_OK) {
     delete bt;
     return r;
@@ -719,13 +720,13 @@ rmn_status rmn_batch_device_bytes(const rmn_batch_item* items, int32_t n, const 
                                   int64_t* out) {
   clear_error();
   if (!items || n <= 0 || !out) return fail(RMN_ERR_INVALID_ARGUMENT, "a batch needs at least one item and an output");
-  const rmn_batch_options opt = options ? *options : rmn_batch_options{1, 0, 0, 0};
+  const rmn_batch_options opt = options ? *options : rmn_batch_options{1, 0, 0, 0, 0, 0};
   if (opt.pool_workers < 0 || opt.lanes < 0 || opt.lanes > 4)
     return fail(RMN_ERR_INVALID_ARGUMENT, "pool_workers must be >= 0 and lanes lie in [0, 4]");
   std::vector<RenderItem> its;
   rmn_status r = make_items(items, n, its, false);
   if (r != RMN_OK) return r;
-  *out = (int64_t)batch_device_bytes(its.data(), n, opt.pool_workers, opt.lanes);
+  *out = (int64_t)batch_device_bytes(its.data(), n, opt.pool_workers, opt.lanes, opt.ray_order);
   return RMN_OK;
 }
 
@@ -747,10 +748,10 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
     cudaGetLastError();
     free_b = 0;
   }
-  auto fits = [&](int slots, int pool, int lanes) {
+  auto fits = [&](int slots, int pool, int lanes, int order) {
     std::vector<RenderItem> f = full;
     for (RenderItem& it : f) it.args.slots_per_unit = slots;
-    return batch_device_bytes(f.data(), n, pool, lanes) <= free_b / 2;
+    return batch_device_bytes(f.data(), n, pool, lanes, order) <= free_b / 2;
   };
   // the batch cannot be built at all when its default unit records and the
   // smallest pool exceed what is free
@@ -790,33 +791,37 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
   const int pools[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
   const int lanes[] = {2, 3, 4};
   // candidate 0: the library's own choice (the items' slots_per_unit, pool,
-  // lanes and stack left at 0); then the grid at the default stack; last, the
-  // fastest so far with the deeper stack build, where the default is the
-  // shallow one (the stack must hold every tree, so only larger stacks are
-  // admissible; they cost shared memory and so persistent blocks per SM)
+  // lanes, stack and ray order left at 0); then the grid at the default
+  // stack; then the fastest so far with the deeper stack build, where the
+  // default is the shallow one (the stack must hold every tree, so only
+  // larger stacks are admissible; they cost shared memory and so persistent
+  // blocks per SM); last, the fastest so far with its ray queues binned
   const int stack_def = default_stack_entries(its.data(), n);
   rmn_tune_result best{0, 0, 1e30, 0.0, 0, 0, stack_def, 0};
   std::vector<int> proxy_slots(its.size());
   for (size_t i = 0; i < its.size(); ++i) proxy_slots[i] = its[i].args.slots_per_unit;
   const int grid = 4 * 4 * 3;
-  for (int ci = -1; ci <= grid && r == RMN_OK; ++ci) {
-    const bool is_default = ci < 0, stack_pass = ci == grid;
-    if (stack_pass && stack_def == RMN_STACK) break;
-    const int si = ci < 0 || stack_pass ? 0 : ci / 12, pi = ci < 0 || stack_pass ? 0 : (ci / 3) % 4,
-              li = ci < 0 || stack_pass ? 0 : ci % 3;
+  for (int ci = -1; ci <= grid + 1 && r == RMN_OK; ++ci) {
+    const bool is_default = ci < 0, stack_pass = ci == grid, order_pass = ci == grid + 1;
+    if (stack_pass && stack_def == RMN_STACK) continue;
+    const bool refine = stack_pass || order_pass;
+    const int si = ci < 0 || refine ? 0 : ci / 12, pi = ci < 0 || refine ? 0 : (ci / 3) % 4,
+              li = ci < 0 || refine ? 0 : ci % 3;
     int cs = is_default ? 0 : slots[si], cp = is_default ? 0 : pools[pi], cl = is_default ? 0 : lanes[li];
-    int ck = stack_def;
-    if (stack_pass) {
+    int ck = stack_def, co = 0;
+    if (refine) {
       cs = best.slots_per_unit;
       cp = best.pool_workers;
       cl = best.lanes;
-      ck = RMN_STACK;
-    } else if (!is_default && !fits(cs, cp, cl)) {
+      ck = stack_pass ? RMN_STACK : best.stack_entries;
+      co = order_pass ? 1 : 0;
+      if (order_pass && !fits(cs, cp, cl, co)) continue;
+    } else if (!is_default && !fits(cs, cp, cl, 0)) {
       continue;
     }
     for (size_t i = 0; i < its.size(); ++i) its[i].args.slots_per_unit = cs == 0 ? proxy_slots[i] : cs;
     BatchState* b = nullptr;
-    r = batch_create(its.data(), n, true, cp, cl, ck, st, &b);
+    r = batch_create(its.data(), n, true, cp, cl, ck, co, st, &b);
     if (r != RMN_OK) break;
     r = batch_launch(b, st);  // warm-up
     if (r == RMN_OK) {
@@ -837,6 +842,7 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
       best.pool_workers = cp;
       best.lanes = cl;
       best.stack_entries = ck;
+      best.ray_order = co;
     }
   }
   if (e0) cudaEventDestroy(e0);

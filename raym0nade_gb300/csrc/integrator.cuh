@@ -15,8 +15,10 @@ struct Params {
   int glass;      // the scene has transmissive or half-opaque materials
   int slots16;    // slots of a pixel behind such a first vertex
   float inv_spp16;
-  int S;  // slots per unit
-  int K;  // units per pixel
+  int S;   // slots per path unit
+  int K;   // units per pixel
+  int Sd;  // slots per light-sample unit
+  int Kd;  // light-sample units per pixel (0: every unit holds S consecutive slots)
   uint64_t seed;
 };
 
@@ -24,6 +26,11 @@ struct Params {
 // shorter units shorten the drain at the end of a render, longer ones need
 // fewer partial records (112 B each).
 constexpr int kDefaultSlotsPerUnit = 16;
+// Slots of a light-sample unit at least: a worker draws a unit's first-vertex
+// light samples up to 8 at a time, each with its shadow ray, in one round
+// trip (a light sample is one shadow ray, so a long unit of them drains no
+// slower than a short path unit).
+constexpr int kLightSlotsPerUnit = 8;
 
 inline Params make_params(const rmn_render_args& a, bool glass = false) {
   Params p;
@@ -46,19 +53,39 @@ inline Params make_params(const rmn_render_args& a, bool glass = false) {
   p.slots16 = p.spp_d + spp_i * 16;  // renderPixel's MultiSampleForRefraction
   p.inv_spp16 = 1.0f / (float)(spp_i * 16);
   const int layout = glass ? p.slots16 : p.slots;  // units are cut for the largest pixel
-  // lanes_per_pixel > 0 fixes the number of units per pixel; 0 cuts the
-  // slots into units of kDefaultSlotsPerUnit.
+  // lanes_per_pixel > 0 fixes the number of units per pixel, each of S
+  // consecutive slots; 0 cuts the light-sample slots into units of Sd =
+  // max(S, kLightSlotsPerUnit) and the path slots into units of S =
+  // slots_per_unit (kDefaultSlotsPerUnit if 0).
   if (a.lanes_per_pixel > 0) {
     p.K = a.lanes_per_pixel;
     p.S = (layout + p.K - 1) / p.K;
     if (p.S < 1) p.S = 1;
+    p.Sd = p.S;
+    p.Kd = 0;
   } else {
     p.S = a.slots_per_unit > 0 ? a.slots_per_unit : kDefaultSlotsPerUnit;
-    p.K = (layout + p.S - 1) / p.S;
+    p.Sd = p.S > kLightSlotsPerUnit ? p.S : kLightSlotsPerUnit;
+    p.Kd = (p.spp_d + p.Sd - 1) / p.Sd;
+    p.K = p.Kd + (layout - p.spp_d + p.S - 1) / p.S;
     if (p.K < 1) p.K = 1;
   }
   p.seed = a.seed;
   return p;
+}
+
+// Slots [j0, j1) of unit `sub` of a pixel with `pix_slots` sample slots:
+// the first Kd units hold the light-sample slots, Sd each, the others the
+// path slots, S each; with Kd = 0 unit k holds slots [k S, (k + 1) S).
+__host__ __device__ __forceinline__ void unit_slots(const Params& p, int sub, int pix_slots, int& j0, int& j1) {
+  if (sub < p.Kd) {
+    j0 = sub * p.Sd;
+    j1 = min(j0 + p.Sd, p.spp_d);
+  } else {
+    j0 = (p.Kd ? p.spp_d : 0) + (sub - p.Kd) * p.S;
+    j1 = min(j0 + p.S, pix_slots);
+  }
+  if (j0 > j1) j0 = j1;
 }
 
 // The camera ray's unnormalised direction for pixel (x, y) (renderPixel,

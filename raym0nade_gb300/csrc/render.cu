@@ -95,9 +95,11 @@ struct Queues {
 // Worker pool in HBM (structure of arrays).
 struct Pool {
   int W;
-  int4* unit;      // job, pixel, j (current slot), j1 (end of unit)
-  int4* ph;        // phase, rng counter, depth, flags
-  long long* uid;  // global unit index (partial record)
+  // the worker's header, 2 per worker in one 32-byte sector, read and
+  // written whole by every logic kernel: (job, pixel, j = current slot, j1 =
+  // end of unit), (rng counter, phase | depth << 4 | flags << 12, global
+  // unit index = the partial record, low and high word)
+  int4* hdr;
   float4* ro;      // ray origin, t_min
   float4* rd;      // ray direction, t_max (closest) or aim depth (shadow)
   float2* res;     // closest: (leaf-order triangle, t); shadow: (occluded, -)
@@ -410,11 +412,21 @@ __device__ __forceinline__ void push_rays(int* q, unsigned int* qn, int w, int n
   for (int k = 0; k < n; ++k) q[first + k] = ~(w * kDirectBatch + k);
 }
 
-__device__ __forceinline__ void store_worker(const Pool& P, int w, int4 ph, int phase, const RmnRng& rng, int4 un) {
-  ph.x = phase;
-  ph.y = (int)rng.ctr;
-  P.ph[w] = ph;
-  P.unit[w] = un;
+// The header in registers: un = (job, pixel, j, j1), ph = (phase, rng
+// counter, depth, flags), uid = the unit's partial record.
+__device__ __forceinline__ void load_worker(const Pool& P, int w, int4& ph, int4& un, long long& uid) {
+  const int4 a = P.hdr[2 * (size_t)w], b = P.hdr[2 * (size_t)w + 1];
+  un = a;
+  ph = make_int4(b.y & 15, b.x, (b.y >> 4) & 255, b.y >> 12);
+  uid = (long long)(((unsigned long long)(unsigned)b.w << 32) | (unsigned)b.z);
+}
+__device__ __forceinline__ int worker_job(const Pool& P, int w) { return P.hdr[2 * (size_t)w].x; }
+__device__ __forceinline__ void store_worker(const Pool& P, int w, const int4& ph, int phase, const RmnRng& rng,
+                                             const int4& un, long long uid) {
+  P.hdr[2 * (size_t)w] = un;
+  P.hdr[2 * (size_t)w + 1] = make_int4((int)rng.ctr, phase | (ph.z << 4) | (ph.w << 12),
+                                       (int)(unsigned)(unsigned long long)uid,
+                                       (int)(unsigned)((unsigned long long)uid >> 32));
 }
 
 // sampleRay's body at a hit (src/render.cpp:121-312) for worker w: emit an
@@ -554,15 +566,16 @@ __global__ void __launch_bounds__(128, 8) shade_kernel(const Job* __restrict__ j
   QLen* out = &ctl->q[par];
   for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
     const int w = in[idx];
-    int4 ph = P.ph[w];
-    int4 un = P.unit[w];
+    int4 ph, un;
+    long long uid;
+    load_worker(P, w, ph, un, uid);
     const Job* J = &jobs[un.x];
     const Params& p = J->p;
     const DevScene& s = J->s;
     RmnRng rng;
     rng.key = rmn_stream_key(p.seed, (uint32_t)un.y, (uint32_t)un.z);
     rng.ctr = (unsigned)ph.y;
-    float4* part = parts + (size_t)P.uid[w] * RMN_PART_F4;
+    float4* part = parts + (size_t)uid * RMN_PART_F4;
     // sampleRay's body, src/render.cpp:121-312
     float2 res = P.res[w];
     int h = __float_as_int(res.x);
@@ -582,7 +595,7 @@ __global__ void __launch_bounds__(128, 8) shade_kernel(const Job* __restrict__ j
                       : shade_hit<false>(J, P, w, rng, ph, un, part, res, o, dir, status);
     }
     if (phase == PH_SLOT) un.z++;
-    store_worker(P, w, ph, phase, rng, un);
+    store_worker(P, w, ph, phase, rng, un, uid);
     if (phase == PH_WAIT_CLOSEST) push(Q.c[par], &out->c, w);
     else if (phase == PH_NEE) push(Q.nee, &out->nee, w);
     else push(Q.slot, &out->slot, w);
@@ -596,8 +609,9 @@ __global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ job
   const int* in = Q.nw[par ^ 1];
   for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
     const int w = idx < a ? in[idx] : Q.nee[idx - a];
-    int4 ph = P.ph[w];
-    int4 un = P.unit[w];
+    int4 ph, un;
+    long long uid;
+    load_worker(P, w, ph, un, uid);
     const Job* J = &jobs[un.x];
     RmnRng rng;
     rng.key = rmn_stream_key(J->p.seed, (uint32_t)un.y, (uint32_t)un.z);
@@ -609,7 +623,7 @@ __global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ job
       const float4 pa = P.pa[w], pb = P.pb[w];
       const float3 base = indirect_base_of(*J, un.y);
       const float inv_spp = inv_spp_of(*J, un.y);
-      float4* part = parts + (size_t)P.uid[w] * RMN_PART_F4;
+      float4* part = parts + (size_t)uid * RMN_PART_F4;
       for (int k = 0; k < dk.y; ++k) {
         const size_t rid = (size_t)w * kDirectBatch + k;
         if (P.dres[rid] != 0.0f) continue;
@@ -623,7 +637,7 @@ __global__ void __launch_bounds__(128, 8) nee_kernel(const Job* __restrict__ job
       if (queued) P.dk[w] = make_int2(cnt, queued);
     }
     if (!queued) un.z++;
-    store_worker(P, w, ph, queued ? PH_WAIT_NEE : PH_SLOT, rng, un);
+    store_worker(P, w, ph, queued ? PH_WAIT_NEE : PH_SLOT, rng, un, uid);
     if (queued) {
       push_rays(Q.sn[par], &out->sn, w, queued);
       push(Q.nw[par], &out->nw, w);
@@ -693,7 +707,8 @@ __device__ __noinline__ void first_bounce_glass(const Pool& P, int w, const Surf
 constexpr int kFetchTile = 32;
 __device__ __forceinline__ void unit_of_fetch(const Params& p, long long local, int& pixel, int& sub) {
   const int K = p.K;
-  const int Kd = min(K, (p.spp_d + p.S - 1) / p.S);  // units starting with a light-sample slot
+  // units starting with a light-sample slot
+  const int Kd = p.Kd ? p.Kd : min(K, (p.spp_d + p.S - 1) / p.S);
   const long long per_tile = (long long)kFetchTile * K;
   const long long tile = local / per_tile;
   const int r = (int)(local - tile * per_tile);
@@ -721,10 +736,10 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
   unsigned long long slots_done = 0;
   for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
     const int w = idx < a ? in[idx] : Q.slot[idx - a];
-    int4 ph = P.ph[w];
+    int4 ph, un;
+    long long uid;
+    load_worker(P, w, ph, un, uid);
     int phase = ph.x;
-    int4 un = P.unit[w];
-    long long uid = P.uid[w];
     const Job* J = phase == PH_FETCH ? nullptr : &jobs[un.x];
     RmnRng rng;
     rng.key = 0;
@@ -770,7 +785,8 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
         // first vertex (renderPixel, src/render.cpp:497-499); the units of a
         // scene with such materials are laid out for that many
         const int pix_slots = (J->p.glass && !(gb0[17] > 1.0f - RMN_EPS)) ? J->p.slots16 : J->p.slots;
-        int j1 = min(pix_slots, sub * J->p.S + J->p.S), j0 = min(sub * J->p.S, j1);
+        int j0, j1;
+        unit_slots(J->p, sub, pix_slots, j0, j1);
         float4* part = parts + (size_t)uid * RMN_PART_F4;
 #pragma unroll
         for (int k = 0; k < 6; ++k) part[k] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
@@ -847,8 +863,7 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
       phase = PH_WAIT_CLOSEST;
       break;
     }
-    store_worker(P, w, ph, phase, rng, un);
-    P.uid[w] = uid;
+    store_worker(P, w, ph, phase, rng, un, uid);
     if (phase == PH_WAIT_DIRECT) push(Q.sd[par], &out->sd, w);
     else if (phase == PH_WAIT_CLOSEST) push(Q.c[par], &out->c, w);
   }
@@ -911,7 +926,7 @@ __global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) qtrace_
           w = q[i];
           const int wk = (!SHADOW || w >= 0) ? w : (~w) / kDirectBatch;
           float4 o = P.ro[wk], d = (!SHADOW || w >= 0) ? P.rd[wk] : P.drd[~w];
-          jb = P.unit[wk].x;
+          jb = worker_job(P, wk);
           s = jobs[jb].s;
           alpha = ALPHA && s.has_alpha != 0;
           r = make_tray(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
@@ -957,6 +972,94 @@ __global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) qtrace_
     atomicAdd(&ctr->leaves, (unsigned long long)tc.leaves);
     atomicAdd(&ctr->tris, (unsigned long long)tc.tris);
   }
+}
+
+
+// Ray binning (batch option ray_order): before a traversal launch, its queue
+// is reordered by a bucket key -- the ray's job, the octant of its direction
+// and a cell of its origin in an 8 x 8 x 8 grid over the job's scene box --
+// with a counting sort, so the lanes of a warp trace rays that start close
+// together and head the same way: they fetch the same upper nodes and walk
+// more alike. Only the order in which rays are taken from the queue changes;
+// each ray's visits and answer are its own, so images are unchanged.
+constexpr int kBins = 4096;
+
+__device__ __forceinline__ unsigned ray_bin(const Job* __restrict__ jobs, const Pool& P, int w, bool shadow) {
+  const int wk = (!shadow || w >= 0) ? w : (~w) / kDirectBatch;
+  const float4 o = P.ro[wk];
+  const float4 d = (!shadow || w >= 0) ? P.rd[wk] : P.drd[~w];
+  const int jb = worker_job(P, wk);
+  const DevNode* nodes = jobs[jb].s.nodes;
+  const int root = jobs[jb].s.root;
+  unsigned cell = 0;
+  if (root >= 0) {
+    const DevNode* n = nodes + root;
+    const float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
+    const float lx = fminf(A.x, B.z), ly = fminf(A.y, B.w), lz = fminf(A.z, C.x);
+    const float hx = fmaxf(A.w, C.y), hy = fmaxf(B.x, C.z), hz = fmaxf(B.y, C.w);
+    auto q = [](float v, float lo, float hi) {
+      const float f = (v - lo) / fmaxf(hi - lo, 1e-20f) * 8.0f;
+      return (unsigned)fminf(fmaxf(f, 0.0f), 7.0f);
+    };
+    cell = q(o.x, lx, hx) | q(o.y, ly, hy) << 3 | q(o.z, lz, hz) << 6;
+  }
+  const unsigned oct = (d.x < 0.0f ? 1u : 0u) | (d.y < 0.0f ? 2u : 0u) | (d.z < 0.0f ? 4u : 0u);
+  return ((cell << 3) | oct) ^ (((unsigned)jb * 2654435761u) >> 20);
+}
+
+// Counts the queue's rays per bucket (block histograms in shared memory,
+// added into `bins`) and keeps each entry's bucket.
+template <bool SHADOW>
+__global__ void __launch_bounds__(256) bin_count_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+                                                        int par, unsigned* bins, uint16_t* qb) {
+  __shared__ unsigned h[kBins];
+  for (int i = threadIdx.x; i < kBins; i += blockDim.x) h[i] = 0;
+  __syncthreads();
+  const unsigned n = SHADOW ? ctl->q[par].sn : ctl->q[par].c;
+  const int* q = SHADOW ? Q.sn[par] : Q.c[par];
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned b = ray_bin(jobs, P, q[i], SHADOW) & (kBins - 1);
+    qb[i] = (uint16_t)b;
+    atomicAdd(&h[b], 1u);
+  }
+  __syncthreads();
+  for (int i = threadIdx.x; i < kBins; i += blockDim.x)
+    if (h[i]) atomicAdd(&bins[i], h[i]);
+}
+
+// Exclusive prefix sum of the kBins bucket counts, in place (one block of
+// 1024 threads, 4 buckets each).
+__global__ void __launch_bounds__(1024) bin_scan_kernel(unsigned* bins) {
+  __shared__ unsigned part[1024];
+  const int t = threadIdx.x;
+  unsigned v[4], s = 0;
+  for (int k = 0; k < 4; ++k) {
+    v[k] = bins[4 * t + k];
+    s += v[k];
+  }
+  part[t] = s;
+  __syncthreads();
+  for (int off = 1; off < 1024; off <<= 1) {
+    const unsigned x = t >= off ? part[t - off] : 0u;
+    __syncthreads();
+    part[t] += x;
+    __syncthreads();
+  }
+  unsigned run = part[t] - s;
+  for (int k = 0; k < 4; ++k) {
+    bins[4 * t + k] = run;
+    run += v[k];
+  }
+}
+
+// Writes each queue entry to the next free place of its bucket.
+template <bool SHADOW>
+__global__ void __launch_bounds__(256) bin_scatter_kernel(Queues Q, Ctl* ctl, int par, unsigned* bins,
+                                                          const uint16_t* qb, int* out) {
+  const unsigned n = SHADOW ? ctl->q[par].sn : ctl->q[par].c;
+  const int* q = SHADOW ? Q.sn[par] : Q.c[par];
+  for (unsigned i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    out[atomicAdd(&bins[qb[i]], 1u)] = q[i];
 }
 
 
@@ -1058,6 +1161,14 @@ struct BatchState {
   bool shallow = true;        // the traversal runs its RMN_STACK_SMALL-entry build
   Pool pool[kMaxLanes] = {};  // each lane's share of the worker arrays
   Queues q[kMaxLanes] = {};
+  // ray binning (ray_order): per lane, the reordered closest and shadow
+  // queues, each entry's bucket, and the two queues' bucket counters
+  bool binned = false;
+  struct Bins {
+    int *sc = nullptr, *ss = nullptr;
+    uint16_t* qb = nullptr;
+    unsigned* bins = nullptr;
+  } bin[kMaxLanes];
   std::vector<void*> allocs;
   cudaGraphExec_t init_exec = nullptr, chunk_exec = nullptr, fin_exec = nullptr;
   bool use_graph = false;
@@ -1106,7 +1217,7 @@ static cudaError_t launch_init(BatchState* b, cudaStream_t st, Counters* ctr) {
   const int nj = (int)b->table.jobs.size(), tp = b->table.total_pix;
   cudaError_t e = cudaMemsetAsync(b->d_ctl, 0, sizeof(CtlBlock), st);
   for (int l = 0; l < b->lanes && e == cudaSuccess; ++l)
-    e = cudaMemsetAsync(b->pool[l].ph, 0, sizeof(int4) * (size_t)b->pool[l].W, st);
+    e = cudaMemsetAsync(b->pool[l].hdr, 0, 2 * sizeof(int4) * (size_t)b->pool[l].W, st);
   if (e != cudaSuccess) return e;
   const int pb = (tp + 127) / 128;
   if (ctr) {
@@ -1159,16 +1270,31 @@ static cudaError_t launch_iteration(BatchState* b, int lane, cudaStream_t st, Co
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[1], st);
   const int lb = (P.W + 127) / 128;
+  Queues QT = Q;  // the queues the traversal reads: reordered by bucket when binning
+  if (b->binned) {
+    const BatchState::Bins& bb = b->bin[lane];
+    e = cudaMemsetAsync(bb.bins, 0, 2 * kBins * sizeof(unsigned), st);
+    if (e != cudaSuccess) return e;
+    const int gb = sms * 4;
+    bin_count_kernel<false><<<gb, 256, 0, st>>>(b->d_jobs, P, Q, ctl, par, bb.bins, bb.qb);
+    bin_scan_kernel<<<1, 1024, 0, st>>>(bb.bins);
+    bin_scatter_kernel<false><<<gb, 256, 0, st>>>(Q, ctl, par, bb.bins, bb.qb, bb.sc);
+    bin_count_kernel<true><<<gb, 256, 0, st>>>(b->d_jobs, P, Q, ctl, par, bb.bins + kBins, bb.qb);
+    bin_scan_kernel<<<1, 1024, 0, st>>>(bb.bins + kBins);
+    bin_scatter_kernel<true><<<gb, 256, 0, st>>>(Q, ctl, par, bb.bins + kBins, bb.qb, bb.ss);
+    QT.c[par] = bb.sc;
+    QT.sn[par] = bb.ss;
+  }
   if (ctr) {
-    if (b->alpha && b->shallow) launch_qtrace<true, true, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
-    else if (b->alpha) launch_qtrace<true, true, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
-    else if (b->shallow) launch_qtrace<true, false, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
-    else launch_qtrace<true, false, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
+    if (b->alpha && b->shallow) launch_qtrace<true, true, RMN_STACK_SMALL>(b, P, QT, ctl, par, ctr, lb, st);
+    else if (b->alpha) launch_qtrace<true, true, RMN_STACK>(b, P, QT, ctl, par, ctr, lb, st);
+    else if (b->shallow) launch_qtrace<true, false, RMN_STACK_SMALL>(b, P, QT, ctl, par, ctr, lb, st);
+    else launch_qtrace<true, false, RMN_STACK>(b, P, QT, ctl, par, ctr, lb, st);
   } else {
-    if (b->alpha && b->shallow) launch_qtrace<false, true, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
-    else if (b->alpha) launch_qtrace<false, true, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
-    else if (b->shallow) launch_qtrace<false, false, RMN_STACK_SMALL>(b, P, Q, ctl, par, ctr, lb, st);
-    else launch_qtrace<false, false, RMN_STACK>(b, P, Q, ctl, par, ctr, lb, st);
+    if (b->alpha && b->shallow) launch_qtrace<false, true, RMN_STACK_SMALL>(b, P, QT, ctl, par, ctr, lb, st);
+    else if (b->alpha) launch_qtrace<false, true, RMN_STACK>(b, P, QT, ctl, par, ctr, lb, st);
+    else if (b->shallow) launch_qtrace<false, false, RMN_STACK_SMALL>(b, P, QT, ctl, par, ctr, lb, st);
+    else launch_qtrace<false, false, RMN_STACK>(b, P, QT, ctl, par, ctr, lb, st);
   }
   if (ev) cudaEventRecord(ev[3], st);
   return cudaGetLastError();
@@ -1304,7 +1430,9 @@ void batch_destroy(BatchState* b) {
 // Bytes of one worker's state, shadow-ray slots and queue entries (media and
 // ray differentials where a scene needs them).
 static size_t worker_bytes(bool glass, bool tex) {
-  return 4 * sizeof(int4) + sizeof(long long) + 2 * sizeof(float4) + sizeof(float2) + 8 * sizeof(float4) +
+  // header 32 B, ray origin and direction, path factors, answer, NEE
+  // vertex and weights, light-sample rays, queue entries
+  return 4 * sizeof(int4) + 2 * sizeof(float4) + sizeof(float2) + 8 * sizeof(float4) +
          sizeof(int4) + kDirectBatch * (3 * sizeof(float4) + sizeof(float)) + sizeof(int2) +
          sizeof(int) * (2 * (3 + kDirectBatch) + 2) + (glass ? RMN_MEDIA * 20 + 4 : 0) + (tex ? 3 * sizeof(float4) : 0);
 }
@@ -1339,7 +1467,8 @@ void default_slots_per_unit(const RenderItem* items, int n, int* S) {
     const bool glass = items[i].scene->dev.has_glass != 0;
     a.slots_per_unit = 1;
     const Params p1 = make_params(a, glass);
-    int s = (long long)p1.W * p1.H * p1.K <= (1LL << 26) ? 2 : 4;
+    const long long slots = (long long)p1.W * p1.H * (glass ? p1.slots16 : p1.slots);
+    int s = slots <= (1LL << 26) ? 2 : 4;
     for (;; s *= 2) {
       a.slots_per_unit = s;
       const Params p = make_params(a, glass);
@@ -1358,7 +1487,7 @@ int default_stack_entries(const RenderItem* items, int n) {
 }
 
 rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int pool_workers, int lanes,
-                        int stack_entries, cudaStream_t st, BatchState** out) {
+                        int stack_entries, int ray_order, cudaStream_t st, BatchState** out) {
   *out = nullptr;
   // the traversal stack must hold every item's deepest path of deferred
   // children; a larger one only costs occupancy
@@ -1378,6 +1507,7 @@ rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int p
   build_jobs(items, n, &b->table);
   b->table.slots = S_def;
   b->use_graph = use_graph;
+  b->binned = ray_order != 0;
   b->lanes = lanes > 0 ? std::min(lanes, kMaxLanes) : kDefaultLanes;
   // workers per lane; no more lanes and workers than there are units; the
   // default pool halves while the workers would take more than a quarter of
@@ -1410,9 +1540,7 @@ rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int p
   alloc((void**)&b->d_parts, sizeof(float4) * RMN_PART_F4 * (size_t)b->table.total_units);
   Pool P{};
   P.W = (int)W;
-  alloc((void**)&P.unit, sizeof(int4) * W);
-  alloc((void**)&P.ph, sizeof(int4) * W);
-  alloc((void**)&P.uid, sizeof(long long) * W);
+  alloc((void**)&P.hdr, 2 * sizeof(int4) * W);
   alloc((void**)&P.ro, sizeof(float4) * W);
   alloc((void**)&P.rd, sizeof(float4) * W);
   alloc((void**)&P.res, sizeof(float2) * W);
@@ -1444,9 +1572,7 @@ rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int p
     Pool& L = b->pool[l];
     L.W = (int)per;
     if (e == cudaSuccess) {
-      L.unit = P.unit + o;
-      L.ph = P.ph + o;
-      L.uid = P.uid + o;
+      L.hdr = P.hdr + 2 * o;
       L.ro = P.ro + o;
       L.rd = P.rd + o;
       L.res = P.res + o;
@@ -1475,6 +1601,13 @@ rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int p
     }
     alloc((void**)&Q.nee, sizeof(int) * per);
     alloc((void**)&Q.slot, sizeof(int) * per);
+    if (b->binned) {
+      BatchState::Bins& bb = b->bin[l];
+      alloc((void**)&bb.sc, sizeof(int) * per);
+      alloc((void**)&bb.ss, sizeof(int) * kDirectBatch * per);
+      alloc((void**)&bb.qb, sizeof(uint16_t) * kDirectBatch * per);
+      alloc((void**)&bb.bins, sizeof(unsigned) * 2 * kBins);
+    }
   }
   if (e == cudaSuccess) e = cudaMemcpy(b->d_jobs, b->table.jobs.data(), jb, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(b->d_status, 0, sizeof(int));
@@ -1527,7 +1660,7 @@ rmn_status batch_update(BatchState* b, const rmn_render_args* args, int n, cudaS
     const Params q = make_params(a, j.p.glass != 0);
     const Params& p = j.p;
     if (q.W != p.W || q.H != p.H || q.spp != p.spp || q.maxd != p.maxd || q.spp_d != p.spp_d || q.S != p.S ||
-        q.K != p.K || q.slots != p.slots || q.slots16 != p.slots16)
+        q.K != p.K || q.Sd != p.Sd || q.Kd != p.Kd || q.slots != p.slots || q.slots16 != p.slots16)
       return fail(RMN_ERR_INVALID_ARGUMENT,
                   "rmn_batch_update: item %d changes the image size, spp, P_Direct, max depth or unit split",
                   b->table.item[k]);
@@ -1546,7 +1679,7 @@ size_t batch_job_bytes() { return sizeof(Job); }
 // Device bytes batch_create would take for these items: the unit partials,
 // and per worker its state, shadow-ray slots and queue entries (media and
 // ray differentials where a scene needs them).
-size_t batch_device_bytes(const RenderItem* items_in, int n, int pool_workers, int lanes) {
+size_t batch_device_bytes(const RenderItem* items_in, int n, int pool_workers, int lanes, int ray_order) {
   // items that leave the unit split open take the library's default
   std::vector<RenderItem> items(items_in, items_in + n);
   std::vector<int> S(n, 0);
@@ -1563,7 +1696,14 @@ size_t batch_device_bytes(const RenderItem* items_in, int n, int pool_workers, i
   const int nl = lanes > 0 ? std::min(lanes, kMaxLanes) : kDefaultLanes;
   long long per = pool_workers > 0 ? pool_workers : kDefaultPoolWorkers;
   per = std::min<long long>(per, (t.total_units + nl - 1) / nl);
-  return sizeof(float4) * RMN_PART_F4 * (size_t)t.total_units + worker_bytes(glass, tex) * (size_t)per * nl;
+  // binning: the reordered queues and each entry's bucket, per worker; the
+  // bucket counters per lane
+  const size_t bin_bytes =
+      ray_order ? (sizeof(int) * (1 + kDirectBatch) + sizeof(uint16_t) * kDirectBatch) * (size_t)per * nl +
+                      sizeof(unsigned) * 2 * kBins * nl
+                : 0;
+  return sizeof(float4) * RMN_PART_F4 * (size_t)t.total_units + worker_bytes(glass, tex) * (size_t)per * nl +
+         bin_bytes;
 }
 int batch_items(const BatchState* b) { return (int)b->table.jobs.size(); }
 

@@ -86,15 +86,17 @@ void noalloc_forget_addresses();
 
 // stack_entries: the traversal kernels' deferred-child stack, RMN_STACK_SMALL
 // or RMN_STACK entries (0: the smallest that holds every item's tree).
+// ray_order: 1 bins each ray queue by origin cell and direction octant
+// before it is traced, 0 traces the queues in the order they were filled.
 rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool_workers, int lanes,
-                        int stack_entries, cudaStream_t st, BatchState** out);
+                        int stack_entries, int ray_order, cudaStream_t st, BatchState** out);
 // The traversal stack the library picks for these items (RMN_STACK_SMALL when
 // every tree is at most RMN_STACK_SMALL - 1 deep, else RMN_STACK).
 int default_stack_entries(const RenderItem* items, int n);
 rmn_status batch_launch(BatchState* b, cudaStream_t st);
 rmn_status batch_update(BatchState* b, const rmn_render_args* args, int n, cudaStream_t st);
 size_t batch_job_bytes();
-size_t batch_device_bytes(const RenderItem* items, int n, int pool_workers, int lanes);
+size_t batch_device_bytes(const RenderItem* items, int n, int pool_workers, int lanes, int ray_order = 0);
 void default_slots_per_unit(const RenderItem* items, int n, int* S);
 int batch_items(const BatchState* b);
 rmn_status batch_status(BatchState* b, cudaStream_t st);

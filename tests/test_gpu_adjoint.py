@@ -199,3 +199,80 @@ def test_adjoint_argument_errors():
     with pytest.raises(api.RmnError) as e:
         api.adjoint(mg, a, pg, g)
     assert e.value.status == 4  # RMN_ERR_UNSUPPORTED
+
+
+def test_c5_all_parameters_against_central_differences():
+    """The differentiation configuration itself: the 16-material Cornell box
+    at 512 x 512, depth 16, the L2 loss to a target rendered at parameters
+    perturbed by up to +-10%, and all 16 x 5 parameters.
+
+    The adjoint is checked at the sample count of its differences (1024 spp
+    per seed; the timed configuration's 32 spp has another expectation,
+    because the firefly clamp's bias depends on the sample count):
+    * base colour and emission: central differences with common random
+      numbers, h = 1e-3, differentiate the realisation the adjoint replays:
+      within 2% (measured: 1e-4);
+    * roughness: the difference of one realisation is dominated by jumps
+      (branch flips, moved hits), so the means over 8 seeds (8192 spp in all)
+      are compared, h = 1e-2 (at h = 1e-3 the jumps' variance, which grows
+      as 1/h, is several times larger), within 2% plus four standard errors;
+    * parameters that leave the scene unchanged (emission scale of the 15
+      materials without emission) have an exactly zero difference: their
+      adjoint must be exactly zero."""
+    w, spp, maxd = 512, 1024, 16
+    p0 = scenes.cornell16_params()
+    cam = lambda n: scenes.cornell_camera(w, w, n, max_depth=maxd)
+
+    def fwd(params, seed, n):
+        m = api.Model(scenes.cornell16(params))
+        a = api.RenderArgs.from_camera(cam(n), seed=seed)
+        ph = api.render(m, a)
+        return m, a, ph, ph.shade(api.Full)
+
+    rng = np.random.default_rng(5)
+    pt = p0.copy()
+    pt[:, 0:4] *= rng.uniform(0.9, 1.1, (16, 4))
+    pt[:, 4] *= 1.1
+    g = (2.0 * (fwd(p0, 98, 256)[3] - fwd(pt, 99, 256)[3])).reshape(-1, 3).contiguous()
+    gd = g.double()
+    phi = lambda params, seed: float((fwd(params, seed, spp)[3].reshape(-1, 3).double() * gd).sum())
+    base = scenes.cornell16(p0).materials
+
+    def unchanged(params):
+        return np.array_equal(scenes.cornell16(params).materials, base)
+
+    def fd(i, k, h, seed):
+        pp, pm = p0.copy(), p0.copy()
+        pp[i, k] += h
+        pm[i, k] -= h
+        if unchanged(pp) and unchanged(pm):
+            return None
+        return (phi(pp, seed) - phi(pm, seed)) / (2.0 * h)
+
+    seeds = list(range(1, 9))
+    adj = []
+    for s in seeds:
+        m, a, ph, _ = fwd(p0, s, spp)
+        adj.append(api.adjoint(m, a, ph, g).cpu().numpy().astype(np.float64))
+    adj = np.array(adj)
+    # base colour and emission, seed 1: the realisation's derivative
+    a1, f1, zero = [], [], []
+    for i in range(16):
+        for k in (0, 1, 2, 4):
+            d = fd(i, k, 1e-3, seeds[0])
+            if d is None:
+                zero.append(adj[0, i, k])
+            else:
+                a1.append(adj[0, i, k])
+                f1.append(d)
+    assert len(zero) == 15 and np.all(np.array(zero) == 0.0)
+    _check_rel(np.array(a1), np.array(f1), rel=0.02)
+    # roughness: means over the seeds
+    F = np.array([[fd(i, 3, 1e-2, s) for i in range(16)] for s in seeds])
+    A = adj[:, :, 3]
+    n = len(seeds)
+    ma, mf = A.mean(0), F.mean(0)
+    se = np.sqrt(A.var(0, ddof=1) / n + F.var(0, ddof=1) / n)
+    tol = 0.02 * np.abs(mf) + 4.0 * se + 1e-3 * np.abs(mf).max()
+    print("roughness adjoint", np.round(ma, 1), "differences", np.round(mf, 1), "standard error", np.round(se, 1))
+    assert (np.abs(ma - mf) <= tol).all(), np.c_[ma, mf, se]

@@ -41,10 +41,11 @@ def test_autotune_returns_a_candidate_and_its_images_match():
     free = _free_bytes()
     res = api.autotune(items, pixel_fraction=0.25)
     assert res["slots_per_unit"] in SLOTS and res["pool_workers"] in POOLS and res["lanes"] in LANES
-    assert res["stack_entries"] in STACKS
+    assert res["stack_entries"] in STACKS and res["ray_order"] in (0, 1)
     # these trees are shallow: both stack builds are admissible, the shallow
-    # one is the default and the deeper one is timed once more
-    assert res["candidates"] >= 2
+    # one is the default and the deeper one is timed once more; then binned
+    # ray queues
+    assert res["candidates"] >= 3
     assert 0.0 < res["best_ms"] <= res["default_ms"]
     # the choice fits the tuner's memory cap: half of the free device memory
     for m, a, ph in items:
@@ -53,7 +54,7 @@ def test_autotune_returns_a_candidate_and_its_images_match():
     # a batch built with the tuned settings renders every item exactly as
     # rmn_render does with the same slots per unit
     b = api.Batch(items, use_graph=True, pool_workers=res["pool_workers"], lanes=res["lanes"],
-                  stack_entries=res["stack_entries"])
+                  stack_entries=res["stack_entries"], ray_order=res["ray_order"])
     b.render()
     torch.cuda.synchronize()
     for m, a, ph in items:
@@ -61,18 +62,26 @@ def test_autotune_returns_a_candidate_and_its_images_match():
             assert np.array_equal(x, y, equal_nan=True)
 
 
-def test_stack_builds_give_identical_images():
+@pytest.mark.parametrize("use_graph", [True, False])
+def test_stack_builds_and_ray_order_give_identical_images(use_graph):
+    """Both traversal stack builds, with and without binned ray queues, give
+    every item exactly its rmn_render images (twice in a row)."""
     items = _uneven_items()
     solo = [_photo_np(api.render(m, a)) for m, a, _ in items]
     for stack in (23, 27):
-        b = api.Batch(items, use_graph=True, stack_entries=stack)
-        b.render()
-        torch.cuda.synchronize()
-        for (m, a, ph), ref in zip(items, solo):
-            for x, y in zip(_photo_np(ph), ref):
-                assert np.array_equal(x, y, equal_nan=True)
+        for order in (0, 1):
+            b = api.Batch(items, use_graph=use_graph, stack_entries=stack, ray_order=order, lanes=2)
+            for _ in range(2):
+                b.render()
+                torch.cuda.synchronize()
+                for (m, a, ph), ref in zip(items, solo):
+                    for x, y in zip(_photo_np(ph), ref):
+                        assert np.array_equal(x, y, equal_nan=True)
     with pytest.raises(api.RmnError) as e:
         api.Batch(items, stack_entries=24)
+    assert e.value.status == 1
+    with pytest.raises(api.RmnError) as e:
+        api.Batch(items, ray_order=2)
     assert e.value.status == 1
 
 
@@ -80,7 +89,9 @@ def test_device_bytes_counts_units_and_workers():
     items = _uneven_items()[:1]  # 128 x 128 Cornell, 32 spp
     m, a, ph = items[0]
     a.slots_per_unit = 4
-    units = 128 * 128 * ((int(32 * 0.7) + (32 - int(32 * 0.7)) + 3) // 4)
+    # light-sample slots in units of max(4, 8), path slots in units of 4
+    spp_d = int(32 * 0.7)
+    units = 128 * 128 * ((spp_d + 7) // 8 + (32 - spp_d + 3) // 4)
     one = api.batch_device_bytes(items, 128, 1)
     two = api.batch_device_bytes(items, 256, 1)
     per_worker = (two - one) / 128

@@ -198,21 +198,24 @@ def test_converged_matches_reference(case):
 
     The reference's estimator is heavy-tailed, so relative MSE between two
     independent 4096-spp renders is well above 1e-3 for the reference
-    against itself (Cornell 6.7e-3: ten pixels carry a third of it). The
-    gates therefore compare with the reference's own floor:
+    against itself (Cornell 5.0e-3 to 6.7e-3: ten pixels carry a third of
+    it). The gates therefore compare with the reference's own floor, from
+    four independent reference renders:
     * relative MSE, GPU against each reference render, averaged over 8 GPU
-      seeds: at most 1.1x the relative MSE between the two reference renders
-      (equal in expectation for the same estimator, larger by the squared
-      bias if the GPU were biased);
-    * bias: per pixel, z = (mean of the two reference renders - mean of 8 GPU
-      renders) / sqrt(s2 (1/2 + 1/8)), s2 the luminance variance across 8
+      seeds and the 4 references: at most 1.1x the relative MSE between two
+      reference renders, averaged over the pairs (equal in expectation for
+      the same estimator, larger by the squared bias if the GPU were
+      biased);
+    * bias: per pixel, z = (mean of the reference renders - mean of 8 GPU
+      renders) / sqrt(s2 (1/4 + 1/8)), s2 the luminance variance across 8
       further, independent GPU renders (so z has mean 0 exactly when the
       estimators agree, whatever the tails); the mean z over the image and
       over every 16 x 16 block must be within 4.5 and 5 standard errors of 0;
     * mean luminance within 0.5%; relative MSE <= 1e-3 on 4x4-binned
       images (the reference against itself: 4e-4 and below)."""
     z = np.load(os.path.join(GOLDEN, f"converged_{case}.npz"))
-    A, B = z["linear_a"].astype(np.float64), z["linear_b"].astype(np.float64)
+    R = [z[k].astype(np.float64) for k in sorted(z.files) if k.startswith("linear_")]
+    A = R[0]
     sc, cam = converged_case(case)
     m = api.Model(sc)
     G = []
@@ -223,21 +226,24 @@ def test_converged_matches_reference(case):
             assert np.allclose(lin, linear_image(g).reshape(A.shape), rtol=1e-5, atol=1e-6)
         G.append(lin)
     G = np.stack(G)
-    k = len(G) // 2
-    floor = _rel_mse(A, B)
-    gpu = np.mean([(_rel_mse(g, A) + _rel_mse(g, B)) / 2.0 for g in G[:k]])
-    gpu_floor = np.mean([_rel_mse(G[i], G[i + 1]) for i in range(0, k, 2)])
+    k, nr = len(G) // 2, len(R)
+    floor = np.mean([_rel_mse(R[i], R[j]) for i in range(nr) for j in range(nr) if i != j])
+    gpu = np.mean([_rel_mse(g, r) for g in G[:k] for r in R])
+    gpu_floor = np.mean([_rel_mse(G[i], G[j]) for i in range(k) for j in range(k) if i != j])
     binned = _rel_mse(_bin(G[0]), _bin(A))
-    lum_g, lum_r = (G[:k] @ LUM).mean(), ((A + B) @ LUM).mean() / 2.0
+    Rm = np.mean(R, axis=0)
+    lum_g, lum_r = (G[:k] @ LUM).mean(), (Rm @ LUM).mean()
     # bias
     L = G @ LUM
     mean_g, var_g = L[:k].mean(0), L[k:].var(0, ddof=1)
-    Lr = ((A + B) @ LUM) / 2.0
-    live = var_g > 0
-    zs = (Lr - mean_g)[live] / np.sqrt(var_g[live] * (0.5 + 1.0 / k))
+    Lr = Rm @ LUM
+    # pixels whose GPU renders vary by less than float rounding (misses,
+    # emitters seen directly) are deterministic: compared directly below
+    live = var_g > (1e-5 * np.maximum(np.abs(mean_g), 1e-12)) ** 2
+    zs = (Lr - mean_g)[live] / np.sqrt(var_g[live] * (1.0 / nr + 1.0 / k))
     zmean = zs.mean() / (zs.std() / np.sqrt(zs.size))
     zmap = np.full(live.shape, np.nan)
-    zmap[live] = (Lr - mean_g)[live] / np.sqrt(var_g[live] * (0.5 + 1.0 / k))
+    zmap[live] = zs
     h, w = zmap.shape
     blocks = []
     for y in range(0, h - 15, 16):
@@ -247,8 +253,8 @@ def test_converged_matches_reference(case):
             if b.size >= 64:
                 blocks.append(b.mean() / (b.std() / np.sqrt(b.size)))
     blocks = np.array(blocks)
-    # pixels whose GPU renders do not vary (misses, emitters seen directly)
-    # must equal the reference there
+    # the deterministic pixels must equal the reference's (the sky's lookup
+    # differs in the last bits between CUDA's and glibc's atan2f / acosf)
     np.testing.assert_allclose(L[0][~live], Lr[~live], rtol=2e-3, atol=1e-6)
     print(f"{case}: rel-MSE GPU-ref {gpu:.3e}, ref-ref {floor:.3e} (ratio {gpu / floor:.3f}), GPU-GPU "
           f"{gpu_floor:.3e}; binned {binned:.3e}; mean luminance {lum_g:.6f} vs {lum_r:.6f}; "
