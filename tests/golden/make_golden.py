@@ -39,9 +39,10 @@ Fixtures (numpy .npz, compressed):
                      m * 2^(e - 136), BC blocks through oracle/image_codecs.py.
                      Needs no reference; ``--images`` writes them alone.
   converged_<case>.npz  converged reference images for the image-parity
-                     tests: Photo::shade(Full) before gamma (float16) of two
-                     independent 4096-spp renders (per-pixel seeds 4096 and
-                     8192) of each case of CONVERGED_CASES -- the Cornell
+                     tests: Photo::shade(Full) before gamma (float16) of four
+                     independent 4096-spp renders (per-pixel seeds 4096,
+                     8192, 12288, 16384: linear_a .. linear_d) of each case
+                     of CONVERGED_CASES -- the Cornell
                      workload (256 x 256, depth 16, P_Direct 0.7), a
                      heightfield under the synthetic sun in sky mode
                      (192 x 108) and the glass Cornell box (128 x 128).
@@ -349,7 +350,7 @@ def mips():
 
 
 CONVERGED_CASES = ("cornell", "sky", "glass")
-CONVERGED_SEEDS = (4096, 8192)
+CONVERGED_SEEDS = (4096, 8192, 12288, 16384)
 
 
 def converged_case(name):
@@ -376,8 +377,8 @@ def converged_case(name):
 
 
 def converged(names=CONVERGED_CASES):
-    """Two independent 4096-spp renders of each case by the reference's own
-    renderer (per-pixel mt19937 seeds differ between the two), on all host
+    """Four independent 4096-spp renders of each case by the reference's own
+    renderer (per-pixel mt19937 seeds differ between them), on all host
     threads; the linear composite of each is stored as float16."""
     import time
     bindings.build(with_reference=True)
@@ -386,7 +387,7 @@ def converged(names=CONVERGED_CASES):
         sc, cam = converged_case(name)
         rs = R.scene(sc)
         out = dict(args=cam.packed(), seeds=np.asarray(CONVERGED_SEEDS, np.int64))
-        for tag, seed in zip("ab", CONVERGED_SEEDS):
+        for tag, seed in zip("abcd", CONVERGED_SEEDS):
             t0 = time.time()
             rec = rs.render(cam, seed=seed, threads=os.cpu_count() or 8)
             lin = R.compose(rec, 1.0, gamma=False)
