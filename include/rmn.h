@@ -453,11 +453,15 @@ rmn_status rmn_scene_texture_get(const rmn_scene* scene, int32_t texture, int32_
 
 /* A model read from disk as Model::Model(model_folder, model_name,
  * skyMap_name) reads it (src/model.cpp:124-215): a Wavefront OBJ file
- * (model_folder + model_name) with its MTL libraries, the textures they name
- * decoded (PNG / DDS, RGB expanded to RGBA) and the sky map
- * (model_folder + skyMap_name, Radiance HDR; "null" or NULL: none). Meshes,
- * materials and texture slots follow assimp's OBJ import and
- * Material::loadMaterialProperties: name, opacity and textures only.
+ * (model_folder + model_name) with its MTL libraries, or a binary FBX file
+ * (a name ending in .fbx, any case; versions with 32- and 64-bit records,
+ * raw or zlib arrays), the textures they name decoded (PNG / DDS, RGB
+ * expanded to RGBA) and the sky map (model_folder + skyMap_name, Radiance
+ * HDR; "null" or NULL: none). Meshes, materials and texture slots follow
+ * assimp's OBJ and FBX imports (FBX: every vertex through its model's world
+ * and geometric transform, normals through the inverse transpose) and
+ * Material::loadMaterialProperties: name, opacity and textures only. An
+ * ASCII FBX file gives RMN_ERR_UNSUPPORTED.
  * rmn_model_desc lays it out for rmn_scene_create; the arrays stay owned by
  * the model until rmn_model_free. A file that cannot be read or parsed gives
  * RMN_ERR_INVALID_ARGUMENT (the message names file and line); a texture of

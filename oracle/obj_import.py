@@ -253,12 +253,37 @@ def load_model(model_folder: str, model_name: str, skyMap_name: str = "null") ->
         if os.path.exists(p):
             lib_mats.extend(parse_mtl(p))
     # assimp's OBJ material list: its default material first, then the MTL's
+    # (a repeated name takes its last definition), then usemtl names no MTL
+    # file defines, in order of use
     names = [DEFAULT_MATERIAL] + [m["name"] for m in lib_mats]
     by_name = {m["name"]: m for m in lib_mats}
+    index_of = {n: i for i, n in enumerate(names)}
+    indexed = []
+    for mat, pos, nrm, uv, tris in meshes:
+        if mat not in index_of:
+            index_of[mat] = len(names)
+            names.append(mat)
+        indexed.append((index_of[mat], pos, nrm, uv, tris))
+    specs = [by_name.get(n, {"name": n, "opacity": np.float32(1.0), "textures": {}}) for n in names]
+    return assemble_model(model_folder, model_name, specs, indexed, skyMap_name)
+
+
+def assemble_model(model_folder: str, model_name: str, specs: list, meshes: list,
+                   skyMap_name: str = "null") -> "scenes.Scene":
+    """The steps Model::Model takes after assimp's import, whatever the file
+    format (src/model.cpp:172-215, src/material.cpp:150-336): texture files
+    loaded once each in order of first use, a glass material row where the
+    opacity is below 0.99, vertex normals (the geometric normal where a mesh
+    has none, FixInfacingNormals where it has them), (0, 0) where a mesh has
+    no uvs, and the sky. specs: dicts with name, opacity and textures by
+    slot; meshes: (material index, positions, normals or None, uvs or None,
+    indices)."""
+    model_path = model_folder + model_name
+    names = [s["name"] for s in specs]
     cache, textures = {}, []
     mat_rows, mat_tex = [], []
-    for name in names:
-        spec = by_name.get(name, {"name": name, "opacity": np.float32(1.0), "textures": {}})
+    for spec in specs:
+        name = spec["name"]
         slots = [-1, -1, -1, -1]
         for slot in sorted(spec["textures"]):
             p = url_decode((model_folder + spec["textures"][slot]).replace("\\", "/"))
@@ -276,18 +301,10 @@ def load_model(model_folder: str, model_name: str, skyMap_name: str = "null") ->
         row[3] = 0.0  # no constant diffuse texel: white unless a texture is given
         mat_rows.append(row)
         mat_tex.append(slots)
-    index_of = {n: i for i, n in enumerate(names)}
 
     pos_l, nrm_l, uv_l, idx_l, first, mesh_mat = [], [], [], [], [0], []
     nv = 0
     for mat, pos, nrm, uv, tris in meshes:
-        if mat not in index_of:  # a usemtl name the MTL files do not define
-            index_of[mat] = len(names)
-            names.append(mat)
-            row = scenes.material()
-            row[3] = 0.0
-            mat_rows.append(row)
-            mat_tex.append([-1, -1, -1, -1])
         if nrm is None:
             a, b, c = pos[tris[:, 0]], pos[tris[:, 1]], pos[tris[:, 2]]
             g = np.cross(b - a, c - a)
@@ -305,7 +322,7 @@ def load_model(model_folder: str, model_name: str, skyMap_name: str = "null") ->
         idx_l.append(tris + nv)
         nv += pos.shape[0]
         first.append(first[-1] + tris.shape[0])
-        mesh_mat.append(index_of[mat])
+        mesh_mat.append(mat)
     if not idx_l:
         raise ValueError(f"{model_path}: no triangles")
     env = None

@@ -117,9 +117,10 @@ def load_texture(filename: str):
 
 def load_model(model_folder: str, model_name: str, skyMap_name: str = "null") -> "_scenes.Scene":
     """Model::Model(model_folder, model_name, skyMap_name) for a Wavefront
-    OBJ/MTL model, read by the library (rmn_model_read): the OBJ file
-    model_folder + model_name, its MTL libraries, the PNG/DDS textures they
-    name and the Radiance sky map model_folder + skyMap_name ("null": none),
+    OBJ/MTL or binary FBX model, read by the library (rmn_model_read): the
+    file model_folder + model_name (FBX by a .fbx name), its MTL libraries,
+    the PNG/DDS textures they name and the Radiance sky map
+    model_folder + skyMap_name ("null": none),
     as a Scene of arrays (copies). Raises ValueError for a file that cannot
     be read or parsed (the message names file and line)."""
     lib = _lib.load()

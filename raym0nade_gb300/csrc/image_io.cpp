@@ -912,6 +912,10 @@ bool read_file(const char* path, std::vector<uint8_t>& out) {
 
 namespace rmn {
 
+const char* zlib_inflate(const uint8_t* p, size_t n, std::vector<uint8_t>& out, size_t want) {
+  return zlib_decompress(p, n, out, want);
+}
+
 // zlib stream (RFC 1950) of `data`: greedy LZ77 over a 32 KiB window (hash
 // chains on 3-byte prefixes, at most kChain candidates per position, a match
 // of kNice bytes taken at once) and

@@ -452,25 +452,23 @@ rmn_material glass_material(const std::string& name) {
   return m;
 }
 
-rmn_status read_model(const std::string& folder, const std::string& name, const std::string& sky, rmn_model& M) {
-  std::vector<float> P, T, N;
-  std::vector<MeshRun> meshes;
-  std::vector<std::string> mtllibs;
-  rmn_status st = parse_obj(folder + name, P, T, N, meshes, mtllibs);
-  if (st != RMN_OK) return st;
-  std::vector<MtlSpec> lib;
-  for (const std::string& m : mtllibs)
-    if ((st = parse_mtl(folder + m, lib)) != RMN_OK) return st;
+// One mesh of the model as the importers hand it over: position, normal
+// and uv per corner (normals: all_n, else geometric normals are made; uvs:
+// all_t, else (0, 0)), triangles over the corners, the material's index.
+struct BuildMesh {
+  std::vector<float> pos, nrm, uv;
+  bool all_n = false, all_t = false;
+  std::vector<int32_t> tris;
+  int material = 0;
+};
 
-  // materials: the default one, the libraries' (a repeated name takes its
-  // last definition), then usemtl names nobody defines
-  std::vector<std::string>& names = M.material_names;
-  names.assign(1, kDefaultMaterial);
-  std::map<std::string, const MtlSpec*> by_name;
-  for (const MtlSpec& m : lib) {
-    names.push_back(m.name);
-    by_name[m.name] = &m;
-  }
+// What both importers share: the materials (their textures decoded on up to
+// 16 threads, taken in order of first use), the meshes (geometric normals
+// where a mesh has none, FixInfacingNormals where it has them) and the sky.
+rmn_status finish_model(const std::string& folder, const std::string& name, const std::vector<MtlSpec>& specs,
+                        std::vector<BuildMesh>& meshes, const std::string& sky, rmn_model& M) {
+  M.material_names.clear();
+  for (const MtlSpec& sp : specs) M.material_names.push_back(sp.name);
   // texture files in order of first use, decoded on several threads; the
   // results are taken in that order, so indices and the first error are
   // those of one-by-one loading
@@ -484,14 +482,7 @@ rmn_status read_model(const std::string& folder, const std::string& name, const 
   std::vector<TexJob> jobs;
   std::map<std::string, int> job_of;
   std::vector<std::array<int, 4>> mat_jobs;
-  std::vector<const MtlSpec*> specs;
-  std::vector<MtlSpec> defaults;
-  defaults.reserve(names.size());
-  for (const std::string& n : names) {
-    auto it = by_name.find(n);
-    if (it == by_name.end()) defaults.push_back(MtlSpec{n, 1.0f, {}});
-    const MtlSpec& spec = it != by_name.end() ? *it->second : defaults.back();
-    specs.push_back(&spec);
+  for (const MtlSpec& spec : specs) {
     std::array<int, 4> js = {-1, -1, -1, -1};
     for (const auto& kv : spec.textures) {
       std::string p = folder + kv.second;
@@ -531,53 +522,27 @@ rmn_status read_model(const std::string& folder, const std::string& name, const 
     M.texels.push_back(std::move(jobs[j].img.bytes));
     M.textures.push_back(rmn_texture{jobs[j].img.w, jobs[j].img.h, 4, nullptr});
   }
-  for (size_t i = 0; i < names.size(); ++i) {
+  for (size_t i = 0; i < specs.size(); ++i) {
     int32_t slots[4];
     for (int k = 0; k < 4; ++k) slots[k] = mat_jobs[i][k] < 0 ? -1 : tex_of[mat_jobs[i][k]];
-    M.materials.push_back(specs[i]->opacity < 0.99f ? glass_material(names[i]) : default_material());  // float test
+    M.materials.push_back(specs[i].opacity < 0.99f ? glass_material(specs[i].name) : default_material());  // float test
     M.material_textures.insert(M.material_textures.end(), slots, slots + 4);
   }
-  std::map<std::string, int> index_of;
-  for (size_t i = 0; i < names.size(); ++i) index_of[names[i]] = (int)i;
 
   M.mesh_first.assign(1, 0);
-  for (const MeshRun& mr : meshes) {
-    auto it = index_of.find(mr.mat);
-    if (it == index_of.end()) {
-      it = index_of.emplace(mr.mat, (int)names.size()).first;
-      names.push_back(mr.mat);
-      M.materials.push_back(default_material());
-      for (int k = 0; k < 4; ++k) M.material_textures.push_back(-1);
-    }
-    const size_t nc = mr.corners.size();
-    bool all_n = true, all_t = true;
-    for (const Corner& c : mr.corners) {
-      if (c.v < 0 || c.v >= (long long)(P.size() / 3))
-        return fail(RMN_ERR_INVALID_ARGUMENT, "%s%s: a face refers to a vertex that does not exist", folder.c_str(),
-                    name.c_str());
-      if (c.t >= (long long)(T.size() / 2) || c.n >= (long long)(N.size() / 3) || c.t < -1 || c.n < -1)
-        return fail(RMN_ERR_INVALID_ARGUMENT,
-                    "%s%s: a face refers to a texture coordinate or normal that does not exist", folder.c_str(),
-                    name.c_str());
-      all_n = all_n && c.n >= 0;
-      all_t = all_t && c.t >= 0;
-    }
-    std::vector<float> pos(3 * nc), nrm(3 * nc), uv(2 * nc, 0.0f);
-    for (size_t i = 0; i < nc; ++i) {
-      const Corner& c = mr.corners[i];
-      for (int k = 0; k < 3; ++k) pos[3 * i + k] = P[3 * c.v + k];
-      if (all_n)
-        for (int k = 0; k < 3; ++k) nrm[3 * i + k] = N[3 * c.n + k];
-      if (all_t)
-        for (int k = 0; k < 2; ++k) uv[2 * i + k] = T[2 * c.t + k];
-    }
-    const size_t nt = mr.tris.size() / 3;
-    if (!all_n) {  // geometric normals, written corner 0, 1, 2 of every triangle in turn
+  for (BuildMesh& mb : meshes) {
+    std::vector<float>& pos = mb.pos;
+    std::vector<float>& nrm = mb.nrm;
+    const size_t nc = pos.size() / 3;
+    nrm.resize(3 * nc, 0.0f);
+    if (!mb.all_t) mb.uv.assign(2 * nc, 0.0f);
+    const size_t nt = mb.tris.size() / 3;
+    if (!mb.all_n) {  // geometric normals, written corner 0, 1, 2 of every triangle in turn
       std::vector<float> g(3 * nt);
       for (size_t t = 0; t < nt; ++t) {
-        const float* a = &pos[3 * mr.tris[3 * t]];
-        const float* b = &pos[3 * mr.tris[3 * t + 1]];
-        const float* c = &pos[3 * mr.tris[3 * t + 2]];
+        const float* a = &pos[3 * mb.tris[3 * t]];
+        const float* b = &pos[3 * mb.tris[3 * t + 1]];
+        const float* c = &pos[3 * mb.tris[3 * t + 2]];
         const float e1[3] = {b[0] - a[0], b[1] - a[1], b[2] - a[2]};
         const float e2[3] = {c[0] - a[0], c[1] - a[1], c[2] - a[2]};
         float x = e1[1] * e2[2], y = e1[2] * e2[0], z = e1[0] * e2[1];
@@ -595,7 +560,7 @@ rmn_status read_model(const std::string& folder, const std::string& name, const 
       }
       for (int k = 0; k < 3; ++k)
         for (size_t t = 0; t < nt; ++t)
-          for (int j = 0; j < 3; ++j) nrm[3 * mr.tris[3 * t + k] + j] = g[3 * t + j];
+          for (int j = 0; j < 3; ++j) nrm[3 * mb.tris[3 * t + k] + j] = g[3 * t + j];
     } else if (nc > 0) {  // FixInfacingNormals: moved box smaller than the vertices' box -> flip
       float lo0[3], hi0[3], lo1[3], hi1[3];
       for (int k = 0; k < 3; ++k) {
@@ -621,10 +586,10 @@ rmn_status read_model(const std::string& folder, const std::string& name, const 
     const int32_t base = (int32_t)(M.positions.size() / 3);
     M.positions.insert(M.positions.end(), pos.begin(), pos.end());
     M.normals.insert(M.normals.end(), nrm.begin(), nrm.end());
-    M.uvs.insert(M.uvs.end(), uv.begin(), uv.end());
-    for (int32_t i : mr.tris) M.indices.push_back(base + i);
+    M.uvs.insert(M.uvs.end(), mb.uv.begin(), mb.uv.end());
+    for (int32_t i : mb.tris) M.indices.push_back(base + i);
     M.mesh_first.push_back(M.mesh_first.back() + (int32_t)nt);
-    M.mesh_material.push_back(it->second);
+    M.mesh_material.push_back(mb.material);
   }
   if (M.indices.empty()) return fail(RMN_ERR_INVALID_ARGUMENT, "%s%s: no triangles", folder.c_str(), name.c_str());
   for (size_t i = 0; i < M.textures.size(); ++i) M.textures[i].texels = M.texels[i].data();
@@ -644,6 +609,108 @@ rmn_status read_model(const std::string& folder, const std::string& name, const 
     }
   }
   return RMN_OK;
+}
+
+rmn_status read_obj_model(const std::string& folder, const std::string& name, const std::string& sky,
+                          rmn_model& M) {
+  std::vector<float> P, T, N;
+  std::vector<MeshRun> meshes;
+  std::vector<std::string> mtllibs;
+  rmn_status st = parse_obj(folder + name, P, T, N, meshes, mtllibs);
+  if (st != RMN_OK) return st;
+  std::vector<MtlSpec> lib;
+  for (const std::string& m : mtllibs)
+    if ((st = parse_mtl(folder + m, lib)) != RMN_OK) return st;
+
+  // materials: the default one, the libraries' (a repeated name takes its
+  // last definition), then usemtl names nobody defines, in order of use
+  std::vector<MtlSpec> specs;
+  std::map<std::string, const MtlSpec*> by_name;
+  for (const MtlSpec& m : lib) by_name[m.name] = &m;
+  std::vector<std::string> names(1, kDefaultMaterial);
+  for (const MtlSpec& m : lib) names.push_back(m.name);
+  std::map<std::string, int> index_of;
+  for (size_t i = 0; i < names.size(); ++i) index_of[names[i]] = (int)i;
+  for (const MeshRun& mr : meshes)
+    if (!index_of.count(mr.mat)) {
+      index_of.emplace(mr.mat, (int)names.size());
+      names.push_back(mr.mat);
+    }
+  for (const std::string& n : names) {
+    auto it = by_name.find(n);
+    specs.push_back(it != by_name.end() ? *it->second : MtlSpec{n, 1.0f, {}});
+  }
+
+  std::vector<BuildMesh> built;
+  for (const MeshRun& mr : meshes) {
+    const size_t nc = mr.corners.size();
+    bool all_n = true, all_t = true;
+    for (const Corner& c : mr.corners) {
+      if (c.v < 0 || c.v >= (long long)(P.size() / 3))
+        return fail(RMN_ERR_INVALID_ARGUMENT, "%s%s: a face refers to a vertex that does not exist", folder.c_str(),
+                    name.c_str());
+      if (c.t >= (long long)(T.size() / 2) || c.n >= (long long)(N.size() / 3) || c.t < -1 || c.n < -1)
+        return fail(RMN_ERR_INVALID_ARGUMENT,
+                    "%s%s: a face refers to a texture coordinate or normal that does not exist", folder.c_str(),
+                    name.c_str());
+      all_n = all_n && c.n >= 0;
+      all_t = all_t && c.t >= 0;
+    }
+    BuildMesh mb;
+    mb.pos.resize(3 * nc);
+    mb.nrm.resize(3 * nc);
+    mb.uv.assign(2 * nc, 0.0f);
+    for (size_t i = 0; i < nc; ++i) {
+      const Corner& c = mr.corners[i];
+      for (int k = 0; k < 3; ++k) mb.pos[3 * i + k] = P[3 * c.v + k];
+      if (all_n)
+        for (int k = 0; k < 3; ++k) mb.nrm[3 * i + k] = N[3 * c.n + k];
+      if (all_t)
+        for (int k = 0; k < 2; ++k) mb.uv[2 * i + k] = T[2 * c.t + k];
+    }
+    mb.all_n = all_n;
+    mb.all_t = true;  // missing uvs are (0, 0) already
+    mb.tris = mr.tris;
+    mb.material = index_of[mr.mat];
+    built.push_back(std::move(mb));
+  }
+  return finish_model(folder, name, specs, built, sky, M);
+}
+
+// A binary FBX model (fbx.cpp) through the same material, normal and sky
+// steps.
+rmn_status read_fbx_model(const std::string& folder, const std::string& name, const std::string& sky,
+                          rmn_model& M) {
+  std::vector<rmn::FbxMesh> fm;
+  std::vector<rmn::FbxMaterial> fmats;
+  rmn_status st = rmn::read_fbx(folder + name, fm, fmats);
+  if (st != RMN_OK) return st;
+  std::vector<MtlSpec> specs;
+  for (const rmn::FbxMaterial& m : fmats) {
+    MtlSpec sp{m.name, m.opacity, {}};
+    for (int k = 0; k < 4; ++k)
+      if (!m.textures[k].empty()) sp.textures[k] = m.textures[k];
+    specs.push_back(sp);
+  }
+  std::vector<BuildMesh> built;
+  for (rmn::FbxMesh& m : fm) {
+    BuildMesh mb;
+    mb.pos = std::move(m.pos);
+    mb.nrm = std::move(m.nrm);
+    mb.uv = std::move(m.uv);
+    mb.all_n = m.has_nrm;
+    mb.all_t = m.has_uv;
+    mb.tris = std::move(m.tris);
+    mb.material = m.material;
+    built.push_back(std::move(mb));
+  }
+  return finish_model(folder, name, specs, built, sky, M);
+}
+
+rmn_status read_model(const std::string& folder, const std::string& name, const std::string& sky, rmn_model& M) {
+  std::string ext = name.size() >= 4 ? lower(name.substr(name.size() - 4)) : "";
+  if (ext == ".fbx") return read_fbx_model(folder, name, sky, M);
+  return read_obj_model(folder, name, sky, M);
 }
 
 }  // namespace

@@ -70,8 +70,29 @@ struct DecodedImage {
 // Decode `path` as RMN_IMAGE_PNG / _DDS / _HDR (the size only with header_only).
 rmn_status decode_image_file(const char* path, int kind, bool header_only, DecodedImage& img);
 
+// A binary FBX model as assimp's import with PreTransformVertices and
+// Triangulate leaves it (fbx.cpp): per mesh (a geometry's polygons of one
+// material) the world-space position, normal and uv of every polygon
+// corner, the fan triangles over the corners and the material's index; per
+// material its name, opacity and texture file names by RMN_TEX_* slot.
+struct FbxMesh {
+  std::vector<float> pos, nrm, uv;
+  bool has_nrm = false, has_uv = false;
+  std::vector<int32_t> tris;
+  int material = -1;
+};
+struct FbxMaterial {
+  std::string name;
+  float opacity = 1.0f;
+  std::string textures[4];
+};
+rmn_status read_fbx(const std::string& path, std::vector<FbxMesh>& meshes, std::vector<FbxMaterial>& materials);
+
 // A zlib stream of n bytes (image_io.cpp): LZ77 + dynamic Huffman blocks.
 std::vector<uint8_t> zlib_compress(const uint8_t* data, size_t n);
+// Inflates a zlib stream of n bytes that must hold exactly `want` bytes
+// (image_io.cpp); nullptr, or what is wrong with the stream.
+const char* zlib_inflate(const uint8_t* p, size_t n, std::vector<uint8_t>& out, size_t want);
 
 // CRC-32 of PNG chunks (ISO 3309 polynomial), shared by the writer and the reader.
 uint32_t png_crc32(uint32_t crc, const uint8_t* p, size_t n);
