@@ -50,14 +50,14 @@ FALLBACK_HBM_GBS = 6800.0
 # shadow queues) of one batch64 render at the launch configurations given
 # beside them, summed from ncu captures (metrics dram__bytes_read.sum,
 # dram__bytes_write.sum, lts__t_bytes.sum) of
-#   python bench.py --profile-case batch --slots 2 --pool 8388608 --lanes L
+#   python bench.py --profile-case batch --slots 2 --pool 8388608 --lanes L --stack 27
 # (ncu cannot run inside the timed region). The line takes the capture of
 # the timed configuration, and says so, or else the first and says that.
 BATCH64_TRAVERSAL_BYTES = [
-    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 3, "stack_entries": 23, "ray_order": 0},
-     "dram": 157.9e9, "l2": 2359.7e9},
-    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 2, "stack_entries": 23, "ray_order": 0},
-     "dram": 172.1e9, "l2": 2388.7e9},
+    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 2, "stack_entries": 27, "ray_order": 0},
+     "dram": 170.9e9, "l2": 2386.2e9},
+    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 3, "stack_entries": 27, "ray_order": 0},
+     "dram": 156.9e9, "l2": 2362.9e9},
 ]
 
 
@@ -723,9 +723,11 @@ def run_gpu(args, rank, world, dist):
               "copy_rate": l2_peak, "frac_of_copy_rate": l2_gbs / l2_peak, "same_config": same,
               "source": "ncu lts__t_bytes.sum over the same launches; copy_rate: a device copy between two "
                         "L2-resident 24 MiB buffers, measured here"}
-    limiter = ("instruction issue under SIMT divergence: in steady state (ncu) the traversal uses 71-78 % of its "
-               "issue slots with 10-11 of 32 lanes active per instruction; its measured DRAM traffic is a small "
-               "share of the algorithmic bytes (L1/L2 hits) and neither DRAM nor L2 runs near its rate")
+    limiter = ("instruction issue and dependent-load latency: in steady state (ncu) the traversal uses 66-69 % of "
+               "its issue slots with 17.7-18.6 of 32 lanes active per instruction (warp-cooperative leaves), "
+               "stalled mostly on L1/L2 loads (long scoreboard 3.3 per issue) and fixed-latency dependencies "
+               "(2.9); its measured DRAM traffic is a small share of the algorithmic bytes (L1/L2 hits) and "
+               "neither DRAM nor L2 runs near its rate")
     base, _ = cpu_baseline(insts) if args.cpu_baseline else (None, None)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,

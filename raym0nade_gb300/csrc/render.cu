@@ -878,19 +878,19 @@ __global__ void seed_kernel(Queues Q, Ctl* ctl, int W) {
   if (i == 0) ctl->q[1].sd = (unsigned)W;
 }
 
-constexpr int kFetchBudget = 16;  // node visits between refill checks
-
 // Persistent traversal of one queue. Each lane owns one queued worker's ray;
-// every 16 node visits, lanes whose ray is answered take the next queue
-// entries (one warp-aggregated atomic), so a warp does not wait for its
-// longest ray. The rays of a batch belong to different scenes; each lane
-// traverses its own job's BVH. ALPHA: the batch has scenes with alpha-tested
+// after every round of inner-node steps and warp-cooperative leaf tests
+// (trace.cuh: coop_nodes, coop_leaves), lanes whose ray is answered take the
+// next queue entries (one warp-aggregated atomic), so a warp does not wait
+// for its longest ray. The rays of a batch belong to different scenes; each
+// lane traverses its own job's BVH, and the leaf phase tests a triangle
+// against its owner's scene. ALPHA: the batch has scenes with alpha-tested
 // materials, whose queries retry past cut-away texels (a separate build, so
 // the common case keeps its register budget). STACK: the shared stack's
 // entries (RMN_STACK, or RMN_STACK_SMALL for batches of shallower trees, with
-// 9 instead of 8 blocks per SM).
+// 8 instead of 7 blocks per SM).
 template <bool SHADOW, bool COUNT, bool ALPHA, int STACK>
-__global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+__global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) qtrace_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
                                                      int par, int* status, Counters* ctr) {
   const int lane = threadIdx.x & 31;
   const unsigned lt = (1u << lane) - 1u;
@@ -908,10 +908,15 @@ __global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) qtrace_
   int jb = 0;        // the lane's job
   bool alpha = false;
   // the deferred-child stack in shared memory (launched with 128 threads)
+  // and the leaf-phase keys of each warp
   __shared__ int2 sstack[STACK * 128];
+  __shared__ unsigned long long skeys[128];
   TravT<SharedStackN<STACK>> t;
   t.stack.base = sstack + threadIdx.x;
-  DevScene s;
+  t.ti = t.te = 0;
+  unsigned long long* keys = skeys + (threadIdx.x & ~31);
+  const DevNode* nodes = nullptr;  // the lane's job's tree and triangles
+  const float4* tri = nullptr;
   TraceCounters tc = {0, 0, 0, 0, 0};
   for (;;) {
     unsigned need = __ballot_sync(0xffffffffu, !active && !retired);
@@ -927,16 +932,19 @@ __global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) qtrace_
           const int wk = (!SHADOW || w >= 0) ? w : (~w) / kDirectBatch;
           float4 o = P.ro[wk], d = (!SHADOW || w >= 0) ? P.rd[wk] : P.drd[~w];
           jb = worker_job(P, wk);
-          s = jobs[jb].s;
-          alpha = ALPHA && s.has_alpha != 0;
+          const DevScene& js = jobs[jb].s;
+          nodes = js.nodes;
+          tri = js.tri;
+          alpha = ALPHA && js.has_alpha != 0;
+          const int root = js.root;
           r = make_tray(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
           tmin = o.w;
           if (SHADOW) {
             aim = d.w;
-            trav_begin(s, t, aim + RMN_EPS);  // HitRecord(eps, aimDepth + eps)
+            trav_begin(root, t, aim + RMN_EPS);  // HitRecord(eps, aimDepth + eps)
             if (COUNT) tc.shadow++;
           } else {
-            trav_begin(s, t, d.w);
+            trav_begin(root, t, d.w);
             if (COUNT) tc.closest++;
           }
           searches = 0;
@@ -947,9 +955,9 @@ __global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) qtrace_
       }
     }
     if (__ballot_sync(0xffffffffu, active) == 0) break;
-    if (!active) continue;
-    int st = trav_run<SHADOW, COUNT>(s, r, tmin, aim, t, kFetchBudget, &tc, !alpha);
-    if (st == 0) continue;
+    int st = coop_nodes<COUNT>(nodes, r, tmin, t, active, kCoopSteps, &tc);
+    if (coop_leaves<SHADOW, false>(tri, r, tmin, aim, t, !alpha, keys)) st = 1;
+    if (!active || st == 0) continue;
     // Model::rayHit / rayHit_test retry past cut-away texels (the texture
     // tables are read through the job table, not kept in registers)
     if (ALPHA && st == 1 && alpha && !(SHADOW && t.tmax >= aim) &&

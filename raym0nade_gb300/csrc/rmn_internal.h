@@ -64,11 +64,16 @@ RMN_HD float3 mix3(float3 x, float3 y, float a) { return x * (1.0f - a) + y * a;
 #define RMN_LEAF_MAX 10               // LeafBagSize, src/bvh.cpp:16
 // traversal stack entries: trees up to depth 26 (median splits of < 2^27
 // triangles stay below 26 levels); 27 x 8 B x 128 threads of shared memory
-// lets 8 persistent traversal blocks share an SM
+// (with the leaf keys) lets 7 persistent traversal blocks share an SM
 #define RMN_STACK 27
 // A shallower stack for batches whose trees are at most RMN_STACK_SMALL - 1
 // deep: less shared memory, one more persistent traversal block per SM.
 #define RMN_STACK_SMALL 23
+// Persistent traversal kernels (trace.cuh, warp-cooperative leaves): inner-
+// node steps per round, and blocks per SM for a shared stack of S entries
+// (S * 1 KiB of stack plus 1 KiB of leaf keys per 128-thread block).
+constexpr int kCoopSteps = 4;
+#define RMN_COOP_BLOCKS(S) ((S) <= RMN_STACK_SMALL ? 8 : 7)
 
 // ------------------------------------------------------------ layout ------
 // Two-child node (64 B): the boxes of both children plus their references,

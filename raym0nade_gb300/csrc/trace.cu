@@ -5,22 +5,21 @@
 // hits as the reference does; other intervals are bare BVH queries.
 //
 // Work distribution: a persistent grid (a multiple of the SM count). Each
-// lane owns one ray at a time; every 16 node visits the lanes whose ray is
-// answered take new rays from a global counter (one warp-aggregated atomic),
-// so a warp no longer waits for its longest ray (Aila & Laine, "Understanding
-// the efficiency of ray traversal on GPUs", HPG 2009: persistent threads with
-// dynamic ray fetch).
+// lane owns one ray at a time; after every round of inner-node steps and
+// warp-cooperative leaf tests (trace.cuh, coop_nodes / coop_leaves) the
+// lanes whose ray is answered take new rays from a global counter (one
+// warp-aggregated atomic), so a warp no longer waits for its longest ray
+// (Aila & Laine, "Understanding the efficiency of ray traversal on GPUs",
+// HPG 2009: persistent threads with dynamic ray fetch).
 #include "rmn_host.h"
 #include "trace.cuh"
 
 namespace {
 
-constexpr int kFetchBudget = 16;  // node visits between refill checks
-
 // STACK: shared stack entries (RMN_STACK_SMALL for trees that fit it: one
 // more block per SM).
 template <bool SHADOW, int STACK>
-__global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) trace_kernel(DevScene s, const float4* __restrict__ rays, int64_t n,
+__global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) trace_kernel(DevScene s, const float4* __restrict__ rays, int64_t n,
                                                     float4* __restrict__ hits, uint8_t* __restrict__ occ,
                                                     unsigned long long* __restrict__ next, int* status) {
   const int lane = threadIdx.x & 31;
@@ -32,9 +31,13 @@ __global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) trace_k
   int searches = 0;
   bool retry = false;
   // the deferred-child stack in shared memory (launched with 128 threads)
+  // and the leaf-phase keys of each warp
   __shared__ int2 sstack[STACK * 128];
+  __shared__ unsigned long long skeys[128];
   TravT<SharedStackN<STACK>> t;
   t.stack.base = sstack + threadIdx.x;
+  t.ti = t.te = 0;
+  unsigned long long* keys = skeys + (threadIdx.x & ~31);
   for (;;) {
     // lanes without a ray take the next ones from the batch
     unsigned need = __ballot_sync(0xffffffffu, !active && !retired);
@@ -68,9 +71,9 @@ __global__ void __launch_bounds__(128, STACK <= RMN_STACK_SMALL ? 9 : 8) trace_k
       }
     }
     if (__ballot_sync(0xffffffffu, active) == 0) return;
-    if (!active) continue;
-    int st = trav_run<SHADOW, false>(s, r, tmin, aim, t, kFetchBudget, nullptr, !retry);
-    if (st == 0) continue;
+    int st = coop_nodes<false>(s.nodes, r, tmin, t, active, kCoopSteps, nullptr);
+    if (coop_leaves<SHADOW, true>(s.tri, r, tmin, aim, t, !retry, keys)) st = 1;
+    if (!active || st == 0) continue;
     if (st == -2) atomicExch(status, (int)rmn::kDevStackOverflow);
     else if (retry && !(SHADOW && t.tmax >= aim) && alpha_again(s, r, t, tmin, restart, searches, !SHADOW)) continue;
     if (SHADOW) {

@@ -111,17 +111,23 @@ struct TravT {
   int hit;     // leaf-order triangle index of the closest hit so far, -1 none
   int ti, te;  // triangles [ti, te) of the current leaf still to test
   float tmax;
+  bool pop;    // cooperative traversal: the next step pops the stack
   Stack stack;
 };
 using Trav = TravT<LocalStack>;
 
 template <class Stack>
-RMN_D void trav_begin(const DevScene& s, TravT<Stack>& t, float tmax) {
-  t.cur = s.root;
+RMN_D void trav_begin(int root, TravT<Stack>& t, float tmax) {
+  t.cur = root;
   t.sp = 0;
   t.hit = -1;
   t.ti = t.te = 0;
   t.tmax = tmax;
+  t.pop = false;
+}
+template <class Stack>
+RMN_D void trav_begin(const DevScene& s, TravT<Stack>& t, float tmax) {
+  trav_begin(s.root, t, tmax);
 }
 
 // Runs up to `budget` steps; a step is one inner node (both child boxes) or
@@ -203,6 +209,191 @@ RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav
       }
     }
   }
+}
+
+
+// ------------------------------------------------ warp-cooperative leaves
+// The persistent traversal kernels split each round in two warp-wide
+// phases. (1) Every lane takes up to `steps` inner-node steps exactly as
+// trav_run does (same boxes, same near-first order, same deferred pops),
+// stopping when it reaches a leaf. (2) The triangles of all the warp's
+// pending leaves are spread over the 32 lanes, 32 at a time, and each ray
+// keeps the smallest (t, leaf-order index) among its leaf's triangles with
+// t_min < t < t_max: what testing the leaf in order with a strict t < t_max
+// gives (the first of equal distances wins). The next round pops the stack
+// with that t_max, as the recursion returns after the leaf. So every ray
+// visits the nodes and leaves it visits in trav_run and ends with the same
+// hit and distance, while a leaf's 6-10 triangles no longer occupy one lane
+// for 6-10 steps with the other lanes idle or on another branch. An
+// occlusion query with `early` is answered by the leaf that holds a hit
+// nearer than aim (trav_run stops at that hit inside the leaf: the same
+// answer).
+
+// Order of (t, index) as an unsigned key: t's bits made monotone (zero's
+// sign dropped, as float comparison ignores it), the index below.
+RMN_D unsigned long long leaf_key(float t, int tri) {
+  unsigned u = __float_as_uint(t + 0.0f);
+  u = (u & 0x80000000u) ? ~u : (u | 0x80000000u);
+  return ((unsigned long long)u << 32) | (unsigned)tri;
+}
+RMN_D float leaf_key_t(unsigned long long k) {
+  unsigned u = (unsigned)(k >> 32);
+  u = (u & 0x80000000u) ? (u & 0x7fffffffu) : ~u;
+  return __uint_as_float(u);
+}
+
+// Phase 1, called by all 32 lanes of a warp; `go`: the lane has a query in
+// flight. Returns 1 when the lane's query is answered (its stack ran out),
+// -2 on stack overflow, 0 otherwise (a leaf pending: t.ti < t.te, or steps
+// left over).
+template <bool COUNT, class Stack>
+RMN_D int coop_nodes(const DevNode* __restrict__ nodes, const TRay& r, float tmin, TravT<Stack>& t, bool go,
+                     int steps, TraceCounters* cnt) {
+  int res = 0;
+#pragma unroll 1
+  for (int step = 0; step < steps; ++step) {
+    const bool g = go && res == 0 && t.ti >= t.te;
+    if (!__any_sync(0xffffffffu, g)) break;
+    if (!g) continue;
+    if (t.pop) {
+      t.pop = false;
+      for (;;) {
+        if (t.sp == 0) {
+          res = 1;
+          break;
+        }
+        --t.sp;
+        const int2 e = t.stack.get(t.sp);
+        if (__int_as_float(e.y) < t.tmax) {
+          t.cur = e.x;
+          break;
+        }
+      }
+      if (res) continue;
+    }
+    if (t.cur >= 0) {
+      const DevNode* n = nodes + t.cur;
+      float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
+      int4 D = __ldg(&n->d);
+      if (COUNT) cnt->inner++;
+      float tl0, tl1;
+      bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, t.tmax, tl0);
+      bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, t.tmax, tl1);
+      int nref, fref;
+      bool hn, hf;
+      float tlf;
+      if (tl0 < tl1) {
+        nref = D.x; hn = h0; fref = D.y; hf = h1; tlf = tl1;
+      } else {
+        nref = D.y; hn = h1; fref = D.x; hf = h0; tlf = tl0;
+      }
+      if (hn) {
+        if (hf) {
+          if (t.sp >= Stack::kCap) {
+            res = -2;
+            continue;
+          }
+          t.stack.put(t.sp, make_int2(fref, __float_as_int(tlf)));
+          ++t.sp;
+        }
+        t.cur = nref;
+      } else if (hf && tlf < t.tmax) {
+        t.cur = fref;
+      } else {
+        t.pop = true;
+        continue;
+      }
+    }
+    if (t.cur < 0) {  // a leaf: its triangles wait for phase 2, then a pop
+      const int x = ~t.cur;
+      const int count = x & 15;
+      if (COUNT) { cnt->leaves++; cnt->tris += count; }
+      if (count > 0) {
+        t.ti = x >> 4;
+        t.te = t.ti + count;
+      }
+      t.pop = true;
+    }
+  }
+  return res;
+}
+
+// Phase 2, called by all 32 lanes of a warp. `tri`: the lane's triangle
+// records (SAME_TRI: one scene for the whole warp, so its pointer is not
+// exchanged); `keys`: 32 entries of shared memory for this warp. Clears the
+// pending leaves; returns true for a lane whose occlusion query (ANY with
+// `early`) is answered.
+template <bool ANY, bool SAME_TRI, class Stack>
+RMN_D bool coop_leaves(const float4* __restrict__ tri, const TRay& r, float tmin, float aim, TravT<Stack>& t,
+                       bool early, unsigned long long* keys) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int cnt = t.ti < t.te ? t.te - t.ti : 0;
+  if (!__any_sync(FULL, cnt > 0)) return false;
+  int incl = cnt;  // inclusive prefix sum of the lanes' triangle counts
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int v = __shfl_up_sync(FULL, incl, off);
+    if (lane >= off) incl += v;
+  }
+  const int total = __shfl_sync(FULL, incl, 31);
+  const int excl = incl - cnt;
+  keys[lane] = ~0ull;
+  __syncwarp();
+#pragma unroll 1
+  for (int base = 0; base < total; base += 32) {
+    const int k = base + lane;
+    // owner: the first lane whose inclusive count exceeds k
+    int lo = 0;
+#pragma unroll
+    for (int st = 16; st >= 1; st >>= 1) {
+      const int v = __shfl_sync(FULL, incl, lo + st - 1);
+      if (v <= k) lo += st;
+    }
+    const int ow = min(lo, 31);
+    const int first = __shfl_sync(FULL, t.ti, ow) - __shfl_sync(FULL, excl, ow);
+    TRay q;
+    q.o.x = __shfl_sync(FULL, r.o.x, ow);
+    q.o.y = __shfl_sync(FULL, r.o.y, ow);
+    q.o.z = __shfl_sync(FULL, r.o.z, ow);
+    q.d.x = __shfl_sync(FULL, r.d.x, ow);
+    q.d.y = __shfl_sync(FULL, r.d.y, ow);
+    q.d.z = __shfl_sync(FULL, r.d.z, ow);
+    const float qmin = __shfl_sync(FULL, tmin, ow);
+    const float qmax = __shfl_sync(FULL, t.tmax, ow);
+    const float4* qtri = tri;
+    if (!SAME_TRI) {
+      const unsigned long long p = reinterpret_cast<unsigned long long>(tri);
+      const unsigned lo32 = __shfl_sync(FULL, (unsigned)p, ow), hi32 = __shfl_sync(FULL, (unsigned)(p >> 32), ow);
+      qtri = reinterpret_cast<const float4*>(((unsigned long long)hi32 << 32) | lo32);
+    }
+    if (k < total) {
+      const int i = first + k;
+      const float4* tp = qtri + 3 * i;
+      float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+      const float th = tri_t(q, f3(a), f3(b), f3(c), b.w);
+      if (qmin < th && th < qmax) atomicMin(&keys[ow], leaf_key(th, i));
+    }
+  }
+  __syncwarp();
+  bool answered = false;
+  if (cnt > 0) {
+    const unsigned long long kk = keys[lane];
+    if (kk != ~0ull) {
+      t.hit = (int)(unsigned)(kk & 0xffffffffu);
+      float th = leaf_key_t(kk);
+      if (th == 0.0f) {  // a zero distance keeps the sign its own test gives
+        const float4* tp = tri + 3 * t.hit;
+        float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+        th = tri_t(r, f3(a), f3(b), f3(c), b.w);
+      }
+      t.tmax = th;
+      answered = ANY && early && th < aim;
+    }
+    t.ti = t.te;
+  }
+  __syncwarp();
+  return answered;
 }
 
 // One whole query without the alpha retry (scenes without alpha-tested

@@ -74,6 +74,31 @@ def test_closest_bounded_interval(port):
     assert np.array_equal(f, pf) and np.array_equal(t, pt)
 
 
+def test_closest_exact_ties_and_zero_distances(port):
+    """Every triangle twice (same vertices: every hit an exact tie, the first
+    in leaf order wins), rays aimed at centroids, and rays starting on a
+    triangle with t_min < 0 (distances of +-0): ids and t bit-identical to
+    the oracle, whichever lanes test a leaf's triangles."""
+    s = scenes.random_soup(4000, 71)
+    s.indices = np.concatenate([s.indices, s.indices[::-1]]).astype(np.int32)
+    s.mesh_first = np.array([0, s.indices.shape[0]], np.int32)
+    rng = np.random.default_rng(72)
+    cen = s.positions[s.indices].mean(1).astype(np.float32)
+    n = 60000
+    rays = scenes.random_rays(n, 73)
+    tgt = cen[rng.integers(0, cen.shape[0], n)]
+    d = tgt.astype(np.float64) - rays[:, 0:3]
+    rays[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    z = n // 4  # origins on a centroid, t_min -1
+    rays[:z, 0:3] = tgt[:z]
+    rays[:z, 3] = np.float32(-1.0)
+    m = api.Model(s)
+    f, t, _ = gpu_closest(m, rays)
+    pf, pt, _ = port.scene(s).trace_closest(rays)
+    assert np.array_equal(f, pf) and np.array_equal(t.view(np.int32), pt.view(np.int32))
+    assert (pf >= 0).mean() > 0.9 and (pt[:z] == 0).any()
+
+
 def test_shadow_matches_oracle(port):
     soup = tie_soup(20000, 43)
     sr = scenes.random_rays(200000, 44, shadow=True)
