@@ -14,11 +14,12 @@
 //     jitter, as the reference), closest hit, hit shading -> G-buffer.
 //  2. per iteration, until no worker is left, over a pool of W workers
 //     (path state in HBM, structure of arrays):
-//     shade_kernel, nee_kernel, slot_kernel -- the integrator's logic, split
-//                        by phase so that each kernel runs over a compacted
-//                        list of the workers in its phase (see below); every
-//                        worker ends the iteration with one ray queued or
-//                        retired;
+//     shade_kernel, nee_kernel, slot_kernel, light_kernel, path_kernel --
+//                        the integrator's logic, split by phase so that each
+//                        kernel runs over a compacted list of the workers in
+//                        its phase (see below); a worker ends the iteration
+//                        with a ray queued, retired, or (rarely) handed to
+//                        the next iteration's slot_kernel;
 //     qtrace_kernel<closest>, qtrace_kernel<shadow> -- persistent traversal
 //                        of the ray queues with per-lane dynamic ray fetch.
 //     Traversal thus runs at the occupancy of a 64-register kernel, and the
@@ -68,6 +69,7 @@ struct QLen {
   unsigned int c, sn;           // ray queues: closest, shadow
   unsigned int sd, nw;          // workers waiting for first-vertex / NEE shadow answers
   unsigned int nee, slot;       // hand-offs to nee_kernel / slot_kernel within the iteration
+  unsigned int light, path;     // hand-offs from slot_kernel to light_kernel / path_kernel
   unsigned int c_next, s_next;  // fetch cursors of the trace kernels
 };
 // Control words of one lane (an independent wavefront over its own share of
@@ -90,6 +92,8 @@ struct Queues {
   int* nw[2];  // workers waiting for their terminating vertex's light samples
   int* nee;
   int* slot;
+  int* light;
+  int* path;
 };
 
 // Worker pool in HBM (structure of arrays).
@@ -343,7 +347,7 @@ __device__ __forceinline__ T agg_inc(T* ctr) {
 
 __device__ __forceinline__ void push(int* q, unsigned int* qn, int w) { q[agg_inc(qn)] = w; }
 
-// The logic of one iteration runs as three kernels, each over a compacted
+// The logic of one iteration runs as five kernels, each over a compacted
 // list of the workers in its phase, so a warp executes one phase's code:
 //   shade_kernel  closest-hit answers (sampleRay's body): emit the sky or an
 //                 emitter, start the terminating vertex's light samples, or
@@ -352,9 +356,11 @@ __device__ __forceinline__ void push(int* q, unsigned int* qn, int w) { q[agg_in
 //                 workers shade_kernel handed over: emit, then draw the next
 //                 light sample (shadow queue) until the vertex is done;
 //   slot_kernel   shadow answers of first-vertex light samples and the
-//                 workers whose slot ended in the two kernels before: start
-//                 the next slot (fetching units) until one queues a ray, or
-//                 retire when no unit is left.
+//                 workers whose slot ended in the two kernels before: fetch
+//                 units until one has a slot left (or retire when no unit is
+//                 left), and hand the worker on by the kind of that slot:
+//   light_kernel  a batch of first-vertex light samples (shadow queue);
+//   path_kernel   the first bounce of an indirect path (closest-hit queue).
 // Ray queues are double-buffered by iteration parity: the queues filled in
 // iteration i are traced in iteration i and consumed in iteration i + 1.
 
@@ -725,15 +731,27 @@ __device__ __forceinline__ void unit_of_fetch(const Params& p, long long local, 
   }
 }
 
-template <bool COUNT>
+// The slot hand-off, in three kernels so that each warp runs one kind of
+// work with the registers and code of that kind alone:
+//  * slot_kernel: workers whose slot ended (from shade / nee) and workers
+//    whose first-vertex light samples were answered (the iteration before)
+//    -- adds the answers, fetches units until one has a slot left, and
+//    hands the worker to light_kernel (its next slot is a light-sample slot)
+//    or path_kernel;
+//  * light_kernel: up to kDirectBatch light-sample slots of the unit (the
+//    shadow rays queued, the worker waits for their answers);
+//  * path_kernel: the first bounce of the unit's next path slot (a closest-
+//    hit ray queued).
+// A light batch that queues no ray, or path slots that all end at the first
+// vertex, leave the worker to the next iteration's slot_kernel. Results do
+// not depend on these hand-offs: every slot draws from its own stream and
+// adds into its own unit's record.
 __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jobs, int njobs, Pool P, Queues Q,
                                                       Ctl* ctl, unsigned long long* next_unit, int par,
-                                                      long long total_units, float4* __restrict__ parts,
-                                                      Counters* ctr) {
+                                                      long long total_units, float4* __restrict__ parts) {
   QLen* out = &ctl->q[par];
   const unsigned a = ctl->q[par ^ 1].sd, n = a + out->slot;
   const int* in = Q.sd[par ^ 1];
-  unsigned long long slots_done = 0;
   for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
     const int w = idx < a ? in[idx] : Q.slot[idx - a];
     int4 ph, un;
@@ -765,8 +783,8 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
       un.z += dk.x;
       phase = PH_SLOT;
     }
-    // Start slots until one queues a ray; every pass advances the slot or
-    // takes a new unit, so the loop ends within the units of the batch.
+    // fetch units until one has a slot left; every pass takes a new unit,
+    // so the loop ends within the units of the batch
     for (;;) {
       if (phase == PH_FETCH) {
         unsigned long long u = agg_inc(next_unit);
@@ -801,45 +819,95 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
         phase = PH_FETCH;
         continue;
       }
-      const Params& p = J->p;
-      const DevScene& s = J->s;
-      Surf g = load_first_vertex(*J, un.y);
-      if (un.z < p.spp_d) {
-        // sampleDirectLightFromFirstIntersection, src/render.cpp:425-437:
-        // up to kDirectBatch consecutive light-sample slots at once, each
-        // from its own stream; the samples without a shadow ray add nothing
-        const int c = min(min(un.w, p.spp_d) - un.z, kDirectBatch);
-        if (COUNT) slots_done += (unsigned long long)c;
-        float3 Vd = -norm3(g.pos - p.pos);
-        float lwt[8];
-        float tot = 0.0f;
-        int n = 0;
-        if (!(len3(g.emis) > 0.0f) && (s.sky_w != 0 || light_weights(s, g, Vd, lwt, tot))) {
-          for (int k = 0; k < c; ++k) {
-            RmnRng rk = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)(un.z + k));
-            float3 dir;
-            float aim;
-            LSample ls;
-            if (!light_gen(s, g, Vd, lwt, tot, p.spp_d, rk, dir, aim, ls)) continue;
-            const size_t rid = (size_t)w * kDirectBatch + n++;
-            P.drd[rid] = make_float4(dir.x, dir.y, dir.z, aim);
-            P.dpend[2 * rid] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
-            P.dpend[2 * rid + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
-          }
-        }
-        if (n == 0) {
-          un.z += c;
-          continue;
-        }
-        P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
-        P.dk[w] = make_int2(c, n);
-        push_rays(Q.sn[par], &out->sn, w, n);
-        phase = PH_WAIT_DIRECT;
-        break;
+      break;
+    }
+    store_worker(P, w, ph, phase, rng, un, uid);
+    if (phase == PH_DONE) continue;
+    if (un.z < J->p.spp_d) push(Q.light, &out->light, w);
+    else push(Q.path, &out->path, w);
+  }
+}
+
+// sampleDirectLightFromFirstIntersection, src/render.cpp:425-437: up to
+// kDirectBatch consecutive light-sample slots of the worker's unit at once,
+// each from its own stream; the samples without a shadow ray add nothing.
+template <bool COUNT>
+__global__ void __launch_bounds__(128, 8) light_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+                                                       int par, Counters* ctr) {
+  QLen* out = &ctl->q[par];
+  const unsigned n = out->light;
+  unsigned long long slots_done = 0;
+  for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const int w = Q.light[idx];
+    int4 ph, un;
+    long long uid;
+    load_worker(P, w, ph, un, uid);
+    const Job* J = &jobs[un.x];
+    const Params& p = J->p;
+    const DevScene& s = J->s;
+    RmnRng rng;
+    rng.key = 0;
+    rng.ctr = (unsigned)ph.y;
+    Surf g = load_first_vertex(*J, un.y);
+    const int c = min(min(un.w, p.spp_d) - un.z, kDirectBatch);
+    if (COUNT) slots_done += (unsigned long long)c;
+    float3 Vd = -norm3(g.pos - p.pos);
+    float lwt[8];
+    float tot = 0.0f;
+    int nr = 0;
+    if (!(len3(g.emis) > 0.0f) && (s.sky_w != 0 || light_weights(s, g, Vd, lwt, tot))) {
+      for (int k = 0; k < c; ++k) {
+        RmnRng rk = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)(un.z + k));
+        float3 dir;
+        float aim;
+        LSample ls;
+        if (!light_gen(s, g, Vd, lwt, tot, p.spp_d, rk, dir, aim, ls)) continue;
+        const size_t rid = (size_t)w * kDirectBatch + nr++;
+        P.drd[rid] = make_float4(dir.x, dir.y, dir.z, aim);
+        P.dpend[2 * rid] = make_float4(ls.bsdf.x, ls.bsdf.y, ls.bsdf.z, ls.weight);
+        P.dpend[2 * rid + 1] = make_float4(ls.light.x, ls.light.y, ls.light.z, 0.0f);
       }
+    }
+    int phase;
+    if (nr == 0) {
+      un.z += c;  // nothing to wait for: the next iteration's slot_kernel goes on
+      phase = PH_SLOT;
+    } else {
+      P.ro[w] = make_float4(g.pos.x, g.pos.y, g.pos.z, RMN_EPS);
+      P.dk[w] = make_int2(c, nr);
+      push_rays(Q.sn[par], &out->sn, w, nr);
+      phase = PH_WAIT_DIRECT;
+    }
+    store_worker(P, w, ph, phase, rng, un, uid);
+    push(Q.sd[par], &out->sd, w);
+  }
+  if (COUNT && slots_done) atomicAdd(&ctr->slots, slots_done);
+}
+
+// sampleIndirectLightFromFirstIntersection, src/render.cpp:314-423: the
+// first bounce of the unit's next path slot that has one.
+template <bool COUNT>
+__global__ void __launch_bounds__(128, 8) path_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+                                                      int par, Counters* ctr) {
+  QLen* out = &ctl->q[par];
+  const unsigned n = out->path;
+  unsigned long long slots_done = 0;
+  for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const int w = Q.path[idx];
+    int4 ph, un;
+    long long uid;
+    load_worker(P, w, ph, un, uid);
+    const Job* J = &jobs[un.x];
+    const Params& p = J->p;
+    const DevScene& s = J->s;
+    RmnRng rng;
+    rng.key = 0;
+    rng.ctr = (unsigned)ph.y;
+    int phase = PH_SLOT;
+    while (un.z < un.w) {
+      Surf g = load_first_vertex(*J, un.y);
       rng = rmn_rng(p.seed, (uint32_t)un.y, (uint32_t)un.z);
       if (COUNT) slots_done++;
-      // sampleIndirectLightFromFirstIntersection, src/render.cpp:314-423
       if (len3(g.emis) > 0.0f) {
         un.z++;
         continue;
@@ -864,8 +932,8 @@ __global__ void __launch_bounds__(128, 8) slot_kernel(const Job* __restrict__ jo
       break;
     }
     store_worker(P, w, ph, phase, rng, un, uid);
-    if (phase == PH_WAIT_DIRECT) push(Q.sd[par], &out->sd, w);
-    else if (phase == PH_WAIT_CLOSEST) push(Q.c[par], &out->c, w);
+    if (phase == PH_WAIT_CLOSEST) push(Q.c[par], &out->c, w);
+    else push(Q.sd[par], &out->sd, w);  // unit used up: the next iteration's slot_kernel fetches
   }
   if (COUNT && slots_done) atomicAdd(&ctr->slots, slots_done);
 }
@@ -1251,7 +1319,7 @@ static void launch_qtrace(BatchState* b, const Pool& P, const Queues& Q, Ctl* ct
   qtrace_kernel<true, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
 }
 
-// Iteration k of a chunk (parity k & 1) of one lane: the three logic
+// Iteration k of a chunk (parity k & 1) of one lane: the five logic
 // kernels, then the two traversal kernels. ev (optional) records [0] before
 // the logic, [1] after it and [3] after the traversal.
 static cudaError_t launch_iteration(BatchState* b, int lane, cudaStream_t st, Counters* ctr, int k,
@@ -1268,12 +1336,14 @@ static cudaError_t launch_iteration(BatchState* b, int lane, cudaStream_t st, Co
   const int gs = sms * blocks_per_sm(shade_kernel), gn = sms * blocks_per_sm(nee_kernel);
   shade_kernel<<<gs, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_parts, b->d_status);
   nee_kernel<<<gn, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_parts);
+  slot_kernel<<<sms * blocks_per_sm(slot_kernel), 128, 0, st>>>(
+      b->d_jobs, nj, P, Q, ctl, &b->d_ctl->next_unit, par, b->table.total_units, b->d_parts);
   if (ctr) {
-    slot_kernel<true><<<sms * blocks_per_sm(slot_kernel<true>), 128, 0, st>>>(
-        b->d_jobs, nj, P, Q, ctl, &b->d_ctl->next_unit, par, b->table.total_units, b->d_parts, ctr);
+    light_kernel<true><<<sms * blocks_per_sm(light_kernel<true>), 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, ctr);
+    path_kernel<true><<<sms * blocks_per_sm(path_kernel<true>), 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, ctr);
   } else {
-    slot_kernel<false><<<sms * blocks_per_sm(slot_kernel<false>), 128, 0, st>>>(
-        b->d_jobs, nj, P, Q, ctl, &b->d_ctl->next_unit, par, b->table.total_units, b->d_parts, ctr);
+    light_kernel<false><<<sms * blocks_per_sm(light_kernel<false>), 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, ctr);
+    path_kernel<false><<<sms * blocks_per_sm(path_kernel<false>), 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, ctr);
   }
   if ((e = cudaGetLastError()) != cudaSuccess) return e;
   if (ev) cudaEventRecord(ev[1], st);
@@ -1442,7 +1512,7 @@ static size_t worker_bytes(bool glass, bool tex) {
   // vertex and weights, light-sample rays, queue entries
   return 4 * sizeof(int4) + 2 * sizeof(float4) + sizeof(float2) + 8 * sizeof(float4) +
          sizeof(int4) + kDirectBatch * (3 * sizeof(float4) + sizeof(float)) + sizeof(int2) +
-         sizeof(int) * (2 * (3 + kDirectBatch) + 2) + (glass ? RMN_MEDIA * 20 + 4 : 0) + (tex ? 3 * sizeof(float4) : 0);
+         sizeof(int) * (2 * (3 + kDirectBatch) + 4) + (glass ? RMN_MEDIA * 20 + 4 : 0) + (tex ? 3 * sizeof(float4) : 0);
 }
 
 static size_t free_device_bytes() {
@@ -1609,6 +1679,8 @@ rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int p
     }
     alloc((void**)&Q.nee, sizeof(int) * per);
     alloc((void**)&Q.slot, sizeof(int) * per);
+    alloc((void**)&Q.light, sizeof(int) * per);
+    alloc((void**)&Q.path, sizeof(int) * per);
     if (b->binned) {
       BatchState::Bins& bb = b->bin[l];
       alloc((void**)&bb.sc, sizeof(int) * per);
