@@ -302,8 +302,11 @@ rmn_status rmn_batch_device_bytes(const rmn_batch_item* items, int32_t n, const 
  * full-size batch would take more than half of the free device memory (the
  * library's own choice is always timed) -- on a proxy of the batch whose
  * images keep every item's scene, spp, depth and field of view but only
- * `pixel_fraction` (0 < f <= 1) of its pixels (rmn_batch_device_bytes
- * gives a candidate's full size); then the fastest of those
+ * `pixel_fraction` (0 < f <= 1) of its pixels, each candidate's workers
+ * per lane scaled by the same fraction for its proxy run (at least 4096),
+ * so that a worker has as much work as in the full batch
+ * (rmn_batch_device_bytes gives a candidate's full size); then the fastest
+ * of those
  * once more with the other traversal stack build where the batch's trees
  * allow both (27 entries instead of 23), then the fastest with its ray
  * queues binned (ray_order 1). Returns the fastest. Set each item's

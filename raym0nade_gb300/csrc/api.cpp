@@ -759,13 +759,21 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
     return fail(RMN_ERR_OUT_OF_MEMORY, "autotune: no configuration of this batch fits in the %zu free device bytes",
                 free_b);
   // Proxy renders: the same scenes, spp, depth and field of view at a
-  // fraction of the pixels, into buffers owned by the tuner.
+  // fraction of the pixels, into buffers owned by the tuner. A candidate's
+  // pool is scaled by the same fraction for its proxy run, so each worker
+  // has as many units to work through as in the full batch: the proxy then
+  // runs the full batch's number of wavefront iterations, its fill and its
+  // drain, instead of a pool the size of the full batch's draining after
+  // one pass over a sixteenth of the work.
   const float scale = std::sqrt(pixel_fraction);
   std::vector<void*> bufs;
   cudaError_t e = cudaSuccess;
+  double pix_full = 0.0, pix_proxy = 0.0;
   for (RenderItem& it : its) {
     rmn_render_args& a = it.args;
     int w = std::max(8, (int)std::lround(a.width * scale)), h = std::max(8, (int)std::lround(a.height * scale));
+    pix_full += (double)a.width * a.height;
+    pix_proxy += (double)w * h;
     a.accuracy *= (float)a.width / (float)w;
     a.width = w;
     a.height = h;
@@ -820,8 +828,11 @@ rmn_status rmn_batch_autotune(const rmn_batch_item* items, int32_t n, float pixe
       continue;
     }
     for (size_t i = 0; i < its.size(); ++i) its[i].args.slots_per_unit = cs == 0 ? proxy_slots[i] : cs;
+    const double f = pix_proxy / pix_full;
+    const int proxy_pool =
+        (int)std::max<double>(4096.0, std::round((cp > 0 ? cp : kDefaultPoolWorkers) * f / 128.0) * 128.0);
     BatchState* b = nullptr;
-    r = batch_create(its.data(), n, true, cp, cl, ck, co, st, &b);
+    r = batch_create(its.data(), n, true, proxy_pool, cl, ck, co, st, &b);
     if (r != RMN_OK) break;
     r = batch_launch(b, st);  // warm-up
     if (r == RMN_OK) {

@@ -1050,6 +1050,76 @@ __global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) qtrace_kernel(con
   }
 }
 
+// The shadow queue of a batch without alpha-tested materials: occlusion
+// with pending leaves (trace.cuh, occ_nodes / occ_leaves), the same answer
+// as the ordered search of qtrace_kernel<true, ...> in fewer instructions.
+template <bool COUNT, int STACK>
+__global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) qocc_kernel(const Job* __restrict__ jobs, Pool P,
+                                                                           Queues Q, Ctl* ctl, int par,
+                                                                           int* status, Counters* ctr) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  QLen* ql = &ctl->q[par];
+  const unsigned n = ql->sn;
+  unsigned int* next = &ql->s_next;
+  const int* q = Q.sn[par];
+  bool active = false, retired = false;
+  int w = 0;
+  TRay r;
+  float tmin = 0.0f, aim = 0.0f;
+  __shared__ int2 sstack[STACK * 128];
+  OccT<SharedStackN<STACK>> t;
+  t.stack.base = sstack + threadIdx.x;
+  t.c0 = t.c1 = 0;
+  const DevNode* nodes = nullptr;
+  const float4* tri = nullptr;
+  TraceCounters tc = {0, 0, 0, 0, 0};
+  for (;;) {
+    unsigned need = __ballot_sync(0xffffffffu, !active && !retired);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned base = 0;
+      if (lane == leader) base = atomicAdd(next, (unsigned)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!active && !retired) {
+        unsigned i = base + __popc(need & lt);
+        if (i < n) {
+          w = q[i];
+          const int wk = w >= 0 ? w : (~w) / kDirectBatch;
+          float4 o = P.ro[wk], d = w >= 0 ? P.rd[wk] : P.drd[~w];
+          const DevScene& js = jobs[worker_job(P, wk)].s;
+          nodes = js.nodes;
+          tri = js.tri;
+          r = make_tray(f3(o.x, o.y, o.z), f3(d.x, d.y, d.z));
+          tmin = o.w;
+          aim = d.w;
+          occ_begin(js.root, t);
+          if (COUNT) tc.shadow++;
+          active = true;
+        } else {
+          retired = true;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, active) == 0) break;
+    // boxes against HitRecord(eps, aimDepth + eps) throughout
+    const int st = occ_nodes<COUNT>(nodes, r, tmin, aim + RMN_EPS, t, active, kOccSteps, &tc);
+    const bool occ = occ_leaves<false>(tri, r, tmin, aim, t);
+    if (!active || (st == 0 && !occ)) continue;
+    const float occluded = (occ && st != -2) ? 1.0f : 0.0f;
+    if (w >= 0) P.res[w] = make_float2(occluded, 0.0f);
+    else P.dres[~w] = occluded;
+    if (st == -2) atomicExch(status, 1);
+    active = false;
+  }
+  if (COUNT) {
+    atomicAdd(&ctr->shadow, (unsigned long long)tc.shadow);
+    atomicAdd(&ctr->inner, (unsigned long long)tc.inner);
+    atomicAdd(&ctr->leaves, (unsigned long long)tc.leaves);
+    atomicAdd(&ctr->tris, (unsigned long long)tc.tris);
+  }
+}
+
 
 // Ray binning (batch option ray_order): before a traversal launch, its queue
 // is reordered by a bucket key -- the ray's job, the octant of its direction
@@ -1212,7 +1282,7 @@ int blocks_per_sm(K kernel) {
 
 namespace rmn {
 
-constexpr int kDefaultPoolWorkers = 1 << 22;  // per lane, fewer when device memory is short
+
 constexpr int kDefaultLanes = 3;
 constexpr int kIterationsPerChunk = 8;
 constexpr long long kMaxIterations = 1LL << 22;  // bound on the iteration loop; a finite render never reaches it
@@ -1316,7 +1386,8 @@ static void launch_qtrace(BatchState* b, const Pool& P, const Queues& Q, Ctl* ct
   int tb = device_sms() * blocks_per_sm(qtrace_kernel<false, COUNT, ALPHA, STACK>);
   if (tb > lb) tb = lb;
   qtrace_kernel<false, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
-  qtrace_kernel<true, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+  if (ALPHA) qtrace_kernel<true, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+  else qocc_kernel<COUNT, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
 }
 
 // Iteration k of a chunk (parity k & 1) of one lane: the five logic

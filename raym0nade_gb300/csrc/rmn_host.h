@@ -114,6 +114,9 @@ rmn_status batch_create(const RenderItem* items, int n, bool use_graph, int pool
 // The traversal stack the library picks for these items (RMN_STACK_SMALL when
 // every tree is at most RMN_STACK_SMALL - 1 deep, else RMN_STACK).
 int default_stack_entries(const RenderItem* items, int n);
+// Workers per lane when a batch leaves the pool size open (fewer when device
+// memory is short).
+constexpr int kDefaultPoolWorkers = 1 << 22;
 rmn_status batch_launch(BatchState* b, cudaStream_t st);
 rmn_status batch_update(BatchState* b, const rmn_render_args* args, int n, cudaStream_t st);
 size_t batch_job_bytes();

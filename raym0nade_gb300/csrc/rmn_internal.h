@@ -73,6 +73,7 @@ RMN_HD float3 mix3(float3 x, float3 y, float a) { return x * (1.0f - a) + y * a;
 // node steps per round, and blocks per SM for a shared stack of S entries
 // (S * 1 KiB of stack plus 1 KiB of leaf keys per 128-thread block).
 constexpr int kCoopSteps = 4;
+constexpr int kOccSteps = 6;  // occlusion queries with pending leaves (trace.cuh, occ_nodes)
 #define RMN_COOP_BLOCKS(S) ((S) <= RMN_STACK_SMALL ? 8 : 7)
 
 // ------------------------------------------------------------ layout ------

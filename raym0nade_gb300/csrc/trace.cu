@@ -90,6 +90,54 @@ __global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) trace_kernel(DevS
   }
 }
 
+// Occlusion queries of a scene without alpha-tested materials: pending
+// leaves, order-free (trace.cuh, occ_nodes / occ_leaves).
+template <int STACK>
+__global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) occ_kernel(DevScene s, const float4* __restrict__ rays,
+                                                                          int64_t n, uint8_t* __restrict__ occ,
+                                                                          unsigned long long* __restrict__ next,
+                                                                          int* status) {
+  const int lane = threadIdx.x & 31;
+  const unsigned lt = (1u << lane) - 1u;
+  bool active = false, retired = false;
+  int64_t i = 0;
+  TRay r;
+  float aim = 0.0f;
+  __shared__ int2 sstack[STACK * 128];
+  OccT<SharedStackN<STACK>> t;
+  t.stack.base = sstack + threadIdx.x;
+  t.c0 = t.c1 = 0;
+  for (;;) {
+    unsigned need = __ballot_sync(0xffffffffu, !active && !retired);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      unsigned long long base = 0;
+      if (lane == leader) base = atomicAdd(next, (unsigned long long)__popc(need));
+      base = __shfl_sync(0xffffffffu, base, leader);
+      if (!active && !retired) {
+        i = (int64_t)(base + __popc(need & lt));
+        if (i < n) {
+          float4 r0 = __ldg(rays + 2 * i), r1 = __ldg(rays + 2 * i + 1);
+          r = make_tray(f3(r0.x, r0.y, r0.z), f3(r1.x, r1.y, r1.z));
+          aim = r1.w;
+          occ_begin(s.root, t);
+          active = true;
+        } else {
+          retired = true;
+        }
+      }
+    }
+    if (__ballot_sync(0xffffffffu, active) == 0) return;
+    // HitRecord(eps, aimDepth + eps); occluded iff a hit is nearer than aimDepth
+    const int st = occ_nodes<false>(s.nodes, r, RMN_EPS, aim + RMN_EPS, t, active, kOccSteps, nullptr);
+    const bool o = occ_leaves<true>(s.tri, r, RMN_EPS, aim, t);
+    if (!active || (st == 0 && !o)) continue;
+    if (st == -2) atomicExch(status, (int)rmn::kDevStackOverflow);
+    occ[i] = (o && st != -2) ? 1 : 0;
+    active = false;
+  }
+}
+
 int persistent_blocks(const void* kernel, int threads) {
   int dev = 0, sms = 0, per_sm = 0;
   cudaGetDevice(&dev);
@@ -103,10 +151,13 @@ template <bool SHADOW, int STACK>
 void launch_kernel(const DevScene& s, const float4* rays, int64_t n, float4* hits, uint8_t* occ,
                    unsigned long long* next, int* status, cudaStream_t stream) {
   const int threads = 128;
-  int blocks = persistent_blocks((const void*)trace_kernel<SHADOW, STACK>, threads);
+  const bool order_free = SHADOW && !s.has_alpha;
+  int blocks = order_free ? persistent_blocks((const void*)occ_kernel<STACK>, threads)
+                          : persistent_blocks((const void*)trace_kernel<SHADOW, STACK>, threads);
   int64_t need = (n + threads - 1) / threads;
   if (need < blocks) blocks = (int)need;
-  trace_kernel<SHADOW, STACK><<<blocks, threads, 0, stream>>>(s, rays, n, hits, occ, next, status);
+  if (order_free) occ_kernel<STACK><<<blocks, threads, 0, stream>>>(s, rays, n, occ, next, status);
+  else trace_kernel<SHADOW, STACK><<<blocks, threads, 0, stream>>>(s, rays, n, hits, occ, next, status);
 }
 
 cudaError_t launch(bool shadow, const DevScene& s, const rmn_ray* rays, int64_t n, rmn_hit* hits, uint8_t* occ,

@@ -396,6 +396,186 @@ RMN_D bool coop_leaves(const float4* __restrict__ tri, const TRay& r, float tmin
   return answered;
 }
 
+
+// ------------------------------------------ occlusion with pending leaves
+// An occlusion query asks whether any triangle lies at eps < t < aim. The
+// reference answers it with a closest-hit search over (eps, aim + eps) and
+// compares the distance found with aim (Model::rayHit_test); any hit nearer
+// than aim makes that distance nearer than aim, whatever the order of
+// visits. So the occlusion kernels of scenes without alpha-tested materials
+// drop the order: a lane that reaches a leaf keeps it pending and goes on
+// stepping -- popping its stack -- until it holds two leaves or its steps
+// for the round are used up, and the warp then tests the triangles of all
+// pending leaves together, 32 at a time, one bit per ray for "a hit nearer
+// than aim". The boxes are tested against the query's interval as it
+// starts, (eps, aim + eps), which the reference's interval never exceeds,
+// so every triangle the reference tests is tested here: the answers agree
+// unless an occluder's distance lies within float rounding of a box's entry
+// distance while another surface lies between aim and aim + eps (the
+// reference can then skip the box). Scenes with alpha-tested materials keep
+// the ordered search, which their retry past cut-away hits needs.
+template <class Stack>
+struct OccT {
+  int cur, sp;
+  int a0, c0, a1, c1;  // pending leaves: first triangle, count (c1 > 0 only with c0 > 0)
+  bool pop;
+  Stack stack;
+};
+
+template <class Stack>
+RMN_D void occ_begin(int root, OccT<Stack>& t) {
+  t.cur = root;
+  t.sp = 0;
+  t.c0 = t.c1 = 0;
+  t.pop = false;
+}
+
+// Phase 1 (all 32 lanes): up to `steps` inner-node steps for lanes with
+// `go` that hold fewer than two pending leaves. Returns 1 once the lane's
+// stack is used up (its pending leaves, if any, still to test), -2 on
+// stack overflow, 0 otherwise.
+template <bool COUNT, class Stack>
+RMN_D int occ_nodes(const DevNode* __restrict__ nodes, const TRay& r, float tmin, float tmax, OccT<Stack>& t,
+                    bool go, int steps, TraceCounters* cnt) {
+  int res = 0;
+#pragma unroll 1
+  for (int step = 0; step < steps; ++step) {
+    const bool g = go && res == 0 && t.c1 == 0;
+    if (!__any_sync(0xffffffffu, g)) break;
+    if (!g) continue;
+    if (t.pop) {
+      t.pop = false;
+      for (;;) {
+        if (t.sp == 0) {
+          res = 1;
+          break;
+        }
+        --t.sp;
+        const int2 e = t.stack.get(t.sp);
+        if (__int_as_float(e.y) < tmax) {
+          t.cur = e.x;
+          break;
+        }
+      }
+      if (res) continue;
+    }
+    if (t.cur >= 0) {
+      const DevNode* n = nodes + t.cur;
+      float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
+      int4 D = __ldg(&n->d);
+      if (COUNT) cnt->inner++;
+      float tl0, tl1;
+      bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, tmax, tl0);
+      bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, tmax, tl1);
+      int nref, fref;
+      bool hn, hf;
+      float tlf;
+      if (tl0 < tl1) {
+        nref = D.x; hn = h0; fref = D.y; hf = h1; tlf = tl1;
+      } else {
+        nref = D.y; hn = h1; fref = D.x; hf = h0; tlf = tl0;
+      }
+      if (hn) {
+        if (hf) {
+          if (t.sp >= Stack::kCap) {
+            res = -2;
+            continue;
+          }
+          t.stack.put(t.sp, make_int2(fref, __float_as_int(tlf)));
+          ++t.sp;
+        }
+        t.cur = nref;
+      } else if (hf && tlf < tmax) {
+        t.cur = fref;
+      } else {
+        t.pop = true;
+        continue;
+      }
+    }
+    if (t.cur < 0) {  // a leaf: kept pending, and on to the next node
+      const int x = ~t.cur;
+      const int count = x & 15;
+      if (COUNT) { cnt->leaves++; cnt->tris += count; }
+      if (count > 0) {
+        if (t.c0 == 0) {
+          t.a0 = x >> 4;
+          t.c0 = count;
+        } else {
+          t.a1 = x >> 4;
+          t.c1 = count;
+        }
+      }
+      t.pop = true;
+    }
+  }
+  return res;
+}
+
+// Phase 2 (all 32 lanes): the pending leaves' triangles, 32 at a time;
+// true for a lane whose ray has a hit at eps < t < aim (`tmin` = eps).
+// Clears the pending leaves. SAME_TRI as in coop_leaves.
+template <bool SAME_TRI, class Stack>
+RMN_D bool occ_leaves(const float4* __restrict__ tri, const TRay& r, float tmin, float aim, OccT<Stack>& t) {
+  const unsigned FULL = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  const int cnt = t.c0 + t.c1;
+  if (!__any_sync(FULL, cnt > 0)) return false;
+  int incl = cnt;
+#pragma unroll
+  for (int off = 1; off < 32; off <<= 1) {
+    const int v = __shfl_up_sync(FULL, incl, off);
+    if (lane >= off) incl += v;
+  }
+  const int total = __shfl_sync(FULL, incl, 31);
+  const int excl = incl - cnt;
+  unsigned occluded = 0;  // bit per owner lane
+#pragma unroll 1
+  for (int base = 0; base < total; base += 32) {
+    const int k = base + lane;
+    int lo = 0;
+#pragma unroll
+    for (int st = 16; st >= 1; st >>= 1) {
+      const int v = __shfl_sync(FULL, incl, lo + st - 1);
+      if (v <= k) lo += st;
+    }
+    const int ow = min(lo, 31);
+    const int loc = k - __shfl_sync(FULL, excl, ow);
+    const int oa0 = __shfl_sync(FULL, t.a0, ow), oc0 = __shfl_sync(FULL, t.c0, ow);
+    const int oa1 = __shfl_sync(FULL, t.a1, ow);
+    TRay q;
+    q.o.x = __shfl_sync(FULL, r.o.x, ow);
+    q.o.y = __shfl_sync(FULL, r.o.y, ow);
+    q.o.z = __shfl_sync(FULL, r.o.z, ow);
+    q.d.x = __shfl_sync(FULL, r.d.x, ow);
+    q.d.y = __shfl_sync(FULL, r.d.y, ow);
+    q.d.z = __shfl_sync(FULL, r.d.z, ow);
+    const float qmin = __shfl_sync(FULL, tmin, ow), qaim = __shfl_sync(FULL, aim, ow);
+    const float4* qtri = tri;
+    if (!SAME_TRI) {
+      const unsigned long long p = reinterpret_cast<unsigned long long>(tri);
+      const unsigned lo32 = __shfl_sync(FULL, (unsigned)p, ow), hi32 = __shfl_sync(FULL, (unsigned)(p >> 32), ow);
+      qtri = reinterpret_cast<const float4*>(((unsigned long long)hi32 << 32) | lo32);
+    }
+    bool h = false;
+    if (k < total) {
+      const int i = loc < oc0 ? oa0 + loc : oa1 + (loc - oc0);
+      const float4* tp = qtri + 3 * i;
+      float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
+      const float th = tri_t(q, f3(a), f3(b), f3(c), b.w);
+      h = qmin < th && th < qaim;
+    }
+    // the owners of the lanes that found an occluder
+    unsigned m = __ballot_sync(FULL, h);
+    while (m) {
+      const int src = __ffs(m) - 1;
+      m &= m - 1;
+      occluded |= 1u << __shfl_sync(FULL, ow, src);
+    }
+  }
+  t.c0 = t.c1 = 0;
+  return (occluded >> lane) & 1u;
+}
+
 // One whole query without the alpha retry (scenes without alpha-tested
 // materials), its deferred-child stack in shared memory at `stk` (entry e
 // at stk[e * 128], see SharedStackN). Same answer as trace().
