@@ -46,18 +46,20 @@ sys.path.insert(0, ROOT)
 METRIC = "Mpaths/s at rel-MSE≤1e-3 (batched vs per-scene launch); adjoint/forward time"
 UNIT = "Mpaths/s"
 FALLBACK_HBM_GBS = 6800.0
-# DRAM and L2 bytes (read + write) of the traversal launches (closest and
-# shadow queues) of one batch64 render at the launch configurations given
-# beside them, summed from ncu captures (metrics dram__bytes_read.sum,
-# dram__bytes_write.sum, lts__t_bytes.sum) of
-#   python bench.py --profile-case batch --slots 2 --pool 8388608 --lanes L --stack 27
+# DRAM and L2 bytes (read + write) of the traversal launches (closest queue:
+# qtrace_kernel, shadow queue: qocc_kernel) of one batch64 render at the
+# launch configurations given beside them, summed from ncu captures (metrics
+# dram__bytes_read.sum, dram__bytes_write.sum, lts__t_bytes.sum) of
+#   python bench.py --profile-case batch --slots 2 --pool 8388608 --lanes L --stack S
 # (ncu cannot run inside the timed region). The line takes the capture of
 # the timed configuration, and says so, or else the first and says that.
 BATCH64_TRAVERSAL_BYTES = [
-    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 2, "stack_entries": 27, "ray_order": 0},
-     "dram": 170.9e9, "l2": 2386.2e9},
+    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 4, "stack_entries": 23, "ray_order": 0},
+     "dram": 148.0e9, "l2": 2342.3e9},
+    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 3, "stack_entries": 23, "ray_order": 0},
+     "dram": 162.3e9, "l2": 2364.7e9},
     {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 3, "stack_entries": 27, "ray_order": 0},
-     "dram": 156.9e9, "l2": 2362.9e9},
+     "dram": 161.1e9, "l2": 2213.2e9},
 ]
 
 
@@ -715,7 +717,8 @@ def run_gpu(args, rank, world, dist):
         cfg = cap["config"]
         same = timed == cfg
         traffic = cap["dram"]
-        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum over every qtrace_kernel launch of one "
+        traffic_src = ("ncu dram__bytes_read.sum + dram__bytes_write.sum over every qtrace_kernel and qocc_kernel "
+                       "launch of one "
                        "batch64 render at " + json.dumps(cfg) + ("" if same else "; NOT the timed configuration"))
         l2_peak = l2_copy_gbs(stream)
         l2_gbs = cap["l2"] / (trace_ms_live / 1e3) / 1e9
@@ -723,11 +726,12 @@ def run_gpu(args, rank, world, dist):
               "copy_rate": l2_peak, "frac_of_copy_rate": l2_gbs / l2_peak, "same_config": same,
               "source": "ncu lts__t_bytes.sum over the same launches; copy_rate: a device copy between two "
                         "L2-resident 24 MiB buffers, measured here"}
-    limiter = ("instruction issue and dependent-load latency: in steady state (ncu) the traversal uses 66-69 % of "
-               "its issue slots with 17.7-18.6 of 32 lanes active per instruction (warp-cooperative leaves), "
-               "stalled mostly on L1/L2 loads (long scoreboard 3.3 per issue) and fixed-latency dependencies "
-               "(2.9); its measured DRAM traffic is a small share of the algorithmic bytes (L1/L2 hits) and "
-               "neither DRAM nor L2 runs near its rate")
+    limiter = ("instruction issue and dependent-load latency: in steady state (ncu) the closest-hit traversal "
+               "uses 66 % of its issue slots with 17.6 of 32 lanes active per instruction (warp-cooperative "
+               "leaves), the occlusion traversal 72 % with 19.9 lanes (pending leaves), both stalled mostly on "
+               "L1/L2 loads (long scoreboard 2.8-3.4 per issue) and fixed-latency dependencies (2.9); their "
+               "measured DRAM traffic is a small share of the algorithmic bytes (L1/L2 hits) and neither DRAM "
+               "nor L2 runs near its rate")
     base, _ = cpu_baseline(insts) if args.cpu_baseline else (None, None)
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -750,7 +754,7 @@ def run_gpu(args, rank, world, dist):
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_source": traffic_src,
                      "per": "step (all traversal launches of one step)",
-                     "kernel": "qtrace_kernel (closest + shadow queues)", "peak_source": peak_src,
+                     "kernel": "qtrace_kernel (closest queue) + qocc_kernel (shadow queue)", "peak_source": peak_src,
                      "bytes_model": "64 B per inner-node visit + 36 B per triangle test + 40 B per queued ray",
                      "algorithmic_bytes_per_step": alg_bytes, "trace_share": trace_share,
                      "logic_share": logic_share, "iterations": prof["iterations"],
