@@ -62,14 +62,27 @@ RMN_D bool box_hit(const TRay& r, float3 lo, float3 hi, float tmin, float tmax, 
   return L < R;
 }
 
-// RayTriangleIntersection (Moller-Trumbore), src/geometry.cpp:63-87.
+// RayTriangleIntersection (Moller-Trumbore), src/geometry.cpp:63-87, with
+// a division-free pre-test: u = RN(RN(1/a) * x), x = dot(s, h). Where x / a
+// lies below -1e-5 or above 1 + 1e-5 (compared as x * sign(a) against the
+// rounded products 1e-5 * |a| and 1.00001 * |a|), the two roundings (a
+// relative error below 2^-23) cannot bring u into [0, 1], so the
+// reference rejects the triangle too -- by its u test, or earlier by its
+// degeneracy test; both give "no hit". Such triangles, most of the tested
+// ones, skip the two divisions. Non-finite a or x fail both comparisons and
+// take the reference's path, as does every triangle that may be hit: the
+// values computed for a hit are the reference's, operation for operation.
 RMN_D float tri_t(const TRay& r, float3 v0, float3 e1, float3 e2, float len_e1) {
   float3 h = cross3(r.d, e2);
   float a = dot3(e1, h);
+  float3 s = r.o - v0;
+  const float x = dot3(s, h);
+  const float aa = fabsf(a);
+  const float xs = a < 0.0f ? -x : x;
+  if (xs < -1e-5f * aa || xs > 1.00001f * aa) return INFINITY;
   if (fabsf(a) / len_e1 < RMN_EPS) return INFINITY;
   float f = 1.0f / a;
-  float3 s = r.o - v0;
-  float u = f * dot3(s, h);
+  float u = f * x;
   if (u < 0.0f || u > 1.0f) return INFINITY;
   float3 q = cross3(s, e1);
   float v = f * dot3(r.d, q);
