@@ -391,8 +391,8 @@ rmn_status launch_adjoint(const rmn_scene* scene, const rmn_render_args& args, c
   const int ng = nmats * kGradPerMat;
   double* acc = nullptr;
   int* status = nullptr;
-  cudaError_t e = cudaMallocAsync(reinterpret_cast<void**>(&acc), (size_t)ng * sizeof(double) + 16, st);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (adjoint)");
+  cudaError_t e = rmn::staging_malloc(reinterpret_cast<void**>(&acc), (size_t)ng * sizeof(double) + 16, st);
+  if (e != cudaSuccess) return cuda_fail(e, "staging allocation (adjoint)");
   status = reinterpret_cast<int*>(acc + ng);
   e = cudaMemsetAsync(acc, 0, (size_t)ng * sizeof(double) + 16, st);
   const long long total = (long long)J.p.W * J.p.H * J.p.slots;

@@ -36,8 +36,8 @@ rmn_status stage_in(const void* host_or_dev, size_t bytes, cudaStream_t st, Arg*
     out->dev = const_cast<void*>(host_or_dev);
     return RMN_OK;
   }
-  cudaError_t e = cudaMallocAsync(&out->dev, bytes ? bytes : 1, st);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (staging)");
+  cudaError_t e = rmn::staging_malloc(&out->dev, bytes ? bytes : 1, st);
+  if (e != cudaSuccess) return cuda_fail(e, "staging allocation (staging)");
   out->owned = true;
   if (bytes) {
     e = cudaMemcpyAsync(out->dev, host_or_dev, bytes, cudaMemcpyHostToDevice, st);
@@ -51,8 +51,8 @@ rmn_status stage_out(void* host_or_dev, size_t bytes, cudaStream_t st, Arg* out)
     out->dev = host_or_dev;
     return RMN_OK;
   }
-  cudaError_t e = cudaMallocAsync(&out->dev, bytes ? bytes : 1, st);
-  if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (staging)");
+  cudaError_t e = rmn::staging_malloc(&out->dev, bytes ? bytes : 1, st);
+  if (e != cudaSuccess) return cuda_fail(e, "staging allocation (staging)");
   out->owned = true;
   return RMN_OK;
 }
@@ -74,8 +74,8 @@ void release(Arg& a, cudaStream_t st) {
 struct Status {
   int* dev = nullptr;
   rmn_status init(cudaStream_t st) {
-    cudaError_t e = cudaMallocAsync(&dev, sizeof(int), st);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (status)");
+    cudaError_t e = rmn::staging_malloc(reinterpret_cast<void**>(&dev), sizeof(int), st);
+    if (e != cudaSuccess) return cuda_fail(e, "staging allocation (status)");
     e = cudaMemsetAsync(dev, 0, sizeof(int), st);
     if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync (status)");
     return RMN_OK;
@@ -131,8 +131,8 @@ rmn_status post_device(const float* dd, const float* ds, const float* id, const 
   const bool dof = (options & RMN_SHADE_DEPTH_OF_FIELD) != 0, bloom = (options & RMN_SHADE_BLOOM) != 0;
   float* tmp = nullptr;
   if (fx) {
-    cudaError_t e = cudaMallocAsync(&tmp, npx * 12, st);
-    if (e != cudaSuccess) return cuda_fail(e, "cudaMallocAsync (post)");
+    cudaError_t e = rmn::staging_malloc(reinterpret_cast<void**>(&tmp), npx * 12, st);
+    if (e != cudaSuccess) return cuda_fail(e, "staging allocation (post)");
   }
   float* target = fx ? tmp : out;
   // the gamma of compose itself only when nothing runs between shade and gamma
@@ -513,8 +513,8 @@ rmn_status rmn_compose(const rmn_image* image, int32_t width, int32_t height, fl
   if (r == RMN_OK) r = stage_out(rgb, npx * 12, st, &o);
   bool fx = (options & RMN_SHADE_FXAA) != 0;
   if (r == RMN_OK && fx) {
-    cudaError_t e = cudaMallocAsync(&tmp.dev, npx * 12, st);
-    if (e != cudaSuccess) r = cuda_fail(e, "cudaMallocAsync (compose)");
+    cudaError_t e = rmn::staging_malloc(&tmp.dev, npx * 12, st);
+    if (e != cudaSuccess) r = cuda_fail(e, "staging allocation (compose)");
     tmp.owned = true;
   }
   if (r == RMN_OK) {
@@ -570,8 +570,8 @@ static rmn_status render_one(rmn_scene* scene, const rmn_render_args* args, cons
     if (image->gbuffer) {
       r = stage_out(image->gbuffer, npx * RMN_GBUFFER_FLOATS * 4, st, &gb);
     } else {
-      cudaError_t e = cudaMallocAsync(&gb.dev, npx * RMN_GBUFFER_FLOATS * 4, st);
-      if (e != cudaSuccess) r = cuda_fail(e, "cudaMallocAsync (G-buffer)");
+      cudaError_t e = rmn::staging_malloc(&gb.dev, npx * RMN_GBUFFER_FLOATS * 4, st);
+      if (e != cudaSuccess) r = cuda_fail(e, "staging allocation (G-buffer)");
       gb.owned = true;
     }
   }

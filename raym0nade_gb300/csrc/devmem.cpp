@@ -6,6 +6,14 @@
 // a render. Blocks returned by a batch are kept per device and handed to the
 // next batch that asks for a size between the block's half and its size, up
 // to kCacheLimit bytes per device; rmn_release_cached_memory frees them.
+//
+// The calls' short-lived buffers (host arrays staged through the device,
+// intermediate images, status words) are stream-ordered allocations from a
+// memory pool of the library's own per device, which keeps up to
+// kStagingKeep bytes across stream synchronisations. The device's default
+// pool gives its memory back at every synchronisation (release threshold
+// 0), so each call of a loop such as one rmn_compose per image mapped its
+// buffers anew: about 0.2 ms a call.
 #include <map>
 #include <mutex>
 #include <unordered_map>
@@ -16,6 +24,39 @@ namespace rmn {
 namespace {
 
 constexpr size_t kCacheLimit = size_t(16) << 30;
+constexpr uint64_t kStagingKeep = uint64_t(1) << 30;
+
+std::mutex g_pool_mu;
+std::unordered_map<int, cudaMemPool_t> g_pools;
+
+// The library's staging pool of the current device (created on first use).
+cudaError_t staging_pool(cudaMemPool_t* out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_pool_mu);
+  auto it = g_pools.find(dev);
+  if (it != g_pools.end()) {
+    *out = it->second;
+    return cudaSuccess;
+  }
+  cudaMemPoolProps props = {};
+  props.allocType = cudaMemAllocationTypePinned;
+  props.location.type = cudaMemLocationTypeDevice;
+  props.location.id = dev;
+  cudaMemPool_t pool = nullptr;
+  e = cudaMemPoolCreate(&pool, &props);
+  if (e != cudaSuccess) return e;
+  uint64_t keep = kStagingKeep;
+  e = cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+  if (e != cudaSuccess) {
+    cudaMemPoolDestroy(pool);
+    return e;
+  }
+  g_pools[dev] = pool;
+  *out = pool;
+  return cudaSuccess;
+}
 
 struct DeviceCache {
   std::multimap<size_t, void*> free_blocks;  // size -> block
@@ -77,7 +118,18 @@ void cached_free(void* p) {
   c.cached += bytes;
 }
 
+cudaError_t staging_malloc(void** p, size_t bytes, cudaStream_t st) {
+  cudaMemPool_t pool = nullptr;
+  cudaError_t e = staging_pool(&pool);
+  if (e != cudaSuccess) return e;
+  return cudaMallocFromPoolAsync(p, bytes ? bytes : 1, pool, st);
+}
+
 void release_cached_memory() {
+  {
+    std::lock_guard<std::mutex> lock(g_pool_mu);
+    for (auto& kv : g_pools) cudaMemPoolTrimTo(kv.second, 0);
+  }
   std::lock_guard<std::mutex> lock(g_mu);
   int dev = 0;
   cudaGetDevice(&dev);

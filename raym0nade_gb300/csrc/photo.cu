@@ -440,7 +440,7 @@ struct DevScratch {
   T* get(size_t count) {
     void* p = nullptr;
     if (err != cudaSuccess) return nullptr;
-    err = cudaMallocAsync(&p, count * sizeof(T) + 16, st);
+    err = rmn::staging_malloc(&p, count * sizeof(T) + 16, st);
     if (err != cudaSuccess) return nullptr;
     ptrs.push_back(p);
     return static_cast<T*>(p);
@@ -536,7 +536,7 @@ cudaError_t dof_plan_create(const float* gbuf, int W, int H, float focus, float 
   cudaError_t e = cudaSuccess;
   auto alloc = [&](size_t bytes) -> void* {
     void* q = nullptr;
-    if (e == cudaSuccess) e = cudaMallocAsync(&q, bytes + 16, st);
+    if (e == cudaSuccess) e = rmn::staging_malloc(&q, bytes + 16, st);
     if (e == cudaSuccess) p->allocs.push_back(q);
     return e == cudaSuccess ? q : nullptr;
   };

@@ -101,6 +101,9 @@ uint32_t png_crc32(uint32_t crc, const uint8_t* p, size_t n);
 cudaError_t cached_malloc(void** p, size_t bytes);
 void cached_free(void* p);
 void release_cached_memory();
+// A stream-ordered allocation from the library's staging pool (devmem.cpp),
+// freed with cudaFreeAsync.
+cudaError_t staging_malloc(void** p, size_t bytes, cudaStream_t st);
 // Forgets the device addresses rmn_compose_noalloc resolved (after a device
 // reset they name nothing); the next call on each device resolves them anew.
 void noalloc_forget_addresses();

@@ -164,7 +164,7 @@ cudaError_t launch(bool shadow, const DevScene& s, const rmn_ray* rays, int64_t 
                    int* status, cudaStream_t stream) {
   if (n <= 0) return cudaSuccess;
   unsigned long long* next = nullptr;
-  cudaError_t e = cudaMallocAsync(&next, sizeof(unsigned long long), stream);
+  cudaError_t e = rmn::staging_malloc(reinterpret_cast<void**>(&next), sizeof(unsigned long long), stream);
   if (e != cudaSuccess) return e;
   e = cudaMemsetAsync(next, 0, sizeof(unsigned long long), stream);
   if (e == cudaSuccess) {
