@@ -210,7 +210,9 @@ rmn_status rmn_scene_destroy(rmn_scene* scene);
 rmn_status rmn_scene_info_get(const rmn_scene* scene, rmn_scene_info* info);
 
 /* Renders keep the device memory of their worker pools and queues for the
- * next render (up to 16 GiB per device); this frees it, and makes
+ * next render (up to 16 GiB per device), and the calls' short-lived
+ * buffers come from a memory pool of the library's own that keeps up to
+ * 1 GiB per device between calls; this frees both, and makes
  * rmn_compose_noalloc resolve its array's device address again (call it
  * after a cudaDeviceReset). No counterpart in the reference. */
 rmn_status rmn_release_cached_memory(void);
