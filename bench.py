@@ -54,12 +54,10 @@ FALLBACK_HBM_GBS = 6800.0
 # (ncu cannot run inside the timed region). The line takes the capture of
 # the timed configuration, and says so, or else the first and says that.
 BATCH64_TRAVERSAL_BYTES = [
-    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 4, "stack_entries": 23, "ray_order": 0},
-     "dram": 148.0e9, "l2": 2342.3e9},
     {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 3, "stack_entries": 23, "ray_order": 0},
-     "dram": 162.3e9, "l2": 2364.7e9},
-    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 3, "stack_entries": 27, "ray_order": 0},
-     "dram": 161.1e9, "l2": 2213.2e9},
+     "dram": 161.3e9, "l2": 2252.4e9},
+    {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 4, "stack_entries": 23, "ray_order": 0},
+     "dram": 147.1e9, "l2": 2230.2e9},
 ]
 
 
@@ -727,9 +725,9 @@ def run_gpu(args, rank, world, dist):
               "source": "ncu lts__t_bytes.sum over the same launches; copy_rate: a device copy between two "
                         "L2-resident 24 MiB buffers, measured here"}
     limiter = ("instruction issue and dependent-load latency: in steady state (ncu) the closest-hit traversal "
-               "uses 66 % of its issue slots with 17.6 of 32 lanes active per instruction (warp-cooperative "
-               "leaves), the occlusion traversal 72 % with 19.9 lanes (pending leaves), both stalled mostly on "
-               "L1/L2 loads (long scoreboard 2.8-3.4 per issue) and fixed-latency dependencies (2.9); their "
+               "uses 67 % of its issue slots with 17.5 of 32 lanes active per instruction (warp-cooperative "
+               "leaves), the occlusion traversal 74 % with 19.5 lanes (pending leaves), both stalled mostly on "
+               "L1/L2 loads (long scoreboard 2.4-3.1 per issue) and fixed-latency dependencies (2.8-2.9); their "
                "measured DRAM traffic is a small share of the algorithmic bytes (L1/L2 hits) and neither DRAM "
                "nor L2 runs near its rate")
     base, _ = cpu_baseline(insts) if args.cpu_baseline else (None, None)
@@ -796,6 +794,8 @@ def profile_case(a):
       fxaa      rmn_compose(Full | gamma | FXAA) of a --size WxH image
       post      the textured room at --size WxH, then rmn_export_set twice
       textured  rmn_render of the textured room at --size WxH, twice
+      mips      rmn_scene_create of the textured room with its eight
+                textures at 2048 x 2048, twice (device mip chains)
     """
     import torch
 
@@ -855,6 +855,15 @@ def profile_case(a):
             m.rayHit_test(sr)
         torch.cuda.synchronize()
         print("trace", m.info(), "rays", a.rays)
+    elif a.profile_case == "mips":
+        rng = np.random.default_rng(2)
+        room = scenes.textured_room()
+        room.textures = [rng.integers(0, 256, (2048, 2048, 4), dtype=np.uint8) for _ in room.textures]
+        for _ in range(2):
+            m = api.Model(room)
+            del m
+        torch.cuda.synchronize()
+        print("mips", len(room.textures), "textures of 2048 x 2048")
     elif a.profile_case in ("post", "textured"):
         w, h = (int(x) for x in a.size.split("x")) if "x" in a.size else (1920, 1080)
         m = api.Model(scenes.textured_room())
@@ -897,7 +906,7 @@ def main():
     ap.add_argument("--no-autotune", dest="autotune", action="store_false")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false")
     ap.add_argument("--no-configs", dest="configs", action="store_false")
-    ap.add_argument("--profile-case", choices=["render", "trace", "batch", "adjoint", "fxaa", "post", "textured"],
+    ap.add_argument("--profile-case", choices=["render", "trace", "batch", "adjoint", "fxaa", "post", "textured", "mips"],
                     help="run one small case for a profiler instead of the benchmark (see profile_case)")
     ap.add_argument("--tris", type=int, default=2_000_000)
     ap.add_argument("--size", default="256")
