@@ -745,9 +745,9 @@ def run_gpu(args, rank, world, dist):
                 "d2h_bytes_per_step": d2h,
                 "call": "rmn_batch_update (cameras and seeds from pinned host memory) + rmn_batch_render + "
                         "rmn_compose(Full|gamma|FXAA) of every instance into pinned host memory; wall clock"},
-        # per batched step: G-buffer kernel, one seed kernel per lane, 7 kernels
-        # per wavefront iteration and lane (13 with binned ray queues), finalize
-        "gpu_launches": args.steps * (2 + lanes + (13 if tune and tune["ray_order"] else 7) * lanes *
+        # per batched step: G-buffer kernel, one seed kernel per lane, 8 kernels
+        # per wavefront iteration and lane (14 with binned ray queues), finalize
+        "gpu_launches": args.steps * (2 + lanes + (14 if tune and tune["ray_order"] else 8) * lanes *
                                       prof["iterations"]),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "traffic": traffic, "traffic_source": traffic_src,

@@ -14,13 +14,15 @@
 //     jitter, as the reference), closest hit, hit shading -> G-buffer.
 //  2. per iteration, until no worker is left, over a pool of W workers
 //     (path state in HBM, structure of arrays):
-//     shade_kernel, nee_kernel, slot_kernel, light_kernel, path_kernel --
+//     shade_kernel, bounce_kernel, nee_kernel, slot_kernel, light_kernel,
+//     path_kernel --
 //                        the integrator's logic, split by phase so that each
 //                        kernel runs over a compacted list of the workers in
 //                        its phase (see below); a worker ends the iteration
 //                        with a ray queued, retired, or (rarely) handed to
 //                        the next iteration's slot_kernel;
-//     qtrace_kernel<closest>, qtrace_kernel<shadow> -- persistent traversal
+//     qtrace_kernel<closest>, qocc_kernel (qtrace_kernel<shadow> in batches
+//                        with alpha-tested materials) -- persistent traversal
 //                        of the ray queues with per-lane dynamic ray fetch.
 //     Traversal thus runs at the occupancy of a 64-register kernel, and the
 //     shading code runs on warps of one phase each.
@@ -70,6 +72,7 @@ struct QLen {
   unsigned int sd, nw;          // workers waiting for first-vertex / NEE shadow answers
   unsigned int nee, slot;       // hand-offs to nee_kernel / slot_kernel within the iteration
   unsigned int light, path;     // hand-offs from slot_kernel to light_kernel / path_kernel
+  unsigned int bounce;          // hand-off from shade_kernel to bounce_kernel
   unsigned int c_next, s_next;  // fetch cursors of the trace kernels
 };
 // Control words of one lane (an independent wavefront over its own share of
@@ -94,6 +97,7 @@ struct Queues {
   int* slot;
   int* light;
   int* path;
+  int* bounce;
 };
 
 // Worker pool in HBM (structure of arrays).
@@ -144,7 +148,7 @@ __device__ __forceinline__ void store_diff(const Pool& P, int w, const RayDiff& 
 //   [6] (its Clum or -1, S, n, its sample id = slot * 8 + index in the path's samples)
 #define RMN_PART_F4 7
 
-enum Phase { PH_FETCH = 0, PH_SLOT, PH_WAIT_DIRECT, PH_WAIT_CLOSEST, PH_NEE, PH_WAIT_NEE, PH_DONE };
+enum Phase { PH_FETCH = 0, PH_SLOT, PH_WAIT_DIRECT, PH_WAIT_CLOSEST, PH_NEE, PH_WAIT_NEE, PH_DONE, PH_BOUNCE };
 
 // First-vertex light samples a worker draws at once: consecutive direct
 // slots of its unit, each with its own shadow ray in the same queue.
@@ -347,16 +351,18 @@ __device__ __forceinline__ T agg_inc(T* ctr) {
 
 __device__ __forceinline__ void push(int* q, unsigned int* qn, int w) { q[agg_inc(qn)] = w; }
 
-// The logic of one iteration runs as five kernels, each over a compacted
+// The logic of one iteration runs as six kernels, each over a compacted
 // list of the workers in its phase, so a warp executes one phase's code:
 //   shade_kernel  closest-hit answers (sampleRay's body): emit the sky or an
 //                 emitter, start the terminating vertex's light samples, or
-//                 sample the next bounce (closest-hit queue);
+//                 sample the next bounce (closest-hit queue) -- on opaque,
+//                 untextured surfaces handing that to
+//   bounce_kernel the reflection sample and the next closest-hit ray;
 //   nee_kernel    shadow answers of terminating-vertex light samples and the
 //                 workers shade_kernel handed over: emit, then draw the next
 //                 light sample (shadow queue) until the vertex is done;
 //   slot_kernel   shadow answers of first-vertex light samples and the
-//                 workers whose slot ended in the two kernels before: fetch
+//                 workers whose slot ended in the kernels before: fetch
 //                 units until one has a slot left (or retire when no unit is
 //                 left), and hand the worker on by the kind of that slot:
 //   light_kernel  a batch of first-vertex light samples (shadow queue);
@@ -511,6 +517,17 @@ RMN_D int shade_hit(const Job* J, const Pool& P, int w, RmnRng& rng, int4& ph, c
       P.nk[w] = make_int4(0, cnt, sf.entering ? 1 : 0, reflect ? 0 : 1);
       phase = PH_NEE;
     }
+  } else if (!GLASS && !s.has_tex) {
+    // the bounce of an opaque, untextured surface: bounce_kernel samples it
+    // from this record (the NEE vertex's slots, free at a bounce)
+    float4* nv = P.nv + 6 * (size_t)w;
+    nv[0] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, p_rr);
+    nv[1] = make_float4(sf.shapeN.x, sf.shapeN.y, sf.shapeN.z, sf.roughness);
+    nv[2] = make_float4(sf.surfN.x, sf.surfN.y, sf.surfN.z, sf.metallic);
+    nv[3] = make_float4(sf.base.x, sf.base.y, sf.base.z, sf.eta);
+    nv[4] = make_float4(V.x, V.y, V.z, sf.specular);
+    nv[5] = make_float4(rf, sf.opacity, nee ? 1.0f : 0.0f, 0.0f);
+    phase = PH_BOUNCE;
   } else {
     float3 nd, wv;
     int nf = 0;
@@ -604,6 +621,70 @@ __global__ void __launch_bounds__(128, 8) shade_kernel(const Job* __restrict__ j
     store_worker(P, w, ph, phase, rng, un, uid);
     if (phase == PH_WAIT_CLOSEST) push(Q.c[par], &out->c, w);
     else if (phase == PH_NEE) push(Q.nee, &out->nee, w);
+    else if (phase == PH_BOUNCE) push(Q.bounce, &out->bounce, w);
+    else push(Q.slot, &out->slot, w);
+  }
+}
+
+// The bounces shade_kernel handed over (opaque, untextured surfaces): the
+// reflection sample of sampleRay (src/render.cpp:238-250) and the next
+// closest-hit ray, in the operations and order of shade_hit's own bounce
+// (pr = 1 and no absorption on an opaque surface). A warp here runs the
+// reflection sampler alone, not beside emission and light-sample starts.
+__global__ void __launch_bounds__(128, 6) bounce_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+                                                        int par) {
+  QLen* out = &ctl->q[par];
+  const unsigned n = out->bounce;
+  for (unsigned idx = blockIdx.x * blockDim.x + threadIdx.x; idx < n; idx += gridDim.x * blockDim.x) {
+    const int w = Q.bounce[idx];
+    int4 ph, un;
+    long long uid;
+    load_worker(P, w, ph, un, uid);
+    const Params& p = jobs[un.x].p;
+    RmnRng rng;
+    rng.key = rmn_stream_key(p.seed, (uint32_t)un.y, (uint32_t)un.z);
+    rng.ctr = (unsigned)ph.y;
+    const float4* nv = P.nv + 6 * (size_t)w;
+    const float4 a = nv[0], b = nv[1], c = nv[2], d = nv[3], e = nv[4], f = nv[5];
+    Surf sf = default_surf();
+    sf.pos = f3(a.x, a.y, a.z);
+    sf.shapeN = f3(b.x, b.y, b.z);
+    sf.roughness = b.w;
+    sf.surfN = f3(c.x, c.y, c.z);
+    sf.metallic = c.w;
+    sf.base = f3(d.x, d.y, d.z);
+    sf.eta = d.w;
+    sf.specular = e.w;
+    sf.opacity = f.y;
+    const float3 V = f3(e.x, e.y, e.z);
+    const float p_rr = a.w, rf = f.x;
+    const bool nee = f.z != 0.0f;
+    const int depth = ph.z;
+    float3 nd, wv;
+    int nf = 0;
+    sample_reflect(sf, V, rng, nd, wv, nf);
+    wv = wv / 1.0f;  // / P_reflect (1 on an opaque surface)
+    if (nee) wv = wv / p_rr;
+    int phase = PH_SLOT;
+    if (any_finite3(nd) && depth != p.maxd) {
+      wv = wv * f3(1.0f);  // no absorption outside media
+      const float4 pb = P.pb[w];
+      float3 thr = f3(pb.x, pb.y, pb.z) * wv;
+      P.pb[w] = make_float4(thr.x, thr.y, thr.z, rf);
+      if (nf > 0) {
+        float4 pa = P.pa[w];
+        pa.w = pa.w * (1.0f / (float)(1 + nf));
+        P.pa[w] = pa;
+      }
+      P.ro[w] = make_float4(sf.pos.x, sf.pos.y, sf.pos.z, RMN_EPS);
+      P.rd[w] = make_float4(nd.x, nd.y, nd.z, INFINITY);
+      ph.z = depth + 1;
+      ph.w = nee ? FL_EXCLUDE : 0;
+      phase = PH_WAIT_CLOSEST;
+    }
+    if (phase == PH_SLOT) un.z++;
+    store_worker(P, w, ph, phase, rng, un, uid);
+    if (phase == PH_WAIT_CLOSEST) push(Q.c[par], &out->c, w);
     else push(Q.slot, &out->slot, w);
   }
 }
@@ -1392,7 +1473,7 @@ static void launch_qtrace(BatchState* b, const Pool& P, const Queues& Q, Ctl* ct
   else qocc_kernel<COUNT, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
 }
 
-// Iteration k of a chunk (parity k & 1) of one lane: the five logic
+// Iteration k of a chunk (parity k & 1) of one lane: the six logic
 // kernels, then the two traversal kernels. ev (optional) records [0] before
 // the logic, [1] after it and [3] after the traversal.
 static cudaError_t launch_iteration(BatchState* b, int lane, cudaStream_t st, Counters* ctr, int k,
@@ -1408,6 +1489,7 @@ static cudaError_t launch_iteration(BatchState* b, int lane, cudaStream_t st, Co
   const int sms = device_sms();
   const int gs = sms * blocks_per_sm(shade_kernel), gn = sms * blocks_per_sm(nee_kernel);
   shade_kernel<<<gs, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_parts, b->d_status);
+  bounce_kernel<<<sms * blocks_per_sm(bounce_kernel), 128, 0, st>>>(b->d_jobs, P, Q, ctl, par);
   nee_kernel<<<gn, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_parts);
   slot_kernel<<<sms * blocks_per_sm(slot_kernel), 128, 0, st>>>(
       b->d_jobs, nj, P, Q, ctl, &b->d_ctl->next_unit, par, b->table.total_units, b->d_parts);
@@ -1585,7 +1667,7 @@ static size_t worker_bytes(bool glass, bool tex) {
   // vertex and weights, light-sample rays, queue entries
   return 4 * sizeof(int4) + 2 * sizeof(float4) + sizeof(float2) + 8 * sizeof(float4) +
          sizeof(int4) + kDirectBatch * (3 * sizeof(float4) + sizeof(float)) + sizeof(int2) +
-         sizeof(int) * (2 * (3 + kDirectBatch) + 4) + (glass ? RMN_MEDIA * 20 + 4 : 0) + (tex ? 3 * sizeof(float4) : 0);
+         sizeof(int) * (2 * (3 + kDirectBatch) + 5) + (glass ? RMN_MEDIA * 20 + 4 : 0) + (tex ? 3 * sizeof(float4) : 0);
 }
 
 static size_t free_device_bytes() {
@@ -1754,6 +1836,7 @@ rmn_status batch_create(const RenderItem* items_in, int n, bool use_graph, int p
     alloc((void**)&Q.slot, sizeof(int) * per);
     alloc((void**)&Q.light, sizeof(int) * per);
     alloc((void**)&Q.path, sizeof(int) * per);
+    alloc((void**)&Q.bounce, sizeof(int) * per);
     if (b->binned) {
       BatchState::Bins& bb = b->bin[l];
       alloc((void**)&bb.sc, sizeof(int) * per);
