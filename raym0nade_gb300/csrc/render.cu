@@ -1469,7 +1469,8 @@ static void launch_qtrace(BatchState* b, const Pool& P, const Queues& Q, Ctl* ct
   int tb = device_sms() * blocks_per_sm(qtrace_kernel<false, COUNT, ALPHA, STACK>);
   if (tb > lb) tb = lb;
   qtrace_kernel<false, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
-  if (ALPHA) qtrace_kernel<true, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+  // the shadow queue: ordered search with the alpha-test retry, else order-free occlusion
+  if constexpr (ALPHA) qtrace_kernel<true, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
   else qocc_kernel<COUNT, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
 }
 
