@@ -30,6 +30,8 @@ instances (weak scaling) and the maximum time over ranks is reported.
 from __future__ import annotations
 
 import argparse
+import contextlib
+import ctypes
 import json
 import math
 import os
@@ -225,6 +227,25 @@ def cpu_sample_render(scs, insts, threads):
     return paths, secs
 
 
+@contextlib.contextmanager
+def native_stdout_to_stderr():
+    """Sends what native code writes to stdout (the reference's BVH::build
+    prints the size of every tree it builds) to stderr for the duration, so
+    that stdout carries the JSON line alone."""
+    sys.stdout.flush()
+    saved = os.dup(1)
+    os.dup2(2, 1)
+    try:
+        yield
+    finally:
+        try:
+            ctypes.CDLL(None).fflush(None)
+        except (OSError, AttributeError):
+            pass
+        os.dup2(saved, 1)
+        os.close(saved)
+
+
 def cpu_baseline(insts):
     from oracle import bindings
     if not os.path.exists(bindings.PORT_SO):
@@ -232,7 +253,8 @@ def cpu_baseline(insts):
     kind = "reference" if bindings.have_ref() else "port"
     lib = bindings.OracleLib("ref" if kind == "reference" else "port")
     threads = os.cpu_count() or 8
-    scs = [lib.scene(i.scene) for i in insts]
+    with native_stdout_to_stderr():
+        scs = [lib.scene(i.scene) for i in insts]
     paths, secs = cpu_sample_render(scs, insts, threads)
     npx = sum(cpu_sample_pixels(i).size for i in insts)
     return {"value": paths / secs / 1e6, "unit": UNIT, "cores": threads, "kind": kind,

@@ -582,7 +582,7 @@ __device__ __noinline__ int shade_hit_glass(const Job* J, const Pool& P, int w, 
   return shade_hit<true>(J, P, w, rng, ph, un, part, res, o, dir, status);
 }
 
-__global__ void __launch_bounds__(128, 6) shade_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
+__global__ void __launch_bounds__(128, 8) shade_kernel(const Job* __restrict__ jobs, Pool P, Queues Q, Ctl* ctl,
                                                        int par, float4* __restrict__ parts, int* status) {
   const unsigned n = ctl->q[par ^ 1].c;
   const int* in = Q.c[par ^ 1];
