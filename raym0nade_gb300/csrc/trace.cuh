@@ -143,6 +143,46 @@ RMN_D void trav_begin(const DevScene& s, TravT<Stack>& t, float tmax) {
   trav_begin(s.root, t, tmax);
 }
 
+// One inner-node step of dfs_rayHit (src/bvh.cpp:70-88): both child boxes
+// against [tmin, tmax]; the nearer entry goes first (ties: the right child),
+// the other is deferred with its entry distance when both are hit, or taken
+// directly when only it is hit and it starts before tmax. Returns 0 with
+// `cur` the next node (inner or leaf), 1 when neither child is entered (the
+// caller pops), -2 when the stack would overflow.
+template <bool COUNT, class Stack>
+RMN_D int inner_step(const DevNode* __restrict__ nodes, const TRay& r, float tmin, float tmax, int& cur, int& sp,
+                     Stack& stack, TraceCounters* cnt) {
+  const DevNode* n = nodes + cur;
+  float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
+  int4 D = __ldg(&n->d);
+  if (COUNT) cnt->inner++;
+  float tl0, tl1;
+  bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, tmax, tl0);
+  bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, tmax, tl1);
+  int nref, fref;
+  bool hn, hf;
+  float tlf;
+  if (tl0 < tl1) {
+    nref = D.x; hn = h0; fref = D.y; hf = h1; tlf = tl1;
+  } else {
+    nref = D.y; hn = h1; fref = D.x; hf = h0; tlf = tl0;
+  }
+  if (hn) {
+    if (hf) {
+      if (sp >= Stack::kCap) return -2;
+      stack.put(sp, make_int2(fref, __float_as_int(tlf)));
+      ++sp;
+    }
+    cur = nref;
+    return 0;
+  }
+  if (hf && tlf < tmax) {
+    cur = fref;
+    return 0;
+  }
+  return 1;
+}
+
 // Runs up to `budget` steps; a step is one inner node (both child boxes) or
 // one triangle of a leaf, so lanes of a warp at inner nodes and lanes in
 // leaves advance together instead of waiting for a whole leaf. Returns 1
@@ -171,34 +211,9 @@ RMN_D int trav_run(const DevScene& s, const TRay& r, float tmin, float aim, Trav
     } else {
       const int cur = t.cur;
       if (cur >= 0) {
-        const DevNode* n = s.nodes + cur;
-        float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
-        int4 D = __ldg(&n->d);
-        if (COUNT) cnt->inner++;
-        float tl0, tl1;
-        bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, t.tmax, tl0);
-        bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, t.tmax, tl1);
-        int nref, fref;
-        bool hn, hf;
-        float tlf;
-        if (tl0 < tl1) {
-          nref = D.x; hn = h0; fref = D.y; hf = h1; tlf = tl1;
-        } else {
-          nref = D.y; hn = h1; fref = D.x; hf = h0; tlf = tl0;
-        }
-        if (hn) {
-          if (hf) {
-            if (t.sp >= Stack::kCap) return -2;
-            t.stack.put(t.sp, make_int2(fref, __float_as_int(tlf)));
-            ++t.sp;
-          }
-          t.cur = nref;
-          continue;
-        }
-        if (hf && tlf < t.tmax) {
-          t.cur = fref;
-          continue;
-        }
+        const int k = inner_step<COUNT>(s.nodes, r, tmin, t.tmax, t.cur, t.sp, t.stack, cnt);
+        if (k == -2) return -2;
+        if (k == 0) continue;
       } else {
         const int x = ~cur;
         const int count = x & 15;
@@ -285,34 +300,12 @@ RMN_D int coop_nodes(const DevNode* __restrict__ nodes, const TRay& r, float tmi
       if (res) continue;
     }
     if (t.cur >= 0) {
-      const DevNode* n = nodes + t.cur;
-      float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
-      int4 D = __ldg(&n->d);
-      if (COUNT) cnt->inner++;
-      float tl0, tl1;
-      bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, t.tmax, tl0);
-      bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, t.tmax, tl1);
-      int nref, fref;
-      bool hn, hf;
-      float tlf;
-      if (tl0 < tl1) {
-        nref = D.x; hn = h0; fref = D.y; hf = h1; tlf = tl1;
-      } else {
-        nref = D.y; hn = h1; fref = D.x; hf = h0; tlf = tl0;
+      const int k = inner_step<COUNT>(nodes, r, tmin, t.tmax, t.cur, t.sp, t.stack, cnt);
+      if (k == -2) {
+        res = -2;
+        continue;
       }
-      if (hn) {
-        if (hf) {
-          if (t.sp >= Stack::kCap) {
-            res = -2;
-            continue;
-          }
-          t.stack.put(t.sp, make_int2(fref, __float_as_int(tlf)));
-          ++t.sp;
-        }
-        t.cur = nref;
-      } else if (hf && tlf < t.tmax) {
-        t.cur = fref;
-      } else {
+      if (k == 1) {
         t.pop = true;
         continue;
       }
@@ -473,34 +466,12 @@ RMN_D int occ_nodes(const DevNode* __restrict__ nodes, const TRay& r, float tmin
       if (res) continue;
     }
     if (t.cur >= 0) {
-      const DevNode* n = nodes + t.cur;
-      float4 A = __ldg(&n->a), B = __ldg(&n->b), C = __ldg(&n->c);
-      int4 D = __ldg(&n->d);
-      if (COUNT) cnt->inner++;
-      float tl0, tl1;
-      bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, tmax, tl0);
-      bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, tmax, tl1);
-      int nref, fref;
-      bool hn, hf;
-      float tlf;
-      if (tl0 < tl1) {
-        nref = D.x; hn = h0; fref = D.y; hf = h1; tlf = tl1;
-      } else {
-        nref = D.y; hn = h1; fref = D.x; hf = h0; tlf = tl0;
+      const int k = inner_step<COUNT>(nodes, r, tmin, tmax, t.cur, t.sp, t.stack, cnt);
+      if (k == -2) {
+        res = -2;
+        continue;
       }
-      if (hn) {
-        if (hf) {
-          if (t.sp >= Stack::kCap) {
-            res = -2;
-            continue;
-          }
-          t.stack.put(t.sp, make_int2(fref, __float_as_int(tlf)));
-          ++t.sp;
-        }
-        t.cur = nref;
-      } else if (hf && tlf < tmax) {
-        t.cur = fref;
-      } else {
+      if (k == 1) {
         t.pop = true;
         continue;
       }
