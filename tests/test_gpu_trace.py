@@ -108,6 +108,52 @@ def test_shadow_matches_oracle(port):
     assert np.array_equal(occ, port.scene(soup).trace_shadow(sr))
 
 
+def _surface_rays(sc, n, seed, shadow):
+    """Rays leaving the surface of a scene: from a random point of a random
+    triangle, 1e-3 along its upward normal, into the upper hemisphere;
+    shadow rays with aims U(0.1, 50). Many cross the mesh near shared edges."""
+    rng = np.random.default_rng(seed)
+    P, I = sc.positions.astype(np.float64), sc.indices
+    t = rng.integers(0, I.shape[0], n)
+    a, b, c = P[I[t, 0]], P[I[t, 1]], P[I[t, 2]]
+    u, v = rng.random(n), rng.random(n)
+    m = u + v > 1
+    u[m], v[m] = 1 - u[m], 1 - v[m]
+    p = a + (b - a) * u[:, None] + (c - a) * v[:, None]
+    nrm = np.cross(b - a, c - a)
+    nrm /= np.linalg.norm(nrm, axis=1, keepdims=True)
+    nrm *= np.sign(nrm[:, 1:2] + 1e-12)
+    d = rng.standard_normal((n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d = d * np.sign((d * nrm).sum(1, keepdims=True))
+    r = np.zeros((n, 8), np.float32)
+    r[:, 0:3] = p + nrm * 1e-3
+    r[:, 3] = 1e-4
+    r[:, 4:7] = d
+    r[:, 7] = np.inf if not shadow else rng.uniform(0.1, 50.0, n)
+    return r
+
+
+def test_heightfield_surface_rays_match_oracle(port):
+    """A closed heightfield mesh (every edge shared by two triangles, often
+    in different leaves) and rays leaving its surface: closest hits (the
+    reference's visit order, warp-cooperative leaves) and occlusion (the
+    order-free kernel with pending leaves) identical to the oracle's
+    ordered search."""
+    hf = scenes.heightfield(500, seed=3)
+    m = api.Model(hf)
+    cr = _surface_rays(hf, 400_000, 81, False)
+    sr = _surface_rays(hf, 400_000, 82, True)
+    ps = port.scene(hf)
+    f, t, _ = gpu_closest(m, cr)
+    pf, pt, _ = ps.trace_closest(cr, threads=os.cpu_count() or 8)
+    assert np.array_equal(f, pf) and np.array_equal(t.view(np.int32), pt.view(np.int32))
+    occ = m.rayHit_test(torch.from_numpy(sr).cuda()).cpu().numpy()
+    ref = ps.trace_shadow(sr, threads=os.cpu_count() or 8)
+    assert np.array_equal(occ, ref)
+    assert 0.05 < ref.mean() < 0.95 and (pf >= 0).mean() > 0.05
+
+
 def test_cornell_queries(port):
     c = scenes.cornell()
     rays = scenes.random_rays(100000, 45)
