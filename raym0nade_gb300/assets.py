@@ -12,9 +12,9 @@ import into a ``Scene``.
   dispatch on the file extension, "png"/"PNG" or "dds"/"DDS", anything else
   printed as unsupported and left empty.
 * ``load_model`` is Model::Model(model_folder, model_name, skyMap_name)
-  (src/model.cpp:172-215) for Wavefront OBJ/MTL files, read natively by
-  the library (rmn_model_read, csrc/model_io.cpp); assimp, which the
-  reference imports with, is not part of this build. Materials follow
+  (src/model.cpp:172-215) for Wavefront OBJ/MTL and binary FBX files, read
+  natively by the library (rmn_model_read, csrc/model_io.cpp, csrc/fbx.cpp);
+  the library does not use assimp, which the reference imports with. Materials follow
   Material::loadMaterialProperties (src/material.cpp:300-336): only the
   name, the opacity and the textures are read -- the MTL's colours (Kd, Ks,
   Ke) are not, as in the reference.

@@ -1,6 +1,6 @@
 // Binary FBX models for Model::Model (src/model.cpp:172-215), which reads
 // them with assimp (aiProcess_Triangulate | PreTransformVertices |
-// SortByPType | FixInfacingNormals). assimp is not part of this build; what
+// SortByPType | FixInfacingNormals). The library does not use assimp; what
 // its FBX import does is restated here from the container's published
 // description (the node-record layout Blender's and assimp's readers
 // document) and assimp's documented behaviour:

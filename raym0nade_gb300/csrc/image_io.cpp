@@ -12,7 +12,7 @@
 //           SkyBox::load (src/component.cpp:69-114) consumes it: Radiance
 //           RGBE to float32 RGB, flat or run-length-encoded scanlines.
 //
-// libpng, imageio and FreeImage are not part of this build. The formats are
+// The library uses none of libpng, imageio and FreeImage. The formats are
 // decoded from their published specifications: PNG (ISO/IEC 15948) with zlib
 // and deflate (RFC 1950, RFC 1951); Radiance RGBE (G. Ward, "Real Pixels",
 // Graphics Gems II, and the Radiance file format notes); the DirectDraw

@@ -5,7 +5,7 @@
 //
 // The reference imports with assimp (aiProcess_Triangulate |
 // PreTransformVertices | SortByPType | FixInfacingNormals, with
-// AI_CONFIG_PP_PTV_KEEP_HIERARCHY); assimp is not part of this build. What it
+// AI_CONFIG_PP_PTV_KEEP_HIERARCHY); the library does not use assimp. What it
 // does for OBJ files is restated from its documented behaviour:
 //  * one mesh per run of faces with the same object/group and material; a
 //    vertex per face corner; polygons as a fan from their first corner;
