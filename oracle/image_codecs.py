@@ -1,5 +1,5 @@
 """Oracle for the texture front-end. TEST INFRASTRUCTURE ONLY: imported by
-tests/ as the checker of rmn_image_load and of the device mip chains, never
+tests/ to check rmn_image_load and the device mip chains against, never
 by the library.
 
 ``mip_chain`` restates ImageData::generateMipmaps (src/material.cpp:107-129)

@@ -76,9 +76,9 @@ void ref_photo(float* recs, int w, int h, int stages, int options, const float* 
 #endif
 
 // Per-pixel seed of the reference's Generator in the deterministic render
-// driver: the reference seeds one mt19937 per worker thread
-// (src/render.cpp:658-661), which makes images depend on scheduling; the
-// driver seeds one per pixel instead.
+// loop: the reference seeds one mt19937 per worker thread
+// (src/render.cpp:658-661), which makes images depend on scheduling; this
+// loop seeds one per pixel instead.
 static inline uint32_t orc_pixel_seed(uint64_t seed, uint32_t pixel) {
   uint64_t z = seed * 0x9E3779B97F4A7C15ULL + (uint64_t)pixel * 0xBF58476D1CE4E5B9ULL + 1u;
   z = (z ^ (z >> 31)) * 0x94D049BB133111EBULL;

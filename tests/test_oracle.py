@@ -252,7 +252,7 @@ MIP_SIZES = [(21, 37), (1, 64), (3, 300), (16, 2048), (255, 257), (1, 1), (600, 
 
 
 def test_mip_chain_matches_reference(ref_tex):
-    """oracle/image_codecs.mip_chain (the checker of the device-built chains)
+    """oracle/image_codecs.mip_chain (what the device-built chains are checked against)
     against the reference's own ImageData::generateMipmaps, level for level."""
     from oracle.image_codecs import mip_chain
     rng = np.random.default_rng(31)
