@@ -1137,7 +1137,7 @@ __global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) qtrace_kernel(con
 // with pending leaves (trace.cuh, occ_nodes / occ_leaves), the same answer
 // as the ordered search of qtrace_kernel<true, ...> in fewer instructions.
 template <bool COUNT, int STACK>
-__global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) qocc_kernel(const Job* __restrict__ jobs, Pool P,
+__global__ void __launch_bounds__(128, RMN_OCC_BLOCKS) qocc_kernel(const Job* __restrict__ jobs, Pool P,
                                                                            Queues Q, Ctl* ctl, int par,
                                                                            int* status, Counters* ctr) {
   const int lane = threadIdx.x & 31;
@@ -1150,8 +1150,9 @@ __global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) qocc_kernel(const
   int w = 0;
   TRay r;
   float tmin = 0.0f, aim = 0.0f;
-  __shared__ int2 sstack[STACK * 128];
-  OccT<SharedStackN<STACK>> t;
+  __shared__ int sstack[STACK * 128];  // node references: occlusion pops skip nothing
+  __shared__ OccExchange xch;
+  OccT<SharedStackRefN<STACK>> t;
   t.stack.base = sstack + threadIdx.x;
   t.c0 = t.c1 = 0;
   const DevNode* nodes = nullptr;
@@ -1187,7 +1188,7 @@ __global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) qocc_kernel(const
     if (__ballot_sync(0xffffffffu, active) == 0) break;
     // boxes against HitRecord(eps, aimDepth + eps) throughout
     const int st = occ_nodes<COUNT>(nodes, r, tmin, aim + RMN_EPS, t, active, kOccSteps, &tc);
-    const bool occ = occ_leaves<false>(tri, r, tmin, aim, t);
+    const bool occ = occ_leaves<false>(tri, r, tmin, aim, t, xch);
     if (!active || (st == 0 && !occ)) continue;
     const float occluded = (occ && st != -2) ? 1.0f : 0.0f;
     if (w >= 0) P.res[w] = make_float2(occluded, 0.0f);
@@ -1470,8 +1471,13 @@ static void launch_qtrace(BatchState* b, const Pool& P, const Queues& Q, Ctl* ct
   if (tb > lb) tb = lb;
   qtrace_kernel<false, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
   // the shadow queue: ordered search with the alpha-test retry, else order-free occlusion
-  if constexpr (ALPHA) qtrace_kernel<true, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
-  else qocc_kernel<COUNT, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+  if constexpr (ALPHA) {
+    qtrace_kernel<true, COUNT, ALPHA, STACK><<<tb, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+  } else {
+    int ob = device_sms() * blocks_per_sm(qocc_kernel<COUNT, STACK>);
+    if (ob > lb) ob = lb;
+    qocc_kernel<COUNT, STACK><<<ob, 128, 0, st>>>(b->d_jobs, P, Q, ctl, par, b->d_status, ctr);
+  }
 }
 
 // Iteration k of a chunk (parity k & 1) of one lane: the six logic

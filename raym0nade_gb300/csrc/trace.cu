@@ -93,7 +93,7 @@ __global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) trace_kernel(DevS
 // Occlusion queries of a scene without alpha-tested materials: pending
 // leaves, order-free (trace.cuh, occ_nodes / occ_leaves).
 template <int STACK>
-__global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) occ_kernel(DevScene s, const float4* __restrict__ rays,
+__global__ void __launch_bounds__(128, RMN_OCC_BLOCKS) occ_kernel(DevScene s, const float4* __restrict__ rays,
                                                                           int64_t n, uint8_t* __restrict__ occ,
                                                                           unsigned long long* __restrict__ next,
                                                                           int* status) {
@@ -103,8 +103,9 @@ __global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) occ_kernel(DevSce
   int64_t i = 0;
   TRay r;
   float aim = 0.0f;
-  __shared__ int2 sstack[STACK * 128];
-  OccT<SharedStackN<STACK>> t;
+  __shared__ int sstack[STACK * 128];  // node references: occlusion pops skip nothing
+  __shared__ OccExchange xch;
+  OccT<SharedStackRefN<STACK>> t;
   t.stack.base = sstack + threadIdx.x;
   t.c0 = t.c1 = 0;
   for (;;) {
@@ -130,7 +131,7 @@ __global__ void __launch_bounds__(128, RMN_COOP_BLOCKS(STACK)) occ_kernel(DevSce
     if (__ballot_sync(0xffffffffu, active) == 0) return;
     // HitRecord(eps, aimDepth + eps); occluded iff a hit is nearer than aimDepth
     const int st = occ_nodes<false>(s.nodes, r, RMN_EPS, aim + RMN_EPS, t, active, kOccSteps, nullptr);
-    const bool o = occ_leaves<true>(s.tri, r, RMN_EPS, aim, t);
+    const bool o = occ_leaves<true>(s.tri, r, RMN_EPS, aim, t, xch);
     if (!active || (st == 0 && !o)) continue;
     if (st == -2) atomicExch(status, (int)rmn::kDevStackOverflow);
     occ[i] = (o && st != -2) ? 1 : 0;

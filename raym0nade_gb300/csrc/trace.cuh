@@ -116,6 +116,15 @@ struct SharedStackN {
   RMN_D int2 get(int i) const { return base[i * 128]; }
 };
 using SharedStack = SharedStackN<RMN_STACK>;
+// References only (order-free occlusion): get() reports an entry distance of
+// -inf, so a pop never skips an entry.
+template <int N>
+struct SharedStackRefN {
+  static constexpr int kCap = N;
+  int* base;
+  RMN_D void put(int i, int2 v) { base[i * 128] = v.x; }
+  RMN_D int2 get(int i) const { return make_int2(base[i * 128], __float_as_int(-INFINITY)); }
+};
 
 template <class Stack>
 struct TravT {
@@ -495,14 +504,31 @@ RMN_D int occ_nodes(const DevNode* __restrict__ nodes, const TRay& r, float tmin
   return res;
 }
 
+// The leaf phase's exchange in shared memory, per 128-thread block: each
+// lane with pending triangles writes its ray, its leaves and (batch
+// kernels) its triangle array once, and its lane index into its warp's
+// owner table for each of its triangles; the lane testing triangle k of the
+// warp's list reads its owner and the owner's data from there.
+constexpr int kOccOwn = 32 * 30;  // per warp: 32 lanes x two leaves of at most 15 triangles
+struct OccExchange {
+  float4 ray[2 * 128];         // (origin, aim), (direction, t_min)
+  int4 leaf[128];              // a0, c0, a1, first index of the lane's triangles in the warp's list
+  const float4* tri[128];
+  unsigned char own[4][kOccOwn];
+};
+
 // Phase 2 (all 32 lanes): the pending leaves' triangles, 32 at a time;
-// true for a lane whose ray has a hit at eps < t < aim (`tmin` = eps).
-// Clears the pending leaves. SAME_TRI as in coop_leaves.
+// true for a lane whose ray has a hit at tmin < t < aim. Clears the pending
+// leaves. SAME_TRI: one scene for the whole warp (its triangle array is not
+// exchanged).
 template <bool SAME_TRI, class Stack>
-RMN_D bool occ_leaves(const float4* __restrict__ tri, const TRay& r, float tmin, float aim, OccT<Stack>& t) {
+RMN_D bool occ_leaves(const float4* __restrict__ tri, const TRay& r, float tmin, float aim, OccT<Stack>& t,
+                      OccExchange& x) {
   const unsigned FULL = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  const int cnt = t.c0 + t.c1;
+  const int wb = threadIdx.x & ~31;
+  unsigned char* own = x.own[threadIdx.x >> 5];
+  const int cnt = t.c0 + t.c1;  // at most 30
   if (!__any_sync(FULL, cnt > 0)) return false;
   int incl = cnt;
 #pragma unroll
@@ -510,43 +536,36 @@ RMN_D bool occ_leaves(const float4* __restrict__ tri, const TRay& r, float tmin,
     const int v = __shfl_up_sync(FULL, incl, off);
     if (lane >= off) incl += v;
   }
-  const int total = __shfl_sync(FULL, incl, 31);
+  const int total = __shfl_sync(FULL, incl, 31);  // at most kOccOwn
   const int excl = incl - cnt;
+  if (cnt > 0) {
+    x.ray[2 * threadIdx.x] = make_float4(r.o.x, r.o.y, r.o.z, aim);
+    x.ray[2 * threadIdx.x + 1] = make_float4(r.d.x, r.d.y, r.d.z, tmin);
+    x.leaf[threadIdx.x] = make_int4(t.a0, t.c0, t.a1, excl);
+    if (!SAME_TRI) x.tri[threadIdx.x] = tri;
+    for (int k = excl; k < incl; ++k) own[k] = (unsigned char)lane;
+  }
+  __syncwarp();
   unsigned occluded = 0;  // bit per owner lane
 #pragma unroll 1
   for (int base = 0; base < total; base += 32) {
     const int k = base + lane;
-    int lo = 0;
-#pragma unroll
-    for (int st = 16; st >= 1; st >>= 1) {
-      const int v = __shfl_sync(FULL, incl, lo + st - 1);
-      if (v <= k) lo += st;
-    }
-    const int ow = min(lo, 31);
-    const int loc = k - __shfl_sync(FULL, excl, ow);
-    const int oa0 = __shfl_sync(FULL, t.a0, ow), oc0 = __shfl_sync(FULL, t.c0, ow);
-    const int oa1 = __shfl_sync(FULL, t.a1, ow);
-    TRay q;
-    q.o.x = __shfl_sync(FULL, r.o.x, ow);
-    q.o.y = __shfl_sync(FULL, r.o.y, ow);
-    q.o.z = __shfl_sync(FULL, r.o.z, ow);
-    q.d.x = __shfl_sync(FULL, r.d.x, ow);
-    q.d.y = __shfl_sync(FULL, r.d.y, ow);
-    q.d.z = __shfl_sync(FULL, r.d.z, ow);
-    const float qmin = __shfl_sync(FULL, tmin, ow), qaim = __shfl_sync(FULL, aim, ow);
-    const float4* qtri = tri;
-    if (!SAME_TRI) {
-      const unsigned long long p = reinterpret_cast<unsigned long long>(tri);
-      const unsigned lo32 = __shfl_sync(FULL, (unsigned)p, ow), hi32 = __shfl_sync(FULL, (unsigned)(p >> 32), ow);
-      qtri = reinterpret_cast<const float4*>(((unsigned long long)hi32 << 32) | lo32);
-    }
     bool h = false;
+    int ow = 0;
     if (k < total) {
-      const int i = loc < oc0 ? oa0 + loc : oa1 + (loc - oc0);
-      const float4* tp = qtri + 3 * i;
+      ow = own[k];
+      const int o = wb + ow;
+      const int4 lf = x.leaf[o];
+      const float4 ra = x.ray[2 * o], rb = x.ray[2 * o + 1];
+      const int loc = k - lf.w;  // in [0, c0 + c1) of the owner; loc >= c0 only when c1 > 0
+      const int i = loc < lf.y ? lf.x + loc : lf.z + (loc - lf.y);
+      TRay q;
+      q.o = f3(ra.x, ra.y, ra.z);
+      q.d = f3(rb.x, rb.y, rb.z);
+      const float4* tp = (SAME_TRI ? tri : x.tri[o]) + 3 * i;
       float4 a = __ldg(tp), b = __ldg(tp + 1), c = __ldg(tp + 2);
       const float th = tri_t(q, f3(a), f3(b), f3(c), b.w);
-      h = qmin < th && th < qaim;
+      h = rb.w < th && th < ra.w;
     }
     // the owners of the lanes that found an occluder
     unsigned m = __ballot_sync(FULL, h);
@@ -556,6 +575,7 @@ RMN_D bool occ_leaves(const float4* __restrict__ tri, const TRay& r, float tmin,
       occluded |= 1u << __shfl_sync(FULL, ow, src);
     }
   }
+  __syncwarp();
   t.c0 = t.c1 = 0;
   return (occluded >> lane) & 1u;
 }
