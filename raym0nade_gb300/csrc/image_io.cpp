@@ -160,6 +160,34 @@ const uint16_t kDistBase[30] = {1,   2,   3,   4,   5,   7,    9,    13,   17,  
 const uint8_t kDistExtra[30] = {0, 0, 0, 0, 1, 1, 2, 2, 3, 3, 4, 4, 5, 5, 6, 6, 7, 7, 8, 8, 9, 9, 10, 10, 11, 11, 12, 12, 13, 13};
 const uint8_t kCodeLengthOrder[19] = {16, 17, 18, 0, 8, 7, 9, 6, 10, 5, 11, 4, 12, 3, 13, 2, 14, 1, 15};
 
+// A back-reference: dst[0, len) = the bytes d before each, dst[k] =
+// dst[k - d] in order, with len <= room (the bytes left in the output).
+// Writes may run up to 7 bytes past len while they stay within room: those
+// bytes lie ahead of the output position and are written again before any
+// back-reference can read them.
+inline void copy_match(uint8_t* dst, size_t d, size_t len, size_t room) {
+  const uint8_t* src = dst - d;
+  if (d >= 8 && len + 7 <= room) {  // 8 bytes at a time: each read lies wholly before its write
+    for (size_t k = 0; k < len; k += 8) {
+      uint64_t v;
+      std::memcpy(&v, src + k, 8);
+      std::memcpy(dst + k, &v, 8);
+    }
+    return;
+  }
+  if (d < 8 && len > 16) {  // a short period: copy the pattern at doubling distances
+    size_t done = 0, span = d;  // dst[-d, done) holds the pattern; span = done + d
+    while (done < len) {
+      const size_t n = span < len - done ? span : len - done;
+      std::memcpy(dst + done, src, n);  // from dst - d, span (a multiple of d) before, no overlap
+      done += n;
+      span += n;
+    }
+    return;
+  }
+  for (size_t k = 0; k < len; ++k) dst[k] = src[k];
+}
+
 // A deflate stream into out[0, cap); *produced = bytes written. Returns
 // nullptr or a description of what is wrong with the stream.
 const char* inflate_stream(BitReader& br, uint8_t* out, size_t cap, size_t* produced) {
@@ -262,18 +290,32 @@ const char* inflate_stream(BitReader& br, uint8_t* out, size_t cap, size_t* prod
       const size_t d = kDistBase[ds] + e;
       if (d > o) return "distance before the start of the data";
       if (o + len > cap) return "more image data than the image holds";
-      for (size_t k = 0; k < len; ++k, ++o) out[o] = out[o - d];
+      copy_match(out + o, d, len, cap - o);
+      o += len;
     }
   } while (!final_block);
   *produced = o;
   return nullptr;
 }
 
+// Adler-32 (RFC 1950 section 8.2). Over 16 bytes p[0..15] the sums advance
+// as a += sum p[k], b += 16 a + sum (16 - k) p[k]: the same values the byte
+// loop reaches, from sums that do not depend on one another.
 uint32_t adler32(const uint8_t* p, size_t n) {
   uint32_t a = 1, b = 0;
   while (n) {
     const size_t m = n < 5552 ? n : 5552;  // largest run without overflow of b
-    for (size_t i = 0; i < m; ++i) {
+    size_t i = 0;
+    for (; i + 16 <= m; i += 16) {
+      uint32_t s1 = 0, s2 = 0;
+      for (int k = 0; k < 16; ++k) {
+        s1 += p[i + k];
+        s2 += (uint32_t)(16 - k) * p[i + k];
+      }
+      b += 16 * a + s2;
+      a += s1;
+    }
+    for (; i < m; ++i) {
       a += p[i];
       b += a;
     }
@@ -536,10 +578,49 @@ inline int paeth(int a, int b, int c) {
   return mbc < pa ? bc : a;
 }
 
+// unfilter_row for B bytes per pixel and a row of whole pixels (n a multiple
+// of B): the left (a) and upper-left (c) bytes of the B channels stay in
+// registers from one pixel to the next instead of being read back from the
+// row just written.
+template <int B>
+void unfilter_pixels(int ft, const uint8_t* src, const uint8_t* up, uint8_t* out, size_t n) {
+  int a[B], c[B];
+  for (int j = 0; j < B; ++j) {  // the first pixel: a = c = 0
+    const int v = ft == 2 || ft == 4 ? up[j] : ft == 3 ? up[j] >> 1 : 0;
+    a[j] = out[j] = (uint8_t)(src[j] + v);
+    c[j] = up[j];
+  }
+  switch (ft) {
+    case 1:
+      for (size_t i = B; i < n; i += B)
+#pragma GCC unroll 4
+        for (int j = 0; j < B; ++j) a[j] = out[i + j] = (uint8_t)(src[i + j] + a[j]);
+      break;
+    case 3:
+      for (size_t i = B; i < n; i += B)
+#pragma GCC unroll 4
+        for (int j = 0; j < B; ++j) a[j] = out[i + j] = (uint8_t)(src[i + j] + ((a[j] + up[i + j]) >> 1));
+      break;
+    case 4:
+      for (size_t i = B; i < n; i += B)
+#pragma GCC unroll 4
+        for (int j = 0; j < B; ++j) {
+          const int b = up[i + j];
+          a[j] = out[i + j] = (uint8_t)(src[i + j] + paeth(a[j], b, c[j]));
+          c[j] = b;
+        }
+      break;
+  }
+}
+
 // One scanline's filter undone (ISO/IEC 15948 section 9): each byte plus the
 // predictor from the left (a), upper (b) and upper-left (c) reconstructed
 // bytes; bpp = bytes per complete pixel, at least 1.
 void unfilter_row(int ft, const uint8_t* src, const uint8_t* up, uint8_t* out, size_t n, int bpp) {
+  if ((ft == 1 || ft == 3 || ft == 4) && n >= (size_t)bpp && n % bpp == 0) {
+    if (bpp == 3) return unfilter_pixels<3>(ft, src, up, out, n);
+    if (bpp == 4) return unfilter_pixels<4>(ft, src, up, out, n);
+  }
   const size_t k = (size_t)bpp < n ? (size_t)bpp : n;
   switch (ft) {
     case 0:
@@ -657,10 +738,14 @@ rmn_status decode_png(const std::vector<uint8_t>& f, bool header_only, Decoded& 
       const uint8_t* src = &raw[at_raw + 1];
       at_raw += 1 + stride;
       if (ft > 4) return fail(RMN_ERR_INVALID_ARGUMENT, "PNG: bad filter type %d", ft);
-      unfilter_row(ft, src, prev.data(), cur.data(), stride, bpp);
-      // samples of this row to 8-bit RGB
       const size_t y = ps.y0 + r * ps.dy;
       uint8_t* px = &img.bytes[(y * w + ps.x0) * 3];
+      if (depth == 8 && ctype == 2 && !interlace) {  // the image's own rows are the scanlines
+        unfilter_row(ft, src, r ? px - stride : prev.data(), px, stride, bpp);
+        continue;
+      }
+      unfilter_row(ft, src, prev.data(), cur.data(), stride, bpp);
+      // samples of this row to 8-bit RGB
       const size_t step = 3 * (size_t)ps.dx;
       const uint8_t* q = cur.data();
       if (depth == 8 && ctype == 2 && ps.dx == 1) {

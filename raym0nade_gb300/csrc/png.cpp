@@ -15,16 +15,26 @@
 
 namespace {
 
+// CRC-32 of ISO 3309 / PNG section 5.5 (reflected polynomial 0xEDB88320),
+// eight bytes per step by "slicing-by-8" (Kounavis and Berry, 2008): t[k][b]
+// is the CRC of byte b followed by k zero bytes, so the eight bytes' table
+// entries are independent loads XORed together.
 struct CrcTable {
-  uint32_t t[256];
+  uint32_t t[8][256];
   CrcTable() {
     for (uint32_t n = 0; n < 256; ++n) {
       uint32_t c = n;
       for (int k = 0; k < 8; ++k) c = (c & 1) ? 0xEDB88320u ^ (c >> 1) : c >> 1;
-      t[n] = c;
+      t[0][n] = c;
     }
+    for (int k = 1; k < 8; ++k)
+      for (int n = 0; n < 256; ++n) t[k][n] = t[0][t[k - 1][n] & 0xff] ^ (t[k - 1][n] >> 8);
   }
 };
+
+inline uint32_t load_le32(const uint8_t* p) {
+  return (uint32_t)p[0] | (uint32_t)p[1] << 8 | (uint32_t)p[2] << 16 | (uint32_t)p[3] << 24;
+}
 
 void put32(std::vector<uint8_t>& v, uint32_t x) {
   v.push_back((uint8_t)(x >> 24));
@@ -57,8 +67,15 @@ namespace rmn {
 
 uint32_t png_crc32(uint32_t crc, const uint8_t* p, size_t n) {
   static const CrcTable table;  // initialised once, thread-safe
+  const auto& t = table.t;
   crc = ~crc;
-  for (size_t i = 0; i < n; ++i) crc = table.t[(crc ^ p[i]) & 0xff] ^ (crc >> 8);
+  size_t i = 0;
+  for (; i + 8 <= n; i += 8) {
+    const uint32_t lo = crc ^ load_le32(p + i), hi = load_le32(p + i + 4);
+    crc = t[7][lo & 0xff] ^ t[6][lo >> 8 & 0xff] ^ t[5][lo >> 16 & 0xff] ^ t[4][lo >> 24] ^ t[3][hi & 0xff] ^
+          t[2][hi >> 8 & 0xff] ^ t[1][hi >> 16 & 0xff] ^ t[0][hi >> 24];
+  }
+  for (; i < n; ++i) crc = t[0][(crc ^ p[i]) & 0xff] ^ (crc >> 8);
   return ~crc;
 }
 

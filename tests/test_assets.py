@@ -87,6 +87,21 @@ def test_png_large_image_dynamic_blocks(tmp_path):
     assert np.array_equal(got, s[..., :3].astype(np.uint8))
 
 
+def test_png_back_references_of_every_short_period(tmp_path):
+    """Deflate matches whose distance is below, at and above 8 bytes, long
+    and short, some ending on the last byte of the image data: gray rows
+    that repeat a random pattern of 1-17 bytes."""
+    rng = np.random.default_rng(11)
+    for period in range(1, 18):
+        for w in (period + 1, 19, 40, 263, 600):
+            pattern = rng.integers(0, 256, period)
+            h = int(rng.integers(1, 4))
+            s = np.resize(pattern, (h, w, 1))
+            data = F.encode_png(s, 0, 8, filters=(0,), level=9)
+            got = assets.load_png(write(tmp_path, "p.png", data))
+            assert np.array_equal(got, np.repeat(s, 3, axis=2).astype(np.uint8)), (period, w, h)
+
+
 def test_png_reads_what_save_png_writes(tmp_path):
     lib = _lib.load()
     rng = np.random.default_rng(3)
@@ -484,6 +499,12 @@ def test_save_png_compresses_and_round_trips(tmp_path, kind):
     want = np.clip(img * np.float32(255), 0, 255).astype(np.uint8)
     assert np.array_equal(image_codecs.png_read(p), want)
     assert np.array_equal(assets.load_png(p), want)
+    data, at, chunks = open(p, "rb").read(), 8, 0
+    while at < len(data):  # every chunk's CRC-32 as zlib computes it
+        n = int.from_bytes(data[at:at + 4], "big")
+        assert int.from_bytes(data[at + 8 + n:at + 12 + n], "big") == zlib.crc32(data[at + 4:at + 8 + n])
+        at, chunks = at + 12 + n, chunks + 1
+    assert at == len(data) and chunks >= 3
     size, raw = os.path.getsize(p), h * (1 + 3 * w)
     if kind in ("smooth", "flat"):
         assert size < 0.1 * raw
