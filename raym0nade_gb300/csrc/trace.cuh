@@ -62,6 +62,28 @@ RMN_D bool box_hit(const TRay& r, float3 lo, float3 hi, float tmin, float tmax, 
   return L < R;
 }
 
+// A box test that accepts every box box_hit accepts (and a few more), for
+// queries whose answer does not depend on the order of visits or on the
+// entry distances (occlusion), on rays with no axis under the
+// origin-inside rule (r.par == 0). The slab distances are box_hit's own
+// values (same operations); L = max(tmin, entries) is box_hit's final tL
+// whenever box_hit runs to the end; box_hit's final tR is
+// g(min(g(min(g(min(tmax, fx)), fy)), fz)) with g(m) = RN(m + eps),
+// monotone with g(m) >= m, which is at most g(g(g(min(tmax, fx, fy, fz))))
+// = R here. So box_hit's tL < tR implies L < R.
+RMN_D bool box_any(const TRay& r, float3 lo, float3 hi, float tmin, float tmax, float& tL) {
+  const float x0 = (lo.x - r.o.x) * r.inv.x, x1 = (hi.x - r.o.x) * r.inv.x;
+  const float y0 = (lo.y - r.o.y) * r.inv.y, y1 = (hi.y - r.o.y) * r.inv.y;
+  const float z0 = (lo.z - r.o.z) * r.inv.z, z1 = (hi.z - r.o.z) * r.inv.z;
+  const float L = fmaxf(fmaxf(tmin, fminf(x0, x1)), fmaxf(fminf(y0, y1), fminf(z0, z1)));
+  float R = fminf(fminf(tmax, fmaxf(x0, x1)), fminf(fmaxf(y0, y1), fmaxf(z0, z1)));
+  R += RMN_EPS;
+  R += RMN_EPS;
+  R += RMN_EPS;
+  tL = L;
+  return L < R;
+}
+
 // RayTriangleIntersection (Moller-Trumbore), src/geometry.cpp:63-87, with
 // a division-free pre-test: u = RN(RN(1/a) * x), x = dot(s, h). Where x / a
 // lies below -1e-5 or above 1 + 1e-5 (compared as x * sign(a) against the
@@ -157,8 +179,9 @@ RMN_D void trav_begin(const DevScene& s, TravT<Stack>& t, float tmax) {
 // the other is deferred with its entry distance when both are hit, or taken
 // directly when only it is hit and it starts before tmax. Returns 0 with
 // `cur` the next node (inner or leaf), 1 when neither child is entered (the
-// caller pops), -2 when the stack would overflow.
-template <bool COUNT, class Stack>
+// caller pops), -2 when the stack would overflow. WIDE (occlusion): rays
+// without an axis under the origin-inside rule take box_any.
+template <bool COUNT, bool WIDE = false, class Stack>
 RMN_D int inner_step(const DevNode* __restrict__ nodes, const TRay& r, float tmin, float tmax, int& cur, int& sp,
                      Stack& stack, TraceCounters* cnt) {
   const DevNode* n = nodes + cur;
@@ -166,8 +189,14 @@ RMN_D int inner_step(const DevNode* __restrict__ nodes, const TRay& r, float tmi
   int4 D = __ldg(&n->d);
   if (COUNT) cnt->inner++;
   float tl0, tl1;
-  bool h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, tmax, tl0);
-  bool h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, tmax, tl1);
+  bool h0, h1;
+  if (WIDE && r.par == 0) {
+    h0 = box_any(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, tmax, tl0);
+    h1 = box_any(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, tmax, tl1);
+  } else {
+    h0 = box_hit(r, f3(A.x, A.y, A.z), f3(A.w, B.x, B.y), tmin, tmax, tl0);
+    h1 = box_hit(r, f3(B.z, B.w, C.x), f3(C.y, C.z, C.w), tmin, tmax, tl1);
+  }
   int nref, fref;
   bool hn, hf;
   float tlf;
@@ -475,7 +504,7 @@ RMN_D int occ_nodes(const DevNode* __restrict__ nodes, const TRay& r, float tmin
       if (res) continue;
     }
     if (t.cur >= 0) {
-      const int k = inner_step<COUNT>(nodes, r, tmin, tmax, t.cur, t.sp, t.stack, cnt);
+      const int k = inner_step<COUNT, true>(nodes, r, tmin, tmax, t.cur, t.sp, t.stack, cnt);
       if (k == -2) {
         res = -2;
         continue;
