@@ -57,9 +57,9 @@ FALLBACK_HBM_GBS = 6800.0
 # the timed configuration, and says so, or else the first and says that.
 BATCH64_TRAVERSAL_BYTES = [
     {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 3, "stack_entries": 23, "ray_order": 0},
-     "dram": 161.9e9, "l2": 2245.0e9},
+     "dram": 161.6e9, "l2": 2256.7e9},
     {"config": {"slots_per_unit": 2, "pool_workers": 1 << 23, "lanes": 4, "stack_entries": 23, "ray_order": 0},
-     "dram": 147.1e9, "l2": 2230.2e9},
+     "dram": 147.6e9, "l2": 2235.1e9},
 ]
 
 
@@ -747,9 +747,9 @@ def run_gpu(args, rank, world, dist):
               "source": "ncu lts__t_bytes.sum over the same launches; copy_rate: a device copy between two "
                         "L2-resident 24 MiB buffers, measured here"}
     limiter = ("instruction issue and dependent-load latency: in steady state (ncu) the closest-hit traversal "
-               "uses 68 % of its issue slots with 17.5 of 32 lanes active per instruction (warp-cooperative "
-               "leaves), the occlusion traversal 75 % with 18.6 lanes (pending leaves), both stalled mostly on "
-               "L1/L2 loads (long scoreboard 2.5-3.1 per issue) and fixed-latency dependencies (2.8-2.9); their "
+               "uses 67 % of its issue slots with 17.5 of 32 lanes active per instruction (warp-cooperative "
+               "leaves), the occlusion traversal 69 % with 18.5 lanes (pending leaves), both stalled mostly on "
+               "L1/L2 loads (long scoreboard 3.1-3.9 per issue) and fixed-latency dependencies (2.3-2.9); their "
                "measured DRAM traffic is a small share of the algorithmic bytes (L1/L2 hits) and neither DRAM "
                "nor L2 runs near its rate")
     base, _ = cpu_baseline(insts) if args.cpu_baseline else (None, None)
