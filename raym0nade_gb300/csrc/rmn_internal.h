@@ -73,7 +73,7 @@ RMN_HD float3 mix3(float3 x, float3 y, float a) { return x * (1.0f - a) + y * a;
 // node steps per round, and blocks per SM for a shared stack of S entries
 // (S * 1 KiB of stack plus 1 KiB of leaf keys per 128-thread block).
 constexpr int kCoopSteps = 4;
-constexpr int kOccSteps = 6;  // occlusion queries with pending leaves (trace.cuh, occ_nodes)
+constexpr int kOccSteps = 10;  // occlusion queries with pending leaves (trace.cuh, occ_nodes)
 // Occlusion kernels: a stack of node references (S * 512 B) and the leaf
 // exchange (about 11 KB) per 128-thread block leave room for 8 blocks per SM.
 #define RMN_OCC_BLOCKS 8
