@@ -23,6 +23,7 @@
 // corners without texture coordinates (0, 0) (the reference dereferences
 // assimp's missing arrays). RGB images become RGBA with opaque alpha (the
 // reference leaves ImageData::channels unset for PNG files).
+#include <algorithm>
 #include <array>
 #include <atomic>
 #include <cerrno>
@@ -55,6 +56,33 @@ namespace {
 using rmn::fail;
 
 const char* const kDefaultMaterial = "DefaultMaterial";
+
+// fn(0) .. fn(n - 1), each on its own thread (fn(0) on the caller's). Every
+// thread started is joined, also when starting another fails; the first
+// exception of any of them is rethrown here.
+template <class F>
+void run_threads(size_t n, F fn) {
+  std::vector<std::exception_ptr> err(n);
+  auto guarded = [&](size_t k) {
+    try {
+      fn(k);
+    } catch (...) {
+      err[k] = std::current_exception();
+    }
+  };
+  std::vector<std::thread> pool;
+  std::exception_ptr start_err;
+  try {
+    for (size_t k = 1; k < n; ++k) pool.emplace_back(guarded, k);
+  } catch (...) {
+    start_err = std::current_exception();
+  }
+  if (!start_err) guarded(0);
+  for (std::thread& th : pool) th.join();
+  if (start_err) std::rethrow_exception(start_err);
+  for (const std::exception_ptr& e : err)
+    if (e) std::rethrow_exception(e);
+}
 
 bool read_text(const std::string& path, std::string& out) {
   FILE* fp = std::fopen(path.c_str(), "rb");
@@ -283,6 +311,116 @@ sv next_token(sv& s) {
 }
 
 
+// One piece of the OBJ text, parsed on its own: the v / vt / vn values, the
+// face corners and, in order, the statements that shape the meshes. A
+// negative or zero index counts back from the vertices read so far, which
+// include the pieces before this one, so it is kept relative (its bit in
+// `rel`) and completed when the pieces are joined.
+struct ObjOp {
+  enum Kind : uint8_t { kFace, kUseMtl, kClose, kMtlLib } kind;
+  uint32_t a, b;  // kFace: corners [a, a + b); kUseMtl: names[a]; kMtlLib: names [a, a + b)
+};
+struct ObjPiece {
+  std::vector<float> P, T, N;
+  std::vector<Corner> corners;
+  std::vector<uint8_t> rel;  // bit 0 / 1 / 2: v / t / n relative to the counts before the piece
+  std::vector<ObjOp> ops;
+  std::vector<std::string> names;
+  size_t lines = 0;
+  size_t bad_line = 0;  // line of the first statement that cannot be read (within the piece), 0: none
+  std::string bad_text;
+};
+
+// The lines of text[begin, end), which starts a line and ends after a line
+// end (or at the end of the text), in order.
+void parse_obj_piece(sv text, ObjPiece& out) {
+  std::vector<Corner> cs;
+  std::vector<uint8_t> rs;
+  size_t ln = 0, start = 0;
+  for (size_t i = 0; i <= text.size(); ++i) {
+    const char ch = i < text.size() ? text[i] : '\n';
+    if (!(ch == '\n' || ch == '\v' || ch == '\f' || ch == '\x1c' || ch == '\x1d' || ch == '\x1e')) continue;
+    if (i == text.size() && start >= text.size()) break;
+    ++ln;
+    const sv line = sv_strip(text.substr(start, i - start));
+    start = i + 1;
+    if (line.empty() || line[0] == '#') continue;
+    auto bad = [&]() {
+      out.bad_line = ln;
+      out.bad_text = std::string(line.substr(0, 60));
+    };
+    sv rest = line;
+    const sv key = next_token(rest);
+    rest = sv_strip(rest);
+    if (key == "v" || key == "vn") {
+      std::vector<float>& dst = key == "v" ? out.P : out.N;
+      bool ok = true;
+      for (int k = 0; k < 3 && ok; ++k) {
+        double d;
+        ok = sv_double(next_token(rest), &d);
+        if (ok) dst.push_back((float)d);
+      }
+      if (!ok) return bad();
+    } else if (key == "vt") {
+      double u, v = 0.0;
+      if (!sv_double(next_token(rest), &u)) return bad();
+      const sv second = next_token(rest);
+      if (!second.empty() && !sv_double(second, &v)) return bad();
+      out.T.push_back((float)u);
+      out.T.push_back((float)v);
+    } else if (key == "f") {
+      cs.clear();
+      rs.clear();
+      for (sv tok = next_token(rest); !tok.empty(); tok = next_token(rest)) {
+        sv parts[3];
+        int np = 0;
+        size_t a = 0;
+        for (size_t b = 0; b <= tok.size(); ++b)
+          if (b == tok.size() || tok[b] == '/') {
+            if (np < 3) parts[np] = tok.substr(a, b - a);
+            ++np;
+            a = b + 1;
+          }
+        uint8_t r = 0;
+        auto index = [&r](sv s, size_t n, int bit, long long* idx) {
+          long long i;
+          if (!sv_long(s, &i)) return false;
+          if (i > 0) {
+            *idx = i - 1;
+          } else {
+            *idx = (long long)n + i;
+            r |= (uint8_t)bit;
+          }
+          return true;
+        };
+        Corner c{0, -1, -1};
+        if (!index(parts[0], out.P.size() / 3, 1, &c.v)) return bad();
+        if (np > 1 && !parts[1].empty() && !index(parts[1], out.T.size() / 2, 2, &c.t)) return bad();
+        if (np > 2 && !parts[2].empty() && !index(parts[2], out.N.size() / 3, 4, &c.n)) return bad();
+        cs.push_back(c);
+        rs.push_back(r);
+      }
+      if (cs.size() < 3) continue;
+      out.ops.push_back({ObjOp::kFace, (uint32_t)out.corners.size(), (uint32_t)cs.size()});
+      out.corners.insert(out.corners.end(), cs.begin(), cs.end());
+      out.rel.insert(out.rel.end(), rs.begin(), rs.end());
+    } else if (key == "usemtl") {
+      out.ops.push_back({ObjOp::kUseMtl, (uint32_t)out.names.size(), 1});
+      out.names.emplace_back(rest);
+    } else if (key == "o" || key == "g") {
+      out.ops.push_back({ObjOp::kClose, 0, 0});
+    } else if (key == "mtllib") {
+      const uint32_t first = (uint32_t)out.names.size();
+      for (sv m = next_token(rest); !m.empty(); m = next_token(rest)) out.names.emplace_back(m);
+      out.ops.push_back({ObjOp::kMtlLib, first, (uint32_t)out.names.size() - first});
+    }
+  }
+  out.lines = ln;
+}
+
+// Pieces of at least this many bytes, at most one per hardware thread (16 at most).
+constexpr size_t kObjPieceBytes = 64 << 10;
+
 rmn_status parse_obj(const std::string& path, std::vector<float>& P, std::vector<float>& T, std::vector<float>& N,
                      std::vector<MeshRun>& meshes, std::vector<std::string>& mtllibs) {
   std::string raw;
@@ -307,6 +445,24 @@ rmn_status parse_obj(const std::string& path, std::vector<float>& P, std::vector
     }
     std::string().swap(raw);
   }
+  // pieces that start at line starts, parsed on separate threads
+  const size_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t want = std::max<size_t>(1, std::min(hw, t.size() / kObjPieceBytes));
+  std::vector<size_t> cut{0};
+  for (size_t k = 1; k < want; ++k) {
+    size_t j = std::max(cut.back(), t.size() * k / want);
+    while (j < t.size() && !(t[j] == '\n' || t[j] == '\v' || t[j] == '\f' || t[j] == '\x1c' || t[j] == '\x1d' ||
+                             t[j] == '\x1e'))
+      ++j;
+    if (j >= t.size()) break;
+    if (j + 1 > cut.back()) cut.push_back(j + 1);
+  }
+  cut.push_back(t.size());
+  const size_t np = cut.size() - 1;
+  std::vector<ObjPiece> pieces(np);
+  const sv text(t);
+  run_threads(np, [&](size_t k) { parse_obj_piece(text.substr(cut[k], cut[k + 1] - cut[k]), pieces[k]); });
+  // joined in order: the statements replayed as one reader would meet them
   MeshRun cur{kDefaultMaterial, {}, {}};
   auto close = [&]() {
     if (!cur.tris.empty()) {
@@ -317,77 +473,41 @@ rmn_status parse_obj(const std::string& path, std::vector<float>& P, std::vector
     cur.corners.clear();
     cur.tris.clear();
   };
-  std::vector<Corner> cs;
-  size_t ln = 0, start = 0;
-  for (size_t i = 0; i <= t.size(); ++i) {
-    const char ch = i < t.size() ? t[i] : '\n';
-    if (!(ch == '\n' || ch == '\v' || ch == '\f' || ch == '\x1c' || ch == '\x1d' || ch == '\x1e')) continue;
-    if (i == t.size() && start >= t.size()) break;
-    ++ln;
-    const sv line = sv_strip(sv(t).substr(start, i - start));
-    start = i + 1;
-    if (line.empty() || line[0] == '#') continue;
-    auto bad = [&]() {
-      const std::string l(line.substr(0, 60));
-      return fail(RMN_ERR_INVALID_ARGUMENT, "%s:%zu: cannot read '%s'", path.c_str(), ln, l.c_str());
-    };
-    sv rest = line;
-    const sv key = next_token(rest);
-    rest = sv_strip(rest);
-    if (key == "v" || key == "vn") {
-      std::vector<float>& dst = key == "v" ? P : N;
-      for (int k = 0; k < 3; ++k) {
-        double d;
-        if (!sv_double(next_token(rest), &d)) return bad();
-        dst.push_back((float)d);
+  size_t lines_before = 0;
+  for (const ObjPiece& pc : pieces) {
+    if (pc.bad_line)
+      return fail(RMN_ERR_INVALID_ARGUMENT, "%s:%zu: cannot read '%s'", path.c_str(), lines_before + pc.bad_line,
+                  pc.bad_text.c_str());
+    const long long bv = (long long)(P.size() / 3), bt = (long long)(T.size() / 2), bn = (long long)(N.size() / 3);
+    P.insert(P.end(), pc.P.begin(), pc.P.end());
+    T.insert(T.end(), pc.T.begin(), pc.T.end());
+    N.insert(N.end(), pc.N.begin(), pc.N.end());
+    for (const ObjOp& op : pc.ops) {
+      if (op.kind == ObjOp::kFace) {
+        const int32_t base = (int32_t)cur.corners.size();
+        for (uint32_t k = 0; k < op.b; ++k) {
+          Corner c = pc.corners[op.a + k];
+          const uint8_t r = pc.rel[op.a + k];
+          if (r & 1) c.v += bv;
+          if (r & 2) c.t += bt;
+          if (r & 4) c.n += bn;
+          cur.corners.push_back(c);
+        }
+        for (int32_t k = 1; k + 1 < (int32_t)op.b; ++k) {
+          cur.tris.push_back(base);
+          cur.tris.push_back(base + k);
+          cur.tris.push_back(base + k + 1);
+        }
+      } else if (op.kind == ObjOp::kUseMtl) {
+        if (pc.names[op.a] != cur.mat) close();
+        cur.mat = pc.names[op.a];
+      } else if (op.kind == ObjOp::kClose) {
+        close();
+      } else {
+        for (uint32_t k = 0; k < op.b; ++k) mtllibs.push_back(pc.names[op.a + k]);
       }
-    } else if (key == "vt") {
-      double u, v = 0.0;
-      if (!sv_double(next_token(rest), &u)) return bad();
-      const sv second = next_token(rest);
-      if (!second.empty() && !sv_double(second, &v)) return bad();
-      T.push_back((float)u);
-      T.push_back((float)v);
-    } else if (key == "f") {
-      cs.clear();
-      for (sv tok = next_token(rest); !tok.empty(); tok = next_token(rest)) {
-        sv parts[3];
-        int np = 0;
-        size_t a = 0;
-        for (size_t b = 0; b <= tok.size(); ++b)
-          if (b == tok.size() || tok[b] == '/') {
-            if (np < 3) parts[np] = tok.substr(a, b - a);
-            ++np;
-            a = b + 1;
-          }
-        auto index = [](sv s, size_t n, long long* out) {
-          long long i;
-          if (!sv_long(s, &i)) return false;
-          *out = i > 0 ? i - 1 : (long long)n + i;
-          return true;
-        };
-        Corner c{0, -1, -1};
-        if (!index(parts[0], P.size() / 3, &c.v)) return bad();
-        if (np > 1 && !parts[1].empty() && !index(parts[1], T.size() / 2, &c.t)) return bad();
-        if (np > 2 && !parts[2].empty() && !index(parts[2], N.size() / 3, &c.n)) return bad();
-        cs.push_back(c);
-      }
-      if (cs.size() < 3) continue;
-      const int32_t base = (int32_t)cur.corners.size();
-      cur.corners.insert(cur.corners.end(), cs.begin(), cs.end());
-      for (int32_t k = 1; k + 1 < (int32_t)cs.size(); ++k) {
-        cur.tris.push_back(base);
-        cur.tris.push_back(base + k);
-        cur.tris.push_back(base + k + 1);
-      }
-    } else if (key == "usemtl") {
-      if (rest != sv(cur.mat)) close();
-      cur.mat = std::string(rest);
-    } else if (key == "o" || key == "g") {
-      close();
-    } else if (key == "mtllib") {
-      for (sv m = next_token(rest); !m.empty(); m = next_token(rest)) mtllibs.emplace_back(m);
     }
+    lines_before += pc.lines;
   }
   close();
   return RMN_OK;
@@ -509,10 +629,7 @@ rmn_status finish_model(const std::string& folder, const std::string& name, cons
       }
     };
     const size_t nthreads = std::min<size_t>(jobs.size(), std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
-    std::vector<std::thread> pool;
-    for (size_t k = 1; k < nthreads; ++k) pool.emplace_back(work);
-    work();
-    for (std::thread& t : pool) t.join();
+    run_threads(nthreads, [&](size_t) { work(); });
   }
   std::vector<int> tex_of(jobs.size(), -1);
   for (size_t j = 0; j < jobs.size(); ++j) {

@@ -420,7 +420,7 @@ def test_native_importer_matches_oracle(tmp_path, capfd):
         same_scene(assets.load_model(folder, "room.obj", sky), obj_import.load_model(folder, "room.obj", sky))
 
 
-def _random_obj(rng, path):
+def _random_obj(rng, path, parts=(3, 8)):
     """Random OBJ text: objects, groups, material switches, polygons of 3-6
     corners with every corner form and negative indices, degenerate faces,
     normals pointing anywhere (the infacing test), comments, tabs, CRLF line
@@ -428,7 +428,7 @@ def _random_obj(rng, path):
     out = ["mtllib lib.mtl", "# random model"]
     nv = nt = nn = 0
     mats = ["A", "B", "Glass", "Water", "Nope"]
-    for k in range(int(rng.integers(3, 8))):
+    for k in range(int(rng.integers(*parts))):
         out.append(("o" if rng.random() < 0.5 else "g") + f" part{k}")
         for _ in range(int(rng.integers(4, 12))):
             out.append("v %.7g %.7g %.7g" % tuple(rng.normal(0, 2, 3) * 10.0 ** int(rng.integers(-2, 3))))
@@ -471,6 +471,32 @@ def test_native_importer_matches_oracle_random_models(tmp_path):
     for k in range(40):
         _random_obj(rng, folder + f"m{k}.obj")
         same_scene(assets.load_model(folder, f"m{k}.obj"), obj_import.load_model(folder, f"m{k}.obj"))
+
+
+def test_native_importer_large_random_models(tmp_path):
+    """Files of several hundred KB, which the library parses in pieces on
+    separate threads: negative indices, material switches, objects and
+    continued lines across the pieces' seams give the oracle's arrays; a bad
+    statement in a late piece is reported with its line in the whole file."""
+    rng = np.random.default_rng(78)
+    folder = str(tmp_path) + "/"
+    with open(folder + "lib.mtl", "w") as f:
+        f.write("newmtl A\nd 1\nnewmtl B\nTr 0.5\nnewmtl Glass\n  d\t0.2\nnewmtl Water\nd 0.995\n")
+    for k in range(3):
+        _random_obj(rng, folder + f"big{k}.obj", parts=(900, 1000))
+        assert os.path.getsize(folder + f"big{k}.obj") > 8 * 64 * 1024
+        same_scene(assets.load_model(folder, f"big{k}.obj"), obj_import.load_model(folder, f"big{k}.obj"))
+    lines = open(folder + "big0.obj", newline="").read().splitlines()
+    at = len(lines) - 5
+    while not lines[at].startswith("v "):
+        at -= 1
+    lines[at] = "v 1.0 oops 2.0"
+    with open(folder + "bad.obj", "w", newline="") as f:
+        f.write("\n".join(lines) + "\n")
+    # lines as a reader counts them: a backslash at the end of a line joins the next
+    line_no = ("\n".join(lines[:at]) + "\n").replace("\\\n", " ").count("\n") + 1
+    with pytest.raises(ValueError, match=f"bad.obj:{line_no}: cannot read 'v 1.0 oops 2.0'"):
+        assets.load_model(folder, "bad.obj")
 
 
 @pytest.mark.parametrize("kind", ["smooth", "noise", "tiles", "tiny", "flat"])
