@@ -17,7 +17,9 @@
 #include <cmath>
 #include <cstring>
 #include <future>
+#include <vector>
 #include <memory>
+#include <utility>
 #include <mutex>
 #include <thread>
 
@@ -26,6 +28,52 @@
 
 namespace rmn {
 namespace {
+
+// fn(lo, hi) over [0, n) in contiguous ranges, one per hardware thread (16
+// at most) once n is large; each index belongs to one range, so loops whose
+// iterations write only their own slots give the same arrays on any number
+// of threads. A worker's exception is rethrown here, after every worker has
+// finished.
+template <class F>
+void parallel_ranges(size_t n, F fn) {
+  const size_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t parts = std::min(hw, std::max<size_t>(1, n / 16384));
+  if (parts <= 1) {
+    fn((size_t)0, n);
+    return;
+  }
+  std::vector<std::future<void>> workers;
+  for (size_t k = 1; k < parts; ++k)
+    workers.push_back(std::async(std::launch::async, fn, n * k / parts, n * (k + 1) / parts));
+  fn((size_t)0, n / parts);
+  for (std::future<void>& w : workers) w.get();
+}
+
+// An allocator whose default-inserted elements are left uninitialised
+// (default- instead of value-initialised), for the large per-vertex and
+// per-triangle arrays that a parallel loop then fills slot by slot: their
+// pages are first touched by the threads that write them, not zeroed by one
+// thread beforehand.
+template <class T>
+struct NoInit : std::allocator<T> {
+  template <class U>
+  struct rebind {
+    using other = NoInit<U>;
+  };
+  NoInit() = default;
+  template <class U>
+  NoInit(const NoInit<U>&) noexcept {}
+  template <class U>
+  void construct(U* p) noexcept {
+    ::new ((void*)p) U;
+  }
+  template <class U, class... A>
+  void construct(U* p, A&&... a) {
+    ::new ((void*)p) U(std::forward<A>(a)...);
+  }
+};
+template <class T>
+using FillVec = std::vector<T, NoInit<T>>;
 
 struct Item {
   float c[3];
@@ -40,7 +88,7 @@ struct HeapNode {
 struct Builder {
   const float3* pos;
   const int32_t* idx;
-  std::vector<Item> items;
+  FillVec<Item> items;
   std::vector<HeapNode> heap;
 
   float3 vtx(int tri, int k) const { return pos[idx[3 * tri + k]]; }
@@ -145,8 +193,8 @@ bool tangent_frame_finite(float3 e1, float3 e2, const float* uv0, const float* u
   return all_finite3(t) && all_finite3(b);
 }
 
-template <class T>
-rmn_status upload(rmn_scene* s, const std::vector<T>& v, const T** out) {
+template <class T, class A>
+rmn_status upload(rmn_scene* s, const std::vector<T, A>& v, const T** out) {
   *out = nullptr;
   if (v.empty()) return RMN_OK;
   void* p = nullptr;
@@ -339,20 +387,26 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   auto mat_tex = [&](int m, int slot) { return d->material_textures ? d->material_textures[4 * m + slot] : -1; };
 
   const int nt = d->num_triangles;
-  std::vector<float3> pos(d->num_vertices);
-  for (int i = 0; i < d->num_vertices; ++i) pos[i] = f3(d->positions[3 * i], d->positions[3 * i + 1], d->positions[3 * i + 2]);
+  FillVec<float3> pos(d->num_vertices);
+  parallel_ranges(d->num_vertices, [&](size_t lo, size_t hi) {
+    for (size_t i = lo; i < hi; ++i) pos[i] = f3(d->positions[3 * i], d->positions[3 * i + 1], d->positions[3 * i + 2]);
+  });
 
   // ---- BVH (BVH::build, src/bvh.cpp:48-54) ----
   Builder b;
   b.pos = pos.data();
   b.idx = d->indices;
   b.items.resize(nt);
-  for (int t = 0; t < nt; ++t) {
-    float3 c = (b.vtx(t, 0) + b.vtx(t, 1) + b.vtx(t, 2)) / 3.0f;  // Face::center, src/component.cpp:37-39
-    b.items[t] = {{c.x, c.y, c.z}, t};
-  }
+  parallel_ranges(nt, [&](size_t lo, size_t hi) {
+    for (int t = (int)lo; t < (int)hi; ++t) {
+      float3 c = (b.vtx(t, 0) + b.vtx(t, 1) + b.vtx(t, 2)) / 3.0f;  // Face::center, src/component.cpp:37-39
+      b.items[t] = {{c.x, c.y, c.z}, t};
+    }
+  });
   b.heap.assign(heap_slots(1, nt) + 1, HeapNode());
-  int par = std::thread::hardware_concurrency() >= 8 ? 3 : 1;
+  // subtrees on separate threads down to this depth: 2^par of them
+  const unsigned hw = std::thread::hardware_concurrency();
+  const int par = hw >= 16 ? 4 : hw >= 8 ? 3 : 1;
   b.build(1, 0, nt, par);
   Flattener fl{b.heap, {}, 0};
   int root = fl.ref_of(1, 0);
@@ -364,27 +418,29 @@ rmn_status build_scene(const rmn_scene_desc* d, rmn_scene* s) {
   for (int m = 0; m < d->num_meshes; ++m)
     for (int t = d->mesh_first[m]; t < d->mesh_first[m + 1]; ++t) tri_mesh_mat[t] = d->mesh_material[m];
   static const float zero2[2] = {0.0f, 0.0f};
-  std::vector<float4> tri(3 * (size_t)nt), shade(3 * (size_t)nt);
-  for (int i = 0; i < nt; ++i) {
-    int t = b.items[i].id;
-    int i0 = d->indices[3 * t], i1 = d->indices[3 * t + 1], i2 = d->indices[3 * t + 2];
-    float3 v0 = pos[i0], e1 = pos[i1] - v0, e2 = pos[i2] - v0;
-    int flags = 0;
-    float area = len3(cross3(e1, e2)) / 2.0f;
-    if (!(area > 1e-2f)) flags |= RMN_TRI_SMOOTH;
-    const float* u0 = d->uvs ? d->uvs + 2 * i0 : zero2;
-    const float* u1 = d->uvs ? d->uvs + 2 * i1 : zero2;
-    const float* u2 = d->uvs ? d->uvs + 2 * i2 : zero2;
-    if (tangent_frame_finite(e1, e2, u0, u1, u2)) flags |= RMN_TRI_RENORM;
-    tri[3 * i + 0] = make_float4(v0.x, v0.y, v0.z, bits_float(t));
-    tri[3 * i + 1] = make_float4(e1.x, e1.y, e1.z, len3(e1));
-    tri[3 * i + 2] = make_float4(e2.x, e2.y, e2.z, bits_float(flags));
-    for (int k = 0; k < 3; ++k) {
-      int v = d->indices[3 * t + k];
-      float3 n = d->normals ? f3(d->normals[3 * v], d->normals[3 * v + 1], d->normals[3 * v + 2]) : f3(0.0f);
-      shade[3 * i + k] = make_float4(n.x, n.y, n.z, k == 0 ? bits_float(tri_mesh_mat[t]) : 0.0f);
+  FillVec<float4> tri(3 * (size_t)nt), shade(3 * (size_t)nt);
+  parallel_ranges(nt, [&](size_t lo, size_t hi) {
+    for (int i = (int)lo; i < (int)hi; ++i) {
+      int t = b.items[i].id;
+      int i0 = d->indices[3 * t], i1 = d->indices[3 * t + 1], i2 = d->indices[3 * t + 2];
+      float3 v0 = pos[i0], e1 = pos[i1] - v0, e2 = pos[i2] - v0;
+      int flags = 0;
+      float area = len3(cross3(e1, e2)) / 2.0f;
+      if (!(area > 1e-2f)) flags |= RMN_TRI_SMOOTH;
+      const float* u0 = d->uvs ? d->uvs + 2 * i0 : zero2;
+      const float* u1 = d->uvs ? d->uvs + 2 * i1 : zero2;
+      const float* u2 = d->uvs ? d->uvs + 2 * i2 : zero2;
+      if (tangent_frame_finite(e1, e2, u0, u1, u2)) flags |= RMN_TRI_RENORM;
+      tri[3 * i + 0] = make_float4(v0.x, v0.y, v0.z, bits_float(t));
+      tri[3 * i + 1] = make_float4(e1.x, e1.y, e1.z, len3(e1));
+      tri[3 * i + 2] = make_float4(e2.x, e2.y, e2.z, bits_float(flags));
+      for (int k = 0; k < 3; ++k) {
+        int v = d->indices[3 * t + k];
+        float3 n = d->normals ? f3(d->normals[3 * v], d->normals[3 * v + 1], d->normals[3 * v + 2]) : f3(0.0f);
+        shade[3 * i + k] = make_float4(n.x, n.y, n.z, k == 0 ? bits_float(tri_mesh_mat[t]) : 0.0f);
+      }
     }
-  }
+  });
 
   // ---- textures: mip chains, packed level after level ----
   std::vector<DevTex> dtex(textured ? d->num_textures : 0);
