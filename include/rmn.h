@@ -204,7 +204,9 @@ const char* rmn_version(void);
 /* Scene construction: replaces Model::Model's geometry/BVH/light/sky steps
  * (src/model.cpp:172-215) and Material's texture loading and mip chains
  * (src/material.cpp:107-129, 291-302). The arrays of rmn_scene_desc are read
- * on the host (host memory). */
+ * on the host (host memory). The host part runs on up to 16 threads of the
+ * calling process (disjoint BVH subtrees, per-triangle arrays); the result
+ * does not depend on their number. */
 rmn_status rmn_scene_create(const rmn_scene_desc* desc, rmn_scene** out);
 rmn_status rmn_scene_destroy(rmn_scene* scene);
 rmn_status rmn_scene_info_get(const rmn_scene* scene, rmn_scene_info* info);
@@ -471,7 +473,10 @@ rmn_status rmn_scene_texture_get(const rmn_scene* scene, int32_t texture, int32_
  * the model until rmn_model_free. A file that cannot be read or parsed gives
  * RMN_ERR_INVALID_ARGUMENT (the message names file and line); a texture of
  * another type, a DDS that does not decode or a sky map that does not decode
- * is left out with a message on stderr, as the reference goes on without it. */
+ * is left out with a message on stderr, as the reference goes on without it.
+ * The OBJ text (in pieces of at least 64 KB) and the texture files are
+ * parsed on up to 16 threads of the calling process; the model does not
+ * depend on their number. */
 typedef struct rmn_model rmn_model;
 rmn_status rmn_model_read(const char* model_folder, const char* model_name, const char* skyMap_name,
                           rmn_model** out);
