@@ -37,9 +37,12 @@
 #include <array>
 #include <cmath>
 #include <cstdio>
+#include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <map>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "rmn_host.h"
@@ -67,11 +70,44 @@ struct Node {
     return nullptr;
   }
 };
+// Records are moved, never copied, when their parent's array grows, so a
+// property keeps its address from the parse on (the deferred arrays below).
+static_assert(std::is_nothrow_move_constructible<Node>::value, "records must move without copying");
 
 class Reader {
  public:
   Reader(const std::vector<uint8_t>& b, uint32_t version) : b_(b), wide_(version >= 7500) {}
   const char* err = nullptr;
+
+  // The arrays met by records(), inflated (zlib) and converted after the
+  // parse, on several threads. A stream that does not inflate is
+  // reported as the reader would have met it in file order: before any
+  // later defect (every array here lies before the point where records()
+  // stopped), and the first such stream if there are several. After a
+  // parse that failed (`parsed` false) the records that held some of these
+  // arrays are gone: the streams are only inflated to find such an earlier
+  // defect, and nothing is written.
+  bool finish_arrays(bool parsed) {
+    std::atomic<size_t> next{0};
+    rmn::run_threads(std::min(rmn::host_threads(), deferred_.size()), [&](size_t) {
+      std::vector<uint8_t> tmp;
+      for (size_t j; (j = next.fetch_add(1)) < deferred_.size();) {
+        Deferred& a = deferred_[j];
+        if (!a.zlib) {
+          if (parsed) convert(*a.p, b_.data() + a.off, a.count);
+          continue;
+        }
+        a.err = rmn::zlib_inflate(b_.data() + a.off, a.clen, tmp, a.raw);
+        if (!a.err && parsed) convert(*a.p, tmp.data(), a.count);
+      }
+    });
+    for (const Deferred& a : deferred_)  // in file order
+      if (a.err) {
+        err = a.err;
+        return false;
+      }
+    return err == nullptr;
+  }
 
   // Reads the records at `off` up to `end` (or a null record) into `out`.
   bool records(size_t& off, size_t end, std::vector<Node>& out, int depth) {
@@ -87,8 +123,45 @@ class Reader {
   }
 
  private:
+  struct Deferred {
+    Prop* p;  // in its record's property array, which no longer changes size (valid while the records are)
+    size_t off, raw;
+    uint32_t clen, count;
+    bool zlib;  // else the elements' bytes as they are
+    const char* err = nullptr;
+  };
   const std::vector<uint8_t>& b_;
   bool wide_;
+  std::vector<Deferred> deferred_;
+
+  // An array's elements (count of p.type) from their bytes.
+  static void convert(Prop& p, const uint8_t* src, uint32_t count) {
+    if (p.type == 'f' || p.type == 'd') {
+      p.da.resize(count);
+      for (uint32_t k = 0; k < count; ++k) {
+        if (p.type == 'f') {
+          float v;
+          std::memcpy(&v, src + 4 * (size_t)k, 4);
+          p.da[k] = v;
+        } else {
+          std::memcpy(&p.da[k], src + 8 * (size_t)k, 8);
+        }
+      }
+    } else {
+      p.ia.resize(count);
+      for (uint32_t k = 0; k < count; ++k) {
+        if (p.type == 'b') {
+          p.ia[k] = src[k] != 0;
+        } else if (p.type == 'i') {
+          int32_t v;
+          std::memcpy(&v, src + 4 * (size_t)k, 4);
+          p.ia[k] = v;
+        } else {
+          std::memcpy(&p.ia[k], src + 8 * (size_t)k, 8);
+        }
+      }
+    }
+  }
 
   bool bad(const char* m) {
     if (!err) err = m;
@@ -170,43 +243,15 @@ class Reader {
         const size_t esz = p.type == 'b' ? 1 : (p.type == 'f' || p.type == 'i') ? 4 : 8;
         if (count > (1u << 30) / esz) return bad("array too long");
         const size_t raw = (size_t)count * esz;
-        std::vector<uint8_t> tmp;
-        const uint8_t* src;
         if (enc == 0) {
           if (clen != raw) return bad("array length does not match its bytes");
-          src = b_.data() + off;
+          deferred_.push_back({&p, off, raw, clen, count, false});
         } else if (enc == 1) {
-          if (const char* e = rmn::zlib_inflate(b_.data() + off, clen, tmp, raw)) return bad(e);
-          src = tmp.data();
+          deferred_.push_back({&p, off, raw, clen, count, true});
         } else {
           return bad("unknown array encoding");
         }
         off += clen;
-        if (p.type == 'f' || p.type == 'd') {
-          p.da.resize(count);
-          for (uint32_t k = 0; k < count; ++k) {
-            if (p.type == 'f') {
-              float v;
-              std::memcpy(&v, src + 4 * (size_t)k, 4);
-              p.da[k] = v;
-            } else {
-              std::memcpy(&p.da[k], src + 8 * (size_t)k, 8);
-            }
-          }
-        } else {
-          p.ia.resize(count);
-          for (uint32_t k = 0; k < count; ++k) {
-            if (p.type == 'b') {
-              p.ia[k] = src[k] != 0;
-            } else if (p.type == 'i') {
-              int32_t v;
-              std::memcpy(&v, src + 4 * (size_t)k, 4);
-              p.ia[k] = v;
-            } else {
-              std::memcpy(&p.ia[k], src + 8 * (size_t)k, 8);
-            }
-          }
-        }
         return true;
       }
       default:
@@ -359,23 +404,47 @@ std::string object_name(const Node& o) {
   return k == std::string::npos ? s : s.substr(0, k);
 }
 
-// A layer element's value index for corner c of polygon `poly` at control
-// point v, or -1.
-int64_t layer_index(const Node& le, const char* index_name, int64_t c, int64_t poly, int64_t v) {
+// A layer element's mapping (MappingInformationType, default
+// ByPolygonVertex) and reference (ReferenceInformationType, default Direct),
+// read once per geometry.
+struct LayerMap {
+  enum Mode { kByCorner, kByVertex, kByPolygon, kAllSame, kOther } mode = kOther;
+  bool indexed = false;                         // IndexToDirect / Index
+  const std::vector<int64_t>* index = nullptr;  // the index array when indexed (none: every lookup fails)
+};
+
+LayerMap layer_map(const Node& le, const char* index_name) {
   const Node* mt = le.child("MappingInformationType");
   const Node* rt = le.child("ReferenceInformationType");
   const std::string map = mt && !mt->props.empty() ? mt->props[0].s : "ByPolygonVertex";
   const std::string ref = rt && !rt->props.empty() ? rt->props[0].s : "Direct";
-  int64_t k;
-  if (map == "ByPolygonVertex") k = c;
-  else if (map == "ByVertice" || map == "ByVertex") k = v;
-  else if (map == "ByPolygon") k = poly;
-  else if (map == "AllSame") k = 0;
-  else return -1;
-  if (ref == "IndexToDirect" || ref == "Index") {
+  LayerMap m;
+  if (map == "ByPolygonVertex") m.mode = LayerMap::kByCorner;
+  else if (map == "ByVertice" || map == "ByVertex") m.mode = LayerMap::kByVertex;
+  else if (map == "ByPolygon") m.mode = LayerMap::kByPolygon;
+  else if (map == "AllSame") m.mode = LayerMap::kAllSame;
+  m.indexed = ref == "IndexToDirect" || ref == "Index";
+  if (m.indexed) {
     const Node* ix = le.child(index_name);
-    if (!ix || ix->props.empty() || k < 0 || k >= (int64_t)ix->props[0].ia.size()) return -1;
-    k = ix->props[0].ia[(size_t)k];
+    if (ix && !ix->props.empty()) m.index = &ix->props[0].ia;
+  }
+  return m;
+}
+
+// The layer element's value index for corner c of polygon `poly` at control
+// point v, or -1.
+int64_t layer_index(const LayerMap& m, int64_t c, int64_t poly, int64_t v) {
+  int64_t k;
+  switch (m.mode) {
+    case LayerMap::kByCorner: k = c; break;
+    case LayerMap::kByVertex: k = v; break;
+    case LayerMap::kByPolygon: k = poly; break;
+    case LayerMap::kAllSame: k = 0; break;
+    default: return -1;
+  }
+  if (m.indexed) {
+    if (!m.index || k < 0 || k >= (int64_t)m.index->size()) return -1;
+    k = (*m.index)[(size_t)k];
   }
   return k;
 }
@@ -385,15 +454,8 @@ int64_t layer_index(const Node& le, const char* index_name, int64_t c, int64_t p
 namespace rmn {
 
 rmn_status read_fbx(const std::string& path, std::vector<FbxMesh>& meshes, std::vector<FbxMaterial>& materials) {
-  FILE* fp = std::fopen(path.c_str(), "rb");
-  if (!fp) return fail(RMN_ERR_INVALID_ARGUMENT, "could not read %s", path.c_str());
   std::vector<uint8_t> b;
-  {
-    uint8_t buf[1 << 16];
-    size_t n;
-    while ((n = std::fread(buf, 1, sizeof buf, fp)) > 0) b.insert(b.end(), buf, buf + n);
-    std::fclose(fp);
-  }
+  if (!read_whole_file(path.c_str(), b)) return fail(RMN_ERR_INVALID_ARGUMENT, "could not read %s", path.c_str());
   static const char kMagic[] = "Kaydara FBX Binary  ";
   if (b.size() >= 5 && std::memcmp(b.data(), "; FBX", 5) == 0)
     return fail(RMN_ERR_UNSUPPORTED, "%s: ASCII FBX files are not read (binary only)", path.c_str());
@@ -403,7 +465,8 @@ rmn_status read_fbx(const std::string& path, std::vector<FbxMesh>& meshes, std::
   Reader rd(b, version);
   std::vector<Node> top;
   size_t off = 27;
-  if (!rd.records(off, b.size(), top, 0))
+  const bool parsed = rd.records(off, b.size(), top, 0);
+  if (!rd.finish_arrays(parsed) || !parsed)
     return fail(RMN_ERR_INVALID_ARGUMENT, "%s: %s", path.c_str(), rd.err ? rd.err : "malformed");
 
   const Node *objects = nullptr, *conns = nullptr;
@@ -501,6 +564,32 @@ rmn_status read_fbx(const std::string& path, std::vector<FbxMesh>& meshes, std::
     return k;
   };
 
+  // Per model, in order: its geometry's checks, polygons and material
+  // groups, and the materials in order of first use -- everything whose
+  // order matters. The corners of each (model, material) mesh are then
+  // filled on several threads; the first defect in the order above is the
+  // one reported.
+  struct GeomWork {
+    const std::vector<double>* V;
+    const std::vector<int64_t>* PVI;
+    const std::vector<double>* Nd;
+    const std::vector<double>* Ud;
+    LayerMap map_n, map_u;
+    M4 W;
+    double IT[9];
+    bool inv_ok;
+    std::vector<std::pair<int64_t, int64_t>> polys;  // [first corner, end)
+  };
+  struct MeshWork {
+    size_t geom;
+    std::vector<int64_t> polys;  // of the geometry, in order
+    FbxMesh mesh;
+    const char* err = nullptr;
+  };
+  std::vector<GeomWork> geoms;
+  std::vector<MeshWork> work;
+  std::string late_err;  // a defect found before the corners, after the work listed so far
+  geoms.reserve(models.size());
   for (const ModelInfo& mi : models) {
     int64_t gid = 0;
     for (const auto& gm : geom_model)
@@ -512,100 +601,134 @@ rmn_status read_fbx(const std::string& path, std::vector<FbxMesh>& meshes, std::
     const Node& g = *geometry[gid];
     const Node* vn = g.child("Vertices");
     const Node* pn = g.child("PolygonVertexIndex");
-    if (!vn || !pn || vn->props.empty() || pn->props.empty())
-      return fail(RMN_ERR_INVALID_ARGUMENT, "%s: geometry %lld without vertices or polygons", path.c_str(),
-                  (long long)gid);
-    const std::vector<double>& V = vn->props[0].da;
-    const std::vector<int64_t>& PVI = pn->props[0].ia;
+    if (!vn || !pn || vn->props.empty() || pn->props.empty()) {
+      char m[96];
+      std::snprintf(m, sizeof m, "geometry %lld without vertices or polygons", (long long)gid);
+      late_err = m;
+      break;
+    }
+    GeomWork gw;
+    gw.V = &vn->props[0].da;
+    gw.PVI = &pn->props[0].ia;
     const Node* le_n = g.child("LayerElementNormal");
     const Node* le_u = g.child("LayerElementUV");
     const Node* le_m = g.child("LayerElementMaterial");
-    const std::vector<double>* Nd = nullptr;
-    const std::vector<double>* Ud = nullptr;
+    gw.Nd = nullptr;
+    gw.Ud = nullptr;
     if (le_n && le_n->child("Normals") && !le_n->child("Normals")->props.empty())
-      Nd = &le_n->child("Normals")->props[0].da;
-    if (le_u && le_u->child("UV") && !le_u->child("UV")->props.empty()) Ud = &le_u->child("UV")->props[0].da;
-    const M4 W = mul(world(mi), mi.geometric);
-    double IT[9];
-    const bool inv_ok = inverse3(W, IT);
-    // polygons
-    std::vector<std::pair<int64_t, int64_t>> polys;  // [first corner, end)
+      gw.Nd = &le_n->child("Normals")->props[0].da;
+    if (le_u && le_u->child("UV") && !le_u->child("UV")->props.empty()) gw.Ud = &le_u->child("UV")->props[0].da;
+    gw.map_n = le_n ? layer_map(*le_n, "NormalsIndex") : LayerMap();
+    gw.map_u = le_u ? layer_map(*le_u, "UVIndex") : LayerMap();
+    gw.W = mul(world(mi), mi.geometric);
+    gw.inv_ok = inverse3(gw.W, gw.IT);
+    const std::vector<int64_t>& PVI = *gw.PVI;
     for (size_t c = 0, first = 0; c < PVI.size(); ++c)
       if (PVI[c] < 0) {
-        polys.push_back({(int64_t)first, (int64_t)c + 1});
+        gw.polys.push_back({(int64_t)first, (int64_t)c + 1});
         first = c + 1;
       }
     const std::vector<int64_t>& model_mat_ids = model_mats[mi.id];
+    const Node* mat_node = le_m ? le_m->child("Materials") : nullptr;
+    const std::vector<int64_t>* mat_ids = mat_node && !mat_node->props.empty() ? &mat_node->props[0].ia : nullptr;
+    const Node* mat_map = le_m ? le_m->child("MappingInformationType") : nullptr;
+    const bool mat_same = mat_map && !mat_map->props.empty() && mat_map->props[0].s == "AllSame";
     auto poly_material = [&](int64_t poly) -> int64_t {
-      if (!le_m || !le_m->child("Materials") || le_m->child("Materials")->props.empty()) return 0;
-      const std::vector<int64_t>& ms = le_m->child("Materials")->props[0].ia;
-      const Node* mt = le_m->child("MappingInformationType");
-      const bool same = mt && !mt->props.empty() && mt->props[0].s == "AllSame";
-      const int64_t k = same ? 0 : poly;
-      return k >= 0 && k < (int64_t)ms.size() ? ms[(size_t)k] : 0;
+      if (!mat_ids) return 0;
+      const int64_t k = mat_same ? 0 : poly;
+      return k >= 0 && k < (int64_t)mat_ids->size() ? (*mat_ids)[(size_t)k] : 0;
     };
     std::map<int64_t, std::vector<int64_t>> by_mat;  // material index -> polygons
-    for (int64_t p = 0; p < (int64_t)polys.size(); ++p) by_mat[poly_material(p)].push_back(p);
-    for (const auto& bm : by_mat) {
+    for (int64_t p = 0; p < (int64_t)gw.polys.size(); ++p) by_mat[poly_material(p)].push_back(p);
+    const size_t gi = geoms.size();
+    const bool has_nrm = gw.Nd != nullptr && gw.inv_ok, has_uv = gw.Ud != nullptr;
+    geoms.push_back(std::move(gw));
+    for (auto& bm : by_mat) {
       const int64_t li = bm.first;
       const int64_t fid = li >= 0 && li < (int64_t)model_mat_ids.size() ? model_mat_ids[(size_t)li] : 0;
-      FbxMesh mesh;
-      mesh.material = use_material(fid);
-      mesh.has_nrm = Nd != nullptr && inv_ok;
-      mesh.has_uv = Ud != nullptr;
-      for (int64_t p : bm.second) {
-        const int64_t c0 = polys[(size_t)p].first, c1 = polys[(size_t)p].second;
-        if (c1 - c0 < 3) continue;  // lines and points drop out
-        const int32_t base = (int32_t)(mesh.pos.size() / 3);
-        for (int64_t c = c0; c < c1; ++c) {
-          const int64_t vi = PVI[(size_t)c] < 0 ? ~PVI[(size_t)c] : PVI[(size_t)c];
-          if (vi < 0 || 3 * vi + 2 >= (int64_t)V.size())
-            return fail(RMN_ERR_INVALID_ARGUMENT, "%s: a polygon refers to a vertex that does not exist",
-                        path.c_str());
-          const double x = V[3 * vi], y = V[3 * vi + 1], z = V[3 * vi + 2];
-          for (int r = 0; r < 3; ++r) {
-            double s = W[4 * r] * x;
-            s += W[4 * r + 1] * y;
-            s += W[4 * r + 2] * z;
-            s += W[4 * r + 3];
-            mesh.pos.push_back((float)s);
-          }
-          if (mesh.has_nrm) {
-            const int64_t k = layer_index(*le_n, "NormalsIndex", c, p, vi);
-            if (k < 0 || 3 * k + 2 >= (int64_t)Nd->size())
-              return fail(RMN_ERR_INVALID_ARGUMENT, "%s: a normal index is out of range", path.c_str());
-            const double nx = (*Nd)[3 * k], ny = (*Nd)[3 * k + 1], nz = (*Nd)[3 * k + 2];
-            double t[3];
-            for (int r = 0; r < 3; ++r) {  // inverse transpose: column r of the inverse
-              double s = IT[r] * nx;
-              s += IT[3 + r] * ny;
-              s += IT[6 + r] * nz;
-              t[r] = s;
-            }
-            double len = t[0] * t[0];
-            len += t[1] * t[1];
-            len += t[2] * t[2];
-            len = std::sqrt(len);
-            for (int r = 0; r < 3; ++r) mesh.nrm.push_back(len > 0.0 ? (float)(t[r] / len) : 0.0f);
-          }
-          if (mesh.has_uv) {
-            const int64_t k = layer_index(*le_u, "UVIndex", c, p, vi);
-            if (k < 0 || 2 * k + 1 >= (int64_t)Ud->size())
-              return fail(RMN_ERR_INVALID_ARGUMENT, "%s: a uv index is out of range", path.c_str());
-            mesh.uv.push_back((float)(*Ud)[2 * k]);
-            mesh.uv.push_back((float)(*Ud)[2 * k + 1]);
-          }
-        }
-        const int32_t nc = (int32_t)(c1 - c0);
-        for (int32_t k = 1; k + 1 < nc; ++k) {  // a fan from the first corner
-          mesh.tris.push_back(base);
-          mesh.tris.push_back(base + k);
-          mesh.tris.push_back(base + k + 1);
-        }
-      }
-      if (!mesh.tris.empty()) meshes.push_back(std::move(mesh));
+      MeshWork mw;
+      mw.geom = gi;
+      mw.polys = std::move(bm.second);
+      mw.mesh.material = use_material(fid);
+      mw.mesh.has_nrm = has_nrm;
+      mw.mesh.has_uv = has_uv;
+      work.push_back(std::move(mw));
     }
   }
+  // the corners: a vertex per polygon corner in world space, its normal
+  // through the inverse transpose, its uv; polygons as fans
+  auto fill = [&](MeshWork& mw) {
+    const GeomWork& gw = geoms[mw.geom];
+    const std::vector<double>& V = *gw.V;
+    const std::vector<int64_t>& PVI = *gw.PVI;
+    const M4& W = gw.W;
+    const double* IT = gw.IT;
+    FbxMesh& mesh = mw.mesh;
+    for (int64_t p : mw.polys) {
+      const int64_t c0 = gw.polys[(size_t)p].first, c1 = gw.polys[(size_t)p].second;
+      if (c1 - c0 < 3) continue;  // lines and points drop out
+      const int32_t base = (int32_t)(mesh.pos.size() / 3);
+      for (int64_t c = c0; c < c1; ++c) {
+        const int64_t vi = PVI[(size_t)c] < 0 ? ~PVI[(size_t)c] : PVI[(size_t)c];
+        if (vi < 0 || 3 * vi + 2 >= (int64_t)V.size()) {
+          mw.err = "a polygon refers to a vertex that does not exist";
+          return;
+        }
+        const double x = V[3 * vi], y = V[3 * vi + 1], z = V[3 * vi + 2];
+        for (int r = 0; r < 3; ++r) {
+          double s = W[4 * r] * x;
+          s += W[4 * r + 1] * y;
+          s += W[4 * r + 2] * z;
+          s += W[4 * r + 3];
+          mesh.pos.push_back((float)s);
+        }
+        if (mesh.has_nrm) {
+          const int64_t k = layer_index(gw.map_n, c, p, vi);
+          if (k < 0 || 3 * k + 2 >= (int64_t)gw.Nd->size()) {
+            mw.err = "a normal index is out of range";
+            return;
+          }
+          const double nx = (*gw.Nd)[3 * k], ny = (*gw.Nd)[3 * k + 1], nz = (*gw.Nd)[3 * k + 2];
+          double t[3];
+          for (int r = 0; r < 3; ++r) {  // inverse transpose: column r of the inverse
+            double s = IT[r] * nx;
+            s += IT[3 + r] * ny;
+            s += IT[6 + r] * nz;
+            t[r] = s;
+          }
+          double len = t[0] * t[0];
+          len += t[1] * t[1];
+          len += t[2] * t[2];
+          len = std::sqrt(len);
+          for (int r = 0; r < 3; ++r) mesh.nrm.push_back(len > 0.0 ? (float)(t[r] / len) : 0.0f);
+        }
+        if (mesh.has_uv) {
+          const int64_t k = layer_index(gw.map_u, c, p, vi);
+          if (k < 0 || 2 * k + 1 >= (int64_t)gw.Ud->size()) {
+            mw.err = "a uv index is out of range";
+            return;
+          }
+          mesh.uv.push_back((float)(*gw.Ud)[2 * k]);
+          mesh.uv.push_back((float)(*gw.Ud)[2 * k + 1]);
+        }
+      }
+      const int32_t nc = (int32_t)(c1 - c0);
+      for (int32_t k = 1; k + 1 < nc; ++k) {  // a fan from the first corner
+        mesh.tris.push_back(base);
+        mesh.tris.push_back(base + k);
+        mesh.tris.push_back(base + k + 1);
+      }
+    }
+  };
+  std::atomic<size_t> next{0};
+  rmn::run_threads(std::min(rmn::host_threads(), work.size()), [&](size_t) {
+    for (size_t j; (j = next.fetch_add(1)) < work.size();) fill(work[j]);
+  });
+  for (const MeshWork& mw : work)
+    if (mw.err) return fail(RMN_ERR_INVALID_ARGUMENT, "%s: %s", path.c_str(), mw.err);
+  if (!late_err.empty()) return fail(RMN_ERR_INVALID_ARGUMENT, "%s: %s", path.c_str(), late_err.c_str());
+  for (MeshWork& mw : work)
+    if (!mw.mesh.tris.empty()) meshes.push_back(std::move(mw.mesh));
   return RMN_OK;
 }
 

@@ -981,11 +981,27 @@ rmn_status decode_dds(const std::vector<uint8_t>& f, bool header_only, Decoded& 
   return RMN_OK;
 }
 
-bool read_file(const char* path, std::vector<uint8_t>& out) {
+// The size first (one allocation, one read), then whatever follows it: a
+// file whose size cannot be taken, or that grew meanwhile, is read to its end.
+template <class Buf>
+bool read_into(const char* path, Buf& out) {
   FILE* fp = std::fopen(path, "rb");
   if (!fp) return false;
   out.clear();
-  uint8_t buf[1 << 16];
+  long size = -1;
+  if (std::fseek(fp, 0, SEEK_END) == 0) {
+    const long at_end = std::ftell(fp);
+    if (std::fseek(fp, 0, SEEK_SET) != 0) {
+      std::fclose(fp);
+      return false;
+    }
+    size = at_end;
+  }
+  if (size > 0) {
+    out.resize((size_t)size);
+    out.resize(std::fread(&out[0], 1, (size_t)size, fp));
+  }
+  char buf[1 << 16];
   size_t n;
   while ((n = std::fread(buf, 1, sizeof buf, fp)) > 0) out.insert(out.end(), buf, buf + n);
   const bool ok = !std::ferror(fp);
@@ -993,9 +1009,14 @@ bool read_file(const char* path, std::vector<uint8_t>& out) {
   return ok;
 }
 
+bool read_file(const char* path, std::vector<uint8_t>& out) { return read_into(path, out); }
+
 }  // namespace
 
 namespace rmn {
+
+bool read_whole_file(const char* path, std::vector<uint8_t>& out) { return read_into(path, out); }
+bool read_whole_file(const char* path, std::string& out) { return read_into(path, out); }
 
 const char* zlib_inflate(const uint8_t* p, size_t n, std::vector<uint8_t>& out, size_t want) {
   return zlib_decompress(p, n, out, want);

@@ -57,44 +57,9 @@ using rmn::fail;
 
 const char* const kDefaultMaterial = "DefaultMaterial";
 
-// fn(0) .. fn(n - 1), each on its own thread (fn(0) on the caller's). Every
-// thread started is joined, also when starting another fails; the first
-// exception of any of them is rethrown here.
-template <class F>
-void run_threads(size_t n, F fn) {
-  std::vector<std::exception_ptr> err(n);
-  auto guarded = [&](size_t k) {
-    try {
-      fn(k);
-    } catch (...) {
-      err[k] = std::current_exception();
-    }
-  };
-  std::vector<std::thread> pool;
-  std::exception_ptr start_err;
-  try {
-    for (size_t k = 1; k < n; ++k) pool.emplace_back(guarded, k);
-  } catch (...) {
-    start_err = std::current_exception();
-  }
-  if (!start_err) guarded(0);
-  for (std::thread& th : pool) th.join();
-  if (start_err) std::rethrow_exception(start_err);
-  for (const std::exception_ptr& e : err)
-    if (e) std::rethrow_exception(e);
-}
+using rmn::run_threads;
 
-bool read_text(const std::string& path, std::string& out) {
-  FILE* fp = std::fopen(path.c_str(), "rb");
-  if (!fp) return false;
-  out.clear();
-  char buf[1 << 16];
-  size_t n;
-  while ((n = std::fread(buf, 1, sizeof buf, fp)) > 0) out.append(buf, n);
-  const bool ok = !std::ferror(fp);
-  std::fclose(fp);
-  return ok;
-}
+bool read_text(const std::string& path, std::string& out) { return rmn::read_whole_file(path.c_str(), out); }
 
 // Lines as a text reader sees them: "\r\n" and "\r" end lines too, and a
 // backslash before the end of a line continues it (OBJ only).
@@ -446,8 +411,7 @@ rmn_status parse_obj(const std::string& path, std::vector<float>& P, std::vector
     std::string().swap(raw);
   }
   // pieces that start at line starts, parsed on separate threads
-  const size_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const size_t want = std::max<size_t>(1, std::min(hw, t.size() / kObjPieceBytes));
+  const size_t want = std::max<size_t>(1, std::min(rmn::host_threads(), t.size() / kObjPieceBytes));
   std::vector<size_t> cut{0};
   for (size_t k = 1; k < want; ++k) {
     size_t j = std::max(cut.back(), t.size() * k / want);
@@ -628,7 +592,7 @@ rmn_status finish_model(const std::string& folder, const std::string& name, cons
         if (t.st != RMN_OK) t.err = rmn_last_error();
       }
     };
-    const size_t nthreads = std::min<size_t>(jobs.size(), std::max(1u, std::min(16u, std::thread::hardware_concurrency())));
+    const size_t nthreads = std::min<size_t>(jobs.size(), rmn::host_threads());
     run_threads(nthreads, [&](size_t) { work(); });
   }
   std::vector<int> tex_of(jobs.size(), -1);

@@ -1,7 +1,9 @@
 // Host-side internals of librmn: scene object, error reporting and the
 // kernel launchers implemented in the .cu files.
 #pragma once
+#include <exception>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/rmn.h"
@@ -87,6 +89,43 @@ struct FbxMaterial {
   std::string textures[4];
 };
 rmn_status read_fbx(const std::string& path, std::vector<FbxMesh>& meshes, std::vector<FbxMaterial>& materials);
+
+// The whole file, read at its size (image_io.cpp); false if it cannot be
+// opened or read.
+bool read_whole_file(const char* path, std::vector<uint8_t>& out);
+bool read_whole_file(const char* path, std::string& out);
+
+// fn(0) .. fn(n - 1), each on its own thread (fn(0) on the caller's). Every
+// thread started is joined, also when starting another fails; the first
+// exception of any of them is rethrown here.
+template <class F>
+void run_threads(size_t n, F fn) {
+  std::vector<std::exception_ptr> err(n);
+  auto guarded = [&](size_t k) {
+    try {
+      fn(k);
+    } catch (...) {
+      err[k] = std::current_exception();
+    }
+  };
+  std::vector<std::thread> pool;
+  std::exception_ptr start_err;
+  try {
+    for (size_t k = 1; k < n; ++k) pool.emplace_back(guarded, k);
+  } catch (...) {
+    start_err = std::current_exception();
+  }
+  if (!start_err && n > 0) guarded(0);
+  for (std::thread& th : pool) th.join();
+  if (start_err) std::rethrow_exception(start_err);
+  for (const std::exception_ptr& e : err)
+    if (e) std::rethrow_exception(e);
+}
+// Worker threads for host-side parallel work: the hardware threads, 1..16.
+inline size_t host_threads() {
+  const unsigned hw = std::thread::hardware_concurrency();
+  return hw < 1 ? 1 : hw > 16 ? 16 : hw;
+}
 
 // A zlib stream of n bytes (image_io.cpp): LZ77 + dynamic Huffman blocks.
 std::vector<uint8_t> zlib_compress(const uint8_t* data, size_t n);
