@@ -1027,9 +1027,11 @@ const char* zlib_inflate(const uint8_t* p, size_t n, std::vector<uint8_t>& out, 
 // of kNice bytes taken at once) and
 // dynamic-Huffman blocks of up to 2^16 symbols; stored blocks when that
 // would not be smaller.
-std::vector<uint8_t> zlib_compress(const uint8_t* data, size_t n) {
+// Greedy LZ77 over data[s0, s1) with dynamic-Huffman blocks into bw; the
+// last block is final when `last`. Matches stay inside [s0, s1) but may
+// start up to 32 KiB before s0 (those positions only enter the hash chains).
+void deflate_range(const uint8_t* data, size_t n, size_t s0, size_t s1, bool last, BitWriter& bw) {
   constexpr int kHashBits = 15, kWindow = 32768, kChain = 8, kNice = 64, kMaxMatch = 258;
-  std::vector<uint8_t> out = {0x78, 0x9C};
   std::vector<int32_t> head(1 << kHashBits, -1), prev(kWindow, -1);
   auto hash = [&](size_t i) {
     const uint32_t v = (uint32_t)data[i] | (uint32_t)data[i + 1] << 8 | (uint32_t)data[i + 2] << 16;
@@ -1041,14 +1043,15 @@ std::vector<uint8_t> zlib_compress(const uint8_t* data, size_t n) {
     prev[i & (kWindow - 1)] = head[h];
     head[h] = (int32_t)i;
   };
-  BitWriter bw(out);
+  for (size_t i = s0 > (size_t)kWindow ? s0 - kWindow : 0; i < s0; ++i) insert(i);
   std::vector<Symbol> sy;
   sy.reserve(1 << 16);
-  size_t i = 0;
-  while (i < n) {
+  bool wrote_last = false;
+  size_t i = s0;
+  while (i < s1) {
     int best = 0, best_d = 0;
-    if (i + 2 < n) {
-      const size_t limit = std::min<size_t>(kMaxMatch, n - i);
+    if (i + 2 < s1) {
+      const size_t limit = std::min<size_t>(kMaxMatch, s1 - i);
       int32_t cand = head[hash(i)];
       for (int c = 0; c < kChain && cand >= 0 && i - (size_t)cand <= (size_t)kWindow; ++c) {
         const uint8_t* a = data + cand;
@@ -1076,13 +1079,39 @@ std::vector<uint8_t> zlib_compress(const uint8_t* data, size_t n) {
       insert(i);
       ++i;
     }
-    if (sy.size() == (1u << 16) || i == n) {
-      write_block(bw, sy, i == n);
+    if (sy.size() == (1u << 16) || i == s1) {
+      write_block(bw, sy, last && i == s1);
+      wrote_last = last && i == s1;
       sy.clear();
     }
   }
-  if (n == 0) write_block(bw, sy, true);
-  bw.flush();
+  if (last && !wrote_last) write_block(bw, sy, true);  // an empty input
+}
+
+// A zlib stream (RFC 1950) of data[0, n). From 1 MiB on, the data is cut
+// into segments of at least 256 KiB compressed on separate threads, each
+// ended (but the last) by an empty stored block so that the next starts on
+// a byte boundary -- one valid stream, as one thread would write it but for
+// the block boundaries.
+std::vector<uint8_t> zlib_compress(const uint8_t* data, size_t n) {
+  std::vector<uint8_t> out = {0x78, 0x9C};
+  const size_t parts = n >= (1u << 20) ? std::max<size_t>(1, std::min(rmn::host_threads(), n / (256u << 10))) : 1;
+  if (parts == 1) {
+    BitWriter bw(out);
+    deflate_range(data, n, 0, n, true, bw);
+    bw.flush();
+  } else {
+    std::vector<std::vector<uint8_t>> seg(parts);
+    rmn::run_threads(parts, [&](size_t k) {
+      BitWriter bw(seg[k]);
+      const bool last = k + 1 == parts;
+      deflate_range(data, n, n * k / parts, n * (k + 1) / parts, last, bw);
+      if (!last) bw.put(0, 3);  // BFINAL 0, BTYPE 00: a stored block ...
+      bw.flush();               // ... from the next byte boundary
+      if (!last) seg[k].insert(seg[k].end(), {0x00, 0x00, 0xff, 0xff});  // LEN 0, NLEN
+    });
+    for (const std::vector<uint8_t>& sg : seg) out.insert(out.end(), sg.begin(), sg.end());
+  }
   if (out.size() > n + n / 65535 * 5 + 16) {  // incompressible: stored blocks
     out.assign({0x78, 0x01});
     size_t pos = 0;

@@ -83,55 +83,64 @@ rmn_status write_png(const float* rgb, int w, int h, const char* path) {
   // scanlines, each with the filter whose bytes have the smallest sum of
   // magnitudes (bytes read as signed), as libpng's adaptive filtering picks
   const size_t stride = 3 * (size_t)w;
-  std::vector<uint8_t> raw((stride + 1) * h), cur(stride), prev(stride, 0), best(stride), trial(stride);
+  std::vector<uint8_t> raw((stride + 1) * h);
   auto magnitude = [](uint8_t v) -> uint32_t { return v < 128 ? v : 256u - v; };
-  for (int y = 0; y < h; ++y) {
-    for (size_t k = 0; k < stride; ++k) cur[k] = to_byte(rgb[stride * y + k]);
-    uint64_t best_sum = UINT64_MAX;
-    int best_ft = 0;
-    for (int ft = 0; ft < 5; ++ft) {  // one loop per filter type (bpp = 3)
-      uint8_t* t = trial.data();
-      const uint8_t* x = cur.data();
-      const uint8_t* up = prev.data();
-      const size_t k = std::min<size_t>(3, stride);
-      switch (ft) {
-        case 0:
-          std::memcpy(t, x, stride);
-          break;
-        case 1:
-          std::memcpy(t, x, k);
-          for (size_t i = k; i < stride; ++i) t[i] = (uint8_t)(x[i] - x[i - 3]);
-          break;
-        case 2:
-          for (size_t i = 0; i < stride; ++i) t[i] = (uint8_t)(x[i] - up[i]);
-          break;
-        case 3:
-          for (size_t i = 0; i < k; ++i) t[i] = (uint8_t)(x[i] - (up[i] >> 1));
-          for (size_t i = k; i < stride; ++i) t[i] = (uint8_t)(x[i] - ((x[i - 3] + up[i]) >> 1));
-          break;
-        default:
-          for (size_t i = 0; i < k; ++i) t[i] = (uint8_t)(x[i] - up[i]);  // a = c = 0: Paeth picks b
-          for (size_t i = k; i < stride; ++i) {
-            const int a = x[i - 3], b = up[i], c = up[i - 3];
-            const int pa = std::abs(b - c), pb = std::abs(a - c), pc = std::abs(a + b - 2 * c);
-            const int bc = pc < pb ? c : b;
-            t[i] = (uint8_t)(x[i] - ((pc < pb ? pc : pb) < pa ? bc : a));
-          }
-          break;
+  // rows in ranges on separate threads: a row's filter depends only on its
+  // own bytes and the row above, both taken from the image
+  auto filter_rows = [&](int y0, int y1) {
+    std::vector<uint8_t> cur(stride), prev(stride, 0), best(stride), trial(stride);
+    if (y0 > 0)
+      for (size_t k = 0; k < stride; ++k) prev[k] = to_byte(rgb[stride * (y0 - 1) + k]);
+    for (int y = y0; y < y1; ++y) {
+      for (size_t k = 0; k < stride; ++k) cur[k] = to_byte(rgb[stride * y + k]);
+      uint64_t best_sum = UINT64_MAX;
+      int best_ft = 0;
+      for (int ft = 0; ft < 5; ++ft) {  // one loop per filter type (bpp = 3)
+        uint8_t* t = trial.data();
+        const uint8_t* x = cur.data();
+        const uint8_t* up = prev.data();
+        const size_t k = std::min<size_t>(3, stride);
+        switch (ft) {
+          case 0:
+            std::memcpy(t, x, stride);
+            break;
+          case 1:
+            std::memcpy(t, x, k);
+            for (size_t i = k; i < stride; ++i) t[i] = (uint8_t)(x[i] - x[i - 3]);
+            break;
+          case 2:
+            for (size_t i = 0; i < stride; ++i) t[i] = (uint8_t)(x[i] - up[i]);
+            break;
+          case 3:
+            for (size_t i = 0; i < k; ++i) t[i] = (uint8_t)(x[i] - (up[i] >> 1));
+            for (size_t i = k; i < stride; ++i) t[i] = (uint8_t)(x[i] - ((x[i - 3] + up[i]) >> 1));
+            break;
+          default:
+            for (size_t i = 0; i < k; ++i) t[i] = (uint8_t)(x[i] - up[i]);  // a = c = 0: Paeth picks b
+            for (size_t i = k; i < stride; ++i) {
+              const int a = x[i - 3], b = up[i], c = up[i - 3];
+              const int pa = std::abs(b - c), pb = std::abs(a - c), pc = std::abs(a + b - 2 * c);
+              const int bc = pc < pb ? c : b;
+              t[i] = (uint8_t)(x[i] - ((pc < pb ? pc : pb) < pa ? bc : a));
+            }
+            break;
+        }
+        uint64_t sum = 0;
+        for (size_t i = 0; i < stride; ++i) sum += magnitude(t[i]);
+        if (sum < best_sum) {
+          best_sum = sum;
+          best_ft = ft;
+          best.swap(trial);
+        }
       }
-      uint64_t sum = 0;
-      for (size_t i = 0; i < stride; ++i) sum += magnitude(t[i]);
-      if (sum < best_sum) {
-        best_sum = sum;
-        best_ft = ft;
-        best.swap(trial);
-      }
+      uint8_t* r = &raw[(stride + 1) * y];
+      r[0] = (uint8_t)best_ft;
+      std::memcpy(r + 1, best.data(), stride);
+      prev.swap(cur);
     }
-    uint8_t* r = &raw[(stride + 1) * y];
-    r[0] = (uint8_t)best_ft;
-    std::memcpy(r + 1, best.data(), stride);
-    prev.swap(cur);
-  }
+  };
+  const size_t parts = std::max<size_t>(1, std::min(host_threads(), (size_t)h * stride / (256u << 10)));
+  run_threads(parts, [&](size_t k) { filter_rows((int)(h * k / parts), (int)(h * (k + 1) / parts)); });
   const std::vector<uint8_t> z = zlib_compress(raw.data(), raw.size());
 
   std::vector<uint8_t> out = {0x89, 'P', 'N', 'G', '\r', '\n', 0x1a, '\n'};

@@ -499,14 +499,16 @@ def test_native_importer_large_random_models(tmp_path):
         assets.load_model(folder, "bad.obj")
 
 
-@pytest.mark.parametrize("kind", ["smooth", "noise", "tiles", "tiny", "flat"])
+@pytest.mark.parametrize("kind", ["smooth", "noise", "tiles", "tiny", "flat", "large"])
 def test_save_png_compresses_and_round_trips(tmp_path, kind):
     """rmn_save_png's deflate stream: read back by Python's zlib (through
     the oracle's reader) and by the library's own decoder, pixel for pixel;
-    smooth and repetitive images shrink, noise falls back to stored blocks."""
+    smooth and repetitive images shrink, noise falls back to stored blocks.
+    "large" (1080 x 1920) is filtered and compressed in pieces on several
+    threads, the stream's segments joined by empty stored blocks."""
     lib = _lib.load()
     rng = np.random.default_rng(5)
-    h, w = {"tiny": (1, 2), "tiles": (300, 700)}.get(kind, (240, 320))
+    h, w = {"tiny": (1, 2), "tiles": (300, 700), "large": (1080, 1920)}.get(kind, (240, 320))
     yy, xx = np.mgrid[0:h, 0:w].astype(np.float32)
     if kind == "smooth":
         img = np.stack([xx / w, yy / h, (xx + yy) / (w + h)], -1)
@@ -517,6 +519,9 @@ def test_save_png_compresses_and_round_trips(tmp_path, kind):
         img = np.tile(tile, (h // 20 + 1, w // 37 + 1, 1))[:h, :w]
     elif kind == "flat":
         img = np.full((h, w, 3), 0.25, np.float32)
+    elif kind == "large":  # a gradient with mild noise and a repeated band (matches across segments)
+        img = np.stack([xx / w, yy / h, (xx + yy) / (w + h)], -1) + rng.normal(0, 0.01, (h, w, 3))
+        img[500:560] = img[100:160]
     else:
         img = rng.random((h, w, 3), dtype=np.float32)
     img = np.ascontiguousarray(img, np.float32)
@@ -536,6 +541,8 @@ def test_save_png_compresses_and_round_trips(tmp_path, kind):
         assert size < 0.1 * raw
     if kind == "tiles":
         assert size < 0.2 * raw
+    if kind == "large":
+        assert size < 0.6 * raw
     if kind == "noise":
         assert size < raw * 1.01 + 200
 
