@@ -930,32 +930,36 @@ rmn_status decode_dds(const std::vector<uint8_t>& f, bool header_only, Decoded& 
   if (block) {
     const size_t bw = (w + 3) / 4, bh = (h + 3) / 4;
     if (bw * bh * block > avail) return fail(RMN_ERR_INVALID_ARGUMENT, "DDS: truncated block data");
-    uint8_t tex[16][4];
-    for (size_t by = 0; by < bh; ++by)
-      for (size_t bx = 0; bx < bw; ++bx) {
-        const uint8_t* blk = data + (by * bw + bx) * block;
-        color_block(kind == 1 ? blk : blk + 8, kind == 1, tex);
-        if (kind == 2) {  // explicit 4-bit alpha, expanded by 17
-          for (int t = 0; t < 16; ++t) tex[t][3] = (uint8_t)(((blk[t >> 1] >> (4 * (t & 1))) & 15) * 17);
-        } else if (kind == 3) {  // interpolated alpha
-          const int a0 = blk[0], a1 = blk[1];
-          int pal[8] = {a0, a1};
-          if (a0 > a1) {
-            for (int k = 2; k < 8; ++k) pal[k] = ((8 - k) * a0 + (k - 1) * a1) / 7;
-          } else {
-            for (int k = 2; k < 6; ++k) pal[k] = ((6 - k) * a0 + (k - 1) * a1) / 5;
-            pal[6] = 0;
-            pal[7] = 255;
+    // rows of blocks in ranges on separate threads: each writes its own pixel rows
+    const size_t parts = std::max<size_t>(1, std::min(rmn::host_threads(), bw * bh / 16384));
+    rmn::run_threads(parts, [&](size_t part) {
+      uint8_t tex[16][4];
+      for (size_t by = bh * part / parts; by < bh * (part + 1) / parts; ++by)
+        for (size_t bx = 0; bx < bw; ++bx) {
+          const uint8_t* blk = data + (by * bw + bx) * block;
+          color_block(kind == 1 ? blk : blk + 8, kind == 1, tex);
+          if (kind == 2) {  // explicit 4-bit alpha, expanded by 17
+            for (int t = 0; t < 16; ++t) tex[t][3] = (uint8_t)(((blk[t >> 1] >> (4 * (t & 1))) & 15) * 17);
+          } else if (kind == 3) {  // interpolated alpha
+            const int a0 = blk[0], a1 = blk[1];
+            int pal[8] = {a0, a1};
+            if (a0 > a1) {
+              for (int k = 2; k < 8; ++k) pal[k] = ((8 - k) * a0 + (k - 1) * a1) / 7;
+            } else {
+              for (int k = 2; k < 6; ++k) pal[k] = ((6 - k) * a0 + (k - 1) * a1) / 5;
+              pal[6] = 0;
+              pal[7] = 255;
+            }
+            uint64_t bits = 0;
+            for (int k = 0; k < 6; ++k) bits |= (uint64_t)blk[2 + k] << (8 * k);
+            for (int t = 0; t < 16; ++t) tex[t][3] = (uint8_t)pal[bits >> (3 * t) & 7];
           }
-          uint64_t bits = 0;
-          for (int k = 0; k < 6; ++k) bits |= (uint64_t)blk[2 + k] << (8 * k);
-          for (int t = 0; t < 16; ++t) tex[t][3] = (uint8_t)pal[bits >> (3 * t) & 7];
+          for (int t = 0; t < 16; ++t) {
+            const size_t x = bx * 4 + (t & 3), y = by * 4 + (t >> 2);
+            if (x < w && y < h) std::memcpy(&img.bytes[(y * w + x) * 4], tex[t], 4);
+          }
         }
-        for (int t = 0; t < 16; ++t) {
-          const size_t x = bx * 4 + (t & 3), y = by * 4 + (t >> 2);
-          if (x < w && y < h) std::memcpy(&img.bytes[(y * w + x) * 4], tex[t], 4);
-        }
-      }
+    });
     return RMN_OK;
   }
   const size_t px_bytes = bitcount / 8, pitch = (size_t)w * px_bytes;
