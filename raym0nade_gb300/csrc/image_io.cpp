@@ -25,9 +25,13 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <condition_variable>
 #include <cstring>
+#include <mutex>
 #include <stdexcept>
 #include <string>
+#include <system_error>
+#include <thread>
 #include <vector>
 
 #include "rmn_host.h"
@@ -188,10 +192,47 @@ inline void copy_match(uint8_t* dst, size_t d, size_t len, size_t room) {
   for (size_t k = 0; k < len; ++k) dst[k] = src[k];
 }
 
+// How far an inflate has come, for a thread that consumes its output while
+// it runs: out[0, ready) is final (a match copied 8 bytes at a time may
+// write a few bytes past its end, never before it).
+class InflateProgress {
+ public:
+  void publish(size_t ready) {
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      ready_ = ready;
+    }
+    cv_.notify_all();
+  }
+  void finish() {  // the producer stopped, finished or not
+    {
+      std::lock_guard<std::mutex> lk(m_);
+      done_ = true;
+    }
+    cv_.notify_all();
+  }
+  // Waits until out[0, need) is final (true) or the producer stopped short of it (false).
+  bool wait_for(size_t need) {
+    std::unique_lock<std::mutex> lk(m_);
+    cv_.wait(lk, [&] { return ready_ >= need || done_; });
+    return ready_ >= need;
+  }
+
+ private:
+  std::mutex m_;
+  std::condition_variable cv_;
+  size_t ready_ = 0;
+  bool done_ = false;
+};
+constexpr size_t kPublishStep = 64 << 10;
+
 // A deflate stream into out[0, cap); *produced = bytes written. Returns
-// nullptr or a description of what is wrong with the stream.
-const char* inflate_stream(BitReader& br, uint8_t* out, size_t cap, size_t* produced) {
-  size_t o = 0;
+// nullptr or a description of what is wrong with the stream. With `prog`,
+// the output so far is published at least every 64 KiB of matches and at
+// every block's end.
+const char* inflate_stream(BitReader& br, uint8_t* out, size_t cap, size_t* produced,
+                           InflateProgress* prog = nullptr) {
+  size_t o = 0, next_pub = kPublishStep;
   Huffman lit, dist, lens;
   uint32_t final_block = 0;
   do {
@@ -214,6 +255,7 @@ const char* inflate_stream(BitReader& br, uint8_t* out, size_t cap, size_t* prod
       std::memcpy(out + o, br.p + br.pos, len);
       o += len;
       br.pos += len;
+      if (prog) prog->publish(o);
       continue;
     }
     if (type == 3) return "invalid deflate block type";
@@ -292,7 +334,12 @@ const char* inflate_stream(BitReader& br, uint8_t* out, size_t cap, size_t* prod
       if (o + len > cap) return "more image data than the image holds";
       copy_match(out + o, d, len, cap - o);
       o += len;
+      if (prog && o >= next_pub) {
+        prog->publish(o);
+        next_pub = o + kPublishStep;
+      }
     }
+    if (prog) prog->publish(o);
   } while (!final_block);
   *produced = o;
   return nullptr;
@@ -301,8 +348,8 @@ const char* inflate_stream(BitReader& br, uint8_t* out, size_t cap, size_t* prod
 // Adler-32 (RFC 1950 section 8.2). Over 16 bytes p[0..15] the sums advance
 // as a += sum p[k], b += 16 a + sum (16 - k) p[k]: the same values the byte
 // loop reaches, from sums that do not depend on one another.
-uint32_t adler32(const uint8_t* p, size_t n) {
-  uint32_t a = 1, b = 0;
+uint32_t adler32(const uint8_t* p, size_t n, uint32_t start = 1) {
+  uint32_t a = start & 0xffff, b = start >> 16;
   while (n) {
     const size_t m = n < 5552 ? n : 5552;  // largest run without overflow of b
     size_t i = 0;
@@ -327,23 +374,33 @@ uint32_t adler32(const uint8_t* p, size_t n) {
   return b << 16 | a;
 }
 
-// A zlib stream (RFC 1950) that must inflate to exactly `want` bytes.
-const char* zlib_decompress(const uint8_t* p, size_t n, std::vector<uint8_t>& out, size_t want) {
+// The zlib stream's header and deflate data into out[0, want) (sized by the
+// caller), and its Adler-32 field into *check: everything but the checksum
+// comparison.
+const char* zlib_inflate_only(const uint8_t* p, size_t n, uint8_t* out, size_t want, uint32_t* check,
+                              InflateProgress* prog) {
   if (n < 2) return "truncated zlib stream";
   if ((p[0] & 15) != 8 || (p[0] >> 4) > 7 || ((unsigned)p[0] << 8 | p[1]) % 31 != 0) return "bad zlib header";
   if (p[1] & 0x20) return "zlib preset dictionary";
-  out.assign(want, 0);
   BitReader br(p + 2, n - 2);
   size_t got = 0;
-  if (const char* err = inflate_stream(br, out.data(), want, &got)) return err;
+  if (const char* err = inflate_stream(br, out, want, &got, prog)) return err;
   if (got != want) return "less image data than the image holds";
   br.byte_align();
-  uint32_t check = 0;
+  *check = 0;
   for (int i = 0; i < 4; ++i) {
     uint32_t b;
     if (!br.get(8, &b)) return "truncated zlib checksum";
-    check = check << 8 | b;
+    *check = *check << 8 | b;
   }
+  return nullptr;
+}
+
+// A zlib stream (RFC 1950) that must inflate to exactly `want` bytes.
+const char* zlib_decompress(const uint8_t* p, size_t n, std::vector<uint8_t>& out, size_t want) {
+  out.assign(want, 0);
+  uint32_t check = 0;
+  if (const char* err = zlib_inflate_only(p, n, out.data(), want, &check, nullptr)) return err;
   if (check != adler32(out.data(), out.size())) return "zlib checksum mismatch";
   return nullptr;
 }
@@ -716,63 +773,115 @@ rmn_status decode_png(const std::vector<uint8_t>& f, bool header_only, Decoded& 
     const size_t rows = (h - passes[k].y0 + passes[k].dy - 1) / passes[k].dy;
     want += rows * (1 + (cols * bits + 7) / 8);
   }
-  std::vector<uint8_t> raw;
-  if (const char* err = zlib_decompress(idat.data(), idat.size(), raw, want))
-    return fail(RMN_ERR_INVALID_ARGUMENT, "PNG: %s", err);
-
   img.bytes.assign((size_t)w * h * 3, 0);
   const int maxv = (1 << depth) - 1;
   const int gray_scale = depth < 8 ? 255 / maxv : 1;  // png_set_expand_gray_1_2_4_to_8
-  size_t at_raw = 0;
-  std::vector<uint8_t> prev, cur;
-  for (int k = 0; k < npass; ++k) {
-    const Pass& ps = passes[k];
-    if (ps.x0 >= (int)w || ps.y0 >= (int)h) continue;
-    const size_t cols = (w - ps.x0 + ps.dx - 1) / ps.dx;
-    const size_t rows = (h - ps.y0 + ps.dy - 1) / ps.dy;
-    const size_t stride = (cols * bits + 7) / 8;
-    prev.assign(stride, 0);
-    cur.assign(stride, 0);
-    for (size_t r = 0; r < rows; ++r) {
-      const uint8_t ft = raw[at_raw];
-      const uint8_t* src = &raw[at_raw + 1];
-      at_raw += 1 + stride;
-      if (ft > 4) return fail(RMN_ERR_INVALID_ARGUMENT, "PNG: bad filter type %d", ft);
-      const size_t y = ps.y0 + r * ps.dy;
-      uint8_t* px = &img.bytes[(y * w + ps.x0) * 3];
-      if (depth == 8 && ctype == 2 && !interlace) {  // the image's own rows are the scanlines
-        unfilter_row(ft, src, r ? px - stride : prev.data(), px, stride, bpp);
-        continue;
-      }
-      unfilter_row(ft, src, prev.data(), cur.data(), stride, bpp);
-      // samples of this row to 8-bit RGB
-      const size_t step = 3 * (size_t)ps.dx;
-      const uint8_t* q = cur.data();
-      if (depth == 8 && ctype == 2 && ps.dx == 1) {
-        std::memcpy(px, q, cols * 3);
-      } else if (depth == 8 && (ctype == 2 || ctype == 6)) {
-        for (size_t i = 0; i < cols; ++i, px += step, q += nch) px[0] = q[0], px[1] = q[1], px[2] = q[2];
-      } else if (depth == 16 && (ctype == 2 || ctype == 6)) {  // png_set_strip_16: the high byte
-        for (size_t i = 0; i < cols; ++i, px += step, q += 2 * nch) px[0] = q[0], px[1] = q[2], px[2] = q[4];
-      } else if (depth >= 8 && (ctype == 0 || ctype == 4)) {
-        const size_t adv = (size_t)nch * (depth / 8);
-        for (size_t i = 0; i < cols; ++i, px += step, q += adv) px[0] = px[1] = px[2] = q[0];
-      } else {  // 1/2/4/8-bit gray or palette indices
-        for (size_t i = 0; i < cols; ++i, px += step) {
-          const size_t bit = i * depth;
-          const int v = depth == 8 ? q[i] : (q[bit >> 3] >> (8 - depth - (bit & 7))) & maxv;
-          if (ctype == 0) {
-            px[0] = px[1] = px[2] = (uint8_t)(v * gray_scale);
-          } else if ((size_t)v * 3 + 2 < palette.size()) {
-            px[0] = palette[v * 3];
-            px[1] = palette[v * 3 + 1];
-            px[2] = palette[v * 3 + 2];
-          }  // an index past the palette stays black
+  std::vector<uint8_t> raw(want);
+  // The scanlines, in stream order: each waits (with `prog`) until the
+  // inflate has produced it, and the Adler-32 of the bytes taken so far is
+  // kept in *adler / *taken. Returns -1, or the first row's filter type
+  // byte that is not one.
+  auto unfilter_all = [&](InflateProgress* prog, uint32_t* adler, size_t* taken) -> int {
+    size_t at_raw = 0;
+    std::vector<uint8_t> prev, cur;
+    for (int k = 0; k < npass; ++k) {
+      const Pass& ps = passes[k];
+      if (ps.x0 >= (int)w || ps.y0 >= (int)h) continue;
+      const size_t cols = (w - ps.x0 + ps.dx - 1) / ps.dx;
+      const size_t rows = (h - ps.y0 + ps.dy - 1) / ps.dy;
+      const size_t stride = (cols * bits + 7) / 8;
+      prev.assign(stride, 0);
+      cur.assign(stride, 0);
+      for (size_t r = 0; r < rows; ++r) {
+        if (prog && !prog->wait_for(at_raw + 1 + stride)) return -1;  // the inflate stopped short
+        const uint8_t ft = raw[at_raw];
+        const uint8_t* src = &raw[at_raw + 1];
+        *adler = adler32(&raw[at_raw], 1 + stride, *adler);
+        at_raw += 1 + stride;
+        *taken = at_raw;
+        if (ft > 4) return ft;
+        const size_t y = ps.y0 + r * ps.dy;
+        uint8_t* px = &img.bytes[(y * w + ps.x0) * 3];
+        if (depth == 8 && ctype == 2 && !interlace) {  // the image's own rows are the scanlines
+          unfilter_row(ft, src, r ? px - stride : prev.data(), px, stride, bpp);
+          continue;
         }
+        unfilter_row(ft, src, prev.data(), cur.data(), stride, bpp);
+        // samples of this row to 8-bit RGB
+        const size_t step = 3 * (size_t)ps.dx;
+        const uint8_t* q = cur.data();
+        if (depth == 8 && ctype == 2 && ps.dx == 1) {
+          std::memcpy(px, q, cols * 3);
+        } else if (depth == 8 && (ctype == 2 || ctype == 6)) {
+          for (size_t i = 0; i < cols; ++i, px += step, q += nch) px[0] = q[0], px[1] = q[1], px[2] = q[2];
+        } else if (depth == 16 && (ctype == 2 || ctype == 6)) {  // png_set_strip_16: the high byte
+          for (size_t i = 0; i < cols; ++i, px += step, q += 2 * nch) px[0] = q[0], px[1] = q[2], px[2] = q[4];
+        } else if (depth >= 8 && (ctype == 0 || ctype == 4)) {
+          const size_t adv = (size_t)nch * (depth / 8);
+          for (size_t i = 0; i < cols; ++i, px += step, q += adv) px[0] = px[1] = px[2] = q[0];
+        } else {  // 1/2/4/8-bit gray or palette indices
+          for (size_t i = 0; i < cols; ++i, px += step) {
+            const size_t bit = i * depth;
+            const int v = depth == 8 ? q[i] : (q[bit >> 3] >> (8 - depth - (bit & 7))) & maxv;
+            if (ctype == 0) {
+              px[0] = px[1] = px[2] = (uint8_t)(v * gray_scale);
+            } else if ((size_t)v * 3 + 2 < palette.size()) {
+              px[0] = palette[v * 3];
+              px[1] = palette[v * 3 + 1];
+              px[2] = palette[v * 3 + 2];
+            }  // an index past the palette stays black
+          }
+        }
+        std::swap(prev, cur);
       }
-      std::swap(prev, cur);
+    }
+    return -1;
+  };
+  // From 1 MiB of scanline data on, the rows are unfiltered on a second
+  // thread while the stream inflates. A defect is reported as a reader that
+  // inflated everything first would: the stream's (its checksum included)
+  // before a row's.
+  uint32_t check = 0, adler = 1;
+  size_t taken = 0;
+  const char* zerr = nullptr;
+  int bad_ft = -1;
+  bool piped = false;
+  if (want >= (1u << 20)) {
+    InflateProgress prog;
+    std::exception_ptr rexc;
+    std::thread rows;
+    try {
+      rows = std::thread([&] {
+        try {
+          bad_ft = unfilter_all(&prog, &adler, &taken);
+        } catch (...) {
+          rexc = std::current_exception();
+        }
+      });
+      piped = true;
+    } catch (const std::system_error&) {  // no thread: one after the other below
+    }
+    if (piped) {
+      try {
+        zerr = zlib_inflate_only(idat.data(), idat.size(), raw.data(), want, &check, &prog);
+      } catch (...) {
+        prog.finish();
+        rows.join();
+        throw;
+      }
+      prog.finish();
+      rows.join();
+      if (rexc) std::rethrow_exception(rexc);
     }
   }
+  if (!piped) {
+    zerr = zlib_inflate_only(idat.data(), idat.size(), raw.data(), want, &check, nullptr);
+    if (!zerr) bad_ft = unfilter_all(nullptr, &adler, &taken);
+  }
+  if (zerr) return fail(RMN_ERR_INVALID_ARGUMENT, "PNG: %s", zerr);
+  if (taken < want) adler = adler32(raw.data() + taken, want - taken, adler);  // rows stopped at a defect
+  if (adler != check) return fail(RMN_ERR_INVALID_ARGUMENT, "PNG: zlib checksum mismatch");
+  if (bad_ft >= 0) return fail(RMN_ERR_INVALID_ARGUMENT, "PNG: bad filter type %d", bad_ft);
   return RMN_OK;
 }
 

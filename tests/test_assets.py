@@ -102,6 +102,41 @@ def test_png_back_references_of_every_short_period(tmp_path):
             assert np.array_equal(got, np.repeat(s, 3, axis=2).astype(np.uint8)), (period, w, h)
 
 
+def test_png_large_stream_defects_in_order(tmp_path):
+    """Images with more than 1 MiB of scanlines, whose rows the library
+    unfilters while the stream still inflates: the stream's defects are
+    reported before a row's, as when everything is inflated first -- a bad
+    filter byte in an early row with a wrong checksum gives the checksum
+    error, alone it gives the filter error, and a stream cut short is
+    reported as such."""
+    rng = np.random.default_rng(12)
+    h, w = 400, 1024  # 400 x (1 + 3072) bytes of scanlines
+    s = rng.integers(0, 256, (h, w, 3))
+    good = F.encode_png(s, 2, 8, filters=(1, 4, 2), level=6)
+    assert np.array_equal(assets.load_png(write(tmp_path, "ok.png", good)), s.astype(np.uint8))
+    sig, ihdr = good[:8], good[8:33]
+    rows = b"".join(bytes([4]) + s[y].astype(np.uint8).tobytes() for y in range(h))
+
+    def png(raw, z=None):
+        z = zlib.compress(raw, 6) if z is None else z
+        return sig + ihdr + F._chunk(b"IDAT", z) + F._chunk(b"IEND", b"")
+
+    bad_row = bytearray(rows)
+    bad_row[3 * (1 + 3 * w)] = 9  # row 3's filter byte
+    with pytest.raises(assets.ImageError, match="bad filter type 9"):
+        assets.load_png(write(tmp_path, "f.png", png(bytes(bad_row))))
+    z = bytearray(zlib.compress(bytes(bad_row), 6))
+    z[-1] ^= 1  # and the Adler-32 wrong
+    with pytest.raises(assets.ImageError, match="zlib checksum mismatch"):
+        assets.load_png(write(tmp_path, "c.png", png(None, bytes(z))))
+    z = zlib.compress(rows[: len(rows) // 2], 6)  # half the scanlines
+    with pytest.raises(assets.ImageError, match="less image data"):
+        assets.load_png(write(tmp_path, "s.png", png(None, z)))
+    z = zlib.compress(bytes(bad_row), 6)
+    with pytest.raises(assets.ImageError, match="truncated"):
+        assets.load_png(write(tmp_path, "t.png", png(None, z[: len(z) // 3])))
+
+
 def test_png_reads_what_save_png_writes(tmp_path):
     lib = _lib.load()
     rng = np.random.default_rng(3)
