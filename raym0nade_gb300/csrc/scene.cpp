@@ -36,17 +36,8 @@ namespace {
 // finished.
 template <class F>
 void parallel_ranges(size_t n, F fn) {
-  const size_t hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const size_t parts = std::min(hw, std::max<size_t>(1, n / 16384));
-  if (parts <= 1) {
-    fn((size_t)0, n);
-    return;
-  }
-  std::vector<std::future<void>> workers;
-  for (size_t k = 1; k < parts; ++k)
-    workers.push_back(std::async(std::launch::async, fn, n * k / parts, n * (k + 1) / parts));
-  fn((size_t)0, n / parts);
-  for (std::future<void>& w : workers) w.get();
+  const size_t parts = std::min(host_threads(), std::max<size_t>(1, n / 16384));
+  run_threads(parts, [&](size_t k) { fn(n * k / parts, n * (k + 1) / parts); });
 }
 
 // An allocator whose default-inserted elements are left uninitialised
