@@ -467,7 +467,7 @@ def config_timings(args, stream, flush, barrier):
 
 
 def asset_decode_timings(repeats):
-    """rmn_image_load (host, one thread) on full-size asset files written
+    """rmn_image_load (host; the threads the library takes for large files) on full-size asset files written
     here: a 2048x1024 run-length-encoded Radiance sky, a 2048x2048 DXT5 DDS
     texture and a 2048x2048 RGB PNG (zlib level 6, Sub / Up / Paeth rows).
     Best of `repeats` wall-clock decodes each."""
