@@ -610,8 +610,9 @@ rmn_status finish_model(const std::string& folder, const std::string& name, cons
     M.material_textures.insert(M.material_textures.end(), slots, slots + 4);
   }
 
-  M.mesh_first.assign(1, 0);
-  for (BuildMesh& mb : meshes) {
+  // each mesh's normals (geometric, or its own after the infacing test) and
+  // uvs, meshes on separate threads; then the meshes in order
+  auto prepare = [](BuildMesh& mb) {
     std::vector<float>& pos = mb.pos;
     std::vector<float>& nrm = mb.nrm;
     const size_t nc = pos.size() / 3;
@@ -664,6 +665,18 @@ rmn_status finish_model(const std::string& folder, const std::string& name, cons
       if (v0 > 0.0f && v1 < v0)
         for (float& v : nrm) v = -v;
     }
+  };
+  {
+    std::atomic<size_t> next{0};
+    run_threads(std::min(meshes.size(), rmn::host_threads()), [&](size_t) {
+      for (size_t j; (j = next.fetch_add(1)) < meshes.size();) prepare(meshes[j]);
+    });
+  }
+  M.mesh_first.assign(1, 0);
+  for (BuildMesh& mb : meshes) {
+    const std::vector<float>& pos = mb.pos;
+    const std::vector<float>& nrm = mb.nrm;
+    const size_t nt = mb.tris.size() / 3;
     const int32_t base = (int32_t)(M.positions.size() / 3);
     M.positions.insert(M.positions.end(), pos.begin(), pos.end());
     M.normals.insert(M.normals.end(), nrm.begin(), nrm.end());
